@@ -1,0 +1,223 @@
+"""gsolver_gb300 -- GB300-native (sm_103a) z-step core of the gsolver_solid_qdht path.
+
+Python mirror of the C ABI in include/gs_abi.h (ctypes, no torch types).  The compute
+path is libgsolver_gb300.so built in-tree by gsolver_gb300.build; importing a handle
+fails loudly if that library is missing: there is no CPU fallback.
+
+``Propagator`` mirrors the reference's hot-path functions on one pulse:
+  set_field / get_field  <- FIELD, BIGBUFFER2 host globals (solver.h:169)
+  nl_step                <- calculate_NLstep (propagator.cu:268-426)
+  lstep                  <- ht_run + calculate_Lstep + ht_run (propagator.cu:179-213)
+  qdht                   <- ht_run -> qdht_plan::run_many (fhatha.cpp:218-230)
+  step                   <- propagator() (propagator.cu:125-266)
+Physics errors raise ``GsError`` with the reference's exception text.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libgsolver_gb300.so")
+
+GS_OK, GS_ERR_ARG, GS_ERR_CUDA, GS_ERR_BLAST, GS_ERR_NAN, GS_ERR_COLLAPSE = 0, 1, 2, 3, 4, 5
+GS_ERR_STATE, GS_ERR_UNSUPPORTED, GS_ERR_NOMEM = 6, 7, 8
+PREC_FP64, PREC_MIXED = 0, 1
+
+# every function declared in include/gs_abi.h
+ABI_FUNCTIONS = (
+    "gs_create", "gs_upload_tables", "gs_set_field", "gs_get_field", "gs_nl_step", "gs_get_nl",
+    "gs_lstep", "gs_qdht", "gs_step", "gs_launch_count", "gs_qdht_timing", "gs_destroy",
+    "gs_last_error", "gs_status_string",
+)
+
+
+class GsError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(msg)
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("n_r", C.c_int), ("n_t", C.c_int), ("precision", C.c_int), ("nonlinear", C.c_int),
+        ("device", C.c_int), ("reserved0", C.c_int),
+        ("tstep", C.c_double), ("tmin", C.c_double), ("tmax", C.c_double), ("omega0", C.c_double),
+        ("ionrate_denom", C.c_double), ("neutral_density", C.c_double), ("rho0", C.c_double),
+        ("ionization_potential", C.c_double), ("ponderomotive", C.c_double),
+        ("avalanche_cs", C.c_double), ("recombination_tau", C.c_double),
+        ("raman_fraction", C.c_double), ("n2", C.c_double),
+        ("omega_min", C.c_double), ("omega_max", C.c_double), ("max_tolerance", C.c_double),
+    ]
+
+
+class Tables(C.Structure):
+    _fields_ = [(k, C.c_void_p) for k in (
+        "rate_ln", "plasma_func", "raman_func", "kerr", "omega", "wavenum", "ho_disp", "kt2",
+        "qdht_c", "qdht_m1")]
+
+
+_lib = None
+
+
+def load_library(path: str | None = None):
+    """Load libgsolver_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise RuntimeError(f"{p} is missing: build it with `python -m gsolver_gb300.build` "
+                           "(the GPU path has no fallback)")
+    L = C.CDLL(p)
+    V, D, I = C.c_void_p, C.c_double, C.c_int
+    PD = C.POINTER(C.c_double)
+    L.gs_create.argtypes = [C.POINTER(Params), C.POINTER(V)]
+    L.gs_upload_tables.argtypes = [V, C.POINTER(Tables)]
+    L.gs_set_field.argtypes = [V, V, V]
+    L.gs_get_field.argtypes = [V, V, V]
+    L.gs_nl_step.argtypes = [V, D, PD, PD]
+    L.gs_get_nl.argtypes = [V, V]
+    L.gs_lstep.argtypes = [V, D]
+    L.gs_qdht.argtypes = [V, V]
+    L.gs_step.argtypes = [V, D, D, D, PD, C.POINTER(C.c_uint), PD, PD]
+    L.gs_launch_count.argtypes = [V]
+    L.gs_launch_count.restype = C.c_longlong
+    L.gs_qdht_timing.argtypes = [V, I, PD, C.POINTER(C.c_int)]
+    L.gs_destroy.argtypes = [V]
+    L.gs_last_error.argtypes = [V]
+    L.gs_last_error.restype = C.c_char_p
+    L.gs_status_string.argtypes = [I]
+    L.gs_status_string.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+PARAM_KEYS = ("tstep", "tmin", "tmax", "omega0", "ionrate_denom", "neutral_density",
+              "ionization_potential", "ponderomotive", "avalanche_cs", "recombination_tau",
+              "raman_fraction", "n2", "omega_min", "omega_max", "max_tolerance")
+
+
+class Propagator:
+    """One pulse on one GPU behind the C ABI.  ``setup`` is a dict with the scalar
+    parameters and FP64 tables (keys as in gs_params / gs_tables); see
+    gsolver_gb300.setup.build_setup for the product's own builder."""
+
+    def __init__(self, setup: dict, precision: int = PREC_FP64, nonlinear: bool = True, device: int = 0):
+        self.L = load_library()
+        self.nr, self.nt = int(setup["n_r"]), int(setup["n_t"])
+        p = Params()
+        p.n_r, p.n_t, p.precision, p.nonlinear, p.device = self.nr, self.nt, int(precision), int(bool(nonlinear)), int(device)
+        for k in PARAM_KEYS:
+            setattr(p, k, float(setup[k]))
+        p.rho0 = float(setup.get("rho0", 0.0))
+        self.params = p
+        h = C.c_void_p()
+        rc = self.L.gs_create(C.byref(p), C.byref(h))
+        if rc:
+            raise GsError(rc, self.L.gs_last_error(None).decode())
+        self.h = h
+        self._keep = {}
+        t = Tables()
+        for k, dt in (("rate_ln", np.float64), ("plasma_func", np.complex128), ("raman_func", np.complex128),
+                      ("kerr", np.float64), ("omega", np.float64), ("wavenum", np.complex128),
+                      ("ho_disp", np.float64), ("kt2", np.float64), ("qdht_m1", np.float64)):
+            a = np.ascontiguousarray(setup[k], dtype=dt)
+            self._keep[k] = a
+            setattr(t, k, a.ctypes.data)
+        cm = np.asfortranarray(np.asarray(setup["qdht_c"], dtype=np.float64))   # C[i + n_r*j]
+        self._keep["qdht_c"] = cm
+        t.qdht_c = cm.ctypes.data
+        self._check(self.L.gs_upload_tables(self.h, C.byref(t)))
+
+    def _check(self, rc):
+        if rc:
+            raise GsError(rc, self.L.gs_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.gs_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _arr(self, a):
+        a = np.ascontiguousarray(a, dtype=np.complex128)
+        if a.shape != (self.nr, self.nt):
+            raise ValueError(f"expected shape {(self.nr, self.nt)}, got {a.shape}")
+        return a
+
+    def set_field(self, field, spec=None):
+        f = self._arr(field)
+        s = self._arr(spec) if spec is not None else None
+        self._check(self.L.gs_set_field(self.h, _ptr(f), _ptr(s)))
+
+    def get_field(self, want_spec=True):
+        f = np.empty((self.nr, self.nt), np.complex128)
+        s = np.empty((self.nr, self.nt), np.complex128) if want_spec else None
+        self._check(self.L.gs_get_field(self.h, _ptr(f), _ptr(s)))
+        return (f, s) if want_spec else f
+
+    def nl_step(self, dz):
+        a2, n2 = C.c_double(), C.c_double()
+        self._check(self.L.gs_nl_step(self.h, float(dz), C.byref(a2), C.byref(n2)))
+        return a2.value, n2.value
+
+    def get_nl(self):
+        b = np.empty((self.nr, self.nt), np.complex128)
+        self._check(self.L.gs_get_nl(self.h, _ptr(b)))
+        return b
+
+    def lstep(self, dz):
+        self._check(self.L.gs_lstep(self.h, float(dz)))
+
+    def qdht(self, data):
+        d = np.array(self._arr(data), copy=True)
+        self._check(self.L.gs_qdht(self.h, _ptr(d)))
+        return d
+
+    def step(self, current_z, znet_cur, znet_prev, zstep, step_n=0):
+        dz = C.c_double(zstep)
+        sn = C.c_uint(step_n)
+        a2, n2 = C.c_double(), C.c_double()
+        self._check(self.L.gs_step(self.h, float(current_z), float(znet_cur), float(znet_prev),
+                                   C.byref(dz), C.byref(sn), C.byref(a2), C.byref(n2)))
+        return dz.value, sn.value, a2.value, n2.value
+
+    def launch_count(self):
+        return int(self.L.gs_launch_count(self.h))
+
+    def qdht_timing(self, enable=True):
+        ms, n = C.c_double(), C.c_int()
+        self._check(self.L.gs_qdht_timing(self.h, int(enable), C.byref(ms), C.byref(n)))
+        return ms.value, n.value
+
+    def run(self, znet, dz0, steps=None, on_dump=None):
+        """The z-loop of solver_main.cpp:202-225 over ZNET; on_dump(n_z, self) at each
+        ZNET point.  Returns (final z, zstep, STEP_N, propagator calls)."""
+        cz = float(znet[0]); n_z = 0; step_n = 0; zstep = float(dz0); calls = 0
+        nz = len(znet)
+        while True:
+            if cz >= znet[n_z]:
+                if on_dump:
+                    on_dump(n_z, self)
+                if n_z == nz - 1:
+                    break
+                n_z += 1
+            if steps is not None and calls >= steps:
+                break
+            zstep, step_n, _, _ = self.step(cz, znet[n_z], znet[n_z - 1], zstep, step_n)
+            step_n += 1
+            calls += 1
+            cz += zstep
+        return cz, zstep, step_n, calls

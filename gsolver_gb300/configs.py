@@ -1,0 +1,118 @@
+"""Reference-format configs and dispersion tables for the benchmark workloads.
+
+The reference reads whitespace ``KEY value`` configs (process_input.cpp:297-482) and RAW
+dispersion files (type 3: int type, int N, double omega[N], double n[2N];
+process_input.cpp:677-721).  Its HO dispersion only accepts RAW files
+(process_input.cpp:864), so Sellmeier media are tabulated here onto an omega grid that
+covers the whole spectral window.
+
+Workloads (synthetic: no dataset, the pulse is generated):
+  fused_silica_c1   N_R=256,  N_T=2048,  R=600 um, 400 fs window, 1 mm in 500 fixed steps
+  fused_silica_c2   N_R=1024, N_T=16384, R=1.2 mm, 1.6 ps window, 3 mm, adaptive (tol 1e-6)
+  hot_solid         small high-intensity grids where Keldysh, avalanche, loss and plasma
+                    defocusing all act (peak ~5e13 W/cm^2)
+"""
+from __future__ import annotations
+
+import math
+import os
+
+import numpy as np
+
+LIGHT_VELOCITY = 299792458.0
+
+# Malitson fused silica: n^2 - 1 = sum B_i lam^2 / (lam^2 - C_i^2), lam in um
+MALITSON_B = (0.6961663, 0.4079426, 0.8974794)
+MALITSON_C = (0.0684043, 0.1162414, 9.896161)
+
+
+def sellmeier_n(lam_um, B=MALITSON_B, Cum=MALITSON_C):
+    lam2 = np.asarray(lam_um, dtype=np.float64) ** 2
+    n2 = 1.0 + sum(b * lam2 / (lam2 - c * c) for b, c in zip(B, Cum))
+    return np.sqrt(n2)
+
+
+def argon_n(lam_um, pressure=1.0):
+    lam2 = np.asarray(lam_um, dtype=np.float64) ** 2
+    return 1.0 + pressure * 5.547e-4 * (1 + 5.15e-3 / lam2 + 4.19e-5 / lam2 ** 2)
+
+
+def write_rawdisp(path, omega, n):
+    omega = np.ascontiguousarray(omega, dtype=np.float64)
+    n = np.asarray(n)
+    inter = np.empty(2 * len(omega))
+    inter[0::2] = np.real(n)
+    inter[1::2] = np.imag(n) if np.iscomplexobj(n) else 0.0
+    with open(path, "wb") as f:
+        f.write(np.array([3, len(omega)], dtype=np.int32).tobytes())
+        f.write(omega.tobytes())
+        f.write(inter.tobytes())
+
+
+def tabulate_medium(path, medium="fused_silica", lam_min_um=0.2, lam_max_um=5.0, npts=20001):
+    """RAW table uniform in omega between 2 pi c / lam_max and 2 pi c / lam_min."""
+    wmin = 2 * math.pi * LIGHT_VELOCITY / (lam_max_um * 1e-6)
+    wmax = 2 * math.pi * LIGHT_VELOCITY / (lam_min_um * 1e-6)
+    omega = np.linspace(wmin, wmax, npts)
+    lam_um = 2 * math.pi * LIGHT_VELOCITY / omega * 1e6
+    n = sellmeier_n(lam_um) if medium == "fused_silica" else argon_n(lam_um)
+    write_rawdisp(path, omega, n)
+    return path
+
+
+def _fmt(d):
+    return "\n".join(f"{k} {v}" for k, v in d.items()) + "\n"
+
+
+SILICA_NL = {
+    "NONLIN_REFRINDEX": "2.5e-20", "RAMAN_FRACTION": "0.18", "TAU_RAMAN": "32e-15",
+    "OMEGA_RAMAN": repr(1 / 12.2e-15), "IONIZATION_POTENTIAL": "9", "NEUTRAL_DENSITY": "2.1e28",
+    "COLLISION_TAU": "1.7e-15", "RECOMBINATION_TAU": "150e-15", "AMBIENT_CARRIERS": "0",
+}
+
+
+def fused_silica_c1(dirpath):
+    """256 x 2048, collimated 800 nm 50 fs w0 = 100 um 3 P_cr pulse, 1 mm in 500 steps."""
+    tabulate_medium(os.path.join(dirpath, "fused_silica.rawdisp"))
+    d = {"LAMBDA_V": "8e-7", "N_T": "2048", "T_MIN": "-200e-15", "T_MAX": "200e-15",
+         "DISPERSION_FILE": "fused_silica.rawdisp", "N_R": "256", "R_MAX": "6e-4",
+         "N_Z": "501", "Z_MIN": "0", "Z_MAX": "1e-3", "ZNET_TYPE": "e", "MAX_TOLERANCE": "1e3",
+         "PULSE_SHAPE": "gg", "DURATION_FWHM": "50e-15", "DIAMETER_FWHM": repr(100e-6 * math.sqrt(2 * math.log(2))),
+         "POWER_CR": "3", "WAVEFRONT_RADIUS": "1e100", "CE_PHASE": "0"}
+    d.update(SILICA_NL)
+    p = os.path.join(dirpath, "fused_silica_c1.txt")
+    with open(p, "w") as f:
+        f.write(_fmt(d))
+    return p
+
+
+def fused_silica_c2(dirpath):
+    """1024 x 16384, same pulse, R = 1.2 mm, 1.6 ps window, 3 mm, adaptive dz (tol 1e-6)."""
+    tabulate_medium(os.path.join(dirpath, "fused_silica.rawdisp"))
+    d = {"LAMBDA_V": "8e-7", "N_T": "16384", "T_MIN": "-0.8e-12", "T_MAX": "0.8e-12",
+         "DISPERSION_FILE": "fused_silica.rawdisp", "N_R": "1024", "R_MAX": "1.2e-3",
+         "N_Z": "31", "Z_MIN": "0", "Z_MAX": "3e-3", "ZNET_TYPE": "e", "MAX_TOLERANCE": "1e-6",
+         "PULSE_SHAPE": "gg", "DURATION_FWHM": "50e-15", "DIAMETER_FWHM": repr(100e-6 * math.sqrt(2 * math.log(2))),
+         "POWER_CR": "3", "WAVEFRONT_RADIUS": "1e100", "CE_PHASE": "0"}
+    d.update(SILICA_NL)
+    p = os.path.join(dirpath, "fused_silica_c2.txt")
+    with open(p, "w") as f:
+        f.write(_fmt(d))
+    return p
+
+
+def hot_solid(dirpath, n_r=32, n_t=2048, power_cr=30.0, w0=10e-6, window=400e-15, r_max=None,
+              tol=1e3, z_max=2e-5, n_z=11, name="hot_solid"):
+    """Small fused-silica grid with a tightly focused, strongly ionizing pulse."""
+    tabulate_medium(os.path.join(dirpath, "fused_silica.rawdisp"))
+    r_max = r_max or 6 * w0
+    d = {"LAMBDA_V": "8e-7", "N_T": str(n_t), "T_MIN": repr(-window / 2), "T_MAX": repr(window / 2),
+         "DISPERSION_FILE": "fused_silica.rawdisp", "N_R": str(n_r), "R_MAX": repr(r_max),
+         "N_Z": str(n_z), "Z_MIN": "0", "Z_MAX": repr(z_max), "ZNET_TYPE": "e", "MAX_TOLERANCE": repr(tol),
+         "PULSE_SHAPE": "gg", "DURATION_FWHM": "50e-15", "DIAMETER_FWHM": repr(w0 * math.sqrt(2 * math.log(2))),
+         "POWER_CR": repr(power_cr), "WAVEFRONT_RADIUS": "1e100", "CE_PHASE": "0"}
+    d.update(SILICA_NL)
+    p = os.path.join(dirpath, name + ".txt")
+    with open(p, "w") as f:
+        f.write(_fmt(d))
+    return p

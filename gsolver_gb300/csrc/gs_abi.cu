@@ -1,0 +1,518 @@
+// gs_abi.cu -- the C ABI (include/gs_abi.h): device state of one pulse and the z-step
+// orchestration (propagator / calculate_NLstep / calculate_Lstep / ht_run).
+//
+// HBM layout per handle (n_r x n_t complex, row-major, omega contiguous, spectral rows in
+// FFT position order):  A = FIELD (r,omega), S = BIGBUFFER2 (k,omega),
+// NB = BIGBUFFER1 (r,omega), KP = previous RK4 stage, E = time-domain field of the
+// stage, U = three scratch rows per radial point (loss, rho*E, Kerr source).
+// FP64 handles hold double2, mixed handles float2 (their QDHT tables stay FP64 at
+// set-up and are split for the tensor cores).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/gs_abi.h"
+#include "gs_internal.cuh"
+#include "gs_kernels.h"
+#include "gs_qdht_tc.h"
+
+using namespace gs;
+
+static std::string g_create_error;
+
+struct gs_handle {
+    gs_params p{};
+    int nr = 0, nt = 0, P = 1, M = 0, logM = 0;
+    bool fp64 = true;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    size_t esz = 16;           // bytes per complex element
+    void *A = nullptr, *S = nullptr, *NB = nullptr, *KP = nullptr, *E = nullptr, *U = nullptr;
+    void* tw = nullptr;        // twiddles, position-order independent
+    void *pf = nullptr, *rm = nullptr, *kerr = nullptr, *rate = nullptr;
+    double *omega = nullptr, *ho = nullptr, *kt2 = nullptr, *Cm = nullptr, *m1 = nullptr;
+    double2* wavenum = nullptr;
+    double2* staging = nullptr;
+    int* perm_dev = nullptr;
+    unsigned* err_dev = nullptr;
+    unsigned long long* max_dev = nullptr;
+    std::vector<int> perm;
+    gs::QdhtTc* tc = nullptr;  // mixed-precision QDHT (tcgen05)
+    bool tables_ok = false, field_ok = false;
+    long long launches = 0;
+    double qdht_ms = 0;
+    int qdht_n = 0;
+    bool time_qdht = false, ev_pending = false;
+    std::string err;
+};
+
+static int fail(gs_handle* h, int code, const std::string& msg) {
+    if (h) h->err = msg; else g_create_error = msg;
+    return code;
+}
+static int cuda_fail(gs_handle* h, cudaError_t e, const char* where) {
+    return fail(h, GS_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+#define CK(h, expr)                                                    \
+    do {                                                               \
+        cudaError_t _e = (expr);                                       \
+        if (_e != cudaSuccess) return cuda_fail((h), _e, #expr);       \
+    } while (0)
+
+static int ilog2(int n) { int l = 0; while ((1 << l) < n) l++; return l; }
+
+// Position -> omega index of the device FFT (gs_internal.cuh): frequency k = k2 + P*k1
+// sits at position k2*M + p_local(k1), p_local the mixed-radix digit reversal of the
+// radix-16 decimation-in-frequency stages.
+static std::vector<int> fft_position_map(int N, int P, int M, int logM) {
+    const int J = fft_num_stages(logM);
+    std::vector<int> R(J), sub(J), pre(J);
+    int prod = 1;
+    for (int j = 0; j < J; j++) {
+        R[j] = fft_stage_radix(logM, j);
+        pre[j] = prod;
+        prod *= R[j];
+        sub[j] = M / prod;
+    }
+    std::vector<int> perm(N);
+    for (int p = 0; p < N; p++) {
+        const int k2 = p / M, pl = p % M;
+        int k1 = 0;
+        for (int j = 0; j < J; j++) k1 += ((pl / sub[j]) % R[j]) * pre[j];
+        perm[p] = k2 + P * k1;
+    }
+    return perm;
+}
+
+// Exported functions take C linkage from their declarations in gs_abi.h.
+
+const char* gs_status_string(int s) {
+    switch (s) {
+        case GS_OK: return "ok";
+        case GS_ERR_ARG: return "bad argument";
+        case GS_ERR_CUDA: return "CUDA error";
+        case GS_ERR_BLAST: return "Attention!!!! Intensity is too big! Keep away, blast is possible.";
+        case GS_ERR_NAN: return "float_type photoionization_function(...): Intensity is nan!";
+        case GS_ERR_COLLAPSE: return "Minimum Z step size reached, collapse is possible!";
+        case GS_ERR_STATE: return "call out of order";
+        case GS_ERR_UNSUPPORTED: return "unsupported grid";
+        case GS_ERR_NOMEM: return "device allocation failed";
+        default: return "unknown status";
+    }
+}
+
+const char* gs_last_error(const gs_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+long long gs_launch_count(const gs_handle* h) { return h ? h->launches : 0; }
+
+static void free_all(gs_handle* h) {
+    void* ptrs[] = {h->A, h->S, h->NB, h->KP, h->E, h->U, h->tw, h->pf, h->rm, h->kerr, h->rate,
+                    h->omega, h->ho, h->kt2, h->Cm, h->m1, h->wavenum, h->staging, h->perm_dev,
+                    h->err_dev, h->max_dev};
+    for (void* q : ptrs) if (q) cudaFree(q);
+    if (h->tc) gs::qdht_tc_destroy(h->tc);
+    if (h->ev0) cudaEventDestroy(h->ev0);
+    if (h->ev1) cudaEventDestroy(h->ev1);
+    if (h->st) cudaStreamDestroy(h->st);
+}
+
+int gs_create(const gs_params* prm, gs_handle** out) {
+    if (!prm || !out) return fail(nullptr, GS_ERR_ARG, "null argument");
+    *out = nullptr;
+    const int nr = prm->n_r, nt = prm->n_t;
+    if (nr < 1 || nt < 64 || (nt & (nt - 1))) return fail(nullptr, GS_ERR_UNSUPPORTED, "n_t must be a power of two >= 64, n_r >= 1");
+    if (prm->precision != GS_PREC_FP64 && prm->precision != GS_PREC_MIXED) return fail(nullptr, GS_ERR_ARG, "precision");
+    gs_handle* h = new gs_handle();
+    h->p = *prm;
+    h->nr = nr;
+    h->nt = nt;
+    h->fp64 = prm->precision == GS_PREC_FP64;
+    h->esz = h->fp64 ? 16 : 8;
+    const int mmax = h->fp64 ? 8192 : 16384;   // one row of M complex in <= 128 KiB shared memory
+    h->M = nt <= mmax ? nt : mmax;
+    h->P = nt / h->M;
+    if (h->P > 8) { delete h; return fail(nullptr, GS_ERR_UNSUPPORTED, "n_t too large"); }
+    h->logM = ilog2(h->M);
+    cudaError_t e = cudaSetDevice(prm->device);
+    if (e != cudaSuccess) { delete h; return fail(nullptr, GS_ERR_CUDA, cudaGetErrorString(e)); }
+    auto al = [&](void** q, size_t n) -> bool { return cudaMalloc(q, n) == cudaSuccess; };
+    const size_t nel = (size_t)nr * nt;
+    bool ok = cudaStreamCreateWithFlags(&h->st, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreate(&h->ev0) == cudaSuccess && cudaEventCreate(&h->ev1) == cudaSuccess;
+    ok = ok && al(&h->A, nel * h->esz) && al(&h->S, nel * h->esz) && al(&h->NB, nel * h->esz) &&
+         al(&h->KP, nel * h->esz) && al(&h->E, nel * h->esz) && al(&h->U, 3 * nel * h->esz) &&
+         al(&h->tw, (size_t)nt * h->esz) && al(&h->pf, (size_t)nt * h->esz) && al(&h->rm, (size_t)nt * h->esz) &&
+         al(&h->kerr, (size_t)nt * h->esz / 2) && al(&h->rate, 8192 * h->esz / 2) &&
+         al((void**)&h->omega, nt * 8) && al((void**)&h->ho, nt * 8) && al((void**)&h->kt2, nr * 8) &&
+         al((void**)&h->Cm, (size_t)nr * nr * 8) && al((void**)&h->m1, nr * 8) &&
+         al((void**)&h->wavenum, nt * 16) && al((void**)&h->staging, nel * 16) &&
+         al((void**)&h->perm_dev, nt * 4) && al((void**)&h->err_dev, 4) && al((void**)&h->max_dev, 16);
+    if (!ok) {
+        cudaGetLastError();
+        free_all(h);
+        delete h;
+        return fail(nullptr, GS_ERR_NOMEM, "device allocation failed");
+    }
+    h->perm = fft_position_map(nt, h->P, h->M, h->logM);
+    e = cudaMemcpy(h->perm_dev, h->perm.data(), nt * 4, cudaMemcpyHostToDevice);
+    // twiddles exp(-2 pi i j / N)
+    std::vector<double> tw(2 * (size_t)nt);
+    for (int j = 0; j < nt; j++) {
+        const double a = 2.0 * M_PI * (double)j / (double)nt;
+        tw[2 * j] = std::cos(a);
+        tw[2 * j + 1] = -std::sin(a);
+    }
+    if (e == cudaSuccess) {
+        if (h->fp64) {
+            e = cudaMemcpy(h->tw, tw.data(), nt * 16, cudaMemcpyHostToDevice);
+        } else {
+            std::vector<float> twf(tw.begin(), tw.end());
+            e = cudaMemcpy(h->tw, twf.data(), nt * 8, cudaMemcpyHostToDevice);
+        }
+    }
+    if (e == cudaSuccess) e = h->fp64 ? fft_set_smem<double>(h->M) : fft_set_smem<float>(h->M);
+    if (e == cudaSuccess) {
+        double k[20], b = 1.0;
+        for (int n = 1; n <= 20; n++) { b *= (0.5 - (n - 1)) / n; k[n - 1] = b; }
+        e = qdht_set_sqrt_ho(k);
+    }
+    if (e != cudaSuccess) {
+        std::string m = cudaGetErrorString(e);
+        free_all(h);
+        delete h;
+        return fail(nullptr, GS_ERR_CUDA, m);
+    }
+    if (!h->fp64) {
+        std::string m;
+        h->tc = gs::qdht_tc_create(nr, nt, h->st, &m);
+        if (!h->tc) {
+            free_all(h);
+            delete h;
+            return fail(nullptr, GS_ERR_UNSUPPORTED, "mixed QDHT: " + m);
+        }
+    }
+    *out = h;
+    return GS_OK;
+}
+
+int gs_destroy(gs_handle* h) {
+    if (!h) return GS_OK;
+    cudaSetDevice(h->p.device);
+    cudaStreamSynchronize(h->st);
+    free_all(h);
+    delete h;
+    return GS_OK;
+}
+
+template <typename T>
+static std::vector<T> permuted(const double* src, const std::vector<int>& perm, int comps) {
+    std::vector<T> o(perm.size() * comps);
+    for (size_t p = 0; p < perm.size(); p++)
+        for (int c = 0; c < comps; c++) o[p * comps + c] = (T)src[(size_t)perm[p] * comps + c];
+    return o;
+}
+
+int gs_upload_tables(gs_handle* h, const gs_tables* t) {
+    if (!h || !t) return fail(h, GS_ERR_ARG, "null argument");
+    if (!t->rate_ln || !t->plasma_func || !t->raman_func || !t->kerr || !t->omega || !t->wavenum ||
+        !t->ho_disp || !t->kt2 || !t->qdht_c || !t->qdht_m1)
+        return fail(h, GS_ERR_ARG, "missing table");
+    CK(h, cudaSetDevice(h->p.device));
+    const int nt = h->nt, nr = h->nr;
+    auto up = [&](void* dst, const void* src, size_t n) { return cudaMemcpy(dst, src, n, cudaMemcpyHostToDevice); };
+    if (h->fp64) {
+        auto pf = permuted<double>(t->plasma_func, h->perm, 2);
+        auto rm = permuted<double>(t->raman_func, h->perm, 2);
+        auto ke = permuted<double>(t->kerr, h->perm, 1);
+        CK(h, up(h->pf, pf.data(), nt * 16));
+        CK(h, up(h->rm, rm.data(), nt * 16));
+        CK(h, up(h->kerr, ke.data(), nt * 8));
+        CK(h, up(h->rate, t->rate_ln, 8192 * 8));
+    } else {
+        auto pf = permuted<float>(t->plasma_func, h->perm, 2);
+        auto rm = permuted<float>(t->raman_func, h->perm, 2);
+        auto ke = permuted<float>(t->kerr, h->perm, 1);
+        std::vector<float> rate(t->rate_ln, t->rate_ln + 8192);
+        CK(h, up(h->pf, pf.data(), nt * 8));
+        CK(h, up(h->rm, rm.data(), nt * 8));
+        CK(h, up(h->kerr, ke.data(), nt * 4));
+        CK(h, up(h->rate, rate.data(), 8192 * 4));
+    }
+    auto om = permuted<double>(t->omega, h->perm, 1);
+    auto wn = permuted<double>(t->wavenum, h->perm, 2);
+    auto ho = permuted<double>(t->ho_disp, h->perm, 1);
+    CK(h, up(h->omega, om.data(), nt * 8));
+    CK(h, up(h->wavenum, wn.data(), nt * 16));
+    CK(h, up(h->ho, ho.data(), nt * 8));
+    CK(h, up(h->kt2, t->kt2, nr * 8));
+    CK(h, up(h->Cm, t->qdht_c, (size_t)nr * nr * 8));
+    CK(h, up(h->m1, t->qdht_m1, nr * 8));
+    if (h->tc) {
+        std::string m;
+        if (gs::qdht_tc_set_matrix(h->tc, t->qdht_c, t->qdht_m1, &m)) return fail(h, GS_ERR_CUDA, "mixed QDHT matrix: " + m);
+    }
+    h->tables_ok = true;
+    return GS_OK;
+}
+
+static LstepArgs lstep_args(gs_handle* h, double dz) {
+    LstepArgs L;
+    L.dz = dz;
+    L.omega = h->omega;
+    L.wavenum = h->wavenum;
+    L.ho = h->ho;
+    L.kt2 = h->kt2;
+    L.omega_min = h->p.omega_min;
+    L.omega_max = h->p.omega_max;
+    return L;
+}
+
+// QDHT of device array X -> Y (mode: plain / fused linear step / masked input).
+static int run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz) {
+    LstepArgs L = lstep_args(h, dz);
+    if (h->fp64) {
+        CK(h, launch_qdht64(mode, h->Cm, h->m1, (const double*)X, (double*)Y, h->nr, 2 * h->nt, L, h->st, &h->launches));
+    } else {
+        std::string m;
+        cudaError_t e = gs::qdht_tc_run(h->tc, mode, (const float*)X, (float*)Y, L, &h->launches, &m);
+        if (e != cudaSuccess) return fail(h, GS_ERR_CUDA, "mixed QDHT: " + m + " " + cudaGetErrorString(e));
+    }
+    return GS_OK;
+}
+
+int gs_qdht_timing(gs_handle* h, int enable, double* ms_total, int* launches) {
+    if (!h) return GS_ERR_ARG;
+    if (ms_total) *ms_total = h->qdht_ms;
+    if (launches) *launches = h->qdht_n;
+    h->qdht_ms = 0;
+    h->qdht_n = 0;
+    h->time_qdht = enable != 0;
+    h->ev_pending = false;
+    return GS_OK;
+}
+
+// fold the CUDA-event time of the last fused QDHT pair into the totals (stream is idle)
+static int collect_qdht_time(gs_handle* h) {
+    if (!h->ev_pending) return GS_OK;
+    float ms = 0;
+    CK(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+    h->qdht_ms += ms;
+    h->qdht_n += 2;
+    h->ev_pending = false;
+    return GS_OK;
+}
+
+static int permute_in(gs_handle* h, const double* host, void* dst) {
+    const size_t nel = (size_t)h->nr * h->nt;
+    CK(h, cudaMemcpyAsync(h->staging, host, nel * 16, cudaMemcpyHostToDevice, h->st));
+    cudaError_t e = h->fp64 ? launch_permute<double>(+1, h->staging, dst, h->perm_dev, h->nt, nel, h->st, &h->launches)
+                            : launch_permute<float>(+1, h->staging, dst, h->perm_dev, h->nt, nel, h->st, &h->launches);
+    CK(h, e);
+    return GS_OK;
+}
+static int permute_out(gs_handle* h, const void* src, double* host) {
+    const size_t nel = (size_t)h->nr * h->nt;
+    cudaError_t e = h->fp64 ? launch_permute<double>(-1, src, h->staging, h->perm_dev, h->nt, nel, h->st, &h->launches)
+                            : launch_permute<float>(-1, src, h->staging, h->perm_dev, h->nt, nel, h->st, &h->launches);
+    CK(h, e);
+    CK(h, cudaMemcpyAsync(host, h->staging, nel * 16, cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    return GS_OK;
+}
+
+int gs_set_field(gs_handle* h, const double* field, const double* spec) {
+    if (!h || !field) return fail(h, GS_ERR_ARG, "null argument");
+    if (!h->tables_ok) return fail(h, GS_ERR_STATE, "tables not uploaded");
+    CK(h, cudaSetDevice(h->p.device));
+    int rc = permute_in(h, field, h->A);
+    if (rc) return rc;
+    if (spec) {
+        rc = permute_in(h, spec, h->S);
+    } else {
+        rc = run_qdht(h, QDHT_PLAIN, h->A, h->S, 0.0);
+    }
+    if (rc) return rc;
+    CK(h, cudaStreamSynchronize(h->st));
+    h->field_ok = true;
+    return GS_OK;
+}
+
+int gs_get_field(gs_handle* h, double* field, double* spec) {
+    if (!h) return GS_ERR_ARG;
+    if (!h->field_ok) return fail(h, GS_ERR_STATE, "field not set");
+    CK(h, cudaSetDevice(h->p.device));
+    int rc = GS_OK;
+    if (field) rc = permute_out(h, h->A, field);
+    if (!rc && spec) rc = permute_out(h, h->S, spec);
+    return rc;
+}
+
+int gs_get_nl(gs_handle* h, double* bb1) {
+    if (!h || !bb1) return GS_ERR_ARG;
+    CK(h, cudaSetDevice(h->p.device));
+    return permute_out(h, h->NB, bb1);
+}
+
+template <typename Rl>
+static int nl_step_impl(gs_handle* h, double dz) {
+    using T2 = typename Vec2<Rl>::T;
+    const int nr = h->nr, nt = h->nt;
+    const size_t nel = (size_t)nr * nt;
+    T2* A = (T2*)h->A;
+    T2* NB = (T2*)h->NB;
+    T2* KP = (T2*)h->KP;
+    T2* E = (T2*)h->E;
+    T2* U1 = (T2*)h->U;
+    T2* U2 = U1 + nel;
+    T2* U3 = U2 + nel;
+    if (!h->p.nonlinear) {
+        CK(h, launch_zero_nl<Rl>(A, NB, nel, h->max_dev, h->st, &h->launches));
+        return GS_OK;
+    }
+    const bool raman = h->p.raman_fraction > 0.001;
+    const bool kerr_on = h->p.n2 != 0;
+    FftArgs<Rl> fa{};
+    fa.N = nt; fa.M = h->M; fa.P = h->P; fa.logM = h->logM;
+    fa.tw = (const T2*)h->tw;
+    fa.max_out = h->max_dev;
+    PlasmaArgs<Rl> pa{};
+    pa.N = nt; pa.e = E; pa.u1 = U1; pa.u2 = U2; pa.u3 = U3;
+    pa.rate = (const Rl*)h->rate; pa.err = h->err_dev; pa.raman = raman;
+    pa.tstep_scaled = h->p.tstep * h->p.ionrate_denom;
+    pa.neutral_density = h->p.neutral_density; pa.rho0 = h->p.rho0;
+    pa.ionization_potential = h->p.ionization_potential; pa.ponderomotive = h->p.ponderomotive;
+    pa.avalanche_cs = h->p.avalanche_cs; pa.recombination_tau = h->p.recombination_tau;
+    SpecArgs<Rl> sa{};
+    sa.N = nt; sa.rows = nr; sa.u1 = U1; sa.u2 = U2; sa.u3 = U3;
+    sa.pf = (const T2*)h->pf; sa.rm = (const T2*)h->rm; sa.kerr = (const Rl*)h->kerr;
+    sa.raman = raman; sa.kerr_on = kerr_on; sa.nb = NB; sa.kp = KP; sa.max_out = h->max_dev + 1;
+    for (int s = 0; s < 4; s++) {
+        // stage input A + c*dz*k_prev, E = IFFT(.)/N   (propagator.cu:386-396, 640-641)
+        FftArgs<Rl> f1 = fa;
+        f1.rows = nr; f1.spre = 1; f1.kp = KP;
+        f1.cdz = (s == 0) ? 0.0 : (s < 3 ? dz * 0.5 : dz);
+        f1.track_max = (s == 0); f1.tpost = 1;
+        CK(h, launch_fft<Rl>(+1, A, E, f1, h->st, &h->launches));
+        CK(h, launch_plasma<Rl>(pa, nr, h->st, &h->launches));
+        FftArgs<Rl> f2 = fa;
+        f2.rows = (kerr_on ? 3 : 2) * nr;
+        CK(h, launch_fft<Rl>(-1, U1, U1, f2, h->st, &h->launches));
+        CK(h, launch_spec1<Rl>(sa, h->st, &h->launches));
+        if (kerr_on && raman) {
+            FftArgs<Rl> f3 = fa;
+            f3.rows = nr; f3.tpost = 2; f3.e = E;
+            CK(h, launch_fft<Rl>(+1, U3, U3, f3, h->st, &h->launches));
+            FftArgs<Rl> f4 = fa;
+            f4.rows = nr;
+            CK(h, launch_fft<Rl>(-1, U3, U3, f4, h->st, &h->launches));
+        }
+        SpecArgs<Rl> s2 = sa;
+        s2.stage = s;
+        CK(h, launch_spec2<Rl>(s2, h->st, &h->launches));
+    }
+    return GS_OK;
+}
+
+static int nl_step(gs_handle* h, double dz, double* max_a2, double* max_nl2) {
+    CK(h, cudaMemsetAsync(h->max_dev, 0, 16, h->st));
+    CK(h, cudaMemsetAsync(h->err_dev, 0, 4, h->st));
+    int rc = h->fp64 ? nl_step_impl<double>(h, dz) : nl_step_impl<float>(h, dz);
+    if (rc) return rc;
+    unsigned long long mx[2];
+    unsigned err = 0;
+    CK(h, cudaMemcpyAsync(mx, h->max_dev, 16, cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaMemcpyAsync(&err, h->err_dev, 4, cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    double a2, n2;
+    std::memcpy(&a2, &mx[0], 8);
+    std::memcpy(&n2, &mx[1], 8);
+    if (max_a2) *max_a2 = a2;
+    if (max_nl2) *max_nl2 = n2;
+    // an overflowing stage input can turn into NaN in later RK4 stages: the blast comes first
+    if (err & 1u) return fail(h, GS_ERR_BLAST, gs_status_string(GS_ERR_BLAST));
+    if (err & 2u) return fail(h, GS_ERR_NAN, gs_status_string(GS_ERR_NAN));
+    return GS_OK;
+}
+
+int gs_nl_step(gs_handle* h, double zstep, double* max_a2, double* max_nl2) {
+    if (!h) return GS_ERR_ARG;
+    if (!h->tables_ok || !h->field_ok) return fail(h, GS_ERR_STATE, "tables / field not set");
+    CK(h, cudaSetDevice(h->p.device));
+    return nl_step(h, zstep, max_a2, max_nl2);
+}
+
+static int lstep(gs_handle* h, double dz) {
+    if (h->time_qdht) CK(h, cudaEventRecord(h->ev0, h->st));
+    int rc = run_qdht(h, QDHT_LSTEP, h->NB, h->S, dz);
+    if (rc) return rc;
+    rc = run_qdht(h, QDHT_MASKED, h->S, h->A, dz);
+    if (rc) return rc;
+    if (h->time_qdht) {
+        CK(h, cudaEventRecord(h->ev1, h->st));
+        h->ev_pending = true;
+    }
+    return GS_OK;
+}
+
+int gs_lstep(gs_handle* h, double zstep) {
+    if (!h) return GS_ERR_ARG;
+    if (!h->tables_ok || !h->field_ok) return fail(h, GS_ERR_STATE, "tables / field not set");
+    CK(h, cudaSetDevice(h->p.device));
+    int rc = lstep(h, zstep);
+    if (rc) return rc;
+    CK(h, cudaStreamSynchronize(h->st));
+    return collect_qdht_time(h);
+}
+
+int gs_qdht(gs_handle* h, double* data) {
+    if (!h || !data) return GS_ERR_ARG;
+    if (!h->tables_ok) return fail(h, GS_ERR_STATE, "tables not uploaded");
+    CK(h, cudaSetDevice(h->p.device));
+    const size_t nel = (size_t)h->nr * h->nt;
+    char* U1 = (char*)h->U;
+    void* U2 = U1 + nel * h->esz;
+    int rc = permute_in(h, data, U1);
+    if (!rc) rc = run_qdht(h, QDHT_PLAIN, U1, U2, 0.0);
+    if (!rc) rc = permute_out(h, U2, data);
+    return rc;
+}
+
+int gs_step(gs_handle* h, double current_z, double znet_cur, double znet_prev, double* zstep_inout,
+            unsigned* step_n_inout, double* max_a2_out, double* max_nl2_out) {
+    if (!h || !zstep_inout) return GS_ERR_ARG;
+    if (!h->tables_ok || !h->field_ok) return fail(h, GS_ERR_STATE, "tables / field not set");
+    CK(h, cudaSetDevice(h->p.device));
+    const double tol = h->p.max_tolerance;
+    double zstep = *zstep_inout;
+    for (;;) {
+        double max_a2 = 0, max_nl2 = 0;
+        int rc = nl_step(h, zstep, &max_a2, &max_nl2);
+        if (rc) return rc;
+        // propagator.cu:147-164
+        bool repeat = false;
+        if (zstep * zstep * max_nl2 > tol * tol * max_a2) {
+            repeat = true;
+            if (step_n_inout) (*step_n_inout)++;
+        }
+        zstep = 0.5 * tol * std::sqrt(max_a2 / max_nl2);
+        if (zstep < 1e-10 * (znet_cur - znet_prev) || !(zstep > 0)) {
+            *zstep_inout = zstep;
+            return fail(h, GS_ERR_COLLAPSE, gs_status_string(GS_ERR_COLLAPSE));
+        }
+        const double lim = znet_cur - current_z;
+        if (lim < zstep) zstep = lim;
+        if (max_a2_out) *max_a2_out = max_a2;
+        if (max_nl2_out) *max_nl2_out = max_nl2;
+        if (!repeat) {
+            *zstep_inout = zstep;
+            rc = lstep(h, zstep);
+            if (rc) return rc;
+            CK(h, cudaStreamSynchronize(h->st));
+            return collect_qdht_time(h);
+        }
+    }
+}

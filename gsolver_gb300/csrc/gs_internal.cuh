@@ -1,0 +1,165 @@
+// gs_internal.cuh -- shared device helpers of the GB300 UPPE core.
+//
+// Complex numbers are double2 / float2 (re, im).  Spectral rows are stored in the
+// FFT's "position order" (see fft_position_map in gs_abi.cu): the forward FFT leaves
+// its output digit-reversed and the inverse FFT consumes that order, so no reordering
+// pass is ever run on the device; every per-omega table is uploaded in the same order.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "gs_kernels.h"
+
+namespace gs {
+
+template <typename R> using C2 = typename Vec2<R>::T;
+
+template <typename T2> __device__ __forceinline__ T2 mk(double x, double y);
+template <> __device__ __forceinline__ double2 mk<double2>(double x, double y) { return make_double2(x, y); }
+template <> __device__ __forceinline__ float2 mk<float2>(double x, double y) { return make_float2((float)x, (float)y); }
+
+template <typename T2> __device__ __forceinline__ T2 cadd(T2 a, T2 b) { a.x += b.x; a.y += b.y; return a; }
+template <typename T2> __device__ __forceinline__ T2 csub(T2 a, T2 b) { a.x -= b.x; a.y -= b.y; return a; }
+// (a.x + i a.y)(b.x + i b.y) with the naive formula (what std::complex gives for finite values)
+template <typename T2> __device__ __forceinline__ T2 cmul(T2 a, T2 b) {
+    T2 r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+template <typename T2> __device__ __forceinline__ T2 cconj(T2 a) { a.y = -a.y; return a; }
+
+// error word bits written by kernels (host maps them to the reference's exceptions)
+enum : unsigned { ERRBIT_BLAST = 1u, ERRBIT_NAN = 2u };
+
+// Non-negative doubles order like their bit patterns: max-reduce through 64-bit atomics.
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
+    atomicMax(addr, (unsigned long long)__double_as_longlong(v));
+}
+
+// ------------------------------------------------------------------ register DFTs --
+// Constant 16th roots of unity, cos / sin(2*pi*j/16) for j = 0..7.
+__device__ __forceinline__ double root16c(int j) {
+    const double c[8] = {1.0, 0.92387953251128674, 0.70710678118654757, 0.38268343236508978,
+                         0.0, -0.38268343236508978, -0.70710678118654757, -0.92387953251128674};
+    return c[j];
+}
+__device__ __forceinline__ double root16s(int j) {
+    const double s[8] = {0.0, 0.38268343236508978, 0.70710678118654757, 0.92387953251128674,
+                         1.0, 0.92387953251128674, 0.70710678118654757, 0.38268343236508978};
+    return s[j];
+}
+
+// v * exp(SIGN * 2*pi*i * k / R)   (k < R/2, R | 16)
+template <int R, int SIGN, typename Rl, typename T2>
+__device__ __forceinline__ T2 twc(T2 v, int k) {
+    const int j = k * (16 / R);
+    if (j == 0) return v;
+    if (j == 4) {  // multiply by SIGN*i
+        T2 r;
+        if (SIGN < 0) { r.x = v.y; r.y = -v.x; } else { r.x = -v.y; r.y = v.x; }
+        return r;
+    }
+    const Rl c = (Rl)root16c(j), s = (Rl)(SIGN * root16s(j));
+    T2 r;
+    r.x = v.x * c - v.y * s;
+    r.y = v.x * s + v.y * c;
+    return r;
+}
+
+// In-register radix-2 decimation-in-time DFT of size R (1,2,4,8,16), natural order in/out.
+template <int R, int SIGN, typename Rl, typename T2> struct RegDFT {
+    static __device__ __forceinline__ void run(T2* x) {
+        T2 e[R / 2], o[R / 2];
+#pragma unroll
+        for (int i = 0; i < R / 2; i++) { e[i] = x[2 * i]; o[i] = x[2 * i + 1]; }
+        RegDFT<R / 2, SIGN, Rl, T2>::run(e);
+        RegDFT<R / 2, SIGN, Rl, T2>::run(o);
+#pragma unroll
+        for (int k = 0; k < R / 2; k++) {
+            T2 t = twc<R, SIGN, Rl>(o[k], k);
+            x[k] = cadd(e[k], t);
+            x[k + R / 2] = csub(e[k], t);
+        }
+    }
+};
+template <int SIGN, typename Rl, typename T2> struct RegDFT<1, SIGN, Rl, T2> {
+    static __device__ __forceinline__ void run(T2*) {}
+};
+
+// -------------------------------------------------------------- shared-memory FFT --
+// One radix-R stage on a row of length M held in shared memory.
+// Forward (SIGN=-1, decimation in frequency): butterfly (q, block) reads R elements at
+// stride sub=S/R, DFT_R, multiplies output r by w_S^{q r}, writes them back in place.
+// Inverse (SIGN=+1) undoes the forward stage (conjugate twiddle first, then DFT_R).
+// tw[j] = exp(-2*pi*i*j/Nfull); a sub-row of length M = Nfull/twstride uses tw[j*twstride].
+template <int R, int SIGN, typename Rl>
+__device__ __forceinline__ void fft_stage(C2<Rl>* buf, int M, int S, const C2<Rl>* __restrict__ tw,
+                                          int twstride, int tid, int nthr) {
+    using T2 = C2<Rl>;
+    const int sub = S / R;
+    const int nb = M / R;
+    const int scale = (M / S) * twstride;
+    for (int b = tid; b < nb; b += nthr) {
+        const int q = b & (sub - 1);
+        const int base = (b / sub) * S + q;
+        T2 x[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) x[r] = buf[base + sub * r];
+        if (SIGN > 0) {
+#pragma unroll
+            for (int r = 1; r < R; r++) x[r] = cmul(x[r], cconj(__ldg(&tw[q * r * scale])));
+        }
+        RegDFT<R, SIGN, Rl, T2>::run(x);
+        if (SIGN < 0) {
+#pragma unroll
+            for (int r = 1; r < R; r++) x[r] = cmul(x[r], __ldg(&tw[q * r * scale]));
+        }
+#pragma unroll
+        for (int r = 0; r < R; r++) buf[base + sub * r] = x[r];
+    }
+}
+
+template <int SIGN, typename Rl>
+__device__ __forceinline__ void fft_stage_rt(int R, C2<Rl>* buf, int M, int S, const C2<Rl>* tw,
+                                             int twstride, int tid, int nthr) {
+    switch (R) {
+        case 16: fft_stage<16, SIGN, Rl>(buf, M, S, tw, twstride, tid, nthr); break;
+        case 8: fft_stage<8, SIGN, Rl>(buf, M, S, tw, twstride, tid, nthr); break;
+        case 4: fft_stage<4, SIGN, Rl>(buf, M, S, tw, twstride, tid, nthr); break;
+        case 2: fft_stage<2, SIGN, Rl>(buf, M, S, tw, twstride, tid, nthr); break;
+        default: break;
+    }
+}
+
+// Radix schedule of an M-point FFT (M = 2^m): 16, 16, ..., then 2^(m mod 4).
+__host__ __device__ inline int fft_num_stages(int logM) { return logM / 4 + ((logM % 4) ? 1 : 0); }
+__host__ __device__ inline int fft_stage_radix(int logM, int j) {
+    return (j < logM / 4) ? 16 : (1 << (logM % 4));
+}
+
+// Full in-place M-point FFT in shared memory (caller syncs before and after).
+template <int SIGN, typename Rl>
+__device__ void smem_fft(C2<Rl>* buf, int M, int logM, const C2<Rl>* tw, int twstride, int tid, int nthr) {
+    const int J = fft_num_stages(logM);
+    if (SIGN < 0) {
+        int S = M;
+        for (int j = 0; j < J; j++) {
+            const int R = fft_stage_radix(logM, j);
+            fft_stage_rt<SIGN, Rl>(R, buf, M, S, tw, twstride, tid, nthr);
+            __syncthreads();
+            S /= R;
+        }
+    } else {
+        // stage j works on sub-problems of size S_j = M / (R_0 ... R_{j-1})
+        for (int j = J - 1; j >= 0; j--) {
+            int S = M;
+            for (int i = 0; i < j; i++) S /= fft_stage_radix(logM, i);
+            const int R = fft_stage_radix(logM, j);
+            fft_stage_rt<SIGN, Rl>(R, buf, M, S, tw, twstride, tid, nthr);
+            __syncthreads();
+        }
+    }
+}
+
+}  // namespace gs

@@ -1,0 +1,74 @@
+// gs_kernels.h -- argument blocks and launchers shared between the orchestration
+// (gs_abi.cu) and the kernel translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+
+namespace gs {
+
+template <typename Rl> struct Vec2;
+template <> struct Vec2<double> { using T = double2; };
+template <> struct Vec2<float> { using T = float2; };
+
+template <typename Rl> struct FftArgs {
+    int N, M, P, logM, rows;                 // rows of length N = P*M
+    const typename Vec2<Rl>::T* tw;          // exp(-2 pi i j / N), j < N
+    int spre;                                // spectral-side load op (inverse)
+    double cdz;                              // stage coefficient c*dz (SPRE_STAGE)
+    const typename Vec2<Rl>::T* kp;          // previous RK4 stage (SPRE_STAGE)
+    int track_max;                           // max |input|^2 -> max_out
+    unsigned long long* max_out;
+    int tpost;                               // time-side store op (inverse)
+    const typename Vec2<Rl>::T* e;           // time-domain field (TPOST_DIVN_MULE)
+};
+
+template <typename Rl> struct PlasmaArgs {
+    int N;
+    const typename Vec2<Rl>::T* e;
+    typename Vec2<Rl>::T *u1, *u2, *u3;
+    const Rl* rate;
+    unsigned* err;
+    int raman;
+    double tstep_scaled, neutral_density, rho0, ionization_potential, ponderomotive;
+    double avalanche_cs, recombination_tau;
+};
+
+template <typename Rl> struct SpecArgs {
+    int N, rows;
+    typename Vec2<Rl>::T *u1, *u2, *u3;
+    const typename Vec2<Rl>::T *pf, *rm;
+    const Rl* kerr;
+    int raman, kerr_on, stage;
+    typename Vec2<Rl>::T *nb, *kp;
+    unsigned long long* max_out;
+};
+
+template <typename Rl>
+cudaError_t launch_fft(int sign, const typename Vec2<Rl>::T* in, typename Vec2<Rl>::T* out, FftArgs<Rl> a,
+                       cudaStream_t st, long long* nlaunch);
+template <typename Rl> cudaError_t fft_set_smem(int M);
+template <typename Rl> cudaError_t launch_plasma(PlasmaArgs<Rl> a, int rows, cudaStream_t st, long long* nlaunch);
+template <typename Rl> cudaError_t launch_spec1(SpecArgs<Rl> a, cudaStream_t st, long long* nlaunch);
+template <typename Rl> cudaError_t launch_spec2(SpecArgs<Rl> a, cudaStream_t st, long long* nlaunch);
+template <typename Rl>
+cudaError_t launch_zero_nl(const typename Vec2<Rl>::T* A, typename Vec2<Rl>::T* nb, size_t total,
+                           unsigned long long* max_out, cudaStream_t st, long long* nlaunch);
+template <typename Rl>
+cudaError_t launch_permute(int dir, const void* src, void* dst, const int* perm, int N, size_t total,
+                           cudaStream_t st, long long* nlaunch);
+
+// ---- QDHT: Y[i][c] = m1_i * sum_j C(i,j) X[j][c] / m1_j over the 2*n_t real columns
+struct LstepArgs {
+    double dz;
+    const double* omega;      // position order
+    const double2* wavenum;   // position order
+    const double* ho;         // position order
+    const double* kt2;        // [n_r]
+    double omega_min, omega_max;
+};
+enum { QDHT_PLAIN = 0, QDHT_LSTEP = 1, QDHT_MASKED = 2 };
+cudaError_t launch_qdht64(int mode, const double* C, const double* m1, const double* X, double* Y, int nr,
+                          int ncols, const LstepArgs& L, cudaStream_t st, long long* nlaunch);
+cudaError_t qdht_set_sqrt_ho(const double* coeffs20);
+
+}  // namespace gs

@@ -1,0 +1,443 @@
+// gs_nl.cu -- kernels of the nonlinear RK4 increment (calculate_NLstep, propagator.cu:268-426).
+//
+// One RK4 stage of one radial row is the reference's calculate_NLresponse
+// (propagator.cu:629-783): six length-N_T FFTs, the causal plasma recurrence
+// (ionization.cpp:9-95) and pointwise spectral products.  Here every piece runs batched
+// over all N_r rows:
+//   fft_sub_kernel    one CTA per (sub-)row, the row resident in shared memory,
+//                     radix-16 register butterflies; fused stage input A + c*dz*k_prev,
+//                     max|A|^2, 1/N scaling and the time-domain products.
+//   fft_cross_kernel  the radix-P first/last pass when N_T exceeds one CTA's shared
+//                     memory (N_T = P * M): coalesced, one thread per (row, n1).
+//   plasma_kernel     intensities and rates in parallel, the carrier-density recurrence
+//                     sequentially per row (it is not linear: clamps and the quadratic
+//                     avalanche term), then loss and rho*E in parallel.
+//   spec1/spec2       spectral combination and the RK4 accumulation with max|N|^2.
+// Templates instantiate the FP64 parity path (double) and the mixed path (float).
+#include "gs_kernels.h"
+#include "gs_internal.cuh"
+
+namespace gs {
+
+// solver.h:55-107 constants of the ionization table
+#define GS_ION_TOL 0.003304003148325
+#define GS_ION_MIN_LN 29.933606208922594
+#define GS_INT_DENOM_LN 36.841361487904734
+
+// ------------------------------------------------------------------ FFT kernels --
+// Spectral-side load ops (inverse transforms) and time-side ops.
+enum { SPRE_NONE = 0, SPRE_STAGE = 1 };
+enum { TPOST_STORE = 0, TPOST_DIVN = 1, TPOST_DIVN_MULE = 2 };
+
+template <typename Rl, int SIGN>
+__global__ void __launch_bounds__(sizeof(Rl) == 8 ? 256 : 512) fft_sub_kernel(const C2<Rl>* __restrict__ in, C2<Rl>* __restrict__ out,
+                                                      FftArgs<Rl> a) {
+    using T2 = C2<Rl>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T2* buf = reinterpret_cast<T2*>(smem_raw);
+    const int M = a.M;
+    const size_t base = (size_t)blockIdx.x * M;   // sub-rows are contiguous blocks of M
+    const int tid = threadIdx.x, nthr = blockDim.x;
+
+    // ---- load (with the spectral-side op for inverse transforms)
+    double lmax = 0.0;
+    for (int i = tid; i < M; i += nthr) {
+        T2 v = in[base + i];
+        if (SIGN > 0 && a.spre == SPRE_STAGE) {
+            if (a.track_max) {
+                double m = (double)v.x * (double)v.x + (double)v.y * (double)v.y;
+                lmax = fmax(lmax, m);
+            }
+            if (a.cdz != 0) {
+                T2 k = a.kp[base + i];
+                v.x = v.x + (Rl)a.cdz * k.x;
+                v.y = v.y + (Rl)a.cdz * k.y;
+            }
+        }
+        buf[i] = v;
+    }
+    if (SIGN > 0 && a.track_max) {
+        for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+        if ((tid & 31) == 0) atomic_max_nonneg(a.max_out, lmax);
+    }
+    __syncthreads();
+    smem_fft<SIGN, Rl>(buf, M, a.logM, a.tw, a.P, tid, nthr);
+
+    // ---- store (time-side op only when this kernel finishes an inverse transform)
+    const Rl rn = (Rl)a.N;
+    for (int i = tid; i < M; i += nthr) {
+        T2 v = buf[i];
+        if (SIGN > 0 && a.P == 1 && a.tpost != TPOST_STORE) {
+            v.x = v.x / rn;
+            v.y = v.y / rn;
+            if (a.tpost == TPOST_DIVN_MULE) v = cmul(v, a.e[base + i]);
+        }
+        out[base + i] = v;
+    }
+}
+
+template <typename Rl, int SIGN, int P>
+__global__ void __launch_bounds__(256) fft_cross_kernel(const C2<Rl>* __restrict__ in, C2<Rl>* __restrict__ out,
+                                                        FftArgs<Rl> a) {
+    using T2 = C2<Rl>;
+    const int M = a.M;
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const size_t total = (size_t)a.rows * M;
+    if (idx >= total) return;
+    const size_t row = idx / M;
+    const int n1 = (int)(idx - row * M);
+    const size_t base = row * (size_t)a.N;
+    T2 x[P];
+    if (SIGN < 0) {
+        // forward: y_k2[n1] = w_N^{n1 k2} sum_n2 x[n1 + M n2] w_P^{n2 k2}, stored at k2*M + n1
+#pragma unroll
+        for (int n2 = 0; n2 < P; n2++) x[n2] = in[base + n1 + (size_t)M * n2];
+        RegDFT<P, -1, Rl, T2>::run(x);
+#pragma unroll
+        for (int k2 = 1; k2 < P; k2++) x[k2] = cmul(x[k2], __ldg(&a.tw[n1 * k2]));
+#pragma unroll
+        for (int k2 = 0; k2 < P; k2++) out[base + (size_t)k2 * M + n1] = x[k2];
+    } else {
+        // inverse: x[n1 + M n2] = sum_k2 w_P^{-n2 k2} (w_N^{-n1 k2} z_k2[n1])
+#pragma unroll
+        for (int k2 = 0; k2 < P; k2++) x[k2] = in[base + (size_t)k2 * M + n1];
+#pragma unroll
+        for (int k2 = 1; k2 < P; k2++) x[k2] = cmul(x[k2], cconj(__ldg(&a.tw[n1 * k2])));
+        RegDFT<P, +1, Rl, T2>::run(x);
+        const Rl rn = (Rl)a.N;
+#pragma unroll
+        for (int n2 = 0; n2 < P; n2++) {
+            T2 v = x[n2];
+            const size_t o = base + n1 + (size_t)M * n2;
+            if (a.tpost != TPOST_STORE) {
+                v.x = v.x / rn;
+                v.y = v.y / rn;
+                if (a.tpost == TPOST_DIVN_MULE) v = cmul(v, a.e[o]);
+            }
+            out[o] = v;
+        }
+    }
+}
+
+// ------------------------------------------------------------------- plasma ----
+// photoionization_function without the rho > rho_n test (ionization.cpp:98-147,
+// KELDYSH solid branch): 0 below 1e13 W/m^2, log-interpolated table above.
+template <typename Rl>
+__device__ __forceinline__ Rl photo_rate(Rl I, const Rl* __restrict__ tab, unsigned* err) {
+    if (I < (Rl)(1e13 / 1e16)) return (Rl)0;
+    Rl lnI = log(I) + (Rl)GS_INT_DENOM_LN;
+    if (isnan(lnI)) { atomicOr(err, ERRBIT_NAN); return (Rl)0; }
+    int n = (int)floor((lnI - (Rl)GS_ION_MIN_LN) / (Rl)GS_ION_TOL);
+    if (n > 8192 - 2) { atomicOr(err, ERRBIT_BLAST); return (Rl)0; }
+    if (n < 0) return (Rl)0;
+    Rl lnIn = (Rl)GS_ION_MIN_LN + n * (Rl)GS_ION_TOL;
+    Rl w0 = __ldg(&tab[n]), w1 = __ldg(&tab[n + 1]);
+    Rl lnW = w0 + (lnI - lnIn) * (w1 - w0) / (Rl)GS_ION_TOL;
+    return exp(lnW);
+}
+
+// calculate_plasmadensity_losses_small (ionization.cpp:9-95), single-level branch, for
+// one row per CTA.  Inputs: E (time row).  Outputs: U1 = loss, U2 = rho*E,
+// U3 = |E|^2 (Raman on) or |E|^2 * E (Raman off).  The first recurrence step sees
+// E_0 = 0 as the reference does (ionization.cpp:25).
+template <typename Rl>
+__global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
+    using T2 = C2<Rl>;
+    constexpr int CH = 1024;
+    __shared__ Rl sW[CH], sG[CH], sR[CH];
+    __shared__ Rl prevW, prevG;
+    const int N = a.N;
+    const size_t base = (size_t)blockIdx.x * N;
+    const T2* E = a.e + base;
+    T2* U1 = a.u1 + base;
+    T2* U2 = a.u2 + base;
+    T2* U3 = a.u3 + base;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const Rl ND = (Rl)a.neutral_density;
+    const Rl tstep = (Rl)a.tstep_scaled;
+    const Rl U = (Rl)a.ionization_potential, Pc = (Rl)a.ponderomotive;
+    const Rl AV = (Rl)a.avalanche_cs, TAU = (Rl)a.recombination_tau;
+
+    // phase A: W_t and the avalanche prefactor g_t = AV/(U + P I_t) * I_t (t >= 1)
+    for (int t = tid; t < N; t += nthr) {
+        Rl W = 0, g = 0;
+        if (t > 0) {
+            T2 e = E[t];
+            Rl I = e.x * e.x + e.y * e.y;
+            W = photo_rate<Rl>(I, a.rate, a.err);
+            g = AV / (U + Pc * I) * I;
+        }
+        U1[t] = T2{W, g};
+    }
+    __syncthreads();
+
+    // phase B: the sequential Heun recurrence, CH samples at a time through shared memory
+    Rl ro = (Rl)a.rho0;
+    for (int c0 = 0; c0 < N; c0 += CH) {
+        const int cn = min(CH, N - c0);
+        for (int i = tid; i < cn; i += nthr) {
+            T2 v = U1[c0 + i];
+            sW[i] = v.x;
+            sG[i] = v.y;
+        }
+        // the previous chunk's last (W, g) (prevW/prevG) feeds this chunk's first sample
+        __syncthreads();
+        if (tid == 0) {
+            Rl W0 = (c0 == 0) ? (Rl)0 : prevW, g0 = (c0 == 0) ? (Rl)0 : prevG;
+            int i0 = 0;
+            if (c0 == 0) { sR[0] = ro; i0 = 1; W0 = sW[0]; g0 = sG[0]; }
+            for (int i = i0; i < cn; i++) {
+                const Rl W1 = sW[i], g1 = sG[i];
+                // k1 at (E_{t-1}, rho)
+                Rl W01 = (ro > ND) ? (Rl)0 : W0;
+                Rl av = (ro < 0 || ro > ND) ? (Rl)0 : g0 * ro * (1 - ro / ND);
+                Rl rc = (ro > 0) ? (ro / TAU) : (Rl)0;
+                Rl k1 = tstep * (W01 + av - rc);
+                Rl r2 = ro + k1;
+                Rl W11 = (r2 > ND) ? (Rl)0 : W1;
+                av = (r2 < 0 || r2 > ND) ? (Rl)0 : g1 * r2 * (1 - r2 / ND);
+                rc = (r2 > 0) ? (r2 / TAU) : (Rl)0;
+                Rl k2 = tstep * (W11 + av - rc);
+                ro += (Rl)0.5 * (k1 + k2);
+                if (ro > ND) ro = ND;
+                sR[i] = ro;
+                W0 = W1;
+                g0 = g1;
+            }
+            prevW = W0;
+            prevG = g0;
+        }
+        __syncthreads();
+        for (int i = tid; i < cn; i += nthr) {
+            T2 v = U2[c0 + i];   // scratch slot for rho until phase C
+            v.x = sR[i];
+            U2[c0 + i] = v;
+        }
+        __syncthreads();
+    }
+    __syncthreads();
+
+    // phase C: loss[t] (uses W_t, I_t, rho_t at step t+1), rho*E, intensity terms
+    for (int t = tid; t < N; t += nthr) {
+        T2 e = E[t];
+        Rl rho = U2[t].x;
+        T2 w = U1[t];
+        T2 loss = T2{0, 0};
+        if (t < N - 1 && t > 0) {
+            Rl I0 = e.x * e.x + e.y * e.y;
+            Rl W01 = (rho > ND) ? (Rl)0 : w.x;
+            // the reference compares the intensity with the log threshold (ionization.cpp:43)
+            if (I0 > (Rl)GS_ION_MIN_LN) {
+                Rl s = -(Rl)0.5 * W01 * (U + Pc * I0) / I0;
+                loss = T2{s * e.x, s * e.y};
+            }
+        }
+        U1[t] = loss;
+        U2[t] = T2{rho * e.x, rho * e.y};
+        Rl I = e.x * e.x + e.y * e.y;
+        U3[t] = a.raman ? T2{I, (Rl)0} : T2{I * e.x - (Rl)0 * e.y, I * e.y + (Rl)0 * e.x};
+    }
+}
+
+// ------------------------------------------------------------- spectral ops ----
+template <typename Rl>
+__global__ void spec1_kernel(SpecArgs<Rl> a) {
+    using T2 = C2<Rl>;
+    const size_t total = (size_t)a.rows * a.N;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int p = (int)(i % a.N);
+        // N = FFT(loss) + FFT(rho E) * PLASMA_FUNC (propagator.cu:679-686)
+        a.u1[i] = cadd(a.u1[i], cmul(a.u2[i], a.pf[p]));
+        if (a.raman) a.u3[i] = cmul(a.u3[i], a.rm[p]);   // FFT(I) * RAMAN_FUNCTION
+    }
+}
+
+template <typename Rl>
+__global__ void spec2_kernel(SpecArgs<Rl> a) {
+    using T2 = C2<Rl>;
+    const size_t total = (size_t)a.rows * a.N;
+    double lmax = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const int p = (int)(i % a.N);
+        T2 k = a.u1[i];
+        if (a.kerr_on) {   // += -j * KERR_PROFILE * FFT(Q E)
+            const Rl K = a.kerr[p];
+            T2 q = a.u3[i];
+            k.x += K * q.y;
+            k.y += -K * q.x;
+        }
+        T2 nb;
+        if (a.stage == 0) {
+            nb = k;
+        } else if (a.stage < 3) {
+            T2 o = a.nb[i];
+            nb = T2{o.x + (Rl)2 * k.x, o.y + (Rl)2 * k.y};
+        } else {
+            T2 o = a.nb[i];
+            nb = T2{(o.x + k.x) / (Rl)6, (o.y + k.y) / (Rl)6};
+            double m = (double)nb.x * (double)nb.x + (double)nb.y * (double)nb.y;
+            lmax = fmax(lmax, m);
+        }
+        a.nb[i] = nb;
+        if (a.stage < 3) a.kp[i] = k;
+    }
+    if (a.stage == 3) {
+        for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+        if ((threadIdx.x & 31) == 0) atomic_max_nonneg(a.max_out, lmax);
+    }
+}
+
+// zero NL response (NONLINEARITY_ON undefined): BIGBUFFER1 = 0 and max|A|^2
+template <typename Rl>
+__global__ void zero_nl_kernel(const C2<Rl>* __restrict__ A, C2<Rl>* __restrict__ nb, size_t total,
+                               unsigned long long* max_out) {
+    double lmax = 0.0;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        C2<Rl> v = A[i];
+        lmax = fmax(lmax, (double)v.x * (double)v.x + (double)v.y * (double)v.y);
+        nb[i] = C2<Rl>{0, 0};
+    }
+    for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(max_out, lmax);
+}
+
+// natural <-> position order, with precision conversion from / to FP64 staging
+template <typename Rl>
+__global__ void permute_in_kernel(const double2* __restrict__ src, C2<Rl>* __restrict__ dst,
+                                  const int* __restrict__ perm, int N, size_t total) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t row = i / N;
+        const int p = (int)(i - row * N);
+        double2 v = src[row * N + perm[p]];
+        dst[i] = C2<Rl>{(Rl)v.x, (Rl)v.y};
+    }
+}
+template <typename Rl>
+__global__ void permute_out_kernel(const C2<Rl>* __restrict__ src, double2* __restrict__ dst,
+                                   const int* __restrict__ perm, int N, size_t total) {
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t row = i / N;
+        const int p = (int)(i - row * N);
+        C2<Rl> v = src[i];
+        dst[row * N + perm[p]] = make_double2((double)v.x, (double)v.y);
+    }
+}
+
+// ------------------------------------------------------------------ launchers --
+template <typename Rl>
+static int fft_threads(int M) {
+    const int maxt = sizeof(Rl) == 8 ? 256 : 512;
+    int t = M / 16;
+    if (t < 32) t = 32;
+    if (t > maxt) t = maxt;
+    return t;
+}
+
+template <typename Rl>
+cudaError_t launch_fft(int sign, const C2<Rl>* in, C2<Rl>* out, FftArgs<Rl> a, cudaStream_t st, long long* nlaunch) {
+    // a.rows full rows of length a.N = a.P * a.M
+    const size_t smem = (size_t)a.M * sizeof(C2<Rl>);
+    const int nsub = a.rows * a.P;
+    const int thr = fft_threads<Rl>(a.M);
+    const int cross_thr = 256;
+    const unsigned cross_blocks = (unsigned)(((size_t)a.rows * a.M + cross_thr - 1) / cross_thr);
+    if (sign < 0) {
+        const C2<Rl>* src = in;
+        if (a.P > 1) {
+            switch (a.P) {
+                case 2: fft_cross_kernel<Rl, -1, 2><<<cross_blocks, cross_thr, 0, st>>>(in, out, a); break;
+                case 4: fft_cross_kernel<Rl, -1, 4><<<cross_blocks, cross_thr, 0, st>>>(in, out, a); break;
+                case 8: fft_cross_kernel<Rl, -1, 8><<<cross_blocks, cross_thr, 0, st>>>(in, out, a); break;
+                default: return cudaErrorInvalidValue;
+            }
+            (*nlaunch)++;
+            src = out;
+        }
+        fft_sub_kernel<Rl, -1><<<nsub, thr, smem, st>>>(src, out, a);
+        (*nlaunch)++;
+    } else {
+        C2<Rl>* mid = out;
+        fft_sub_kernel<Rl, +1><<<nsub, thr, smem, st>>>(in, mid, a);
+        (*nlaunch)++;
+        if (a.P > 1) {
+            switch (a.P) {
+                case 2: fft_cross_kernel<Rl, +1, 2><<<cross_blocks, cross_thr, 0, st>>>(mid, out, a); break;
+                case 4: fft_cross_kernel<Rl, +1, 4><<<cross_blocks, cross_thr, 0, st>>>(mid, out, a); break;
+                case 8: fft_cross_kernel<Rl, +1, 8><<<cross_blocks, cross_thr, 0, st>>>(mid, out, a); break;
+                default: return cudaErrorInvalidValue;
+            }
+            (*nlaunch)++;
+        }
+    }
+    return cudaGetLastError();
+}
+
+template <typename Rl>
+cudaError_t fft_set_smem(int M) {
+    const int smem = M * (int)sizeof(C2<Rl>);
+    cudaError_t e = cudaFuncSetAttribute(fft_sub_kernel<Rl, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(fft_sub_kernel<Rl, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+}
+
+static unsigned grid_for(size_t total, int thr) {
+    size_t b = (total + thr - 1) / thr;
+    if (b > 152 * 32) b = 152 * 32;
+    if (b < 1) b = 1;
+    return (unsigned)b;
+}
+
+template <typename Rl>
+cudaError_t launch_plasma(PlasmaArgs<Rl> a, int rows, cudaStream_t st, long long* nlaunch) {
+    plasma_kernel<Rl><<<rows, 256, 0, st>>>(a);
+    (*nlaunch)++;
+    return cudaGetLastError();
+}
+
+template <typename Rl>
+cudaError_t launch_spec1(SpecArgs<Rl> a, cudaStream_t st, long long* nlaunch) {
+    spec1_kernel<Rl><<<grid_for((size_t)a.rows * a.N, 256), 256, 0, st>>>(a);
+    (*nlaunch)++;
+    return cudaGetLastError();
+}
+
+template <typename Rl>
+cudaError_t launch_spec2(SpecArgs<Rl> a, cudaStream_t st, long long* nlaunch) {
+    spec2_kernel<Rl><<<grid_for((size_t)a.rows * a.N, 256), 256, 0, st>>>(a);
+    (*nlaunch)++;
+    return cudaGetLastError();
+}
+
+template <typename Rl>
+cudaError_t launch_zero_nl(const C2<Rl>* A, C2<Rl>* nb, size_t total, unsigned long long* max_out,
+                           cudaStream_t st, long long* nlaunch) {
+    zero_nl_kernel<Rl><<<grid_for(total, 256), 256, 0, st>>>(A, nb, total, max_out);
+    (*nlaunch)++;
+    return cudaGetLastError();
+}
+
+template <typename Rl>
+cudaError_t launch_permute(int dir, const void* src, void* dst, const int* perm, int N, size_t total,
+                           cudaStream_t st, long long* nlaunch) {
+    if (dir > 0)
+        permute_in_kernel<Rl><<<grid_for(total, 256), 256, 0, st>>>((const double2*)src, (C2<Rl>*)dst, perm, N, total);
+    else
+        permute_out_kernel<Rl><<<grid_for(total, 256), 256, 0, st>>>((const C2<Rl>*)src, (double2*)dst, perm, N, total);
+    (*nlaunch)++;
+    return cudaGetLastError();
+}
+
+#define GS_INST(Rl)                                                                                          \
+    template cudaError_t launch_fft<Rl>(int, const C2<Rl>*, C2<Rl>*, FftArgs<Rl>, cudaStream_t, long long*); \
+    template cudaError_t fft_set_smem<Rl>(int);                                                              \
+    template cudaError_t launch_plasma<Rl>(PlasmaArgs<Rl>, int, cudaStream_t, long long*);                   \
+    template cudaError_t launch_spec1<Rl>(SpecArgs<Rl>, cudaStream_t, long long*);                           \
+    template cudaError_t launch_spec2<Rl>(SpecArgs<Rl>, cudaStream_t, long long*);                           \
+    template cudaError_t launch_zero_nl<Rl>(const C2<Rl>*, C2<Rl>*, size_t, unsigned long long*,             \
+                                            cudaStream_t, long long*);                                       \
+    template cudaError_t launch_permute<Rl>(int, const void*, void*, const int*, int, size_t, cudaStream_t,  \
+                                            long long*);
+GS_INST(double)
+GS_INST(float)
+
+}  // namespace gs

@@ -1,0 +1,23 @@
+// gs_qdht_tc.h -- mixed-precision QDHT on the tcgen05 tensor cores (3xTF32, FP32 accumulate).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+
+#include "gs_kernels.h"
+
+namespace gs {
+
+struct QdhtTc;
+
+// Plan for an n_r x n_r real matrix applied to [n_r][n_t] complex float rows.
+// Returns nullptr (and a message) when the grid is not supported.
+QdhtTc* qdht_tc_create(int nr, int nt, cudaStream_t st, std::string* msg);
+// Upload C (element (i,j) at C[i + nr*j]) and m1; builds the split hi/lo operands.
+int qdht_tc_set_matrix(QdhtTc* q, const double* C, const double* m1, std::string* msg);
+// Y = QDHT(X) with the given mode (QDHT_PLAIN / QDHT_LSTEP / QDHT_MASKED).
+cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const LstepArgs& L, long long* nlaunch,
+                        std::string* msg);
+void qdht_tc_destroy(QdhtTc* q);
+
+}  // namespace gs

@@ -1,0 +1,146 @@
+/*
+ * gs_abi.h -- C ABI of the GB300 UPPE z-step core (gsolver_solid_qdht hot path).
+ *
+ * Plain pointers and sizes only.  Every entry point returns an int status (GS_OK = 0);
+ * gs_last_error() gives the message, which for physics errors is the reference's own
+ * exception string.  A handle owns one CUDA stream on one device and is not
+ * thread-safe: one host thread drives it.
+ *
+ * Complex arrays are interleaved (re, im) doubles.  Field arrays are row-major
+ * [n_r][n_t] with omega contiguous and omega in the reference's own order
+ * (omega0 + k*dw for k < n_t/2, then the negative offsets), i.e. the layout of the
+ * reference's FIELD / BIGBUFFER1 / BIGBUFFER2 (propagator.cu:380, 593).
+ *
+ * Reference interfaces replaced (paths within the reference project):
+ *   gs_create + gs_upload_tables  <- initialize_variables()/cuda_load_const()
+ *                                    (solver_main.cpp:265-398, propagator.cu:999-1108)
+ *   gs_set_field / gs_get_field   <- the host FIELD / BIGBUFFER2 globals (solver.h:169)
+ *   gs_nl_step                    <- calculate_NLstep(float_type*, float_type*)
+ *                                    (propagator.cu:121, 268-426)
+ *   gs_lstep                      <- ht_run(BIGBUFFER1) + calculate_Lstep() + ht_run(FIELD)
+ *                                    (propagator.cu:179-213, 516-626)
+ *   gs_qdht                       <- ht_run(f_complex*, f_complex*) (solver.h:337-346)
+ *                                    -> qdht_plan::run_many (fhatha.cpp:218-230)
+ *   gs_step                       <- propagator() (solver.h:269, propagator.cu:125-266)
+ *   gs_destroy                    <- destroy_variables()/cuda_free_const()
+ *                                    (solver_main.cpp:415-440)
+ */
+#ifndef GS_ABI_H
+#define GS_ABI_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GS_ABI_VERSION 1
+
+typedef struct gs_handle gs_handle;
+
+enum gs_status {
+    GS_OK = 0,
+    GS_ERR_ARG = 1,         /* bad argument / size */
+    GS_ERR_CUDA = 2,        /* CUDA runtime error (message in gs_last_error) */
+    GS_ERR_BLAST = 3,       /* "Attention!!!! Intensity is too big! Keep away, blast is possible." */
+    GS_ERR_NAN = 4,         /* "float_type photoionization_function(...): Intensity is nan!" */
+    GS_ERR_COLLAPSE = 5,    /* "Minimum Z step size reached, collapse is possible!" */
+    GS_ERR_STATE = 6,       /* call out of order (tables / field not set) */
+    GS_ERR_UNSUPPORTED = 7, /* grid not supported by this build */
+    GS_ERR_NOMEM = 8        /* device allocation failed */
+};
+
+enum gs_precision {
+    GS_PREC_FP64 = 0,       /* plain FP64 GPU path: the parity path against the FP64 reference */
+    GS_PREC_MIXED = 1       /* FP32 elementwise/FFT + tcgen05 3xTF32 QDHT with FP32 accumulation */
+};
+
+/* Scalars of the hot path, in the reference's scaled units
+ * (solver_main.cpp:385-393, process_input.cpp:58, ionization.cpp:11). */
+typedef struct gs_params {
+    int n_r, n_t;                 /* N_R (QDHT points), N_T (power of two, >= 64) */
+    int precision;                /* enum gs_precision */
+    int nonlinear;                /* 1: NONLINEARITY_ON; 0: zero NL response (shipped build) */
+    int device;                   /* CUDA device ordinal */
+    int reserved0;
+    double tstep, tmin, tmax, omega0;
+    double ionrate_denom;         /* IONRATE_DENOM (1e20 for the solid build) */
+    double neutral_density;       /* NEUTRAL_DENSITY */
+    double rho0;                  /* start carrier density of each plasma recurrence */
+    double ionization_potential;  /* U_i * IONRATE_DENOM / INTENSITY_DENOM */
+    double ponderomotive;         /* PONDEROMOTIVE_COEFFICIENT * IONRATE_DENOM */
+    double avalanche_cs;          /* AVALANCHE_CROSSSECTION */
+    double recombination_tau;     /* RECOMBINATION_TAU * IONRATE_DENOM */
+    double raman_fraction;        /* RAMAN_FRACTION */
+    double n2;                    /* NONLIN_REFRINDEX * INTENSITY_DENOM */
+    double omega_min, omega_max;  /* spectral window of the linear step */
+    double max_tolerance;         /* MAX_TOLERANCE of the step controller */
+} gs_params;
+
+/* Per-omega / per-k tables (host pointers, FP64, reference omega order). */
+typedef struct gs_tables {
+    const double* rate_ln;        /* IONIZATION_RATE_LN[8192] */
+    const double* plasma_func;    /* PLASMA_FUNC, complex [n_t] */
+    const double* raman_func;     /* RAMAN_FUNCTION, complex [n_t] */
+    const double* kerr;           /* KERR_PROFILE [n_t] */
+    const double* omega;          /* OMEGA [n_t] */
+    const double* wavenum;        /* WAVENUMBER, complex [n_t] */
+    const double* ho_disp;        /* HO_DISPERSION [n_t] */
+    const double* kt2;            /* transverse wavenumber squared per QDHT point [n_r] */
+    const double* qdht_c;         /* qdht_plan::C, [n_r*n_r], element (i,j) at C[i + n_r*j] */
+    const double* qdht_m1;        /* qdht_plan::m1 [n_r] */
+} gs_tables;
+
+/* Create a handle: allocates device state for one pulse on params->device. */
+int gs_create(const gs_params* params, gs_handle** out);
+
+/* Upload the tables (cuda_load_const).  Required before any step. */
+int gs_upload_tables(gs_handle* h, const gs_tables* tables);
+
+/* Set FIELD (r,omega) and BIGBUFFER2 (k,omega).  spec_k_omega may be NULL, in which case
+ * BIGBUFFER2 = ht_run(FIELD), as process_input.cpp:68-73 does at start-up. */
+int gs_set_field(gs_handle* h, const double* field_r_omega, const double* spec_k_omega);
+
+/* Copy FIELD and/or BIGBUFFER2 back to the host (either pointer may be NULL). */
+int gs_get_field(gs_handle* h, double* field_r_omega, double* spec_k_omega);
+
+/* calculate_NLstep: BIGBUFFER1 = RK4 increment of the NL response with step zstep;
+ * returns max |FIELD|^2 and max |BIGBUFFER1|^2. */
+int gs_nl_step(gs_handle* h, double zstep, double* max_a2, double* max_nl2);
+
+/* Copy BIGBUFFER1 (the last NL increment, (r,omega)) to the host. */
+int gs_get_nl(gs_handle* h, double* bb1_r_omega);
+
+/* ht_run(BIGBUFFER1) -> calculate_Lstep(zstep) -> ht_run(FIELD). */
+int gs_lstep(gs_handle* h, double zstep);
+
+/* ht_run on a host array [n_r][n_t] complex, in place. */
+int gs_qdht(gs_handle* h, double* data_r_omega);
+
+/* One propagator() call: repeats NL attempts until the controller accepts.
+ * current_z = CURRENT_Z, znet_cur = ZNET[n_Z], znet_prev = ZNET[n_Z-1];
+ * zstep_inout = ZSTEP, step_n_inout = STEP_N (incremented per rejected attempt, as the
+ * reference does); max_a2 / max_nl2 (may be NULL) of the accepted attempt. */
+int gs_step(gs_handle* h, double current_z, double znet_cur, double znet_prev,
+            double* zstep_inout, unsigned* step_n_inout, double* max_a2, double* max_nl2);
+
+/* Number of kernel launches issued on the handle's stream since creation. */
+long long gs_launch_count(const gs_handle* h);
+
+/* CUDA-event timing of the fused QDHT + linear-step kernels (the pair launched by each
+ * accepted gs_step / gs_lstep), on the handle's stream.  Returns the milliseconds and
+ * launch count accumulated since the previous call, then resets them; enable != 0 keeps
+ * timing on.  No extra synchronisation: the step's own final sync is reused. */
+int gs_qdht_timing(gs_handle* h, int enable, double* ms_total, int* launches);
+
+/* Release all device state. */
+int gs_destroy(gs_handle* h);
+
+/* Message of the last failed call on h (or of the last gs_create failure if h is NULL). */
+const char* gs_last_error(const gs_handle* h);
+
+/* Fixed string for a status code. */
+const char* gs_status_string(int status);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
