@@ -29,8 +29,11 @@ PREC_FP64, PREC_MIXED = 0, 1
 # every function declared in include/gs_abi.h
 ABI_FUNCTIONS = (
     "gs_create", "gs_upload_tables", "gs_set_field", "gs_get_field", "gs_nl_step", "gs_get_nl",
-    "gs_lstep", "gs_qdht", "gs_step", "gs_launch_count", "gs_qdht_timing", "gs_destroy",
+    "gs_lstep", "gs_qdht", "gs_step", "gs_stream", "gs_launch_count", "gs_qdht_timing", "gs_destroy",
     "gs_last_error", "gs_status_string",
+    # include/gs_setup.h
+    "gs_setup_from_config", "gs_setup_last_error", "gs_setup_grid", "gs_setup_params",
+    "gs_setup_tables", "gs_setup_field", "gs_setup_znet", "gs_setup_destroy",
 )
 
 
@@ -83,6 +86,8 @@ def load_library(path: str | None = None):
     L.gs_lstep.argtypes = [V, D]
     L.gs_qdht.argtypes = [V, V]
     L.gs_step.argtypes = [V, D, D, D, PD, C.POINTER(C.c_uint), PD, PD]
+    L.gs_stream.argtypes = [V]
+    L.gs_stream.restype = V
     L.gs_launch_count.argtypes = [V]
     L.gs_launch_count.restype = C.c_longlong
     L.gs_qdht_timing.argtypes = [V, I, PD, C.POINTER(C.c_int)]
@@ -107,7 +112,7 @@ PARAM_KEYS = ("tstep", "tmin", "tmax", "omega0", "ionrate_denom", "neutral_densi
 class Propagator:
     """One pulse on one GPU behind the C ABI.  ``setup`` is a dict with the scalar
     parameters and FP64 tables (keys as in gs_params / gs_tables); see
-    gsolver_gb300.setup.build_setup for the product's own builder."""
+    ``Setup(config).as_dict()`` for the product's own builder."""
 
     def __init__(self, setup: dict, precision: int = PREC_FP64, nonlinear: bool = True, device: int = 0):
         self.L = load_library()
@@ -194,6 +199,17 @@ class Propagator:
                                    C.byref(dz), C.byref(sn), C.byref(a2), C.byref(n2)))
         return dz.value, sn.value, a2.value, n2.value
 
+    def stream_ptr(self):
+        return int(self.L.gs_stream(self.h) or 0)
+
+    def set_field_ptr(self, field_ptr, spec_ptr=None):
+        """gs_set_field from raw host pointers (e.g. pinned buffers)."""
+        self._check(self.L.gs_set_field(self.h, C.c_void_p(field_ptr), C.c_void_p(spec_ptr) if spec_ptr else None))
+
+    def get_field_ptr(self, field_ptr, spec_ptr=None):
+        self._check(self.L.gs_get_field(self.h, C.c_void_p(field_ptr) if field_ptr else None,
+                                        C.c_void_p(spec_ptr) if spec_ptr else None))
+
     def launch_count(self):
         return int(self.L.gs_launch_count(self.h))
 
@@ -221,3 +237,74 @@ class Propagator:
             calls += 1
             cz += zstep
         return cz, zstep, step_n, calls
+
+
+# ----------------------------------------------------------------- host set-up --
+class Setup:
+    """Product set-up of one pulse from a reference-format config (include/gs_setup.h).
+
+    ``as_dict()`` returns the same keys Propagator takes, built by the library's own C++
+    (no oracle involved)."""
+
+    def __init__(self, config_path: str, overrides: dict | None = None, noise_seed: int = 0,
+                 noise_sigma: float = 0.0):
+        L = load_library()
+        V = C.c_void_p
+        L.gs_setup_from_config.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p),
+                                           C.c_ulonglong, C.c_double, C.POINTER(V)]
+        L.gs_setup_last_error.restype = C.c_char_p
+        L.gs_setup_grid.argtypes = [V, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        L.gs_setup_params.argtypes = [V, C.POINTER(Params)]
+        L.gs_setup_tables.argtypes = [V, C.POINTER(Tables)]
+        L.gs_setup_field.argtypes = [V, V]
+        L.gs_setup_znet.argtypes = [V, V, C.POINTER(C.c_double), C.POINTER(C.c_double), V]
+        L.gs_setup_destroy.argtypes = [V]
+        self.L = L
+        ov = overrides or {}
+        keys = (C.c_char_p * max(1, len(ov)))(*[k.encode() for k in ov])
+        vals = (C.c_char_p * max(1, len(ov)))(*[str(v).encode() for v in ov.values()])
+        s = V()
+        rc = L.gs_setup_from_config(config_path.encode(), len(ov), keys, vals, int(noise_seed), float(noise_sigma),
+                                    C.byref(s))
+        if rc:
+            raise GsError(rc, L.gs_setup_last_error().decode())
+        self.s = s
+
+    def __del__(self):
+        if getattr(self, "s", None):
+            self.L.gs_setup_destroy(self.s)
+            self.s = None
+
+    def as_dict(self) -> dict:
+        L = self.L
+        nr, nt, nz = C.c_int(), C.c_int(), C.c_int()
+        L.gs_setup_grid(self.s, C.byref(nr), C.byref(nt), C.byref(nz))
+        nr, nt, nz = nr.value, nt.value, nz.value
+        p = Params()
+        L.gs_setup_params(self.s, C.byref(p))
+        t = Tables()
+        L.gs_setup_tables(self.s, C.byref(t))
+
+        def grab(ptr, n, dt=np.float64):
+            return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_double)), shape=(n,)).copy().view(dt)
+        d = {k: getattr(p, k) for k in PARAM_KEYS}
+        d.update(n_r=nr, n_t=nt, rho0=p.rho0)
+        d["rate_ln"] = grab(t.rate_ln, 8192)
+        d["plasma_func"] = grab(t.plasma_func, 2 * nt, np.complex128)
+        d["raman_func"] = grab(t.raman_func, 2 * nt, np.complex128)
+        d["kerr"] = grab(t.kerr, nt)
+        d["omega"] = grab(t.omega, nt)
+        d["wavenum"] = grab(t.wavenum, 2 * nt, np.complex128)
+        d["ho_disp"] = grab(t.ho_disp, nt)
+        d["kt2"] = grab(t.kt2, nr)
+        d["qdht_c"] = grab(t.qdht_c, nr * nr).reshape(nr, nr, order="F")
+        d["qdht_m1"] = grab(t.qdht_m1, nr)
+        f = np.empty((nr, nt), np.complex128)
+        L.gs_setup_field(self.s, f.ctypes.data_as(C.c_void_p))
+        d["field"] = f
+        zn = np.empty(nz)
+        dz0, rmax = C.c_double(), C.c_double()
+        x = np.empty(nr)
+        L.gs_setup_znet(self.s, zn.ctypes.data_as(C.c_void_p), C.byref(dz0), C.byref(rmax), x.ctypes.data_as(C.c_void_p))
+        d.update(znet=zn, init_zstep=dz0.value, r_max=rmax.value, qdht_x=x)
+        return d

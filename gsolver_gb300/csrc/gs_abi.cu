@@ -109,6 +109,8 @@ const char* gs_last_error(const gs_handle* h) { return h ? h->err.c_str() : g_cr
 
 long long gs_launch_count(const gs_handle* h) { return h ? h->launches : 0; }
 
+void* gs_stream(const gs_handle* h) { return h ? (void*)h->st : nullptr; }
+
 static void free_all(gs_handle* h) {
     void* ptrs[] = {h->A, h->S, h->NB, h->KP, h->E, h->U, h->tw, h->pf, h->rm, h->kerr, h->rate,
                     h->omega, h->ho, h->kt2, h->Cm, h->m1, h->wavenum, h->staging, h->perm_dev,

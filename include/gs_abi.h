@@ -122,6 +122,9 @@ int gs_qdht(gs_handle* h, double* data_r_omega);
 int gs_step(gs_handle* h, double current_z, double znet_cur, double znet_prev,
             double* zstep_inout, unsigned* step_n_inout, double* max_a2, double* max_nl2);
 
+/* The handle's CUDA stream (a cudaStream_t), for callers that time or order work on it. */
+void* gs_stream(const gs_handle* h);
+
 /* Number of kernel launches issued on the handle's stream since creation. */
 long long gs_launch_count(const gs_handle* h);
 

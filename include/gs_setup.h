@@ -1,0 +1,48 @@
+/*
+ * gs_setup.h -- host set-up of one pulse from a reference-format config (C ABI).
+ *
+ * Builds, in FP64 on the host, everything the z-step core needs before its loop: the
+ * gs_params scalars, the gs_tables arrays, the start field and the z net.  Reference
+ * start-up replaced (paths within the reference project):
+ *   gs_setup_from_config  <- process_input() (process_input.cpp:33-95): load_info,
+ *                            load_nonlindata, initialize_variables (solver_main.cpp:265-398),
+ *                            calc_ionization_rate (ionization.cpp:313-355),
+ *                            calc_raman_function (solver_main.cpp:401-413),
+ *                            load_kerr_th_profiles (process_input.cpp:966-975),
+ *                            create_gg (pulse_gg.cpp:6-124), init_zstep_kerr (734-753)
+ *   overrides             <- the argv "KEY value" pairs every load_named* consults first
+ * The config's DISPERSION_FILE is resolved relative to the config file's directory.
+ * Start-field noise: noise_sigma != 0 multiplies the carrier by (1 + sigma (n1 + i n2))
+ * with seeded normals n1, n2 (splitmix64 + Box-Muller) in place of the reference's
+ * unseeded uniform NOISE_LEVEL draw.
+ */
+#ifndef GS_SETUP_H
+#define GS_SETUP_H
+
+#include "gs_abi.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct gs_setup gs_setup;
+
+int gs_setup_from_config(const char* config_path, int n_overrides, const char* const* keys,
+                         const char* const* values, unsigned long long noise_seed, double noise_sigma,
+                         gs_setup** out);
+const char* gs_setup_last_error(void);
+int gs_setup_grid(const gs_setup* s, int* n_r, int* n_t, int* n_z);
+/* scalars; the caller sets precision, nonlinear and device before gs_create */
+int gs_setup_params(const gs_setup* s, gs_params* out);
+/* pointers into memory owned by s (valid until gs_setup_destroy) */
+int gs_setup_tables(const gs_setup* s, gs_tables* out);
+/* start FIELD (r, omega), n_r*n_t interleaved complex, already divided by FIELD_DENOM */
+int gs_setup_field(const gs_setup* s, double* field_r_omega);
+/* ZNET[n_z], the first ZSTEP, R_MAX and the QDHT points x_n (r = x_n * R_MAX); any may be NULL */
+int gs_setup_znet(const gs_setup* s, double* znet, double* init_zstep, double* r_max, double* qdht_x);
+int gs_setup_destroy(gs_setup* s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
