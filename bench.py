@@ -1,0 +1,352 @@
+#!/usr/bin/env python
+"""bench.py -- field-point z-steps/s of the gsolver_solid_qdht z-step on GB300.
+
+A "step" is one accepted propagator() call (RK4 nonlinear increment, forward QDHT with
+the fused linear step, inverse QDHT) on the 1024 x 16384 fused-silica workload
+(R = 1.2 mm, 1.6 ps window, collimated 800 nm 50 fs 3 P_cr pulse, adaptive dz with
+MAX_TOLERANCE 1e-6), set up by the library's own C++ from a reference-format config.
+Synthetic: the pulse is generated (seeded 1e-4 complex Gaussian noise), no dataset.
+
+  value   device throughput (inputs resident in HBM), CUDA events on the handle's stream
+  e2e     the same metric through the public C ABI with pinned host buffers: every step
+          copies FIELD and BIGBUFFER2 in and out (the host globals propagator() works on)
+  fp64    the plain FP64 GPU path on the same workload, and the mixed path's relative L2
+          error against it after the same fixed-dz steps from the same start
+  roofline  the mixed QDHT kernels (tcgen05), algorithmic 8 N_r flop per field-point step
+  cpu_baseline  the CPU oracle (a port of the reference algorithm) on a bounded sample
+
+Multi-GPU: replicas only (one independent pulse per rank), value = total / max time.
+``--impl reference`` times the reference algorithm's CPU implementation (the oracle port,
+the reference itself needs MPI/FFTW/GSL) on the host cores, same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "field-point z-steps/s"
+UNIT = "field-point z-steps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1"])
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    r = int(os.environ.get("RANK", "0"))
+    w = int(os.environ.get("WORLD_SIZE", "1"))
+    lr = int(os.environ.get("LOCAL_RANK", "0"))
+    return r, w, lr
+
+
+def make_config(workload):
+    from gsolver_gb300 import configs
+    d = tempfile.mkdtemp(prefix="gs_bench_")
+    if workload == "c2":
+        return configs.fused_silica_c2(d), {"workload": "fused_silica_1024x16384", "n_r": 1024, "n_t": 16384,
+                                             "r_max_m": 1.2e-3, "window_s": 1.6e-12, "z_max_m": 3e-3,
+                                             "max_tolerance": 1e-6}
+    return configs.fused_silica_c1(d), {"workload": "fused_silica_256x2048", "n_r": 256, "n_t": 2048,
+                                         "r_max_m": 6e-4, "window_s": 4e-13, "z_max_m": 1e-3,
+                                         "max_tolerance": 1e3}
+
+
+class Clocks:
+    """nvidia-smi sampler (200 ms) running during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = tempfile.mktemp(prefix="gs_clocks_", suffix=".csv")
+
+    def __enter__(self):
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.close()
+
+    def summary(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 8:
+                    rows.append(parts)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [float(r[0]) for r in rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({n for r in rows for n, v in zip(names, r[4:8]) if v.lower().startswith("active")})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def run_z_steps(P, S, state, k):
+    """k accepted propagator() calls continuing the z-loop (solver_main.cpp:202-225)."""
+    znet = S["znet"]
+    for _ in range(k):
+        cz, n_z, zstep, step_n = state["z"], state["n_z"], state["zstep"], state["step_n"]
+        if cz >= znet[n_z]:
+            if n_z == len(znet) - 1:
+                raise RuntimeError("workload ran past its last ZNET point")
+            n_z += 1
+        zstep, step_n, _, _ = P.step(cz, znet[n_z], znet[n_z - 1], zstep, step_n)
+        state.update(z=cz + zstep, n_z=n_z, zstep=zstep, step_n=step_n + 1)
+
+
+def new_state(S):
+    return {"z": float(S["znet"][0]), "n_z": 0, "zstep": float(S["init_zstep"]), "step_n": 0}
+
+
+def read_profile_traffic():
+    """Per-launch DRAM bytes of the mixed QDHT kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "qdht_tc_fused_silica_1024x16384.md")
+    try:
+        with open(p) as f:
+            m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read())
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs"), d.get("bf16_tflops"), d.get("bf16_tflops_sustained"), "measured"
+    except OSError:
+        return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+def cpu_prepare(cfg_path):
+    """Oracle set-up of the workload (numpy restatement of the reference start-up)."""
+    from oracle import oracle, tables
+    oracle.build()
+    return tables.build(tables.Config.from_file(cfg_path), noise_seed=1234, noise_sigma=1e-4)
+
+
+def cpu_sample(T, nthreads=None):
+    """Oracle on the host cores: one RK4 NL step + linear step on a quarter of the rows
+    and both QDHTs on a quarter of the omega columns of the full grid, extrapolated to a
+    full step.  Returns (value, description, cores)."""
+    from oracle import oracle, tables
+    nr, nt = T["n_r"], T["n_t"]
+    cores = nthreads or os.cpu_count() or 1
+    rows = list(np.linspace(0, nr - 1, min(nr, max(2 * cores, nr // 4))).astype(int))
+    Ts = dict(T)
+    Ts["n_r"] = len(rows)
+    Ts["kt2"] = T["kt2"][rows]
+    O_rows = oracle.Oracle(Ts, nthreads=cores)
+    sub = np.ascontiguousarray(T["field"][rows])
+    dz = tables.init_zstep_kerr(T, T["field"])
+    t0 = time.perf_counter()
+    bb1, _, _ = O_rows.nl_step(sub, dz)
+    O_rows.lstep(bb1, sub, dz)
+    t_rows = time.perf_counter() - t0
+    cols = min(nt, max(32 * cores, nt // 4))
+    data = np.ascontiguousarray(T["field"][:, :cols])
+    Tq = dict(T)
+    Tq["n_t"] = cols
+    Oq = oracle.Oracle(Tq, nthreads=cores)
+    t0 = time.perf_counter()
+    d1 = Oq.qdht(data)
+    Oq.qdht(d1)
+    t_cols = time.perf_counter() - t0
+    t_step = t_rows * nr / len(rows) + t_cols * nt / cols
+    desc = (f"oracle (C port of the reference z-step, OpenMP {cores} threads, radix-2 FFT): RK4 NL step + "
+            f"linear step on {len(rows)} of {nr} rows, forward+inverse QDHT on {cols} of {nt} omega columns, "
+            f"extrapolated to one {nr}x{nt} step ({t_step:.2f} s)")
+    return nr * nt / t_step, desc, cores
+
+
+def reference_arm(args, rank, world):
+    if rank != 0:
+        return
+    cfg, conf = make_config(args.workload)
+    T = cpu_prepare(cfg)
+    vals = []
+    desc, cores = "", 1
+    for i in range(args.warmup + args.steps):
+        v, desc, cores = cpu_sample(T)
+        if i >= args.warmup:
+            vals.append(v)
+    value = float(np.median(vals))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": conf,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, lrank = dist_info()
+    if args.impl == "reference":
+        reference_arm(args, rank, world)
+        return
+    import torch
+    import gsolver_gb300 as gs
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(lrank)
+    cfg, conf = make_config(args.workload)
+    S = gs.Setup(cfg, noise_seed=1234 + rank, noise_sigma=1e-4).as_dict()
+    nr, nt = S["n_r"], S["n_t"]
+    prec = gs.PREC_MIXED if args.precision == "mixed" else gs.PREC_FP64
+    try:
+        P = gs.Propagator(S, precision=prec, device=lrank)
+    except gs.GsError as e:
+        if prec == gs.PREC_MIXED:
+            print(f"# mixed path unavailable ({e}); timing the FP64 path", file=sys.stderr)
+            prec = gs.PREC_FP64
+            P = gs.Propagator(S, precision=prec, device=lrank)
+        else:
+            raise
+    P.set_field(S["field"])
+    state = new_state(S)
+    run_z_steps(P, S, state, args.warmup)
+    stream = torch.cuda.ExternalStream(P.stream_ptr(), device=lrank)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    P.qdht_timing(enable=True)
+    n0 = P.launch_count()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with Clocks(lrank) as clk:
+        e0.record(stream)
+        run_z_steps(P, S, state, args.steps)
+        e1.record(stream)
+        e1.synchronize()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = P.launch_count() - n0
+    q_ms, q_n = P.qdht_timing(enable=False)
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = nr * nt * args.steps * world / (ms / 1e3)
+
+    # roofline: the QDHT pair (forward + fused linear step, inverse), 2*N_r^2*(2 N_t) flop each
+    hbm, bf16, bf16s, pk_kind = peaks()
+    flop_launch = 2.0 * nr * nr * 2 * nt
+    per_launch_ms = q_ms / max(q_n, 1)
+    achieved = flop_launch / (per_launch_ms / 1e3) / 1e12 if q_n else None
+    roof = {"bound": "tensor", "kernel": "qdht_tc" if prec == gs.PREC_MIXED else "qdht64 (FP64 CUDA cores)",
+            "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+            "frac": (achieved / bf16) if achieved else None, "traffic": read_profile_traffic() if prec == gs.PREC_MIXED else None,
+            "peak_kind": f"{pk_kind} cuBLAS bf16 burst", "launch_ms": per_launch_ms,
+            "qdht_share_of_step": (q_ms / ms) if ms else None,
+            "note": "algorithmic flop (8 N_r per field-point step); 3xTF32 executes 3x; TF32 tensor peak is half the bf16 peak"}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32+3xtf32" if prec == gs.PREC_MIXED else "f64",
+            "data": "synthetic (seeded Gaussian pulse + 1e-4 complex noise; no dataset)",
+            "config": dict(conf, precision="mixed" if prec == gs.PREC_MIXED else "fp64",
+                           parallelism=f"replicas{world}", l2="inputs larger than L2 (state ~1 GB per pulse)",
+                           z_reached_m=state["z"], dz_last_m=state["zstep"]),
+            "gpu_launches": launches, "roofline": roof, "clocks": clk.summary()}
+
+    # e2e through the public API with pinned host buffers
+    if not args.no_e2e:
+        f_h = torch.empty((nr, nt), dtype=torch.complex128, pin_memory=True)
+        s_h = torch.empty((nr, nt), dtype=torch.complex128, pin_memory=True)
+        P.get_field_ptr(f_h.data_ptr(), s_h.data_ptr())
+        ke = max(2, min(args.steps, 10))
+        t0 = time.perf_counter()
+        for _ in range(ke):
+            P.set_field_ptr(f_h.data_ptr(), s_h.data_ptr())
+            run_z_steps(P, S, state, 1)
+            P.get_field_ptr(f_h.data_ptr(), s_h.data_ptr())
+        te = time.perf_counter() - t0
+        line["e2e"] = {"value": nr * nt * ke / te, "unit": UNIT, "h2d_bytes_per_step": 2 * nr * nt * 16,
+                       "d2h_bytes_per_step": 2 * nr * nt * 16, "steps": ke,
+                       "api": "gs_set_field(FIELD, BIGBUFFER2) + gs_step + gs_get_field(FIELD, BIGBUFFER2)"}
+
+    # FP64 path on the same workload + mixed-vs-FP64 field error after the same fixed-dz steps
+    if prec == gs.PREC_MIXED and args.fp64_steps > 0:
+        P64 = gs.Propagator(S, precision=gs.PREC_FP64, device=lrank)
+        P64.set_field(S["field"])
+        st64 = new_state(S)
+        run_z_steps(P64, S, st64, 1)
+        s64 = torch.cuda.ExternalStream(P64.stream_ptr(), device=lrank)
+        a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a0.record(s64)
+        run_z_steps(P64, S, st64, args.fp64_steps)
+        a1.record(s64)
+        a1.synchronize()
+        ms64 = a0.elapsed_time(a1)
+        v64 = nr * nt * args.fp64_steps / (ms64 / 1e3)
+        # accuracy: both paths from the start field, fixed dz = first ZSTEP
+        nerr = 5
+        dz = float(S["init_zstep"])
+        for Q in (P, P64):
+            Q.set_field(S["field"])
+            for _ in range(nerr):
+                Q.nl_step(dz)
+                Q.lstep(dz)
+        fm = P.get_field(want_spec=False)
+        fd = P64.get_field(want_spec=False)
+        err = float(np.linalg.norm(fm - fd) / np.linalg.norm(fd))
+        line["fp64"] = {"value": v64, "unit": UNIT, "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps,
+                        "mixed_speedup": value / world / v64,
+                        "mixed_rel_l2_field_err": err, "err_steps": nerr, "err_dz_m": dz}
+        P64.close()
+
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, desc, cores = cpu_sample(cpu_prepare(cfg))
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": desc}
+    P.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -74,11 +74,16 @@ void fft(std::vector<cd>& a, int sign) {   // unnormalised, FFTW sign convention
         j ^= bit;
         if (i < j) std::swap(a[i], a[j]);
     }
+    std::vector<cd> tw(n / 2);
+    for (size_t k = 0; k < n / 2; k++) {
+        const double ang = sign * 2.0 * M_PI * (double)k / (double)n;
+        tw[k] = cd(std::cos(ang), std::sin(ang));
+    }
     for (size_t len = 2; len <= n; len <<= 1) {
+        const size_t step = n / len;
         for (size_t i = 0; i < n; i += len)
             for (size_t k = 0; k < len / 2; k++) {
-                const double ang = sign * 2.0 * M_PI * (double)k / (double)len;
-                const cd w(std::cos(ang), std::sin(ang));
+                const cd w = tw[k * step];
                 const cd u = a[i + k], v = a[i + k + len / 2] * w;
                 a[i + k] = u + v;
                 a[i + k + len / 2] = u - v;
