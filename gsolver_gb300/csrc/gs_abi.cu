@@ -256,6 +256,8 @@ int gs_upload_tables(gs_handle* h, const gs_tables* t) {
     if (h->tc) {
         std::string m;
         if (gs::qdht_tc_set_matrix(h->tc, t->qdht_c, t->qdht_m1, &m)) return fail(h, GS_ERR_CUDA, "mixed QDHT matrix: " + m);
+        if (gs::qdht_tc_set_lstep(h->tc, om.data(), wn.data(), ho.data(), t->kt2, h->p.omega_min, h->p.omega_max, &m))
+            return fail(h, GS_ERR_CUDA, "mixed QDHT: " + m);
     }
     h->tables_ok = true;
     return GS_OK;
@@ -297,8 +299,13 @@ int gs_qdht_timing(gs_handle* h, int enable, double* ms_total, int* launches) {
     return GS_OK;
 }
 
-// fold the CUDA-event time of the last fused QDHT pair into the totals (stream is idle)
+// fold the CUDA-event time of the last fused QDHT pair into the totals (stream is idle);
+// also surfaces an expired wait recorded by the tensor-core kernel
 static int collect_qdht_time(gs_handle* h) {
+    if (h->tc) {
+        std::string m;
+        if (gs::qdht_tc_check(h->tc, &m)) return fail(h, GS_ERR_CUDA, m);
+    }
     if (!h->ev_pending) return GS_OK;
     float ms = 0;
     CK(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
@@ -480,6 +487,7 @@ int gs_qdht(gs_handle* h, double* data) {
     int rc = permute_in(h, data, U1);
     if (!rc) rc = run_qdht(h, QDHT_PLAIN, U1, U2, 0.0);
     if (!rc) rc = permute_out(h, U2, data);
+    if (!rc) rc = collect_qdht_time(h);
     return rc;
 }
 

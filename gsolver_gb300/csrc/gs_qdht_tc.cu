@@ -1,19 +1,540 @@
-// gs_qdht_tc.cu -- placeholder until the tcgen05 kernel lands: mixed handles are refused.
+// gs_qdht_tc.cu -- mixed-precision QDHT on the 5th-generation tensor cores (sm_103a).
+//
+// ht_run (qdht_plan::run_many, fhatha.cpp:218-230) is the real GEMM
+//   Y[i][c] = sum_j H(i,j) X[j][c],  H(i,j) = m1_i C(i,j) / m1_j   (folded in FP64 at set-up)
+// over the 2*n_t interleaved (re, im) float columns of a [n_r][n_t] complex array.
+// It runs as 3xTF32 with FP32 accumulation: H = Hh + Hl and X = Xh + Xl split into
+// round-to-nearest TF32 parts, D = Hh Xh + Hh Xl + Hl Xh (relative error ~2^-21).
+//
+// One CTA computes a 128 (i) x 128 (c) tile, K looped in blocks of 32 (one 128-byte
+// swizzle row of FP32), 3 pipeline stages of 64 KiB in shared memory:
+//   warp 0      TMA producer: cp.async.bulk.tensor loads of the Hh/Hl tiles (SWIZZLE_128B)
+//               onto an mbarrier with expect-tx; owns the TMEM allocation.
+//   warp 1      MMA issuer: one thread issues tcgen05.mma.kind::tf32 (M=128, N=128, K=8)
+//               x 4 K-steps x 3 terms per stage, accumulator in TMEM (128 columns), and
+//               tcgen05.commit releases the stage.
+//   warps 2-9   B producers: read the X block from global memory (coalesced), apply the
+//               spectral-window mask of the inverse transform, split into TF32 hi/lo and
+//               write them K-major in the 128B-swizzled layout the MMA descriptor reads;
+//               then the epilogue: tcgen05.ld of the accumulator and either a plain store
+//               or the fused calculate_Lstep update of BIGBUFFER2 (propagator.cu:570-625).
+// Every mbarrier wait is bounded; on expiry the kernel records an error, drains what it
+// issued, frees TMEM and returns.
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gs_internal.cuh"
 #include "gs_qdht_tc.h"
 
 namespace gs {
-struct QdhtTc {};
-QdhtTc* qdht_tc_create(int, int, cudaStream_t, std::string* msg) {
-    if (msg) *msg = "mixed-precision QDHT not built";
-    return nullptr;
+
+namespace tc {
+
+constexpr int BM = 128, BN = 128, BK = 32, STAGES = 3;
+constexpr int TILE_BYTES = BM * BK * 4;                 // 16 KiB: one 128 x 32 FP32 tile
+constexpr int STAGE_BYTES = 4 * TILE_BYTES;             // Ah, Al, Bh, Bl
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int THREADS = 320;
+constexpr int NCONV = 256;                              // warps 2..9
+constexpr unsigned WAIT_LIMIT = 1u << 24;   // far above any legitimate wait (~0.1 ms)
+
+__constant__ float c_sqrt_ho_f[20];
+
+struct TcArgs {
+    const float* X;
+    float* Y;
+    int nr, ncols, mode;
+    float dz;
+    const float* kr;
+    const float* ki;
+    const float* ho;
+    const float* kt2;
+    const int* kmax;
+    unsigned* err;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
 }
-int qdht_tc_set_matrix(QdhtTc*, const double*, const double*, std::string* msg) {
-    if (msg) *msg = "not built";
-    return 1;
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
 }
-cudaError_t qdht_tc_run(QdhtTc*, int, const float*, float*, const LstepArgs&, long long*, std::string* msg) {
-    if (msg) *msg = "not built";
-    return cudaErrorNotSupported;
+
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, unsigned parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
 }
-void qdht_tc_destroy(QdhtTc*) {}
+
+// bounded wait: false when the limit expired
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+    for (unsigned it = 0; it < WAIT_LIMIT; it++)
+        if (mbar_try(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            smem_u32(dst)),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// tcgen05 shared-memory matrix descriptor: K-major, 128-byte swizzle, 8-row groups 1024 B apart
+__device__ __forceinline__ uint64_t make_desc(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)1 << 16;                 // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(1024 >> 4) << 32;       // stride byte offset: next 8-row group
+    d |= (uint64_t)1 << 46;                 // descriptor version (sm_100 family)
+    d |= (uint64_t)2 << 61;                 // SWIZZLE_128B
+    return d;
+}
+
+// instruction descriptor: kind::tf32, D = F32, A = B = TF32, both K-major, M = 128, N = 128
+__host__ __device__ constexpr uint32_t make_idesc() {
+    return (1u << 4)                     // D format F32
+           | (2u << 7)                   // A format TF32
+           | (2u << 10)                  // B format TF32
+           | ((uint32_t)(BN >> 3) << 17)  // N / 8
+           | ((uint32_t)(BM >> 4) << 24); // M / 16
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ float tf32_rna(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+}
+
+__device__ __forceinline__ void st_shared_v4(uint32_t addr, float a, float b, float c, float d) {
+    asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(a), "f"(b), "f"(c), "f"(d) : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+          "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
+          "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
+          "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+    for (int k = 0; k < 32; k++) v[k] = __uint_as_float(r[k]);
+}
+
+__device__ __forceinline__ float sqrt_ho_f(float x) {
+    float r = 0.f, xn = x;
+#pragma unroll
+    for (int j = 0; j < 20; j++) { r = fmaf(c_sqrt_ho_f[j], xn, r); xn *= x; }
+    return r;
+}
+
+__global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_constant__ CUtensorMap map_hi,
+                                                             const __grid_constant__ CUtensorMap map_lo, TcArgs a) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* bars = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+    uint64_t* full_a = bars;                  // [STAGES]  TMA tx
+    uint64_t* full_b = bars + STAGES;         // [STAGES]  256 converter arrivals
+    uint64_t* empty = bars + 2 * STAGES;      // [STAGES]  MMA commit
+    uint64_t* done = bars + 3 * STAGES;       // accumulator ready
+    uint32_t* tmem_slot = (uint32_t*)(bars + 3 * STAGES + 1);
+    volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int MT = a.nr / BM;
+    const int m_tile = blockIdx.x % MT, n_tile = blockIdx.x / MT;
+    const int m0 = m_tile * BM, c0 = n_tile * BN;
+    const int nk = a.nr / BK;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES; s++) {
+            mbar_init(&full_a[s], 1);
+            mbar_init(&full_b[s], NCONV);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(done, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(BN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        // ------------------------------------------------ TMA producer (A = Hh, Hl)
+        if (lane == 0) {
+            int issued = 0;
+            for (int kb = 0; kb < nk; kb++) {
+                const int s = kb % STAGES;
+                if (kb >= STAGES && !mbar_wait(&empty[s], ((kb / STAGES) + 1) & 1)) {
+                    atomicOr(a.err, 4u);
+                    *abort_flag = 1;
+                    break;
+                }
+                if (*abort_flag) break;
+                unsigned char* st = smem + s * STAGE_BYTES;
+                mbar_expect_tx(&full_a[s], 2 * TILE_BYTES);
+                tma_load_2d(st, &map_hi, kb * BK, m0, &full_a[s]);
+                tma_load_2d(st + TILE_BYTES, &map_lo, kb * BK, m0, &full_a[s]);
+                issued = kb + 1;
+            }
+            // drain: every issued TMA load has landed before the CTA may exit
+            for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; kb++)
+                if (!mbar_wait(&full_a[kb % STAGES], (kb / STAGES) & 1)) atomicOr(a.err, 4u);
+        }
+    } else if (warp == 1) {
+        // ------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            const uint32_t idesc = make_idesc();
+            uint32_t acc = 0;
+            for (int kb = 0; kb < nk; kb++) {
+                const int s = kb % STAGES;
+                const unsigned ph = (kb / STAGES) & 1;
+                if (!mbar_wait(&full_a[s], ph) || !mbar_wait(&full_b[s], ph)) {
+                    atomicOr(a.err, 8u);
+                    *abort_flag = 1;
+                    break;
+                }
+                if (*abort_flag) break;
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                unsigned char* st = smem + s * STAGE_BYTES;
+                const uint32_t ah = smem_u32(st), al = ah + TILE_BYTES;
+                const uint32_t bh = ah + 2 * TILE_BYTES, bl = ah + 3 * TILE_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < BK / 8; kk++) {
+                    const uint32_t off = kk * 32;   // 8 TF32 = 32 bytes along K inside the swizzle row
+                    mma_tf32(tmem, make_desc(al + off), make_desc(bh + off), idesc, acc);
+                    acc = 1;
+                    mma_tf32(tmem, make_desc(ah + off), make_desc(bl + off), idesc, 1);
+                    mma_tf32(tmem, make_desc(ah + off), make_desc(bh + off), idesc, 1);
+                }
+                mma_commit(&empty[s]);
+            }
+            mma_commit(done);
+        }
+    } else {
+        // ------------------------------------------------ B producers (X -> TF32 hi/lo, K-major)
+        const int t = threadIdx.x - 64;        // 0..255
+        const int n = t & (BN - 1), kh = t >> 7;
+        const int c = c0 + n;
+        const int kmx = (a.mode == QDHT_MASKED) ? a.kmax[c >> 1] : 0x7fffffff;
+        const float* xcol = a.X + c;
+        float xv[16];
+        auto fetch = [&](int kb) {
+            const int j0 = kb * BK + 16 * kh;
+#pragma unroll
+            for (int u = 0; u < 16; u++) {
+                const int j = j0 + u;
+                const float v = __ldg(xcol + (size_t)j * a.ncols);
+                xv[u] = (j > kmx) ? 0.f : v;
+            }
+        };
+        fetch(0);
+        const uint32_t rowoff = (uint32_t)((n >> 3) * 1024 + (n & 7) * 128);
+        for (int kb = 0; kb < nk; kb++) {
+            const int s = kb % STAGES;
+            if (kb >= STAGES && !mbar_wait(&empty[s], ((kb / STAGES) + 1) & 1)) {
+                atomicOr(a.err, 16u);
+                *abort_flag = 1;
+                break;
+            }
+            if (*abort_flag) break;
+            float hi[16], lo[16];
+#pragma unroll
+            for (int u = 0; u < 16; u++) {
+                hi[u] = tf32_rna(xv[u]);
+                lo[u] = tf32_rna(xv[u] - hi[u]);
+            }
+            if (kb + 1 < nk) fetch(kb + 1);
+            const uint32_t bh = smem_u32(smem + s * STAGE_BYTES + 2 * TILE_BYTES) + rowoff;
+            const uint32_t bl = bh + TILE_BYTES;
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                const uint32_t ch = (uint32_t)((((4 * kh + q) ^ (n & 7))) << 4);
+                st_shared_v4(bh + ch, hi[4 * q], hi[4 * q + 1], hi[4 * q + 2], hi[4 * q + 3]);
+                st_shared_v4(bl + ch, lo[4 * q], lo[4 * q + 1], lo[4 * q + 2], lo[4 * q + 3]);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(&full_b[s]);
+        }
+
+        // ------------------------------------------------ epilogue
+        const bool ok = mbar_wait(done, 0);
+        if (!ok) atomicOr(a.err, 32u);
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (ok && !*abort_flag) {
+            const int q = warp & 3;                 // TMEM lane quarter of this warp
+            const int half = (warp - 2) >> 2;       // which 64 columns
+            const int i = m0 + 32 * q + lane;
+            const float kt2i = a.kt2 ? a.kt2[i] : 0.f;
+            for (int cc = 0; cc < 2; cc++) {
+                const int col0 = 64 * half + 32 * cc;
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)col0, v);
+                float* yrow = a.Y + (size_t)i * a.ncols + c0 + col0;
+                if (a.mode != QDHT_LSTEP) {
+#pragma unroll
+                    for (int k = 0; k < 32; k += 4)
+                        *reinterpret_cast<float4*>(yrow + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+                } else {
+                    const int p0 = (c0 + col0) >> 1;
+#pragma unroll 4
+                    for (int e = 0; e < 16; e++) {
+                        const int p = p0 + e;
+                        if (i > a.kmax[p]) continue;        // outside the window: BIGBUFFER2 untouched
+                        const float k1 = a.kr[p], k2 = a.ki[p];
+                        const float sq = sqrt_ho_f(-kt2i / k1 / k1);
+                        float2 b2 = *reinterpret_cast<float2*>(yrow + 2 * e);
+                        const float inv = 1.f / (1.f + sq);
+                        b2.x += a.dz * v[2 * e] * inv;
+                        b2.y += a.dz * v[2 * e + 1] * inv;
+                        float sn, cs;
+                        sincosf(a.dz * (-a.ho[p] - sq * k1), &sn, &cs);
+                        const float m = expf(a.dz * k2);
+                        const float pr = m * cs, pi = m * sn;
+                        float2 f;
+                        f.x = b2.x * pr - b2.y * pi;
+                        f.y = b2.x * pi + b2.y * pr;
+                        *reinterpret_cast<float2*>(yrow + 2 * e) = f;
+                    }
+                }
+            }
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+
+    __syncthreads();
+    if (warp == 1 && lane == 0) {
+        // the accumulator is released only after every issued MMA has completed
+        if (!mbar_try(done, 0) && !mbar_wait(done, 0)) atomicOr(a.err, 64u);
+    }
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN));
+    }
+}
+
+}  // namespace tc
+
+struct QdhtTc {
+    int nr = 0, nt = 0;
+    cudaStream_t st = nullptr;
+    float *hh = nullptr, *hl = nullptr;
+    float *kr = nullptr, *ki = nullptr, *ho = nullptr, *kt2 = nullptr;
+    int* kmax = nullptr;
+    unsigned* err = nullptr;
+    CUtensorMap map_hi, map_lo;
+    bool have_lstep = false;
+};
+
+static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
+    }
+    return fn;
+}
+
+QdhtTc* qdht_tc_create(int nr, int nt, cudaStream_t st, std::string* msg) {
+    if (nr % tc::BM != 0) {
+        if (msg) *msg = "the tensor-core QDHT needs N_R to be a multiple of 128";
+        return nullptr;
+    }
+    if ((2 * nt) % tc::BN != 0) {
+        if (msg) *msg = "N_T must be a multiple of 64";
+        return nullptr;
+    }
+    if (!get_encode()) {
+        if (msg) *msg = "cuTensorMapEncodeTiled unavailable";
+        return nullptr;
+    }
+    QdhtTc* q = new QdhtTc();
+    q->nr = nr;
+    q->nt = nt;
+    q->st = st;
+    bool ok = cudaMalloc(&q->hh, (size_t)nr * nr * 4) == cudaSuccess && cudaMalloc(&q->hl, (size_t)nr * nr * 4) == cudaSuccess &&
+              cudaMalloc(&q->kr, nt * 4) == cudaSuccess && cudaMalloc(&q->ki, nt * 4) == cudaSuccess &&
+              cudaMalloc(&q->ho, nt * 4) == cudaSuccess && cudaMalloc(&q->kt2, nr * 4) == cudaSuccess &&
+              cudaMalloc(&q->kmax, nt * 4) == cudaSuccess && cudaMalloc(&q->err, 4) == cudaSuccess;
+    if (ok) ok = cudaMemset(q->err, 0, 4) == cudaSuccess;
+    if (ok) ok = cudaFuncSetAttribute(tc::qdht_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES) ==
+                 cudaSuccess;
+    if (!ok) {
+        if (msg) *msg = "allocation / attribute failed";
+        qdht_tc_destroy(q);
+        return nullptr;
+    }
+    auto enc = get_encode();
+    for (int w = 0; w < 2; w++) {
+        CUtensorMap* m = w ? &q->map_lo : &q->map_hi;
+        cuuint64_t gdim[2] = {(cuuint64_t)nr, (cuuint64_t)nr};           // {K (j), M (i)}
+        cuuint64_t gstride[1] = {(cuuint64_t)nr * 4};
+        cuuint32_t box[2] = {(cuuint32_t)tc::BK, (cuuint32_t)tc::BM};   // 32 floats = 128 B inner
+        cuuint32_t estr[2] = {1, 1};
+        CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, w ? (void*)q->hl : (void*)q->hh, gdim, gstride, box, estr,
+                         CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) {
+            if (msg) *msg = "cuTensorMapEncodeTiled failed";
+            qdht_tc_destroy(q);
+            return nullptr;
+        }
+    }
+    float k[20];
+    double b = 1.0;
+    for (int n = 1; n <= 20; n++) { b *= (0.5 - (n - 1)) / n; k[n - 1] = (float)b; }
+    if (cudaMemcpyToSymbol(tc::c_sqrt_ho_f, k, sizeof(k)) != cudaSuccess) {
+        if (msg) *msg = "constant upload failed";
+        qdht_tc_destroy(q);
+        return nullptr;
+    }
+    return q;
+}
+
+int qdht_tc_set_matrix(QdhtTc* q, const double* C, const double* m1, std::string* msg) {
+    const int nr = q->nr;
+    std::vector<float> hh((size_t)nr * nr), hl((size_t)nr * nr);
+    for (int i = 0; i < nr; i++)
+        for (int j = 0; j < nr; j++) {
+            const double h = m1[i] * C[(size_t)i + (size_t)nr * j] / m1[j];
+            // round-to-nearest TF32 (10 explicit mantissa bits) high part, FP32 remainder
+            float f = (float)h;
+            uint32_t u;
+            std::memcpy(&u, &f, 4);
+            u = (u + 0x1000u) & 0xFFFFE000u;
+            float hi;
+            std::memcpy(&hi, &u, 4);
+            hh[(size_t)i * nr + j] = hi;
+            hl[(size_t)i * nr + j] = (float)(h - (double)hi);
+        }
+    if (cudaMemcpy(q->hh, hh.data(), hh.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemcpy(q->hl, hl.data(), hl.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+        if (msg) *msg = "matrix upload failed";
+        return 1;
+    }
+    return 0;
+}
+
+int qdht_tc_set_lstep(QdhtTc* q, const double* omega, const double* wavenum, const double* ho, const double* kt2,
+                      double omega_min, double omega_max, std::string* msg) {
+    const int nt = q->nt, nr = q->nr;
+    std::vector<float> kr(nt), ki(nt), hf(nt), k2(nr);
+    std::vector<int> kmax(nt);
+    for (int p = 0; p < nt; p++) {
+        kr[p] = (float)wavenum[2 * p];
+        ki[p] = (float)wavenum[2 * p + 1];
+        hf[p] = (float)ho[p];
+        // calculate_Lstep's window, decided in FP64: omega in [min, max] and kt2 <= 0.25 Re(k^2)
+        int km = -1;
+        if (!(omega[p] < omega_min || omega[p] > omega_max)) {
+            const double lim = 0.25 * (wavenum[2 * p] * wavenum[2 * p] - wavenum[2 * p + 1] * wavenum[2 * p + 1]);
+            for (int k = 0; k < nr; k++)
+                if (!(kt2[k] > lim)) km = k;
+        }
+        kmax[p] = km;
+    }
+    for (int k = 0; k < nr; k++) k2[k] = (float)kt2[k];
+    bool ok = cudaMemcpy(q->kr, kr.data(), nt * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(q->ki, ki.data(), nt * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(q->ho, hf.data(), nt * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(q->kt2, k2.data(), nr * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(q->kmax, kmax.data(), nt * 4, cudaMemcpyHostToDevice) == cudaSuccess;
+    if (!ok) {
+        if (msg) *msg = "linear-step table upload failed";
+        return 1;
+    }
+    q->have_lstep = true;
+    return 0;
+}
+
+cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const LstepArgs& L, long long* nlaunch,
+                        std::string* msg) {
+    if (mode != QDHT_PLAIN && !q->have_lstep) {
+        if (msg) *msg = "linear-step tables not set";
+        return cudaErrorInvalidValue;
+    }
+    tc::TcArgs a;
+    a.X = X;
+    a.Y = Y;
+    a.nr = q->nr;
+    a.ncols = 2 * q->nt;
+    a.mode = mode;
+    a.dz = (float)L.dz;
+    a.kr = q->kr;
+    a.ki = q->ki;
+    a.ho = q->ho;
+    a.kt2 = q->kt2;
+    a.kmax = q->kmax;
+    a.err = q->err;
+    const unsigned grid = (unsigned)((q->nr / tc::BM) * (a.ncols / tc::BN));
+    tc::qdht_tc_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, q->st>>>(q->map_hi, q->map_lo, a);
+    (*nlaunch)++;
+    return cudaGetLastError();
+}
+
+int qdht_tc_check(QdhtTc* q, std::string* msg) {
+    unsigned e = 0;
+    if (cudaMemcpy(&e, q->err, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return 1;
+    if (e) {
+        if (msg) *msg = "tensor-core QDHT wait expired (code " + std::to_string(e) + ")";
+        cudaMemset(q->err, 0, 4);
+        return 1;
+    }
+    return 0;
+}
+
+void qdht_tc_destroy(QdhtTc* q) {
+    if (!q) return;
+    void* ptrs[] = {q->hh, q->hl, q->kr, q->ki, q->ho, q->kt2, q->kmax, q->err};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete q;
+}
+
 }  // namespace gs

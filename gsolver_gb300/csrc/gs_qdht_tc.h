@@ -15,6 +15,11 @@ struct QdhtTc;
 QdhtTc* qdht_tc_create(int nr, int nt, cudaStream_t st, std::string* msg);
 // Upload C (element (i,j) at C[i + nr*j]) and m1; builds the split hi/lo operands.
 int qdht_tc_set_matrix(QdhtTc* q, const double* C, const double* m1, std::string* msg);
+// Linear-step tables (position order, FP64): k(omega), HO dispersion, kt^2 and the window.
+int qdht_tc_set_lstep(QdhtTc* q, const double* omega, const double* wavenum, const double* ho, const double* kt2,
+                      double omega_min, double omega_max, std::string* msg);
+// Nonzero (with a message) if a kernel recorded an expired wait since the last check.
+int qdht_tc_check(QdhtTc* q, std::string* msg);
 // Y = QDHT(X) with the given mode (QDHT_PLAIN / QDHT_LSTEP / QDHT_MASKED).
 cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const LstepArgs& L, long long* nlaunch,
                         std::string* msg);
