@@ -40,7 +40,7 @@ constexpr int STAGE_BYTES = 4 * TILE_BYTES;             // Ah, Al, Bh, Bl
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
 constexpr int THREADS = 320;
 constexpr int NCONV = 256;                              // warps 2..9
-constexpr unsigned WAIT_LIMIT = 1u << 24;   // far above any legitimate wait (~0.1 ms)
+constexpr unsigned long long WAIT_NS = 200ull * 1000 * 1000;   // 200 ms; legitimate waits are < 1 ms
 
 __constant__ float c_sqrt_ho_f[20];
 
@@ -65,21 +65,38 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
 }
 
+// non-blocking probe of the phase with the given parity
 __device__ __forceinline__ bool mbar_try(uint64_t* bar, unsigned parity) {
     uint32_t ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(ok)
         : "r"(smem_u32(bar)), "r"(parity)
         : "memory");
     return ok != 0;
 }
 
-// bounded wait: false when the limit expired
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// wall-clock bounded wait: false when WAIT_NS expired
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
-    for (unsigned it = 0; it < WAIT_LIMIT; it++)
+    if (mbar_try(bar, parity)) return true;
+    const unsigned long long t0 = globaltimer_ns();
+    for (;;) {
         if (mbar_try(bar, parity)) return true;
-    return false;
+        if (globaltimer_ns() - t0 > WAIT_NS) return false;
+        __nanosleep(64);
+    }
+}
+
+// first expired wait of a launch: code | k-block << 8 | warp << 20, kept for the host
+__device__ __forceinline__ void record_stall(unsigned* err, unsigned code, int kb, int warp) {
+    atomicOr(err, code);
+    atomicCAS(err + 1, 0u, code | ((unsigned)(kb & 0xfff) << 8) | ((unsigned)warp << 20));
 }
 
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
@@ -191,6 +208,7 @@ __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_consta
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
+    __syncwarp();
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
                      "r"(BN));
@@ -208,7 +226,7 @@ __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_consta
             for (int kb = 0; kb < nk; kb++) {
                 const int s = kb % STAGES;
                 if (kb >= STAGES && !mbar_wait(&empty[s], ((kb / STAGES) + 1) & 1)) {
-                    atomicOr(a.err, 4u);
+                    record_stall(a.err, 4u, kb, warp);
                     *abort_flag = 1;
                     break;
                 }
@@ -221,8 +239,9 @@ __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_consta
             }
             // drain: every issued TMA load has landed before the CTA may exit
             for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; kb++)
-                if (!mbar_wait(&full_a[kb % STAGES], (kb / STAGES) & 1)) atomicOr(a.err, 4u);
+                if (!mbar_wait(&full_a[kb % STAGES], (kb / STAGES) & 1)) record_stall(a.err, 128u, kb, warp);
         }
+        __syncwarp();   // the warp reconverges before any block-wide barrier
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
@@ -231,8 +250,13 @@ __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_consta
             for (int kb = 0; kb < nk; kb++) {
                 const int s = kb % STAGES;
                 const unsigned ph = (kb / STAGES) & 1;
-                if (!mbar_wait(&full_a[s], ph) || !mbar_wait(&full_b[s], ph)) {
-                    atomicOr(a.err, 8u);
+                if (!mbar_wait(&full_a[s], ph)) {
+                    record_stall(a.err, 8u, kb, warp);
+                    *abort_flag = 1;
+                    break;
+                }
+                if (!mbar_wait(&full_b[s], ph)) {
+                    record_stall(a.err, 256u, kb, warp);
                     *abort_flag = 1;
                     break;
                 }
@@ -253,6 +277,7 @@ __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_consta
             }
             mma_commit(done);
         }
+        __syncwarp();
     } else {
         // ------------------------------------------------ B producers (X -> TF32 hi/lo, K-major)
         const int t = threadIdx.x - 64;        // 0..255
@@ -275,7 +300,7 @@ __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_consta
         for (int kb = 0; kb < nk; kb++) {
             const int s = kb % STAGES;
             if (kb >= STAGES && !mbar_wait(&empty[s], ((kb / STAGES) + 1) & 1)) {
-                atomicOr(a.err, 16u);
+                record_stall(a.err, 16u, kb, warp);
                 *abort_flag = 1;
                 break;
             }
@@ -300,10 +325,10 @@ __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_consta
         }
 
         // ------------------------------------------------ epilogue
-        const bool ok = mbar_wait(done, 0);
-        if (!ok) atomicOr(a.err, 32u);
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0) ? 1 : 0) != 0;
+        if (!ok && lane == 0) record_stall(a.err, 32u, nk, warp);
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (ok && !*abort_flag) {
+        if (ok && !__any_sync(0xffffffffu, *abort_flag)) {   // warp-uniform: tcgen05.ld is .sync.aligned
             const int q = warp & 3;                 // TMEM lane quarter of this warp
             const int half = (warp - 2) >> 2;       // which 64 columns
             const int i = m0 + 32 * q + lane;
@@ -345,9 +370,10 @@ __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_consta
     }
 
     __syncthreads();
-    if (warp == 1 && lane == 0) {
+    if (warp == 1) {
         // the accumulator is released only after every issued MMA has completed
-        if (!mbar_try(done, 0) && !mbar_wait(done, 0)) atomicOr(a.err, 64u);
+        if (lane == 0 && !mbar_wait(done, 0)) record_stall(a.err, 64u, nk, warp);
+        __syncwarp();
     }
     __syncthreads();
     if (warp == 0) {
@@ -401,8 +427,8 @@ QdhtTc* qdht_tc_create(int nr, int nt, cudaStream_t st, std::string* msg) {
     bool ok = cudaMalloc(&q->hh, (size_t)nr * nr * 4) == cudaSuccess && cudaMalloc(&q->hl, (size_t)nr * nr * 4) == cudaSuccess &&
               cudaMalloc(&q->kr, nt * 4) == cudaSuccess && cudaMalloc(&q->ki, nt * 4) == cudaSuccess &&
               cudaMalloc(&q->ho, nt * 4) == cudaSuccess && cudaMalloc(&q->kt2, nr * 4) == cudaSuccess &&
-              cudaMalloc(&q->kmax, nt * 4) == cudaSuccess && cudaMalloc(&q->err, 4) == cudaSuccess;
-    if (ok) ok = cudaMemset(q->err, 0, 4) == cudaSuccess;
+              cudaMalloc(&q->kmax, nt * 4) == cudaSuccess && cudaMalloc(&q->err, 8) == cudaSuccess;
+    if (ok) ok = cudaMemset(q->err, 0, 8) == cudaSuccess;
     if (ok) ok = cudaFuncSetAttribute(tc::qdht_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES) ==
                  cudaSuccess;
     if (!ok) {
@@ -519,11 +545,14 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
 }
 
 int qdht_tc_check(QdhtTc* q, std::string* msg) {
-    unsigned e = 0;
-    if (cudaMemcpy(&e, q->err, 4, cudaMemcpyDeviceToHost) != cudaSuccess) return 1;
-    if (e) {
-        if (msg) *msg = "tensor-core QDHT wait expired (code " + std::to_string(e) + ")";
-        cudaMemset(q->err, 0, 4);
+    unsigned e[2] = {0, 0};
+    if (cudaMemcpy(e, q->err, 8, cudaMemcpyDeviceToHost) != cudaSuccess) return 1;
+    if (e[0]) {
+        if (msg)
+            *msg = "tensor-core QDHT wait expired (codes " + std::to_string(e[0]) + ", first: code " +
+                   std::to_string(e[1] & 0xff) + " k-block " + std::to_string((e[1] >> 8) & 0xfff) + " warp " +
+                   std::to_string(e[1] >> 20) + ")";
+        cudaMemset(q->err, 0, 8);
         return 1;
     }
     return 0;
