@@ -53,6 +53,7 @@ class Params(C.Structure):
         ("avalanche_cs", C.c_double), ("recombination_tau", C.c_double),
         ("raman_fraction", C.c_double), ("n2", C.c_double),
         ("omega_min", C.c_double), ("omega_max", C.c_double), ("max_tolerance", C.c_double),
+        ("raman_tau", C.c_double), ("raman_omega", C.c_double),
     ]
 
 
@@ -122,6 +123,8 @@ class Propagator:
         for k in PARAM_KEYS:
             setattr(p, k, float(setup[k]))
         p.rho0 = float(setup.get("rho0", 0.0))
+        p.raman_tau = float(setup.get("raman_tau", 0.0))
+        p.raman_omega = float(setup.get("raman_omega", 0.0))
         self.params = p
         h = C.c_void_p()
         rc = self.L.gs_create(C.byref(p), C.byref(h))
@@ -288,7 +291,7 @@ class Setup:
         def grab(ptr, n, dt=np.float64):
             return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_double)), shape=(n,)).copy().view(dt)
         d = {k: getattr(p, k) for k in PARAM_KEYS}
-        d.update(n_r=nr, n_t=nt, rho0=p.rho0)
+        d.update(n_r=nr, n_t=nt, rho0=p.rho0, raman_tau=p.raman_tau, raman_omega=p.raman_omega)
         d["rate_ln"] = grab(t.rate_ln, 8192)
         d["plasma_func"] = grab(t.plasma_func, 2 * nt, np.complex128)
         d["raman_func"] = grab(t.raman_func, 2 * nt, np.complex128)

@@ -9,6 +9,10 @@ covers the whole spectral window.
 Workloads (synthetic: no dataset, the pulse is generated):
   fused_silica_c1   N_R=256,  N_T=2048,  R=600 um, 400 fs window, 1 mm in 500 fixed steps
   fused_silica_c2   N_R=1024, N_T=16384, R=1.2 mm, 1.6 ps window, 3 mm, adaptive (tol 1e-6)
+  argon_c5          N_R=512, N_T=32768, 3.9 um 80 fs w0 = 1 mm 4 P_cr pulse in 1 atm argon,
+                    2 ps window, R = 4 mm (R unstated by the workload; 4 w0 chosen), z = 20 cm,
+                    solid-path Keldysh rate with Ip = 15.76 eV (the gas PPT build is not on
+                    this path)
   hot_solid         small high-intensity grids where Keldysh, avalanche, loss and plasma
                     defocusing all act (peak ~5e13 W/cm^2)
 """
@@ -96,6 +100,28 @@ def fused_silica_c2(dirpath):
          "POWER_CR": "3", "WAVEFRONT_RADIUS": "1e100", "CE_PHASE": "0"}
     d.update(SILICA_NL)
     p = os.path.join(dirpath, "fused_silica_c2.txt")
+    with open(p, "w") as f:
+        f.write(_fmt(d))
+    return p
+
+
+ARGON_NL = {
+    "NONLIN_REFRINDEX": "1e-23", "RAMAN_FRACTION": "0", "TAU_RAMAN": "32e-15", "OMEGA_RAMAN": "1e13",
+    "IONIZATION_POTENTIAL": "15.76", "NEUTRAL_DENSITY": "2.5e25", "COLLISION_TAU": "190e-15",
+    "RECOMBINATION_TAU": "1e30", "AMBIENT_CARRIERS": "0",
+}
+
+
+def argon_c5(dirpath, n_r=512, n_t=32768, cep=0.0, name="argon_c5"):
+    """Argon filament at 3.9 um (Sellmeier n-1 = 5.547e-4 (1 + 5.15e-3/lam^2 + 4.19e-5/lam^4))."""
+    tabulate_medium(os.path.join(dirpath, "argon.rawdisp"), medium="argon", lam_min_um=0.15, lam_max_um=20.0)
+    d = {"LAMBDA_V": "3.9e-6", "N_T": str(n_t), "T_MIN": "-1e-12", "T_MAX": "1e-12",
+         "DISPERSION_FILE": "argon.rawdisp", "N_R": str(n_r), "R_MAX": "4e-3",
+         "N_Z": "201", "Z_MIN": "0", "Z_MAX": "0.2", "ZNET_TYPE": "e", "MAX_TOLERANCE": "1e-3",
+         "PULSE_SHAPE": "gg", "DURATION_FWHM": "80e-15", "DIAMETER_FWHM": repr(1e-3 * math.sqrt(2 * math.log(2))),
+         "POWER_CR": "4", "WAVEFRONT_RADIUS": "1e100", "CE_PHASE": repr(cep)}
+    d.update(ARGON_NL)
+    p = os.path.join(dirpath, name + ".txt")
     with open(p, "w") as f:
         f.write(_fmt(d))
     return p

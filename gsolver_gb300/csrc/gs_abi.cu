@@ -384,6 +384,8 @@ static int nl_step_impl(gs_handle* h, double dz) {
     }
     const bool raman = h->p.raman_fraction > 0.001;
     const bool kerr_on = h->p.n2 != 0;
+    // the oscillator recurrence replaces the RAMAN_FUNCTION FFT pair when its parameters are known
+    const bool raman_scan = raman && kerr_on && h->p.raman_tau > 0 && h->p.raman_omega > 0;
     FftArgs<Rl> fa{};
     fa.N = nt; fa.M = h->M; fa.P = h->P; fa.logM = h->logM;
     fa.tw = (const T2*)h->tw;
@@ -395,10 +397,24 @@ static int nl_step_impl(gs_handle* h, double dz) {
     pa.neutral_density = h->p.neutral_density; pa.rho0 = h->p.rho0;
     pa.ionization_potential = h->p.ionization_potential; pa.ponderomotive = h->p.ponderomotive;
     pa.avalanche_cs = h->p.avalanche_cs; pa.recombination_tau = h->p.recombination_tau;
+    pa.raman_scan = raman_scan;
+    if (raman_scan) {
+        const double dt = h->p.tstep, tau = h->p.raman_tau, om = h->p.raman_omega;
+        const double M = dt * (1 + om * om * tau * tau) / tau / (om * tau);   // solver_main.cpp:403
+        pa.fRM = h->p.raman_fraction * M;
+        pa.one_minus_fR = 1 - h->p.raman_fraction;
+        pa.dt_over_tau = dt / tau;
+        pa.dt_omega = dt * om;
+        const double m1 = std::exp(-dt / tau), mN = std::exp(-(double)nt * dt / tau);
+        pa.a_re = m1 * std::cos(om * dt);
+        pa.a_im = m1 * std::sin(om * dt);
+        pa.aN_re = mN * std::cos(om * dt * nt);
+        pa.aN_im = mN * std::sin(om * dt * nt);
+    }
     SpecArgs<Rl> sa{};
     sa.N = nt; sa.rows = nr; sa.u1 = U1; sa.u2 = U2; sa.u3 = U3;
     sa.pf = (const T2*)h->pf; sa.rm = (const T2*)h->rm; sa.kerr = (const Rl*)h->kerr;
-    sa.raman = raman; sa.kerr_on = kerr_on; sa.nb = NB; sa.kp = KP; sa.max_out = h->max_dev + 1;
+    sa.raman = raman && !raman_scan; sa.kerr_on = kerr_on; sa.nb = NB; sa.kp = KP; sa.max_out = h->max_dev + 1;
     for (int s = 0; s < 4; s++) {
         // stage input A + c*dz*k_prev, E = IFFT(.)/N   (propagator.cu:386-396, 640-641)
         FftArgs<Rl> f1 = fa;
@@ -411,7 +427,7 @@ static int nl_step_impl(gs_handle* h, double dz) {
         f2.rows = (kerr_on ? 3 : 2) * nr;
         CK(h, launch_fft<Rl>(-1, U1, U1, f2, h->st, &h->launches));
         CK(h, launch_spec1<Rl>(sa, h->st, &h->launches));
-        if (kerr_on && raman) {
+        if (kerr_on && raman && !raman_scan) {
             FftArgs<Rl> f3 = fa;
             f3.rows = nr; f3.tpost = 2; f3.e = E;
             CK(h, launch_fft<Rl>(+1, U3, U3, f3, h->st, &h->launches));

@@ -28,9 +28,12 @@ template <typename Rl> struct PlasmaArgs {
     typename Vec2<Rl>::T *u1, *u2, *u3;
     const Rl* rate;
     unsigned* err;
-    int raman;
+    int raman;        // 1: U3 = |E|^2 for the FFT convolution; 0: U3 = |E|^2 E (Raman off)
+    int raman_scan;   // 1: U3 = Q E with Q from the one-pole recurrence below
     double tstep_scaled, neutral_density, rho0, ionization_potential, ponderomotive;
     double avalanche_cs, recombination_tau;
+    // Raman oscillator h_k = fRM Im(a^k), a = exp(dt (-1/tau + i Omega)); circular wrap a^N
+    double a_re, a_im, aN_re, aN_im, fRM, one_minus_fR, dt_over_tau, dt_omega;
 };
 
 template <typename Rl> struct SpecArgs {

@@ -302,7 +302,86 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
         U1[t] = loss;
         U2[t] = T2{rho * e.x, rho * e.y};
         Rl I = e.x * e.x + e.y * e.y;
-        U3[t] = a.raman ? T2{I, (Rl)0} : T2{I * e.x - (Rl)0 * e.y, I * e.y + (Rl)0 * e.x};
+        if (!a.raman_scan) U3[t] = a.raman ? T2{I, (Rl)0} : T2{I * e.x - (Rl)0 * e.y, I * e.y + (Rl)0 * e.x};
+    }
+    if (!a.raman_scan) return;
+
+    // phase D: the delayed Kerr source Q = (1 - f_R) I + h (*) I without FFTs.  The
+    // reference forms IFFT(FFT(I) R)/N with R = FFT(h) + 1 - f_R (solver_main.cpp:401-413,
+    // propagator.cu:697-705): a circular convolution with h_k = fRM Im(a^k).  With the
+    // causal one-pole sum z_t = a z_{t-1} + I_t it is exactly
+    //     (h (*) I)_t = fRM Im((1 - a^N) z_t + a^{t+1} z_{N-1}),
+    // and z is a linear recurrence: chunk-local sums, an exclusive scan of chunk starts
+    // (complex affine maps with the common multiplier a^L), then a second chunk pass.
+    __syncthreads();
+    const T2 ra = T2{(Rl)a.a_re, (Rl)a.a_im};
+    T2 zl = T2{0, 0};
+    T2 aL = T2{1, 0};
+    if (c < P) {
+        for (int i = 0; i < L; i++) {
+            const T2 e = E[c * L + i];
+            zl = cmul(ra, zl);
+            zl.x += e.x * e.x + e.y * e.y;
+            aL = cmul(aL, ra);
+        }
+    }
+    // exclusive scan over chunks: start_{c+1} = aL * start_c + zl_c
+    {
+        T2 A = aL, B = zl;
+        const int lane = tid & 31, wid = tid >> 5;
+        if (c >= P) { A = T2{1, 0}; B = T2{0, 0}; }
+        for (int o = 1; o < 32; o <<= 1) {
+            T2 pa, pb;
+            pa.x = __shfl_up_sync(0xffffffffu, A.x, o); pa.y = __shfl_up_sync(0xffffffffu, A.y, o);
+            pb.x = __shfl_up_sync(0xffffffffu, B.x, o); pb.y = __shfl_up_sync(0xffffffffu, B.y, o);
+            if (lane >= o) { B = cadd(cmul(A, pb), B); A = cmul(A, pa); }
+        }
+        __shared__ T2 wA[8], wB[8];
+        __shared__ T2 zend;
+        if (lane == 31) { wA[wid] = A; wB[wid] = B; }
+        __syncthreads();
+        if (wid == 0) {
+            const int nw = nthr >> 5;
+            T2 xa = lane < nw ? wA[lane] : T2{1, 0}, xb = lane < nw ? wB[lane] : T2{0, 0};
+            for (int o = 1; o < 32; o <<= 1) {
+                T2 pa, pb;
+                pa.x = __shfl_up_sync(0xffffffffu, xa.x, o); pa.y = __shfl_up_sync(0xffffffffu, xa.y, o);
+                pb.x = __shfl_up_sync(0xffffffffu, xb.x, o); pb.y = __shfl_up_sync(0xffffffffu, xb.y, o);
+                if (lane >= o) { xb = cadd(cmul(xa, pb), xb); xa = cmul(xa, pa); }
+            }
+            if (lane < nw) { wA[lane] = xa; wB[lane] = xb; }
+            if (lane == nw - 1) zend = xb;   // z_{N-1}: all chunks composed from start 0
+        }
+        __syncthreads();
+        if (wid > 0) { B = cadd(cmul(A, wB[wid - 1]), B); }
+        // inclusive prefix B = z at the end of chunk c; the start of chunk c is the end of c-1
+        __shared__ T2 cend[256];
+        cend[tid] = B;
+        __syncthreads();
+        const T2 zs = (c == 0) ? T2{0, 0} : cend[c - 1];
+        const T2 zN = zend;
+        if (c < P) {
+            const T2 oma = T2{(Rl)(1.0 - a.aN_re), (Rl)(-a.aN_im)};
+            // a^{t+1} at the first sample of the chunk, then advanced by a
+            const double k0 = (double)(c * L + 1);
+            const double mag = exp(-k0 * a.dt_over_tau);
+            double sn, cs;
+            sincos(k0 * a.dt_omega, &sn, &cs);
+            T2 pw = T2{(Rl)(mag * cs), (Rl)(mag * sn)};
+            T2 z = zs;
+            const Rl fRM = (Rl)a.fRM, omf = (Rl)a.one_minus_fR;
+            for (int i = 0; i < L; i++) {
+                const int t = c * L + i;
+                const T2 e = E[t];
+                const Rl I = e.x * e.x + e.y * e.y;
+                z = cmul(ra, z);
+                z.x += I;
+                const T2 v = cadd(cmul(oma, z), cmul(pw, zN));
+                const Rl Q = omf * I + fRM * v.y;
+                U3[t] = T2{Q * e.x, Q * e.y};
+                pw = cmul(pw, ra);
+            }
+        }
     }
 }
 

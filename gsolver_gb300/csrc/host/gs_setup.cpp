@@ -418,6 +418,8 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
     p.omega_min = omin;
     p.omega_max = omax;
     p.max_tolerance = tol;
+    p.raman_tau = tauR;
+    p.raman_omega = omR;
     s->rate = std::move(rate); s->pf = std::move(pf); s->rm = std::move(rm); s->kerr = std::move(kerr);
     s->omega = std::move(om); s->wavenum = std::move(wn); s->ho = std::move(ho); s->kt2 = std::move(kt2);
     s->C = std::move(Cm); s->m1 = std::move(m1); s->x = std::move(x); s->field = std::move(field);

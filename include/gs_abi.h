@@ -73,6 +73,9 @@ typedef struct gs_params {
     double n2;                    /* NONLIN_REFRINDEX * INTENSITY_DENOM */
     double omega_min, omega_max;  /* spectral window of the linear step */
     double max_tolerance;         /* MAX_TOLERANCE of the step controller */
+    double raman_tau, raman_omega; /* TAU_RAMAN, OMEGA_RAMAN: when both > 0 the delayed Kerr
+                                      response is computed from this oscillator by an exact
+                                      recurrence instead of the RAMAN_FUNCTION FFT pair */
 } gs_params;
 
 /* Per-omega / per-k tables (host pointers, FP64, reference omega order). */

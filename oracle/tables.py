@@ -367,7 +367,7 @@ def build(cfg: Config, noise_seed: int | None = None, noise_sigma: float | None 
         recombination_tau=tau_rec_s, ionization_potential=Ui_s, ponderomotive=pond_s,
         avalanche_cs=aval, plasma_func=pf, rate_ln=rate, raman_func=raman, kerr=kerr,
         qdht_c=Q["C"], qdht_m1=Q["m1"], qdht_x=Q["x"], qdht_V=Q["V"], kt2=kt2,
-        ionrate_denom=IONRATE_DENOM,
+        ionrate_denom=IONRATE_DENOM, raman_tau=tauR, raman_omega=omR,
     ))
     T["field"] = create_gg(cfg, T, noise_seed, noise_sigma)
     return T

@@ -190,3 +190,40 @@ def test_collapse_error():
         P.step(0.0, T["znet"][1], T["znet"][0], 1e-9)
     assert ei.value.code == gs.GS_ERR_COLLAPSE
     assert "collapse" in str(ei.value)
+
+
+def test_argon_parity_no_raman():
+    """3.9 um argon (Raman off, Ip 15.76 eV, ~6e13 W/cm^2): NL step and three propagator() calls."""
+    d = tempfile.mkdtemp(prefix="gs_ar_")
+    p = configs.argon_c5(d, n_r=64, n_t=4096)
+    T = tables.build(tables.Config.from_file(p), noise_seed=3, noise_sigma=1e-4)
+    O = oracle.Oracle(T)
+    dz0 = tables.init_zstep_kerr(T, T["field"])
+    bb1, a2, n2 = O.nl_step(T["field"], dz0)
+    P = gs.Propagator(T)
+    P.set_field(T["field"])
+    P.nl_step(dz0)
+    assert rel(P.get_nl(), bb1) < TOL
+    out, st = O.run(T["field"], dz0, steps=3)
+    P.set_field(T["field"])
+    cz, zstep, step_n, calls = P.run(T["znet"], dz0, steps=3)
+    assert rel(P.get_field(want_spec=False), st["field"]) < TOL
+
+
+def test_fused_silica_256x2048_steps():
+    """The CPU-runnable fused-silica workload (256 x 2048) at full size, five propagator() calls,
+    set up by the product's own C++ and by the oracle (they agree to 1e-12)."""
+    d = tempfile.mkdtemp(prefix="gs_c1_")
+    p = configs.fused_silica_c1(d)
+    S = gs.Setup(p, noise_seed=1234, noise_sigma=1e-4).as_dict()
+    T = tables.build(tables.Config.from_file(p), noise_seed=1234, noise_sigma=1e-4)
+    O = oracle.Oracle(T)
+    out, st = O.run(T["field"], S["init_zstep"], steps=5)
+    P = gs.Propagator(S)
+    P.set_field(S["field"])
+    P.run(S["znet"], S["init_zstep"], steps=5)
+    f = P.get_field(want_spec=False)
+    assert rel(f, st["field"]) < TOL
+    dg, dr = O.dumps(f), O.dumps(st["field"])
+    assert rel(dg["f"], dr["f"]) < TOL
+    assert rel(dg["mI"], dr["mI"]) < TOL
