@@ -34,6 +34,7 @@ ABI_FUNCTIONS = (
     # include/gs_setup.h
     "gs_setup_from_config", "gs_setup_last_error", "gs_setup_grid", "gs_setup_params",
     "gs_setup_tables", "gs_setup_field", "gs_setup_znet", "gs_setup_destroy",
+    "gs_run_config", "gs_run_last_error", "gs_dump_reductions", "gs_get_time_field",
 )
 
 
@@ -61,6 +62,11 @@ class Tables(C.Structure):
     _fields_ = [(k, C.c_void_p) for k in (
         "rate_ln", "plasma_func", "raman_func", "kerr", "omega", "wavenum", "ho_disp", "kt2",
         "qdht_c", "qdht_m1")]
+
+
+class RunStats(C.Structure):
+    _fields_ = [("calls", C.c_longlong), ("step_n", C.c_uint), ("n_z", C.c_int), ("z", C.c_double),
+                ("zstep", C.c_double), ("seconds", C.c_double)]
 
 
 _lib = None
@@ -97,6 +103,11 @@ def load_library(path: str | None = None):
     L.gs_last_error.restype = C.c_char_p
     L.gs_status_string.argtypes = [I]
     L.gs_status_string.restype = C.c_char_p
+    L.gs_dump_reductions.argtypes = [V, V, D, V, V, V, V, V]
+    L.gs_get_time_field.argtypes = [V, V]
+    L.gs_run_config.argtypes = [C.c_char_p, C.c_char_p, I, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), I, I,
+                                C.c_ulonglong, D, C.c_longlong, C.POINTER(RunStats)]
+    L.gs_run_last_error.restype = C.c_char_p
     _lib = L
     return L
 
@@ -213,6 +224,21 @@ class Propagator:
         self._check(self.L.gs_get_field(self.h, C.c_void_p(field_ptr) if field_ptr else None,
                                         C.c_void_p(spec_ptr) if spec_ptr else None))
 
+    def dumps(self, qdht_x, r_max):
+        """Device reductions of the current FIELD for the .udf dumps (gs_dump_reductions)."""
+        nr, nt = self.nr, self.nt
+        out = {"mI": np.empty(nr), "f": np.empty(nr), "pm": np.empty(nr), "fa": np.empty(nt, np.complex128),
+               "s": np.empty(nt)}
+        x = np.ascontiguousarray(qdht_x, dtype=np.float64)
+        self._check(self.L.gs_dump_reductions(self.h, _ptr(x), float(r_max), _ptr(out["mI"]), _ptr(out["f"]),
+                                              _ptr(out["pm"]), _ptr(out["fa"]), _ptr(out["s"])))
+        return out
+
+    def time_field(self):
+        e = np.empty((self.nr, self.nt), np.complex128)
+        self._check(self.L.gs_get_time_field(self.h, _ptr(e)))
+        return e
+
     def launch_count(self):
         return int(self.L.gs_launch_count(self.h))
 
@@ -311,3 +337,18 @@ class Setup:
         L.gs_setup_znet(self.s, zn.ctypes.data_as(C.c_void_p), C.byref(dz0), C.byref(rmax), x.ctypes.data_as(C.c_void_p))
         d.update(znet=zn, init_zstep=dz0.value, r_max=rmax.value, qdht_x=x)
         return d
+
+
+def run_config(config_path: str, out_dir: str = ".", overrides: dict | None = None, precision: int = PREC_FP64,
+               device: int = 0, noise_seed: int = 0, noise_sigma: float = 0.0, max_calls: int = -1) -> dict:
+    """The reference's whole run (main loop + .udf dumps) on one GPU (gs_run_config)."""
+    L = load_library()
+    ov = overrides or {}
+    keys = (C.c_char_p * max(1, len(ov)))(*[k.encode() for k in ov])
+    vals = (C.c_char_p * max(1, len(ov)))(*[str(v).encode() for v in ov.values()])
+    st = RunStats()
+    rc = L.gs_run_config(config_path.encode(), out_dir.encode(), len(ov), keys, vals, int(precision), int(device),
+                         int(noise_seed), float(noise_sigma), int(max_calls), C.byref(st))
+    if rc:
+        raise GsError(rc, L.gs_run_last_error().decode())
+    return {k: getattr(st, k) for k, _ in RunStats._fields_}

@@ -47,6 +47,7 @@ struct gs_handle {
     double qdht_ms = 0;
     int qdht_n = 0;
     bool time_qdht = false, ev_pending = false;
+    double* dump_dev = nullptr;   // 3 n_r + 2 n_t doubles of reduction output, r weights
     std::string err;
 };
 
@@ -114,7 +115,7 @@ void* gs_stream(const gs_handle* h) { return h ? (void*)h->st : nullptr; }
 static void free_all(gs_handle* h) {
     void* ptrs[] = {h->A, h->S, h->NB, h->KP, h->E, h->U, h->tw, h->pf, h->rm, h->kerr, h->rate,
                     h->omega, h->ho, h->kt2, h->Cm, h->m1, h->wavenum, h->staging, h->perm_dev,
-                    h->err_dev, h->max_dev};
+                    h->err_dev, h->max_dev, h->dump_dev};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (h->tc) gs::qdht_tc_destroy(h->tc);
     if (h->ev0) cudaEventDestroy(h->ev0);
@@ -367,6 +368,35 @@ int gs_get_nl(gs_handle* h, double* bb1) {
 }
 
 template <typename Rl>
+static PlasmaArgs<Rl> plasma_args(gs_handle* h, bool raman, bool raman_scan) {
+    using T2 = typename Vec2<Rl>::T;
+    const size_t nel = (size_t)h->nr * h->nt;
+    T2* U1 = (T2*)h->U;
+    PlasmaArgs<Rl> pa{};
+    pa.N = h->nt; pa.e = (const T2*)h->E; pa.u1 = U1; pa.u2 = U1 + nel; pa.u3 = U1 + 2 * nel;
+    pa.rate = (const Rl*)h->rate; pa.err = h->err_dev; pa.raman = raman;
+    pa.tstep_scaled = h->p.tstep * h->p.ionrate_denom;
+    pa.neutral_density = h->p.neutral_density; pa.rho0 = h->p.rho0;
+    pa.ionization_potential = h->p.ionization_potential; pa.ponderomotive = h->p.ponderomotive;
+    pa.avalanche_cs = h->p.avalanche_cs; pa.recombination_tau = h->p.recombination_tau;
+    pa.raman_scan = raman_scan;
+    if (raman_scan) {
+        const double dt = h->p.tstep, tau = h->p.raman_tau, om = h->p.raman_omega;
+        const double M = dt * (1 + om * om * tau * tau) / tau / (om * tau);   // solver_main.cpp:403
+        pa.fRM = h->p.raman_fraction * M;
+        pa.one_minus_fR = 1 - h->p.raman_fraction;
+        pa.dt_over_tau = dt / tau;
+        pa.dt_omega = dt * om;
+        const double m1 = std::exp(-dt / tau), mN = std::exp(-(double)h->nt * dt / tau);
+        pa.a_re = m1 * std::cos(om * dt);
+        pa.a_im = m1 * std::sin(om * dt);
+        pa.aN_re = mN * std::cos(om * dt * h->nt);
+        pa.aN_im = mN * std::sin(om * dt * h->nt);
+    }
+    return pa;
+}
+
+template <typename Rl>
 static int nl_step_impl(gs_handle* h, double dz) {
     using T2 = typename Vec2<Rl>::T;
     const int nr = h->nr, nt = h->nt;
@@ -390,27 +420,7 @@ static int nl_step_impl(gs_handle* h, double dz) {
     fa.N = nt; fa.M = h->M; fa.P = h->P; fa.logM = h->logM;
     fa.tw = (const T2*)h->tw;
     fa.max_out = h->max_dev;
-    PlasmaArgs<Rl> pa{};
-    pa.N = nt; pa.e = E; pa.u1 = U1; pa.u2 = U2; pa.u3 = U3;
-    pa.rate = (const Rl*)h->rate; pa.err = h->err_dev; pa.raman = raman;
-    pa.tstep_scaled = h->p.tstep * h->p.ionrate_denom;
-    pa.neutral_density = h->p.neutral_density; pa.rho0 = h->p.rho0;
-    pa.ionization_potential = h->p.ionization_potential; pa.ponderomotive = h->p.ponderomotive;
-    pa.avalanche_cs = h->p.avalanche_cs; pa.recombination_tau = h->p.recombination_tau;
-    pa.raman_scan = raman_scan;
-    if (raman_scan) {
-        const double dt = h->p.tstep, tau = h->p.raman_tau, om = h->p.raman_omega;
-        const double M = dt * (1 + om * om * tau * tau) / tau / (om * tau);   // solver_main.cpp:403
-        pa.fRM = h->p.raman_fraction * M;
-        pa.one_minus_fR = 1 - h->p.raman_fraction;
-        pa.dt_over_tau = dt / tau;
-        pa.dt_omega = dt * om;
-        const double m1 = std::exp(-dt / tau), mN = std::exp(-(double)nt * dt / tau);
-        pa.a_re = m1 * std::cos(om * dt);
-        pa.a_im = m1 * std::sin(om * dt);
-        pa.aN_re = mN * std::cos(om * dt * nt);
-        pa.aN_im = mN * std::sin(om * dt * nt);
-    }
+    PlasmaArgs<Rl> pa = plasma_args<Rl>(h, raman, raman_scan);
     SpecArgs<Rl> sa{};
     sa.N = nt; sa.rows = nr; sa.u1 = U1; sa.u2 = U2; sa.u3 = U3;
     sa.pf = (const T2*)h->pf; sa.rm = (const T2*)h->rm; sa.kerr = (const Rl*)h->kerr;
@@ -426,8 +436,9 @@ static int nl_step_impl(gs_handle* h, double dz) {
         FftArgs<Rl> f2 = fa;
         f2.rows = (kerr_on ? 3 : 2) * nr;
         CK(h, launch_fft<Rl>(-1, U1, U1, f2, h->st, &h->launches));
-        CK(h, launch_spec1<Rl>(sa, h->st, &h->launches));
-        if (kerr_on && raman && !raman_scan) {
+        const bool fft_raman = kerr_on && raman && !raman_scan;
+        if (fft_raman) CK(h, launch_spec1<Rl>(sa, h->st, &h->launches));
+        if (fft_raman) {
             FftArgs<Rl> f3 = fa;
             f3.rows = nr; f3.tpost = 2; f3.e = E;
             CK(h, launch_fft<Rl>(+1, U3, U3, f3, h->st, &h->launches));
@@ -437,6 +448,7 @@ static int nl_step_impl(gs_handle* h, double dz) {
         }
         SpecArgs<Rl> s2 = sa;
         s2.stage = s;
+        s2.fuse_plasma = !fft_raman;
         CK(h, launch_spec2<Rl>(s2, h->st, &h->launches));
     }
     return GS_OK;
@@ -541,4 +553,106 @@ int gs_step(gs_handle* h, double current_z, double znet_cur, double znet_prev, d
             return collect_qdht_time(h);
         }
     }
+}
+
+// ------------------------------------------------------------------ dump reductions --
+template <typename Rl>
+static int dump_impl(gs_handle* h, const double* qdht_x, double r_max, double* max_I, double* flux,
+                     double* plasma_max, double* field_axis, double* avg_spectrum) {
+    using T2 = typename Vec2<Rl>::T;
+    const int nr = h->nr, nt = h->nt;
+    if (!h->dump_dev) CK(h, cudaMalloc((void**)&h->dump_dev, sizeof(double) * (4 * (size_t)nr + 2 * (size_t)nt)));
+    double* d_maxI = h->dump_dev;
+    double* d_flux = d_maxI + nr;
+    double* d_pmax = d_flux + nr;
+    double* d_w = d_pmax + nr;
+    double* d_spec = d_w + nr;
+    // E = BW-FFT(FIELD)/N_T, natural time order
+    FftArgs<Rl> f{};
+    f.N = nt; f.M = h->M; f.P = h->P; f.logM = h->logM; f.rows = nr;
+    f.tw = (const T2*)h->tw; f.tpost = 1;
+    CK(h, launch_fft<Rl>(+1, (const T2*)h->A, (T2*)h->E, f, h->st, &h->launches));
+    if (max_I || flux) CK(h, launch_row_intensity<Rl>((const T2*)h->E, nr, nt, h->p.tstep, d_maxI, d_flux, h->st, &h->launches));
+    if (plasma_max) {
+        CK(h, cudaMemsetAsync(h->err_dev, 0, 4, h->st));
+        PlasmaArgs<Rl> pa = plasma_args<Rl>(h, true, false);
+        CK(h, launch_plasma<Rl>(pa, nr, h->st, &h->launches));
+        CK(h, launch_row_max_re<Rl>((const T2*)h->U + (size_t)nr * nt, nr, nt, d_pmax, h->st, &h->launches));
+    }
+    std::vector<double> spec_pos;
+    if (avg_spectrum) {
+        if (!qdht_x || nr < 2) return fail(h, GS_ERR_ARG, "average spectrum needs the QDHT points");
+        // dump_type_average_spectrum_class, uniaxial branch (dump_types.cpp:441-453)
+        std::vector<double> w(nr);
+        w[0] = qdht_x[0] * (qdht_x[1] - qdht_x[0]);
+        for (int r = 1; r < nr; r++) w[r] = qdht_x[r] * (qdht_x[r] - qdht_x[r - 1]);
+        CK(h, cudaMemcpyAsync(d_w, w.data(), sizeof(double) * nr, cudaMemcpyHostToDevice, h->st));
+        CK(h, launch_spectrum<Rl>((const T2*)h->A, nr, nt, d_w, r_max * r_max / 2.0, d_spec, h->st, &h->launches));
+        spec_pos.resize(nt);
+        CK(h, cudaMemcpyAsync(spec_pos.data(), d_spec, sizeof(double) * nt, cudaMemcpyDeviceToHost, h->st));
+    }
+    if (max_I) CK(h, cudaMemcpyAsync(max_I, d_maxI, sizeof(double) * nr, cudaMemcpyDeviceToHost, h->st));
+    if (flux) CK(h, cudaMemcpyAsync(flux, d_flux, sizeof(double) * nr, cudaMemcpyDeviceToHost, h->st));
+    if (plasma_max) CK(h, cudaMemcpyAsync(plasma_max, d_pmax, sizeof(double) * nr, cudaMemcpyDeviceToHost, h->st));
+    std::vector<T2> axis;
+    if (field_axis) {
+        axis.resize(nt);
+        CK(h, cudaMemcpyAsync(axis.data(), h->E, sizeof(T2) * nt, cudaMemcpyDeviceToHost, h->st));
+    }
+    unsigned err = 0;
+    CK(h, cudaMemcpyAsync(&err, h->err_dev, 4, cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    for (int t = 0; t < (field_axis ? nt : 0); t++) {
+        field_axis[2 * t] = (double)axis[t].x;
+        field_axis[2 * t + 1] = (double)axis[t].y;
+    }
+    if (avg_spectrum)
+        for (int p = 0; p < nt; p++) avg_spectrum[h->perm[p]] = spec_pos[p];
+    if (err & 1u) return fail(h, GS_ERR_BLAST, gs_status_string(GS_ERR_BLAST));
+    if (err & 2u) return fail(h, GS_ERR_NAN, gs_status_string(GS_ERR_NAN));
+    return GS_OK;
+}
+
+int gs_dump_reductions(gs_handle* h, const double* qdht_x, double r_max, double* max_I, double* flux,
+                       double* plasma_max, double* field_axis, double* avg_spectrum) {
+    if (!h) return GS_ERR_ARG;
+    if (!h->tables_ok || !h->field_ok) return fail(h, GS_ERR_STATE, "tables / field not set");
+    CK(h, cudaSetDevice(h->p.device));
+    return h->fp64 ? dump_impl<double>(h, qdht_x, r_max, max_I, flux, plasma_max, field_axis, avg_spectrum)
+                   : dump_impl<float>(h, qdht_x, r_max, max_I, flux, plasma_max, field_axis, avg_spectrum);
+}
+
+int gs_get_time_field(gs_handle* h, double* e_r_t) {
+    if (!h || !e_r_t) return GS_ERR_ARG;
+    if (!h->tables_ok || !h->field_ok) return fail(h, GS_ERR_STATE, "tables / field not set");
+    CK(h, cudaSetDevice(h->p.device));
+    const size_t nel = (size_t)h->nr * h->nt;
+    cudaError_t e;
+    if (h->fp64) {
+        FftArgs<double> f{};
+        f.N = h->nt; f.M = h->M; f.P = h->P; f.logM = h->logM; f.rows = h->nr;
+        f.tw = (const double2*)h->tw; f.tpost = 1;
+        e = launch_fft<double>(+1, (const double2*)h->A, h->staging, f, h->st, &h->launches);
+    } else {
+        FftArgs<float> f{};
+        f.N = h->nt; f.M = h->M; f.P = h->P; f.logM = h->logM; f.rows = h->nr;
+        f.tw = (const float2*)h->tw; f.tpost = 1;
+        e = launch_fft<float>(+1, (const float2*)h->A, (float2*)h->E, f, h->st, &h->launches);
+        if (e == cudaSuccess) {
+            // widen to FP64 in natural order (time rows are natural): identity permutation copy
+            std::vector<float2> tmp(nel);
+            e = cudaMemcpyAsync(tmp.data(), h->E, nel * 8, cudaMemcpyDeviceToHost, h->st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(h->st);
+            for (size_t i = 0; e == cudaSuccess && i < nel; i++) {
+                e_r_t[2 * i] = tmp[i].x;
+                e_r_t[2 * i + 1] = tmp[i].y;
+            }
+            CK(h, e);
+            return GS_OK;
+        }
+    }
+    CK(h, e);
+    CK(h, cudaMemcpyAsync(e_r_t, h->staging, nel * 16, cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    return GS_OK;
 }

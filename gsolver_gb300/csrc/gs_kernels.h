@@ -42,6 +42,7 @@ template <typename Rl> struct SpecArgs {
     const typename Vec2<Rl>::T *pf, *rm;
     const Rl* kerr;
     int raman, kerr_on, stage;
+    int fuse_plasma;   // spec2 also adds PLASMA_FUNC * FFT(rho E) (spec1 skipped)
     typename Vec2<Rl>::T *nb, *kp;
     unsigned long long* max_out;
 };
@@ -59,6 +60,17 @@ cudaError_t launch_zero_nl(const typename Vec2<Rl>::T* A, typename Vec2<Rl>::T* 
 template <typename Rl>
 cudaError_t launch_permute(int dir, const void* src, void* dst, const int* perm, int N, size_t total,
                            cudaStream_t st, long long* nlaunch);
+
+// ---- dump reductions (gs_dumps.cu)
+template <typename Rl>
+cudaError_t launch_row_intensity(const typename Vec2<Rl>::T* E, int rows, int N, double tstep, double* maxI,
+                                 double* flux, cudaStream_t st, long long* nl);
+template <typename Rl>
+cudaError_t launch_row_max_re(const typename Vec2<Rl>::T* U, int rows, int N, double* out, cudaStream_t st,
+                              long long* nl);
+template <typename Rl>
+cudaError_t launch_spectrum(const typename Vec2<Rl>::T* F, int nr, int N, const double* w, double scale,
+                            double* out, cudaStream_t st, long long* nl);
 
 // ---- QDHT: Y[i][c] = m1_i * sum_j C(i,j) X[j][c] / m1_j over the 2*n_t real columns
 struct LstepArgs {

@@ -406,6 +406,8 @@ __global__ void spec2_kernel(SpecArgs<Rl> a) {
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         const int p = (int)(i % a.N);
         T2 k = a.u1[i];
+        // fused spec1 (no FFT Raman pair pending): FFT(loss) + FFT(rho E) * PLASMA_FUNC
+        if (a.fuse_plasma) k = cadd(k, cmul(a.u2[i], a.pf[p]));
         if (a.kerr_on) {   // += -j * KERR_PROFILE * FFT(Q E)
             const Rl K = a.kerr[p];
             T2 q = a.u3[i];

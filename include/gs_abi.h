@@ -137,6 +137,19 @@ long long gs_launch_count(const gs_handle* h);
  * timing on.  No extra synchronisation: the step's own final sync is reused. */
 int gs_qdht_timing(gs_handle* h, int enable, double* ms_total, int* launches);
 
+/* Reductions of the current FIELD behind the reference's .udf dumps (dump_types.cpp,
+ * FILTER_TYPE NO), computed on the device; any output may be NULL:
+ *   max_I[n_r], flux[n_r]   dump_type_maxI_class / dump_type_flux_class (104-165)
+ *   plasma_max[n_r]         dump_type_plasma_max_class (535-555)
+ *   field_axis[n_t]         complex E(t) at r = 0, dump_type_field_axis_class (404-417)
+ *   avg_spectrum[n_t]       dump_type_average_spectrum_class (427-457); needs qdht_x (the
+ *                           QDHT points x_n) and r_max */
+int gs_dump_reductions(gs_handle* h, const double* qdht_x, double r_max, double* max_I, double* flux,
+                       double* plasma_max, double* field_axis, double* avg_spectrum);
+
+/* The time-domain field BW-FFT(FIELD)/N_T, [n_r][n_t] complex: dump_type_full_class (77-97). */
+int gs_get_time_field(gs_handle* h, double* e_r_t);
+
 /* Release all device state. */
 int gs_destroy(gs_handle* h);
 

@@ -42,6 +42,24 @@ int gs_setup_field(const gs_setup* s, double* field_r_omega);
 int gs_setup_znet(const gs_setup* s, double* znet, double* init_zstep, double* r_max, double* qdht_x);
 int gs_setup_destroy(gs_setup* s);
 
+/* Outcome of gs_run_config. */
+typedef struct gs_run_stats {
+    long long calls;      /* propagator() calls */
+    unsigned step_n;      /* STEP_N (accepted + rejected attempts, as the reference counts) */
+    int n_z;              /* last ZNET index reached */
+    double z, zstep;      /* CURRENT_Z, ZSTEP at exit */
+    double seconds;       /* wall time of the z-loop */
+} gs_run_stats;
+
+/* The whole run of one config on one GPU: main() of the reference (solver_main.cpp:151-251)
+ * with the z-loop (202-225) and the .udf dumps (dumps.cpp, dump_types.cpp: flux, maxI,
+ * field_axis, plasma_max, average_spectrum, full; FILTER_TYPE NO) written under out_dir with
+ * the reference's file layout.  max_calls < 0 runs to the last ZNET point. */
+int gs_run_config(const char* config_path, const char* out_dir, int n_overrides, const char* const* keys,
+                  const char* const* values, int precision, int device, unsigned long long noise_seed,
+                  double noise_sigma, long long max_calls, gs_run_stats* stats);
+const char* gs_run_last_error(void);
+
 #ifdef __cplusplus
 }
 #endif
