@@ -28,6 +28,7 @@ struct gs_handle {
     gs_params p{};
     int nr = 0, nt = 0, P = 1, M = 0, logM = 0;
     bool fp64 = true;
+    bool fused = false;        // one-CTA rows: the fused front/back kernels per RK4 stage
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     size_t esz = 16;           // bytes per complex element
@@ -177,7 +178,9 @@ int gs_create(const gs_params* prm, gs_handle** out) {
             e = cudaMemcpy(h->tw, twf.data(), nt * 8, cudaMemcpyHostToDevice);
         }
     }
-    if (e == cudaSuccess) e = h->fp64 ? fft_set_smem<double>(h->M) : fft_set_smem<float>(h->M);
+    if (e == cudaSuccess) e = h->fp64 ? fft_set_smem<double>(h->M, nt) : fft_set_smem<float>(h->M, nt);
+    h->fused = h->P == 1 && (h->fp64 ? nl_fused_supported<double>(nt) : nl_fused_supported<float>(nt));
+    if (e == cudaSuccess && h->fused) e = h->fp64 ? nl_fused_setup<double>(nt) : nl_fused_setup<float>(nt);
     if (e == cudaSuccess) {
         double k[20], b = 1.0;
         for (int n = 1; n <= 20; n++) { b *= (0.5 - (n - 1)) / n; k[n - 1] = b; }
@@ -425,6 +428,19 @@ static int nl_step_impl(gs_handle* h, double dz) {
     sa.N = nt; sa.rows = nr; sa.u1 = U1; sa.u2 = U2; sa.u3 = U3;
     sa.pf = (const T2*)h->pf; sa.rm = (const T2*)h->rm; sa.kerr = (const Rl*)h->kerr;
     sa.raman = raman && !raman_scan; sa.kerr_on = kerr_on; sa.nb = NB; sa.kp = KP; sa.max_out = h->max_dev + 1;
+    if (h->fused && (raman_scan || !raman)) {
+        for (int s = 0; s < 4; s++) {
+            FftArgs<Rl> f1 = fa;
+            f1.rows = nr; f1.kp = KP;
+            f1.cdz = (s == 0) ? 0.0 : (s < 3 ? dz * 0.5 : dz);
+            f1.track_max = (s == 0);
+            CK(h, launch_nl_front<Rl>(f1, pa, A, nr, h->st, &h->launches));
+            SpecArgs<Rl> s2 = sa;
+            s2.stage = s;
+            CK(h, launch_nl_back<Rl>(fa, s2, nr, h->st, &h->launches));
+        }
+        return GS_OK;
+    }
     for (int s = 0; s < 4; s++) {
         // stage input A + c*dz*k_prev, E = IFFT(.)/N   (propagator.cu:386-396, 640-641)
         FftArgs<Rl> f1 = fa;

@@ -88,14 +88,35 @@ template <int SIGN, typename Rl, typename T2> struct RegDFT<1, SIGN, Rl, T2> {
 };
 
 // -------------------------------------------------------------- shared-memory FFT --
-// One radix-R stage on a row of length M held in shared memory.
+// A row of M complex lives in shared memory with one pad slot per 16 elements
+// (element i at pad16(i)): every radix-16/8/4/2 stage below then touches 16 distinct
+// 8-byte bank pairs per half-warp (checked for each stage shape: sub >= 16, sub = 8, 4, 1).
+__host__ __device__ __forceinline__ int pad16(int i) { return i + (i >> 4); }
+__host__ __device__ __forceinline__ int padded_len(int M) { return M + (M >> 4); }
+
+// Twiddles w(j) = exp(-2 pi i j / N) from two shared tables: w = hi[j >> 6] * lo[j & 63].
+template <typename Rl> struct TwTab {
+    const C2<Rl>* hi;
+    const C2<Rl>* lo;
+    __device__ __forceinline__ C2<Rl> operator()(int j) const { return cmul(hi[j >> 6], lo[j & 63]); }
+};
+
+// fill hi[N/64] and lo[64] from the global table tw[j] = exp(-2 pi i j / N)
+template <typename Rl>
+__device__ __forceinline__ void load_twiddles(C2<Rl>* hi, C2<Rl>* lo, const C2<Rl>* __restrict__ tw, int N, int tid,
+                                              int nthr) {
+    for (int j = tid; j < N / 64; j += nthr) hi[j] = tw[j * 64];
+    for (int j = tid; j < 64; j += nthr) lo[j] = tw[j];
+}
+
+// One radix-R stage on a padded row of length M.
 // Forward (SIGN=-1, decimation in frequency): butterfly (q, block) reads R elements at
 // stride sub=S/R, DFT_R, multiplies output r by w_S^{q r}, writes them back in place.
 // Inverse (SIGN=+1) undoes the forward stage (conjugate twiddle first, then DFT_R).
-// tw[j] = exp(-2*pi*i*j/Nfull); a sub-row of length M = Nfull/twstride uses tw[j*twstride].
+// A sub-row of length M = N/twstride uses w_M^k = w_N^{k twstride}.
 template <int R, int SIGN, typename Rl>
-__device__ __forceinline__ void fft_stage(C2<Rl>* buf, int M, int S, const C2<Rl>* __restrict__ tw,
-                                          int twstride, int tid, int nthr) {
+__device__ __forceinline__ void fft_stage(C2<Rl>* buf, int M, int S, const TwTab<Rl>& tw, int twstride, int tid,
+                                          int nthr) {
     using T2 = C2<Rl>;
     const int sub = S / R;
     const int nb = M / R;
@@ -105,24 +126,24 @@ __device__ __forceinline__ void fft_stage(C2<Rl>* buf, int M, int S, const C2<Rl
         const int base = (b / sub) * S + q;
         T2 x[R];
 #pragma unroll
-        for (int r = 0; r < R; r++) x[r] = buf[base + sub * r];
-        if (SIGN > 0) {
+        for (int r = 0; r < R; r++) x[r] = buf[pad16(base + sub * r)];
+        if (SIGN > 0 && q != 0) {
 #pragma unroll
-            for (int r = 1; r < R; r++) x[r] = cmul(x[r], cconj(__ldg(&tw[q * r * scale])));
+            for (int r = 1; r < R; r++) x[r] = cmul(x[r], cconj(tw(q * r * scale)));
         }
         RegDFT<R, SIGN, Rl, T2>::run(x);
-        if (SIGN < 0) {
+        if (SIGN < 0 && q != 0) {
 #pragma unroll
-            for (int r = 1; r < R; r++) x[r] = cmul(x[r], __ldg(&tw[q * r * scale]));
+            for (int r = 1; r < R; r++) x[r] = cmul(x[r], tw(q * r * scale));
         }
 #pragma unroll
-        for (int r = 0; r < R; r++) buf[base + sub * r] = x[r];
+        for (int r = 0; r < R; r++) buf[pad16(base + sub * r)] = x[r];
     }
 }
 
 template <int SIGN, typename Rl>
-__device__ __forceinline__ void fft_stage_rt(int R, C2<Rl>* buf, int M, int S, const C2<Rl>* tw,
-                                             int twstride, int tid, int nthr) {
+__device__ __forceinline__ void fft_stage_rt(int R, C2<Rl>* buf, int M, int S, const TwTab<Rl>& tw, int twstride,
+                                             int tid, int nthr) {
     switch (R) {
         case 16: fft_stage<16, SIGN, Rl>(buf, M, S, tw, twstride, tid, nthr); break;
         case 8: fft_stage<8, SIGN, Rl>(buf, M, S, tw, twstride, tid, nthr); break;
@@ -138,9 +159,9 @@ __host__ __device__ inline int fft_stage_radix(int logM, int j) {
     return (j < logM / 4) ? 16 : (1 << (logM % 4));
 }
 
-// Full in-place M-point FFT in shared memory (caller syncs before and after).
+// Full in-place M-point FFT of a padded shared row (caller syncs before; ends synced).
 template <int SIGN, typename Rl>
-__device__ void smem_fft(C2<Rl>* buf, int M, int logM, const C2<Rl>* tw, int twstride, int tid, int nthr) {
+__device__ void smem_fft(C2<Rl>* buf, int M, int logM, const TwTab<Rl>& tw, int twstride, int tid, int nthr) {
     const int J = fft_num_stages(logM);
     if (SIGN < 0) {
         int S = M;

@@ -50,7 +50,7 @@ template <typename Rl> struct SpecArgs {
 template <typename Rl>
 cudaError_t launch_fft(int sign, const typename Vec2<Rl>::T* in, typename Vec2<Rl>::T* out, FftArgs<Rl> a,
                        cudaStream_t st, long long* nlaunch);
-template <typename Rl> cudaError_t fft_set_smem(int M);
+template <typename Rl> cudaError_t fft_set_smem(int M, int N);
 template <typename Rl> cudaError_t launch_plasma(PlasmaArgs<Rl> a, int rows, cudaStream_t st, long long* nlaunch);
 template <typename Rl> cudaError_t launch_spec1(SpecArgs<Rl> a, cudaStream_t st, long long* nlaunch);
 template <typename Rl> cudaError_t launch_spec2(SpecArgs<Rl> a, cudaStream_t st, long long* nlaunch);
@@ -60,6 +60,15 @@ cudaError_t launch_zero_nl(const typename Vec2<Rl>::T* A, typename Vec2<Rl>::T* 
 template <typename Rl>
 cudaError_t launch_permute(int dir, const void* src, void* dst, const int* perm, int N, size_t total,
                            cudaStream_t st, long long* nlaunch);
+
+// ---- fused RK4 stage (gs_nl_fused.cu), rows that fit one CTA's shared memory
+template <typename Rl> bool nl_fused_supported(int N);
+template <typename Rl> cudaError_t nl_fused_setup(int N);
+template <typename Rl>
+cudaError_t launch_nl_front(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2<Rl>::T* A, int rows,
+                            cudaStream_t st, long long* nl);
+template <typename Rl>
+cudaError_t launch_nl_back(FftArgs<Rl> f, SpecArgs<Rl> s, int rows, cudaStream_t st, long long* nl);
 
 // ---- dump reductions (gs_dumps.cu)
 template <typename Rl>

@@ -14,30 +14,34 @@
 //                     avalanche term), then loss and rho*E in parallel.
 //   spec1/spec2       spectral combination and the RK4 accumulation with max|N|^2.
 // Templates instantiate the FP64 parity path (double) and the mixed path (float).
-#include "gs_kernels.h"
 #include "gs_internal.cuh"
+#include "gs_kernels.h"
+#include "gs_plasma.cuh"
 
 namespace gs {
-
-// solver.h:55-107 constants of the ionization table
-#define GS_ION_TOL 0.003304003148325
-#define GS_ION_MIN_LN 29.933606208922594
-#define GS_INT_DENOM_LN 36.841361487904734
 
 // ------------------------------------------------------------------ FFT kernels --
 // Spectral-side load ops (inverse transforms) and time-side ops.
 enum { SPRE_NONE = 0, SPRE_STAGE = 1 };
 enum { TPOST_STORE = 0, TPOST_DIVN = 1, TPOST_DIVN_MULE = 2 };
 
+// shared memory of fft_sub_kernel: the padded row, then the two twiddle tables
+template <typename Rl> __host__ __device__ inline size_t fft_smem_bytes(int M, int N) {
+    return ((size_t)padded_len(M) + N / 64 + 64) * sizeof(typename Vec2<Rl>::T);
+}
+
 template <typename Rl, int SIGN>
-__global__ void __launch_bounds__(sizeof(Rl) == 8 ? 256 : 512) fft_sub_kernel(const C2<Rl>* __restrict__ in, C2<Rl>* __restrict__ out,
-                                                      FftArgs<Rl> a) {
+__global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) fft_sub_kernel(const C2<Rl>* __restrict__ in,
+                                                                              C2<Rl>* __restrict__ out, FftArgs<Rl> a) {
     using T2 = C2<Rl>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T2* buf = reinterpret_cast<T2*>(smem_raw);
     const int M = a.M;
+    T2* twh = buf + padded_len(M);
+    T2* twl = twh + a.N / 64;
     const size_t base = (size_t)blockIdx.x * M;   // sub-rows are contiguous blocks of M
     const int tid = threadIdx.x, nthr = blockDim.x;
+    load_twiddles<Rl>(twh, twl, a.tw, a.N, tid, nthr);
 
     // ---- load (with the spectral-side op for inverse transforms)
     double lmax = 0.0;
@@ -54,19 +58,20 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 256 : 512) fft_sub_kernel(co
                 v.y = v.y + (Rl)a.cdz * k.y;
             }
         }
-        buf[i] = v;
+        buf[pad16(i)] = v;
     }
     if (SIGN > 0 && a.track_max) {
         for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
         if ((tid & 31) == 0) atomic_max_nonneg(a.max_out, lmax);
     }
     __syncthreads();
-    smem_fft<SIGN, Rl>(buf, M, a.logM, a.tw, a.P, tid, nthr);
+    const TwTab<Rl> tw{twh, twl};
+    smem_fft<SIGN, Rl>(buf, M, a.logM, tw, a.P, tid, nthr);
 
     // ---- store (time-side op only when this kernel finishes an inverse transform)
     const Rl rn = (Rl)a.N;
     for (int i = tid; i < M; i += nthr) {
-        T2 v = buf[i];
+        T2 v = buf[pad16(i)];
         if (SIGN > 0 && a.P == 1 && a.tpost != TPOST_STORE) {
             v.x = v.x / rn;
             v.y = v.y / rn;
@@ -120,22 +125,6 @@ __global__ void __launch_bounds__(256) fft_cross_kernel(const C2<Rl>* __restrict
 }
 
 // ------------------------------------------------------------------- plasma ----
-// photoionization_function without the rho > rho_n test (ionization.cpp:98-147,
-// KELDYSH solid branch): 0 below 1e13 W/m^2, log-interpolated table above.
-template <typename Rl>
-__device__ __forceinline__ Rl photo_rate(Rl I, const Rl* __restrict__ tab, unsigned* err) {
-    if (I < (Rl)(1e13 / 1e16)) return (Rl)0;
-    Rl lnI = log(I) + (Rl)GS_INT_DENOM_LN;
-    if (isnan(lnI)) { atomicOr(err, ERRBIT_NAN); return (Rl)0; }
-    int n = (int)floor((lnI - (Rl)GS_ION_MIN_LN) / (Rl)GS_ION_TOL);
-    if (n > 8192 - 2) { atomicOr(err, ERRBIT_BLAST); return (Rl)0; }
-    if (n < 0) return (Rl)0;
-    Rl lnIn = (Rl)GS_ION_MIN_LN + n * (Rl)GS_ION_TOL;
-    Rl w0 = __ldg(&tab[n]), w1 = __ldg(&tab[n + 1]);
-    Rl lnW = w0 + (lnI - lnIn) * (w1 - w0) / (Rl)GS_ION_TOL;
-    return exp(lnW);
-}
-
 // calculate_plasmadensity_losses_small (ionization.cpp:9-95), single-level branch, for
 // one row per CTA.  Inputs: E (time row).  Outputs: U1 = loss, U2 = rho*E,
 // U3 = |E|^2 (Raman on) or |E|^2 * E (Raman off).  The first recurrence step sees
@@ -474,7 +463,7 @@ __global__ void permute_out_kernel(const C2<Rl>* __restrict__ src, double2* __re
 // ------------------------------------------------------------------ launchers --
 template <typename Rl>
 static int fft_threads(int M) {
-    const int maxt = sizeof(Rl) == 8 ? 256 : 512;
+    const int maxt = sizeof(Rl) == 8 ? 512 : 1024;
     int t = M / 16;
     if (t < 32) t = 32;
     if (t > maxt) t = maxt;
@@ -484,7 +473,7 @@ static int fft_threads(int M) {
 template <typename Rl>
 cudaError_t launch_fft(int sign, const C2<Rl>* in, C2<Rl>* out, FftArgs<Rl> a, cudaStream_t st, long long* nlaunch) {
     // a.rows full rows of length a.N = a.P * a.M
-    const size_t smem = (size_t)a.M * sizeof(C2<Rl>);
+    const size_t smem = fft_smem_bytes<Rl>(a.M, a.N);
     const int nsub = a.rows * a.P;
     const int thr = fft_threads<Rl>(a.M);
     const int cross_thr = 256;
@@ -521,8 +510,8 @@ cudaError_t launch_fft(int sign, const C2<Rl>* in, C2<Rl>* out, FftArgs<Rl> a, c
 }
 
 template <typename Rl>
-cudaError_t fft_set_smem(int M) {
-    const int smem = M * (int)sizeof(C2<Rl>);
+cudaError_t fft_set_smem(int M, int N) {
+    const int smem = (int)fft_smem_bytes<Rl>(M, N);
     cudaError_t e = cudaFuncSetAttribute(fft_sub_kernel<Rl, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(fft_sub_kernel<Rl, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
@@ -577,7 +566,7 @@ cudaError_t launch_permute(int dir, const void* src, void* dst, const int* perm,
 
 #define GS_INST(Rl)                                                                                          \
     template cudaError_t launch_fft<Rl>(int, const C2<Rl>*, C2<Rl>*, FftArgs<Rl>, cudaStream_t, long long*); \
-    template cudaError_t fft_set_smem<Rl>(int);                                                              \
+    template cudaError_t fft_set_smem<Rl>(int, int);                                                              \
     template cudaError_t launch_plasma<Rl>(PlasmaArgs<Rl>, int, cudaStream_t, long long*);                   \
     template cudaError_t launch_spec1<Rl>(SpecArgs<Rl>, cudaStream_t, long long*);                           \
     template cudaError_t launch_spec2<Rl>(SpecArgs<Rl>, cudaStream_t, long long*);                           \

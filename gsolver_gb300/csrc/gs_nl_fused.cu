@@ -1,0 +1,326 @@
+// gs_nl_fused.cu -- one RK4 stage of calculate_NLstep in two kernels per row, for rows that
+// fit one CTA's shared memory (N_t <= 16384 complex float / 8192 complex double).
+//
+//   nl_front_kernel  stage input X = A + c dz k_prev, E = IFFT(X)/N_t (shared memory),
+//                    then with E resident: photoionization rates, the Heun carrier-density
+//                    recurrence by multiple shooting (ionization.cpp:9-95), the Raman
+//                    response as an exact one-pole recurrence (solver_main.cpp:401-413,
+//                    propagator.cu:697-705), and the three source rows
+//                    loss(t), rho(t) E(t), Q(t) E(t) written once.
+//   nl_back_kernel   FFT of the three sources in turn, N = FFT(loss) + PLASMA_FUNC FFT(rho E)
+//                    - j KERR_PROFILE FFT(Q E) (propagator.cu:679-710), and the RK4
+//                    accumulation of calculate_NLstep (propagator.cu:386-421) with max |N|^2.
+// Versus the separate kernels this removes the E round trip and every pass of the
+// recurrences over global memory: per stage ~88 B per field point of HBM traffic.
+#include "gs_internal.cuh"
+#include "gs_kernels.h"
+#include "gs_plasma.cuh"
+
+namespace gs {
+
+__host__ __device__ __forceinline__ int pad32(int i) { return i + (i >> 5); }
+// rate slots: padded row, rounded to 4 elements so that what follows stays 16-byte aligned
+__host__ __device__ __forceinline__ int wb_count(int N) { return (N + N / 32 + 1 + 3) & ~3; }
+
+template <typename Rl> struct FrontSmem {
+    static __host__ __device__ size_t bytes(int N, int nthr) {
+        using T2 = typename Vec2<Rl>::T;
+        return (size_t)padded_len(N) * sizeof(T2)       // E row
+               + (size_t)(N / 64 + 64) * sizeof(T2)     // twiddle tables
+               + (size_t)wb_count(N) * sizeof(Rl)       // photoionization rates W_t
+               + (size_t)nthr * sizeof(Rl)              // chunk starts of the density
+               + (size_t)nthr * sizeof(T2)              // chunk ends of the Raman sum
+               + 64 * sizeof(T2) + 64 * sizeof(Rl) + 64;   // scan scratch, flags
+    }
+};
+
+template <typename Rl>
+__global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(FftArgs<Rl> f, PlasmaArgs<Rl> a,
+                                                                              const typename Vec2<Rl>::T* __restrict__ A) {
+    using T2 = C2<Rl>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int N = f.N;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    T2* E = reinterpret_cast<T2*>(smem_raw);
+    T2* twh = E + padded_len(N);
+    T2* twl = twh + N / 64;
+    Rl* Wb = reinterpret_cast<Rl*>(twl + 64);
+    Rl* s_start = Wb + wb_count(N);
+    T2* cend = reinterpret_cast<T2*>(s_start + nthr);
+    T2* scA = cend + nthr;
+    T2* scB = scA + 32;
+    Rl* rA = reinterpret_cast<Rl*>(scB + 32);
+    Rl* rB = rA + 32;
+    int* flag = reinterpret_cast<int*>(rB + 32);
+    const size_t base = (size_t)blockIdx.x * N;
+
+    // ---- stage input and inverse FFT (propagator.cu:386-396, 640-641)
+    load_twiddles<Rl>(twh, twl, f.tw, N, tid, nthr);
+    double lmax = 0.0;
+    for (int i = tid; i < N; i += nthr) {
+        T2 v = A[base + i];
+        if (f.track_max) lmax = fmax(lmax, (double)v.x * (double)v.x + (double)v.y * (double)v.y);
+        if (f.cdz != 0) {
+            const T2 k = f.kp[base + i];
+            v.x = v.x + (Rl)f.cdz * k.x;
+            v.y = v.y + (Rl)f.cdz * k.y;
+        }
+        E[pad16(i)] = v;
+    }
+    if (f.track_max) {
+        for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+        if ((tid & 31) == 0) atomic_max_nonneg(f.max_out, lmax);
+    }
+    __syncthreads();
+    const TwTab<Rl> tw{twh, twl};
+    smem_fft<+1, Rl>(E, N, f.logM, tw, 1, tid, nthr);
+    const Rl rn = (Rl)N;
+    const Rl ND = (Rl)a.neutral_density, tstep = (Rl)a.tstep_scaled;
+    const Rl U = (Rl)a.ionization_potential, Pc = (Rl)a.ponderomotive, AV = (Rl)a.avalanche_cs;
+    const Rl invND = (Rl)1 / ND, invTAU = (Rl)1 / (Rl)a.recombination_tau;
+    // E /= N and the rates W_t (the first sample is treated as E_0 = 0: W_0 = g_0 = 0)
+    for (int t = tid; t < N; t += nthr) {
+        T2 e = E[pad16(t)];
+        e.x = e.x / rn;
+        e.y = e.y / rn;
+        E[pad16(t)] = e;
+        Wb[pad32(t)] = (t > 0) ? photo_rate<Rl>(e.x * e.x + e.y * e.y, a.rate, a.err) : (Rl)0;
+    }
+    __syncthreads();
+
+    auto g_of = [&](int t) -> Rl {
+        if (t == 0) return (Rl)0;
+        const T2 e = E[pad16(t)];
+        const Rl I = e.x * e.x + e.y * e.y;
+        return AV / (U + Pc * I) * I;
+    };
+    const int L = N / nthr;          // chunk of consecutive samples per thread
+    const int c = tid;
+    const int t0 = c * L;
+    // the exact recurrence over this thread's chunk from start value s (rho_{t0-1})
+    auto run_chunk = [&](Rl s, Rl* dout) -> Rl {
+        Rl ro = s, d = (Rl)1;
+        Rl W0 = (t0 > 0) ? Wb[pad32(t0 - 1)] : (Rl)0, g0 = (t0 > 0) ? g_of(t0 - 1) : (Rl)0;
+        for (int i = 0; i < L; i++) {
+            const int t = t0 + i;
+            const Rl W1 = Wb[pad32(t)], g1 = g_of(t);
+            if (t > 0) ro = heun_step<Rl>(ro, W0, g0, W1, g1, tstep, ND, invND, invTAU, &d);
+            W0 = W1;
+            g0 = g1;
+        }
+        *dout = d;
+        return ro;
+    };
+
+    // ---- carrier density by multiple shooting (Newton on the chunk starts)
+    s_start[c] = (c == 0) ? (Rl)a.rho0 : (Rl)0;
+    if (tid == 0) *flag = 0;
+    __syncthreads();
+    const Rl tol = sizeof(Rl) == 8 ? (Rl)1e-13 : (Rl)1e-6;
+    for (int it = 0; it < 16; it++) {
+        const Rl sc = s_start[c];
+        Rl D;
+        const Rl e = run_chunk(sc, &D);
+        Rl Am = D, Bm = e - D * sc;
+        block_affine_scan<Rl>(Am, Bm, (Rl)1, (Rl)0, rA, rB);
+        const Rl next = Am * s_start[0] + Bm;          // start of chunk c + 1
+        Rl change = 0, mag = 0;
+        __syncthreads();
+        if (c + 1 < nthr) {
+            change = fabs(next - s_start[c + 1]);
+            mag = fabs(next);
+            s_start[c + 1] = next;
+        }
+        for (int o = 16; o > 0; o >>= 1) {
+            change = fmax(change, __shfl_xor_sync(0xffffffffu, change, o));
+            mag = fmax(mag, __shfl_xor_sync(0xffffffffu, mag, o));
+        }
+        if ((tid & 31) == 0) { rA[tid >> 5] = change; rB[tid >> 5] = mag; }
+        __syncthreads();
+        if (tid == 0) {
+            Rl cm = 0, mm = 0;
+            for (int w = 0; w < (nthr >> 5); w++) { cm = fmax(cm, rA[w]); mm = fmax(mm, rB[w]); }
+            *flag = (cm <= tol * mm) ? 1 : 0;
+        }
+        __syncthreads();
+        if (*flag) break;
+        __syncthreads();
+    }
+
+    // ---- Raman: z_t = a z_{t-1} + I_t, chunk sums then an exclusive scan of chunk starts
+    const bool rscan = a.raman_scan != 0;
+    const T2 ra = T2{(Rl)a.a_re, (Rl)a.a_im};
+    T2 zs = T2{0, 0}, zN = T2{0, 0};
+    if (rscan) {
+        T2 zl = T2{0, 0}, aL = T2{1, 0};
+        for (int i = 0; i < L; i++) {
+            const T2 e = E[pad16(t0 + i)];
+            zl = cmul(ra, zl);
+            zl.x += e.x * e.x + e.y * e.y;
+            aL = cmul(aL, ra);
+        }
+        T2 Am = aL, Bm = zl;
+        block_affine_scan<T2>(Am, Bm, T2{1, 0}, T2{0, 0}, scA, scB);
+        cend[c] = Bm;                                   // z at the end of chunk c
+        __syncthreads();
+        zs = (c == 0) ? T2{0, 0} : cend[c - 1];
+        zN = cend[nthr - 1];
+    }
+
+    // ---- final pass: density, Raman Q and the three source rows
+    {
+        Rl ro = s_start[c], d = 1;
+        Rl W0 = (t0 > 0) ? Wb[pad32(t0 - 1)] : (Rl)0, g0 = (t0 > 0) ? g_of(t0 - 1) : (Rl)0;
+        T2 z = zs;
+        T2 pw = T2{0, 0};
+        if (rscan) {
+            const double k0 = (double)(t0 + 1);
+            const double mg = exp(-k0 * a.dt_over_tau);
+            double sn, cs;
+            sincos(k0 * a.dt_omega, &sn, &cs);
+            pw = T2{(Rl)(mg * cs), (Rl)(mg * sn)};
+        }
+        const T2 oma = T2{(Rl)(1.0 - a.aN_re), (Rl)(-a.aN_im)};
+        const Rl fRM = (Rl)a.fRM, omf = (Rl)a.one_minus_fR;
+        for (int i = 0; i < L; i++) {
+            const int t = t0 + i;
+            const T2 e = E[pad16(t)];
+            const Rl I = e.x * e.x + e.y * e.y;
+            const Rl W1 = Wb[pad32(t)];
+            const Rl g1 = (t == 0) ? (Rl)0 : AV / (U + Pc * I) * I;
+            if (t > 0) ro = heun_step<Rl>(ro, W0, g0, W1, g1, tstep, ND, invND, invTAU, &d);
+            W0 = W1;
+            g0 = g1;
+            // loss[t] (ionization.cpp:43): W at (E_t, rho_t), the reference's log-threshold test
+            T2 loss = T2{0, 0};
+            if (t > 0 && t < N - 1 && I > (Rl)GS_ION_MIN_LN) {
+                const Rl W01 = (ro > ND) ? (Rl)0 : W1;
+                const Rl sl = -(Rl)0.5 * W01 * (U + Pc * I) / I;
+                loss = T2{sl * e.x, sl * e.y};
+            }
+            Rl Q = I;   // Kerr without Raman: |E|^2 E
+            if (rscan) {
+                z = cmul(ra, z);
+                z.x += I;
+                const T2 v = cadd(cmul(oma, z), cmul(pw, zN));
+                Q = omf * I + fRM * v.y;
+                pw = cmul(pw, ra);
+            }
+            a.u1[base + t] = loss;
+            a.u2[base + t] = T2{ro * e.x, ro * e.y};
+            a.u3[base + t] = T2{Q * e.x, Q * e.y};
+        }
+    }
+}
+
+// shared memory of nl_back_kernel: padded row + twiddles
+template <typename Rl>
+__global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_back_kernel(FftArgs<Rl> f, SpecArgs<Rl> s) {
+    using T2 = C2<Rl>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int N = f.N;
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    T2* buf = reinterpret_cast<T2*>(smem_raw);
+    T2* twh = buf + padded_len(N);
+    T2* twl = twh + N / 64;
+    const size_t base = (size_t)blockIdx.x * N;
+    load_twiddles<Rl>(twh, twl, f.tw, N, tid, nthr);
+    const TwTab<Rl> tw{twh, twl};
+    T2* acc = s.kp;   // the new k doubles as the accumulator of the three spectra
+    double lmax = 0.0;
+    for (int src = 0; src < (s.kerr_on ? 3 : 2); src++) {
+        const T2* in = src == 0 ? s.u1 : (src == 1 ? s.u2 : s.u3);
+        for (int i = tid; i < N; i += nthr) buf[pad16(i)] = in[base + i];
+        __syncthreads();
+        smem_fft<-1, Rl>(buf, N, f.logM, tw, 1, tid, nthr);
+        const bool last = src == (s.kerr_on ? 2 : 1);
+        for (int p = tid; p < N; p += nthr) {
+            const T2 v = buf[pad16(p)];
+            T2 k;
+            if (src == 0) {
+                k = v;
+            } else if (src == 1) {
+                k = cadd(acc[base + p], cmul(v, s.pf[p]));   // FFT(loss) + FFT(rho E) PLASMA_FUNC
+            } else {
+                k = acc[base + p];
+                const Rl K = s.kerr[p];                      // += -j KERR_PROFILE FFT(Q E)
+                k.x += K * v.y;
+                k.y += -K * v.x;
+            }
+            if (!last) {
+                acc[base + p] = k;
+                continue;
+            }
+            // RK4: (k1 + 2 k2 + 2 k3 + k4) / 6 accumulated in that order (propagator.cu:412)
+            T2 nb;
+            if (s.stage == 0) {
+                nb = k;
+            } else if (s.stage < 3) {
+                const T2 o = s.nb[base + p];
+                nb = T2{o.x + (Rl)2 * k.x, o.y + (Rl)2 * k.y};
+            } else {
+                const T2 o = s.nb[base + p];
+                nb = T2{(o.x + k.x) / (Rl)6, (o.y + k.y) / (Rl)6};
+                lmax = fmax(lmax, (double)nb.x * (double)nb.x + (double)nb.y * (double)nb.y);
+            }
+            s.nb[base + p] = nb;
+            if (s.stage < 3) acc[base + p] = k;
+        }
+        __syncthreads();
+    }
+    if (s.stage == 3) {
+        for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+        if ((tid & 31) == 0) atomic_max_nonneg(s.max_out, lmax);
+    }
+}
+
+template <typename Rl> static int fused_threads(int N) {
+    const int maxt = sizeof(Rl) == 8 ? 512 : 1024;
+    int t = N / 16;
+    if (t < 32) t = 32;
+    if (t > maxt) t = maxt;
+    return t;
+}
+
+template <typename Rl> bool nl_fused_supported(int N) {
+    const int nthr = fused_threads<Rl>(N);
+    return N % nthr == 0 && FrontSmem<Rl>::bytes(N, nthr) <= 227 * 1024;
+}
+
+template <typename Rl> cudaError_t nl_fused_setup(int N) {
+    const int nthr = fused_threads<Rl>(N);
+    cudaError_t e = cudaFuncSetAttribute(nl_front_kernel<Rl>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)FrontSmem<Rl>::bytes(N, nthr));
+    if (e != cudaSuccess) return e;
+    const int bb = (int)(((size_t)padded_len(N) + N / 64 + 64) * sizeof(typename Vec2<Rl>::T));
+    return cudaFuncSetAttribute(nl_back_kernel<Rl>, cudaFuncAttributeMaxDynamicSharedMemorySize, bb);
+}
+
+template <typename Rl>
+cudaError_t launch_nl_front(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2<Rl>::T* A, int rows, cudaStream_t st,
+                            long long* nl) {
+    const int nthr = fused_threads<Rl>(f.N);
+    nl_front_kernel<Rl><<<rows, nthr, FrontSmem<Rl>::bytes(f.N, nthr), st>>>(f, a, A);
+    (*nl)++;
+    return cudaGetLastError();
+}
+
+template <typename Rl>
+cudaError_t launch_nl_back(FftArgs<Rl> f, SpecArgs<Rl> s, int rows, cudaStream_t st, long long* nl) {
+    const int nthr = fused_threads<Rl>(f.N);
+    const size_t bb = ((size_t)padded_len(f.N) + f.N / 64 + 64) * sizeof(typename Vec2<Rl>::T);
+    nl_back_kernel<Rl><<<rows, nthr, bb, st>>>(f, s);
+    (*nl)++;
+    return cudaGetLastError();
+}
+
+#define GS_FUSED_INST(Rl)                                                                                         \
+    template bool nl_fused_supported<Rl>(int);                                                                    \
+    template cudaError_t nl_fused_setup<Rl>(int);                                                                 \
+    template cudaError_t launch_nl_front<Rl>(FftArgs<Rl>, PlasmaArgs<Rl>, const typename Vec2<Rl>::T*, int,        \
+                                             cudaStream_t, long long*);                                           \
+    template cudaError_t launch_nl_back<Rl>(FftArgs<Rl>, SpecArgs<Rl>, int, cudaStream_t, long long*);
+GS_FUSED_INST(double)
+GS_FUSED_INST(float)
+
+}  // namespace gs
