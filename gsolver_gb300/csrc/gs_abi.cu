@@ -592,6 +592,7 @@ static int dump_impl(gs_handle* h, const double* qdht_x, double r_max, double* m
     if (plasma_max) {
         CK(h, cudaMemsetAsync(h->err_dev, 0, 4, h->st));
         PlasmaArgs<Rl> pa = plasma_args<Rl>(h, true, false);
+        pa.density_only = 1;
         CK(h, launch_plasma<Rl>(pa, nr, h->st, &h->launches));
         CK(h, launch_row_max_re<Rl>((const T2*)h->U + (size_t)nr * nt, nr, nt, d_pmax, h->st, &h->launches));
     }

@@ -273,6 +273,8 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
     if (c < P) run_chunk(s_start[c], true, nullptr);
     __syncthreads();
 
+    if (a.density_only) return;
+
     // phase C: loss[t] (uses W_t, I_t, rho_t at step t+1), rho*E, intensity terms
     for (int t = tid; t < N; t += nthr) {
         T2 e = E[t];
