@@ -35,6 +35,7 @@ ABI_FUNCTIONS = (
     "gs_setup_from_config", "gs_setup_last_error", "gs_setup_grid", "gs_setup_params",
     "gs_setup_tables", "gs_setup_field", "gs_setup_znet", "gs_setup_destroy",
     "gs_run_config", "gs_run_last_error", "gs_dump_reductions", "gs_get_time_field",
+    "gs_plasma_max_noalloc", "gs_noalloc_max_samples", "gs_noalloc_last_error",
 )
 
 

@@ -28,6 +28,8 @@
 #ifndef GS_ABI_H
 #define GS_ABI_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -149,6 +151,29 @@ int gs_dump_reductions(gs_handle* h, const double* qdht_x, double r_max, double*
 
 /* The time-domain field BW-FFT(FIELD)/N_T, [n_r][n_t] complex: dump_type_full_class (77-97). */
 int gs_get_time_field(gs_handle* h, double* e_r_t);
+
+/* Carrier-density maxima without any device allocation.  No counterpart in the reference:
+ * it is an addition for host code that cannot allocate device memory where it needs this
+ * result (for example an application whose own allocator has reserved the GPU's memory and
+ * refuses further cudaMalloc calls from the libraries it links).  It runs the FP64 plasma
+ * recurrence of calculate_plasmadensity_losses_small on caller-owned device buffers:
+ *   e_r_t_dev[rows][n_t]  complex time-domain field (interleaved doubles)
+ *   rate_ln_dev[8192]     IONIZATION_RATE_LN
+ *   plasma_max_dev[rows]  output: max over t of the carrier density per row
+ * with the scalars of *params (n_t and the plasma constants), on `stream` (a cudaStream_t,
+ * NULL for the default stream); it synchronises that stream before returning.  Its scratch
+ * is one fixed 16 MiB array inside the library, held on every GPU that loads the library
+ * until the process exits; rows * n_t may not exceed gs_noalloc_max_samples() (524,280) —
+ * larger requests are refused with GS_ERR_ARG.  The first call on a device does a one-time
+ * set-up (it looks up the array's device address with that device current); make that first
+ * call before any stream capture begins.  All calls share the array, so calls that overlap on
+ * the GPU (other streams, other host threads) race. */
+int gs_plasma_max_noalloc(const gs_params* params, const double* rate_ln_dev, const double* e_r_t_dev, int rows,
+                          double* plasma_max_dev, void* stream);
+/* Largest rows * n_t accepted by gs_plasma_max_noalloc. */
+size_t gs_noalloc_max_samples(void);
+/* Message of the last failed gs_plasma_max_noalloc call. */
+const char* gs_noalloc_last_error(void);
 
 /* Release all device state. */
 int gs_destroy(gs_handle* h);
