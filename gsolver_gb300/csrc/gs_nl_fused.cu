@@ -52,24 +52,47 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
     Rl* rA = reinterpret_cast<Rl*>(scB + 32);
     Rl* rB = rA + 32;
     int* flag = reinterpret_cast<int*>(rB + 32);
+    T2* cend_aL = reinterpret_cast<T2*>(reinterpret_cast<unsigned char*>(flag) + 16);   // a^L (flag area is 64 B)
     const size_t base = (size_t)blockIdx.x * N;
 
     // ---- stage input and inverse FFT (propagator.cu:386-396, 640-641)
     load_twiddles<Rl>(twh, twl, f.tw, N, tid, nthr);
-    double lmax = 0.0;
-    for (int i = tid; i < N; i += nthr) {
-        T2 v = A[base + i];
-        if (f.track_max) lmax = fmax(lmax, (double)v.x * (double)v.x + (double)v.y * (double)v.y);
-        if (f.cdz != 0) {
-            const T2 k = f.kp[base + i];
-            v.x = v.x + (Rl)f.cdz * k.x;
-            v.y = v.y + (Rl)f.cdz * k.y;
+    // N / nthr = 16 elements per thread (2 when N < 512): loads issued together
+    Rl lmax = 0;
+    const Rl cdz = (Rl)f.cdz;
+    const int per = N / nthr;
+    if (per == 16) {
+        T2 v[16];
+#pragma unroll
+        for (int u = 0; u < 16; u++) v[u] = A[base + tid + u * nthr];
+        if (f.track_max) {
+#pragma unroll
+            for (int u = 0; u < 16; u++) lmax = fmax(lmax, v[u].x * v[u].x + v[u].y * v[u].y);
         }
-        E[pad16(i)] = v;
+        if (f.cdz != 0) {
+            T2 k[16];
+#pragma unroll
+            for (int u = 0; u < 16; u++) k[u] = f.kp[base + tid + u * nthr];
+#pragma unroll
+            for (int u = 0; u < 16; u++) { v[u].x = v[u].x + cdz * k[u].x; v[u].y = v[u].y + cdz * k[u].y; }
+        }
+#pragma unroll
+        for (int u = 0; u < 16; u++) E[pad16(tid + u * nthr)] = v[u];
+    } else {
+        for (int i = tid; i < N; i += nthr) {
+            T2 v = A[base + i];
+            if (f.track_max) lmax = fmax(lmax, v.x * v.x + v.y * v.y);
+            if (f.cdz != 0) {
+                const T2 k = f.kp[base + i];
+                v.x = v.x + cdz * k.x;
+                v.y = v.y + cdz * k.y;
+            }
+            E[pad16(i)] = v;
+        }
     }
     if (f.track_max) {
         for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-        if ((tid & 31) == 0) atomic_max_nonneg(f.max_out, lmax);
+        if ((tid & 31) == 0) atomic_max_nonneg(f.max_out, (double)lmax);
     }
     __syncthreads();
     const TwTab<Rl> tw{twh, twl};
@@ -159,6 +182,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
             zl.x += e.x * e.x + e.y * e.y;
             aL = cmul(aL, ra);
         }
+        if (c == 0) cend_aL[0] = aL;                   // a^L, common to all chunks
         T2 Am = aL, Bm = zl;
         block_affine_scan<T2>(Am, Bm, T2{1, 0}, T2{0, 0}, scA, scB);
         cend[c] = Bm;                                   // z at the end of chunk c
@@ -174,11 +198,13 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
         T2 z = zs;
         T2 pw = T2{0, 0};
         if (rscan) {
-            const double k0 = (double)(t0 + 1);
-            const double mg = exp(-k0 * a.dt_over_tau);
-            double sn, cs;
-            sincos(k0 * a.dt_omega, &sn, &cs);
-            pw = T2{(Rl)(mg * cs), (Rl)(mg * sn)};
+            // a^{t0+1} = a (a^L)^c by binary powering (no transcendental per thread)
+            T2 b = cend_aL[0], pr = T2{1, 0};
+            for (int e = c; e > 0; e >>= 1) {
+                if (e & 1) pr = cmul(pr, b);
+                b = cmul(b, b);
+            }
+            pw = cmul(pr, ra);
         }
         const T2 oma = T2{(Rl)(1.0 - a.aN_re), (Rl)(-a.aN_im)};
         const Rl fRM = (Rl)a.fRM, omf = (Rl)a.one_minus_fR;
@@ -227,10 +253,18 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_back_kernel(F
     load_twiddles<Rl>(twh, twl, f.tw, N, tid, nthr);
     const TwTab<Rl> tw{twh, twl};
     T2* acc = s.kp;   // the new k doubles as the accumulator of the three spectra
-    double lmax = 0.0;
+    Rl lmax = 0;
     for (int src = 0; src < (s.kerr_on ? 3 : 2); src++) {
         const T2* in = src == 0 ? s.u1 : (src == 1 ? s.u2 : s.u3);
-        for (int i = tid; i < N; i += nthr) buf[pad16(i)] = in[base + i];
+        if (N / nthr == 16) {
+            T2 v[16];
+#pragma unroll
+            for (int u = 0; u < 16; u++) v[u] = in[base + tid + u * nthr];
+#pragma unroll
+            for (int u = 0; u < 16; u++) buf[pad16(tid + u * nthr)] = v[u];
+        } else {
+            for (int i = tid; i < N; i += nthr) buf[pad16(i)] = in[base + i];
+        }
         __syncthreads();
         smem_fft<-1, Rl>(buf, N, f.logM, tw, 1, tid, nthr);
         const bool last = src == (s.kerr_on ? 2 : 1);
@@ -261,7 +295,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_back_kernel(F
             } else {
                 const T2 o = s.nb[base + p];
                 nb = T2{(o.x + k.x) / (Rl)6, (o.y + k.y) / (Rl)6};
-                lmax = fmax(lmax, (double)nb.x * (double)nb.x + (double)nb.y * (double)nb.y);
+                lmax = fmax(lmax, nb.x * nb.x + nb.y * nb.y);
             }
             s.nb[base + p] = nb;
             if (s.stage < 3) acc[base + p] = k;
@@ -270,7 +304,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_back_kernel(F
     }
     if (s.stage == 3) {
         for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-        if ((tid & 31) == 0) atomic_max_nonneg(s.max_out, lmax);
+        if ((tid & 31) == 0) atomic_max_nonneg(s.max_out, (double)lmax);
     }
 }
 
