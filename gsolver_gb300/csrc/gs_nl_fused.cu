@@ -102,12 +102,35 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
     const Rl U = (Rl)a.ionization_potential, Pc = (Rl)a.ponderomotive, AV = (Rl)a.avalanche_cs;
     const Rl invND = (Rl)1 / ND, invTAU = (Rl)1 / (Rl)a.recombination_tau;
     // E /= N and the rates W_t (the first sample is treated as E_0 = 0: W_0 = g_0 = 0)
-    for (int t = tid; t < N; t += nthr) {
-        T2 e = E[pad16(t)];
-        e.x = e.x / rn;
-        e.y = e.y / rn;
-        E[pad16(t)] = e;
-        Wb[pad32(t)] = (t > 0) ? photo_rate<Rl>(e.x * e.x + e.y * e.y, a.rate, a.err) : (Rl)0;
+    // in batches of 8 samples per thread so that the table reads (L2: the carve-out leaves
+    // little L1) are in flight together
+    for (int tb = tid; tb < N; tb += 8 * nthr) {
+        int n[8];
+        Rl dl[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const int t = tb + u * nthr;
+            n[u] = -1;
+            dl[u] = 0;
+            if (t < N) {
+                T2 e = E[pad16(t)];
+                e.x = e.x / rn;
+                e.y = e.y / rn;
+                E[pad16(t)] = e;
+                if (t > 0) n[u] = photo_index<Rl>(e.x * e.x + e.y * e.y, &dl[u], a.err);
+            }
+        }
+        Rl w0[8], w1[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            w0[u] = n[u] >= 0 ? __ldg(&a.rate[n[u]]) : (Rl)0;
+            w1[u] = n[u] >= 0 ? __ldg(&a.rate[n[u] + 1]) : (Rl)0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const int t = tb + u * nthr;
+            if (t < N) Wb[pad32(t)] = n[u] >= 0 ? photo_rate_from<Rl>(w0[u], w1[u], dl[u]) : (Rl)0;
+        }
     }
     __syncthreads();
 
@@ -268,37 +291,53 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_back_kernel(F
         __syncthreads();
         smem_fft<-1, Rl>(buf, N, f.logM, tw, 1, tid, nthr);
         const bool last = src == (s.kerr_on ? 2 : 1);
-        for (int p = tid; p < N; p += nthr) {
-            const T2 v = buf[pad16(p)];
-            T2 k;
-            if (src == 0) {
-                k = v;
-            } else if (src == 1) {
-                k = cadd(acc[base + p], cmul(v, s.pf[p]));   // FFT(loss) + FFT(rho E) PLASMA_FUNC
-            } else {
-                k = acc[base + p];
-                const Rl K = s.kerr[p];                      // += -j KERR_PROFILE FFT(Q E)
-                k.x += K * v.y;
-                k.y += -K * v.x;
+        // batches of SB points per thread: every global read of a batch is issued before use
+        constexpr int SB = 4;
+        for (int pb = tid; pb < N; pb += SB * nthr) {
+            T2 v[SB], ac[SB], o[SB], c[SB];
+#pragma unroll
+            for (int u = 0; u < SB; u++) {
+                const int p = pb + u * nthr;
+                const bool in = p < N;
+                v[u] = in ? buf[pad16(p)] : T2{0, 0};
+                ac[u] = (in && src > 0) ? acc[base + p] : T2{0, 0};
+                // the spectral coefficient: PLASMA_FUNC for FFT(rho E), -j KERR_PROFILE for FFT(Q E)
+                if (src == 1) c[u] = in ? s.pf[p] : T2{0, 0};
+                else if (src == 2) c[u] = T2{(Rl)0, in ? -s.kerr[p] : (Rl)0};
+                else c[u] = T2{(Rl)1, (Rl)0};
+                o[u] = (in && last && s.stage > 0) ? s.nb[base + p] : T2{0, 0};
             }
-            if (!last) {
-                acc[base + p] = k;
-                continue;
+#pragma unroll
+            for (int u = 0; u < SB; u++) {
+                const int p = pb + u * nthr;
+                if (p >= N) continue;
+                T2 k;
+                if (src == 0) {
+                    k = v[u];
+                } else if (src == 1) {
+                    k = cadd(ac[u], cmul(v[u], c[u]));        // FFT(loss) + FFT(rho E) PLASMA_FUNC
+                } else {
+                    k = ac[u];                                 // += -j KERR_PROFILE FFT(Q E)
+                    k.x += -c[u].y * v[u].y;
+                    k.y += c[u].y * v[u].x;
+                }
+                if (!last) {
+                    acc[base + p] = k;
+                    continue;
+                }
+                // RK4: (k1 + 2 k2 + 2 k3 + k4) / 6 accumulated in that order (propagator.cu:412)
+                T2 nb;
+                if (s.stage == 0) {
+                    nb = k;
+                } else if (s.stage < 3) {
+                    nb = T2{o[u].x + (Rl)2 * k.x, o[u].y + (Rl)2 * k.y};
+                } else {
+                    nb = T2{(o[u].x + k.x) / (Rl)6, (o[u].y + k.y) / (Rl)6};
+                    lmax = fmax(lmax, nb.x * nb.x + nb.y * nb.y);
+                }
+                s.nb[base + p] = nb;
+                if (s.stage < 3) acc[base + p] = k;
             }
-            // RK4: (k1 + 2 k2 + 2 k3 + k4) / 6 accumulated in that order (propagator.cu:412)
-            T2 nb;
-            if (s.stage == 0) {
-                nb = k;
-            } else if (s.stage < 3) {
-                const T2 o = s.nb[base + p];
-                nb = T2{o.x + (Rl)2 * k.x, o.y + (Rl)2 * k.y};
-            } else {
-                const T2 o = s.nb[base + p];
-                nb = T2{(o.x + k.x) / (Rl)6, (o.y + k.y) / (Rl)6};
-                lmax = fmax(lmax, nb.x * nb.x + nb.y * nb.y);
-            }
-            s.nb[base + p] = nb;
-            if (s.stage < 3) acc[base + p] = k;
         }
         __syncthreads();
     }

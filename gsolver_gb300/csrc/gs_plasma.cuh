@@ -25,6 +25,25 @@ __device__ __forceinline__ Rl photo_rate(Rl I, const Rl* __restrict__ tab, unsig
     return exp(lnW);
 }
 
+// photo_rate split in two so that a batch of table reads can be issued together: returns the
+// table index n (-1 where the rate is 0) and dl = lnI - lnI_n; the rate is then
+// photo_rate_from(tab[n], tab[n + 1], dl), bit-identical to photo_rate.
+template <typename Rl>
+__device__ __forceinline__ int photo_index(Rl I, Rl* dl, unsigned* err) {
+    if (I < (Rl)(1e13 / 1e16)) return -1;
+    Rl lnI = log(I) + (Rl)GS_INT_DENOM_LN;
+    if (isnan(lnI)) { atomicOr(err, ERRBIT_NAN); return -1; }
+    int n = (int)floor((lnI - (Rl)GS_ION_MIN_LN) / (Rl)GS_ION_TOL);
+    if (n > 8192 - 2) { atomicOr(err, ERRBIT_BLAST); return -1; }
+    if (n < 0) return -1;
+    *dl = lnI - ((Rl)GS_ION_MIN_LN + n * (Rl)GS_ION_TOL);
+    return n;
+}
+template <typename Rl>
+__device__ __forceinline__ Rl photo_rate_from(Rl w0, Rl w1, Rl dl) {
+    return exp(w0 + dl * (w1 - w0) / (Rl)GS_ION_TOL);
+}
+
 // One Heun step of the carrier density (ionization.cpp:29-40) from rho with rates (W0, g0)
 // at the previous sample and (W1, g1) at this one (g = AV I / (U + P I)); returns the new
 // density and multiplies *d by d(new)/d(rho).
