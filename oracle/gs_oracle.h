@@ -96,6 +96,22 @@ int gso_propagator(const gso_ctx* c, double* field, double* bb1, double* bb2,
 int gso_row_reductions(const gso_ctx* c, const double* field, double* out_maxI,
                        double* out_flux, double* out_pmax);
 
+/* ---- adjoint (gs_oracle_adj.c): cotangents g = dJ/dRe + i dJ/dIm of a real objective ---- */
+
+/* (dN/dY)^H kbar for calculate_NLresponse at the spectral row Y. */
+int gso_nl_response_vjp(const gso_ctx* c, const double* Y, const double* kbar, double* ybar);
+
+/* Adjoint of calculate_NLstep's RK4 increment at FIELD = field with stage step zstep:
+   abar = (dR/dA)^H rbar over all rows. */
+int gso_nl_step_vjp(const gso_ctx* c, const double* field, double zstep, const double* rbar, double* abar);
+
+/* Adjoint of calculate_Lstep: fbar = cotangent of FIELD (k,omega) after the step, sbar
+   in: of BIGBUFFER2 after, out: before; b1bar out: of BIGBUFFER1 (k,omega). */
+int gso_lstep_vjp(const gso_ctx* c, const double* fbar, double* sbar, double* b1bar, double zstep);
+
+/* Transposed QDHT in place: per column x *= m1; y = C x; y /= m1 (H^T, C symmetric). */
+int gso_qdht_transposed(const gso_ctx* c, double* data);
+
 #ifdef __cplusplus
 }
 #endif

@@ -51,7 +51,7 @@ _lib = None
 
 def build():
     """Compile the oracle library (make, gcc) if it is missing or stale."""
-    src = [os.path.join(HERE, f) for f in ("gs_oracle.c", "gs_oracle.h", "Makefile")]
+    src = [os.path.join(HERE, f) for f in ("gs_oracle.c", "gs_oracle_adj.c", "gs_oracle.h", "Makefile")]
     if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(s) for s in src):
         return LIB
     subprocess.run(["make", "-s", "-C", HERE], check=True)
@@ -72,6 +72,10 @@ def lib():
         L.gso_lstep.argtypes = [P, P, P, P, C.c_double]
         L.gso_propagator.argtypes = [P, P, P, P, P, C.c_double, C.c_double, C.c_double, P, P, P]
         L.gso_row_reductions.argtypes = [P, P, P, P, P]
+        L.gso_nl_response_vjp.argtypes = [P, P, P, P]
+        L.gso_nl_step_vjp.argtypes = [P, P, C.c_double, P, P]
+        L.gso_lstep_vjp.argtypes = [P, P, P, P, C.c_double]
+        L.gso_qdht_transposed.argtypes = [P, P]
         _lib = L
     return _lib
 
@@ -213,3 +217,62 @@ class Oracle:
             calls += 1
             cz += zstep
         return out, {"field": f, "bb2": bb2, "z": cz, "zstep": zstep, "step_n": step_n, "n_z": n_z}
+
+    # -- adjoint (gs_oracle_adj.c) ------------------------------------------
+    def nl_response_vjp(self, y_row, kbar_row):
+        y = np.ascontiguousarray(y_row, dtype=np.complex128)
+        kb = np.ascontiguousarray(kbar_row, dtype=np.complex128)
+        out = np.empty_like(y)
+        _check(self.L.gso_nl_response_vjp(self.cp, _p(y), _p(kb), _p(out)))
+        return out
+
+    def nl_step_vjp(self, field, dz, rbar):
+        f = np.ascontiguousarray(field, dtype=np.complex128)
+        rb = np.ascontiguousarray(rbar, dtype=np.complex128)
+        out = np.empty_like(f)
+        _check(self.L.gso_nl_step_vjp(self.cp, _p(f), float(dz), _p(rb), _p(out)))
+        return out
+
+    def lstep_vjp(self, fbar_k, sbar, dz):
+        """Returns (cotangent of BIGBUFFER2 before the step, of BIGBUFFER1 in (k,omega))."""
+        fb = np.ascontiguousarray(fbar_k, dtype=np.complex128)
+        sb = np.array(sbar, dtype=np.complex128, order="C", copy=True)
+        b1 = np.empty_like(sb)
+        _check(self.L.gso_lstep_vjp(self.cp, _p(fb), _p(sb), _p(b1), float(dz)))
+        return sb, b1
+
+    def qdht_t(self, data):
+        d = np.array(data, dtype=np.complex128, order="C", copy=True)
+        _check(self.L.gso_qdht_transposed(self.cp, _p(d)))
+        return d
+
+    def forward_fixed(self, field, dz_rk, dz_lin):
+        """propagator() calls with the step sizes given (RK4 stages use dz_rk[n], the linear
+        step dz_lin[n]; the controller is bypassed).  Returns (FIELD, BIGBUFFER2) after."""
+        f = np.array(field, dtype=np.complex128, copy=True)
+        s = self.qdht(f)
+        for a, b in zip(dz_rk, dz_lin):
+            bb1, _, _ = self.nl_step(f, a)
+            fk, s = self.lstep(self.qdht(bb1), s, b)
+            f = self.qdht(fk)
+        return f, s
+
+    def gradient(self, field, dz_rk, dz_lin, weights):
+        """J = sum w |FIELD_final|^2 after forward_fixed and dJ/dFIELD_0 (g = dJ/dRe + i dJ/dIm)
+        by the adjoint, storing every step's FIELD."""
+        f = np.array(field, dtype=np.complex128, copy=True)
+        s = self.qdht(f)
+        hist = []
+        for a, b in zip(dz_rk, dz_lin):
+            hist.append(f)
+            bb1, _, _ = self.nl_step(f, a)
+            fk, s = self.lstep(self.qdht(bb1), s, b)
+            f = self.qdht(fk)
+        J = float(np.sum(weights * (f.real ** 2 + f.imag ** 2)))
+        ab = 2 * weights * f
+        sb = np.zeros_like(f)
+        for n in range(len(hist) - 1, -1, -1):
+            sb, b1 = self.lstep_vjp(self.qdht_t(ab), sb, dz_lin[n])
+            ab = self.nl_step_vjp(hist[n], dz_rk[n], self.qdht_t(b1))
+        ab = ab + self.qdht_t(sb)
+        return J, ab
