@@ -13,6 +13,8 @@ Synthetic: the pulse is generated (seeded 1e-4 complex Gaussian noise), no datas
   fp64    the plain FP64 GPU path on the same workload, and the mixed path's relative L2
           error against it after the same fixed-dz steps from the same start
   roofline  the mixed QDHT kernels (tcgen05), algorithmic 8 N_r flop per field-point step
+  adjoint the gradient workload (256 x 4096, 1000 steps): forward vs forward+adjoint time
+          and the gradient's accuracy (see adjoint_leg)
   cpu_baseline  the CPU oracle (a port of the reference algorithm) on a bounded sample
 
 Multi-GPU: replicas only (one independent pulse per rank), value = total / max time.
@@ -50,6 +52,9 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--adjoint-steps", type=int, default=1000)
+    ap.add_argument("--adjoint-check-steps", type=int, default=100)
     return ap.parse_args()
 
 
@@ -221,6 +226,64 @@ def reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def adjoint_leg(args, lrank):
+    """The adjoint workload: fused silica 256 x 4096, 2 mm in 1000 fixed 2 um steps, seeded
+    degree-6 spectral phase on the input, J = energy in the 500-600 nm band (average_spectrum
+    radial weights).  Times gs_forward_fixed and gs_gradient (forward + sqrt(N)-checkpointed
+    adjoint) on the mixed path, both through the C ABI with host fields, and checks the
+    gradient on the first `adjoint_check_steps` steps against the FP64 adjoint and fourth-order
+    central differences of the FP64 forward along one seeded direction."""
+    import gsolver_gb300 as gs
+    from gsolver_gb300 import configs
+    d = tempfile.mkdtemp(prefix="gs_bench_adj_")
+    S = gs.Setup(configs.fused_silica_c4(d), noise_seed=1234, noise_sigma=1e-4).as_dict()
+    A0 = S["field"] * np.exp(1j * configs.spectral_phase(S["omega"], S["omega0"], 50e-15, seed=4))[None, :]
+    w = configs.band_weights(S["omega"], S["qdht_x"], S["r_max"], 500e-9, 600e-9)
+    n = args.adjoint_steps
+    rk, lin = configs.clamp_schedule(S["znet"], S["init_zstep"], n)
+    Pm = gs.Propagator(S, precision=gs.PREC_MIXED, device=lrank)
+
+    def timed(f, reps=2):
+        f()   # warm-up: allocations, transposed-QDHT set-up
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            r = f()
+        return (time.perf_counter() - t0) / reps * 1e3, r
+
+    tf, (J, _) = timed(lambda: Pm.forward_fixed(A0, rk, lin, w))
+    tg, (Jg, gm) = timed(lambda: Pm.gradient(A0, rk, lin, w))
+    out = {"workload": "fused_silica_256x4096_adjoint", "n_r": 256, "n_t": 4096, "steps": n, "dz_m": 2e-6,
+           "objective": "band energy 500-600 nm, average_spectrum radial weights",
+           "checkpoint_stride": int(np.ceil(np.sqrt(n))), "precision": "mixed",
+           "forward_ms": tf, "gradient_ms": tg, "cost_ratio": tg / tf,
+           "note": "gradient_ms = forward + adjoint (one gs_gradient call); cost_ratio = gradient / forward"}
+    m = args.adjoint_check_steps
+    if m > 0:
+        P64 = gs.Propagator(S, precision=gs.PREC_FP64, device=lrank)
+        J64, g64 = P64.gradient(A0, rk[:m], lin[:m], w)
+        _, gmm = Pm.gradient(A0, rk[:m], lin[:m], w)
+        h = 1e-5
+        Jf = lambda A: P64.forward_fixed(A, rk[:m], lin[:m], w)[0]
+        chk = {"steps": m, "grad_rel_l2_mixed_vs_fp64": float(np.linalg.norm(gmm - g64) / np.linalg.norm(g64)),
+               "fd": "fourth-order central differences of the FP64 forward, h = 1e-5, along the FP64 gradient "
+                     "(well conditioned) and along one seeded random direction"}
+        rnd = np.random.default_rng(11).standard_normal(A0.shape) + 1j * np.random.default_rng(12).standard_normal(A0.shape)
+        for name, v in (("gradient_dir", g64), ("random_dir", rnd)):
+            v = v * (np.linalg.norm(A0) / np.linalg.norm(v))
+            fd = (-Jf(A0 + 2 * h * v) + 8 * Jf(A0 + h * v) - 8 * Jf(A0 - h * v) + Jf(A0 - 2 * h * v)) / (12 * h)
+            d64 = float(np.sum((np.conj(g64) * v).real))
+            dm = float(np.sum((np.conj(gmm) * v).real))
+            # conditioning |g||v| / |<g, v>|: a gradient error e (relative L2) moves the
+            # directional derivative by up to e times this
+            cond = float(np.linalg.norm(g64) * np.linalg.norm(v) / abs(d64))
+            chk[name] = {"fd_rel_err_fp64": abs(d64 - fd) / abs(fd), "fd_rel_err_mixed": abs(dm - fd) / abs(fd),
+                         "conditioning": cond}
+        out["check"] = chk
+        P64.close()
+    Pm.close()
+    return out
+
+
 def main():
     args = parse()
     rank, world, lrank = dist_info()
@@ -337,6 +400,9 @@ def main():
                         "mixed_speedup": value / world / v64,
                         "mixed_rel_l2_field_err": err, "err_steps": nerr, "err_dz_m": dz}
         P64.close()
+
+    if prec == gs.PREC_MIXED and not args.no_adjoint and args.workload == "c2":
+        line["adjoint"] = adjoint_leg(args, lrank)
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, desc, cores = cpu_sample(cpu_prepare(cfg))

@@ -36,6 +36,7 @@ ABI_FUNCTIONS = (
     "gs_setup_tables", "gs_setup_field", "gs_setup_znet", "gs_setup_destroy",
     "gs_run_config", "gs_run_last_error", "gs_dump_reductions", "gs_get_time_field",
     "gs_plasma_max_noalloc", "gs_noalloc_max_samples", "gs_noalloc_last_error",
+    "gs_forward_fixed", "gs_gradient", "gs_adjoint_step",
 )
 
 
@@ -109,6 +110,9 @@ def load_library(path: str | None = None):
     L.gs_run_config.argtypes = [C.c_char_p, C.c_char_p, I, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p), I, I,
                                 C.c_ulonglong, D, C.c_longlong, C.POINTER(RunStats)]
     L.gs_run_last_error.restype = C.c_char_p
+    L.gs_forward_fixed.argtypes = [V, V, I, V, V, V, PD, V]
+    L.gs_gradient.argtypes = [V, V, I, V, V, V, I, PD, V]
+    L.gs_adjoint_step.argtypes = [V, D, D, V, V]
     _lib = L
     return L
 
@@ -247,6 +251,44 @@ class Propagator:
         ms, n = C.c_double(), C.c_int()
         self._check(self.L.gs_qdht_timing(self.h, int(enable), C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    # -- gradients (gs_forward_fixed / gs_gradient / gs_adjoint_step) ---------------
+    def _schedule(self, dz_rk, dz_lin):
+        a = np.ascontiguousarray(dz_rk, dtype=np.float64)
+        b = np.ascontiguousarray(dz_lin, dtype=np.float64)
+        if a.shape != b.shape or a.ndim != 1:
+            raise ValueError("dz_rk and dz_lin must be 1-D of equal length")
+        return a, b
+
+    def forward_fixed(self, field, dz_rk, dz_lin, weights):
+        """propagator() calls with the given step sizes; returns (J, FIELD after) with
+        J = sum(weights * |FIELD after|^2)."""
+        f = np.ascontiguousarray(field, dtype=np.complex128)
+        a, b = self._schedule(dz_rk, dz_lin)
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        out = np.empty_like(f)
+        J = C.c_double()
+        self._check(self.L.gs_forward_fixed(self.h, _ptr(f), len(a), _ptr(a), _ptr(b), _ptr(w), C.byref(J), _ptr(out)))
+        return J.value, out
+
+    def gradient(self, field, dz_rk, dz_lin, weights, checkpoint_stride=0):
+        """(J, dJ/dRe(FIELD_0) + i dJ/dIm(FIELD_0)) by the adjoint."""
+        f = np.ascontiguousarray(field, dtype=np.complex128)
+        a, b = self._schedule(dz_rk, dz_lin)
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        g = np.empty_like(f)
+        J = C.c_double()
+        self._check(self.L.gs_gradient(self.h, _ptr(f), len(a), _ptr(a), _ptr(b), _ptr(w), int(checkpoint_stride),
+                                       C.byref(J), _ptr(g)))
+        return J.value, g
+
+    def adjoint_step(self, dz_rk, dz_lin, field_bar, spec_bar):
+        """Run one step forward from the current state and map the cotangents of (FIELD,
+        BIGBUFFER2) after it to those before it."""
+        fb = np.array(field_bar, dtype=np.complex128, order="C", copy=True)
+        sb = np.array(spec_bar, dtype=np.complex128, order="C", copy=True)
+        self._check(self.L.gs_adjoint_step(self.h, float(dz_rk), float(dz_lin), _ptr(fb), _ptr(sb)))
+        return fb, sb
 
     def run(self, znet, dz0, steps=None, on_dump=None):
         """The z-loop of solver_main.cpp:202-225 over ZNET; on_dump(n_z, self) at each

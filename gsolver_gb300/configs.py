@@ -9,6 +9,10 @@ covers the whole spectral window.
 Workloads (synthetic: no dataset, the pulse is generated):
   fused_silica_c1   N_R=256,  N_T=2048,  R=600 um, 400 fs window, 1 mm in 500 fixed steps
   fused_silica_c2   N_R=1024, N_T=16384, R=1.2 mm, 1.6 ps window, 3 mm, adaptive (tol 1e-6)
+  fused_silica_c4   N_R=256,  N_T=4096,  R=600 um, 800 fs window, 2 mm in 1000 fixed steps;
+                    the adjoint workload: a seeded degree-6 spectral phase on the input
+                    (spectral_phase) and the output energy in the 500-600 nm band
+                    (band_weights) as the objective
   argon_c5          N_R=512, N_T=32768, 3.9 um 80 fs w0 = 1 mm 4 P_cr pulse in 1 atm argon,
                     2 ps window, R = 4 mm (R unstated by the workload; 4 w0 chosen), z = 20 cm,
                     solid-path Keldysh rate with Ip = 15.76 eV (the gas PPT build is not on
@@ -103,6 +107,63 @@ def fused_silica_c2(dirpath):
     with open(p, "w") as f:
         f.write(_fmt(d))
     return p
+
+
+def fused_silica_c4(dirpath):
+    """256 x 4096, the C1 pulse (800 nm, 50 fs, w0 = 100 um, 3 P_cr) over 2 mm in 1000 fixed
+    2 um steps (the C1 step size; MAX_TOLERANCE large so the ZNET clamp sets dz).  The window
+    (800 fs) and R (600 um) are not stated by the workload: C1's time step and radius."""
+    tabulate_medium(os.path.join(dirpath, "fused_silica.rawdisp"))
+    d = {"LAMBDA_V": "8e-7", "N_T": "4096", "T_MIN": "-400e-15", "T_MAX": "400e-15",
+         "DISPERSION_FILE": "fused_silica.rawdisp", "N_R": "256", "R_MAX": "6e-4",
+         "N_Z": "1001", "Z_MIN": "0", "Z_MAX": "2e-3", "ZNET_TYPE": "e", "MAX_TOLERANCE": "1e3",
+         "PULSE_SHAPE": "gg", "DURATION_FWHM": "50e-15", "DIAMETER_FWHM": repr(100e-6 * math.sqrt(2 * math.log(2))),
+         "POWER_CR": "3", "WAVEFRONT_RADIUS": "1e100", "CE_PHASE": "0"}
+    d.update(SILICA_NL)
+    p = os.path.join(dirpath, "fused_silica_c4.txt")
+    with open(p, "w") as f:
+        f.write(_fmt(d))
+    return p
+
+
+def spectral_phase(omega, omega0, duration_fwhm, seed, degree=6):
+    """phi(omega) = sum_{k=2..degree} c_k x^k, x = (omega - omega0)/d_omega, c_k ~ N(0,1) rad
+    (numpy PCG64, the seed given); d_omega = 4 ln2 / duration_fwhm, the intensity FWHM
+    bandwidth of the transform-limited pulse."""
+    c = np.random.default_rng(seed).standard_normal(degree - 1)
+    x = (np.asarray(omega) - omega0) * duration_fwhm / (4 * math.log(2))
+    return sum(ck * x ** (k + 2) for k, ck in enumerate(c))
+
+
+def band_weights(omega, qdht_x, r_max, lo_m, hi_m):
+    """Objective weights [n_r][n_t]: the average_spectrum radial weights
+    (dump_types.cpp:427-457: x_0 (x_1 - x_0), x_i (x_i - x_{i-1}), times R^2/2) on the
+    spectral band lo_m..hi_m (wavelengths), zero outside it."""
+    om = np.asarray(omega)
+    band = (om >= 2 * math.pi * LIGHT_VELOCITY / hi_m) & (om <= 2 * math.pi * LIGHT_VELOCITY / lo_m)
+    x = np.asarray(qdht_x)
+    wr = np.empty_like(x)
+    wr[0] = x[0] * (x[1] - x[0])
+    wr[1:] = x[1:] * (x[1:] - x[:-1])
+    return np.outer(wr * r_max * r_max / 2, band.astype(float))
+
+
+def clamp_schedule(znet, dz0, steps):
+    """(dz_rk, dz_lin) of `steps` propagator() calls when the controller's proposal always
+    exceeds the distance to the next ZNET point (MAX_TOLERANCE large): the z-loop of
+    solver_main.cpp:202-225 with the clamp of propagator.cu:164; RK4 stages use the previous
+    ZSTEP, the linear step the clamped one."""
+    cz, n_z, zstep = float(znet[0]), 0, float(dz0)
+    rk, lin = [], []
+    for _ in range(steps):
+        if cz >= znet[n_z]:
+            n_z += 1
+        new = float(znet[n_z]) - cz
+        rk.append(zstep)
+        lin.append(new)
+        zstep = new
+        cz += new
+    return np.array(rk), np.array(lin)
 
 
 ARGON_NL = {

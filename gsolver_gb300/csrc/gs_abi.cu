@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "../../include/gs_abi.h"
+#include "gs_handle.h"
 #include "gs_internal.cuh"
 #include "gs_kernels.h"
 #include "gs_qdht_tc.h"
@@ -24,46 +25,22 @@ using namespace gs;
 
 static std::string g_create_error;
 
-struct gs_handle {
-    gs_params p{};
-    int nr = 0, nt = 0, P = 1, M = 0, logM = 0;
-    bool fp64 = true;
-    bool fused = false;        // one-CTA rows: the fused front/back kernels per RK4 stage
-    cudaStream_t st = nullptr;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    size_t esz = 16;           // bytes per complex element
-    void *A = nullptr, *S = nullptr, *NB = nullptr, *KP = nullptr, *E = nullptr, *U = nullptr;
-    void* tw = nullptr;        // twiddles, position-order independent
-    void *pf = nullptr, *rm = nullptr, *kerr = nullptr, *rate = nullptr;
-    double *omega = nullptr, *ho = nullptr, *kt2 = nullptr, *Cm = nullptr, *m1 = nullptr;
-    double2* wavenum = nullptr;
-    double2* staging = nullptr;
-    int* perm_dev = nullptr;
-    unsigned* err_dev = nullptr;
-    unsigned long long* max_dev = nullptr;
-    std::vector<int> perm;
-    gs::QdhtTc* tc = nullptr;  // mixed-precision QDHT (tcgen05)
-    bool tables_ok = false, field_ok = false;
-    long long launches = 0;
-    double qdht_ms = 0;
-    int qdht_n = 0;
-    bool time_qdht = false, ev_pending = false;
-    double* dump_dev = nullptr;   // 3 n_r + 2 n_t doubles of reduction output, r weights
-    std::string err;
-};
 
-static int fail(gs_handle* h, int code, const std::string& msg) {
+using gsi::fail;
+using gsi::cuda_fail;
+using gsi::run_qdht;
+using gsi::permute_in;
+using gsi::permute_out;
+using gsi::lstep;
+using gsi::plasma_args;
+
+int gsi::fail(gs_handle* h, int code, const std::string& msg) {
     if (h) h->err = msg; else g_create_error = msg;
     return code;
 }
-static int cuda_fail(gs_handle* h, cudaError_t e, const char* where) {
+int gsi::cuda_fail(gs_handle* h, cudaError_t e, const char* where) {
     return fail(h, GS_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
-#define CK(h, expr)                                                    \
-    do {                                                               \
-        cudaError_t _e = (expr);                                       \
-        if (_e != cudaSuccess) return cuda_fail((h), _e, #expr);       \
-    } while (0)
 
 static int ilog2(int n) { int l = 0; while ((1 << l) < n) l++; return l; }
 
@@ -116,9 +93,10 @@ void* gs_stream(const gs_handle* h) { return h ? (void*)h->st : nullptr; }
 static void free_all(gs_handle* h) {
     void* ptrs[] = {h->A, h->S, h->NB, h->KP, h->E, h->U, h->tw, h->pf, h->rm, h->kerr, h->rate,
                     h->omega, h->ho, h->kt2, h->Cm, h->m1, h->wavenum, h->staging, h->perm_dev,
-                    h->err_dev, h->max_dev, h->dump_dev};
+                    h->err_dev, h->max_dev, h->dump_dev, h->m1inv, h->adj, h->adj_w};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (h->tc) gs::qdht_tc_destroy(h->tc);
+    if (h->tcT) gs::qdht_tc_destroy(h->tcT);
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->st) cudaStreamDestroy(h->st);
@@ -257,6 +235,21 @@ int gs_upload_tables(gs_handle* h, const gs_tables* t) {
     CK(h, up(h->kt2, t->kt2, nr * 8));
     CK(h, up(h->Cm, t->qdht_c, (size_t)nr * nr * 8));
     CK(h, up(h->m1, t->qdht_m1, nr * 8));
+    {
+        // the transposed QDHT of the adjoint: H^T = diag(1/m1) C diag(m1) (C symmetric)
+        std::vector<double> inv(nr);
+        for (int i = 0; i < nr; i++) inv[i] = 1.0 / t->qdht_m1[i];
+        if (!h->m1inv) CK(h, cudaMalloc((void**)&h->m1inv, nr * 8));
+        CK(h, up(h->m1inv, inv.data(), nr * 8));
+        if (!h->fp64) {
+            h->c_host.assign(t->qdht_c, t->qdht_c + (size_t)nr * nr);
+            h->m1inv_host = inv;
+            if (h->tcT) {   // tables replaced: rebuild on the next adjoint call
+                gs::qdht_tc_destroy(h->tcT);
+                h->tcT = nullptr;
+            }
+        }
+    }
     if (h->tc) {
         std::string m;
         if (gs::qdht_tc_set_matrix(h->tc, t->qdht_c, t->qdht_m1, &m)) return fail(h, GS_ERR_CUDA, "mixed QDHT matrix: " + m);
@@ -280,7 +273,7 @@ static LstepArgs lstep_args(gs_handle* h, double dz) {
 }
 
 // QDHT of device array X -> Y (mode: plain / fused linear step / masked input).
-static int run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz) {
+int gsi::run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz) {
     LstepArgs L = lstep_args(h, dz);
     if (h->fp64) {
         CK(h, launch_qdht64(mode, h->Cm, h->m1, (const double*)X, (double*)Y, h->nr, 2 * h->nt, L, h->st, &h->launches));
@@ -319,7 +312,7 @@ static int collect_qdht_time(gs_handle* h) {
     return GS_OK;
 }
 
-static int permute_in(gs_handle* h, const double* host, void* dst) {
+int gsi::permute_in(gs_handle* h, const double* host, void* dst) {
     const size_t nel = (size_t)h->nr * h->nt;
     CK(h, cudaMemcpyAsync(h->staging, host, nel * 16, cudaMemcpyHostToDevice, h->st));
     cudaError_t e = h->fp64 ? launch_permute<double>(+1, h->staging, dst, h->perm_dev, h->nt, nel, h->st, &h->launches)
@@ -327,7 +320,7 @@ static int permute_in(gs_handle* h, const double* host, void* dst) {
     CK(h, e);
     return GS_OK;
 }
-static int permute_out(gs_handle* h, const void* src, double* host) {
+int gsi::permute_out(gs_handle* h, const void* src, double* host) {
     const size_t nel = (size_t)h->nr * h->nt;
     cudaError_t e = h->fp64 ? launch_permute<double>(-1, src, h->staging, h->perm_dev, h->nt, nel, h->st, &h->launches)
                             : launch_permute<float>(-1, src, h->staging, h->perm_dev, h->nt, nel, h->st, &h->launches);
@@ -371,7 +364,7 @@ int gs_get_nl(gs_handle* h, double* bb1) {
 }
 
 template <typename Rl>
-static PlasmaArgs<Rl> plasma_args(gs_handle* h, bool raman, bool raman_scan) {
+PlasmaArgs<Rl> gsi::plasma_args(gs_handle* h, bool raman, bool raman_scan) {
     using T2 = typename Vec2<Rl>::T;
     const size_t nel = (size_t)h->nr * h->nt;
     T2* U1 = (T2*)h->U;
@@ -399,8 +392,15 @@ static PlasmaArgs<Rl> plasma_args(gs_handle* h, bool raman, bool raman_scan) {
     return pa;
 }
 
+template gs::PlasmaArgs<double> gsi::plasma_args<double>(gs_handle*, bool, bool);
+template gs::PlasmaArgs<float> gsi::plasma_args<float>(gs_handle*, bool, bool);
+
+bool gsi::raman_scan_on(const gs_handle* h) {
+    return h->p.raman_fraction > 0.001 && h->p.n2 != 0 && h->p.raman_tau > 0 && h->p.raman_omega > 0;
+}
+
 template <typename Rl>
-static int nl_step_impl(gs_handle* h, double dz) {
+static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
     using T2 = typename Vec2<Rl>::T;
     const int nr = h->nr, nt = h->nt;
     const size_t nel = (size_t)nr * nt;
@@ -428,13 +428,22 @@ static int nl_step_impl(gs_handle* h, double dz) {
     sa.N = nt; sa.rows = nr; sa.u1 = U1; sa.u2 = U2; sa.u3 = U3;
     sa.pf = (const T2*)h->pf; sa.rm = (const T2*)h->rm; sa.kerr = (const Rl*)h->kerr;
     sa.raman = raman && !raman_scan; sa.kerr_on = kerr_on; sa.nb = NB; sa.kp = KP; sa.max_out = h->max_dev + 1;
-    if (h->fused && (raman_scan || !raman)) {
+    // without Kerr the Raman response is never used: the fused stage applies
+    const bool fused = h->fused && (raman_scan || !raman || !kerr_on);
+    if (tape && !fused) return fail(h, GS_ERR_UNSUPPORTED, "recording the RK4 stages needs rows that fit one CTA");
+    if (fused) {
         for (int s = 0; s < 4; s++) {
             FftArgs<Rl> f1 = fa;
             f1.rows = nr; f1.kp = KP;
             f1.cdz = (s == 0) ? 0.0 : (s < 3 ? dz * 0.5 : dz);
             f1.track_max = (s == 0);
-            CK(h, launch_nl_front<Rl>(f1, pa, A, nr, h->st, &h->launches));
+            PlasmaArgs<Rl> ps = pa;
+            if (tape) {
+                ps.tape_e = (T2*)tape->e[s];
+                ps.tape_rho = (Rl*)tape->rho[s];
+                ps.tape_q = (Rl*)tape->q[s];
+            }
+            CK(h, launch_nl_front<Rl>(f1, ps, A, nr, h->st, &h->launches));
             SpecArgs<Rl> s2 = sa;
             s2.stage = s;
             CK(h, launch_nl_back<Rl>(fa, s2, nr, h->st, &h->launches));
@@ -470,6 +479,10 @@ static int nl_step_impl(gs_handle* h, double dz) {
     return GS_OK;
 }
 
+int gsi::nl_stages(gs_handle* h, double dz, const GsTape* tape) {
+    return h->fp64 ? nl_step_impl<double>(h, dz, tape) : nl_step_impl<float>(h, dz, tape);
+}
+
 static int nl_step(gs_handle* h, double dz, double* max_a2, double* max_nl2) {
     CK(h, cudaMemsetAsync(h->max_dev, 0, 16, h->st));
     CK(h, cudaMemsetAsync(h->err_dev, 0, 4, h->st));
@@ -498,7 +511,7 @@ int gs_nl_step(gs_handle* h, double zstep, double* max_a2, double* max_nl2) {
     return nl_step(h, zstep, max_a2, max_nl2);
 }
 
-static int lstep(gs_handle* h, double dz) {
+int gsi::lstep(gs_handle* h, double dz) {
     if (h->time_qdht) CK(h, cudaEventRecord(h->ev0, h->st));
     int rc = run_qdht(h, QDHT_LSTEP, h->NB, h->S, dz);
     if (rc) return rc;

@@ -1,0 +1,78 @@
+// gs_handle.h -- the device state behind a gs_handle and the orchestration helpers that
+// gs_abi.cu (forward) and gs_adjoint.cu (adjoint) share.  Private to the library.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gs_abi.h"
+#include "gs_kernels.h"
+#include "gs_qdht_tc.h"
+
+// Per-stage record of the four RK4 stages of one step for the adjoint: E/N (complex),
+// rho and Q (real), [n_r][n_t] each, natural time order.
+struct GsTape {
+    void* e[4];
+    void* rho[4];
+    void* q[4];
+};
+
+struct gs_handle {
+    gs_params p{};
+    int nr = 0, nt = 0, P = 1, M = 0, logM = 0;
+    bool fp64 = true;
+    bool fused = false;        // one-CTA rows: the fused front/back kernels per RK4 stage
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    size_t esz = 16;           // bytes per complex element
+    void *A = nullptr, *S = nullptr, *NB = nullptr, *KP = nullptr, *E = nullptr, *U = nullptr;
+    void* tw = nullptr;        // twiddles, position-order independent
+    void *pf = nullptr, *rm = nullptr, *kerr = nullptr, *rate = nullptr;
+    double *omega = nullptr, *ho = nullptr, *kt2 = nullptr, *Cm = nullptr, *m1 = nullptr;
+    double2* wavenum = nullptr;
+    double2* staging = nullptr;
+    int* perm_dev = nullptr;
+    unsigned* err_dev = nullptr;
+    unsigned long long* max_dev = nullptr;
+    std::vector<int> perm;
+    gs::QdhtTc* tc = nullptr;  // mixed-precision QDHT (tcgen05)
+    bool tables_ok = false, field_ok = false;
+    long long launches = 0;
+    double qdht_ms = 0;
+    int qdht_n = 0;
+    bool time_qdht = false, ev_pending = false;
+    double* dump_dev = nullptr;   // 3 n_r + 2 n_t doubles of reduction output, r weights
+    std::string err;
+    // adjoint (gs_adjoint.cu)
+    double* m1inv = nullptr;                   // 1/m1: the transposed QDHT (FP64 path)
+    std::vector<double> c_host, m1inv_host;    // mixed: C and 1/m1, to build the transposed matrix
+    gs::QdhtTc* tcT = nullptr;                 // mixed transposed QDHT (tcgen05)
+    void* adj = nullptr;                       // one allocation: adjoint buffers, checkpoints, tape
+    size_t adj_bytes = 0;
+    double* adj_w = nullptr;                   // objective weights (position order) + partial sums
+    size_t adj_w_bytes = 0;
+};
+
+namespace gsi {
+int fail(gs_handle* h, int code, const std::string& msg);
+int cuda_fail(gs_handle* h, cudaError_t e, const char* where);
+// QDHT of device array X -> Y (gs::QDHT_PLAIN / _LSTEP / _MASKED)
+int run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz);
+// calculate_NLstep's four RK4 stages: NB = RK4 increment of A (no host sync); with a tape
+// the stages are recorded (fused rows only)
+int nl_stages(gs_handle* h, double dz, const GsTape* tape);
+// QDHT(NB) with the linear step into S, then A = QDHT(window S) (no host sync)
+int lstep(gs_handle* h, double dz);
+int permute_in(gs_handle* h, const double* host, void* dst);
+int permute_out(gs_handle* h, const void* src, double* host);
+template <typename Rl> gs::PlasmaArgs<Rl> plasma_args(gs_handle* h, bool raman, bool raman_scan);
+// the Raman recurrence applies (oscillator parameters known, Kerr on)
+bool raman_scan_on(const gs_handle* h);
+}  // namespace gsi
+
+#define CK(h, expr)                                                    \
+    do {                                                               \
+        cudaError_t _e = (expr);                                       \
+        if (_e != cudaSuccess) return gsi::cuda_fail((h), _e, #expr);  \
+    } while (0)

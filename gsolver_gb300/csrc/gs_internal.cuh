@@ -93,6 +93,10 @@ template <int SIGN, typename Rl, typename T2> struct RegDFT<1, SIGN, Rl, T2> {
 // 8-byte bank pairs per half-warp (checked for each stage shape: sub >= 16, sub = 8, 4, 1).
 __host__ __device__ __forceinline__ int pad16(int i) { return i + (i >> 4); }
 __host__ __device__ __forceinline__ int padded_len(int M) { return M + (M >> 4); }
+// real per-sample rows: one pad word per 32 (conflict-free for chunks of 16 consecutive samples)
+__host__ __device__ __forceinline__ int pad32(int i) { return i + (i >> 5); }
+// slots of such a row, rounded to 4 elements so that what follows stays 16-byte aligned
+__host__ __device__ __forceinline__ int wb_count(int N) { return (N + N / 32 + 1 + 3) & ~3; }
 
 // Twiddles w(j) = exp(-2 pi i j / N) from two shared tables: w = hi[j >> 6] * lo[j & 63].
 template <typename Rl> struct TwTab {

@@ -35,7 +35,43 @@ template <typename Rl> struct PlasmaArgs {
     double avalanche_cs, recombination_tau;
     // Raman oscillator h_k = fRM Im(a^k), a = exp(dt (-1/tau + i Omega)); circular wrap a^N
     double a_re, a_im, aN_re, aN_im, fRM, one_minus_fR, dt_over_tau, dt_omega;
+    // optional record of the stage for the adjoint (fused kernel only): E/N, rho, Q per sample
+    typename Vec2<Rl>::T* tape_e;
+    Rl *tape_rho, *tape_q;
 };
+
+// ---- adjoint of one RK4 stage's NL response (gs_nl_vjp.cu), rows that fit one CTA
+template <typename Rl> struct VjpArgs {
+    int N, logM;
+    const typename Vec2<Rl>::T* tw;
+    const typename Vec2<Rl>::T* kb;       // cotangent of the stage's N (spectral), times kb_scale
+    double kb_scale;
+    const typename Vec2<Rl>::T* tape_e;   // the stage's E/N, rho, Q (natural time order)
+    const Rl *tape_rho, *tape_q;
+    const typename Vec2<Rl>::T* pf;       // PLASMA_FUNC (position order)
+    const Rl* kerr;                       // KERR_PROFILE (position order)
+    const Rl* rate;                       // IONIZATION_RATE_LN
+    typename Vec2<Rl>::T* ebar;           // scratch [rows][N]
+    typename Vec2<Rl>::T* ab;             // cotangent of FIELD: = or += (dN/dY)^H kb
+    int ab_add;
+    const typename Vec2<Rl>::T* rbar;     // next stage's cotangent kb_out = cR rbar + cdz ybar
+    typename Vec2<Rl>::T* kb_out;         // may be kb itself, or null
+    double cR, cdz;
+    int kerr_on, raman_scan;
+    double tstep_scaled, neutral_density, ionization_potential, ponderomotive, avalanche_cs, recombination_tau;
+    double a_re, a_im, aN_re, aN_im, fRM, one_minus_fR;
+};
+template <typename Rl> bool nl_vjp_supported(int N);
+template <typename Rl> cudaError_t nl_vjp_setup(int N);
+template <typename Rl> cudaError_t launch_nl_vjp(const VjpArgs<Rl>& v, int rows, cudaStream_t st, long long* nl);
+// J partial sums of w |A|^2 per block and A_bar = 2 w A; then one block sums the partials
+template <typename Rl>
+cudaError_t launch_adj_seed(const typename Vec2<Rl>::T* A, const double* w, typename Vec2<Rl>::T* ab, size_t n,
+                            double* partial, int nblocks, double* out, cudaStream_t st, long long* nl);
+// y += x over n complex elements
+template <typename Rl>
+cudaError_t launch_cadd(typename Vec2<Rl>::T* y, const typename Vec2<Rl>::T* x, size_t n, cudaStream_t st,
+                        long long* nl);
 
 template <typename Rl> struct SpecArgs {
     int N, rows;
@@ -95,5 +131,10 @@ enum { QDHT_PLAIN = 0, QDHT_LSTEP = 1, QDHT_MASKED = 2 };
 cudaError_t launch_qdht64(int mode, const double* C, const double* m1, const double* X, double* Y, int nr,
                           int ncols, const LstepArgs& L, cudaStream_t st, long long* nlaunch);
 cudaError_t qdht_set_sqrt_ho(const double* coeffs20);
+// adjoint of the linear step (gs_qdht64.cu): fb = cotangent of FIELD (k,omega) after the
+// step, sb of BIGBUFFER2 (in: after, out: before), b1b out: of BIGBUFFER1 (k,omega)
+template <typename Rl>
+cudaError_t launch_lstep_adj(const typename Vec2<Rl>::T* fb, typename Vec2<Rl>::T* sb, typename Vec2<Rl>::T* b1b,
+                             int nr, int nt, const LstepArgs& L, cudaStream_t st, long long* nlaunch);
 
 }  // namespace gs

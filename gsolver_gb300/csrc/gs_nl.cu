@@ -513,7 +513,11 @@ cudaError_t launch_fft(int sign, const C2<Rl>* in, C2<Rl>* out, FftArgs<Rl> a, c
 
 template <typename Rl>
 cudaError_t fft_set_smem(int M, int N) {
-    const int smem = (int)fft_smem_bytes<Rl>(M, N);
+    // a per-kernel ceiling shared by every handle of the process: the device maximum, so
+    // that a handle on a smaller grid never lowers it for a larger one
+    (void)M;
+    (void)N;
+    const int smem = 227 * 1024;
     cudaError_t e = cudaFuncSetAttribute(fft_sub_kernel<Rl, -1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
     if (e != cudaSuccess) return e;
     return cudaFuncSetAttribute(fft_sub_kernel<Rl, +1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);

@@ -18,9 +18,6 @@
 
 namespace gs {
 
-__host__ __device__ __forceinline__ int pad32(int i) { return i + (i >> 5); }
-// rate slots: padded row, rounded to 4 elements so that what follows stays 16-byte aligned
-__host__ __device__ __forceinline__ int wb_count(int N) { return (N + N / 32 + 1 + 3) & ~3; }
 
 template <typename Rl> struct FrontSmem {
     static __host__ __device__ size_t bytes(int N, int nthr) {
@@ -258,6 +255,11 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
             a.u1[base + t] = loss;
             a.u2[base + t] = T2{ro * e.x, ro * e.y};
             a.u3[base + t] = T2{Q * e.x, Q * e.y};
+            if (a.tape_e) {   // what the adjoint of this stage reads back
+                a.tape_e[base + t] = e;
+                a.tape_rho[base + t] = ro;
+                a.tape_q[base + t] = Q;
+            }
         }
     }
 }
@@ -361,12 +363,12 @@ template <typename Rl> bool nl_fused_supported(int N) {
 }
 
 template <typename Rl> cudaError_t nl_fused_setup(int N) {
-    const int nthr = fused_threads<Rl>(N);
-    cudaError_t e = cudaFuncSetAttribute(nl_front_kernel<Rl>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)FrontSmem<Rl>::bytes(N, nthr));
+    // the attribute is a per-kernel ceiling shared by every handle of the process: set the
+    // device maximum so that a handle on a smaller grid never lowers it for a larger one
+    (void)N;
+    cudaError_t e = cudaFuncSetAttribute(nl_front_kernel<Rl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if (e != cudaSuccess) return e;
-    const int bb = (int)(((size_t)padded_len(N) + N / 64 + 64) * sizeof(typename Vec2<Rl>::T));
-    return cudaFuncSetAttribute(nl_back_kernel<Rl>, cudaFuncAttributeMaxDynamicSharedMemorySize, bb);
+    return cudaFuncSetAttribute(nl_back_kernel<Rl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
 }
 
 template <typename Rl>

@@ -70,6 +70,58 @@ __device__ __forceinline__ Rl heun_step(Rl ro, Rl W0, Rl g0, Rl W1, Rl g1, Rl ts
     return rn;
 }
 
+// ---- derivatives for the adjoint -------------------------------------------------------
+// Per-sample rates of one Heun step and their intensity derivatives: the photoionization
+// rate W (log-linear table: dW/dI = W slope / I) and the avalanche prefactor
+// g = AV I / (U + P I) (dg/dI = AV U / (U + P I)^2).  Invalid intensities give 0 (the
+// forward reports them).
+template <typename Rl> struct RateD { Rl W, dW, g, dg; };
+
+template <typename Rl>
+__device__ __forceinline__ RateD<Rl> rate_with_derivs(Rl I, const Rl* __restrict__ tab, Rl U, Rl Pc, Rl AV) {
+    RateD<Rl> r{0, 0, 0, 0};
+    const Rl den = U + Pc * I;
+    r.g = AV / den * I;
+    r.dg = AV * U / (den * den);
+    if (!(I >= (Rl)(1e13 / 1e16))) return r;
+    const Rl lnI = log(I) + (Rl)GS_INT_DENOM_LN;
+    const int n = (int)floor((lnI - (Rl)GS_ION_MIN_LN) / (Rl)GS_ION_TOL);
+    if (n < 0 || n > 8192 - 2) return r;
+    const Rl w0 = __ldg(&tab[n]), w1 = __ldg(&tab[n + 1]);
+    r.W = photo_rate_from<Rl>(w0, w1, lnI - ((Rl)GS_ION_MIN_LN + n * (Rl)GS_ION_TOL));
+    r.dW = r.W * ((w1 - w0) / (Rl)GS_ION_TOL) / I;
+    return r;
+}
+
+// Partial derivatives of heun_step (same branches): d = d rho_t / d rho_{t-1},
+// a = d rho_t / d I_{t-1}, b = d rho_t / d I_t; all 0 where the density is clamped at rho_n.
+template <typename Rl>
+__device__ __forceinline__ void heun_partials(Rl ro, const RateD<Rl>& r0, const RateD<Rl>& r1, Rl tstep, Rl ND,
+                                              Rl invND, Rl invTAU, Rl* d, Rl* a, Rl* b) {
+    const bool in1 = !(ro < 0 || ro > ND);
+    const Rl W01 = (ro > ND) ? (Rl)0 : r0.W, dW01 = (ro > ND) ? (Rl)0 : r0.dW;
+    Rl av = in1 ? r0.g * ro * (1 - ro * invND) : (Rl)0;
+    Rl rc = (ro > 0) ? ro * invTAU : (Rl)0;
+    const Rl k1 = tstep * (W01 + av - rc);
+    const Rl k1r = tstep * ((in1 ? r0.g * (1 - 2 * ro * invND) : (Rl)0) - ((ro > 0) ? invTAU : (Rl)0));
+    const Rl k1I = tstep * (dW01 + (in1 ? r0.dg * ro * (1 - ro * invND) : (Rl)0));
+    const Rl r2 = ro + k1;
+    const bool in2 = !(r2 < 0 || r2 > ND);
+    const Rl W11 = (r2 > ND) ? (Rl)0 : r1.W, dW11 = (r2 > ND) ? (Rl)0 : r1.dW;
+    av = in2 ? r1.g * r2 * (1 - r2 * invND) : (Rl)0;
+    rc = (r2 > 0) ? r2 * invTAU : (Rl)0;
+    const Rl k2 = tstep * (W11 + av - rc);
+    const Rl k2r = tstep * ((in2 ? r1.g * (1 - 2 * r2 * invND) : (Rl)0) - ((r2 > 0) ? invTAU : (Rl)0));
+    const Rl k2I = tstep * (dW11 + (in2 ? r1.dg * r2 * (1 - r2 * invND) : (Rl)0));
+    if (ro + (Rl)0.5 * (k1 + k2) > ND) {
+        *d = 0; *a = 0; *b = 0;
+        return;
+    }
+    *d = 1 + (Rl)0.5 * (k1r + k2r * (1 + k1r));
+    *a = (Rl)0.5 * k1I * (1 + k2r);
+    *b = (Rl)0.5 * k2I;
+}
+
 // Block-wide inclusive scan of affine maps x -> A x + B (composition left to right, i.e.
 // thread c ends with map_c o ... o map_0).  T is the real type or a complex struct with
 // the mul/add helpers below; sA/sB hold 32 entries.  All threads must call it.

@@ -150,4 +150,45 @@ cudaError_t qdht_set_sqrt_ho(const double* coeffs20) {
     return cudaMemcpyToSymbol(c_sqrt_ho, coeffs20, sizeof(double) * 20);
 }
 
+// Adjoint of calculate_Lstep per (k, omega): inside the window T = B2 + dz N/(1+s),
+// FIELD = B2' = T P, so T_bar = conj(P) (FIELD_bar + B2'_bar), B2_bar = T_bar and
+// N_bar = dz T_bar / (1+s); outside it FIELD = 0 and B2 is untouched (B2_bar passes, N_bar = 0).
+// P is evaluated in FP64 as the forward epilogue does.
+template <typename Rl>
+__global__ void lstep_adj_kernel(const C2<Rl>* __restrict__ fb, C2<Rl>* __restrict__ sb, C2<Rl>* __restrict__ b1b,
+                                 int nt, size_t total, LstepArgs L) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const int k = (int)(idx / nt), p = (int)(idx % nt);
+    if (!in_window(L, k, p)) {
+        b1b[idx] = C2<Rl>{0, 0};
+        return;
+    }
+    const double2 kk = L.wavenum[p];
+    const double sq = sqrt_ho(-L.kt2[k] / kk.x / kk.x);
+    const double er = L.dz * kk.y, ei = L.dz * (-L.ho[p] - sq * kk.x);
+    double sn, cs;
+    sincos(ei, &sn, &cs);
+    const double m = exp(er);
+    const double pr = m * cs, pi = m * sn;
+    const C2<Rl> f = fb[idx], s = sb[idx];
+    const double gr = (double)f.x + (double)s.x, gi = (double)f.y + (double)s.y;
+    const double tr = pr * gr + pi * gi, ti = pr * gi - pi * gr;
+    sb[idx] = C2<Rl>{(Rl)tr, (Rl)ti};
+    b1b[idx] = C2<Rl>{(Rl)(L.dz * tr / (1 + sq)), (Rl)(L.dz * ti / (1 + sq))};
+}
+
+template <typename Rl>
+cudaError_t launch_lstep_adj(const typename Vec2<Rl>::T* fb, typename Vec2<Rl>::T* sb, typename Vec2<Rl>::T* b1b,
+                             int nr, int nt, const LstepArgs& L, cudaStream_t st, long long* nlaunch) {
+    const size_t total = (size_t)nr * nt;
+    lstep_adj_kernel<Rl><<<(unsigned)((total + 255) / 256), 256, 0, st>>>(fb, sb, b1b, nt, total, L);
+    (*nlaunch)++;
+    return cudaGetLastError();
+}
+template cudaError_t launch_lstep_adj<double>(const double2*, double2*, double2*, int, int, const LstepArgs&,
+                                              cudaStream_t, long long*);
+template cudaError_t launch_lstep_adj<float>(const float2*, float2*, float2*, int, int, const LstepArgs&,
+                                             cudaStream_t, long long*);
+
 }  // namespace gs

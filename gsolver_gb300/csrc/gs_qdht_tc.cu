@@ -382,6 +382,34 @@ __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_consta
     }
 }
 
+// Adjoint of the fused linear step above, elementwise with the same FP32 tables and
+// window: T_bar = conj(P) (FIELD_bar + B2'_bar), B2_bar = T_bar, N_bar = dz T_bar/(1+s);
+// outside the window B2_bar passes unchanged and N_bar = 0.
+__global__ void lstep_adj_kernel(const float2* __restrict__ fb, float2* __restrict__ sb, float2* __restrict__ b1b,
+                                 int nt, size_t total, float dz, const float* __restrict__ kr,
+                                 const float* __restrict__ ki, const float* __restrict__ ho,
+                                 const float* __restrict__ kt2, const int* __restrict__ kmax) {
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const int i = (int)(idx / nt), p = (int)(idx % nt);
+    if (i > kmax[p]) {
+        b1b[idx] = make_float2(0.f, 0.f);
+        return;
+    }
+    const float k1 = kr[p], k2 = ki[p];
+    const float sq = sqrt_ho_f(-kt2[i] / k1 / k1);
+    const float inv = 1.f / (1.f + sq);
+    float sn, cs;
+    sincosf(dz * (-ho[p] - sq * k1), &sn, &cs);
+    const float m = expf(dz * k2);
+    const float pr = m * cs, pi = m * sn;
+    const float2 f = fb[idx], b = sb[idx];
+    const float gr = f.x + b.x, gi = f.y + b.y;
+    const float tr = pr * gr + pi * gi, ti = pr * gi - pi * gr;
+    sb[idx] = make_float2(tr, ti);
+    b1b[idx] = make_float2(dz * tr * inv, dz * ti * inv);
+}
+
 }  // namespace tc
 
 struct QdhtTc {
@@ -540,6 +568,15 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
     a.err = q->err;
     const unsigned grid = (unsigned)((q->nr / tc::BM) * (a.ncols / tc::BN));
     tc::qdht_tc_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, q->st>>>(q->map_hi, q->map_lo, a);
+    (*nlaunch)++;
+    return cudaGetLastError();
+}
+
+cudaError_t qdht_tc_lstep_adj(QdhtTc* q, const float* fb, float* sb, float* b1b, double dz, long long* nlaunch) {
+    if (!q->have_lstep) return cudaErrorInvalidValue;
+    const size_t total = (size_t)q->nr * q->nt;
+    tc::lstep_adj_kernel<<<(unsigned)((total + 255) / 256), 256, 0, q->st>>>(
+        (const float2*)fb, (float2*)sb, (float2*)b1b, q->nt, total, (float)dz, q->kr, q->ki, q->ho, q->kt2, q->kmax);
     (*nlaunch)++;
     return cudaGetLastError();
 }

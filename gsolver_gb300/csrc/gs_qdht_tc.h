@@ -23,6 +23,10 @@ int qdht_tc_check(QdhtTc* q, std::string* msg);
 // Y = QDHT(X) with the given mode (QDHT_PLAIN / QDHT_LSTEP / QDHT_MASKED).
 cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const LstepArgs& L, long long* nlaunch,
                         std::string* msg);
+// Adjoint of the QDHT_LSTEP epilogue's linear step, elementwise over [n_r][n_t] (FP32, the
+// epilogue's tables): fb = cotangent of FIELD (k,omega), sb of BIGBUFFER2 (in: after the
+// step, out: before), b1b out: of BIGBUFFER1 (k,omega).
+cudaError_t qdht_tc_lstep_adj(QdhtTc* q, const float* fb, float* sb, float* b1b, double dz, long long* nlaunch);
 void qdht_tc_destroy(QdhtTc* q);
 
 }  // namespace gs

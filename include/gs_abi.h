@@ -152,6 +152,28 @@ int gs_dump_reductions(gs_handle* h, const double* qdht_x, double r_max, double*
 /* The time-domain field BW-FFT(FIELD)/N_T, [n_r][n_t] complex: dump_type_full_class (77-97). */
 int gs_get_time_field(gs_handle* h, double* e_r_t);
 
+/* ---- Gradients (no counterpart in the reference: it has no adjoint) ----------------------
+ * A run of n_steps propagator() calls with the step sizes given instead of chosen by the
+ * controller: step n uses dz_rk[n] in its RK4 stages and dz_lin[n] in its linear step (the
+ * old and the new ZSTEP of propagator.cu:139-194), so that a controller-driven run can be
+ * replayed and differentiated exactly.  The objective is
+ *   J = sum_{r, omega} weights[r][omega] |FIELD(r, omega)|^2   after the last step
+ * (weights [n_r][n_t] doubles: e.g. the average_spectrum radial weights inside a spectral
+ * band, dump_types.cpp:427-457).  Fields are [n_r][n_t] complex (interleaved doubles) on the
+ * host; on return the handle holds the final state of the forward run. */
+int gs_forward_fixed(gs_handle* h, const double* field_in, int n_steps, const double* dz_rk, const double* dz_lin,
+                     const double* weights, double* objective, double* field_out);
+/* J as above and grad_field = dJ/dRe(FIELD_0) + i dJ/dIm(FIELD_0) by the hand-written adjoint,
+ * with checkpoints every checkpoint_stride steps (0: ceil(sqrt(n_steps))) and the steps of
+ * each segment re-run from its checkpoint.  Needs rows that fit one CTA (n_t <= 8192 mixed,
+ * <= 4096 FP64) and, with Raman on, the oscillator parameters (raman_tau, raman_omega). */
+int gs_gradient(gs_handle* h, const double* field_in, int n_steps, const double* dz_rk, const double* dz_lin,
+                const double* weights, int checkpoint_stride, double* objective, double* grad_field);
+/* One step of the adjoint from the handle's current state (FIELD_n, BIGBUFFER2_n): the step
+ * is run forward (the handle then holds state n+1) and the cotangents of FIELD (r,omega) and
+ * BIGBUFFER2 (k,omega) after it, field_bar and spec_bar, are replaced by those before it. */
+int gs_adjoint_step(gs_handle* h, double dz_rk, double dz_lin, double* field_bar, double* spec_bar);
+
 /* Carrier-density maxima without any device allocation.  No counterpart in the reference:
  * it is an addition for host code that cannot allocate device memory where it needs this
  * result (for example an application whose own allocator has reserved the GPU's memory and
