@@ -15,6 +15,7 @@ Synthetic: the pulse is generated (seeded 1e-4 complex Gaussian noise), no datas
   roofline  the mixed QDHT kernels (tcgen05), algorithmic 8 N_r flop per field-point step
   adjoint the gradient workload (256 x 4096, 1000 steps): forward vs forward+adjoint time
           and the gradient's accuracy (see adjoint_leg)
+  batch   64 pulses with uneven grids, one CUDA graph launch per z-step (see batch_leg)
   cpu_baseline  the CPU oracle (a port of the reference algorithm) on a bounded sample
 
 Multi-GPU: replicas only (one independent pulse per rank), value = total / max time.
@@ -48,11 +49,16 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c2r256"])
+    ap.add_argument("--only", default=None, choices=["adjoint", "batch"],
+                    help="run one leg alone and print its JSON object (profiling captures)")
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--batch-pulses", type=int, default=64)
+    ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--adjoint-steps", type=int, default=1000)
     ap.add_argument("--adjoint-check-steps", type=int, default=100)
     return ap.parse_args()
@@ -72,6 +78,10 @@ def make_config(workload):
         return configs.fused_silica_c2(d), {"workload": "fused_silica_1024x16384", "n_r": 1024, "n_t": 16384,
                                              "r_max_m": 1.2e-3, "window_s": 1.6e-12, "z_max_m": 3e-3,
                                              "max_tolerance": 1e-6}
+    if workload == "c2r256":
+        return configs.fused_silica_c2_rows(d, 256), {"workload": "fused_silica_256x16384 (profiling case)",
+                                                      "n_r": 256, "n_t": 16384, "r_max_m": 3e-4,
+                                                      "window_s": 1.6e-12, "z_max_m": 3e-3, "max_tolerance": 1e-6}
     return configs.fused_silica_c1(d), {"workload": "fused_silica_256x2048", "n_r": 256, "n_t": 2048,
                                          "r_max_m": 6e-4, "window_s": 4e-13, "z_max_m": 1e-3,
                                          "max_tolerance": 1e3}
@@ -226,6 +236,51 @@ def reference_arm(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def batch_leg(args, lrank):
+    """The batched scan: 64 fused-silica pulses with uneven grids (N_r 128-512, N_t
+    1024-8192) and parameters drawn from a seed, mixed precision, fixed 2 um steps; one CUDA
+    graph launch advances every pulse one z-step.  Aggregate field-point z-steps/s over the
+    batch (CUDA events on the batch stream), with and without the graph."""
+    import torch
+    import gsolver_gb300 as gs
+    from gsolver_gb300 import configs
+    d = tempfile.mkdtemp(prefix="gs_bench_batch_")
+    cfgs = configs.c3_batch(d, seed=0, n=args.batch_pulses)
+    t0 = time.perf_counter()
+    S = [gs.Setup(p, noise_seed=100 + i, noise_sigma=1e-4).as_dict() for i, (p, _) in enumerate(cfgs)]
+    t_setup = time.perf_counter() - t0
+    P = [gs.Propagator(s, precision=gs.PREC_MIXED, device=lrank) for s in S]
+    for s, p in zip(S, P):
+        p.set_field(s["field"])
+    B = gs.Batch(P)
+    dz = np.array([float(s["init_zstep"]) for s in S])
+    pts = sum(s["n_r"] * s["n_t"] for s in S)
+    stream = torch.cuda.ExternalStream(B.stream_ptr(), device=lrank)
+    out = {"workload": f"fused_silica_batch{len(P)}", "pulses": len(P), "points_per_zstep": pts,
+           "grids": sorted({(s["n_r"], s["n_t"]) for s in S}), "precision": "mixed", "dz_m": 2e-6,
+           "host_setup_s": t_setup}
+    for graph in (True, False):
+        B.step(dz, 2, graph=graph)   # warm-up (and graph capture)
+        n0 = B.launch_count()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        e0.record(stream)
+        B.step(dz, args.batch_steps, graph=graph)
+        e1.record(stream)
+        e1.synchronize()
+        wall = time.perf_counter() - t1
+        ms = e0.elapsed_time(e1)
+        key = "graph" if graph else "streams"
+        out[key] = {"value": pts * args.batch_steps / (ms / 1e3), "unit": UNIT, "ms_per_zstep": ms / args.batch_steps,
+                    "wall_ms_per_zstep": wall * 1e3 / args.batch_steps, "steps": args.batch_steps,
+                    "kernels_per_zstep": (B.launch_count() - n0) / args.batch_steps}
+    B.close()
+    for p in P:
+        p.close()
+    return out
+
+
 def adjoint_leg(args, lrank):
     """The adjoint workload: fused silica 256 x 4096, 2 mm in 1000 fixed 2 um steps, seeded
     degree-6 spectral phase on the input, J = energy in the 500-600 nm band (average_spectrum
@@ -292,6 +347,12 @@ def main():
         return
     import torch
     import gsolver_gb300 as gs
+    if args.only:
+        torch.cuda.set_device(lrank)
+        leg = adjoint_leg(args, lrank) if args.only == "adjoint" else batch_leg(args, lrank)
+        if rank == 0:
+            print(json.dumps({args.only: leg}), flush=True)
+        return
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
@@ -403,6 +464,8 @@ def main():
 
     if prec == gs.PREC_MIXED and not args.no_adjoint and args.workload == "c2":
         line["adjoint"] = adjoint_leg(args, lrank)
+    if prec == gs.PREC_MIXED and not args.no_batch and args.workload == "c2":
+        line["batch"] = batch_leg(args, lrank)
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, desc, cores = cpu_sample(cpu_prepare(cfg))

@@ -37,6 +37,8 @@ ABI_FUNCTIONS = (
     "gs_run_config", "gs_run_last_error", "gs_dump_reductions", "gs_get_time_field",
     "gs_plasma_max_noalloc", "gs_noalloc_max_samples", "gs_noalloc_last_error",
     "gs_forward_fixed", "gs_gradient", "gs_adjoint_step",
+    "gs_batch_create", "gs_batch_step", "gs_batch_stream", "gs_batch_launch_count", "gs_batch_last_error",
+    "gs_batch_destroy", "gs_autotune",
 )
 
 
@@ -113,6 +115,16 @@ def load_library(path: str | None = None):
     L.gs_forward_fixed.argtypes = [V, V, I, V, V, V, PD, V]
     L.gs_gradient.argtypes = [V, V, I, V, V, V, I, PD, V]
     L.gs_adjoint_step.argtypes = [V, D, D, V, V]
+    L.gs_batch_create.argtypes = [I, C.POINTER(V), C.POINTER(V)]
+    L.gs_batch_step.argtypes = [V, I, V, I]
+    L.gs_batch_stream.argtypes = [V]
+    L.gs_batch_stream.restype = V
+    L.gs_batch_launch_count.argtypes = [V]
+    L.gs_batch_launch_count.restype = C.c_longlong
+    L.gs_batch_last_error.argtypes = [V]
+    L.gs_batch_last_error.restype = C.c_char_p
+    L.gs_batch_destroy.argtypes = [V]
+    L.gs_autotune.argtypes = [V, C.POINTER(C.c_int), PD]
     _lib = L
     return L
 
@@ -252,6 +264,13 @@ class Propagator:
         self._check(self.L.gs_qdht_timing(self.h, int(enable), C.byref(ms), C.byref(n)))
         return ms.value, n.value
 
+    def autotune(self):
+        """Pick the fused NL kernels' launch shape for this grid (gs_autotune); returns
+        (threads per row, ms per RK4 stage)."""
+        t, ms = C.c_int(), C.c_double()
+        self._check(self.L.gs_autotune(self.h, C.byref(t), C.byref(ms)))
+        return t.value, ms.value
+
     # -- gradients (gs_forward_fixed / gs_gradient / gs_adjoint_step) ---------------
     def _schedule(self, dz_rk, dz_lin):
         a = np.ascontiguousarray(dz_rk, dtype=np.float64)
@@ -380,6 +399,46 @@ class Setup:
         L.gs_setup_znet(self.s, zn.ctypes.data_as(C.c_void_p), C.byref(dz0), C.byref(rmax), x.ctypes.data_as(C.c_void_p))
         d.update(znet=zn, init_zstep=dz0.value, r_max=rmax.value, qdht_x=x)
         return d
+
+
+class Batch:
+    """Independent pulses (Propagator objects on one device) advanced together with fixed
+    per-pulse step sizes; one CUDA graph launch per z-step (gs_batch_*)."""
+
+    def __init__(self, pulses):
+        self.L = load_library()
+        self.pulses = list(pulses)   # kept alive: the batch uses their handles
+        arr = (C.c_void_p * len(self.pulses))(*[p.h.value for p in self.pulses])
+        b = C.c_void_p()
+        rc = self.L.gs_batch_create(len(self.pulses), arr, C.byref(b))
+        if rc:
+            raise GsError(rc, self.L.gs_batch_last_error(None).decode())
+        self.b = b
+
+    def step(self, dz, n_steps=1, graph=True):
+        d = np.ascontiguousarray(dz, dtype=np.float64)
+        if d.shape != (len(self.pulses),):
+            raise ValueError("one step size per pulse")
+        rc = self.L.gs_batch_step(self.b, int(n_steps), _ptr(d), int(bool(graph)))
+        if rc:
+            raise GsError(rc, self.L.gs_batch_last_error(self.b).decode())
+
+    def stream_ptr(self):
+        return self.L.gs_batch_stream(self.b)
+
+    def launch_count(self):
+        return self.L.gs_batch_launch_count(self.b)
+
+    def close(self):
+        if getattr(self, "b", None):
+            self.L.gs_batch_destroy(self.b)
+            self.b = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def run_config(config_path: str, out_dir: str = ".", overrides: dict | None = None, precision: int = PREC_FP64,

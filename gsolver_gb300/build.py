@@ -71,7 +71,7 @@ def build(force=False, verbose=False):
     with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
         objs = list(ex.map(run, jobs))
     tmp = LIB + ".tmp"
-    run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcuda"])
+    run([nvcc] + ARCH + ["-shared", "-o", tmp] + objs + ["-lcuda", "-lpthread"])
     os.replace(tmp, LIB)
     return LIB
 

@@ -13,6 +13,10 @@ Workloads (synthetic: no dataset, the pulse is generated):
                     the adjoint workload: a seeded degree-6 spectral phase on the input
                     (spectral_phase) and the output energy in the 500-600 nm band
                     (band_weights) as the objective
+  fused_silica_c3   64 pulses (c3_batch): N_R in {128, 256, 512}, N_T in {1024 .. 8192},
+                    P ~ U[1, 8] P_cr, CEP ~ U[0, 2 pi), 30-100 fs, w0 50-150 um drawn from a
+                    seed; window 400 fs * N_T / 2048 and R = 6 w0 (unstated by the workload);
+                    1 mm in 500 fixed 2 um steps
   argon_c5          N_R=512, N_T=32768, 3.9 um 80 fs w0 = 1 mm 4 P_cr pulse in 1 atm argon,
                     2 ps window, R = 4 mm (R unstated by the workload; 4 w0 chosen), z = 20 cm,
                     solid-path Keldysh rate with Ip = 15.76 eV (the gas PPT build is not on
@@ -94,6 +98,20 @@ def fused_silica_c1(dirpath):
     return p
 
 
+def fused_silica_c2_rows(dirpath, n_r):
+    """The 1024 x 16384 workload's pulse, window and physics on n_r radial points with R
+    scaled by n_r / 1024 (same radial spacing): a smaller case of the same kernels for
+    profiling captures."""
+    p = fused_silica_c2(dirpath)
+    with open(p) as f:
+        txt = f.read()
+    txt = txt.replace("N_R 1024", f"N_R {n_r}").replace("R_MAX 1.2e-3", f"R_MAX {1.2e-3 * n_r / 1024!r}")
+    q = os.path.join(dirpath, f"fused_silica_c2_{n_r}.txt")
+    with open(q, "w") as f:
+        f.write(txt)
+    return q
+
+
 def fused_silica_c2(dirpath):
     """1024 x 16384, same pulse, R = 1.2 mm, 1.6 ps window, 3 mm, adaptive dz (tol 1e-6)."""
     tabulate_medium(os.path.join(dirpath, "fused_silica.rawdisp"))
@@ -124,6 +142,33 @@ def fused_silica_c4(dirpath):
     with open(p, "w") as f:
         f.write(_fmt(d))
     return p
+
+
+def c3_batch(dirpath, seed=0, n=64):
+    """The batched-scan workload: n fused-silica pulses with uneven grids and parameters
+    drawn from numpy PCG64(seed).  Returns [(config path, draw dict)]."""
+    tabulate_medium(os.path.join(dirpath, "fused_silica.rawdisp"))
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(n):
+        nr = int(rng.choice([128, 256, 512]))
+        nt = int(rng.choice([1024, 2048, 4096, 8192]))
+        pcr = float(rng.uniform(1, 8))
+        cep = float(rng.uniform(0, 2 * math.pi))
+        tau = float(rng.uniform(30e-15, 100e-15))
+        w0 = float(rng.uniform(50e-6, 150e-6))
+        win = 400e-15 * nt / 2048
+        d = {"LAMBDA_V": "8e-7", "N_T": str(nt), "T_MIN": repr(-win / 2), "T_MAX": repr(win / 2),
+             "DISPERSION_FILE": "fused_silica.rawdisp", "N_R": str(nr), "R_MAX": repr(6 * w0),
+             "N_Z": "501", "Z_MIN": "0", "Z_MAX": "1e-3", "ZNET_TYPE": "e", "MAX_TOLERANCE": "1e3",
+             "PULSE_SHAPE": "gg", "DURATION_FWHM": repr(tau), "DIAMETER_FWHM": repr(w0 * math.sqrt(2 * math.log(2))),
+             "POWER_CR": repr(pcr), "WAVEFRONT_RADIUS": "1e100", "CE_PHASE": repr(cep)}
+        d.update(SILICA_NL)
+        p = os.path.join(dirpath, f"fused_silica_c3_{i:02d}.txt")
+        with open(p, "w") as f:
+            f.write(_fmt(d))
+        out.append((p, {"n_r": nr, "n_t": nt, "power_cr": pcr, "cep": cep, "duration_fwhm": tau, "w0": w0}))
+    return out
 
 
 def spectral_phase(omega, omega0, duration_fwhm, seed, degree=6):

@@ -12,7 +12,9 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "../../include/gs_abi.h"
@@ -423,6 +425,7 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
     fa.N = nt; fa.M = h->M; fa.P = h->P; fa.logM = h->logM;
     fa.tw = (const T2*)h->tw;
     fa.max_out = h->max_dev;
+    fa.threads = h->nl_threads;
     PlasmaArgs<Rl> pa = plasma_args<Rl>(h, raman, raman_scan);
     SpecArgs<Rl> sa{};
     sa.N = nt; sa.rows = nr; sa.u1 = U1; sa.u2 = U2; sa.u3 = U3;
@@ -582,6 +585,60 @@ int gs_step(gs_handle* h, double current_z, double znet_cur, double znet_prev, d
             return collect_qdht_time(h);
         }
     }
+}
+
+// ------------------------------------------------------------------ autotuning --
+// Candidate launch shapes of the fused RK4-stage kernels (threads per radial row: the FFT's
+// parallelism and the recurrences' chunk length L = n_t / threads) are timed on this
+// handle's own rows and the fastest is kept; the choice is cached per (precision, n_r, n_t)
+// for the process, so a batch of pulses on the same grid tunes once.
+static std::map<std::tuple<int, int, int>, std::pair<int, double>> g_tune_cache;
+
+int gs_autotune(gs_handle* h, int* threads_out, double* ms_per_stage_out) {
+    if (!h) return GS_ERR_ARG;
+    if (!h->tables_ok || !h->field_ok) return fail(h, GS_ERR_STATE, "tables / field not set");
+    CK(h, cudaSetDevice(h->p.device));
+    const int nt = h->nt;
+    const auto key = std::make_tuple(h->fp64 ? 1 : 0, h->nr, nt);
+    auto it = g_tune_cache.find(key);
+    if (it == g_tune_cache.end()) {
+        int best = 0;
+        double best_ms = 0;
+        if (h->fused && h->p.nonlinear) {
+            const int cand[4] = {nt / 32, nt / 16, nt / 8, nt / 4};
+            for (int c : cand) {
+                const bool ok = h->fp64 ? nl_fused_threads_ok<double>(nt, c) : nl_fused_threads_ok<float>(nt, c);
+                if (!ok) continue;
+                h->nl_threads = c;
+                // stages read FIELD and write only scratch (BIGBUFFER1, the stage buffers)
+                int rc = GS_OK;
+                for (int w = 0; w < 2 && !rc; w++) rc = gsi::nl_stages(h, 0.0, nullptr);
+                if (rc) return rc;
+                CK(h, cudaEventRecord(h->ev0, h->st));
+                const int reps = 5;
+                for (int r = 0; r < reps && !rc; r++) rc = gsi::nl_stages(h, 0.0, nullptr);
+                if (rc) return rc;
+                CK(h, cudaEventRecord(h->ev1, h->st));
+                CK(h, cudaEventSynchronize(h->ev1));
+                float ms = 0;
+                CK(h, cudaEventElapsedTime(&ms, h->ev0, h->ev1));
+                const double per = ms / (4.0 * reps);
+                if (best == 0 || per < best_ms) {
+                    best = c;
+                    best_ms = per;
+                }
+            }
+            CK(h, cudaMemsetAsync(h->err_dev, 0, 4, h->st));
+            CK(h, cudaStreamSynchronize(h->st));
+        }
+        it = g_tune_cache.emplace(key, std::make_pair(best, best_ms)).first;
+    }
+    h->nl_threads = it->second.first;
+    if (threads_out)
+        *threads_out = h->nl_threads > 0 ? h->nl_threads
+                                          : (h->fp64 ? nl_fused_default_threads<double>(nt) : nl_fused_default_threads<float>(nt));
+    if (ms_per_stage_out) *ms_per_stage_out = it->second.second;
+    return GS_OK;
 }
 
 // ------------------------------------------------------------------ dump reductions --

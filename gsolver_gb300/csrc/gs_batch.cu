@@ -1,0 +1,178 @@
+// gs_batch.cu -- many independent pulses advanced together, one CUDA graph launch per z-step
+// (no counterpart in the reference, which runs one pulse per MPI job).
+//
+// Every pulse keeps its own handle (grid, tables, state) and stream.  A z-step of the batch
+// is every pulse's propagator() work -- the four RK4 stages and the QDHT pair with the
+// linear step -- issued on the pulses' own streams between a fork and a join on the
+// batch's stream, so pulses of different grids run concurrently and fill the GPU together.
+// The whole z-step is captured once into a CUDA graph and replayed, so the host issues one
+// launch per z-step instead of ~10 per pulse.  Step sizes are fixed per pulse (the graph
+// holds them; a new set of sizes captures a new graph); the adaptive controller needs a
+// host decision per step and stays with gs_step.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "gs_handle.h"
+
+struct gs_batch {
+    std::vector<gs_handle*> h;
+    int device = 0;
+    cudaStream_t st = nullptr;        // fork / join stream, the graph's launch stream
+    cudaEvent_t fork = nullptr;
+    std::vector<cudaEvent_t> join;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<double> graph_dz;     // the step sizes captured in `exec`
+    long long launches = 0;           // kernels issued (graph replays count their kernels)
+    long long kernels_per_step = 0;
+    std::string err;
+};
+
+static std::string g_batch_err;
+
+static int bfail(gs_batch* b, int code, const std::string& m) {
+    if (b) b->err = m; else g_batch_err = m;
+    return code;
+}
+
+#define BCK(b, expr)                                                                            \
+    do {                                                                                        \
+        cudaError_t _e = (expr);                                                                \
+        if (_e != cudaSuccess) return bfail((b), GS_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e)); \
+    } while (0)
+
+static void batch_free_graph(gs_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->graph_dz.clear();
+}
+
+const char* gs_batch_last_error(const gs_batch* b) { return b ? b->err.c_str() : g_batch_err.c_str(); }
+
+int gs_batch_create(int n, gs_handle* const* pulses, gs_batch** out) {
+    if (!out || n < 1 || !pulses) return bfail(nullptr, GS_ERR_ARG, "gs_batch_create: null argument or n < 1");
+    *out = nullptr;
+    const int dev = pulses[0] ? pulses[0]->p.device : 0;
+    for (int i = 0; i < n; i++) {
+        if (!pulses[i]) return bfail(nullptr, GS_ERR_ARG, "gs_batch_create: null pulse handle");
+        if (pulses[i]->p.device != dev) return bfail(nullptr, GS_ERR_ARG, "gs_batch_create: pulses on different devices");
+        for (int j = 0; j < i; j++)
+            if (pulses[j] == pulses[i]) return bfail(nullptr, GS_ERR_ARG, "gs_batch_create: a pulse appears twice");
+    }
+    cudaError_t e = cudaSetDevice(dev);
+    if (e != cudaSuccess) return bfail(nullptr, GS_ERR_CUDA, cudaGetErrorString(e));
+    gs_batch* b = new gs_batch();
+    b->h.assign(pulses, pulses + n);
+    b->device = dev;
+    b->join.assign(n, nullptr);
+    bool ok = cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) == cudaSuccess &&
+              cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) == cudaSuccess;
+    for (int i = 0; i < n && ok; i++) ok = cudaEventCreateWithFlags(&b->join[i], cudaEventDisableTiming) == cudaSuccess;
+    if (!ok) {
+        cudaGetLastError();
+        gs_batch_destroy(b);
+        return bfail(nullptr, GS_ERR_CUDA, "gs_batch_create: stream/event creation failed");
+    }
+    *out = b;
+    return GS_OK;
+}
+
+int gs_batch_destroy(gs_batch* b) {
+    if (!b) return GS_OK;
+    cudaSetDevice(b->device);
+    batch_free_graph(b);
+    for (cudaEvent_t e : b->join)
+        if (e) cudaEventDestroy(e);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->st) cudaStreamDestroy(b->st);
+    delete b;
+    return GS_OK;
+}
+
+void* gs_batch_stream(const gs_batch* b) { return b ? (void*)b->st : nullptr; }
+
+long long gs_batch_launch_count(const gs_batch* b) { return b ? b->launches : 0; }
+
+// one z-step of every pulse between a fork and a join on b->st (captured or not)
+static int batch_enqueue_step(gs_batch* b, const double* dz, long long* nk) {
+    BCK(b, cudaEventRecord(b->fork, b->st));
+    for (size_t i = 0; i < b->h.size(); i++) {
+        gs_handle* h = b->h[i];
+        const long long l0 = h->launches;
+        BCK(b, cudaStreamWaitEvent(h->st, b->fork, 0));
+        int rc = gsi::nl_stages(h, dz[i], nullptr);
+        if (!rc) rc = gsi::lstep(h, dz[i]);
+        if (rc) return bfail(b, rc, "pulse " + std::to_string(i) + ": " + h->err);
+        BCK(b, cudaEventRecord(b->join[i], h->st));
+        BCK(b, cudaStreamWaitEvent(b->st, b->join[i], 0));
+        *nk += h->launches - l0;
+    }
+    return GS_OK;
+}
+
+int gs_batch_step(gs_batch* b, int n_steps, const double* dz, int use_graph) {
+    if (!b || !dz || n_steps < 0) return bfail(b, GS_ERR_ARG, "gs_batch_step: null argument or n_steps < 0");
+    for (size_t i = 0; i < b->h.size(); i++) {
+        gs_handle* h = b->h[i];
+        if (!h->tables_ok || !h->field_ok) return bfail(b, GS_ERR_STATE, "pulse " + std::to_string(i) + ": tables / field not set");
+        if (!(dz[i] > 0)) return bfail(b, GS_ERR_ARG, "gs_batch_step: step sizes must be > 0");
+        if (h->time_qdht) return bfail(b, GS_ERR_STATE, "pulse " + std::to_string(i) + ": QDHT timing is on");
+    }
+    BCK(b, cudaSetDevice(b->device));
+    for (gs_handle* h : b->h) BCK(b, cudaMemsetAsync(h->err_dev, 0, 4, h->st));
+    // the pulses' streams may hold earlier work: the batch stream waits for all of it
+    for (size_t i = 0; i < b->h.size(); i++) {
+        BCK(b, cudaEventRecord(b->join[i], b->h[i]->st));
+        BCK(b, cudaStreamWaitEvent(b->st, b->join[i], 0));
+    }
+    if (use_graph) {
+        const bool same = b->exec && b->graph_dz.size() == b->h.size() &&
+                          std::equal(b->graph_dz.begin(), b->graph_dz.end(), dz);
+        if (!same) {
+            batch_free_graph(b);
+            long long nk = 0;
+            BCK(b, cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+            const int rc = batch_enqueue_step(b, dz, &nk);
+            cudaGraph_t g = nullptr;
+            const cudaError_t ee = cudaStreamEndCapture(b->st, &g);
+            if (rc) {
+                if (g) cudaGraphDestroy(g);
+                return rc;
+            }
+            if (ee != cudaSuccess) return bfail(b, GS_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(ee));
+            b->graph = g;
+            BCK(b, cudaGraphInstantiate(&b->exec, b->graph, 0));
+            b->graph_dz.assign(dz, dz + b->h.size());
+            b->kernels_per_step = nk;   // kernel nodes of one replay
+        }
+        for (int s = 0; s < n_steps; s++) {
+            BCK(b, cudaGraphLaunch(b->exec, b->st));
+            b->launches += b->kernels_per_step;
+        }
+    } else {
+        for (int s = 0; s < n_steps; s++) {
+            long long nk = 0;
+            const int rc = batch_enqueue_step(b, dz, &nk);
+            if (rc) return rc;
+            b->launches += nk;
+        }
+    }
+    BCK(b, cudaStreamSynchronize(b->st));
+    for (size_t i = 0; i < b->h.size(); i++) {
+        gs_handle* h = b->h[i];
+        unsigned err = 0;
+        BCK(b, cudaMemcpy(&err, h->err_dev, 4, cudaMemcpyDeviceToHost));
+        if (h->tc) {
+            std::string m;
+            if (gs::qdht_tc_check(h->tc, &m)) return bfail(b, GS_ERR_CUDA, "pulse " + std::to_string(i) + ": " + m);
+        }
+        if (err & 1u) return bfail(b, GS_ERR_BLAST, "pulse " + std::to_string(i) + ": " + gs_status_string(GS_ERR_BLAST));
+        if (err & 2u) return bfail(b, GS_ERR_NAN, "pulse " + std::to_string(i) + ": " + gs_status_string(GS_ERR_NAN));
+    }
+    return GS_OK;
+}

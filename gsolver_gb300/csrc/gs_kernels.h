@@ -20,6 +20,7 @@ template <typename Rl> struct FftArgs {
     unsigned long long* max_out;
     int tpost;                               // time-side store op (inverse)
     const typename Vec2<Rl>::T* e;           // time-domain field (TPOST_DIVN_MULE)
+    int threads;                             // fused kernels: threads per row (0: N/16, capped)
 };
 
 template <typename Rl> struct PlasmaArgs {
@@ -100,6 +101,9 @@ cudaError_t launch_permute(int dir, const void* src, void* dst, const int* perm,
 
 // ---- fused RK4 stage (gs_nl_fused.cu), rows that fit one CTA's shared memory
 template <typename Rl> bool nl_fused_supported(int N);
+// a thread count the fused kernels accept for rows of N (multiple of 32, divides N, fits)
+template <typename Rl> bool nl_fused_threads_ok(int N, int threads);
+template <typename Rl> int nl_fused_default_threads(int N);
 template <typename Rl> cudaError_t nl_fused_setup(int N);
 template <typename Rl>
 cudaError_t launch_nl_front(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2<Rl>::T* A, int rows,

@@ -362,6 +362,13 @@ template <typename Rl> bool nl_fused_supported(int N) {
     return N % nthr == 0 && FrontSmem<Rl>::bytes(N, nthr) <= 227 * 1024;
 }
 
+template <typename Rl> bool nl_fused_threads_ok(int N, int t) {
+    const int maxt = sizeof(Rl) == 8 ? 512 : 1024;
+    return t >= 32 && t <= maxt && t % 32 == 0 && N % t == 0 && FrontSmem<Rl>::bytes(N, t) <= 227 * 1024;
+}
+
+template <typename Rl> int nl_fused_default_threads(int N) { return fused_threads<Rl>(N); }
+
 template <typename Rl> cudaError_t nl_fused_setup(int N) {
     // the attribute is a per-kernel ceiling shared by every handle of the process: set the
     // device maximum so that a handle on a smaller grid never lowers it for a larger one
@@ -374,7 +381,7 @@ template <typename Rl> cudaError_t nl_fused_setup(int N) {
 template <typename Rl>
 cudaError_t launch_nl_front(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2<Rl>::T* A, int rows, cudaStream_t st,
                             long long* nl) {
-    const int nthr = fused_threads<Rl>(f.N);
+    const int nthr = f.threads > 0 ? f.threads : fused_threads<Rl>(f.N);
     nl_front_kernel<Rl><<<rows, nthr, FrontSmem<Rl>::bytes(f.N, nthr), st>>>(f, a, A);
     (*nl)++;
     return cudaGetLastError();
@@ -382,7 +389,7 @@ cudaError_t launch_nl_front(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2
 
 template <typename Rl>
 cudaError_t launch_nl_back(FftArgs<Rl> f, SpecArgs<Rl> s, int rows, cudaStream_t st, long long* nl) {
-    const int nthr = fused_threads<Rl>(f.N);
+    const int nthr = f.threads > 0 ? f.threads : fused_threads<Rl>(f.N);
     const size_t bb = ((size_t)padded_len(f.N) + f.N / 64 + 64) * sizeof(typename Vec2<Rl>::T);
     nl_back_kernel<Rl><<<rows, nthr, bb, st>>>(f, s);
     (*nl)++;
@@ -394,7 +401,9 @@ cudaError_t launch_nl_back(FftArgs<Rl> f, SpecArgs<Rl> s, int rows, cudaStream_t
     template cudaError_t nl_fused_setup<Rl>(int);                                                                 \
     template cudaError_t launch_nl_front<Rl>(FftArgs<Rl>, PlasmaArgs<Rl>, const typename Vec2<Rl>::T*, int,        \
                                              cudaStream_t, long long*);                                           \
-    template cudaError_t launch_nl_back<Rl>(FftArgs<Rl>, SpecArgs<Rl>, int, cudaStream_t, long long*);
+    template cudaError_t launch_nl_back<Rl>(FftArgs<Rl>, SpecArgs<Rl>, int, cudaStream_t, long long*);     \
+    template bool nl_fused_threads_ok<Rl>(int, int);                                                             \
+    template int nl_fused_default_threads<Rl>(int);
 GS_FUSED_INST(double)
 GS_FUSED_INST(float)
 

@@ -19,6 +19,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "gs_setup.h"
@@ -66,18 +67,23 @@ struct Cfg {
     }
 };
 
-void fft(std::vector<cd>& a, int sign) {   // unnormalised, FFTW sign convention, n = 2^m
+// twiddles exp(sign 2 pi i k / n), k < n/2, of fft() below
+std::vector<cd> fft_twiddles(size_t n, int sign) {
+    std::vector<cd> tw(n / 2);
+    for (size_t k = 0; k < n / 2; k++) {
+        const double ang = sign * 2.0 * M_PI * (double)k / (double)n;
+        tw[k] = cd(std::cos(ang), std::sin(ang));
+    }
+    return tw;
+}
+
+void fft(std::vector<cd>& a, const std::vector<cd>& tw) {   // unnormalised, FFTW sign convention, n = 2^m
     const size_t n = a.size();
     for (size_t i = 1, j = 0; i < n; i++) {
         size_t bit = n >> 1;
         for (; j & bit; bit >>= 1) j ^= bit;
         j ^= bit;
         if (i < j) std::swap(a[i], a[j]);
-    }
-    std::vector<cd> tw(n / 2);
-    for (size_t k = 0; k < n / 2; k++) {
-        const double ang = sign * 2.0 * M_PI * (double)k / (double)n;
-        tw[k] = cd(std::cos(ang), std::sin(ang));
     }
     for (size_t len = 2; len <= n; len <<= 1) {
         const size_t step = n / len;
@@ -89,6 +95,36 @@ void fft(std::vector<cd>& a, int sign) {   // unnormalised, FFTW sign convention
                 a[i + k + len / 2] = u - v;
             }
     }
+}
+
+void fft(std::vector<cd>& a, int sign) { fft(a, fft_twiddles(a.size(), sign)); }
+
+// f(i, worker) for i < n spread over the host's cores; each i is computed as it would be alone
+template <typename F>
+void parallel_for(int n, F f, unsigned* workers = nullptr) {
+    unsigned nth = std::thread::hardware_concurrency();
+    if (nth < 1) nth = 1;
+    if (nth > 64) nth = 64;
+    if ((int)nth > n) nth = n > 0 ? (unsigned)n : 1u;
+    if (workers) *workers = nth;
+    if (nth == 1) {
+        for (int i = 0; i < n; i++) f(i, 0u);
+        return;
+    }
+    std::vector<std::thread> pool;
+    for (unsigned w = 0; w < nth; w++)
+        pool.emplace_back([&, w]() {
+            for (int i = (int)w; i < n; i += (int)nth) f(i, w);
+        });
+    for (std::thread& t : pool) t.join();
+}
+
+unsigned worker_count(int n) {
+    unsigned nth = std::thread::hardware_concurrency();
+    if (nth < 1) nth = 1;
+    if (nth > 64) nth = 64;
+    if ((int)nth > n) nth = n > 0 ? (unsigned)n : 1u;
+    return nth;
 }
 
 double bessel_j0_zero(int s) {   // s-th positive zero of J0
@@ -296,9 +332,10 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
     const double S = zz[nr], V = S / 2.0 / M_PI;
     std::vector<double> x(nr), m1(nr), Cm((size_t)nr * nr), kt2(nr);
     for (int i = 0; i < nr; i++) m1[i] = std::fabs(::j1(zz[i]));
-    for (int i = 0; i < nr; i++)
+    parallel_for(nr, [&](int i, unsigned) {
         for (int j = 0; j < nr; j++)
             Cm[(size_t)i + (size_t)nr * j] = 2.0 / S * ::j0(zz[i] * zz[j] / S) / m1[i] / m1[j];
+    });
     for (int i = 0; i < nr; i++) {
         x[i] = zz[i] / S;
         const double kt = 2 * M_PI * x[i] * V / rmax;
@@ -319,8 +356,12 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
         wn[2 * i + 1] = k[i].imag();
     }
     // Keldysh table (top entry left at zero as in the reference)
+    // entries are independent: spread them over the host's cores (each is computed exactly
+    // as it would be alone)
     std::vector<double> rate(8192, 0.0);
-    for (int i = 0; i < 8191; i++) rate[i] = keldysh_rate_ln(kMinLn + kTol * i, k0r, Ui, w0, vg, mred) - kIonDenomLn;
+    parallel_for(8191, [&](int i, unsigned) {
+        rate[i] = keldysh_rate_ln(kMinLn + kTol * i, k0r, Ui, w0, vg, mred) - kIonDenomLn;
+    });
     // Raman response
     {
         const double M = tstep * (1 + omR * omR * tauR * tauR) / tauR / (omR * tauR);
@@ -365,8 +406,11 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
     f = cfg.f("WAVEFRONT_RADIUS", f);
     f = cfg.f("WAVEFRONT_RADIUS_DIFFRACTION", f / zR) * zR;
     std::vector<double> field(2 * (size_t)nr * nt);
-    std::vector<cd> row(nt);
-    for (int r = 0; r < nr; r++) {
+    const unsigned nw = worker_count(nr);
+    std::vector<std::vector<cd>> rows(nw, std::vector<cd>(nt));
+    const std::vector<cd> tw_fw = fft_twiddles(nt, -1), tw_bw = fft_twiddles(nt, +1);
+    parallel_for(nr, [&](int r, unsigned wk) {
+        std::vector<cd>& row = rows[wk];
         const double R = x[r] * rmax;
         const double amax = A0 * std::exp(-std::pow(R / ro, 2.0 * sgR));
         for (int t = 0; t < nt; t++) {
@@ -379,21 +423,26 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
             }
             row[t] = (amax * std::exp(-std::pow(T, 2.0 * sgT))) * car;
         }
-        fft(row, -1);
+        fft(row, tw_fw);
         for (int w = 0; w < nt; w++) {
             const double ph = (R * R * k[w].real() / 2.0 / f) - Cw * (om[w] - w0) * (om[w] - w0) / 2;
             const cd v = row[w] * cd(std::cos(ph), std::sin(ph)) / kFieldDenom;
             field[2 * ((size_t)r * nt + w)] = v.real();
             field[2 * ((size_t)r * nt + w) + 1] = v.imag();
         }
-    }
-    // init_zstep_kerr: max |IFFT(FIELD)/N_T|^2
-    double maxI = 0;
-    for (int r = 0; r < nr; r++) {
+    });
+    // init_zstep_kerr: max |IFFT(FIELD)/N_T|^2 (per-row maxima, then their max)
+    std::vector<double> rmaxI(nr, 0.0);
+    parallel_for(nr, [&](int r, unsigned wk) {
+        std::vector<cd>& row = rows[wk];
         for (int w = 0; w < nt; w++) row[w] = cd(field[2 * ((size_t)r * nt + w)], field[2 * ((size_t)r * nt + w) + 1]);
-        fft(row, +1);
-        for (int t = 0; t < nt; t++) maxI = std::max(maxI, std::norm(row[t] / (double)nt));
-    }
+        fft(row, tw_bw);
+        double m = 0;
+        for (int t = 0; t < nt; t++) m = std::max(m, std::norm(row[t] / (double)nt));
+        rmaxI[r] = m;
+    });
+    double maxI = 0;
+    for (int r = 0; r < nr; r++) maxI = std::max(maxI, rmaxI[r]);
     double dz = znet.size() > 1 ? znet[1] - znet[0] : 0;
     const double kNL = w0 / kC * n2s * maxI;
     if (dz * kNL > tol) dz = tol / kNL;

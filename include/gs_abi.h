@@ -152,6 +152,14 @@ int gs_dump_reductions(gs_handle* h, const double* qdht_x, double r_max, double*
 /* The time-domain field BW-FFT(FIELD)/N_T, [n_r][n_t] complex: dump_type_full_class (77-97). */
 int gs_get_time_field(gs_handle* h, double* e_r_t);
 
+/* Autotuning (no counterpart in the reference): times the launch shapes of the fused
+ * RK4-stage kernels (threads per radial row, which also sets the recurrences' chunk length)
+ * on this handle's grid and field and keeps the fastest; the choice is cached per
+ * (precision, n_r, n_t) for the process.  Needs tables and field; leaves FIELD and
+ * BIGBUFFER2 unchanged.  Results stay within the parity bounds for every shape (the chunking
+ * of the recurrences only reorders roundings). */
+int gs_autotune(gs_handle* h, int* threads, double* ms_per_stage);
+
 /* ---- Gradients (no counterpart in the reference: it has no adjoint) ----------------------
  * A run of n_steps propagator() calls with the step sizes given instead of chosen by the
  * controller: step n uses dz_rk[n] in its RK4 stages and dz_lin[n] in its linear step (the
@@ -173,6 +181,24 @@ int gs_gradient(gs_handle* h, const double* field_in, int n_steps, const double*
  * is run forward (the handle then holds state n+1) and the cotangents of FIELD (r,omega) and
  * BIGBUFFER2 (k,omega) after it, field_bar and spec_bar, are replaced by those before it. */
 int gs_adjoint_step(gs_handle* h, double dz_rk, double dz_lin, double* field_bar, double* spec_bar);
+
+/* ---- Batches of independent pulses (no counterpart in the reference: one pulse per job) ----
+ * A batch advances n pulses (each its own handle, grid, tables and stream, all on one
+ * device) together: one z-step of the batch is every pulse's propagator() work with a
+ * fixed step size dz[i] (RK4 stages and linear step), issued concurrently.  With use_graph
+ * the z-step is captured once into a CUDA graph and replayed (one launch per z-step); a
+ * different dz array captures a new graph.  Blast / NaN / tensor-core wait errors are
+ * checked after the n_steps and name the pulse.  The pulses' handles stay owned by the
+ * caller and must outlive the batch; the adaptive controller stays with gs_step. */
+typedef struct gs_batch gs_batch;
+int gs_batch_create(int n, gs_handle* const* pulses, gs_batch** out);
+int gs_batch_step(gs_batch* b, int n_steps, const double* dz, int use_graph);
+/* The batch's cudaStream_t (the graph launches on it; it joins every pulse's stream). */
+void* gs_batch_stream(const gs_batch* b);
+/* Kernels issued by the batch (a graph replay counts its kernel nodes). */
+long long gs_batch_launch_count(const gs_batch* b);
+const char* gs_batch_last_error(const gs_batch* b);
+int gs_batch_destroy(gs_batch* b);
 
 /* Carrier-density maxima without any device allocation.  No counterpart in the reference:
  * it is an addition for host code that cannot allocate device memory where it needs this
