@@ -57,6 +57,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--batch-pulses", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--adjoint-steps", type=int, default=1000)
@@ -254,11 +255,18 @@ def batch_leg(args, lrank):
         p.set_field(s["field"])
     B = gs.Batch(P)
     dz = np.array([float(s["init_zstep"]) for s in S])
+    tuned = None
+    if not args.no_autotune:
+        # default shapes vs every grid's own tuned shape, timed on the whole batch
+        ms_def, ms_tun, chose = B.autotune(dz)
+        tuned = {"ms_per_zstep_default": ms_def, "ms_per_zstep_tuned_per_grid": ms_tun,
+                 "chosen": "tuned per grid" if chose else "default",
+                 "threads": {f"{s['n_r']}x{s['n_t']}": p.nl_threads() for s, p in zip(S, P)}}
     pts = sum(s["n_r"] * s["n_t"] for s in S)
     stream = torch.cuda.ExternalStream(B.stream_ptr(), device=lrank)
     out = {"workload": f"fused_silica_batch{len(P)}", "pulses": len(P), "points_per_zstep": pts,
            "grids": sorted({(s["n_r"], s["n_t"]) for s in S}), "precision": "mixed", "dz_m": 2e-6,
-           "host_setup_s": t_setup}
+           "host_setup_s": t_setup, "autotune": tuned or "off"}
     for graph in (True, False):
         B.step(dz, 2, graph=graph)   # warm-up (and graph capture)
         n0 = B.launch_count()
@@ -297,6 +305,8 @@ def adjoint_leg(args, lrank):
     n = args.adjoint_steps
     rk, lin = configs.clamp_schedule(S["znet"], S["init_zstep"], n)
     Pm = gs.Propagator(S, precision=gs.PREC_MIXED, device=lrank)
+    Pm.set_field(A0)
+    tuned = None if args.no_autotune else Pm.autotune()
 
     def timed(f, reps=2):
         f()   # warm-up: allocations, transposed-QDHT set-up
@@ -310,6 +320,7 @@ def adjoint_leg(args, lrank):
     out = {"workload": "fused_silica_256x4096_adjoint", "n_r": 256, "n_t": 4096, "steps": n, "dz_m": 2e-6,
            "objective": "band energy 500-600 nm, average_spectrum radial weights",
            "checkpoint_stride": int(np.ceil(np.sqrt(n))), "precision": "mixed",
+           "nl_threads_per_row": tuned[0] if tuned else "default",
            "forward_ms": tf, "gradient_ms": tg, "cost_ratio": tg / tf,
            "note": "gradient_ms = forward + adjoint (one gs_gradient call); cost_ratio = gradient / forward"}
     m = args.adjoint_check_steps
@@ -371,6 +382,7 @@ def main():
         else:
             raise
     P.set_field(S["field"])
+    tuned = None if args.no_autotune else P.autotune()   # fused NL launch shape (threads per row)
     state = new_state(S)
     run_z_steps(P, S, state, args.warmup)
     stream = torch.cuda.ExternalStream(P.stream_ptr(), device=lrank)
@@ -413,7 +425,8 @@ def main():
             "data": "synthetic (seeded Gaussian pulse + 1e-4 complex noise; no dataset)",
             "config": dict(conf, precision="mixed" if prec == gs.PREC_MIXED else "fp64",
                            parallelism=f"replicas{world}", l2="inputs larger than L2 (state ~1 GB per pulse)",
-                           z_reached_m=state["z"], dz_last_m=state["zstep"]),
+                           z_reached_m=state["z"], dz_last_m=state["zstep"],
+                           nl_threads_per_row=tuned[0] if tuned else "default"),
             "gpu_launches": launches, "roofline": roof, "clocks": clk.summary()}
 
     # e2e through the public API with pinned host buffers

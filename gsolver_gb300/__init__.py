@@ -38,7 +38,7 @@ ABI_FUNCTIONS = (
     "gs_plasma_max_noalloc", "gs_noalloc_max_samples", "gs_noalloc_last_error",
     "gs_forward_fixed", "gs_gradient", "gs_adjoint_step",
     "gs_batch_create", "gs_batch_step", "gs_batch_stream", "gs_batch_launch_count", "gs_batch_last_error",
-    "gs_batch_destroy", "gs_autotune",
+    "gs_batch_destroy", "gs_autotune", "gs_set_nl_threads", "gs_get_nl_threads", "gs_batch_autotune",
 )
 
 
@@ -125,6 +125,9 @@ def load_library(path: str | None = None):
     L.gs_batch_last_error.restype = C.c_char_p
     L.gs_batch_destroy.argtypes = [V]
     L.gs_autotune.argtypes = [V, C.POINTER(C.c_int), PD]
+    L.gs_set_nl_threads.argtypes = [V, I]
+    L.gs_get_nl_threads.argtypes = [V]
+    L.gs_batch_autotune.argtypes = [V, V, PD, PD, C.POINTER(C.c_int)]
     _lib = L
     return L
 
@@ -263,6 +266,12 @@ class Propagator:
         ms, n = C.c_double(), C.c_int()
         self._check(self.L.gs_qdht_timing(self.h, int(enable), C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    def nl_threads(self, threads=None):
+        """Read, or set (0: default), the fused kernels' threads per row."""
+        if threads is not None:
+            self._check(self.L.gs_set_nl_threads(self.h, int(threads)))
+        return self.L.gs_get_nl_threads(self.h)
 
     def autotune(self):
         """Pick the fused NL kernels' launch shape for this grid (gs_autotune); returns
@@ -422,6 +431,16 @@ class Batch:
         rc = self.L.gs_batch_step(self.b, int(n_steps), _ptr(d), int(bool(graph)))
         if rc:
             raise GsError(rc, self.L.gs_batch_last_error(self.b).decode())
+
+    def autotune(self, dz):
+        """Default vs per-grid tuned launch shapes for the batch as a whole (gs_batch_autotune);
+        returns (ms per z-step default, ms tuned, chose tuned)."""
+        d = np.ascontiguousarray(dz, dtype=np.float64)
+        a, b, c = C.c_double(), C.c_double(), C.c_int()
+        rc = self.L.gs_batch_autotune(self.b, _ptr(d), C.byref(a), C.byref(b), C.byref(c))
+        if rc:
+            raise GsError(rc, self.L.gs_batch_last_error(self.b).decode())
+        return a.value, b.value, bool(c.value)
 
     def stream_ptr(self):
         return self.L.gs_batch_stream(self.b)

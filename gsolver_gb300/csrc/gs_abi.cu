@@ -641,6 +641,22 @@ int gs_autotune(gs_handle* h, int* threads_out, double* ms_per_stage_out) {
     return GS_OK;
 }
 
+int gs_set_nl_threads(gs_handle* h, int threads) {
+    if (!h) return GS_ERR_ARG;
+    if (threads != 0) {
+        const bool ok = h->fp64 ? nl_fused_threads_ok<double>(h->nt, threads) : nl_fused_threads_ok<float>(h->nt, threads);
+        if (!ok || !h->fused) return fail(h, GS_ERR_ARG, "threads per row not valid for this grid");
+    }
+    h->nl_threads = threads;
+    return GS_OK;
+}
+
+int gs_get_nl_threads(const gs_handle* h) {
+    if (!h) return 0;
+    if (h->nl_threads > 0) return h->nl_threads;
+    return h->fp64 ? nl_fused_default_threads<double>(h->nt) : nl_fused_default_threads<float>(h->nt);
+}
+
 // ------------------------------------------------------------------ dump reductions --
 template <typename Rl>
 static int dump_impl(gs_handle* h, const double* qdht_x, double r_max, double* max_I, double* flux,

@@ -168,6 +168,7 @@ int stage_vjps(gs_handle* h, const AdjPtrs& P, const GsTape& tp, double dz) {
     v.recombination_tau = pa.recombination_tau;
     v.a_re = pa.a_re; v.a_im = pa.a_im; v.aN_re = pa.aN_re; v.aN_im = pa.aN_im;
     v.fRM = pa.fRM; v.one_minus_fR = pa.one_minus_fR;
+    v.threads = 0;   // N/16: measured faster for the VJP than the forward's tuned shape at 256x4096
     // R = (k1 + 2 k2 + 2 k3 + k4)/6 with stage inputs A + dz/2 k1, A + dz/2 k2, A + dz k3
     const double cR_next[4] = {0.0, 1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0};   // weight of k_{s-1} in R
     const double cdz_next[4] = {0.0, 0.5 * dz, 0.5 * dz, dz};          // stage s input coefficient

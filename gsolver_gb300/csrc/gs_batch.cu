@@ -176,3 +176,84 @@ int gs_batch_step(gs_batch* b, int n_steps, const double* dz, int use_graph) {
     }
     return GS_OK;
 }
+
+// Batch-level choice between the default launch shapes and every pulse's own tuned shape
+// (gs_autotune, timed alone): concurrent pulses compete for SMs, so a shape that wins alone
+// can lose in the batch.  One graph z-step is timed each way from the same state (FIELD and
+// BIGBUFFER2 of every pulse are saved in a temporary snapshot and restored), and the faster
+// set of shapes is kept.
+int gs_batch_autotune(gs_batch* b, const double* dz, double* ms_default, double* ms_tuned, int* chose_tuned) {
+    if (!b || !dz) return bfail(b, GS_ERR_ARG, "gs_batch_autotune: null argument");
+    BCK(b, cudaSetDevice(b->device));
+    const size_t n = b->h.size();
+    std::vector<int> tuned(n);
+    for (size_t i = 0; i < n; i++) {
+        int t = 0;
+        const int rc = gs_autotune(b->h[i], &t, nullptr);
+        if (rc) return bfail(b, rc, "pulse " + std::to_string(i) + ": " + b->h[i]->err);
+        tuned[i] = b->h[i]->nl_threads;
+    }
+    // snapshot of every pulse's FIELD and BIGBUFFER2 (a temporary allocation: tuning only)
+    std::vector<char*> snap(n, nullptr);
+    for (size_t i = 0; i < n; i++) {
+        gs_handle* h = b->h[i];
+        if (cudaMalloc((void**)&snap[i], 2 * (size_t)h->nr * h->nt * h->esz) != cudaSuccess) {
+            cudaGetLastError();
+            for (char* q : snap)
+                if (q) cudaFree(q);
+            return bfail(b, GS_ERR_NOMEM, "gs_batch_autotune: no memory for the state snapshot");
+        }
+    }
+    auto save = [&](bool restore) -> int {
+        for (size_t i = 0; i < n; i++) {
+            gs_handle* h = b->h[i];
+            const size_t bytes = (size_t)h->nr * h->nt * h->esz;
+            char* st = snap[i];
+            if (!restore) {
+                BCK(b, cudaMemcpyAsync(st, h->A, bytes, cudaMemcpyDeviceToDevice, h->st));
+                BCK(b, cudaMemcpyAsync(st + bytes, h->S, bytes, cudaMemcpyDeviceToDevice, h->st));
+            } else {
+                BCK(b, cudaMemcpyAsync(h->A, st, bytes, cudaMemcpyDeviceToDevice, h->st));
+                BCK(b, cudaMemcpyAsync(h->S, st + bytes, bytes, cudaMemcpyDeviceToDevice, h->st));
+            }
+        }
+        return GS_OK;
+    };
+    cudaEvent_t e0, e1;
+    BCK(b, cudaEventCreate(&e0));
+    BCK(b, cudaEventCreate(&e1));
+    double ms[2] = {0, 0};
+    int rc = GS_OK;
+    for (int pass = 0; pass < 2 && !rc; pass++) {
+        for (size_t i = 0; i < n; i++) b->h[i]->nl_threads = pass ? tuned[i] : 0;
+        batch_free_graph(b);   // shapes are baked into the graph
+        if (!rc && pass == 0) rc = save(false);
+        if (!rc) rc = gs_batch_step(b, 1, dz, 1);   // capture + warm-up
+        if (!rc) rc = save(true);
+        const int reps = 3;
+        if (!rc) {
+            for (gs_handle* h : b->h) cudaStreamSynchronize(h->st);
+            cudaEventRecord(e0, b->st);
+            rc = gs_batch_step(b, reps, dz, 1);
+            cudaEventRecord(e1, b->st);
+            cudaEventSynchronize(e1);
+            float t = 0;
+            cudaEventElapsedTime(&t, e0, e1);
+            ms[pass] = t / reps;
+        }
+        if (!rc) rc = save(true);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    for (gs_handle* h : b->h) cudaStreamSynchronize(h->st);
+    for (char* q : snap) cudaFree(q);
+    if (rc) return rc;
+    const bool use_tuned = ms[1] < ms[0];
+    for (size_t i = 0; i < n; i++) b->h[i]->nl_threads = use_tuned ? tuned[i] : 0;
+    batch_free_graph(b);
+    for (gs_handle* h : b->h) BCK(b, cudaStreamSynchronize(h->st));
+    if (ms_default) *ms_default = ms[0];
+    if (ms_tuned) *ms_tuned = ms[1];
+    if (chose_tuned) *chose_tuned = use_tuned ? 1 : 0;
+    return GS_OK;
+}

@@ -61,6 +61,7 @@ template <typename Rl> struct VjpArgs {
     int kerr_on, raman_scan;
     double tstep_scaled, neutral_density, ionization_potential, ponderomotive, avalanche_cs, recombination_tau;
     double a_re, a_im, aN_re, aN_im, fRM, one_minus_fR;
+    int threads;                          // threads per row (0 or not valid: N/16, capped)
 };
 template <typename Rl> bool nl_vjp_supported(int N);
 template <typename Rl> cudaError_t nl_vjp_setup(int N);

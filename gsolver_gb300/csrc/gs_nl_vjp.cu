@@ -279,7 +279,9 @@ template <typename Rl> cudaError_t nl_vjp_setup(int N) {
 }
 
 template <typename Rl> cudaError_t launch_nl_vjp(const VjpArgs<Rl>& v, int rows, cudaStream_t st, long long* nl) {
-    const int nthr = vjp_threads<Rl>(v.N);
+    int nthr = vjp_threads<Rl>(v.N);
+    const int t = v.threads;
+    if (t >= 32 && t <= 512 && t % 32 == 0 && v.N % t == 0 && vjp_smem<Rl>(v.N, t) <= 227 * 1024) nthr = t;
     nl_vjp_kernel<Rl><<<rows, nthr, vjp_smem<Rl>(v.N, nthr), st>>>(v);
     (*nl)++;
     return cudaGetLastError();

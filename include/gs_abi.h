@@ -159,6 +159,9 @@ int gs_get_time_field(gs_handle* h, double* e_r_t);
  * BIGBUFFER2 unchanged.  Results stay within the parity bounds for every shape (the chunking
  * of the recurrences only reorders roundings). */
 int gs_autotune(gs_handle* h, int* threads, double* ms_per_stage);
+/* Set (0: the default) or read the fused kernels' threads per row for this handle. */
+int gs_set_nl_threads(gs_handle* h, int threads);
+int gs_get_nl_threads(const gs_handle* h);
 
 /* ---- Gradients (no counterpart in the reference: it has no adjoint) ----------------------
  * A run of n_steps propagator() calls with the step sizes given instead of chosen by the
@@ -198,6 +201,10 @@ void* gs_batch_stream(const gs_batch* b);
 /* Kernels issued by the batch (a graph replay counts its kernel nodes). */
 long long gs_batch_launch_count(const gs_batch* b);
 const char* gs_batch_last_error(const gs_batch* b);
+/* Chooses, for the batch as a whole, between the default launch shapes and each pulse's own
+ * gs_autotune shape by timing one graph z-step each way from the same state (the pulses'
+ * FIELD and BIGBUFFER2 are restored afterwards); keeps the faster. */
+int gs_batch_autotune(gs_batch* b, const double* dz, double* ms_default, double* ms_tuned, int* chose_tuned);
 int gs_batch_destroy(gs_batch* b);
 
 /* Carrier-density maxima without any device allocation.  No counterpart in the reference:

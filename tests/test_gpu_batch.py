@@ -54,3 +54,26 @@ def test_batch_rejects_bad_arguments():
         B.step(np.array([1e-6, -1.0, 1e-6, 1e-6]), 1)
     with pytest.raises(gs.GsError):
         gs.Batch([P[0], P[0]])
+
+
+def test_batch_autotune_restores_state_and_keeps_results():
+    S, P = _pulses(gs.PREC_MIXED)
+    dz = np.array([s["init_zstep"] for s in S])
+    for s, p in zip(S, P):
+        p.set_field(s["field"])
+    B = gs.Batch(P)
+    before = [p.get_field(want_spec=True) for p in P]
+    ms_def, ms_tun, chose = B.autotune(dz)
+    assert ms_def > 0 and ms_tun > 0
+    for b, p in zip(before, P):
+        f, sp = p.get_field(want_spec=True)
+        assert np.array_equal(f, b[0]) and np.array_equal(sp, b[1])
+    B.step(dz, 2)
+    # each pulse alone with the same launch shape gives the same result
+    for s, p in zip(S, P):
+        got = p.get_field(want_spec=False)
+        p.set_field(s["field"])
+        for _ in range(2):
+            p.nl_step(float(s["init_zstep"]))
+            p.lstep(float(s["init_zstep"]))
+        assert np.array_equal(p.get_field(want_spec=False), got)
