@@ -51,14 +51,14 @@ class GsError(RuntimeError):
 class Params(C.Structure):
     _fields_ = [
         ("n_r", C.c_int), ("n_t", C.c_int), ("precision", C.c_int), ("nonlinear", C.c_int),
-        ("device", C.c_int), ("reserved0", C.c_int),
+        ("device", C.c_int), ("gas", C.c_int),
         ("tstep", C.c_double), ("tmin", C.c_double), ("tmax", C.c_double), ("omega0", C.c_double),
         ("ionrate_denom", C.c_double), ("neutral_density", C.c_double), ("rho0", C.c_double),
         ("ionization_potential", C.c_double), ("ponderomotive", C.c_double),
         ("avalanche_cs", C.c_double), ("recombination_tau", C.c_double),
         ("raman_fraction", C.c_double), ("n2", C.c_double),
         ("omega_min", C.c_double), ("omega_max", C.c_double), ("max_tolerance", C.c_double),
-        ("raman_tau", C.c_double), ("raman_omega", C.c_double),
+        ("raman_tau", C.c_double), ("raman_omega", C.c_double), ("th_coeff", C.c_double),
     ]
 
 
@@ -156,6 +156,8 @@ class Propagator:
         p.rho0 = float(setup.get("rho0", 0.0))
         p.raman_tau = float(setup.get("raman_tau", 0.0))
         p.raman_omega = float(setup.get("raman_omega", 0.0))
+        p.gas = int(setup.get("gas", 0))
+        p.th_coeff = float(setup.get("th_coeff", 0.0))
         self.params = p
         h = C.c_void_p()
         rc = self.L.gs_create(C.byref(p), C.byref(h))
@@ -388,7 +390,8 @@ class Setup:
         def grab(ptr, n, dt=np.float64):
             return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_double)), shape=(n,)).copy().view(dt)
         d = {k: getattr(p, k) for k in PARAM_KEYS}
-        d.update(n_r=nr, n_t=nt, rho0=p.rho0, raman_tau=p.raman_tau, raman_omega=p.raman_omega)
+        d.update(n_r=nr, n_t=nt, rho0=p.rho0, raman_tau=p.raman_tau, raman_omega=p.raman_omega,
+                 gas=p.gas, th_coeff=p.th_coeff, ion_levels=1, ion_potentials=np.array([p.ionization_potential]))
         d["rate_ln"] = grab(t.rate_ln, 8192)
         d["plasma_func"] = grab(t.plasma_func, 2 * nt, np.complex128)
         d["raman_func"] = grab(t.raman_func, 2 * nt, np.complex128)

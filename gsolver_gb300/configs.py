@@ -218,15 +218,20 @@ ARGON_NL = {
 }
 
 
-def argon_c5(dirpath, n_r=512, n_t=32768, cep=0.0, name="argon_c5"):
-    """Argon filament at 3.9 um (Sellmeier n-1 = 5.547e-4 (1 + 5.15e-3/lam^2 + 4.19e-5/lam^4))."""
+def argon_c5(dirpath, n_r=512, n_t=32768, cep=0.0, name="argon_c5", build="solid_qdht", power_cr=4.0, w0=1e-3,
+             r_max=4e-3, window=2e-12):
+    """Argon filament at 3.9 um (Sellmeier n-1 = 5.547e-4 (1 + 5.15e-3/lam^2 + 4.19e-5/lam^4)).
+    build "gas_qdht" selects the reference's gas binary (gsolver_gas_qdht: PPT multi-level
+    ionization, third harmonic, IONRATE_DENOM 1e10) through the GSOLVER_BUILD key."""
     tabulate_medium(os.path.join(dirpath, "argon.rawdisp"), medium="argon", lam_min_um=0.15, lam_max_um=20.0)
-    d = {"LAMBDA_V": "3.9e-6", "N_T": str(n_t), "T_MIN": "-1e-12", "T_MAX": "1e-12",
-         "DISPERSION_FILE": "argon.rawdisp", "N_R": str(n_r), "R_MAX": "4e-3",
+    d = {"LAMBDA_V": "3.9e-6", "N_T": str(n_t), "T_MIN": repr(-window / 2), "T_MAX": repr(window / 2),
+         "DISPERSION_FILE": "argon.rawdisp", "N_R": str(n_r), "R_MAX": repr(r_max),
          "N_Z": "201", "Z_MIN": "0", "Z_MAX": "0.2", "ZNET_TYPE": "e", "MAX_TOLERANCE": "1e-3",
-         "PULSE_SHAPE": "gg", "DURATION_FWHM": "80e-15", "DIAMETER_FWHM": repr(1e-3 * math.sqrt(2 * math.log(2))),
-         "POWER_CR": "4", "WAVEFRONT_RADIUS": "1e100", "CE_PHASE": repr(cep)}
+         "PULSE_SHAPE": "gg", "DURATION_FWHM": "80e-15", "DIAMETER_FWHM": repr(w0 * math.sqrt(2 * math.log(2))),
+         "POWER_CR": repr(power_cr), "WAVEFRONT_RADIUS": "1e100", "CE_PHASE": repr(cep)}
     d.update(ARGON_NL)
+    if build != "solid_qdht":
+        d["GSOLVER_BUILD"] = build
     p = os.path.join(dirpath, name + ".txt")
     with open(p, "w") as f:
         f.write(_fmt(d))

@@ -95,7 +95,7 @@ void* gs_stream(const gs_handle* h) { return h ? (void*)h->st : nullptr; }
 static void free_all(gs_handle* h) {
     void* ptrs[] = {h->A, h->S, h->NB, h->KP, h->E, h->U, h->tw, h->pf, h->rm, h->kerr, h->rate,
                     h->omega, h->ho, h->kt2, h->Cm, h->m1, h->wavenum, h->staging, h->perm_dev,
-                    h->err_dev, h->max_dev, h->dump_dev, h->m1inv, h->adj, h->adj_w};
+                    h->err_dev, h->max_dev, h->dump_dev, h->m1inv, h->adj, h->adj_w, h->th};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (h->tc) gs::qdht_tc_destroy(h->tc);
     if (h->tcT) gs::qdht_tc_destroy(h->tcT);
@@ -110,6 +110,10 @@ int gs_create(const gs_params* prm, gs_handle** out) {
     const int nr = prm->n_r, nt = prm->n_t;
     if (nr < 1 || nt < 64 || (nt & (nt - 1))) return fail(nullptr, GS_ERR_UNSUPPORTED, "n_t must be a power of two >= 64, n_r >= 1");
     if (prm->precision != GS_PREC_FP64 && prm->precision != GS_PREC_MIXED) return fail(nullptr, GS_ERR_ARG, "precision");
+    if (prm->gas && prm->th_coeff != 0 && prm->n2 != 0 && prm->raman_fraction > 0.001 &&
+        !(prm->raman_tau > 0 && prm->raman_omega > 0))
+        return fail(nullptr, GS_ERR_UNSUPPORTED,
+                    "gas build: the third harmonic with Raman needs the Raman oscillator parameters");
     gs_handle* h = new gs_handle();
     h->p = *prm;
     h->nr = nr;
@@ -258,6 +262,24 @@ int gs_upload_tables(gs_handle* h, const gs_tables* t) {
         if (gs::qdht_tc_set_lstep(h->tc, om.data(), wn.data(), ho.data(), t->kt2, h->p.omega_min, h->p.omega_max, &m))
             return fail(h, GS_ERR_CUDA, "mixed QDHT: " + m);
     }
+    if (h->p.gas && h->p.th_coeff != 0) {
+        // third harmonic (propagator.cu:712-720): th_coeff exp(j phi_t), phi_t =
+        // -2 OMEGA0 (TMIN + t (TMIN - TMAX)/N_T) (the reference's sign of the step; its
+        // OMEGA0 == OMEGA[0] holds on this grid), natural time order, FP64 then stored
+        std::vector<double> th(2 * (size_t)nt);
+        for (int t = 0; t < nt; t++) {
+            const double ph = -2.0 * h->p.omega0 * (h->p.tmin + t * (h->p.tmin - h->p.tmax) / nt);
+            th[2 * t] = h->p.th_coeff * std::cos(ph);
+            th[2 * t + 1] = h->p.th_coeff * std::sin(ph);
+        }
+        if (!h->th) CK(h, cudaMalloc(&h->th, (size_t)nt * h->esz));
+        if (h->fp64) {
+            CK(h, up(h->th, th.data(), nt * 16));
+        } else {
+            std::vector<float> thf(th.begin(), th.end());
+            CK(h, up(h->th, thf.data(), nt * 8));
+        }
+    }
     h->tables_ok = true;
     return GS_OK;
 }
@@ -378,6 +400,8 @@ PlasmaArgs<Rl> gsi::plasma_args(gs_handle* h, bool raman, bool raman_scan) {
     pa.ionization_potential = h->p.ionization_potential; pa.ponderomotive = h->p.ponderomotive;
     pa.avalanche_cs = h->p.avalanche_cs; pa.recombination_tau = h->p.recombination_tau;
     pa.raman_scan = raman_scan;
+    pa.gas = h->p.gas;
+    pa.th = (h->p.gas && h->p.th_coeff != 0) ? (const T2*)h->th : nullptr;
     if (raman_scan) {
         const double dt = h->p.tstep, tau = h->p.raman_tau, om = h->p.raman_omega;
         const double M = dt * (1 + om * om * tau * tau) / tau / (om * tau);   // solver_main.cpp:403

@@ -129,6 +129,7 @@ int run_qdht_t(gs_handle* h, const void* X, void* Y) {
 int check_adjoint_supported(gs_handle* h) {
     if (!h->tables_ok) return gsi::fail(h, GS_ERR_STATE, "tables not uploaded");
     if (!h->p.nonlinear) return GS_OK;
+    if (h->p.gas) return gsi::fail(h, GS_ERR_UNSUPPORTED, "adjoint: the gas build is not differentiated");
     const bool raman = h->p.raman_fraction > 0.001 && h->p.n2 != 0;
     if (raman && !gsi::raman_scan_on(h))
         return gsi::fail(h, GS_ERR_UNSUPPORTED, "adjoint: the Raman response needs its oscillator parameters");

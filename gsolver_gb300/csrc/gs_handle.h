@@ -44,6 +44,7 @@ struct gs_handle {
     int qdht_n = 0;
     bool time_qdht = false, ev_pending = false;
     double* dump_dev = nullptr;   // 3 n_r + 2 n_t doubles of reduction output, r weights
+    void* th = nullptr;           // gas build: third-harmonic factors th_coeff exp(j phi_t), [n_t]
     std::string err;
     // adjoint (gs_adjoint.cu)
     double* m1inv = nullptr;                   // 1/m1: the transposed QDHT (FP64 path)

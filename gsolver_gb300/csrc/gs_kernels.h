@@ -39,6 +39,11 @@ template <typename Rl> struct PlasmaArgs {
     // optional record of the stage for the adjoint (fused kernel only): E/N, rho, Q per sample
     typename Vec2<Rl>::T* tape_e;
     Rl *tape_rho, *tape_q;
+    // gas build: single-level PPT ionization with neutral depletion (no avalanche, no
+    // recombination) and, when th is set, the third-harmonic source th[t] E_t^3 added to the
+    // Kerr source (th[t] = (KERR_TH/KERR) exp(j phi_t), natural time order)
+    int gas;
+    const typename Vec2<Rl>::T* th;
 };
 
 // ---- adjoint of one RK4 stage's NL response (gs_nl_vjp.cu), rows that fit one CTA

@@ -146,6 +146,7 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
     const Rl AV = (Rl)a.avalanche_cs, TAU = (Rl)a.recombination_tau;
 
     // phase A: W_t and the avalanche prefactor g_t = AV/(U + P I_t) * I_t (t >= 1)
+    const bool gas = a.gas != 0;
     for (int t = tid; t < N; t += nthr) {
         Rl W = 0, g = 0;
         if (t > 0) {
@@ -153,6 +154,9 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
             Rl I = e.x * e.x + e.y * e.y;
             W = photo_rate<Rl>(I, a.rate, a.err);
             g = AV / (U + Pc * I) * I;
+            if (gas) W = gas_rate_slot<Rl>(t, I, W);
+        } else if (gas) {
+            W = (Rl)-1;   // the recurrence starts from E_0 = 0
         }
         U1[t] = T2{W, g};
     }
@@ -182,7 +186,10 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
         for (int i = 0; i < L; i++) {
             const int nt = nt0 + i;
             const T2 w1 = U1[nt];
-            if (nt > 0) {
+            if (nt > 0 && gas) {
+                ro = gas_step<Rl>(ro, w0.x, w1.x, tstep, ND, &d);
+                if (write) { T2 v = U2[nt]; v.x = ro; U2[nt] = v; }
+            } else if (nt > 0) {
                 const Rl W0 = w0.x, g0 = w0.y, W1 = w1.x, g1 = w1.y;
                 const bool in1 = !(ro < 0 || ro > ND);
                 Rl W01 = (ro > ND) ? (Rl)0 : W0;
@@ -281,7 +288,14 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
         Rl rho = U2[t].x;
         T2 w = U1[t];
         T2 loss = T2{0, 0};
-        if (t < N - 1 && t > 0) {
+        if (gas) {
+            // loss[t] = tl E_t (ionization.cpp:60-81), where sample t is above the threshold
+            if (t < N - 1 && w.x >= 0) {
+                const Rl I0 = e.x * e.x + e.y * e.y;
+                const Rl s = gas_loss_factor<Rl>(w.x, rho, I0, tstep, ND, U, Pc);
+                loss = T2{s * e.x, s * e.y};
+            }
+        } else if (t < N - 1 && t > 0) {
             Rl I0 = e.x * e.x + e.y * e.y;
             Rl W01 = (rho > ND) ? (Rl)0 : w.x;
             // the reference compares the intensity with the log threshold (ionization.cpp:43)
@@ -293,7 +307,15 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
         U1[t] = loss;
         U2[t] = T2{rho * e.x, rho * e.y};
         Rl I = e.x * e.x + e.y * e.y;
-        if (!a.raman_scan) U3[t] = a.raman ? T2{I, (Rl)0} : T2{I * e.x - (Rl)0 * e.y, I * e.y + (Rl)0 * e.x};
+        if (!a.raman_scan) {
+            T2 src = a.raman ? T2{I, (Rl)0} : T2{I * e.x - (Rl)0 * e.y, I * e.y + (Rl)0 * e.x};
+            if (a.th && !a.raman) {   // third harmonic: + th_t E^3 (the Kerr profile, scaled)
+                const T2 h = cmul(a.th[t], cmul(cmul(e, e), e));
+                src.x += h.x;
+                src.y += h.y;
+            }
+            U3[t] = src;
+        }
     }
     if (!a.raman_scan) return;
 
@@ -369,7 +391,13 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
                 z.x += I;
                 const T2 v = cadd(cmul(oma, z), cmul(pw, zN));
                 const Rl Q = omf * I + fRM * v.y;
-                U3[t] = T2{Q * e.x, Q * e.y};
+                T2 src = T2{Q * e.x, Q * e.y};
+                if (a.th) {
+                    const T2 h = cmul(a.th[t], cmul(cmul(e, e), e));
+                    src.x += h.x;
+                    src.y += h.y;
+                }
+                U3[t] = src;
                 pw = cmul(pw, ra);
             }
         }

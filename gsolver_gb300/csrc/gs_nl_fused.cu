@@ -101,20 +101,23 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
     // E /= N and the rates W_t (the first sample is treated as E_0 = 0: W_0 = g_0 = 0)
     // in batches of 8 samples per thread so that the table reads (L2: the carve-out leaves
     // little L1) are in flight together
+    const bool gas = a.gas != 0;
     for (int tb = tid; tb < N; tb += 8 * nthr) {
         int n[8];
-        Rl dl[8];
+        Rl dl[8], Iv[8];
 #pragma unroll
         for (int u = 0; u < 8; u++) {
             const int t = tb + u * nthr;
             n[u] = -1;
             dl[u] = 0;
+            Iv[u] = 0;
             if (t < N) {
                 T2 e = E[pad16(t)];
                 e.x = e.x / rn;
                 e.y = e.y / rn;
                 E[pad16(t)] = e;
-                if (t > 0) n[u] = photo_index<Rl>(e.x * e.x + e.y * e.y, &dl[u], a.err);
+                Iv[u] = e.x * e.x + e.y * e.y;
+                if (t > 0) n[u] = photo_index<Rl>(Iv[u], &dl[u], a.err);
             }
         }
         Rl w0[8], w1[8];
@@ -126,7 +129,10 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
 #pragma unroll
         for (int u = 0; u < 8; u++) {
             const int t = tb + u * nthr;
-            if (t < N) Wb[pad32(t)] = n[u] >= 0 ? photo_rate_from<Rl>(w0[u], w1[u], dl[u]) : (Rl)0;
+            if (t < N) {
+                const Rl W = n[u] >= 0 ? photo_rate_from<Rl>(w0[u], w1[u], dl[u]) : (Rl)0;
+                Wb[pad32(t)] = gas ? gas_rate_slot<Rl>(t, Iv[u], W) : W;
+            }
         }
     }
     __syncthreads();
@@ -143,6 +149,17 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
     // the exact recurrence over this thread's chunk from start value s (rho_{t0-1})
     auto run_chunk = [&](Rl s, Rl* dout) -> Rl {
         Rl ro = s, d = (Rl)1;
+        if (gas) {   // ionization.cpp:45-60, one level
+            Rl W0 = (t0 > 0) ? Wb[pad32(t0 - 1)] : (Rl)-1;
+            for (int i = 0; i < L; i++) {
+                const int t = t0 + i;
+                const Rl W1 = Wb[pad32(t)];
+                if (t > 0) ro = gas_step<Rl>(ro, W0, W1, tstep, ND, &d);
+                W0 = W1;
+            }
+            *dout = d;
+            return ro;
+        }
         Rl W0 = (t0 > 0) ? Wb[pad32(t0 - 1)] : (Rl)0, g0 = (t0 > 0) ? g_of(t0 - 1) : (Rl)0;
         for (int i = 0; i < L; i++) {
             const int t = t0 + i;
@@ -228,21 +245,32 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
         }
         const T2 oma = T2{(Rl)(1.0 - a.aN_re), (Rl)(-a.aN_im)};
         const Rl fRM = (Rl)a.fRM, omf = (Rl)a.one_minus_fR;
+        if (gas && t0 == 0) W0 = (Rl)-1;
         for (int i = 0; i < L; i++) {
             const int t = t0 + i;
             const T2 e = E[pad16(t)];
             const Rl I = e.x * e.x + e.y * e.y;
             const Rl W1 = Wb[pad32(t)];
-            const Rl g1 = (t == 0) ? (Rl)0 : AV / (U + Pc * I) * I;
-            if (t > 0) ro = heun_step<Rl>(ro, W0, g0, W1, g1, tstep, ND, invND, invTAU, &d);
-            W0 = W1;
-            g0 = g1;
-            // loss[t] (ionization.cpp:43): W at (E_t, rho_t), the reference's log-threshold test
             T2 loss = T2{0, 0};
-            if (t > 0 && t < N - 1 && I > (Rl)GS_ION_MIN_LN) {
-                const Rl W01 = (ro > ND) ? (Rl)0 : W1;
-                const Rl sl = -(Rl)0.5 * W01 * (U + Pc * I) / I;
-                loss = T2{sl * e.x, sl * e.y};
+            if (gas) {
+                if (t > 0) ro = gas_step<Rl>(ro, W0, W1, tstep, ND, &d);
+                W0 = W1;
+                // loss[t] = tl E_t (ionization.cpp:60-81), where sample t is above the threshold
+                if (t < N - 1 && W1 >= 0) {
+                    const Rl sl = gas_loss_factor<Rl>(W1, ro, I, tstep, ND, U, Pc);
+                    loss = T2{sl * e.x, sl * e.y};
+                }
+            } else {
+                const Rl g1 = (t == 0) ? (Rl)0 : AV / (U + Pc * I) * I;
+                if (t > 0) ro = heun_step<Rl>(ro, W0, g0, W1, g1, tstep, ND, invND, invTAU, &d);
+                W0 = W1;
+                g0 = g1;
+                // loss[t] (ionization.cpp:43): W at (E_t, rho_t), the reference's log-threshold test
+                if (t > 0 && t < N - 1 && I > (Rl)GS_ION_MIN_LN) {
+                    const Rl W01 = (ro > ND) ? (Rl)0 : W1;
+                    const Rl sl = -(Rl)0.5 * W01 * (U + Pc * I) / I;
+                    loss = T2{sl * e.x, sl * e.y};
+                }
             }
             Rl Q = I;   // Kerr without Raman: |E|^2 E
             if (rscan) {
@@ -252,9 +280,16 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
                 Q = omf * I + fRM * v.y;
                 pw = cmul(pw, ra);
             }
+            T2 src3 = T2{Q * e.x, Q * e.y};
+            if (a.th) {   // third harmonic (propagator.cu:712-720): + th_t E^3, same KERR profile
+                const T2 e2 = cmul(e, e);
+                const T2 h = cmul(a.th[t], cmul(e2, e));
+                src3.x += h.x;
+                src3.y += h.y;
+            }
             a.u1[base + t] = loss;
             a.u2[base + t] = T2{ro * e.x, ro * e.y};
-            a.u3[base + t] = T2{Q * e.x, Q * e.y};
+            a.u3[base + t] = src3;
             if (a.tape_e) {   // what the adjoint of this stage reads back
                 a.tape_e[base + t] = e;
                 a.tape_rho[base + t] = ro;

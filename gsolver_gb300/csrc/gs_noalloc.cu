@@ -86,6 +86,7 @@ extern "C" int gs_plasma_max_noalloc(const gs_params* p, const double* rate_ln_d
     a.raman = 1;
     a.raman_scan = 0;
     a.density_only = 1;
+    a.gas = p->gas;
     a.tstep_scaled = p->tstep * p->ionrate_denom;
     a.neutral_density = p->neutral_density;
     a.rho0 = p->rho0;

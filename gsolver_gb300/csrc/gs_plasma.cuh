@@ -70,6 +70,43 @@ __device__ __forceinline__ Rl heun_step(Rl ro, Rl W0, Rl g0, Rl W1, Rl g1, Rl ts
     return rn;
 }
 
+// One step of the gas build's ionization with one level (ionization.cpp:45-60): taken only
+// where the previous sample is above IONIZATION_MIN_I (W0 >= 0; below it W0 carries -1);
+// k1 = dt W0 (rho_n - rho), k2 = dt W1 (rho_n - rho - k1), each clamped at 0;
+// rho' = min(rho + (k1 + k2)/2, rho_n).  Multiplies *d by d rho'/d rho.
+template <typename Rl>
+__device__ __forceinline__ Rl gas_step(Rl ro, Rl W0, Rl W1, Rl tstep, Rl ND, Rl* d) {
+    if (W0 < 0) return ro;
+    W1 = W1 < 0 ? (Rl)0 : W1;
+    Rl k1 = tstep * W0 * (ND - ro);
+    Rl dk1 = -tstep * W0;
+    if (k1 < 0) { k1 = 0; dk1 = 0; }
+    Rl k2 = tstep * W1 * (ND - ro - k1);
+    Rl dk2 = -tstep * W1 * (1 + dk1);
+    if (k2 < 0) { k2 = 0; dk2 = 0; }
+    Rl rn = ro + (Rl)0.5 * (k1 + k2);
+    Rl dn = 1 + (Rl)0.5 * (dk1 + dk2);
+    if (rn > ND) { rn = ND; dn = 0; }
+    *d *= dn;
+    return rn;
+}
+
+// Gas-build rate slot of a sample: W(I) where the sample is above IONIZATION_MIN_I (and not
+// the first one, which the recurrence takes as E_0 = 0), -1 otherwise.
+template <typename Rl>
+__device__ __forceinline__ Rl gas_rate_slot(int t, Rl I, Rl W) {
+    return (t > 0 && I > (Rl)(1e13 / 1e16)) ? W : (Rl)-1;
+}
+
+// loss factor of the gas build at a sample above the threshold (ionization.cpp:60):
+// -(k1/dt)/2 (U + P I)/I, k1 = dt W (rho_n - rho) clamped at 0
+template <typename Rl>
+__device__ __forceinline__ Rl gas_loss_factor(Rl W, Rl ro, Rl I, Rl tstep, Rl ND, Rl U, Rl Pc) {
+    Rl k1 = tstep * W * (ND - ro);
+    if (k1 < 0) k1 = 0;
+    return -(Rl)0.5 * k1 / tstep * (U + Pc * I) / I;
+}
+
 // ---- derivatives for the adjoint -------------------------------------------------------
 // Per-sample rates of one Heun step and their intensity derivatives: the photoionization
 // rate W (log-linear table: dW/dI = W slope / I) and the avalanche prefactor

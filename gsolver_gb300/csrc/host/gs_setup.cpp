@@ -37,6 +37,8 @@ const double kTol = 0.003304003148325;    // solver.h:63-74
 const double kMinLn = 29.933606208922594;
 const double kIntDenom = 1e16, kFieldDenom = 1e8, kIonDenom = 1e20, kIonDenomLn = 46.0517018;
 const double kLayerW = 0.1, kLayerB = 10.0;
+const double kIonDenomGas = 1e10, kIonDenomGasLn = 23.025850929940457;   // IONIZATION_GAS (solver.h:86-92)
+const double kHartree = 4.359748124303985e-018;                            // SIconstants.h:35
 
 struct Cfg {
     std::vector<std::pair<std::string, std::string>> pairs, over;
@@ -203,6 +205,37 @@ double keldysh_rate_ln(double lnI, double k0, double U, double w0, double vg, do
            alpha * std::floor(x + 1);
 }
 
+// PPT_rate_ln (ionization.cpp:235-294) without the Yudin-Ivanov correction; n_eff is held
+// in single precision as in the reference (`float neff`).
+double ppt_rate_ln(double lnI, double Ui, double Z, int l, double k0, double w0, double vg) {
+    const double phase_v = w0 / k0;
+    const double E = std::exp(lnI / 2) * std::sqrt(2 * kMu0 * phase_v * phase_v / vg);
+    const double m = kMe;
+    const double g = w0 * std::sqrt(2 * m / kE / kE * Ui) / E;
+    const double Ueff = Ui * (1 + 1.0 / 2.0 / g / g);
+    const double nu = Ueff / kHbar / w0;
+    const int nu0 = (int)std::floor(1 + nu);
+    const double alpha = 2 * (std::asinh(g) - g / std::sqrt(1 + g * g));
+    const double beta = 2 * g / std::sqrt(1 + g * g);
+    const double E0 = std::sqrt(2 * Ui / kE * Ui / kE * Ui / kHbar * m / kHbar);
+    const float neff = (float)(Z / std::sqrt(2 * Ui / kHartree));
+    double Q = 0;
+    if (g > 0.1) {
+        const int sumN = (int)std::ceil(10 / alpha);
+        for (int k = 0; k < sumN; k++) {
+            const double x = k + nu0 - nu;
+            Q += std::exp(-alpha * x) * dawson(std::sqrt(beta * x));
+        }
+    } else {
+        Q = std::sqrt(3 * M_PI) / 4 / g / g;
+    }
+    const double Cnl2 = std::pow(2.0, 2.0 * neff) / (neff * std::tgamma(2 * neff));
+    double lnW = std::log(4 * std::sqrt(2.0) / M_PI * Cnl2) + std::log(2 * E0 / E / std::sqrt(1 + g * g)) * (2 * neff - 1.5);
+    lnW += -2 * nu * (std::asinh(g) - g * std::sqrt(1 + g * g) / (1 + 2 * g * g));
+    lnW += std::log((2 * l + 1) * Ui / kHbar * g * g / (1 + g * g) * Q);
+    return lnW;
+}
+
 struct RawDisp {
     std::vector<double> w, n;   // n interleaved re, im
 };
@@ -323,7 +356,24 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
     const double fR = cfg.f("RAMAN_FRACTION"), tauR = cfg.f("TAU_RAMAN"), omR = cfg.f("OMEGA_RAMAN");
     const double rho_n = cfg.f("NEUTRAL_DENSITY") * P;
     const double tau_rec = cfg.f("RECOMBINATION_TAU"), tau_c = cfg.f("COLLISION_TAU") / P;
-    const double Ui = cfg.f("IONIZATION_POTENTIAL") * kE;
+    // the binary the reference would run: gsolver_solid_qdht (default) or gsolver_gas_qdht
+    const std::string build_kind = cfg.s("GSOLVER_BUILD", "solid_qdht");
+    if (build_kind != "solid_qdht" && build_kind != "gas_qdht")
+        throw std::string("GSOLVER_BUILD ") + build_kind + ": solid_qdht or gas_qdht";
+    const bool gas = build_kind == "gas_qdht";
+    const double ion_denom = gas ? kIonDenomGas : kIonDenom;
+    double th_coeff = 0;
+    if (gas) {
+        if (cfg.f("NONLIN_REFRINDEX4", 0) != 0) throw std::string("NONLIN_REFRINDEX4 != 0 is not supported");
+        if (cfg.s("TH_PROFILE", "NO") != "NO" || cfg.s("KERR_PROFILE", "NO") != "NO")
+            throw std::string("KERR_PROFILE / TH_PROFILE files are not supported");
+        if ((int)cfg.f("IONIZATION_LEVEL_N", 1) != 1)
+            throw std::string("IONIZATION_LEVEL_N > 1 is not supported on the GPU path");
+        th_coeff = (1 - cfg.f("RAMAN_FRACTION")) / 3.0 * cfg.f("TH_FACTOR", 1);
+    }
+    // load_namednumfloat("IONIZATION_POTENTIAL", 1) for the gas build: NAME1, then NAME
+    const double Ui = (gas && cfg.raw("IONIZATION_POTENTIAL1") ? cfg.f("IONIZATION_POTENTIAL1")
+                                                                : cfg.f("IONIZATION_POTENTIAL")) * kE;
     const double mred = cfg.f("REDUCED_MASS", 1);
     const double m = kMe * mred;
     // QDHT plan
@@ -359,9 +409,17 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
     // entries are independent: spread them over the host's cores (each is computed exactly
     // as it would be alone)
     std::vector<double> rate(8192, 0.0);
-    parallel_for(8191, [&](int i, unsigned) {
-        rate[i] = keldysh_rate_ln(kMinLn + kTol * i, k0r, Ui, w0, vg, mred) - kIonDenomLn;
-    });
+    if (gas) {
+        const double Z = cfg.f("PPT_Z", 1);
+        const int l = (int)cfg.f("PPT_L", 0);
+        parallel_for(8191, [&](int i, unsigned) {
+            rate[i] = ppt_rate_ln(kMinLn + kTol * i, Ui, Z, l, k0r, w0, vg) - kIonDenomGasLn;
+        });
+    } else {
+        parallel_for(8191, [&](int i, unsigned) {
+            rate[i] = keldysh_rate_ln(kMinLn + kTol * i, k0r, Ui, w0, vg, mred) - kIonDenomLn;
+        });
+    }
     // Raman response
     {
         const double M = tstep * (1 + omR * omR * tauR * tauR) / tauR / (omR * tauR);
@@ -455,13 +513,15 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
     p.n_t = nt;
     p.nonlinear = 1;
     p.tstep = tstep; p.tmin = tmin; p.tmax = tmax; p.omega0 = w0;
-    p.ionrate_denom = kIonDenom;
+    p.ionrate_denom = ion_denom;
+    p.gas = gas ? 1 : 0;
+    p.th_coeff = th_coeff;
     p.neutral_density = rho_n;
     p.rho0 = 0.0;   // AMBIENT_CARRIERS*2*frand() with AMBIENT_CARRIERS = 0
-    p.ionization_potential = Ui * (kIonDenom / kIntDenom);
-    p.ponderomotive = pond * kIonDenom;
+    p.ionization_potential = Ui * (ion_denom / kIntDenom);
+    p.ponderomotive = pond * ion_denom;
     p.avalanche_cs = aval;
-    p.recombination_tau = tau_rec * kIonDenom;
+    p.recombination_tau = tau_rec * ion_denom;
     p.raman_fraction = fR;
     p.n2 = n2s;
     p.omega_min = omin;

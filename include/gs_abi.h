@@ -62,7 +62,10 @@ typedef struct gs_params {
     int precision;                /* enum gs_precision */
     int nonlinear;                /* 1: NONLINEARITY_ON; 0: zero NL response (shipped build) */
     int device;                   /* CUDA device ordinal */
-    int reserved0;
+    int gas;                      /* 0: the solid build (gsolver_solid_qdht: Keldysh, avalanche,
+                                     recombination); 1: the gas build (gsolver_gas_qdht,
+                                     Makefile:19: PPT rate table, single-level ionization with
+                                     neutral depletion, third harmonic, IONRATE_DENOM 1e10) */
     double tstep, tmin, tmax, omega0;
     double ionrate_denom;         /* IONRATE_DENOM (1e20 for the solid build) */
     double neutral_density;       /* NEUTRAL_DENSITY */
@@ -78,6 +81,8 @@ typedef struct gs_params {
     double raman_tau, raman_omega; /* TAU_RAMAN, OMEGA_RAMAN: when both > 0 the delayed Kerr
                                       response is computed from this oscillator by an exact
                                       recurrence instead of the RAMAN_FUNCTION FFT pair */
+    double th_coeff;              /* gas build: KERR_TH_PROFILE / KERR_PROFILE = (1 - fR)/3
+                                     TH_FACTOR (process_input.cpp:1020); 0: no third harmonic */
 } gs_params;
 
 /* Per-omega / per-k tables (host pointers, FP64, reference omega order). */

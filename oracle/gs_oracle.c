@@ -195,8 +195,86 @@ static double recombination(const gso_ctx* c, double ro)
     return (ro > 0) ? (ro / c->recombination_tau) : 0;
 }
 
+/* photoionization_functionsN (ionization.cpp:150-199), PPT, no Yudin-Ivanov correction:
+   W[i] = exp(lnW_i(I)) per level, 0 below IONIZATION_MIN_I; the reference's CPU branch
+   throws for n < 0 (an intensity a rounding below the table), its GPU branch returns 0:
+   the GPU behaviour is kept. */
+static void gas_rates(const gso_ctx* c, double I, double* W, int* err)
+{
+    for (int i = 0; i < c->levels; i++) W[i] = 0;
+    if (I < IONIZATION_MIN_I / INTENSITY_DENOM) return;
+    double lnI = log(I) + INTENSITY_DENOM_LN;
+    if (isnan(lnI)) { *err = GSO_ERR_NAN; return; }
+    int n = (int)floor((lnI - IONIZATION_MIN_I_LN) / IONIZATION_I_LN_TOLERANCE);
+    if (n > IONIZATION_N - 2) { *err = GSO_ERR_BLAST; return; }
+    if (n < 0) return;
+    for (int i = 0; i < c->levels; i++) {
+        double lnIn = IONIZATION_MIN_I_LN + n * IONIZATION_I_LN_TOLERANCE;
+        double lnWn = c->rate_ln[IONIZATION_N * i + n];
+        double lnWnp = c->rate_ln[IONIZATION_N * i + n + 1];
+        double lnW = lnWn + (lnI - lnIn) * (lnWnp - lnWn) / IONIZATION_I_LN_TOLERANCE;
+        W[i] = exp(lnW);
+    }
+}
+
+/* calculate_plasmadensity_losses_small, MULTI_LEVEL_IONIZATION branch (ionization.cpp:
+   19-24, 45-84): per level Heun steps on the ion densities (no avalanche, no
+   recombination), taken only where the previous sample's intensity exceeds
+   IONIZATION_MIN_I; pro = sum of the levels; loss[nt-1] = tl E[nt-1]. */
+static int plasma_losses_gas(const gso_ctx* c, const double* field, double* pro, int stride, double* loss)
+{
+    const int N = c->n_t, L = c->levels;
+    const double tstep = c->tstep * c->ionrate_denom, ND = c->neutral_density, Pc = c->ponderomotive;
+    double ro[16] = {0}, W[32];
+    int err = GSO_OK;
+    if (L < 1 || L > 16) return GSO_ERR_ARG;
+    if (loss) { loss[0] = 0; loss[1] = 0; }
+    if (pro) pro[0] = 0;
+    double I0 = 0;
+    for (int nt = 1; nt < N; nt++) {
+        double ph = -c->omega0 * (c->tmin + nt * (c->tmax - c->tmin) / N);
+        double pr = cos(ph), pi = sin(ph);
+        double er = field[2 * nt], ei = field[2 * nt + 1];
+        double reE1 = er * pr - ei * pi, imE1 = er * pi + ei * pr;
+        double I1 = reE1 * reE1 + imE1 * imE1;
+        if (pro) pro[(long)nt * stride] = pro[(long)(nt - 1) * stride];
+        double tl = 0;
+        if (I0 > IONIZATION_MIN_I / INTENSITY_DENOM) {
+            gas_rates(c, I0, W, &err);
+            gas_rates(c, I1, W + L, &err);
+            double k1 = tstep * W[0] * (ND - ro[0]);
+            double k2 = tstep * W[L] * (ND - ro[0] - k1);
+            if (k1 < 0) k1 = 0;
+            if (k2 < 0) k2 = 0;
+            ro[0] += 0.5 * (k1 + k2);
+            if (ro[0] > ND) ro[0] = ND;
+            if (pro) pro[(long)nt * stride] = ro[0];
+            tl = -0.5 * k1 / tstep * (c->potentials[0] + Pc * I0) / I0;
+            for (int n = 1; n < L; n++) {
+                k1 = tstep * W[n] * (ro[n - 1] - ro[n]);
+                k2 = tstep * W[L + n] * (ro[n - 1] - ro[n] - k1);
+                if (k1 < 0) k1 = 0;
+                if (k2 < 0) k2 = 0;
+                ro[n] = ro[n] + 0.5 * (k1 + k2);
+                if (ro[n] > ro[n - 1]) ro[n] = ro[n - 1];
+                if (pro) pro[(long)nt * stride] += ro[n];
+                tl -= 0.5 * k1 / tstep * (c->potentials[n] + Pc * I0) / I0;
+            }
+        }
+        if (loss) {
+            loss[2 * (nt - 1)] = tl * field[2 * (nt - 1)];
+            loss[2 * (nt - 1) + 1] = tl * field[2 * (nt - 1) + 1];
+        }
+        I0 = I1;
+        if (err) return err;
+    }
+    if (loss) { loss[2 * (N - 1)] = 0; loss[2 * (N - 1) + 1] = 0; }
+    return err;
+}
+
 int gso_plasma_losses(const gso_ctx* c, const double* field, double* pro, int stride, double* loss)
 {
+    if (c->gas) return plasma_losses_gas(c, field, pro, stride, loss);
     const int N = c->n_t;
     const double tstep = c->tstep * c->ionrate_denom;
     int err = GSO_OK;
@@ -304,6 +382,26 @@ static int nl_response_ws(const gso_ctx* c, const double* in, double* out, doubl
             double K = c->kerr[w];
             B2[2 * w] += K * B1[2 * w + 1];
             B2[2 * w + 1] += -K * B1[2 * w];
+        }
+        /* THIRD_HARMONICS (propagator.cu:712-720): E^3 exp(j phi_t), phi_t =
+           -2 OMEGA0 (TMIN + nt (TMIN - TMAX)/N_T) (the reference's sign of the step), then
+           += -j KERR_TH_PROFILE FFT(.), KERR_TH_PROFILE = KERR_PROFILE th_coeff */
+        if (c->th_coeff != 0) {
+            for (int nt = 0; nt < N; nt++) {
+                double er = E[2 * nt], ei = E[2 * nt + 1];
+                double e2r = er * er - ei * ei, e2i = 2 * er * ei;
+                double e3r = e2r * er - e2i * ei, e3i = e2r * ei + e2i * er;
+                double ph = -2.0 * c->omega0 * (c->tmin + nt * (c->tmin - c->tmax) / N);
+                double cr = cos(ph), ci = sin(ph);
+                B3[2 * nt] = e3r * cr - e3i * ci;
+                B3[2 * nt + 1] = e3r * ci + e3i * cr;
+            }
+            gso_fft(N, B3, B1, -1);
+            for (int w = 0; w < N; w++) {
+                double K = c->kerr[w] * c->th_coeff;
+                B2[2 * w] += K * B1[2 * w + 1];
+                B2[2 * w + 1] += -K * B1[2 * w];
+            }
         }
     }
     memcpy(out, B2, sizeof(double) * 2 * (size_t)N);

@@ -63,6 +63,17 @@ typedef struct gso_ctx {
 
     /* z-step controller */
     double max_tolerance;
+
+    /* gas build (gsolver_gas_qdht, Makefile:19: PPT_IONIZATION, MULTI_LEVEL_IONIZATION,
+       THIRD_HARMONICS; IONRATE_DENOM 1e10): gas != 0 selects the multi-level ionization of
+       ionization.cpp:45-84 with `levels` rate tables (rate_ln holds levels x 8192) and
+       potentials[levels] (scaled as IONIZATION_POTENTIAL); th_coeff = (1 - fR)/3 TH_FACTOR
+       (KERR_TH_PROFILE = KERR_PROFILE th_coeff, process_input.cpp:1020), 0 = no third
+       harmonic. */
+    int gas;
+    int levels;
+    const double* potentials;
+    double th_coeff;
 } gso_ctx;
 
 /* FFTW-convention unnormalised DFT: sign=-1 FFTW_FORWARD, sign=+1 FFTW_BACKWARD. */

@@ -108,6 +108,7 @@ static int nl_vjp_row(const gso_ctx* c, const double* Y, const double* kbar, dou
 {
     const int N = c->n_t;
     if (!c->nonlinear) { memset(ybar, 0, sizeof(double) * 2 * (size_t)N); return GSO_OK; }
+    if (c->gas || c->th_coeff != 0) return GSO_ERR_ARG;   /* the adjoint covers the solid build */
     double* E = ws;                 /* 2N */
     double* rho = E + 2 * N;        /* N  */
     double* Q = rho + N;            /* N  */

@@ -43,6 +43,7 @@ class _Ctx(C.Structure):
         ("ho_disp", C.c_void_p), ("omega_min", C.c_double), ("omega_max", C.c_double),
         ("kt2", C.c_void_p), ("qdht_c", C.c_void_p), ("qdht_m1", C.c_void_p),
         ("max_tolerance", C.c_double),
+        ("gas", C.c_int), ("levels", C.c_int), ("potentials", C.c_void_p), ("th_coeff", C.c_double),
     ]
 
 
@@ -109,6 +110,12 @@ class Oracle:
             a = np.ascontiguousarray(T[k], dtype=dt)
             self.keep[k] = a
             setattr(c, k, a.ctypes.data)
+        c.gas = int(T.get("gas", 0))
+        c.levels = int(T.get("ion_levels", 1))
+        pot = np.ascontiguousarray(T.get("ion_potentials", [T["ionization_potential"]]), dtype=np.float64)
+        self.keep["ion_potentials"] = pot
+        c.potentials = pot.ctypes.data
+        c.th_coeff = float(T.get("th_coeff", 0.0))
         cm = np.asfortranarray(np.asarray(T["qdht_c"], dtype=np.float64))  # C[i + N*j]
         self.keep["qdht_c"] = cm
         c.qdht_c = cm.ctypes.data

@@ -16,6 +16,7 @@ Reference functions restated (file:line):
   initialize_variables (plasma part)  solver_main.cpp:346-393
   calc_raman_function                 solver_main.cpp:401-413
   calc_ionization_rate/keldysh_rate   ionization.cpp:203-232, 313-355
+  PPT_rate_ln (gas build)             ionization.cpp:235-294
   ellipke, dawson                     extmath.cpp:154-294 (restated by scipy.special)
   qdht_plan::qdht_plan                fhatha.cpp:177-198 (GSL Bessel restated by scipy)
   load_kerr_th_profiles               process_input.cpp:966-975
@@ -94,6 +95,17 @@ class Config:
                 raise KeyError(f"load_namedint: parameter {name} not found")
             return int(default)
         return int(_atof(v))
+
+    def num(self, name, i, default=None):
+        """load_namednumfloat (process_input.cpp:321-343): NAMEi, then NAME."""
+        v = self.raw(f"{name}{i}")
+        if v is None:
+            v = self.raw(name)
+        if v is None:
+            if default is None:
+                raise KeyError(f"load_namednumfloat: parameter {name}{i} not found")
+            return float(default)
+        return _atof(v)
 
     def str(self, name, default=None):
         v = self.raw(name)
@@ -249,6 +261,55 @@ def keldysh_table(k0, U, omega0, vg, reduced_mass):
     return t   # top entry left at 0 (ionization.cpp:324)
 
 
+# the gas build (IONIZATION_GAS, solver.h:32-33, 86-92)
+IONRATE_DENOM_GAS = 1e10
+IONRATE_DENOM_GAS_LN = 23.025850929940457
+HARTREE_ENERGY = 4.359748124303985e-018   # SIconstants.h:35
+
+
+def ppt_rate_ln(lnI, Ui, Z, l, k0, omega0, vg):
+    """PPT_rate_ln (ionization.cpp:235-294) without the Yudin-Ivanov correction; n_eff is
+    held in single precision as in the reference (`float neff`)."""
+    phase_v = omega0 / k0
+    E = math.exp(lnI / 2) * math.sqrt(2 * VACUUM_PERMEABILITY * phase_v * phase_v / vg)
+    m = ELECTRON_MASS
+    g = omega0 * math.sqrt(2 * m / ELECTRON_CHARGE / ELECTRON_CHARGE * Ui) / E
+    Ueff = Ui * (1 + 1.0 / 2.0 / g / g)
+    nu = Ueff / PLANCK_CONSTANT_REDUCED / omega0
+    nu0 = int(math.floor(1 + nu))
+    alpha = 2 * (math.asinh(g) - g / math.sqrt(1 + g * g))
+    beta = 2 * g / math.sqrt(1 + g * g)
+    E0 = math.sqrt(2 * Ui / ELECTRON_CHARGE * Ui / ELECTRON_CHARGE * Ui / PLANCK_CONSTANT_REDUCED * m
+                   / PLANCK_CONSTANT_REDUCED)
+    neff = float(np.float32(Z / math.sqrt(2 * Ui / HARTREE_ENERGY)))
+    if g > 0.1:
+        sumN = int(math.ceil(10 / alpha))
+        k = np.arange(sumN, dtype=np.float64)
+        x = k + nu0 - nu
+        Q = float(np.sum(np.exp(-alpha * x) * sps.dawsn(np.sqrt(beta * x))))
+    else:
+        Q = math.sqrt(3 * math.pi) / 4 / g / g
+    Cnl2 = 2.0 ** (2.0 * neff) / (neff * math.gamma(2 * neff))
+    lnW = math.log(4 * math.sqrt(2.0) / math.pi * Cnl2) + math.log(2 * E0 / E / math.sqrt(1 + g * g)) * (2 * neff - 1.5)
+    lnW += -2 * nu * (math.asinh(g) - g * math.sqrt(1 + g * g) / (1 + 2 * g * g))
+    lnW += math.log((2 * l + 1) * Ui / PLANCK_CONSTANT_REDUCED * g * g / (1 + g * g) * Q)
+    return lnW
+
+
+def ppt_tables(potentials, ppt_z, ppt_l, k0, omega0, vg):
+    """calc_ionization_rate, MULTI_LEVEL_IONIZATION + PPT (ionization.cpp:313-331,
+    ionization.h:26-49): level 0 with PPT_Z, level n >= 1 with Z = n + 1; rows of 8192,
+    the top entry of each left at 0."""
+    L = len(potentials)
+    t = np.zeros((L, IONIZATION_N))
+    for n in range(L):
+        Z = ppt_z if n == 0 else n + 1
+        for i in range(IONIZATION_N - 1):
+            lnI = IONIZATION_MIN_I_LN + IONIZATION_I_LN_TOLERANCE * i
+            t[n, i] = ppt_rate_ln(lnI, potentials[n], Z, ppt_l, k0, omega0, vg) - IONRATE_DENOM_GAS_LN
+    return t
+
+
 def sqrt_ho_coeffs():
     k, b = [], 1.0
     for n in range(1, 21):
@@ -340,7 +401,24 @@ def build(cfg: Config, noise_seed: int | None = None, noise_sigma: float | None 
     kw = wavenum.real
     pf = -(alpha / (1.0 + 1j * alpha) / 2.0 / kw * ELECTRON_CHARGE * ELECTRON_CHARGE / m * VACUUM_PERMEABILITY)
 
-    rate = keldysh_table(k0r, Ui, omega0, vg, red_mass)
+    build_kind = cfg.str("GSOLVER_BUILD", "solid_qdht")
+    gas = build_kind == "gas_qdht"
+    if build_kind not in ("solid_qdht", "gas_qdht"):
+        raise ValueError(f"GSOLVER_BUILD {build_kind}: solid_qdht or gas_qdht")
+    ion_denom = IONRATE_DENOM_GAS if gas else IONRATE_DENOM
+    if gas:
+        if cfg.float("NONLIN_REFRINDEX4", 0) != 0:
+            raise ValueError("NONLIN_REFRINDEX4 != 0 is not supported")
+        if cfg.str("TH_PROFILE", "NO") != "NO" or cfg.str("KERR_PROFILE", "NO") != "NO":
+            raise ValueError("KERR_PROFILE / TH_PROFILE files are not supported")
+        levels = int(cfg.float("IONIZATION_LEVEL_N", 1))
+        pots = [cfg.num("IONIZATION_POTENTIAL", i + 1) * ELECTRON_CHARGE for i in range(levels)]
+        Ui = pots[0]
+        rate = ppt_tables(pots, cfg.float("PPT_Z", 1), cfg.int("PPT_L", 0), k0r, omega0, vg)
+        th_coeff = (1 - fR) / 3.0 * cfg.float("TH_FACTOR", 1)
+    else:
+        levels, pots, th_coeff = 1, [Ui], 0.0
+        rate = keldysh_table(k0r, Ui, omega0, vg, red_mass)
 
     # calc_raman_function
     M = tstep * (1 + omR * omR * tauR * tauR) / tauR / (omR * tauR)
@@ -349,10 +427,11 @@ def build(cfg: Config, noise_seed: int | None = None, noise_sigma: float | None 
     raman = np.fft.fft(h.astype(np.complex128)) + (1 - fR)
 
     # scalings (solver_main.cpp:385-393)
-    Ui_s = Ui * (IONRATE_DENOM / INTENSITY_DENOM)
+    Ui_s = Ui * (ion_denom / INTENSITY_DENOM)
+    pots_s = np.array(pots) * (ion_denom / INTENSITY_DENOM)
     n2_s = n2 * INTENSITY_DENOM
-    tau_rec_s = tau_rec * IONRATE_DENOM
-    pond_s = pond * IONRATE_DENOM
+    tau_rec_s = tau_rec * ion_denom
+    pond_s = pond * ion_denom
 
     kerr = n2_s * omega / LIGHT_VELOCITY / kw * omega / LIGHT_VELOCITY
 
@@ -367,7 +446,8 @@ def build(cfg: Config, noise_seed: int | None = None, noise_sigma: float | None 
         recombination_tau=tau_rec_s, ionization_potential=Ui_s, ponderomotive=pond_s,
         avalanche_cs=aval, plasma_func=pf, rate_ln=rate, raman_func=raman, kerr=kerr,
         qdht_c=Q["C"], qdht_m1=Q["m1"], qdht_x=Q["x"], qdht_V=Q["V"], kt2=kt2,
-        ionrate_denom=IONRATE_DENOM, raman_tau=tauR, raman_omega=omR,
+        ionrate_denom=ion_denom, raman_tau=tauR, raman_omega=omR,
+        gas=1 if gas else 0, ion_levels=levels, ion_potentials=pots_s, th_coeff=th_coeff,
     ))
     T["field"] = create_gg(cfg, T, noise_seed, noise_sigma)
     return T

@@ -1,0 +1,60 @@
+"""The gas build on the GPU against the oracle: single-level PPT ionization with neutral
+depletion and the third harmonic (FP64 1e-10; mixed 2e-5), on the fused path (rows in one
+CTA) and the staged path (FP64 N_T = 16384: radix-2 cross pass + 8192-point rows)."""
+import tempfile
+
+import numpy as np
+import pytest
+
+import gsolver_gb300 as gs
+from gsolver_gb300 import configs
+from oracle import oracle, tables
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+def _argon(n_r=16, n_t=4096, power_cr=6.0, w0=9e-4, seed=2):
+    d = tempfile.mkdtemp(prefix="gs_ggas_")
+    p = configs.argon_c5(d, n_r=n_r, n_t=n_t, build="gas_qdht", power_cr=power_cr, w0=w0, r_max=4 * w0)
+    return tables.build(tables.Config.from_file(p), noise_seed=seed, noise_sigma=1e-4)
+
+
+@pytest.mark.parametrize("n_t", [4096, 16384])
+def test_gas_nl_step_fp64(n_t):
+    T = _argon(n_t=n_t, n_r=8 if n_t > 8192 else 16)
+    O = oracle.Oracle(T)
+    dz = tables.init_zstep_kerr(T, T["field"])
+    bb1, a2, n2 = O.nl_step(T["field"], dz)
+    e = np.fft.ifft(T["field"][0])
+    pro, loss = O.plasma(e)
+    assert pro.max() > 1e-4 * T["neutral_density"] and np.abs(loss).max() > 0   # ionization is on
+    P = gs.Propagator(T, precision=gs.PREC_FP64)
+    P.set_field(T["field"])
+    ga2, gn2 = P.nl_step(dz)
+    assert rel(P.get_nl(), bb1) < 1e-10
+    assert abs(gn2 - n2) <= 1e-10 * n2
+
+
+def test_gas_propagator_steps_fp64_and_mixed():
+    T = _argon(n_r=128, n_t=4096)
+    O = oracle.Oracle(T)
+    dz0 = tables.init_zstep_kerr(T, T["field"])
+    out, st = O.run(T["field"], dz0, steps=3)
+    P = gs.Propagator(T, precision=gs.PREC_FP64)
+    P.set_field(T["field"])
+    cz, zstep, step_n, calls = P.run(T["znet"], dz0, steps=3)
+    assert step_n == st["step_n"] and abs(zstep - st["zstep"]) <= 1e-10 * st["zstep"]
+    f = P.get_field(want_spec=False)
+    assert rel(f, st["field"]) < 1e-10
+    d_g, d_r = O.dumps(f), O.dumps(st["field"])
+    assert rel(d_g["pm"], d_r["pm"]) < 1e-10          # plasma_max through the gas recurrence
+    g = P.dumps(T["qdht_x"], T["r_max"])
+    assert rel(g["pm"], d_r["pm"]) < 1e-10            # the device reduction
+    Pm = gs.Propagator(T, precision=gs.PREC_MIXED)
+    Pm.set_field(T["field"])
+    Pm.run(T["znet"], dz0, steps=3)
+    assert rel(Pm.get_field(want_spec=False), st["field"]) < 2e-5
