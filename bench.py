@@ -16,6 +16,7 @@ Synthetic: the pulse is generated (seeded 1e-4 complex Gaussian noise), no datas
   adjoint the gradient workload (256 x 4096, 1000 steps): forward vs forward+adjoint time
           and the gradient's accuracy (see adjoint_leg)
   batch   64 pulses with uneven grids, one CUDA graph launch per z-step (see batch_leg)
+  argon   16 argon pulses on the gas build (PPT, third harmonic), 512 x 32768 (see argon_leg)
   cpu_baseline  the CPU oracle (a port of the reference algorithm) on a bounded sample
 
 Multi-GPU: replicas only (one independent pulse per rank), value = total / max time.
@@ -50,13 +51,16 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c2r256"])
-    ap.add_argument("--only", default=None, choices=["adjoint", "batch"],
+    ap.add_argument("--only", default=None, choices=["adjoint", "batch", "argon"],
                     help="run one leg alone and print its JSON object (profiling captures)")
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-batch", action="store_true")
+    ap.add_argument("--no-argon", action="store_true")
+    ap.add_argument("--argon-pulses", type=int, default=16)
+    ap.add_argument("--argon-steps", type=int, default=5)
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--batch-pulses", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=10)
@@ -289,6 +293,60 @@ def batch_leg(args, lrank):
     return out
 
 
+def argon_leg(args, lrank):
+    """The gas workload: 16 argon pulses (gas build: PPT ionization, third harmonic) at
+    512 x 32768, 3.9 um 80 fs w0 = 1 mm 4 P_cr, CEP swept over [0, 2 pi), mixed precision,
+    one CUDA graph launch per z-step with each pulse's first controller step as its fixed
+    dz; and the mixed path's field error against the FP64 path on one pulse after 3 steps."""
+    import torch
+    import gsolver_gb300 as gs
+    from gsolver_gb300 import configs
+    d = tempfile.mkdtemp(prefix="gs_bench_ar_")
+    n = args.argon_pulses
+    t0 = time.perf_counter()
+    S = []
+    for i in range(n):
+        p = configs.argon_c5(d, cep=2 * np.pi * i / n, name=f"argon_c5_{i:02d}", build="gas_qdht")
+        S.append(gs.Setup(p, noise_seed=200 + i, noise_sigma=1e-4).as_dict())
+    t_setup = time.perf_counter() - t0
+    P = [gs.Propagator(s, precision=gs.PREC_MIXED, device=lrank) for s in S]
+    for s, p in zip(S, P):
+        p.set_field(s["field"])
+    B = gs.Batch(P)
+    dz = np.array([float(s["init_zstep"]) for s in S])
+    pts = sum(s["n_r"] * s["n_t"] for s in S)
+    stream = torch.cuda.ExternalStream(B.stream_ptr(), device=lrank)
+    B.step(dz, 2, graph=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    B.step(dz, args.argon_steps, graph=True)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    out = {"workload": f"argon_gas_batch{n}", "build": "gas_qdht (PPT, third harmonic, IONRATE_DENOM 1e10)",
+           "pulses": n, "n_r": 512, "n_t": 32768, "points_per_zstep": pts, "precision": "mixed",
+           "dz_m": float(dz[0]), "host_setup_s": t_setup, "value": pts * args.argon_steps / (ms / 1e3),
+           "unit": UNIT, "ms_per_zstep": ms / args.argon_steps, "steps": args.argon_steps,
+           "path": "staged kernels (rows of 32768 exceed one CTA's shared memory)"}
+    B.close()
+    for p in P:
+        p.close()
+    # mixed vs FP64 on pulse 0, 3 steps of its first dz
+    fields = []
+    for prec in (gs.PREC_MIXED, gs.PREC_FP64):
+        Q = gs.Propagator(S[0], precision=prec, device=lrank)
+        Q.set_field(S[0]["field"])
+        for _ in range(3):
+            Q.nl_step(float(dz[0]))
+            Q.lstep(float(dz[0]))
+        fields.append(Q.get_field(want_spec=False))
+        Q.close()
+    out["mixed_rel_l2_field_err_vs_fp64"] = float(np.linalg.norm(fields[0] - fields[1]) / np.linalg.norm(fields[1]))
+    out["err_steps"] = 3
+    return out
+
+
 def adjoint_leg(args, lrank):
     """The adjoint workload: fused silica 256 x 4096, 2 mm in 1000 fixed 2 um steps, seeded
     degree-6 spectral phase on the input, J = energy in the 500-600 nm band (average_spectrum
@@ -360,7 +418,7 @@ def main():
     import gsolver_gb300 as gs
     if args.only:
         torch.cuda.set_device(lrank)
-        leg = adjoint_leg(args, lrank) if args.only == "adjoint" else batch_leg(args, lrank)
+        leg = {"adjoint": adjoint_leg, "batch": batch_leg, "argon": argon_leg}[args.only](args, lrank)
         if rank == 0:
             print(json.dumps({args.only: leg}), flush=True)
         return
@@ -479,6 +537,8 @@ def main():
         line["adjoint"] = adjoint_leg(args, lrank)
     if prec == gs.PREC_MIXED and not args.no_batch and args.workload == "c2":
         line["batch"] = batch_leg(args, lrank)
+    if prec == gs.PREC_MIXED and not args.no_argon and args.workload == "c2":
+        line["argon"] = argon_leg(args, lrank)
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, desc, cores = cpu_sample(cpu_prepare(cfg))
