@@ -196,14 +196,15 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
                 Rl av = in1 ? g0 * ro * (1 - ro * invND) : (Rl)0;
                 Rl rc = (ro > 0) ? ro * invTAU : (Rl)0;
                 Rl k1 = tstep * (W01 + av - rc);
-                Rl dk1 = tstep * ((in1 ? g0 * (1 - 2 * ro * invND) : (Rl)0) - ((ro > 0) ? invTAU : (Rl)0));
+                // Newton derivative: one-sided slope from above at rho = 0 (values unchanged)
+                Rl dk1 = tstep * ((in1 ? g0 * (1 - 2 * ro * invND) : (Rl)0) - ((ro >= 0) ? invTAU : (Rl)0));
                 Rl r2 = ro + k1;
                 const bool in2 = !(r2 < 0 || r2 > ND);
                 Rl W11 = (r2 > ND) ? (Rl)0 : W1;
                 av = in2 ? g1 * r2 * (1 - r2 * invND) : (Rl)0;
                 rc = (r2 > 0) ? r2 * invTAU : (Rl)0;
                 Rl k2 = tstep * (W11 + av - rc);
-                Rl dk2 = tstep * ((in2 ? g1 * (1 - 2 * r2 * invND) : (Rl)0) - ((r2 > 0) ? invTAU : (Rl)0)) * (1 + dk1);
+                Rl dk2 = tstep * ((in2 ? g1 * (1 - 2 * r2 * invND) : (Rl)0) - ((r2 >= 0) ? invTAU : (Rl)0)) * (1 + dk1);
                 ro += (Rl)0.5 * (k1 + k2);
                 d *= 1 + (Rl)0.5 * (dk1 + dk2);
                 if (ro > ND) { ro = ND; d = 0; }
@@ -219,7 +220,9 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
     if (c < P) s_start[c] = (c == 0) ? (Rl)a.rho0 : (Rl)0;
     if (tid == 0) s_done = 0;
     __syncthreads();
-    const Rl tol = sizeof(Rl) == 8 ? (Rl)1e-13 : (Rl)1e-6;   // far below the parity bars (1e-10 / 1e-5)
+    // stop when the starts move less than tol (relative): Newton converges quadratically, so
+    // the starts then carry ~tol^2 + rounding; far below the parity bars (1e-10 / 1e-5)
+    const Rl tol = sizeof(Rl) == 8 ? (Rl)1e-13 : (Rl)1e-5;
     for (int it = 0; it < 16; it++) {
         Rl A = 1, B = 0, sc = 0;
         if (c < P) {

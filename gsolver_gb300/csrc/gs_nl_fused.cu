@@ -176,7 +176,9 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
     s_start[c] = (c == 0) ? (Rl)a.rho0 : (Rl)0;
     if (tid == 0) *flag = 0;
     __syncthreads();
-    const Rl tol = sizeof(Rl) == 8 ? (Rl)1e-13 : (Rl)1e-6;
+    // relative change of the starts at which Newton stops (quadratic convergence: the
+    // starts then carry ~tol^2 + rounding)
+    const Rl tol = sizeof(Rl) == 8 ? (Rl)1e-13 : (Rl)1e-5;
     for (int it = 0; it < 16; it++) {
         const Rl sc = s_start[c];
         Rl D;

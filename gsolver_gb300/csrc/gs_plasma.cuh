@@ -55,14 +55,17 @@ __device__ __forceinline__ Rl heun_step(Rl ro, Rl W0, Rl g0, Rl W1, Rl g1, Rl ts
     Rl av = in1 ? g0 * ro * (1 - ro * invND) : (Rl)0;
     Rl rc = (ro > 0) ? ro * invTAU : (Rl)0;
     const Rl k1 = tstep * (W01 + av - rc);
-    const Rl dk1 = tstep * ((in1 ? g0 * (1 - 2 * ro * invND) : (Rl)0) - ((ro > 0) ? invTAU : (Rl)0));
+    // derivatives for Newton's method only: at rho = 0 exactly the recombination term's
+    // one-sided slope from above (rho >= 0 on every trajectory; the values are continuous
+    // there, so nothing computed changes)
+    const Rl dk1 = tstep * ((in1 ? g0 * (1 - 2 * ro * invND) : (Rl)0) - ((ro >= 0) ? invTAU : (Rl)0));
     const Rl r2 = ro + k1;
     const bool in2 = !(r2 < 0 || r2 > ND);
     const Rl W11 = (r2 > ND) ? (Rl)0 : W1;
     av = in2 ? g1 * r2 * (1 - r2 * invND) : (Rl)0;
     rc = (r2 > 0) ? r2 * invTAU : (Rl)0;
     const Rl k2 = tstep * (W11 + av - rc);
-    const Rl dk2 = tstep * ((in2 ? g1 * (1 - 2 * r2 * invND) : (Rl)0) - ((r2 > 0) ? invTAU : (Rl)0)) * (1 + dk1);
+    const Rl dk2 = tstep * ((in2 ? g1 * (1 - 2 * r2 * invND) : (Rl)0) - ((r2 >= 0) ? invTAU : (Rl)0)) * (1 + dk1);
     Rl rn = ro + (Rl)0.5 * (k1 + k2);
     Rl dn = 1 + (Rl)0.5 * (dk1 + dk2);
     if (rn > ND) { rn = ND; dn = 0; }
