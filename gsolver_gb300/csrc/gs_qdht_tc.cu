@@ -13,7 +13,9 @@
 //   warp 1      MMA issuer: one thread issues tcgen05.mma.kind::tf32 (M=128, N=128, K=8)
 //               x 4 K-steps x 3 terms per stage, accumulator in TMEM (128 columns), and
 //               tcgen05.commit releases the stage.
-//   warps 2-9   B producers: read the X block from global memory (coalesced), apply the
+//               It also streams the raw FP32 X tile (32 rows x 128 columns) by TMA into a
+//               2-deep ring.
+//   warps 2-9   B producers: read the X tile from that ring, apply the
 //               spectral-window mask of the inverse transform, split into TF32 hi/lo and
 //               write them K-major in the 128B-swizzled layout the MMA descriptor reads;
 //               then the epilogue: tcgen05.ld of the accumulator and either a plain store
@@ -34,10 +36,11 @@ namespace gs {
 
 namespace tc {
 
-constexpr int BM = 128, BN = 128, BK = 32, STAGES = 3;
+constexpr int BM = 128, BN = 128, BK = 32, STAGES = 3, RAW_STAGES = 2;
 constexpr int TILE_BYTES = BM * BK * 4;                 // 16 KiB: one 128 x 32 FP32 tile
 constexpr int STAGE_BYTES = 4 * TILE_BYTES;             // Ah, Al, Bh, Bl
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int RAW_BYTES = BK * BN * 4;                  // 16 KiB: 32 rows x 128 columns of X
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + RAW_STAGES * RAW_BYTES + 1024 + 256;
 constexpr int THREADS = 320;
 constexpr int NCONV = 256;                              // warps 2..9
 constexpr unsigned long long WAIT_NS = 200ull * 1000 * 1000;   // 200 ms; legitimate waits are < 1 ms
@@ -181,15 +184,19 @@ __device__ __forceinline__ float sqrt_ho_f(float x) {
 }
 
 __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_constant__ CUtensorMap map_hi,
-                                                             const __grid_constant__ CUtensorMap map_lo, TcArgs a) {
+                                                             const __grid_constant__ CUtensorMap map_lo,
+                                                             const __grid_constant__ CUtensorMap map_x, TcArgs a) {
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t* bars = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+    unsigned char* raw = smem + STAGES * STAGE_BYTES;   // [RAW_STAGES] raw X tiles (TMA, unswizzled)
+    uint64_t* bars = (uint64_t*)(raw + RAW_STAGES * RAW_BYTES);
     uint64_t* full_a = bars;                  // [STAGES]  TMA tx
     uint64_t* full_b = bars + STAGES;         // [STAGES]  256 converter arrivals
     uint64_t* empty = bars + 2 * STAGES;      // [STAGES]  MMA commit
     uint64_t* done = bars + 3 * STAGES;       // accumulator ready
-    uint32_t* tmem_slot = (uint32_t*)(bars + 3 * STAGES + 1);
+    uint64_t* raw_full = bars + 3 * STAGES + 1;                 // [RAW_STAGES] TMA tx
+    uint64_t* raw_empty = raw_full + RAW_STAGES;                // [RAW_STAGES] 256 converter arrivals
+    uint32_t* tmem_slot = (uint32_t*)(raw_empty + RAW_STAGES);
     volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -205,6 +212,10 @@ __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_consta
             mbar_init(&empty[s], 1);
         }
         mbar_init(done, 1);
+        for (int r = 0; r < RAW_STAGES; r++) {
+            mbar_init(&raw_full[r], 1);
+            mbar_init(&raw_empty[r], NCONV);
+        }
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -222,7 +233,7 @@ __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_consta
     if (warp == 0) {
         // ------------------------------------------------ TMA producer (A = Hh, Hl)
         if (lane == 0) {
-            int issued = 0;
+            int issued = 0, issued_raw = 0;
             for (int kb = 0; kb < nk; kb++) {
                 const int s = kb % STAGES;
                 if (kb >= STAGES && !mbar_wait(&empty[s], ((kb / STAGES) + 1) & 1)) {
@@ -235,11 +246,23 @@ __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_consta
                 mbar_expect_tx(&full_a[s], 2 * TILE_BYTES);
                 tma_load_2d(st, &map_hi, kb * BK, m0, &full_a[s]);
                 tma_load_2d(st + TILE_BYTES, &map_lo, kb * BK, m0, &full_a[s]);
+                const int r = kb % RAW_STAGES;
+                if (kb >= RAW_STAGES && !mbar_wait(&raw_empty[r], ((kb / RAW_STAGES) + 1) & 1)) {
+                    record_stall(a.err, 512u, kb, warp);
+                    *abort_flag = 1;
+                    issued = kb + 1;
+                    break;
+                }
+                mbar_expect_tx(&raw_full[r], RAW_BYTES);
+                tma_load_2d(raw + r * RAW_BYTES, &map_x, c0, kb * BK, &raw_full[r]);
                 issued = kb + 1;
+                issued_raw = kb + 1;
             }
             // drain: every issued TMA load has landed before the CTA may exit
             for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; kb++)
                 if (!mbar_wait(&full_a[kb % STAGES], (kb / STAGES) & 1)) record_stall(a.err, 128u, kb, warp);
+            for (int kb = (issued_raw > RAW_STAGES ? issued_raw - RAW_STAGES : 0); kb < issued_raw; kb++)
+                if (!mbar_wait(&raw_full[kb % RAW_STAGES], (kb / RAW_STAGES) & 1)) record_stall(a.err, 1024u, kb, warp);
         }
         __syncwarp();   // the warp reconverges before any block-wide barrier
     } else if (warp == 1) {
@@ -284,21 +307,25 @@ __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_consta
         const int n = t & (BN - 1), kh = t >> 7;
         const int c = c0 + n;
         const int kmx = (a.mode == QDHT_MASKED) ? a.kmax[c >> 1] : 0x7fffffff;
-        const float* xcol = a.X + c;
-        float xv[16];
-        auto fetch = [&](int kb) {
-            const int j0 = kb * BK + 16 * kh;
-#pragma unroll
-            for (int u = 0; u < 16; u++) {
-                const int j = j0 + u;
-                const float v = __ldg(xcol + (size_t)j * a.ncols);
-                xv[u] = (j > kmx) ? 0.f : v;
-            }
-        };
-        fetch(0);
         const uint32_t rowoff = (uint32_t)((n >> 3) * 1024 + (n & 7) * 128);
         for (int kb = 0; kb < nk; kb++) {
             const int s = kb % STAGES;
+            const int r = kb % RAW_STAGES;
+            // the raw X tile (32 rows j x 128 columns) from the TMA ring: column n, rows 16 kh ..
+            if (!mbar_wait(&raw_full[r], (kb / RAW_STAGES) & 1)) {
+                record_stall(a.err, 2048u, kb, warp);
+                *abort_flag = 1;
+                break;
+            }
+            float xv[16];
+            const float* rt = reinterpret_cast<const float*>(raw + r * RAW_BYTES) + (16 * kh) * BN + n;
+#pragma unroll
+            for (int u = 0; u < 16; u++) {
+                const int j = kb * BK + 16 * kh + u;
+                const float v = rt[u * BN];
+                xv[u] = (j > kmx) ? 0.f : v;
+            }
+            mbar_arrive(&raw_empty[r]);
             if (kb >= STAGES && !mbar_wait(&empty[s], ((kb / STAGES) + 1) & 1)) {
                 record_stall(a.err, 16u, kb, warp);
                 *abort_flag = 1;
@@ -311,7 +338,6 @@ __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_consta
                 hi[u] = tf32_rna(xv[u]);
                 lo[u] = tf32_rna(xv[u] - hi[u]);
             }
-            if (kb + 1 < nk) fetch(kb + 1);
             const uint32_t bh = smem_u32(smem + s * STAGE_BYTES + 2 * TILE_BYTES) + rowoff;
             const uint32_t bl = bh + TILE_BYTES;
 #pragma unroll
@@ -421,6 +447,8 @@ struct QdhtTc {
     unsigned* err = nullptr;
     CUtensorMap map_hi, map_lo;
     bool have_lstep = false;
+    // tensor maps of the X operands seen so far (the handle's few state arrays)
+    std::vector<std::pair<const float*, CUtensorMap>> xmaps;
 };
 
 static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
@@ -567,7 +595,28 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
     a.kmax = q->kmax;
     a.err = q->err;
     const unsigned grid = (unsigned)((q->nr / tc::BM) * (a.ncols / tc::BN));
-    tc::qdht_tc_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, q->st>>>(q->map_hi, q->map_lo, a);
+    const CUtensorMap* mx = nullptr;
+    for (auto& e : q->xmaps)
+        if (e.first == X) mx = &e.second;
+    if (!mx) {
+        // X as [n_r rows][2 n_t floats]; boxes of 32 rows x 128 columns, unswizzled (the
+        // column coordinate c0 is a multiple of 128 floats: 16-byte aligned)
+        CUtensorMap m;
+        cuuint64_t gdim[2] = {(cuuint64_t)(2 * q->nt), (cuuint64_t)q->nr};
+        cuuint64_t gstride[1] = {(cuuint64_t)(2 * q->nt) * 4};
+        cuuint32_t box[2] = {(cuuint32_t)tc::BN, (cuuint32_t)tc::BK};
+        cuuint32_t estr[2] = {1, 1};
+        CUresult r = get_encode()(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)X, gdim, gstride, box, estr,
+                                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) {
+            if (msg) *msg = "cuTensorMapEncodeTiled (X) failed";
+            return cudaErrorInvalidValue;
+        }
+        q->xmaps.emplace_back(X, m);
+        mx = &q->xmaps.back().second;
+    }
+    tc::qdht_tc_kernel<<<grid, tc::THREADS, tc::SMEM_BYTES, q->st>>>(q->map_hi, q->map_lo, *mx, a);
     (*nlaunch)++;
     return cudaGetLastError();
 }
