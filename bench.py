@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
-    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c2r256"])
+    ap.add_argument("--workload", default="c2", choices=["c2", "c1", "c2r256", "c2r512"])
     ap.add_argument("--only", default=None, choices=["adjoint", "batch", "argon"],
                     help="run one leg alone and print its JSON object (profiling captures)")
     ap.add_argument("--fp64-steps", type=int, default=3)
@@ -83,10 +83,11 @@ def make_config(workload):
         return configs.fused_silica_c2(d), {"workload": "fused_silica_1024x16384", "n_r": 1024, "n_t": 16384,
                                              "r_max_m": 1.2e-3, "window_s": 1.6e-12, "z_max_m": 3e-3,
                                              "max_tolerance": 1e-6}
-    if workload == "c2r256":
-        return configs.fused_silica_c2_rows(d, 256), {"workload": "fused_silica_256x16384 (profiling case)",
-                                                      "n_r": 256, "n_t": 16384, "r_max_m": 3e-4,
-                                                      "window_s": 1.6e-12, "z_max_m": 3e-3, "max_tolerance": 1e-6}
+    if workload in ("c2r256", "c2r512"):
+        nr = int(workload[3:])
+        return configs.fused_silica_c2_rows(d, nr), {"workload": f"fused_silica_{nr}x16384 (profiling case)",
+                                                     "n_r": nr, "n_t": 16384, "r_max_m": 1.2e-3 * nr / 1024,
+                                                     "window_s": 1.6e-12, "z_max_m": 3e-3, "max_tolerance": 1e-6}
     return configs.fused_silica_c1(d), {"workload": "fused_silica_256x2048", "n_r": 256, "n_t": 2048,
                                          "r_max_m": 6e-4, "window_s": 4e-13, "z_max_m": 1e-3,
                                          "max_tolerance": 1e3}
@@ -161,8 +162,9 @@ def new_state(S):
 
 
 def read_profile_traffic():
-    """Per-launch DRAM bytes of the mixed QDHT kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "qdht_tc_fused_silica_1024x16384.md")
+    """Per-launch DRAM bytes of the mixed QDHT kernel from the committed ncu summary (a
+    512-row capture scaled to the 1024-row launch by the rows it processes)."""
+    p = os.path.join(ROOT, "profiles", "qdht_tc_fused_silica_512x16384.md")
     try:
         with open(p) as f:
             m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read())
