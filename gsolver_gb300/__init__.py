@@ -39,6 +39,7 @@ ABI_FUNCTIONS = (
     "gs_forward_fixed", "gs_gradient", "gs_adjoint_step",
     "gs_batch_create", "gs_batch_step", "gs_batch_stream", "gs_batch_launch_count", "gs_batch_last_error",
     "gs_batch_destroy", "gs_autotune", "gs_set_nl_threads", "gs_get_nl_threads", "gs_batch_autotune",
+    "gs_set_apertures", "gs_setup_apertures",
 )
 
 
@@ -128,6 +129,8 @@ def load_library(path: str | None = None):
     L.gs_set_nl_threads.argtypes = [V, I]
     L.gs_get_nl_threads.argtypes = [V]
     L.gs_batch_autotune.argtypes = [V, V, PD, PD, C.POINTER(C.c_int)]
+    L.gs_set_apertures.argtypes = [V, I, V, V, V, D]
+    L.gs_setup_apertures.argtypes = [V, C.POINTER(C.c_int), V, V]
     _lib = L
     return L
 
@@ -176,6 +179,8 @@ class Propagator:
         self._keep["qdht_c"] = cm
         t.qdht_c = cm.ctypes.data
         self._check(self.L.gs_upload_tables(self.h, C.byref(t)))
+        if len(setup.get("aperture_z", ())) > 0:   # apertures of the config (propagator.cu:232-261)
+            self.set_apertures(setup["aperture_z"], setup["aperture_r"], setup["qdht_x"], setup["r_max"])
 
     def _check(self, rc):
         if rc:
@@ -268,6 +273,14 @@ class Propagator:
         ms, n = C.c_double(), C.c_int()
         self._check(self.L.gs_qdht_timing(self.h, int(enable), C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    def set_apertures(self, z, r, qdht_x, r_max):
+        """Apertures in the reference's array order (the last entry is applied first); gs_step
+        applies them after accepted steps (gs_set_apertures)."""
+        z = np.ascontiguousarray(z, dtype=np.float64)
+        r = np.ascontiguousarray(r, dtype=np.float64)
+        x = np.ascontiguousarray(qdht_x, dtype=np.float64)
+        self._check(self.L.gs_set_apertures(self.h, len(z), _ptr(z), _ptr(r), _ptr(x), float(r_max)))
 
     def nl_threads(self, threads=None):
         """Read, or set (0: default), the fused kernels' threads per row."""
@@ -405,6 +418,11 @@ class Setup:
         f = np.empty((nr, nt), np.complex128)
         L.gs_setup_field(self.s, f.ctypes.data_as(C.c_void_p))
         d["field"] = f
+        nap = C.c_int()
+        L.gs_setup_apertures(self.s, C.byref(nap), None, None)
+        az, ar = np.empty(nap.value), np.empty(nap.value)
+        L.gs_setup_apertures(self.s, C.byref(nap), _ptr(az), _ptr(ar))
+        d["aperture_z"], d["aperture_r"] = az, ar
         zn = np.empty(nz)
         dz0, rmax = C.c_double(), C.c_double()
         x = np.empty(nr)

@@ -605,10 +605,37 @@ int gs_step(gs_handle* h, double current_z, double znet_cur, double znet_prev, d
             *zstep_inout = zstep;
             rc = lstep(h, zstep);
             if (rc) return rc;
+            // apertures (propagator.cu:232-261), with CURRENT_Z the z before this step
+            if (!h->ap_z.empty() && current_z >= h->ap_z.back()) {
+                const int k0 = h->ap_row0.back();
+                if (k0 < h->nr)
+                    CK(h, cudaMemsetAsync((char*)h->A + (size_t)k0 * h->nt * h->esz, 0,
+                                          (size_t)(h->nr - k0) * h->nt * h->esz, h->st));
+                rc = run_qdht(h, QDHT_PLAIN, h->A, h->S, 0.0);
+                if (rc) return rc;
+                h->ap_z.pop_back();
+                h->ap_row0.pop_back();
+            }
             CK(h, cudaStreamSynchronize(h->st));
             return collect_qdht_time(h);
         }
     }
+}
+
+int gs_set_apertures(gs_handle* h, int n, const double* z, const double* r, const double* qdht_x, double r_max) {
+    if (!h || n < 0 || (n > 0 && (!z || !r || !qdht_x))) return fail(h, GS_ERR_ARG, "gs_set_apertures: bad argument");
+    h->ap_z.assign(z, z + n);
+    h->ap_row0.assign(n, h->nr);
+    for (int i = 0; i < n; i++) {
+        // rows with R = x_n R_MAX > r are zeroed; x_n increases with n
+        int k0 = h->nr;
+        for (int k = 0; k < h->nr; k++)
+            if (qdht_x[k] * r_max > r[i]) { k0 = k; break; }
+        for (int k = k0; k < h->nr; k++)
+            if (!(qdht_x[k] * r_max > r[i])) return fail(h, GS_ERR_ARG, "gs_set_apertures: QDHT points not increasing");
+        h->ap_row0[i] = k0;
+    }
+    return GS_OK;
 }
 
 // ------------------------------------------------------------------ autotuning --

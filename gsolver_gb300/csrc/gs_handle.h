@@ -45,6 +45,8 @@ struct gs_handle {
     bool time_qdht = false, ev_pending = false;
     double* dump_dev = nullptr;   // 3 n_r + 2 n_t doubles of reduction output, r weights
     void* th = nullptr;           // gas build: third-harmonic factors th_coeff exp(j phi_t), [n_t]
+    std::vector<double> ap_z;      // apertures not yet applied, reference order (last applied first)
+    std::vector<int> ap_row0;      // first row outside each aperture's radius
     std::string err;
     // adjoint (gs_adjoint.cu)
     double* m1inv = nullptr;                   // 1/m1: the transposed QDHT (FP64 path)

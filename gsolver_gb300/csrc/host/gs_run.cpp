@@ -141,6 +141,13 @@ extern "C" int gs_run_config(const char* config_path, const char* out_dir, int n
     rc = gs_create(&p, &h);
     if (!rc) rc = gs_upload_tables(h, &t);
     if (!rc) rc = gs_set_field(h, field.data(), nullptr);
+    if (!rc) {
+        int nap = 0;
+        gs_setup_apertures(S, &nap, nullptr, nullptr);
+        std::vector<double> apz(nap), apr(nap);
+        gs_setup_apertures(S, &nap, apz.data(), apr.data());
+        rc = gs_set_apertures(h, nap, apz.data(), apr.data(), x.data(), r_max);
+    }
     if (rc) {
         g_run_err = gs_last_error(h);
         if (h) gs_destroy(h);

@@ -59,6 +59,14 @@ struct Cfg {
         if (!v) throw std::string("load_namedint: parameter ") + k + " not found";
         return std::atoi(v->c_str());
     }
+    // load_namednumfloat (process_input.cpp:321-343): NAMEi, then NAME
+    double num(const char* k, int i) const {
+        const std::string ki = std::string(k) + std::to_string(i);
+        const std::string* v = raw(ki.c_str());
+        if (!v) v = raw(k);
+        if (!v) throw std::string("load_namednumfloat: parameter ") + ki + " not found";
+        return std::atof(v->c_str());
+    }
     std::string s(const char* k, const char* d = nullptr) const {
         const std::string* v = raw(k);
         if (!v) {
@@ -289,6 +297,7 @@ struct gs_setup {
     int nr = 0, nt = 0;
     gs_params p{};
     std::vector<double> rate, pf, rm, kerr, omega, wavenum, ho, kt2, C, m1, x, field, znet;
+    std::vector<double> ap_z, ap_r;   // apertures, the reference's array order (last applied first)
     double r_max = 0, dz0 = 0, group_velocity = 0;
     std::string err;
 };
@@ -349,6 +358,12 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
     std::vector<double> znet(nz);
     const double zs = (zmax - zmin) / (nz - 1);
     for (int i = 0; i < nz; i++) znet[i] = zmin + i * zs;
+    // apertures (process_input.cpp:176-179): entry i holds APERTURE_Z/R number N-1-i
+    const int n_ap = (int)cfg.f("APERTURE_N", 0);
+    for (int i = 0; i < n_ap; i++) {
+        s->ap_z.push_back(cfg.num("APERTURE_Z", n_ap - i - 1));
+        s->ap_r.push_back(cfg.num("APERTURE_R", n_ap - i - 1));
+    }
     const double ambient = cfg.f("AMBIENT_CARRIERS", 0) * cfg.f("NEUTRAL_DENSITY", 0);
     if (ambient != 0)
         throw std::string("AMBIENT_CARRIERS != 0 draws an unseeded random start density per row; not supported");
@@ -573,6 +588,16 @@ int gs_setup_grid(const gs_setup* s, int* n_r, int* n_t, int* n_z) {
     if (n_r) *n_r = s->nr;
     if (n_t) *n_t = s->nt;
     if (n_z) *n_z = (int)s->znet.size();
+    return GS_OK;
+}
+
+int gs_setup_apertures(const gs_setup* s, int* n, double* z, double* r) {
+    if (!s || !n) return GS_ERR_ARG;
+    *n = (int)s->ap_z.size();
+    for (int i = 0; i < *n; i++) {
+        if (z) z[i] = s->ap_z[i];
+        if (r) r[i] = s->ap_r[i];
+    }
     return GS_OK;
 }
 

@@ -235,6 +235,13 @@ size_t gs_noalloc_max_samples(void);
 /* Message of the last failed gs_plasma_max_noalloc call. */
 const char* gs_noalloc_last_error(void);
 
+/* Apertures (propagator.cu:232-261, process_input.cpp:176-179): n entries in the reference's
+ * array order (z[n-1], r[n-1] is the first applied).  gs_step then applies them as
+ * propagator() does: after an accepted step, when current_z (the z before the step) has
+ * reached z[k-1] of the next aperture k, FIELD rows with qdht_x[row] * r_max > r[k-1] are
+ * zeroed, BIGBUFFER2 = QDHT(FIELD), and the aperture is used up.  Calling again resets them. */
+int gs_set_apertures(gs_handle* h, int n, const double* z, const double* r, const double* qdht_x, double r_max);
+
 /* Release all device state. */
 int gs_destroy(gs_handle* h);
 

@@ -33,6 +33,9 @@ int gs_setup_from_config(const char* config_path, int n_overrides, const char* c
 const char* gs_setup_last_error(void);
 int gs_setup_grid(const gs_setup* s, int* n_r, int* n_t, int* n_z);
 /* scalars; the caller sets precision, nonlinear and device before gs_create */
+/* Apertures (process_input.cpp:176-179, propagator.cu:232-261): *n entries in the
+   reference's array order (entry n-1, APERTURE_Z0/R0, is applied first); z, r may be NULL. */
+int gs_setup_apertures(const gs_setup* s, int* n, double* z, double* r);
 int gs_setup_params(const gs_setup* s, gs_params* out);
 /* pointers into memory owned by s (valid until gs_setup_destroy) */
 int gs_setup_tables(const gs_setup* s, gs_tables* out);

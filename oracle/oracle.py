@@ -158,6 +158,21 @@ class Oracle:
         _check(self.L.gso_lstep(self.cp, _p(f), _p(bb1_k), _p(b2), float(dz)))
         return f, b2
 
+    def apply_apertures(self, field, bb2, current_z, state):
+        """The aperture block at the end of an accepted propagator() call (propagator.cu:
+        232-261): with CURRENT_Z still the z before the step, when it has reached the next
+        aperture's z, FIELD rows whose QDHT radius x_n R_MAX exceeds its radius are zeroed,
+        BIGBUFFER2 = QDHT(FIELD), and the aperture is used up.  `state` holds the count left."""
+        zs, rs = self.T.get("aperture_z", []), self.T.get("aperture_r", [])
+        n = state.setdefault("aperture_n", len(zs))
+        if n > 0 and current_z >= zs[n - 1]:
+            R = np.asarray(self.T["qdht_x"]) * self.T["r_max"]
+            field = np.array(field, copy=True)
+            field[R > rs[n - 1]] = 0.0
+            bb2 = self.qdht(field)
+            state["aperture_n"] = n - 1
+        return field, bb2
+
     def propagator(self, field, bb2, zstep, current_z, znet_cur, znet_prev, step_n=0):
         """One propagator() call; returns (field, bb2, zstep, step_n, max_a2, max_nl2)."""
         f = np.array(field, dtype=np.complex128, order="C", copy=True)
@@ -207,6 +222,7 @@ class Oracle:
         cz = float(znet[0]); n_z = 0; step_n = 0; zstep = float(dz0)
         out = {k: [] for k in ("mI", "f", "pm", "fa", "s", "z")}
         calls = 0
+        ap_state = {}
         while True:
             if cz >= znet[n_z]:
                 if n_z % dump_every == 0 or n_z == nz - 1:
@@ -220,6 +236,7 @@ class Oracle:
             if steps is not None and calls >= steps:
                 break
             f, bb2, zstep, step_n, _, _ = self.propagator(f, bb2, zstep, cz, znet[n_z], znet[n_z - 1], step_n)
+            f, bb2 = self.apply_apertures(f, bb2, cz, ap_state)
             step_n += 1
             calls += 1
             cz += zstep

@@ -7,7 +7,7 @@ checker for the product's own C++ set-up and as input to the C oracle.
 
 Reference functions restated (file:line):
   load_named* config lookups          process_input.cpp:297-482
-  load_info                           process_input.cpp:98-182
+  load_info (incl. apertures)         process_input.cpp:98-182
   calculate_omega                     process_input.cpp:569-582
   calculate_wavenumber                process_input.cpp:585-623
   load_refrindex_raw                  process_input.cpp:677-721
@@ -376,6 +376,11 @@ def build(cfg: Config, noise_seed: int | None = None, noise_sigma: float | None 
     znettype = cfg.str("ZNET_TYPE")
     znet = create_net(zmin, zmax, nz, znettype)
     ambient = cfg.float("AMBIENT_CARRIERS", 0) * cfg.float("NEUTRAL_DENSITY", 0)
+    # apertures (process_input.cpp:176-179): entry i holds APERTURE_Z/R number N-1-i, so the
+    # last entry (number 0) is the first one applied
+    n_ap = int(cfg.float("APERTURE_N", 0))
+    ap_z = np.array([cfg.num("APERTURE_Z", n_ap - i - 1) for i in range(n_ap)])
+    ap_r = np.array([cfg.num("APERTURE_R", n_ap - i - 1) for i in range(n_ap)])
 
     # load_nonlindata
     n2 = cfg.float("NONLIN_REFRINDEX", 0) * P
@@ -448,6 +453,7 @@ def build(cfg: Config, noise_seed: int | None = None, noise_sigma: float | None 
         qdht_c=Q["C"], qdht_m1=Q["m1"], qdht_x=Q["x"], qdht_V=Q["V"], kt2=kt2,
         ionrate_denom=ion_denom, raman_tau=tauR, raman_omega=omR,
         gas=1 if gas else 0, ion_levels=levels, ion_potentials=pots_s, th_coeff=th_coeff,
+        aperture_z=ap_z, aperture_r=ap_r,
     ))
     T["field"] = create_gg(cfg, T, noise_seed, noise_sigma)
     return T

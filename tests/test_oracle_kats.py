@@ -81,3 +81,27 @@ def test_linear_diffraction_of_collimated_gaussian():
         w2 = 2 * np.sum(fl * r ** 3) / np.sum(fl * r)   # second moment of the fluence (QDHT grid)
         wz = w0 * math.sqrt(1 + (z / zR) ** 2)
         assert abs(math.sqrt(w2) / wz - 1) < 2e-2
+
+
+def test_aperture_zeroes_rows_once_in_config_order():
+    """propagator.cu:232-261: after the step whose start z reaches an aperture's z, FIELD
+    rows outside its radius are zero and BIGBUFFER2 = QDHT(FIELD); each aperture once, number
+    0 first (process_input.cpp:176-179 reverses the order)."""
+    import tempfile
+    from gsolver_gb300 import configs
+    d = tempfile.mkdtemp(prefix="gs_ap_")
+    p = configs.fused_silica_c1(d)
+    over = {"N_R": "32", "N_T": "256", "N_Z": "11", "APERTURE_N": "2", "APERTURE_Z0": "0", "APERTURE_R0": "1.5e-4",
+            "APERTURE_Z1": "2.5e-4", "APERTURE_R1": "1e-4"}
+    T = tables.build(tables.Config.from_file(p, overrides=over), noise_seed=1, noise_sigma=1e-4)
+    assert list(T["aperture_z"]) == [2.5e-4, 0.0] and list(T["aperture_r"]) == [1e-4, 1.5e-4]
+    O = oracle.Oracle(T, nonlinear=False)
+    R = np.asarray(T["qdht_x"]) * T["r_max"]
+    dz0 = tables.init_zstep_kerr(T, T["field"])
+    out, st = O.run(T["field"], dz0, steps=1)              # the step from z = 0: aperture 0
+    assert np.all(st["field"][R > 1.5e-4] == 0) and np.abs(st["field"][R <= 1.5e-4]).max() > 0
+    assert np.array_equal(st["bb2"], O.qdht(st["field"]))
+    out, st = O.run(T["field"], dz0, steps=2)               # z = 1e-4 < 2.5e-4: no second one yet
+    assert np.abs(st["field"][R > 1.5e-4]).max() > 0
+    out, st = O.run(T["field"], dz0, steps=4)               # the step from z = 3e-4: aperture 1
+    assert np.all(st["field"][R > 1e-4] == 0)
