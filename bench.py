@@ -254,8 +254,12 @@ def batch_leg(args, lrank):
     d = tempfile.mkdtemp(prefix="gs_bench_batch_")
     cfgs = configs.c3_batch(d, seed=0, n=args.batch_pulses)
     t0 = time.perf_counter()
-    S = [gs.Setup(p, noise_seed=100 + i, noise_sigma=1e-4).as_dict() for i, (p, _) in enumerate(cfgs)]
-    t_setup = time.perf_counter() - t0
+    S = [gs.Setup(p, noise_seed=100 + i, noise_sigma=1e-4, device=lrank).as_dict() for i, (p, _) in enumerate(cfgs)]
+    t_setup = time.perf_counter() - t0                  # device set-up (gs_setup_from_config_dev)
+    t0 = time.perf_counter()
+    for i, (p, _) in enumerate(cfgs):
+        gs.Setup(p, noise_seed=100 + i, noise_sigma=1e-4)
+    t_setup_host = time.perf_counter() - t0             # the same on the host, for comparison
     P = [gs.Propagator(s, precision=gs.PREC_MIXED, device=lrank) for s in S]
     for s, p in zip(S, P):
         p.set_field(s["field"])
@@ -272,7 +276,7 @@ def batch_leg(args, lrank):
     stream = torch.cuda.ExternalStream(B.stream_ptr(), device=lrank)
     out = {"workload": f"fused_silica_batch{len(P)}", "pulses": len(P), "points_per_zstep": pts,
            "grids": sorted({(s["n_r"], s["n_t"]) for s in S}), "precision": "mixed", "dz_m": 2e-6,
-           "host_setup_s": t_setup, "autotune": tuned or "off"}
+           "setup_s_device": t_setup, "setup_s_host": t_setup_host, "autotune": tuned or "off"}
     for graph in (True, False):
         B.step(dz, 2, graph=graph)   # warm-up (and graph capture)
         n0 = B.launch_count()
@@ -309,8 +313,8 @@ def argon_leg(args, lrank):
     S = []
     for i in range(n):
         p = configs.argon_c5(d, cep=2 * np.pi * i / n, name=f"argon_c5_{i:02d}", build="gas_qdht")
-        S.append(gs.Setup(p, noise_seed=200 + i, noise_sigma=1e-4).as_dict())
-    t_setup = time.perf_counter() - t0
+        S.append(gs.Setup(p, noise_seed=200 + i, noise_sigma=1e-4, device=lrank).as_dict())
+    t_setup = time.perf_counter() - t0                  # device set-up (gs_setup_from_config_dev)
     P = [gs.Propagator(s, precision=gs.PREC_MIXED, device=lrank) for s in S]
     for s, p in zip(S, P):
         p.set_field(s["field"])
@@ -328,7 +332,7 @@ def argon_leg(args, lrank):
     ms = e0.elapsed_time(e1)
     out = {"workload": f"argon_gas_batch{n}", "build": "gas_qdht (PPT, third harmonic, IONRATE_DENOM 1e10)",
            "pulses": n, "n_r": 512, "n_t": 32768, "points_per_zstep": pts, "precision": "mixed",
-           "dz_m": float(dz[0]), "host_setup_s": t_setup, "value": pts * args.argon_steps / (ms / 1e3),
+           "dz_m": float(dz[0]), "setup_s_device": t_setup, "value": pts * args.argon_steps / (ms / 1e3),
            "unit": UNIT, "ms_per_zstep": ms / args.argon_steps, "steps": args.argon_steps,
            "path": "staged kernels (rows of 32768 exceed one CTA's shared memory)"}
     B.close()

@@ -39,7 +39,7 @@ ABI_FUNCTIONS = (
     "gs_forward_fixed", "gs_gradient", "gs_adjoint_step",
     "gs_batch_create", "gs_batch_step", "gs_batch_stream", "gs_batch_launch_count", "gs_batch_last_error",
     "gs_batch_destroy", "gs_autotune", "gs_set_nl_threads", "gs_get_nl_threads", "gs_batch_autotune",
-    "gs_set_apertures", "gs_setup_apertures",
+    "gs_set_apertures", "gs_setup_apertures", "gs_setup_from_config_dev",
 )
 
 
@@ -362,11 +362,16 @@ class Setup:
     (no oracle involved)."""
 
     def __init__(self, config_path: str, overrides: dict | None = None, noise_seed: int = 0,
-                 noise_sigma: float = 0.0):
+                 noise_sigma: float = 0.0, device: int | None = None):
+        """device: None builds everything on the host (gs_setup_from_config); a GPU ordinal
+        builds the rate table, the QDHT matrix and the start field there
+        (gs_setup_from_config_dev)."""
         L = load_library()
         V = C.c_void_p
         L.gs_setup_from_config.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p),
                                            C.c_ulonglong, C.c_double, C.POINTER(V)]
+        L.gs_setup_from_config_dev.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_char_p), C.POINTER(C.c_char_p),
+                                               C.c_ulonglong, C.c_double, C.c_int, C.POINTER(V)]
         L.gs_setup_last_error.restype = C.c_char_p
         L.gs_setup_grid.argtypes = [V, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]
         L.gs_setup_params.argtypes = [V, C.POINTER(Params)]
@@ -379,8 +384,12 @@ class Setup:
         keys = (C.c_char_p * max(1, len(ov)))(*[k.encode() for k in ov])
         vals = (C.c_char_p * max(1, len(ov)))(*[str(v).encode() for v in ov.values()])
         s = V()
-        rc = L.gs_setup_from_config(config_path.encode(), len(ov), keys, vals, int(noise_seed), float(noise_sigma),
-                                    C.byref(s))
+        if device is None:
+            rc = L.gs_setup_from_config(config_path.encode(), len(ov), keys, vals, int(noise_seed), float(noise_sigma),
+                                        C.byref(s))
+        else:
+            rc = L.gs_setup_from_config_dev(config_path.encode(), len(ov), keys, vals, int(noise_seed),
+                                            float(noise_sigma), int(device), C.byref(s))
         if rc:
             raise GsError(rc, L.gs_setup_last_error().decode())
         self.s = s

@@ -69,6 +69,8 @@ static std::vector<int> fft_position_map(int N, int P, int M, int logM) {
     return perm;
 }
 
+std::vector<int> gsi::position_map(int N, int P, int M, int logM) { return fft_position_map(N, P, M, logM); }
+
 // Exported functions take C linkage from their declarations in gs_abi.h.
 
 const char* gs_status_string(int s) {

@@ -73,6 +73,8 @@ int permute_out(gs_handle* h, const void* src, double* host);
 template <typename Rl> gs::PlasmaArgs<Rl> plasma_args(gs_handle* h, bool raman, bool raman_scan);
 // the Raman recurrence applies (oscillator parameters known, Kerr on)
 bool raman_scan_on(const gs_handle* h);
+// position -> omega index of the device FFT of rows N = P M (M = 2^logM per CTA)
+std::vector<int> position_map(int N, int P, int M, int logM);
 }  // namespace gsi
 
 #define CK(h, expr)                                                    \

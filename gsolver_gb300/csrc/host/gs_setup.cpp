@@ -23,10 +23,17 @@
 #include <vector>
 
 #include "gs_setup.h"
+#include "gs_init.h"
+#include "gs_init_math.h"
 
 namespace {
 
 using cd = std::complex<double>;
+using gsm::dawson;
+using gsm::ellipke;
+using gsm::keldysh_rate_ln;
+using gsm::ppt_rate_ln;
+using gsm::seeded_normal;
 
 const double kC = 299792458.0;            // SIconstants.h
 const double kMu0 = 1.2566370615e-6;
@@ -148,101 +155,9 @@ double bessel_j0_zero(int s) {   // s-th positive zero of J0
     return x;
 }
 
-void ellipke(double m, double* K, double* E) {   // complete integrals, parameter m, by AGM
-    double a = 1, b = std::sqrt(1 - m), c = std::sqrt(m), sum = 0.5 * c * c, p = 0.5;
-    for (int it = 0; it < 60 && c > 1e-17; it++) {
-        const double an = 0.5 * (a + b), bn = std::sqrt(a * b);
-        c = 0.5 * (a - b);
-        p *= 2;
-        sum += p * c * c;
-        a = an;
-        b = bn;
-    }
-    *K = M_PI / (2 * a);
-    *E = *K * (1 - sum);
-}
 
-double dawson(double x) {
-    const double ax = std::fabs(x);
-    double r;
-    if (ax <= 7.0) {
-        // D(x) = exp(-x^2) sum_n x^(2n+1) / (n! (2n+1))
-        const double x2 = ax * ax;
-        double term = ax, sum = ax;
-        for (int n = 1; n < 400; n++) {
-            term *= x2 / n;
-            const double t = term / (2 * n + 1);
-            sum += t;
-            if (t < 1e-18 * sum) break;
-        }
-        r = std::exp(-x2) * sum;
-    } else {
-        // D(x) ~ 1/(2x) sum_k (2k-1)!! / (2x^2)^k
-        const double y = 1.0 / (2 * ax * ax);
-        double term = 1, sum = 1;
-        for (int k = 1; k < 60; k++) {
-            const double nt = term * (2 * k - 1) * y;
-            if (nt > term) break;
-            term = nt;
-            sum += term;
-            if (term < 1e-18 * sum) break;
-        }
-        r = sum / (2 * ax);
-    }
-    return x < 0 ? -r : r;
-}
 
-double keldysh_rate_ln(double lnI, double k0, double U, double w0, double vg, double mred) {
-    const double phase_v = w0 / k0;
-    const double E = std::exp(lnI / 2) * std::sqrt(2 * phase_v / vg * phase_v * kMu0);
-    const double m = kMe * mred;
-    const double kg = w0 * std::sqrt(m / kE / kE * U) / E;
-    const double G = kg * kg / (1 + kg * kg), X = 1 / (1 + kg * kg);
-    double Kg, Eg, Kx, Ex;
-    ellipke(G, &Kg, &Eg);
-    ellipke(X, &Kx, &Ex);
-    const double alpha = M_PI * (Kg - Eg) / Ex, beta = M_PI * M_PI / 4.0 / Kx / Ex;
-    const double x = 2 / M_PI * U / kHbar / w0 * Ex / std::sqrt(G);
-    const double nu = std::floor(x + 1) - x;
-    int sumN = (int)std::ceil(10 / alpha);
-    sumN = std::min(sumN, 1000);
-    double Q = 0;
-    for (int i = 0; i < sumN; i++) Q += std::exp(-i * alpha) * dawson(std::sqrt(beta * (i + 2 * nu)));
-    Q *= std::sqrt(M_PI / 2 / Kx);
-    return std::log(2 * w0 / 9 / M_PI) + 1.5 * std::log(w0 * m / kHbar) - 0.75 * std::log(G) + std::log(Q) -
-           alpha * std::floor(x + 1);
-}
 
-// PPT_rate_ln (ionization.cpp:235-294) without the Yudin-Ivanov correction; n_eff is held
-// in single precision as in the reference (`float neff`).
-double ppt_rate_ln(double lnI, double Ui, double Z, int l, double k0, double w0, double vg) {
-    const double phase_v = w0 / k0;
-    const double E = std::exp(lnI / 2) * std::sqrt(2 * kMu0 * phase_v * phase_v / vg);
-    const double m = kMe;
-    const double g = w0 * std::sqrt(2 * m / kE / kE * Ui) / E;
-    const double Ueff = Ui * (1 + 1.0 / 2.0 / g / g);
-    const double nu = Ueff / kHbar / w0;
-    const int nu0 = (int)std::floor(1 + nu);
-    const double alpha = 2 * (std::asinh(g) - g / std::sqrt(1 + g * g));
-    const double beta = 2 * g / std::sqrt(1 + g * g);
-    const double E0 = std::sqrt(2 * Ui / kE * Ui / kE * Ui / kHbar * m / kHbar);
-    const float neff = (float)(Z / std::sqrt(2 * Ui / kHartree));
-    double Q = 0;
-    if (g > 0.1) {
-        const int sumN = (int)std::ceil(10 / alpha);
-        for (int k = 0; k < sumN; k++) {
-            const double x = k + nu0 - nu;
-            Q += std::exp(-alpha * x) * dawson(std::sqrt(beta * x));
-        }
-    } else {
-        Q = std::sqrt(3 * M_PI) / 4 / g / g;
-    }
-    const double Cnl2 = std::pow(2.0, 2.0 * neff) / (neff * std::tgamma(2 * neff));
-    double lnW = std::log(4 * std::sqrt(2.0) / M_PI * Cnl2) + std::log(2 * E0 / E / std::sqrt(1 + g * g)) * (2 * neff - 1.5);
-    lnW += -2 * nu * (std::asinh(g) - g * std::sqrt(1 + g * g) / (1 + 2 * g * g));
-    lnW += std::log((2 * l + 1) * Ui / kHbar * g * g / (1 + g * g) * Q);
-    return lnW;
-}
 
 struct RawDisp {
     std::vector<double> w, n;   // n interleaved re, im
@@ -279,17 +194,6 @@ cd refr_index(const RawDisp& d, double w, double P) {
     return cd(renc, imnc);
 }
 
-uint64_t splitmix(uint64_t seed, uint64_t j) {
-    uint64_t z = seed + (j + 1) * 0x9E3779B97F4A7C15ull;
-    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
-    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
-    return z ^ (z >> 31);
-}
-double seeded_normal(uint64_t seed, uint64_t k) {
-    const double u1 = ((double)(splitmix(seed, 2 * k) >> 11) + 0.5) * 0x1.0p-53;
-    const double u2 = ((double)(splitmix(seed, 2 * k + 1) >> 11) + 0.5) * 0x1.0p-53;
-    return std::sqrt(-2.0 * std::log(u1)) * std::cos(2.0 * M_PI * u2);
-}
 
 }  // namespace
 
@@ -302,7 +206,10 @@ struct gs_setup {
     std::string err;
 };
 
-static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double sigma) {
+// dev < 0: everything on the host; dev >= 0: the rate table, the QDHT matrix and the start
+// field are built on that GPU (gs_init.cu), the rest on the host
+static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double sigma, int dev) {
+    std::string derr;
     const double lam = cfg.f("LAMBDA_V");
     const double w0 = 2 * M_PI * kC / lam;
     double tmin = cfg.f("T_MIN", NAN);
@@ -397,10 +304,14 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
     const double S = zz[nr], V = S / 2.0 / M_PI;
     std::vector<double> x(nr), m1(nr), Cm((size_t)nr * nr), kt2(nr);
     for (int i = 0; i < nr; i++) m1[i] = std::fabs(::j1(zz[i]));
-    parallel_for(nr, [&](int i, unsigned) {
-        for (int j = 0; j < nr; j++)
-            Cm[(size_t)i + (size_t)nr * j] = 2.0 / S * ::j0(zz[i] * zz[j] / S) / m1[i] / m1[j];
-    });
+    if (dev >= 0) {
+        if (gsi_dev_qdht_matrix(dev, zz.data(), m1.data(), S, nr, Cm.data(), &derr)) throw "device set-up: " + derr;
+    } else {
+        parallel_for(nr, [&](int i, unsigned) {
+            for (int j = 0; j < nr; j++)
+                Cm[(size_t)i + (size_t)nr * j] = 2.0 / S * ::j0(zz[i] * zz[j] / S) / m1[i] / m1[j];
+        });
+    }
     for (int i = 0; i < nr; i++) {
         x[i] = zz[i] / S;
         const double kt = 2 * M_PI * x[i] * V / rmax;
@@ -424,7 +335,11 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
     // entries are independent: spread them over the host's cores (each is computed exactly
     // as it would be alone)
     std::vector<double> rate(8192, 0.0);
-    if (gas) {
+    if (dev >= 0) {
+        if (gsi_dev_rate_table(dev, gas ? 1 : 0, k0r, Ui, w0, vg, mred, cfg.f("PPT_Z", 1), (int)cfg.f("PPT_L", 0),
+                               gas ? kIonDenomGasLn : kIonDenomLn, kMinLn, kTol, rate.data(), &derr))
+            throw "device set-up: " + derr;
+    } else if (gas) {
         const double Z = cfg.f("PPT_Z", 1);
         const int l = (int)cfg.f("PPT_L", 0);
         parallel_for(8191, [&](int i, unsigned) {
@@ -479,6 +394,17 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
     f = cfg.f("WAVEFRONT_RADIUS", f);
     f = cfg.f("WAVEFRONT_RADIUS_DIFFRACTION", f / zR) * zR;
     std::vector<double> field(2 * (size_t)nr * nt);
+    double maxI = 0;
+    if (dev >= 0) {
+        GgDevArgs g{};
+        g.nr = nr; g.nt = nt; g.tmin = tmin; g.tstep = tstep; g.tau = tau; g.sgT = sgT; g.sgR = sgR; g.cep = cep;
+        g.C = C; g.A0 = A0; g.ro = ro; g.rmax = rmax; g.f = f; g.Cw = Cw; g.w0 = w0; g.field_denom = kFieldDenom;
+        g.sigma = sigma; g.seed = seed;
+        std::vector<double> kr(nt);
+        for (int w = 0; w < nt; w++) kr[w] = k[w].real();
+        if (gsi_dev_create_gg(dev, g, x.data(), kr.data(), om.data(), field.data(), &maxI, &derr))
+            throw "device set-up: " + derr;
+    } else {
     const unsigned nw = worker_count(nr);
     std::vector<std::vector<cd>> rows(nw, std::vector<cd>(nt));
     const std::vector<cd> tw_fw = fft_twiddles(nt, -1), tw_bw = fft_twiddles(nt, +1);
@@ -514,8 +440,8 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
         for (int t = 0; t < nt; t++) m = std::max(m, std::norm(row[t] / (double)nt));
         rmaxI[r] = m;
     });
-    double maxI = 0;
     for (int r = 0; r < nr; r++) maxI = std::max(maxI, rmaxI[r]);
+    }
     double dz = znet.size() > 1 ? znet[1] - znet[0] : 0;
     const double kNL = w0 / kC * n2s * maxI;
     if (dz * kNL > tol) dz = tol / kNL;
@@ -555,8 +481,22 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
 
 static std::string g_setup_err;
 
+static int setup_impl(const char* path, int n_over, const char* const* keys, const char* const* vals,
+                      unsigned long long noise_seed, double noise_sigma, int dev, gs_setup** out);
+
 int gs_setup_from_config(const char* path, int n_over, const char* const* keys, const char* const* vals,
                          unsigned long long noise_seed, double noise_sigma, gs_setup** out) {
+    return setup_impl(path, n_over, keys, vals, noise_seed, noise_sigma, -1, out);
+}
+
+int gs_setup_from_config_dev(const char* path, int n_over, const char* const* keys, const char* const* vals,
+                             unsigned long long noise_seed, double noise_sigma, int device, gs_setup** out) {
+    if (device < 0) { g_setup_err = "gs_setup_from_config_dev: device ordinal < 0"; return GS_ERR_ARG; }
+    return setup_impl(path, n_over, keys, vals, noise_seed, noise_sigma, device, out);
+}
+
+static int setup_impl(const char* path, int n_over, const char* const* keys, const char* const* vals,
+                      unsigned long long noise_seed, double noise_sigma, int dev, gs_setup** out) {
     if (!path || !out) return GS_ERR_ARG;
     *out = nullptr;
     FILE* f = std::fopen(path, "r");
@@ -571,7 +511,7 @@ int gs_setup_from_config(const char* path, int n_over, const char* const* keys, 
     cfg.dir = sl == std::string::npos ? "." : dir.substr(0, sl);
     gs_setup* s = new gs_setup();
     try {
-        build(s, cfg, noise_seed, noise_sigma);
+        build(s, cfg, noise_seed, noise_sigma, dev);
     } catch (const std::string& e) {
         g_setup_err = e;
         delete s;

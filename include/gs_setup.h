@@ -30,6 +30,14 @@ typedef struct gs_setup gs_setup;
 int gs_setup_from_config(const char* config_path, int n_overrides, const char* const* keys,
                          const char* const* values, unsigned long long noise_seed, double noise_sigma,
                          gs_setup** out);
+/* The same set-up with its FP64 builds on GPU `device` (no counterpart in the reference, whose
+   initialisation is host code): the ionization-rate table (Keldysh or PPT series), the QDHT
+   matrix C (N_r^2 Bessel J0 values) and create_gg's start field (envelope, seeded noise, an
+   FFT per row) with the maximum intensity of init_zstep_kerr; the per-omega tables stay on
+   the host.  Results agree with gs_setup_from_config to the roundings of the two math
+   libraries (relative 1e-13 or better), so batched scans can skip the host's O(N_r N_T) work. */
+int gs_setup_from_config_dev(const char* path, int n_over, const char* const* keys, const char* const* vals,
+                             unsigned long long noise_seed, double noise_sigma, int device, gs_setup** out);
 const char* gs_setup_last_error(void);
 int gs_setup_grid(const gs_setup* s, int* n_r, int* n_t, int* n_z);
 /* scalars; the caller sets precision, nonlinear and device before gs_create */

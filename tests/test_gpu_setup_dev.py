@@ -1,0 +1,40 @@
+"""Device-side set-up (gs_setup_from_config_dev: rate table, QDHT matrix and start field
+built on the GPU in FP64) against the host set-up and the oracle."""
+import tempfile
+
+import numpy as np
+import pytest
+
+import gsolver_gb300 as gs
+from gsolver_gb300 import configs
+from oracle import tables
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(np.asarray(a) - np.asarray(b)) / np.linalg.norm(np.asarray(b)))
+
+
+@pytest.mark.parametrize("kind", ["silica_c1", "silica_16384", "argon_gas"])
+def test_device_setup_matches_host(kind):
+    d = tempfile.mkdtemp(prefix="gs_dinit_")
+    if kind == "silica_c1":
+        p = configs.fused_silica_c1(d)
+    elif kind == "silica_16384":   # FFT rows longer than one CTA's FP64 row (radix-2 cross pass)
+        p = configs.fused_silica_c2_rows(d, 128)
+    else:
+        p = configs.argon_c5(d, n_r=128, n_t=8192, build="gas_qdht", power_cr=6.0, w0=9e-4, r_max=3.6e-3)
+    H = gs.Setup(p, noise_seed=5, noise_sigma=1e-4).as_dict()
+    D = gs.Setup(p, noise_seed=5, noise_sigma=1e-4, device=0).as_dict()
+    assert rel(D["rate_ln"], H["rate_ln"]) < 1e-13
+    # CUDA's j0 and the host libm's j0 differ by more than a few ulps at the large arguments
+    # z_i z_j / S (relative error near J0's zeros): ~1e-12 here, far below the FP64 bar of 1e-10
+    assert rel(D["qdht_c"], H["qdht_c"]) < 5e-12
+    assert rel(D["field"], H["field"]) < 1e-13
+    assert abs(D["init_zstep"] - H["init_zstep"]) <= 1e-12 * H["init_zstep"]
+    for k in ("omega", "wavenum", "kerr", "plasma_func", "ho_disp", "kt2", "qdht_m1"):
+        assert np.array_equal(D[k], H[k]), k
+    if kind == "silica_c1":   # and the oracle
+        T = tables.build(tables.Config.from_file(p), noise_seed=5, noise_sigma=1e-4)
+        assert rel(D["field"], T["field"]) < 1e-13 and rel(D["rate_ln"], T["rate_ln"]) < 1e-12
