@@ -289,9 +289,12 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
                 src3.x += h.x;
                 src3.y += h.y;
             }
-            a.u1[base + t] = loss;
-            a.u2[base + t] = T2{ro * e.x, ro * e.y};
-            a.u3[base + t] = src3;
+            // source rows in chunk-interleaved order (sample c L + i at i nthr + c): the warp's
+            // stores are coalesced; nl_back undoes the order when it stages the row
+            const size_t q = base + (size_t)i * nthr + c;
+            a.u1[q] = loss;
+            a.u2[q] = T2{ro * e.x, ro * e.y};
+            a.u3[q] = src3;
             if (a.tape_e) {   // what the adjoint of this stage reads back
                 a.tape_e[base + t] = e;
                 a.tape_rho[base + t] = ro;
@@ -318,14 +321,17 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_back_kernel(F
     Rl lmax = 0;
     for (int src = 0; src < (s.kerr_on ? 3 : 2); src++) {
         const T2* in = src == 0 ? s.u1 : (src == 1 ? s.u2 : s.u3);
-        if (N / nthr == 16) {
+        // the rows arrive in nl_front's chunk-interleaved order: position u nthr + c holds
+        // sample c L + u (L = N / nthr; the same launch shape runs both kernels)
+        const int L = N / nthr;
+        if (L == 16) {
             T2 v[16];
 #pragma unroll
             for (int u = 0; u < 16; u++) v[u] = in[base + tid + u * nthr];
 #pragma unroll
-            for (int u = 0; u < 16; u++) buf[pad16(tid + u * nthr)] = v[u];
+            for (int u = 0; u < 16; u++) buf[pad16(tid * 16 + u)] = v[u];
         } else {
-            for (int i = tid; i < N; i += nthr) buf[pad16(i)] = in[base + i];
+            for (int q = tid; q < N; q += nthr) buf[pad16((q % nthr) * L + q / nthr)] = in[base + q];
         }
         __syncthreads();
         smem_fft<-1, Rl>(buf, N, f.logM, tw, 1, tid, nthr);
