@@ -97,7 +97,7 @@ void* gs_stream(const gs_handle* h) { return h ? (void*)h->st : nullptr; }
 static void free_all(gs_handle* h) {
     void* ptrs[] = {h->A, h->S, h->NB, h->KP, h->E, h->U, h->tw, h->pf, h->rm, h->kerr, h->rate,
                     h->omega, h->ho, h->kt2, h->Cm, h->m1, h->wavenum, h->staging, h->perm_dev,
-                    h->err_dev, h->max_dev, h->dump_dev, h->m1inv, h->adj, h->adj_w, h->th};
+                    h->err_dev, h->max_dev, h->dump_dev, h->m1inv, h->adj, h->adj_w, h->th, h->twb};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (h->tc) gs::qdht_tc_destroy(h->tc);
     if (h->tcT) gs::qdht_tc_destroy(h->tcT);
@@ -162,6 +162,33 @@ int gs_create(const gs_params* prm, gs_handle** out) {
         } else {
             std::vector<float> twf(tw.begin(), tw.end());
             e = cudaMemcpy(h->tw, twf.data(), nt * 8, cudaMemcpyHostToDevice);
+        }
+    }
+    // base twiddles of the radix-16 stages: w_N^{q m scale_j}, m = 1, 2, 3, 4, 8, 12
+    if (e == cudaSuccess) {
+        const int nb = tw_base_count(h->logM);
+        std::vector<double> b(2 * (size_t)nb);
+        const int mult[6] = {1, 2, 3, 4, 8, 12};
+        for (int j = 0; j < h->logM / 4; j++) {
+            const int S = h->M >> (4 * j), sub = S / 16;
+            const long long scale = (long long)(h->M / S) * h->P;
+            const int off = tw_base_offset(h->logM, j);
+            for (int k = 0; k < 6; k++)
+                for (int q = 0; q < sub; q++) {
+                    const long long ex = ((long long)q * mult[k] * scale) % nt;
+                    const double a = 2.0 * M_PI * (double)ex / (double)nt;
+                    b[2 * ((size_t)off + (size_t)k * sub + q)] = std::cos(a);
+                    b[2 * ((size_t)off + (size_t)k * sub + q) + 1] = -std::sin(a);
+                }
+        }
+        e = cudaMalloc(&h->twb, (size_t)(nb > 0 ? nb : 1) * h->esz);
+        if (e == cudaSuccess && nb > 0) {
+            if (h->fp64) {
+                e = cudaMemcpy(h->twb, b.data(), (size_t)nb * 16, cudaMemcpyHostToDevice);
+            } else {
+                std::vector<float> bf(b.begin(), b.end());
+                e = cudaMemcpy(h->twb, bf.data(), (size_t)nb * 8, cudaMemcpyHostToDevice);
+            }
         }
     }
     if (e == cudaSuccess) e = h->fp64 ? fft_set_smem<double>(h->M, nt) : fft_set_smem<float>(h->M, nt);
@@ -450,6 +477,7 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
     FftArgs<Rl> fa{};
     fa.N = nt; fa.M = h->M; fa.P = h->P; fa.logM = h->logM;
     fa.tw = (const T2*)h->tw;
+    fa.twb = (const T2*)h->twb;
     fa.max_out = h->max_dev;
     fa.threads = h->nl_threads;
     PlasmaArgs<Rl> pa = plasma_args<Rl>(h, raman, raman_scan);
@@ -726,6 +754,7 @@ static int dump_impl(gs_handle* h, const double* qdht_x, double r_max, double* m
     FftArgs<Rl> f{};
     f.N = nt; f.M = h->M; f.P = h->P; f.logM = h->logM; f.rows = nr;
     f.tw = (const T2*)h->tw; f.tpost = 1;
+    f.twb = (const T2*)h->twb;
     CK(h, launch_fft<Rl>(+1, (const T2*)h->A, (T2*)h->E, f, h->st, &h->launches));
     if (max_I || flux) CK(h, launch_row_intensity<Rl>((const T2*)h->E, nr, nt, h->p.tstep, d_maxI, d_flux, h->st, &h->launches));
     if (plasma_max) {
@@ -788,11 +817,13 @@ int gs_get_time_field(gs_handle* h, double* e_r_t) {
         FftArgs<double> f{};
         f.N = h->nt; f.M = h->M; f.P = h->P; f.logM = h->logM; f.rows = h->nr;
         f.tw = (const double2*)h->tw; f.tpost = 1;
+        f.twb = (const double2*)h->twb;
         e = launch_fft<double>(+1, (const double2*)h->A, h->staging, f, h->st, &h->launches);
     } else {
         FftArgs<float> f{};
         f.N = h->nt; f.M = h->M; f.P = h->P; f.logM = h->logM; f.rows = h->nr;
         f.tw = (const float2*)h->tw; f.tpost = 1;
+        f.twb = (const float2*)h->twb;
         e = launch_fft<float>(+1, (const float2*)h->A, (float2*)h->E, f, h->st, &h->launches);
         if (e == cudaSuccess) {
             // widen to FP64 in natural order (time rows are natural): identity permutation copy

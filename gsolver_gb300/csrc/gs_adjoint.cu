@@ -153,6 +153,7 @@ int stage_vjps(gs_handle* h, const AdjPtrs& P, const GsTape& tp, double dz) {
     v.N = h->nt;
     v.logM = h->logM;
     v.tw = (const T2*)h->tw;
+    v.twb = (const T2*)h->twb;
     v.pf = (const T2*)h->pf;
     v.kerr = (const Rl*)h->kerr;
     v.rate = (const Rl*)h->rate;

@@ -44,6 +44,7 @@ struct gs_handle {
     int qdht_n = 0;
     bool time_qdht = false, ev_pending = false;
     double* dump_dev = nullptr;   // 3 n_r + 2 n_t doubles of reduction output, r weights
+    void* twb = nullptr;          // per-stage base twiddles of the M-point row FFTs (tw_base_offset)
     void* th = nullptr;           // gas build: third-harmonic factors th_coeff exp(j phi_t), [n_t]
     std::vector<double> ap_z;      // apertures not yet applied, reference order (last applied first)
     std::vector<int> ap_row0;      // first row outside each aperture's radius

@@ -99,11 +99,50 @@ __host__ __device__ __forceinline__ int pad32(int i) { return i + (i >> 5); }
 __host__ __device__ __forceinline__ int wb_count(int N) { return (N + N / 32 + 1 + 3) & ~3; }
 
 // Twiddles w(j) = exp(-2 pi i j / N) from two shared tables: w = hi[j >> 6] * lo[j & 63].
+// `base`, when set, is the per-stage base table below (global memory); the radix-16 stages
+// then take their twiddles from it instead of hi * lo.
 template <typename Rl> struct TwTab {
     const C2<Rl>* hi;
     const C2<Rl>* lo;
+    const C2<Rl>* base = nullptr;
     __device__ __forceinline__ C2<Rl> operator()(int j) const { return cmul(hi[j >> 6], lo[j & 63]); }
 };
+
+// Per-stage base twiddles of an M-point FFT (M = 2^logM) on rows of N = M * twstride.
+// Radix-16 stage j works on sub-problems of size S_j = M / 16^j with sub_j = S_j / 16
+// butterfly offsets q and twiddles w_N^{q r scale_j}, r = 1..15, scale_j = (M / S_j) twstride.
+// The table holds, per stage, six rows of sub_j entries: w_N^{q m scale_j} for
+// m = 1, 2, 3, 4, 8, 12 (each rounded once from the double value); every other r is
+// w^{q (r & 3)} w^{q (r & 12)}, one product of two tabulated values.  Rows are indexed by q:
+// a warp's lanes (consecutive q) read consecutive words.
+__host__ __device__ inline int tw_base_offset(int logM, int j) {
+    int off = 0;
+    for (int i = 0; i < j; i++) off += 6 * ((1 << logM) >> (4 * i + 4));
+    return off;
+}
+__host__ __device__ inline int tw_base_count(int logM) { return tw_base_offset(logM, logM / 4); }
+
+// x[r] *= w^{SIGN-sign q r} for r = 1..15 from the stage's base rows (conjugated for the
+// inverse transform, SIGN > 0)
+template <int SIGN, typename Rl>
+__device__ __forceinline__ void apply_tw16(C2<Rl>* x, const C2<Rl>* __restrict__ stb, int sub, int q) {
+    using T2 = C2<Rl>;
+    T2 b[6];
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+        b[k] = __ldg(stb + k * sub + q);
+        if (SIGN > 0) b[k].y = -b[k].y;
+    }
+#pragma unroll
+    for (int l = 1; l < 4; l++) x[l] = cmul(x[l], b[l - 1]);
+#pragma unroll
+    for (int hi = 1; hi < 4; hi++) {
+        const T2 bh = b[2 + hi];
+        x[4 * hi] = cmul(x[4 * hi], bh);
+#pragma unroll
+        for (int l = 1; l < 4; l++) x[4 * hi + l] = cmul(x[4 * hi + l], cmul(bh, b[l - 1]));
+    }
+}
 
 // fill hi[N/64] and lo[64] from the global table tw[j] = exp(-2 pi i j / N)
 template <typename Rl>
@@ -120,7 +159,7 @@ __device__ __forceinline__ void load_twiddles(C2<Rl>* hi, C2<Rl>* lo, const C2<R
 // A sub-row of length M = N/twstride uses w_M^k = w_N^{k twstride}.
 template <int R, int SIGN, typename Rl>
 __device__ __forceinline__ void fft_stage(C2<Rl>* buf, int M, int S, const TwTab<Rl>& tw, int twstride, int tid,
-                                          int nthr) {
+                                          int nthr, const C2<Rl>* stb) {
     using T2 = C2<Rl>;
     const int sub = S / R;
     const int nb = M / R;
@@ -132,13 +171,21 @@ __device__ __forceinline__ void fft_stage(C2<Rl>* buf, int M, int S, const TwTab
 #pragma unroll
         for (int r = 0; r < R; r++) x[r] = buf[pad16(base + sub * r)];
         if (SIGN > 0 && q != 0) {
+            if (R == 16 && stb) {
+                apply_tw16<SIGN, Rl>(x, stb, sub, q);
+            } else {
 #pragma unroll
-            for (int r = 1; r < R; r++) x[r] = cmul(x[r], cconj(tw(q * r * scale)));
+                for (int r = 1; r < R; r++) x[r] = cmul(x[r], cconj(tw(q * r * scale)));
+            }
         }
         RegDFT<R, SIGN, Rl, T2>::run(x);
         if (SIGN < 0 && q != 0) {
+            if (R == 16 && stb) {
+                apply_tw16<SIGN, Rl>(x, stb, sub, q);
+            } else {
 #pragma unroll
-            for (int r = 1; r < R; r++) x[r] = cmul(x[r], tw(q * r * scale));
+                for (int r = 1; r < R; r++) x[r] = cmul(x[r], tw(q * r * scale));
+            }
         }
 #pragma unroll
         for (int r = 0; r < R; r++) buf[pad16(base + sub * r)] = x[r];
@@ -147,12 +194,12 @@ __device__ __forceinline__ void fft_stage(C2<Rl>* buf, int M, int S, const TwTab
 
 template <int SIGN, typename Rl>
 __device__ __forceinline__ void fft_stage_rt(int R, C2<Rl>* buf, int M, int S, const TwTab<Rl>& tw, int twstride,
-                                             int tid, int nthr) {
+                                             int tid, int nthr, const C2<Rl>* stb) {
     switch (R) {
-        case 16: fft_stage<16, SIGN, Rl>(buf, M, S, tw, twstride, tid, nthr); break;
-        case 8: fft_stage<8, SIGN, Rl>(buf, M, S, tw, twstride, tid, nthr); break;
-        case 4: fft_stage<4, SIGN, Rl>(buf, M, S, tw, twstride, tid, nthr); break;
-        case 2: fft_stage<2, SIGN, Rl>(buf, M, S, tw, twstride, tid, nthr); break;
+        case 16: fft_stage<16, SIGN, Rl>(buf, M, S, tw, twstride, tid, nthr, stb); break;
+        case 8: fft_stage<8, SIGN, Rl>(buf, M, S, tw, twstride, tid, nthr, nullptr); break;
+        case 4: fft_stage<4, SIGN, Rl>(buf, M, S, tw, twstride, tid, nthr, nullptr); break;
+        case 2: fft_stage<2, SIGN, Rl>(buf, M, S, tw, twstride, tid, nthr, nullptr); break;
         default: break;
     }
 }
@@ -171,7 +218,8 @@ __device__ void smem_fft(C2<Rl>* buf, int M, int logM, const TwTab<Rl>& tw, int 
         int S = M;
         for (int j = 0; j < J; j++) {
             const int R = fft_stage_radix(logM, j);
-            fft_stage_rt<SIGN, Rl>(R, buf, M, S, tw, twstride, tid, nthr);
+            const C2<Rl>* stb = (tw.base && R == 16) ? tw.base + tw_base_offset(logM, j) : nullptr;
+            fft_stage_rt<SIGN, Rl>(R, buf, M, S, tw, twstride, tid, nthr, stb);
             __syncthreads();
             S /= R;
         }
@@ -181,7 +229,8 @@ __device__ void smem_fft(C2<Rl>* buf, int M, int logM, const TwTab<Rl>& tw, int 
             int S = M;
             for (int i = 0; i < j; i++) S /= fft_stage_radix(logM, i);
             const int R = fft_stage_radix(logM, j);
-            fft_stage_rt<SIGN, Rl>(R, buf, M, S, tw, twstride, tid, nthr);
+            const C2<Rl>* stb = (tw.base && R == 16) ? tw.base + tw_base_offset(logM, j) : nullptr;
+            fft_stage_rt<SIGN, Rl>(R, buf, M, S, tw, twstride, tid, nthr, stb);
             __syncthreads();
         }
     }

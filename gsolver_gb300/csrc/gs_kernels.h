@@ -21,6 +21,7 @@ template <typename Rl> struct FftArgs {
     int tpost;                               // time-side store op (inverse)
     const typename Vec2<Rl>::T* e;           // time-domain field (TPOST_DIVN_MULE)
     int threads;                             // fused kernels: threads per row (0: N/16, capped)
+    const typename Vec2<Rl>::T* twb;         // per-stage base twiddles (tw_base_offset) or null
 };
 
 template <typename Rl> struct PlasmaArgs {
@@ -67,6 +68,7 @@ template <typename Rl> struct VjpArgs {
     double tstep_scaled, neutral_density, ionization_potential, ponderomotive, avalanche_cs, recombination_tau;
     double a_re, a_im, aN_re, aN_im, fRM, one_minus_fR;
     int threads;                          // threads per row (0 or not valid: N/16, capped)
+    const typename Vec2<Rl>::T* twb;      // per-stage base twiddles (tw_base_offset) or null
 };
 template <typename Rl> bool nl_vjp_supported(int N);
 template <typename Rl> cudaError_t nl_vjp_setup(int N);

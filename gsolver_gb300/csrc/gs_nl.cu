@@ -65,7 +65,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) fft_sub_kernel(c
         if ((tid & 31) == 0) atomic_max_nonneg(a.max_out, lmax);
     }
     __syncthreads();
-    const TwTab<Rl> tw{twh, twl};
+    const TwTab<Rl> tw{twh, twl, a.twb};
     smem_fft<SIGN, Rl>(buf, M, a.logM, tw, a.P, tid, nthr);
 
     // ---- store (time-side op only when this kernel finishes an inverse transform)

@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
         if ((tid & 31) == 0) atomic_max_nonneg(f.max_out, (double)lmax);
     }
     __syncthreads();
-    const TwTab<Rl> tw{twh, twl};
+    const TwTab<Rl> tw{twh, twl, f.twb};
     smem_fft<+1, Rl>(E, N, f.logM, tw, 1, tid, nthr);
     const Rl rn = (Rl)N;
     const Rl ND = (Rl)a.neutral_density, tstep = (Rl)a.tstep_scaled;
@@ -316,7 +316,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_back_kernel(F
     T2* twl = twh + N / 64;
     const size_t base = (size_t)blockIdx.x * N;
     load_twiddles<Rl>(twh, twl, f.tw, N, tid, nthr);
-    const TwTab<Rl> tw{twh, twl};
+    const TwTab<Rl> tw{twh, twl, f.twb};
     T2* acc = s.kp;   // the new k doubles as the accumulator of the three spectra
     Rl lmax = 0;
     for (int src = 0; src < (s.kerr_on ? 3 : 2); src++) {

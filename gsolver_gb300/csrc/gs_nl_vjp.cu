@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(512) nl_vjp_kernel(VjpArgs<Rl> v) {
     T2* Eb = v.ebar + base;
     const Rl ks = (Rl)v.kb_scale;
     load_twiddles<Rl>(twh, twl, v.tw, N, tid, nthr);
-    const TwTab<Rl> tw{twh, twl};
+    const TwTab<Rl> tw{twh, twl, v.twb};
     const int L = N / nthr;
 
     // ---- Kerr: q = IFFT(j K kb)
