@@ -444,6 +444,7 @@ PlasmaArgs<Rl> gsi::plasma_args(gs_handle* h, bool raman, bool raman_scan) {
         pa.aN_re = mN * std::cos(om * dt * h->nt);
         pa.aN_im = mN * std::sin(om * dt * h->nt);
     }
+    plasma_consts<Rl>(pa);
     return pa;
 }
 

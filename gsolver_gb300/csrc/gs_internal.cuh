@@ -127,9 +127,10 @@ __host__ __device__ inline int tw_base_count(int logM) { return tw_base_offset(l
 template <int SIGN, typename Rl>
 __device__ __forceinline__ void apply_tw16(C2<Rl>* x, const C2<Rl>* __restrict__ stb, int sub, int q) {
     using T2 = C2<Rl>;
-    T2 b[6];
+    // w^{q}, w^{2q}, w^{3q} are held; w^{4q}, w^{8q}, w^{12q} are read when used (registers)
+    T2 b[3];
 #pragma unroll
-    for (int k = 0; k < 6; k++) {
+    for (int k = 0; k < 3; k++) {
         b[k] = __ldg(stb + k * sub + q);
         if (SIGN > 0) b[k].y = -b[k].y;
     }
@@ -137,7 +138,8 @@ __device__ __forceinline__ void apply_tw16(C2<Rl>* x, const C2<Rl>* __restrict__
     for (int l = 1; l < 4; l++) x[l] = cmul(x[l], b[l - 1]);
 #pragma unroll
     for (int hi = 1; hi < 4; hi++) {
-        const T2 bh = b[2 + hi];
+        T2 bh = __ldg(stb + (2 + hi) * sub + q);
+        if (SIGN > 0) bh.y = -bh.y;
         x[4 * hi] = cmul(x[4 * hi], bh);
 #pragma unroll
         for (int l = 1; l < 4; l++) x[4 * hi + l] = cmul(x[4 * hi + l], cmul(bh, b[l - 1]));
@@ -210,9 +212,90 @@ __host__ __device__ inline int fft_stage_radix(int logM, int j) {
     return (j < logM / 4) ? 16 : (1 << (logM % 4));
 }
 
+// ---- the same transform with the row length fixed at compile time (the long rows).
+// Element r of butterfly (q, block) of a stage sits at pad16(base) + pad16(sub r): exact
+// for every stage here (sub a power of two; sub >= 16, or q < sub with sub | 16, or q = 0 in
+// the last small-radix stage), so no index math is repeated per element: a butterfly
+// computes one shared address and reads and writes at immediate offsets.
+constexpr int ct_radix(int logM, int j) { return (j < logM / 4) ? 16 : (1 << (logM % 4)); }
+constexpr int ct_stages(int logM) { return logM / 4 + ((logM % 4) ? 1 : 0); }
+constexpr int ct_size(int logM, int j) {   // S_j = M / (R_0 ... R_{j-1})
+    int S = 1 << logM;
+    for (int i = 0; i < j; i++) S /= ct_radix(logM, i);
+    return S;
+}
+
+template <int R, int SIGN, typename Rl, int M, int S>
+__device__ __forceinline__ void fft_stage_ct(C2<Rl>* buf, const TwTab<Rl>& tw, int twstride, int tid, int nthr,
+                                             const C2<Rl>* stb) {
+    using T2 = C2<Rl>;
+    constexpr int sub = S / R;
+    constexpr int nb = M / R;
+    for (int b = tid; b < nb; b += nthr) {
+        const int q = b & (sub - 1);
+        T2* p = buf + pad16((b / sub) * S + q);
+        T2 x[R];
+#pragma unroll
+        for (int r = 0; r < R; r++) x[r] = p[pad16(sub * r)];
+        if (SIGN > 0 && q != 0) {
+            if (R == 16 && stb) {
+                apply_tw16<SIGN, Rl>(x, stb, sub, q);
+            } else {
+                const int scale = (M / S) * twstride;
+#pragma unroll
+                for (int r = 1; r < R; r++) x[r] = cmul(x[r], cconj(tw(q * r * scale)));
+            }
+        }
+        RegDFT<R, SIGN, Rl, T2>::run(x);
+        if (SIGN < 0 && q != 0) {
+            if (R == 16 && stb) {
+                apply_tw16<SIGN, Rl>(x, stb, sub, q);
+            } else {
+                const int scale = (M / S) * twstride;
+#pragma unroll
+                for (int r = 1; r < R; r++) x[r] = cmul(x[r], tw(q * r * scale));
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < R; r++) p[pad16(sub * r)] = x[r];
+    }
+}
+
+template <int SIGN, typename Rl, int LOGM, int J>
+__device__ __forceinline__ void fft_stage_ct_j(C2<Rl>* buf, const TwTab<Rl>& tw, int twstride, int tid, int nthr) {
+    constexpr int R = ct_radix(LOGM, J);
+    const C2<Rl>* stb = (R == 16 && tw.base) ? tw.base + tw_base_offset(LOGM, J) : nullptr;
+    fft_stage_ct<R, SIGN, Rl, (1 << LOGM), ct_size(LOGM, J)>(buf, tw, twstride, tid, nthr, stb);
+    __syncthreads();
+}
+
+template <int SIGN, typename Rl, int LOGM>
+__device__ __forceinline__ void smem_fft_ct(C2<Rl>* buf, const TwTab<Rl>& tw, int twstride, int tid, int nthr) {
+    constexpr int NS = ct_stages(LOGM);
+    static_assert(NS >= 1 && NS <= 4, "rows of 2^4 .. 2^16");
+    if constexpr (SIGN < 0) {   // forward: S_0 = M first
+        fft_stage_ct_j<SIGN, Rl, LOGM, 0>(buf, tw, twstride, tid, nthr);
+        if constexpr (NS > 1) fft_stage_ct_j<SIGN, Rl, LOGM, 1>(buf, tw, twstride, tid, nthr);
+        if constexpr (NS > 2) fft_stage_ct_j<SIGN, Rl, LOGM, 2>(buf, tw, twstride, tid, nthr);
+        if constexpr (NS > 3) fft_stage_ct_j<SIGN, Rl, LOGM, 3>(buf, tw, twstride, tid, nthr);
+    } else {                    // inverse: the stages undone in reverse order
+        if constexpr (NS > 3) fft_stage_ct_j<SIGN, Rl, LOGM, 3>(buf, tw, twstride, tid, nthr);
+        if constexpr (NS > 2) fft_stage_ct_j<SIGN, Rl, LOGM, 2>(buf, tw, twstride, tid, nthr);
+        if constexpr (NS > 1) fft_stage_ct_j<SIGN, Rl, LOGM, 1>(buf, tw, twstride, tid, nthr);
+        fft_stage_ct_j<SIGN, Rl, LOGM, 0>(buf, tw, twstride, tid, nthr);
+    }
+}
+
 // Full in-place M-point FFT of a padded shared row (caller syncs before; ends synced).
+// Rows of 4096 .. 16384 points take the compile-time form above.
 template <int SIGN, typename Rl>
 __device__ void smem_fft(C2<Rl>* buf, int M, int logM, const TwTab<Rl>& tw, int twstride, int tid, int nthr) {
+    switch (logM) {
+        case 12: smem_fft_ct<SIGN, Rl, 12>(buf, tw, twstride, tid, nthr); return;
+        case 13: smem_fft_ct<SIGN, Rl, 13>(buf, tw, twstride, tid, nthr); return;
+        case 14: smem_fft_ct<SIGN, Rl, 14>(buf, tw, twstride, tid, nthr); return;
+        default: break;
+    }
     const int J = fft_num_stages(logM);
     if (SIGN < 0) {
         int S = M;

@@ -14,7 +14,7 @@ template <typename Rl> struct FftArgs {
     int N, M, P, logM, rows;                 // rows of length N = P*M
     const typename Vec2<Rl>::T* tw;          // exp(-2 pi i j / N), j < N
     int spre;                                // spectral-side load op (inverse)
-    double cdz;                              // stage coefficient c*dz (SPRE_STAGE)
+    Rl cdz;                                  // stage coefficient c*dz (SPRE_STAGE), row precision
     const typename Vec2<Rl>::T* kp;          // previous RK4 stage (SPRE_STAGE)
     int track_max;                           // max |input|^2 -> max_out
     unsigned long long* max_out;
@@ -45,7 +45,30 @@ template <typename Rl> struct PlasmaArgs {
     // Kerr source (th[t] = (KERR_TH/KERR) exp(j phi_t), natural time order)
     int gas;
     const typename Vec2<Rl>::T* th;
+    // the scalars above in the rows' precision, converted once on the host (plasma_args):
+    // converting a double on the device runs on the FP64 pipe, which is slow on this GPU
+    struct Consts {
+        Rl ND, invND, tstep, U, Pc, AV, invTAU, rho0, a_re, a_im, oma_re, oma_im, fRM, omf;
+    } k;
 };
+
+// fill PlasmaArgs::k from the double fields (host; call after setting them)
+template <typename Rl> inline void plasma_consts(PlasmaArgs<Rl>& pa) {
+    pa.k.ND = (Rl)pa.neutral_density;
+    pa.k.invND = (Rl)1 / pa.k.ND;
+    pa.k.tstep = (Rl)pa.tstep_scaled;
+    pa.k.U = (Rl)pa.ionization_potential;
+    pa.k.Pc = (Rl)pa.ponderomotive;
+    pa.k.AV = (Rl)pa.avalanche_cs;
+    pa.k.invTAU = (Rl)1 / (Rl)pa.recombination_tau;
+    pa.k.rho0 = (Rl)pa.rho0;
+    pa.k.a_re = (Rl)pa.a_re;
+    pa.k.a_im = (Rl)pa.a_im;
+    pa.k.oma_re = (Rl)(1.0 - pa.aN_re);
+    pa.k.oma_im = (Rl)(-pa.aN_im);
+    pa.k.fRM = (Rl)pa.fRM;
+    pa.k.omf = (Rl)pa.one_minus_fR;
+}
 
 // ---- adjoint of one RK4 stage's NL response (gs_nl_vjp.cu), rows that fit one CTA
 template <typename Rl> struct VjpArgs {

@@ -44,14 +44,11 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) fft_sub_kernel(c
     load_twiddles<Rl>(twh, twl, a.tw, a.N, tid, nthr);
 
     // ---- load (with the spectral-side op for inverse transforms)
-    double lmax = 0.0;
+    Rl lmax = 0;
     for (int i = tid; i < M; i += nthr) {
         T2 v = in[base + i];
         if (SIGN > 0 && a.spre == SPRE_STAGE) {
-            if (a.track_max) {
-                double m = (double)v.x * (double)v.x + (double)v.y * (double)v.y;
-                lmax = fmax(lmax, m);
-            }
+            if (a.track_max) lmax = fmax(lmax, v.x * v.x + v.y * v.y);
             if (a.cdz != 0) {
                 T2 k = a.kp[base + i];
                 v.x = v.x + (Rl)a.cdz * k.x;
@@ -62,7 +59,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) fft_sub_kernel(c
     }
     if (SIGN > 0 && a.track_max) {
         for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-        if ((tid & 31) == 0) atomic_max_nonneg(a.max_out, lmax);
+        if ((tid & 31) == 0) atomic_max_nonneg(a.max_out, (double)lmax);
     }
     __syncthreads();
     const TwTab<Rl> tw{twh, twl, a.twb};
@@ -140,10 +137,7 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
     T2* U2 = a.u2 + base;
     T2* U3 = a.u3 + base;
     const int tid = threadIdx.x, nthr = blockDim.x;
-    const Rl ND = (Rl)a.neutral_density;
-    const Rl tstep = (Rl)a.tstep_scaled;
-    const Rl U = (Rl)a.ionization_potential, Pc = (Rl)a.ponderomotive;
-    const Rl AV = (Rl)a.avalanche_cs, TAU = (Rl)a.recombination_tau;
+    const Rl ND = a.k.ND, tstep = a.k.tstep, U = a.k.U, Pc = a.k.Pc, AV = a.k.AV;
 
     // phase A: W_t and the avalanche prefactor g_t = AV/(U + P I_t) * I_t (t >= 1)
     const bool gas = a.gas != 0;
@@ -171,7 +165,7 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
     // starts, i.e. the sequential recurrence up to rounding.
     const int P = min(nthr, N);
     const int L = N / P;
-    const Rl invND = (Rl)1 / ND, invTAU = (Rl)1 / TAU;
+    const Rl invND = a.k.invND, invTAU = a.k.invTAU;
     Rl* s_start = sW;            // [P] chunk start values
     Rl* s_scanA = sG;            // [P] scan scratch
     Rl* s_scanB = sR;            // [P]
@@ -217,7 +211,7 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
         if (dout) *dout = d;
         return ro;
     };
-    if (c < P) s_start[c] = (c == 0) ? (Rl)a.rho0 : (Rl)0;
+    if (c < P) s_start[c] = (c == 0) ? a.k.rho0 : (Rl)0;
     if (tid == 0) s_done = 0;
     __syncthreads();
     // stop when the starts move less than tol (relative): Newton converges quadratically, so
@@ -330,7 +324,7 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
     // and z is a linear recurrence: chunk-local sums, an exclusive scan of chunk starts
     // (complex affine maps with the common multiplier a^L), then a second chunk pass.
     __syncthreads();
-    const T2 ra = T2{(Rl)a.a_re, (Rl)a.a_im};
+    const T2 ra = T2{a.k.a_re, a.k.a_im};
     T2 zl = T2{0, 0};
     T2 aL = T2{1, 0};
     if (c < P) {
@@ -377,15 +371,20 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
         const T2 zs = (c == 0) ? T2{0, 0} : cend[c - 1];
         const T2 zN = zend;
         if (c < P) {
-            const T2 oma = T2{(Rl)(1.0 - a.aN_re), (Rl)(-a.aN_im)};
-            // a^{t+1} at the first sample of the chunk, then advanced by a
-            const double k0 = (double)(c * L + 1);
-            const double mag = exp(-k0 * a.dt_over_tau);
-            double sn, cs;
-            sincos(k0 * a.dt_omega, &sn, &cs);
-            T2 pw = T2{(Rl)(mag * cs), (Rl)(mag * sn)};
+            const T2 oma = T2{a.k.oma_re, a.k.oma_im};
+            // a^{t+1} at the first sample of the chunk, a (a^L)^c by binary powering (the
+            // chunks share a^L), then advanced by a
+            T2 pw = T2{1, 0};
+            {
+                T2 b = aL;
+                for (int e = c; e > 0; e >>= 1) {
+                    if (e & 1) pw = cmul(pw, b);
+                    b = cmul(b, b);
+                }
+                pw = cmul(pw, ra);
+            }
             T2 z = zs;
-            const Rl fRM = (Rl)a.fRM, omf = (Rl)a.one_minus_fR;
+            const Rl fRM = a.k.fRM, omf = a.k.omf;
             for (int i = 0; i < L; i++) {
                 const int t = c * L + i;
                 const T2 e = E[t];
@@ -424,7 +423,7 @@ template <typename Rl>
 __global__ void spec2_kernel(SpecArgs<Rl> a) {
     using T2 = C2<Rl>;
     const size_t total = (size_t)a.rows * a.N;
-    double lmax = 0.0;
+    Rl lmax = 0;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         const int p = (int)(i % a.N);
         T2 k = a.u1[i];
@@ -445,15 +444,14 @@ __global__ void spec2_kernel(SpecArgs<Rl> a) {
         } else {
             T2 o = a.nb[i];
             nb = T2{(o.x + k.x) / (Rl)6, (o.y + k.y) / (Rl)6};
-            double m = (double)nb.x * (double)nb.x + (double)nb.y * (double)nb.y;
-            lmax = fmax(lmax, m);
+            lmax = fmax(lmax, nb.x * nb.x + nb.y * nb.y);
         }
         a.nb[i] = nb;
         if (a.stage < 3) a.kp[i] = k;
     }
     if (a.stage == 3) {
         for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-        if ((threadIdx.x & 31) == 0) atomic_max_nonneg(a.max_out, lmax);
+        if ((threadIdx.x & 31) == 0) atomic_max_nonneg(a.max_out, (double)lmax);
     }
 }
 
@@ -461,14 +459,14 @@ __global__ void spec2_kernel(SpecArgs<Rl> a) {
 template <typename Rl>
 __global__ void zero_nl_kernel(const C2<Rl>* __restrict__ A, C2<Rl>* __restrict__ nb, size_t total,
                                unsigned long long* max_out) {
-    double lmax = 0.0;
+    Rl lmax = 0;
     for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
         C2<Rl> v = A[i];
-        lmax = fmax(lmax, (double)v.x * (double)v.x + (double)v.y * (double)v.y);
+        lmax = fmax(lmax, v.x * v.x + v.y * v.y);
         nb[i] = C2<Rl>{0, 0};
     }
     for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(max_out, lmax);
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg(max_out, (double)lmax);
 }
 
 // natural <-> position order, with precision conversion from / to FP64 staging

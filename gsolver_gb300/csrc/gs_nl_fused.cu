@@ -95,9 +95,8 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
     const TwTab<Rl> tw{twh, twl, f.twb};
     smem_fft<+1, Rl>(E, N, f.logM, tw, 1, tid, nthr);
     const Rl rn = (Rl)N;
-    const Rl ND = (Rl)a.neutral_density, tstep = (Rl)a.tstep_scaled;
-    const Rl U = (Rl)a.ionization_potential, Pc = (Rl)a.ponderomotive, AV = (Rl)a.avalanche_cs;
-    const Rl invND = (Rl)1 / ND, invTAU = (Rl)1 / (Rl)a.recombination_tau;
+    const Rl ND = a.k.ND, tstep = a.k.tstep, U = a.k.U, Pc = a.k.Pc, AV = a.k.AV;
+    const Rl invND = a.k.invND, invTAU = a.k.invTAU;
     // E /= N and the rates W_t (the first sample is treated as E_0 = 0: W_0 = g_0 = 0)
     // in batches of 8 samples per thread so that the table reads (L2: the carve-out leaves
     // little L1) are in flight together
@@ -173,7 +172,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
     };
 
     // ---- carrier density by multiple shooting (Newton on the chunk starts)
-    s_start[c] = (c == 0) ? (Rl)a.rho0 : (Rl)0;
+    s_start[c] = (c == 0) ? a.k.rho0 : (Rl)0;
     if (tid == 0) *flag = 0;
     __syncthreads();
     // relative change of the starts at which Newton stops (quadratic convergence: the
@@ -211,7 +210,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
 
     // ---- Raman: z_t = a z_{t-1} + I_t, chunk sums then an exclusive scan of chunk starts
     const bool rscan = a.raman_scan != 0;
-    const T2 ra = T2{(Rl)a.a_re, (Rl)a.a_im};
+    const T2 ra = T2{a.k.a_re, a.k.a_im};
     T2 zs = T2{0, 0}, zN = T2{0, 0};
     if (rscan) {
         T2 zl = T2{0, 0}, aL = T2{1, 0};
@@ -245,8 +244,8 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
             }
             pw = cmul(pr, ra);
         }
-        const T2 oma = T2{(Rl)(1.0 - a.aN_re), (Rl)(-a.aN_im)};
-        const Rl fRM = (Rl)a.fRM, omf = (Rl)a.one_minus_fR;
+        const T2 oma = T2{a.k.oma_re, a.k.oma_im};
+        const Rl fRM = a.k.fRM, omf = a.k.omf;
         if (gas && t0 == 0) W0 = (Rl)-1;
         for (int i = 0; i < L; i++) {
             const int t = t0 + i;

@@ -94,6 +94,7 @@ extern "C" int gs_plasma_max_noalloc(const gs_params* p, const double* rate_ln_d
     a.ponderomotive = p->ponderomotive;
     a.avalanche_cs = p->avalanche_cs;
     a.recombination_tau = p->recombination_tau;
+    gs::plasma_consts<double>(a);
     e = gs::launch_plasma<double>(a, rows, st, &nl);
     if (e == cudaSuccess) e = gs::launch_row_max_re<double>(u2, rows, nt, plasma_max_dev, st, &nl);
     if (e != cudaSuccess) return fail(GS_ERR_CUDA, cudaGetErrorString(e));
