@@ -31,12 +31,14 @@ template <typename Rl> struct FrontSmem {
     }
 };
 
-template <typename Rl>
+// LOGN > 0: rows of exactly 2^LOGN points (the row FFT with compile-time sizes and nothing
+// else inlined); LOGN = 0: any fused row length.
+template <typename Rl, int LOGN = 0>
 __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(FftArgs<Rl> f, PlasmaArgs<Rl> a,
                                                                               const typename Vec2<Rl>::T* __restrict__ A) {
     using T2 = C2<Rl>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int N = f.N;
+    const int N = LOGN > 0 ? (1 << LOGN) : f.N;
     const int tid = threadIdx.x, nthr = blockDim.x;
     T2* E = reinterpret_cast<T2*>(smem_raw);
     T2* twh = E + padded_len(N);
@@ -93,7 +95,8 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
     }
     __syncthreads();
     const TwTab<Rl> tw{twh, twl, f.twb};
-    smem_fft<+1, Rl>(E, N, f.logM, tw, 1, tid, nthr);
+    if constexpr (LOGN > 0) smem_fft_ct<+1, Rl, LOGN>(E, tw, 1, tid, nthr);
+    else smem_fft<+1, Rl>(E, N, f.logM, tw, 1, tid, nthr);
     const Rl rn = (Rl)N;
     const Rl ND = a.k.ND, tstep = a.k.tstep, U = a.k.U, Pc = a.k.Pc, AV = a.k.AV;
     const Rl invND = a.k.invND, invTAU = a.k.invTAU;
@@ -304,11 +307,11 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
 }
 
 // shared memory of nl_back_kernel: padded row + twiddles
-template <typename Rl>
+template <typename Rl, int LOGN = 0>
 __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_back_kernel(FftArgs<Rl> f, SpecArgs<Rl> s) {
     using T2 = C2<Rl>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int N = f.N;
+    const int N = LOGN > 0 ? (1 << LOGN) : f.N;
     const int tid = threadIdx.x, nthr = blockDim.x;
     T2* buf = reinterpret_cast<T2*>(smem_raw);
     T2* twh = buf + padded_len(N);
@@ -333,7 +336,8 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_back_kernel(F
             for (int q = tid; q < N; q += nthr) buf[pad16((q % nthr) * L + q / nthr)] = in[base + q];
         }
         __syncthreads();
-        smem_fft<-1, Rl>(buf, N, f.logM, tw, 1, tid, nthr);
+        if constexpr (LOGN > 0) smem_fft_ct<-1, Rl, LOGN>(buf, tw, 1, tid, nthr);
+        else smem_fft<-1, Rl>(buf, N, f.logM, tw, 1, tid, nthr);
         const bool last = src == (s.kerr_on ? 2 : 1);
         // batches of SB points per thread: every global read of a batch is issued before use
         constexpr int SB = 4;
@@ -417,14 +421,29 @@ template <typename Rl> cudaError_t nl_fused_setup(int N) {
     (void)N;
     cudaError_t e = cudaFuncSetAttribute(nl_front_kernel<Rl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if (e != cudaSuccess) return e;
-    return cudaFuncSetAttribute(nl_back_kernel<Rl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    e = cudaFuncSetAttribute(nl_back_kernel<Rl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if constexpr (sizeof(Rl) == 4) {   // the FP32 rows of 16384
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(nl_front_kernel<Rl, 14>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(nl_back_kernel<Rl, 14>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    }
+    return e;
 }
 
 template <typename Rl>
 cudaError_t launch_nl_front(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2<Rl>::T* A, int rows, cudaStream_t st,
                             long long* nl) {
     const int nthr = f.threads > 0 ? f.threads : fused_threads<Rl>(f.N);
-    nl_front_kernel<Rl><<<rows, nthr, FrontSmem<Rl>::bytes(f.N, nthr), st>>>(f, a, A);
+    const size_t sm = FrontSmem<Rl>::bytes(f.N, nthr);
+    bool done = false;
+    if constexpr (sizeof(Rl) == 4) {
+        if (f.N == 16384) {
+            nl_front_kernel<Rl, 14><<<rows, nthr, sm, st>>>(f, a, A);
+            done = true;
+        }
+    }
+    if (!done) nl_front_kernel<Rl><<<rows, nthr, sm, st>>>(f, a, A);
     (*nl)++;
     return cudaGetLastError();
 }
@@ -433,7 +452,14 @@ template <typename Rl>
 cudaError_t launch_nl_back(FftArgs<Rl> f, SpecArgs<Rl> s, int rows, cudaStream_t st, long long* nl) {
     const int nthr = f.threads > 0 ? f.threads : fused_threads<Rl>(f.N);
     const size_t bb = ((size_t)padded_len(f.N) + f.N / 64 + 64) * sizeof(typename Vec2<Rl>::T);
-    nl_back_kernel<Rl><<<rows, nthr, bb, st>>>(f, s);
+    bool done = false;
+    if constexpr (sizeof(Rl) == 4) {
+        if (f.N == 16384) {
+            nl_back_kernel<Rl, 14><<<rows, nthr, bb, st>>>(f, s);
+            done = true;
+        }
+    }
+    if (!done) nl_back_kernel<Rl><<<rows, nthr, bb, st>>>(f, s);
     (*nl)++;
     return cudaGetLastError();
 }
