@@ -31,9 +31,16 @@ template <typename Rl> struct FrontSmem {
     }
 };
 
+// a / b in the rows' precision: FP32 takes the fast reciprocal-based quotient (within 2 ulp;
+// the denominators here, U + P I and I above the rate threshold, are normal numbers)
+template <typename Rl> __device__ __forceinline__ Rl qdiv(Rl a, Rl b) { return a / b; }
+template <> __device__ __forceinline__ float qdiv<float>(float a, float b) { return __fdividef(a, b); }
+
 // LOGN > 0: rows of exactly 2^LOGN points (the row FFT with compile-time sizes and nothing
-// else inlined); LOGN = 0: any fused row length.
-template <typename Rl, int LOGN = 0>
+// else inlined); LOGN = 0: any fused row length.  LC = 16: launched with N/16 threads, so each
+// thread's chunk is 16 consecutive samples starting at a multiple of 16 and its shared-memory
+// slots are at constant offsets (pad16(t0 + i) = pad16(t0) + i, pad32(t0 + i) = pad32(t0) + i).
+template <typename Rl, int LOGN = 0, int LC = 0>
 __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(FftArgs<Rl> f, PlasmaArgs<Rl> a,
                                                                               const typename Vec2<Rl>::T* __restrict__ A) {
     using T2 = C2<Rl>;
@@ -143,19 +150,25 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
         if (t == 0) return (Rl)0;
         const T2 e = E[pad16(t)];
         const Rl I = e.x * e.x + e.y * e.y;
-        return AV / (U + Pc * I) * I;
+        return qdiv<Rl>(AV, U + Pc * I) * I;
     };
-    const int L = N / nthr;          // chunk of consecutive samples per thread
+    const int L = LC > 0 ? LC : N / nthr;   // chunk of consecutive samples per thread
     const int c = tid;
     const int t0 = c * L;
+    // shared-memory slots of sample t0 + i of this chunk
+    const T2* Ec = E + pad16(t0);
+    const Rl* Wc = Wb + pad32(t0);
+    auto e_at = [&](int i) -> T2 { return LC == 16 ? Ec[i] : E[pad16(t0 + i)]; };
+    auto w_at = [&](int i) -> Rl { return LC == 16 ? Wc[i] : Wb[pad32(t0 + i)]; };
     // the exact recurrence over this thread's chunk from start value s (rho_{t0-1})
     auto run_chunk = [&](Rl s, Rl* dout) -> Rl {
         Rl ro = s, d = (Rl)1;
         if (gas) {   // ionization.cpp:45-60, one level
             Rl W0 = (t0 > 0) ? Wb[pad32(t0 - 1)] : (Rl)-1;
+#pragma unroll 4
             for (int i = 0; i < L; i++) {
                 const int t = t0 + i;
-                const Rl W1 = Wb[pad32(t)];
+                const Rl W1 = w_at(i);
                 if (t > 0) ro = gas_step<Rl>(ro, W0, W1, tstep, ND, &d);
                 W0 = W1;
             }
@@ -163,9 +176,13 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
             return ro;
         }
         Rl W0 = (t0 > 0) ? Wb[pad32(t0 - 1)] : (Rl)0, g0 = (t0 > 0) ? g_of(t0 - 1) : (Rl)0;
+#pragma unroll 4
         for (int i = 0; i < L; i++) {
             const int t = t0 + i;
-            const Rl W1 = Wb[pad32(t)], g1 = g_of(t);
+            const Rl W1 = w_at(i);
+            const T2 e = e_at(i);
+            const Rl I = e.x * e.x + e.y * e.y;
+            const Rl g1 = (t == 0) ? (Rl)0 : qdiv<Rl>(AV, U + Pc * I) * I;
             if (t > 0) ro = heun_step<Rl>(ro, W0, g0, W1, g1, tstep, ND, invND, invTAU, &d);
             W0 = W1;
             g0 = g1;
@@ -217,8 +234,9 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
     T2 zs = T2{0, 0}, zN = T2{0, 0};
     if (rscan) {
         T2 zl = T2{0, 0}, aL = T2{1, 0};
+#pragma unroll 4
         for (int i = 0; i < L; i++) {
-            const T2 e = E[pad16(t0 + i)];
+            const T2 e = e_at(i);
             zl = cmul(ra, zl);
             zl.x += e.x * e.x + e.y * e.y;
             aL = cmul(aL, ra);
@@ -250,11 +268,12 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
         const T2 oma = T2{a.k.oma_re, a.k.oma_im};
         const Rl fRM = a.k.fRM, omf = a.k.omf;
         if (gas && t0 == 0) W0 = (Rl)-1;
+#pragma unroll 4
         for (int i = 0; i < L; i++) {
             const int t = t0 + i;
-            const T2 e = E[pad16(t)];
+            const T2 e = e_at(i);
             const Rl I = e.x * e.x + e.y * e.y;
-            const Rl W1 = Wb[pad32(t)];
+            const Rl W1 = w_at(i);
             T2 loss = T2{0, 0};
             if (gas) {
                 if (t > 0) ro = gas_step<Rl>(ro, W0, W1, tstep, ND, &d);
@@ -265,14 +284,14 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
                     loss = T2{sl * e.x, sl * e.y};
                 }
             } else {
-                const Rl g1 = (t == 0) ? (Rl)0 : AV / (U + Pc * I) * I;
+                const Rl g1 = (t == 0) ? (Rl)0 : qdiv<Rl>(AV, U + Pc * I) * I;
                 if (t > 0) ro = heun_step<Rl>(ro, W0, g0, W1, g1, tstep, ND, invND, invTAU, &d);
                 W0 = W1;
                 g0 = g1;
                 // loss[t] (ionization.cpp:43): W at (E_t, rho_t), the reference's log-threshold test
                 if (t > 0 && t < N - 1 && I > (Rl)GS_ION_MIN_LN) {
                     const Rl W01 = (ro > ND) ? (Rl)0 : W1;
-                    const Rl sl = -(Rl)0.5 * W01 * (U + Pc * I) / I;
+                    const Rl sl = qdiv<Rl>(-(Rl)0.5 * W01 * (U + Pc * I), I);
                     loss = T2{sl * e.x, sl * e.y};
                 }
             }
@@ -424,6 +443,8 @@ template <typename Rl> cudaError_t nl_fused_setup(int N) {
     e = cudaFuncSetAttribute(nl_back_kernel<Rl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if constexpr (sizeof(Rl) == 4) {   // the FP32 rows of 16384
         if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(nl_front_kernel<Rl, 14, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        if (e == cudaSuccess)
             e = cudaFuncSetAttribute(nl_front_kernel<Rl, 14>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(nl_back_kernel<Rl, 14>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
@@ -438,7 +459,10 @@ cudaError_t launch_nl_front(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2
     const size_t sm = FrontSmem<Rl>::bytes(f.N, nthr);
     bool done = false;
     if constexpr (sizeof(Rl) == 4) {
-        if (f.N == 16384) {
+        if (f.N == 16384 && nthr == 1024) {
+            nl_front_kernel<Rl, 14, 16><<<rows, nthr, sm, st>>>(f, a, A);
+            done = true;
+        } else if (f.N == 16384) {
             nl_front_kernel<Rl, 14><<<rows, nthr, sm, st>>>(f, a, A);
             done = true;
         }
