@@ -6,8 +6,10 @@
 // It runs as 3xTF32 with FP32 accumulation: H = Hh + Hl and X = Xh + Xl split into
 // round-to-nearest TF32 parts, D = Hh Xh + Hh Xl + Hl Xh (relative error ~2^-21).
 //
-// One CTA computes a 128 (i) x 128 (c) tile, K looped in blocks of 32 (one 128-byte
-// swizzle row of FP32), 3 pipeline stages of 64 KiB in shared memory:
+// Persistent: one CTA per SM walks 128 (i) x 128 (c) output tiles (tile T = row tile T % MT
+// of column tile T / MT, so the row tiles of a column block run side by side and share X in
+// L2), K looped in blocks of 32 (one 128-byte swizzle row of FP32); the 3-stage operand ring
+// (64 KiB stages) and the 2-deep raw X ring run on across tiles:
 //   warp 0      TMA producer: cp.async.bulk.tensor loads of the Hh/Hl tiles (SWIZZLE_128B)
 //               onto an mbarrier with expect-tx; owns the TMEM allocation.
 //   warp 1      MMA issuer: one thread issues tcgen05.mma.kind::tf32 (M=128, N=128, K=8)
@@ -17,9 +19,10 @@
 //               2-deep ring.
 //   warps 2-9   B producers: read the X tile from that ring, apply the
 //               spectral-window mask of the inverse transform, split into TF32 hi/lo and
-//               write them K-major in the 128B-swizzled layout the MMA descriptor reads;
-//               then the epilogue: tcgen05.ld of the accumulator and either a plain store
-//               or the fused calculate_Lstep update of BIGBUFFER2 (propagator.cu:570-625).
+//               write them K-major in the 128B-swizzled layout the MMA descriptor reads.
+//   warps 10-17 epilogue: tcgen05.ld of the accumulator (handed back to the MMA issuer
+//               right after), then either a plain store or the fused calculate_Lstep
+//               update of BIGBUFFER2 (propagator.cu:570-625), overlapping the next tile.
 // Every mbarrier wait is bounded; on expiry the kernel records an error, drains what it
 // issued, frees TMEM and returns.
 #include <cuda.h>
@@ -40,9 +43,10 @@ constexpr int BM = 128, BN = 128, BK = 32, STAGES = 3, RAW_STAGES = 2;
 constexpr int TILE_BYTES = BM * BK * 4;                 // 16 KiB: one 128 x 32 FP32 tile
 constexpr int STAGE_BYTES = 4 * TILE_BYTES;             // Ah, Al, Bh, Bl
 constexpr int RAW_BYTES = BK * BN * 4;                  // 16 KiB: 32 rows x 128 columns of X
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + RAW_STAGES * RAW_BYTES + 1024 + 256;
-constexpr int THREADS = 320;
-constexpr int NCONV = 256;                              // warps 2..9
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + RAW_STAGES * RAW_BYTES + 1024 + 256;   // + barriers, TMEM slot
+constexpr int NCONV = 256;                              // warps 2..9: B producers
+constexpr int NEPI = 8;                                 // warps 10..17: epilogue
+constexpr int THREADS = 64 + NCONV + 32 * NEPI;
 constexpr unsigned long long WAIT_NS = 200ull * 1000 * 1000;   // 200 ms; legitimate waits are < 1 ms
 
 __constant__ float c_sqrt_ho_f[20];
@@ -161,17 +165,22 @@ __device__ __forceinline__ void st_shared_v4(uint32_t addr, float a, float b, fl
     asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(addr), "f"(a), "f"(b), "f"(c), "f"(d) : "memory");
 }
 
+// The load and its tcgen05.wait::ld are one asm statement: tcgen05.ld is asynchronous, so
+// its destination registers may be read only after the wait.  (As two statements the
+// compiler may schedule reads of the registers before the wait, which returns stale values
+// when the load is slow, e.g. while MMAs into another accumulator buffer are running.)
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float* v) {
     uint32_t r[32];
     asm volatile(
         "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, "
-        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];"
+        "%16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31}, [%32];\n"
+        "tcgen05.wait::ld.sync.aligned;"
         : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
           "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]),
           "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]),
           "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
-        : "r"(taddr));
-    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        : "r"(taddr)
+        : "memory");
 #pragma unroll
     for (int k = 0; k < 32; k++) v[k] = __uint_as_float(r[k]);
 }
@@ -193,17 +202,21 @@ __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_consta
     uint64_t* full_a = bars;                  // [STAGES]  TMA tx
     uint64_t* full_b = bars + STAGES;         // [STAGES]  256 converter arrivals
     uint64_t* empty = bars + 2 * STAGES;      // [STAGES]  MMA commit
-    uint64_t* done = bars + 3 * STAGES;       // accumulator ready
+    uint64_t* done = bars + 3 * STAGES;       // every MMA of this CTA complete
     uint64_t* raw_full = bars + 3 * STAGES + 1;                 // [RAW_STAGES] TMA tx
     uint64_t* raw_empty = raw_full + RAW_STAGES;                // [RAW_STAGES] 256 converter arrivals
-    uint32_t* tmem_slot = (uint32_t*)(raw_empty + RAW_STAGES);
+    uint64_t* acc_full = raw_empty + RAW_STAGES;                // MMA commit: accumulator ready
+    uint64_t* acc_empty = acc_full + 1;                         // NEPI epilogue warps: read out
+    uint32_t* tmem_slot = (uint32_t*)(acc_empty + 1);
     volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int MT = a.nr / BM;
-    const int m_tile = blockIdx.x % MT, n_tile = blockIdx.x / MT;
-    const int m0 = m_tile * BM, c0 = n_tile * BN;
+    const int ntiles = MT * (a.ncols / BN);
     const int nk = a.nr / BK;
+    // this CTA's tiles: blockIdx.x + k gridDim.x; tile T is row tile T % MT of column tile
+    // T / MT, so the row tiles of one column block run side by side (X shared in L2)
+    const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < STAGES; s++) {
@@ -216,6 +229,8 @@ __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_consta
             mbar_init(&raw_full[r], 1);
             mbar_init(&raw_empty[r], NCONV);
         }
+        mbar_init(acc_full, 1);
+        mbar_init(acc_empty, NEPI);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -231,138 +246,185 @@ __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_consta
     const uint32_t tmem = *tmem_slot;
 
     if (warp == 0) {
-        // ------------------------------------------------ TMA producer (A = Hh, Hl)
+        // ------------------------------------------------ TMA producer (A = Hh, Hl; raw X)
         if (lane == 0) {
-            int issued = 0, issued_raw = 0;
-            for (int kb = 0; kb < nk; kb++) {
-                const int s = kb % STAGES;
-                if (kb >= STAGES && !mbar_wait(&empty[s], ((kb / STAGES) + 1) & 1)) {
-                    record_stall(a.err, 4u, kb, warp);
-                    *abort_flag = 1;
-                    break;
+            int issued = 0, issued_raw = 0;   // global K-block counters
+            for (int it = 0; it < my_tiles && !*abort_flag; it++) {
+                const int T = blockIdx.x + it * gridDim.x;
+                const int m0 = (T % MT) * BM, c0 = (T / MT) * BN;
+                for (int kb = 0; kb < nk; kb++) {
+                    const int g = it * nk + kb;
+                    const int s = g % STAGES;
+                    if (g >= STAGES && !mbar_wait(&empty[s], ((g / STAGES) + 1) & 1)) {
+                        record_stall(a.err, 4u, kb, warp);
+                        *abort_flag = 1;
+                        break;
+                    }
+                    if (*abort_flag) break;
+                    unsigned char* st = smem + s * STAGE_BYTES;
+                    mbar_expect_tx(&full_a[s], 2 * TILE_BYTES);
+                    tma_load_2d(st, &map_hi, kb * BK, m0, &full_a[s]);
+                    tma_load_2d(st + TILE_BYTES, &map_lo, kb * BK, m0, &full_a[s]);
+                    issued = g + 1;
+                    const int r = g % RAW_STAGES;
+                    if (g >= RAW_STAGES && !mbar_wait(&raw_empty[r], ((g / RAW_STAGES) + 1) & 1)) {
+                        record_stall(a.err, 512u, kb, warp);
+                        *abort_flag = 1;
+                        break;
+                    }
+                    mbar_expect_tx(&raw_full[r], RAW_BYTES);
+                    tma_load_2d(raw + r * RAW_BYTES, &map_x, c0, kb * BK, &raw_full[r]);
+                    issued_raw = g + 1;
                 }
-                if (*abort_flag) break;
-                unsigned char* st = smem + s * STAGE_BYTES;
-                mbar_expect_tx(&full_a[s], 2 * TILE_BYTES);
-                tma_load_2d(st, &map_hi, kb * BK, m0, &full_a[s]);
-                tma_load_2d(st + TILE_BYTES, &map_lo, kb * BK, m0, &full_a[s]);
-                const int r = kb % RAW_STAGES;
-                if (kb >= RAW_STAGES && !mbar_wait(&raw_empty[r], ((kb / RAW_STAGES) + 1) & 1)) {
-                    record_stall(a.err, 512u, kb, warp);
-                    *abort_flag = 1;
-                    issued = kb + 1;
-                    break;
-                }
-                mbar_expect_tx(&raw_full[r], RAW_BYTES);
-                tma_load_2d(raw + r * RAW_BYTES, &map_x, c0, kb * BK, &raw_full[r]);
-                issued = kb + 1;
-                issued_raw = kb + 1;
             }
             // drain: every issued TMA load has landed before the CTA may exit
-            for (int kb = (issued > STAGES ? issued - STAGES : 0); kb < issued; kb++)
-                if (!mbar_wait(&full_a[kb % STAGES], (kb / STAGES) & 1)) record_stall(a.err, 128u, kb, warp);
-            for (int kb = (issued_raw > RAW_STAGES ? issued_raw - RAW_STAGES : 0); kb < issued_raw; kb++)
-                if (!mbar_wait(&raw_full[kb % RAW_STAGES], (kb / RAW_STAGES) & 1)) record_stall(a.err, 1024u, kb, warp);
+            for (int g = (issued > STAGES ? issued - STAGES : 0); g < issued; g++)
+                if (!mbar_wait(&full_a[g % STAGES], (g / STAGES) & 1)) record_stall(a.err, 128u, g % nk, warp);
+            for (int g = (issued_raw > RAW_STAGES ? issued_raw - RAW_STAGES : 0); g < issued_raw; g++)
+                if (!mbar_wait(&raw_full[g % RAW_STAGES], (g / RAW_STAGES) & 1)) record_stall(a.err, 1024u, g % nk, warp);
         }
         __syncwarp();   // the warp reconverges before any block-wide barrier
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
             const uint32_t idesc = make_idesc();
-            uint32_t acc = 0;
-            for (int kb = 0; kb < nk; kb++) {
-                const int s = kb % STAGES;
-                const unsigned ph = (kb / STAGES) & 1;
-                if (!mbar_wait(&full_a[s], ph)) {
-                    record_stall(a.err, 8u, kb, warp);
+            for (int it = 0; it < my_tiles && !*abort_flag; it++) {
+                // the epilogue has read the previous tile's accumulator out of tensor memory
+                if (it >= 1 && !mbar_wait(acc_empty, (it - 1) & 1)) {
+                    record_stall(a.err, 4096u, 0, warp);
                     *abort_flag = 1;
                     break;
                 }
-                if (!mbar_wait(&full_b[s], ph)) {
-                    record_stall(a.err, 256u, kb, warp);
-                    *abort_flag = 1;
-                    break;
-                }
-                if (*abort_flag) break;
                 asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                unsigned char* st = smem + s * STAGE_BYTES;
-                const uint32_t ah = smem_u32(st), al = ah + TILE_BYTES;
-                const uint32_t bh = ah + 2 * TILE_BYTES, bl = ah + 3 * TILE_BYTES;
+                const uint32_t dt = tmem;
+                uint32_t acc = 0;
+                bool ok = true;
+                for (int kb = 0; kb < nk; kb++) {
+                    const int g = it * nk + kb;
+                    const int s = g % STAGES;
+                    const unsigned ph = (g / STAGES) & 1;
+                    if (!mbar_wait(&full_a[s], ph)) {
+                        record_stall(a.err, 8u, kb, warp);
+                        ok = false;
+                        break;
+                    }
+                    if (!mbar_wait(&full_b[s], ph)) {
+                        record_stall(a.err, 256u, kb, warp);
+                        ok = false;
+                        break;
+                    }
+                    if (*abort_flag) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    unsigned char* st = smem + s * STAGE_BYTES;
+                    const uint32_t ah = smem_u32(st), al = ah + TILE_BYTES;
+                    const uint32_t bh = ah + 2 * TILE_BYTES, bl = ah + 3 * TILE_BYTES;
 #pragma unroll
-                for (int kk = 0; kk < BK / 8; kk++) {
-                    const uint32_t off = kk * 32;   // 8 TF32 = 32 bytes along K inside the swizzle row
-                    mma_tf32(tmem, make_desc(al + off), make_desc(bh + off), idesc, acc);
-                    acc = 1;
-                    mma_tf32(tmem, make_desc(ah + off), make_desc(bl + off), idesc, 1);
-                    mma_tf32(tmem, make_desc(ah + off), make_desc(bh + off), idesc, 1);
+                    for (int kk = 0; kk < BK / 8; kk++) {
+                        const uint32_t off = kk * 32;   // 8 TF32 = 32 bytes along K inside the swizzle row
+                        mma_tf32(dt, make_desc(al + off), make_desc(bh + off), idesc, acc);
+                        acc = 1;
+                        mma_tf32(dt, make_desc(ah + off), make_desc(bl + off), idesc, 1);
+                        mma_tf32(dt, make_desc(ah + off), make_desc(bh + off), idesc, 1);
+                    }
+                    mma_commit(&empty[s]);
                 }
-                mma_commit(&empty[s]);
+                if (!ok) {
+                    *abort_flag = 1;
+                    break;
+                }
+                mma_commit(acc_full);
             }
             mma_commit(done);
         }
         __syncwarp();
-    } else {
+    } else if (warp < 2 + NCONV / 32) {
         // ------------------------------------------------ B producers (X -> TF32 hi/lo, K-major)
         const int t = threadIdx.x - 64;        // 0..255
         const int n = t & (BN - 1), kh = t >> 7;
-        const int c = c0 + n;
-        const int kmx = (a.mode == QDHT_MASKED) ? a.kmax[c >> 1] : 0x7fffffff;
         const uint32_t rowoff = (uint32_t)((n >> 3) * 1024 + (n & 7) * 128);
-        for (int kb = 0; kb < nk; kb++) {
-            const int s = kb % STAGES;
-            const int r = kb % RAW_STAGES;
-            // the raw X tile (32 rows j x 128 columns) from the TMA ring: column n, rows 16 kh ..
-            if (!mbar_wait(&raw_full[r], (kb / RAW_STAGES) & 1)) {
-                record_stall(a.err, 2048u, kb, warp);
+        for (int it = 0; it < my_tiles && !*abort_flag; it++) {
+            const int T = blockIdx.x + it * gridDim.x;
+            const int c = (T / MT) * BN + n;
+            const int kmx = (a.mode == QDHT_MASKED) ? a.kmax[c >> 1] : 0x7fffffff;
+            bool ok = true;
+            for (int kb = 0; kb < nk; kb++) {
+                const int g = it * nk + kb;
+                const int s = g % STAGES;
+                const int r = g % RAW_STAGES;
+                // the raw X tile (32 rows j x 128 columns) from the TMA ring: column n, rows 16 kh ..
+                if (!mbar_wait(&raw_full[r], (g / RAW_STAGES) & 1)) {
+                    record_stall(a.err, 2048u, kb, warp);
+                    ok = false;
+                    break;
+                }
+                float xv[16];
+                const float* rt = reinterpret_cast<const float*>(raw + r * RAW_BYTES) + (16 * kh) * BN + n;
+#pragma unroll
+                for (int u = 0; u < 16; u++) {
+                    const int j = kb * BK + 16 * kh + u;
+                    const float v = rt[u * BN];
+                    xv[u] = (j > kmx) ? 0.f : v;
+                }
+                mbar_arrive(&raw_empty[r]);
+                if (g >= STAGES && !mbar_wait(&empty[s], ((g / STAGES) + 1) & 1)) {
+                    record_stall(a.err, 16u, kb, warp);
+                    ok = false;
+                    break;
+                }
+                if (*abort_flag) { ok = false; break; }
+                float hi[16], lo[16];
+#pragma unroll
+                for (int u = 0; u < 16; u++) {
+                    hi[u] = tf32_rna(xv[u]);
+                    lo[u] = tf32_rna(xv[u] - hi[u]);
+                }
+                const uint32_t bh = smem_u32(smem + s * STAGE_BYTES + 2 * TILE_BYTES) + rowoff;
+                const uint32_t bl = bh + TILE_BYTES;
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const uint32_t ch = (uint32_t)((((4 * kh + q) ^ (n & 7))) << 4);
+                    st_shared_v4(bh + ch, hi[4 * q], hi[4 * q + 1], hi[4 * q + 2], hi[4 * q + 3]);
+                    st_shared_v4(bl + ch, lo[4 * q], lo[4 * q + 1], lo[4 * q + 2], lo[4 * q + 3]);
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_arrive(&full_b[s]);
+            }
+            if (!ok) {
                 *abort_flag = 1;
                 break;
             }
-            float xv[16];
-            const float* rt = reinterpret_cast<const float*>(raw + r * RAW_BYTES) + (16 * kh) * BN + n;
-#pragma unroll
-            for (int u = 0; u < 16; u++) {
-                const int j = kb * BK + 16 * kh + u;
-                const float v = rt[u * BN];
-                xv[u] = (j > kmx) ? 0.f : v;
-            }
-            mbar_arrive(&raw_empty[r]);
-            if (kb >= STAGES && !mbar_wait(&empty[s], ((kb / STAGES) + 1) & 1)) {
-                record_stall(a.err, 16u, kb, warp);
-                *abort_flag = 1;
-                break;
-            }
-            if (*abort_flag) break;
-            float hi[16], lo[16];
-#pragma unroll
-            for (int u = 0; u < 16; u++) {
-                hi[u] = tf32_rna(xv[u]);
-                lo[u] = tf32_rna(xv[u] - hi[u]);
-            }
-            const uint32_t bh = smem_u32(smem + s * STAGE_BYTES + 2 * TILE_BYTES) + rowoff;
-            const uint32_t bl = bh + TILE_BYTES;
-#pragma unroll
-            for (int q = 0; q < 4; q++) {
-                const uint32_t ch = (uint32_t)((((4 * kh + q) ^ (n & 7))) << 4);
-                st_shared_v4(bh + ch, hi[4 * q], hi[4 * q + 1], hi[4 * q + 2], hi[4 * q + 3]);
-                st_shared_v4(bl + ch, lo[4 * q], lo[4 * q + 1], lo[4 * q + 2], lo[4 * q + 3]);
-            }
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            mbar_arrive(&full_b[s]);
         }
-
-        // ------------------------------------------------ epilogue
-        const bool ok = __all_sync(0xffffffffu, mbar_wait(done, 0) ? 1 : 0) != 0;
-        if (!ok && lane == 0) record_stall(a.err, 32u, nk, warp);
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (ok && !__any_sync(0xffffffffu, *abort_flag)) {   // warp-uniform: tcgen05.ld is .sync.aligned
-            const int q = warp & 3;                 // TMEM lane quarter of this warp
-            const int half = (warp - 2) >> 2;       // which 64 columns
+    } else {
+        // ------------------------------------------------ epilogue (NEPI warps: two per TMEM
+        // lane quarter, 64 columns each).  Each warp copies its accumulator columns into
+        // registers and hands tensor memory back at once: the MMA issuer then starts the next
+        // tile, and this tile's arithmetic and stores overlap the next tile's main loop.
+        const int ew = warp - 2 - NCONV / 32;   // 0..7
+        const int q = warp & 3;                 // TMEM lane quarter this warp may read
+        const int half = ew >> 2;               // which 64 columns
+        for (int it = 0; it < my_tiles; it++) {
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(acc_full, it & 1) ? 1 : 0) != 0;
+            if (!ok) {
+                if (lane == 0) record_stall(a.err, 32u, it, warp);
+                *abort_flag = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (__any_sync(0xffffffffu, *abort_flag)) break;   // warp-uniform: tcgen05.ld is .sync.aligned
+            const int T = blockIdx.x + it * gridDim.x;
+            const int m0 = (T % MT) * BM, c0 = (T / MT) * BN;
             const int i = m0 + 32 * q + lane;
             const float kt2i = a.kt2 ? a.kt2[i] : 0.f;
+            float acc[64];
+            tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * half), acc);
+            tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * half + 32), acc + 32);
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acc_empty);
+#pragma unroll
             for (int cc = 0; cc < 2; cc++) {
                 const int col0 = 64 * half + 32 * cc;
-                float v[32];
-                tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)col0, v);
+                const float* v = acc + 32 * cc;
                 float* yrow = a.Y + (size_t)i * a.ncols + c0 + col0;
                 if (a.mode != QDHT_LSTEP) {
 #pragma unroll
@@ -370,7 +432,7 @@ __global__ void __launch_bounds__(THREADS, 1) qdht_tc_kernel(const __grid_consta
                         *reinterpret_cast<float4*>(yrow + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
                 } else {
                     const int p0 = (c0 + col0) >> 1;
-#pragma unroll 4
+#pragma unroll
                     for (int e = 0; e < 16; e++) {
                         const int p = p0 + e;
                         if (i > a.kmax[p]) continue;        // outside the window: BIGBUFFER2 untouched
@@ -440,6 +502,7 @@ __global__ void lstep_adj_kernel(const float2* __restrict__ fb, float2* __restri
 
 struct QdhtTc {
     int nr = 0, nt = 0;
+    int sms = 0;   // persistent grid: one CTA per SM
     cudaStream_t st = nullptr;
     float *hh = nullptr, *hl = nullptr;
     float *kr = nullptr, *ki = nullptr, *ho = nullptr, *kt2 = nullptr;
@@ -485,6 +548,9 @@ QdhtTc* qdht_tc_create(int nr, int nt, cudaStream_t st, std::string* msg) {
               cudaMalloc(&q->ho, nt * 4) == cudaSuccess && cudaMalloc(&q->kt2, nr * 4) == cudaSuccess &&
               cudaMalloc(&q->kmax, nt * 4) == cudaSuccess && cudaMalloc(&q->err, 8) == cudaSuccess;
     if (ok) ok = cudaMemset(q->err, 0, 8) == cudaSuccess;
+    int dev = 0;
+    if (ok) ok = cudaGetDevice(&dev) == cudaSuccess &&
+                 cudaDeviceGetAttribute(&q->sms, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess && q->sms > 0;
     if (ok) ok = cudaFuncSetAttribute(tc::qdht_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::SMEM_BYTES) ==
                  cudaSuccess;
     if (!ok) {
@@ -594,7 +660,8 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
     a.kt2 = q->kt2;
     a.kmax = q->kmax;
     a.err = q->err;
-    const unsigned grid = (unsigned)((q->nr / tc::BM) * (a.ncols / tc::BN));
+    const int ntiles = (q->nr / tc::BM) * (a.ncols / tc::BN);
+    const unsigned grid = (unsigned)(ntiles < q->sms ? ntiles : q->sms);
     const CUtensorMap* mx = nullptr;
     for (auto& e : q->xmaps)
         if (e.first == X) mx = &e.second;

@@ -28,7 +28,9 @@ def hot_setup(n_r=128, n_t=1024, power_cr=20.0, tol=1e-2, seed=11, **kw):
     return tables.build(tables.Config.from_file(p), noise_seed=seed, noise_sigma=1e-4)
 
 
-@pytest.mark.parametrize("n_r,n_t", [(128, 64), (256, 512), (512, 256)])
+# (512, 4096) and (1024, 2048): 256 output tiles of 128 x 128, more than the persistent grid
+# (one CTA per SM), so CTAs run several tiles through both accumulator buffers
+@pytest.mark.parametrize("n_r,n_t", [(128, 64), (256, 512), (512, 256), (512, 4096), (1024, 2048)])
 def test_qdht_tensor_cores(n_r, n_t):
     T = hot_setup(n_r=n_r, n_t=n_t)
     rng = np.random.default_rng(n_r + n_t)
@@ -39,6 +41,7 @@ def test_qdht_tensor_cores(n_r, n_t):
     assert rel(y, ref) < QDHT_TOL
     # every output tile is exercised: per-row errors stay small too
     assert max(rel(y[i], ref[i]) for i in range(0, n_r, max(1, n_r // 16))) < 10 * QDHT_TOL
+    assert np.array_equal(P.qdht(x), y)   # the transform is deterministic
 
 
 def test_nl_step_mixed():
