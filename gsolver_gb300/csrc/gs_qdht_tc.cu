@@ -498,6 +498,245 @@ __global__ void lstep_adj_kernel(const float2* __restrict__ fb, float2* __restri
     b1b[idx] = make_float2(dz * tr * inv, dz * ti * inv);
 }
 
+
+// ======================================================================= wide-tile path --
+// For grids with 2 n_t a multiple of 256 the X operand is split once, outside the GEMM:
+//   qdht_split_kernel  X [n_r][2 n_t] -> XhT, XlT [2 n_t][n_r] (TF32 hi / lo parts, K-major:
+//                      the row index j contiguous), with the inverse transform's window mask
+//                      applied; a 32 x 32 shared-memory transpose, coalesced both ways.
+//   qdht_tc2_kernel    the GEMM on 128 (i) x 256 (c) tiles with every operand streamed by TMA
+//                      in the 128-byte-swizzled K-major layout (no conversion in shared
+//                      memory): per 32-deep K-block 96 KiB of TMA writes and 144 KiB of MMA
+//                      reads for 128 x 256 x 32 x 3 products, against 192 KiB + 96 KiB for
+//                      twice the 128-column tiles.  Warp 0 TMA, warp 1 MMA issuer (N = 256),
+//                      warps 2-17 epilogue (four per TMEM lane quarter, 64 columns each).
+constexpr int BN2 = 256, STAGES2 = 2;
+constexpr int A2_BYTES = BM * BK * 4;                   // 16 KiB
+constexpr int B2_BYTES = BN2 * BK * 4;                  // 32 KiB
+constexpr int STAGE2_BYTES = 2 * A2_BYTES + 2 * B2_BYTES;
+constexpr int NEPI2 = 16;
+constexpr int THREADS2 = 64 + 32 * NEPI2;
+constexpr int SMEM2_BYTES = STAGES2 * STAGE2_BYTES + 1024 + 256;
+
+__global__ void __launch_bounds__(256) qdht_split_kernel(const float* __restrict__ X, float* __restrict__ XhT,
+                                                         float* __restrict__ XlT, int nr, int ncols,
+                                                         const int* __restrict__ kmax) {
+    __shared__ float t[32][33];
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
+    const int c0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int j = j0 + ty + 8 * k, c = c0 + tx;
+        float v = X[(size_t)j * ncols + c];
+        if (kmax && j > kmax[c >> 1]) v = 0.f;   // outside the spectral window
+        t[ty + 8 * k][tx] = v;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const int c = c0 + ty + 8 * k, j = j0 + tx;
+        const float v = t[tx][ty + 8 * k];
+        const float hi = tf32_rna(v);
+        XhT[(size_t)c * nr + j] = hi;
+        XlT[(size_t)c * nr + j] = tf32_rna(v - hi);
+    }
+}
+
+__host__ __device__ constexpr uint32_t make_idesc_n(int n) {
+    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+}
+
+// 32 accumulator columns of row i starting at output column cg: a plain store or the fused
+// calculate_Lstep update of BIGBUFFER2 (propagator.cu:570-625)
+__device__ __forceinline__ void epilogue_cols(const TcArgs& a, const float* v, int i, int cg, float kt2i) {
+    float* yrow = a.Y + (size_t)i * a.ncols + cg;
+    if (a.mode != QDHT_LSTEP) {
+#pragma unroll
+        for (int k = 0; k < 32; k += 4)
+            *reinterpret_cast<float4*>(yrow + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+        return;
+    }
+    const int p0 = cg >> 1;
+#pragma unroll
+    for (int e = 0; e < 16; e++) {
+        const int p = p0 + e;
+        if (i > a.kmax[p]) continue;        // outside the window: BIGBUFFER2 untouched
+        const float k1 = a.kr[p], k2 = a.ki[p];
+        const float sq = sqrt_ho_f(-kt2i / k1 / k1);
+        float2 b2 = *reinterpret_cast<float2*>(yrow + 2 * e);
+        const float inv = 1.f / (1.f + sq);
+        b2.x += a.dz * v[2 * e] * inv;
+        b2.y += a.dz * v[2 * e + 1] * inv;
+        float sn, cs;
+        sincosf(a.dz * (-a.ho[p] - sq * k1), &sn, &cs);
+        const float m = expf(a.dz * k2);
+        const float pr = m * cs, pi = m * sn;
+        float2 f;
+        f.x = b2.x * pr - b2.y * pi;
+        f.y = b2.x * pi + b2.y * pr;
+        *reinterpret_cast<float2*>(yrow + 2 * e) = f;
+    }
+}
+
+__global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_constant__ CUtensorMap map_hi,
+                                                               const __grid_constant__ CUtensorMap map_lo,
+                                                               const __grid_constant__ CUtensorMap map_bh,
+                                                               const __grid_constant__ CUtensorMap map_bl, TcArgs a) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    uint64_t* bars = (uint64_t*)(smem + STAGES2 * STAGE2_BYTES);
+    uint64_t* full = bars;                    // [STAGES2] TMA tx
+    uint64_t* empty = bars + STAGES2;         // [STAGES2] MMA commit
+    uint64_t* acc_full = bars + 2 * STAGES2;  // MMA commit: accumulator ready
+    uint64_t* acc_empty = acc_full + 1;       // NEPI2 epilogue warps: read out
+    uint64_t* done = acc_empty + 1;           // every MMA of this CTA complete
+    uint32_t* tmem_slot = (uint32_t*)(done + 1);
+    volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int MT = a.nr / BM;
+    const int ntiles = MT * (a.ncols / BN2);
+    const int nk = a.nr / BK;
+    const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < STAGES2; s++) {
+            mbar_init(&full[s], 1);
+            mbar_init(&empty[s], 1);
+        }
+        mbar_init(acc_full, 1);
+        mbar_init(acc_empty, NEPI2);
+        mbar_init(done, 1);
+        *abort_flag = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                     "r"(BN2));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    if (warp == 0) {
+        // ------------------------------------------------ TMA producer (Hh, Hl, XhT, XlT)
+        if (lane == 0) {
+            int issued = 0;
+            for (int it = 0; it < my_tiles && !*abort_flag; it++) {
+                const int T = blockIdx.x + it * gridDim.x;
+                const int m0 = (T % MT) * BM, c0 = (T / MT) * BN2;
+                for (int kb = 0; kb < nk; kb++) {
+                    const int g = it * nk + kb;
+                    const int s = g % STAGES2;
+                    if (g >= STAGES2 && !mbar_wait(&empty[s], ((g / STAGES2) + 1) & 1)) {
+                        record_stall(a.err, 4u, kb, warp);
+                        *abort_flag = 1;
+                        break;
+                    }
+                    if (*abort_flag) break;
+                    unsigned char* st = smem + s * STAGE2_BYTES;
+                    mbar_expect_tx(&full[s], STAGE2_BYTES);
+                    tma_load_2d(st, &map_hi, kb * BK, m0, &full[s]);
+                    tma_load_2d(st + A2_BYTES, &map_lo, kb * BK, m0, &full[s]);
+                    tma_load_2d(st + 2 * A2_BYTES, &map_bh, kb * BK, c0, &full[s]);
+                    tma_load_2d(st + 2 * A2_BYTES + B2_BYTES, &map_bl, kb * BK, c0, &full[s]);
+                    issued = g + 1;
+                }
+            }
+            for (int g = (issued > STAGES2 ? issued - STAGES2 : 0); g < issued; g++)
+                if (!mbar_wait(&full[g % STAGES2], (g / STAGES2) & 1)) record_stall(a.err, 128u, g % nk, warp);
+        }
+        __syncwarp();
+    } else if (warp == 1) {
+        // ------------------------------------------------ MMA issuer
+        if (lane == 0) {
+            constexpr uint32_t idesc = make_idesc_n(BN2);
+            for (int it = 0; it < my_tiles && !*abort_flag; it++) {
+                if (it >= 1 && !mbar_wait(acc_empty, (it - 1) & 1)) {
+                    record_stall(a.err, 4096u, 0, warp);
+                    *abort_flag = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                uint32_t acc = 0;
+                bool ok = true;
+                for (int kb = 0; kb < nk; kb++) {
+                    const int g = it * nk + kb;
+                    const int s = g % STAGES2;
+                    if (!mbar_wait(&full[s], (g / STAGES2) & 1)) {
+                        record_stall(a.err, 8u, kb, warp);
+                        ok = false;
+                        break;
+                    }
+                    if (*abort_flag) { ok = false; break; }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    unsigned char* st = smem + s * STAGE2_BYTES;
+                    const uint32_t ah = smem_u32(st), al = ah + A2_BYTES;
+                    const uint32_t bh = ah + 2 * A2_BYTES, bl = bh + B2_BYTES;
+#pragma unroll
+                    for (int kk = 0; kk < BK / 8; kk++) {
+                        const uint32_t off = kk * 32;   // 8 TF32 = 32 bytes along K inside the swizzle row
+                        mma_tf32(tmem, make_desc(al + off), make_desc(bh + off), idesc, acc);
+                        acc = 1;
+                        mma_tf32(tmem, make_desc(ah + off), make_desc(bl + off), idesc, 1);
+                        mma_tf32(tmem, make_desc(ah + off), make_desc(bh + off), idesc, 1);
+                    }
+                    mma_commit(&empty[s]);
+                }
+                if (!ok) {
+                    *abort_flag = 1;
+                    break;
+                }
+                mma_commit(acc_full);
+            }
+            mma_commit(done);
+        }
+        __syncwarp();
+    } else {
+        // ------------------------------------------------ epilogue: each warp reads its 64
+        // accumulator columns out, hands tensor memory back, then stores / updates
+        const int q = warp & 3;                 // TMEM lane quarter this warp may read
+        const int part = (warp - 2) >> 2;       // which 64 columns (0..3)
+        for (int it = 0; it < my_tiles; it++) {
+            const bool ok = __all_sync(0xffffffffu, mbar_wait(acc_full, it & 1) ? 1 : 0) != 0;
+            if (!ok) {
+                if (lane == 0) record_stall(a.err, 32u, it, warp);
+                *abort_flag = 1;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            if (__any_sync(0xffffffffu, *abort_flag)) break;   // warp-uniform: tcgen05.ld is .sync.aligned
+            const int T = blockIdx.x + it * gridDim.x;
+            const int m0 = (T % MT) * BM, c0 = (T / MT) * BN2;
+            const int i = m0 + 32 * q + lane;
+            const float kt2i = a.kt2 ? a.kt2[i] : 0.f;
+            float accv[64];
+            tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * part), accv);
+            tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * part + 32), accv + 32);
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) mbar_arrive(acc_empty);
+            epilogue_cols(a, accv, i, c0 + 64 * part, kt2i);
+            epilogue_cols(a, accv + 32, i, c0 + 64 * part + 32, kt2i);
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    }
+
+    __syncthreads();
+    if (warp == 1) {
+        if (lane == 0 && !mbar_wait(done, 0)) record_stall(a.err, 64u, nk, warp);
+        __syncwarp();
+    }
+    __syncthreads();
+    if (warp == 0) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN2));
+    }
+}
+
 }  // namespace tc
 
 struct QdhtTc {
@@ -510,6 +749,10 @@ struct QdhtTc {
     unsigned* err = nullptr;
     CUtensorMap map_hi, map_lo;
     bool have_lstep = false;
+    // wide-tile path (2 n_t a multiple of 256): X split once into K-major TF32 hi / lo parts
+    bool wide = false;
+    float *xhT = nullptr, *xlT = nullptr;   // [2 n_t][n_r]
+    CUtensorMap map_bh, map_bl;
     // tensor maps of the X operands seen so far (the handle's few state arrays)
     std::vector<std::pair<const float*, CUtensorMap>> xmaps;
 };
@@ -570,6 +813,28 @@ QdhtTc* qdht_tc_create(int nr, int nt, cudaStream_t st, std::string* msg) {
                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
         if (r != CUDA_SUCCESS) {
             if (msg) *msg = "cuTensorMapEncodeTiled failed";
+            qdht_tc_destroy(q);
+            return nullptr;
+        }
+    }
+    q->wide = (2 * nt) % tc::BN2 == 0;
+    if (q->wide) {
+        const size_t ncols = 2 * (size_t)nt;
+        bool okw = cudaMalloc(&q->xhT, ncols * nr * 4) == cudaSuccess && cudaMalloc(&q->xlT, ncols * nr * 4) == cudaSuccess &&
+                   cudaFuncSetAttribute(tc::qdht_tc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        tc::SMEM2_BYTES) == cudaSuccess;
+        for (int w = 0; okw && w < 2; w++) {
+            // [2 n_t rows c][n_r floats j]: boxes of 32 j (128 B, swizzled) x 256 c
+            cuuint64_t gdim[2] = {(cuuint64_t)nr, (cuuint64_t)ncols};
+            cuuint64_t gstride[1] = {(cuuint64_t)nr * 4};
+            cuuint32_t box[2] = {(cuuint32_t)tc::BK, (cuuint32_t)tc::BN2};
+            cuuint32_t estr[2] = {1, 1};
+            okw = enc(w ? &q->map_bl : &q->map_bh, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, w ? (void*)q->xlT : (void*)q->xhT,
+                      gdim, gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+        }
+        if (!okw) {
+            if (msg) *msg = "wide-tile QDHT set-up failed";
             qdht_tc_destroy(q);
             return nullptr;
         }
@@ -660,6 +925,19 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
     a.kt2 = q->kt2;
     a.kmax = q->kmax;
     a.err = q->err;
+    if (q->wide) {
+        // split X into the K-major hi / lo operands (the window mask of the inverse applied), then
+        // the GEMM on 128 x 256 tiles
+        dim3 sg((unsigned)(a.ncols / 32), (unsigned)(q->nr / 32));
+        tc::qdht_split_kernel<<<sg, 256, 0, q->st>>>(X, q->xhT, q->xlT, q->nr, a.ncols,
+                                                     mode == QDHT_MASKED ? q->kmax : nullptr);
+        (*nlaunch)++;
+        const int nt2 = (q->nr / tc::BM) * (a.ncols / tc::BN2);
+        const unsigned g2 = (unsigned)(nt2 < q->sms ? nt2 : q->sms);
+        tc::qdht_tc2_kernel<<<g2, tc::THREADS2, tc::SMEM2_BYTES, q->st>>>(q->map_hi, q->map_lo, q->map_bh, q->map_bl, a);
+        (*nlaunch)++;
+        return cudaGetLastError();
+    }
     const int ntiles = (q->nr / tc::BM) * (a.ncols / tc::BN);
     const unsigned grid = (unsigned)(ntiles < q->sms ? ntiles : q->sms);
     const CUtensorMap* mx = nullptr;
@@ -713,7 +991,7 @@ int qdht_tc_check(QdhtTc* q, std::string* msg) {
 
 void qdht_tc_destroy(QdhtTc* q) {
     if (!q) return;
-    void* ptrs[] = {q->hh, q->hl, q->kr, q->ki, q->ho, q->kt2, q->kmax, q->err};
+    void* ptrs[] = {q->hh, q->hl, q->kr, q->ki, q->ho, q->kt2, q->kmax, q->err, q->xhT, q->xlT};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete q;
