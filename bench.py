@@ -12,7 +12,10 @@ Synthetic: the pulse is generated (seeded 1e-4 complex Gaussian noise), no datas
           copies FIELD and BIGBUFFER2 in and out (the host globals propagator() works on)
   fp64    the plain FP64 GPU path on the same workload, and the mixed path's relative L2
           error against it after the same fixed-dz steps from the same start
-  roofline  the mixed QDHT kernels (tcgen05), algorithmic 8 N_r flop per field-point step
+  roofline  the dominant kernel, nl_back (HBM-bound): its one-pass input and output (44 B per
+          field point in complex64) over its CUDA-event launch time; roofline_nl_step the
+          whole NL increment against its 16 B per field point minimum; roofline_qdht the
+          tensor-core QDHT, algorithmic 8 N_r flop per field-point step
   adjoint the gradient workload (256 x 4096, 1000 steps): forward vs forward+adjoint time
           and the gradient's accuracy (see adjoint_leg)
   batch   64 pulses with uneven grids, one CUDA graph launch per z-step (see batch_leg)
@@ -161,10 +164,10 @@ def new_state(S):
     return {"z": float(S["znet"][0]), "n_z": 0, "zstep": float(S["init_zstep"]), "step_n": 0}
 
 
-def read_profile_traffic():
-    """Per-launch DRAM bytes of the mixed QDHT kernel from the committed ncu summary (a
-    512-row capture scaled to the 1024-row launch by the rows it processes)."""
-    p = os.path.join(ROOT, "profiles", "qdht_tc_fused_silica_512x16384.md")
+def read_profile_traffic(name="qdht_tc_fused_silica_512x16384.md"):
+    """Per-launch DRAM bytes of a kernel from its committed ncu summary (a smaller capture
+    scaled to the 1024-row launch by the rows it processes)."""
+    p = os.path.join(ROOT, "profiles", name)
     try:
         with open(p) as f:
             m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read())
@@ -452,6 +455,7 @@ def main():
     stream = torch.cuda.ExternalStream(P.stream_ptr(), device=lrank)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     P.qdht_timing(enable=True)
+    P.nl_timing(enable=True)
     n0 = P.launch_count()
     if world > 1:
         torch.distributed.barrier()
@@ -465,6 +469,7 @@ def main():
     ms = e0.elapsed_time(e1)
     launches = P.launch_count() - n0
     q_ms, q_n = P.qdht_timing(enable=False)
+    nf_ms, nb_ms, n_st = P.nl_timing(enable=False)
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -476,12 +481,35 @@ def main():
     flop_launch = 2.0 * nr * nr * 2 * nt
     per_launch_ms = q_ms / max(q_n, 1)
     achieved = flop_launch / (per_launch_ms / 1e3) / 1e12 if q_n else None
-    roof = {"bound": "tensor", "kernel": "qdht_tc" if prec == gs.PREC_MIXED else "qdht64 (FP64 CUDA cores)",
+    roof_q = {"bound": "tensor", "kernel": "qdht_tc" if prec == gs.PREC_MIXED else "qdht64 (FP64 CUDA cores)",
             "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
             "frac": (achieved / bf16) if achieved else None, "traffic": read_profile_traffic() if prec == gs.PREC_MIXED else None,
             "peak_kind": f"{pk_kind} cuBLAS bf16 burst", "launch_ms": per_launch_ms,
             "qdht_share_of_step": (q_ms / ms) if ms else None,
             "note": "algorithmic flop (8 N_r per field-point step); 3xTF32 executes 3x; TF32 tensor peak is half the bf16 peak"}
+    # the dominant kernel: nl_back (three FFTs of the stage's sources, spectral combination, RK4
+    # sum), HBM-bound by design; its algorithmic bytes per launch are its own input and output
+    # once each: the three source rows (24 B per field point), the RK4 sum read in stages 1-3
+    # and written (6 + 8 B on average), k written in stages 0-2 (6 B on average)
+    esz = 8 if prec == gs.PREC_MIXED else 16
+    nb_launch_ms = nb_ms / n_st if n_st else None
+    nb_bytes = (44 if esz == 8 else 88) * nr * nt
+    nb_ach = nb_bytes / (nb_launch_ms / 1e3) / 1e9 if nb_launch_ms else None
+    nl_step_ms = (nf_ms + nb_ms) / n_st * 4 if n_st else None
+    nl_ach = (16 if esz == 8 else 32) * nr * nt / (nl_step_ms / 1e3) / 1e9 if nl_step_ms else None
+    roof = {"bound": "hbm", "kernel": "nl_back_kernel" if n_st else "staged NL kernels (not timed)",
+            "achieved": nb_ach, "peak": hbm, "unit": "GB/s", "frac": (nb_ach / hbm) if nb_ach and hbm else None,
+            "traffic": read_profile_traffic("nl_fused_silica_256x16384.md") if prec == gs.PREC_MIXED else None,
+            "peak_kind": f"{pk_kind} HBM copy", "launch_ms": nb_launch_ms,
+            "algorithmic_bytes_per_launch": nb_bytes,
+            "share_of_step": (nb_ms / ms) if ms and n_st else None,
+            "front_launch_ms": (nf_ms / n_st) if n_st else None,
+            "note": "CUDA events around each launch on the handle's stream; traffic = ncu DRAM bytes per launch of a "
+                    "256-row capture scaled by rows (writes still in L2 when the kernel ends are not counted)"}
+    roof_nl = {"bound": "hbm", "unit": "GB/s", "peak": hbm, "achieved": nl_ach,
+               "frac": (nl_ach / hbm) if nl_ach and hbm else None, "step_ms": nl_step_ms,
+               "note": "the whole NL increment (4 RK4 stages, 8 launches) against its one-pass minimum: read A and "
+                       "write the NL increment once, 16 B per field point in complex64"}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -491,7 +519,8 @@ def main():
                            parallelism=f"replicas{world}", l2="inputs larger than L2 (state ~1 GB per pulse)",
                            z_reached_m=state["z"], dz_last_m=state["zstep"],
                            nl_threads_per_row=tuned[0] if tuned else "default"),
-            "gpu_launches": launches, "roofline": roof, "clocks": clk.summary()}
+            "gpu_launches": launches, "roofline": roof, "roofline_nl_step": roof_nl, "roofline_qdht": roof_q,
+            "clocks": clk.summary()}
 
     # e2e through the public API with pinned host buffers
     if not args.no_e2e:

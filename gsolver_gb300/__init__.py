@@ -29,7 +29,8 @@ PREC_FP64, PREC_MIXED = 0, 1
 # every function declared in include/gs_abi.h
 ABI_FUNCTIONS = (
     "gs_create", "gs_upload_tables", "gs_set_field", "gs_get_field", "gs_nl_step", "gs_get_nl",
-    "gs_lstep", "gs_qdht", "gs_step", "gs_stream", "gs_launch_count", "gs_qdht_timing", "gs_destroy",
+    "gs_lstep", "gs_qdht", "gs_step", "gs_stream", "gs_launch_count", "gs_qdht_timing", "gs_nl_timing",
+    "gs_destroy",
     "gs_last_error", "gs_status_string",
     # include/gs_setup.h
     "gs_setup_from_config", "gs_setup_last_error", "gs_setup_grid", "gs_setup_params",
@@ -103,6 +104,7 @@ def load_library(path: str | None = None):
     L.gs_launch_count.argtypes = [V]
     L.gs_launch_count.restype = C.c_longlong
     L.gs_qdht_timing.argtypes = [V, I, PD, C.POINTER(C.c_int)]
+    L.gs_nl_timing.argtypes = [V, I, PD, PD, C.POINTER(C.c_int)]
     L.gs_destroy.argtypes = [V]
     L.gs_last_error.argtypes = [V]
     L.gs_last_error.restype = C.c_char_p
@@ -273,6 +275,13 @@ class Propagator:
         ms, n = C.c_double(), C.c_int()
         self._check(self.L.gs_qdht_timing(self.h, int(enable), C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    def nl_timing(self, enable=True):
+        """CUDA-event time of the fused RK4-stage kernels since the previous call:
+        (ms of the front kernels, ms of the back kernels, RK4 stages timed)."""
+        f, b, n = C.c_double(), C.c_double(), C.c_int()
+        self._check(self.L.gs_nl_timing(self.h, int(enable), C.byref(f), C.byref(b), C.byref(n)))
+        return f.value, b.value, n.value
 
     def set_apertures(self, z, r, qdht_x, r_max):
         """Apertures in the reference's array order (the last entry is applied first); gs_step

@@ -104,6 +104,8 @@ static void free_all(gs_handle* h) {
     if (h->ev0) cudaEventDestroy(h->ev0);
     if (h->ev1) cudaEventDestroy(h->ev1);
     if (h->st) cudaStreamDestroy(h->st);
+    for (cudaEvent_t e : h->nl_ev)
+        if (e) cudaEventDestroy(e);
 }
 
 int gs_create(const gs_params* prm, gs_handle** out) {
@@ -338,6 +340,22 @@ int gsi::run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz) {
     return GS_OK;
 }
 
+int gs_nl_timing(gs_handle* h, int enable, double* ms_front, double* ms_back, int* stages) {
+    if (!h) return GS_ERR_ARG;
+    if (ms_front) *ms_front = h->nl_ms_front;
+    if (ms_back) *ms_back = h->nl_ms_back;
+    if (stages) *stages = h->nl_stages_timed;
+    h->nl_ms_front = h->nl_ms_back = 0;
+    h->nl_stages_timed = 0;
+    h->nl_ev_pending = false;
+    if (enable && !h->nl_ev[0]) {
+        CK(h, cudaSetDevice(h->p.device));
+        for (cudaEvent_t& e : h->nl_ev) CK(h, cudaEventCreate(&e));
+    }
+    h->time_nl = enable != 0;
+    return GS_OK;
+}
+
 int gs_qdht_timing(gs_handle* h, int enable, double* ms_total, int* launches) {
     if (!h) return GS_ERR_ARG;
     if (ms_total) *ms_total = h->qdht_ms;
@@ -501,11 +519,16 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
                 ps.tape_rho = (Rl*)tape->rho[s];
                 ps.tape_q = (Rl*)tape->q[s];
             }
+            const bool tm = h->time_nl && !tape;
+            if (tm) CK(h, cudaEventRecord(h->nl_ev[3 * s], h->st));
             CK(h, launch_nl_front<Rl>(f1, ps, A, nr, h->st, &h->launches));
+            if (tm) CK(h, cudaEventRecord(h->nl_ev[3 * s + 1], h->st));
             SpecArgs<Rl> s2 = sa;
             s2.stage = s;
             CK(h, launch_nl_back<Rl>(fa, s2, nr, h->st, &h->launches));
+            if (tm) CK(h, cudaEventRecord(h->nl_ev[3 * s + 2], h->st));
         }
+        if (h->time_nl && !tape) h->nl_ev_pending = true;
         return GS_OK;
     }
     for (int s = 0; s < 4; s++) {
@@ -551,6 +574,17 @@ static int nl_step(gs_handle* h, double dz, double* max_a2, double* max_nl2) {
     CK(h, cudaMemcpyAsync(mx, h->max_dev, 16, cudaMemcpyDeviceToHost, h->st));
     CK(h, cudaMemcpyAsync(&err, h->err_dev, 4, cudaMemcpyDeviceToHost, h->st));
     CK(h, cudaStreamSynchronize(h->st));
+    if (h->nl_ev_pending) {   // fold the stage kernels' event times into the gs_nl_timing totals
+        for (int s = 0; s < 4; s++) {
+            float f = 0, b = 0;
+            CK(h, cudaEventElapsedTime(&f, h->nl_ev[3 * s], h->nl_ev[3 * s + 1]));
+            CK(h, cudaEventElapsedTime(&b, h->nl_ev[3 * s + 1], h->nl_ev[3 * s + 2]));
+            h->nl_ms_front += f;
+            h->nl_ms_back += b;
+        }
+        h->nl_stages_timed += 4;
+        h->nl_ev_pending = false;
+    }
     double a2, n2;
     std::memcpy(&a2, &mx[0], 8);
     std::memcpy(&n2, &mx[1], 8);
