@@ -97,7 +97,7 @@ void* gs_stream(const gs_handle* h) { return h ? (void*)h->st : nullptr; }
 static void free_all(gs_handle* h) {
     void* ptrs[] = {h->A, h->S, h->NB, h->KP, h->E, h->U, h->tw, h->pf, h->rm, h->kerr, h->rate,
                     h->omega, h->ho, h->kt2, h->Cm, h->m1, h->wavenum, h->staging, h->perm_dev,
-                    h->err_dev, h->max_dev, h->dump_dev, h->m1inv, h->adj, h->adj_w, h->th, h->twb};
+                    h->err_dev, h->max_dev, h->dump_dev, h->m1inv, h->adj, h->adj_w, h->th, h->twb, h->row_ion};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (h->tc) gs::qdht_tc_destroy(h->tc);
     if (h->tcT) gs::qdht_tc_destroy(h->tcT);
@@ -142,7 +142,8 @@ int gs_create(const gs_params* prm, gs_handle** out) {
          al((void**)&h->omega, nt * 8) && al((void**)&h->ho, nt * 8) && al((void**)&h->kt2, nr * 8) &&
          al((void**)&h->Cm, (size_t)nr * nr * 8) && al((void**)&h->m1, nr * 8) &&
          al((void**)&h->wavenum, nt * 16) && al((void**)&h->staging, nel * 16) &&
-         al((void**)&h->perm_dev, nt * 4) && al((void**)&h->err_dev, 4) && al((void**)&h->max_dev, 16);
+         al((void**)&h->perm_dev, nt * 4) && al((void**)&h->err_dev, 4) && al((void**)&h->max_dev, 16) &&
+         al((void**)&h->row_ion, (size_t)nr * 4);
     if (!ok) {
         cudaGetLastError();
         free_all(h);
@@ -508,6 +509,8 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
     const bool fused = h->fused && (raman_scan || !raman || !kerr_on);
     if (tape && !fused) return fail(h, GS_ERR_UNSUPPORTED, "recording the RK4 stages needs rows that fit one CTA");
     if (fused) {
+        pa.row_ion = h->row_ion;   // written by each front launch, read by its back launch
+        sa.row_ion = h->row_ion;
         for (int s = 0; s < 4; s++) {
             FftArgs<Rl> f1 = fa;
             f1.rows = nr; f1.kp = KP;

@@ -51,6 +51,7 @@ struct gs_handle {
     int nl_stages_timed = 0;
     double* dump_dev = nullptr;   // 3 n_r + 2 n_t doubles of reduction output, r weights
     void* twb = nullptr;          // per-stage base twiddles of the M-point row FFTs (tw_base_offset)
+    int* row_ion = nullptr;       // [n_r] fused NL kernels: row ionizes in the current RK4 stage
     void* th = nullptr;           // gas build: third-harmonic factors th_coeff exp(j phi_t), [n_t]
     std::vector<double> ap_z;      // apertures not yet applied, reference order (last applied first)
     std::vector<int> ap_row0;      // first row outside each aperture's radius

@@ -45,6 +45,9 @@ template <typename Rl> struct PlasmaArgs {
     // Kerr source (th[t] = (KERR_TH/KERR) exp(j phi_t), natural time order)
     int gas;
     const typename Vec2<Rl>::T* th;
+    // fused front kernel: per row, whether any sample ionizes (some W_t > 0) or rho starts
+    // above 0; where not, the density stays exactly 0, loss and rho E are 0 and are not written
+    int* row_ion;
     // the scalars above in the rows' precision, converted once on the host (plasma_args):
     // converting a double on the device runs on the FP64 pipe, which is slow on this GPU
     struct Consts {
@@ -114,6 +117,7 @@ template <typename Rl> struct SpecArgs {
     int fuse_plasma;   // spec2 also adds PLASMA_FUNC * FFT(rho E) (spec1 skipped)
     typename Vec2<Rl>::T *nb, *kp;
     unsigned long long* max_out;
+    const int* row_ion;   // fused back kernel: rows flagged 0 have only the Kerr source (or none)
 };
 
 template <typename Rl>

@@ -111,6 +111,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
     // in batches of 8 samples per thread so that the table reads (L2: the carve-out leaves
     // little L1) are in flight together
     const bool gas = a.gas != 0;
+    bool anyw = false;   // some sample of this thread is above the rate table's threshold
     for (int tb = tid; tb < N; tb += 8 * nthr) {
         int n[8];
         Rl dl[8], Iv[8];
@@ -141,10 +142,14 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
             if (t < N) {
                 const Rl W = n[u] >= 0 ? photo_rate_from<Rl>(w0[u], w1[u], dl[u]) : (Rl)0;
                 Wb[pad32(t)] = gas ? gas_rate_slot<Rl>(t, Iv[u], W) : W;
+                anyw = anyw || n[u] >= 0;
             }
         }
     }
-    __syncthreads();
+    // W > 0 somewhere (exp of the table is positive above its threshold) or rho starting above
+    // 0: otherwise every Heun / gas step adds exactly 0 and the density stays 0 along the row
+    const bool ion = __syncthreads_or(anyw ? 1 : 0) != 0 || a.k.rho0 != (Rl)0;
+    if (tid == 0 && a.row_ion) a.row_ion[blockIdx.x] = ion ? 1 : 0;
 
     auto g_of = [&](int t) -> Rl {
         if (t == 0) return (Rl)0;
@@ -198,7 +203,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
     // relative change of the starts at which Newton stops (quadratic convergence: the
     // starts then carry ~tol^2 + rounding)
     const Rl tol = sizeof(Rl) == 8 ? (Rl)1e-13 : (Rl)1e-5;
-    for (int it = 0; it < 16; it++) {
+    for (int it = 0; it < (ion ? 16 : 0); it++) {   // no ionization: the starts stay 0
         const Rl sc = s_start[c];
         Rl D;
         const Rl e = run_chunk(sc, &D);
@@ -275,7 +280,9 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
             const Rl I = e.x * e.x + e.y * e.y;
             const Rl W1 = w_at(i);
             T2 loss = T2{0, 0};
-            if (gas) {
+            if (!ion) {
+                // the density stays 0 and there is no loss
+            } else if (gas) {
                 if (t > 0) ro = gas_step<Rl>(ro, W0, W1, tstep, ND, &d);
                 W0 = W1;
                 // loss[t] = tl E_t (ionization.cpp:60-81), where sample t is above the threshold
@@ -313,8 +320,10 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
             // source rows in chunk-interleaved order (sample c L + i at i nthr + c): the warp's
             // stores are coalesced; nl_back undoes the order when it stages the row
             const size_t q = base + (size_t)i * nthr + c;
-            a.u1[q] = loss;
-            a.u2[q] = T2{ro * e.x, ro * e.y};
+            if (ion || !a.row_ion) {   // zero rows are not written: nl_back skips their FFTs
+                a.u1[q] = loss;
+                a.u2[q] = T2{ro * e.x, ro * e.y};
+            }
             a.u3[q] = src3;
             if (a.tape_e) {   // what the adjoint of this stage reads back
                 a.tape_e[base + t] = e;
@@ -340,24 +349,32 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_back_kernel(F
     const TwTab<Rl> tw{twh, twl, f.twb};
     T2* acc = s.kp;   // the new k doubles as the accumulator of the three spectra
     Rl lmax = 0;
-    for (int src = 0; src < (s.kerr_on ? 3 : 2); src++) {
+    // a row without ionization has loss = rho E = 0: only the Kerr source (FFT(0) = 0 adds
+    // nothing), or, with Kerr off, no source at all (k = 0: one pass with a zero spectrum)
+    const bool ion = s.row_ion ? s.row_ion[blockIdx.x] != 0 : true;
+    const int lastsrc = s.kerr_on ? 2 : 1;
+    const int first = ion ? 0 : lastsrc;
+    const bool zero_src = !ion && !s.kerr_on;
+    for (int src = first; src <= lastsrc; src++) {
         const T2* in = src == 0 ? s.u1 : (src == 1 ? s.u2 : s.u3);
-        // the rows arrive in nl_front's chunk-interleaved order: position u nthr + c holds
-        // sample c L + u (L = N / nthr; the same launch shape runs both kernels)
-        const int L = N / nthr;
-        if (L == 16) {
-            T2 v[16];
+        if (!zero_src) {
+            // the rows arrive in nl_front's chunk-interleaved order: position u nthr + c holds
+            // sample c L + u (L = N / nthr; the same launch shape runs both kernels)
+            const int L = N / nthr;
+            if (L == 16) {
+                T2 v[16];
 #pragma unroll
-            for (int u = 0; u < 16; u++) v[u] = in[base + tid + u * nthr];
+                for (int u = 0; u < 16; u++) v[u] = in[base + tid + u * nthr];
 #pragma unroll
-            for (int u = 0; u < 16; u++) buf[pad16(tid * 16 + u)] = v[u];
-        } else {
-            for (int q = tid; q < N; q += nthr) buf[pad16((q % nthr) * L + q / nthr)] = in[base + q];
+                for (int u = 0; u < 16; u++) buf[pad16(tid * 16 + u)] = v[u];
+            } else {
+                for (int q = tid; q < N; q += nthr) buf[pad16((q % nthr) * L + q / nthr)] = in[base + q];
+            }
+            __syncthreads();
+            if constexpr (LOGN > 0) smem_fft_ct<-1, Rl, LOGN>(buf, tw, 1, tid, nthr);
+            else smem_fft<-1, Rl>(buf, N, f.logM, tw, 1, tid, nthr);
         }
-        __syncthreads();
-        if constexpr (LOGN > 0) smem_fft_ct<-1, Rl, LOGN>(buf, tw, 1, tid, nthr);
-        else smem_fft<-1, Rl>(buf, N, f.logM, tw, 1, tid, nthr);
-        const bool last = src == (s.kerr_on ? 2 : 1);
+        const bool last = src == lastsrc;
         // batches of SB points per thread: every global read of a batch is issued before use
         constexpr int SB = 4;
         for (int pb = tid; pb < N; pb += SB * nthr) {
@@ -366,8 +383,8 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_back_kernel(F
             for (int u = 0; u < SB; u++) {
                 const int p = pb + u * nthr;
                 const bool in = p < N;
-                v[u] = in ? buf[pad16(p)] : T2{0, 0};
-                ac[u] = (in && src > 0) ? acc[base + p] : T2{0, 0};
+                v[u] = (in && !zero_src) ? buf[pad16(p)] : T2{0, 0};
+                ac[u] = (in && src > first) ? acc[base + p] : T2{0, 0};
                 // the spectral coefficient: PLASMA_FUNC for FFT(rho E), -j KERR_PROFILE for FFT(Q E)
                 if (src == 1) c[u] = in ? s.pf[p] : T2{0, 0};
                 else if (src == 2) c[u] = T2{(Rl)0, in ? -s.kerr[p] : (Rl)0};
