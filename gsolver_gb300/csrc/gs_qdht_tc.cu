@@ -506,13 +506,14 @@ __global__ void lstep_adj_kernel(const float2* __restrict__ fb, float2* __restri
 //                      applied; a 32 x 32 shared-memory transpose, coalesced both ways.
 //   qdht_tc2_kernel    the GEMM on 128 (i) x 256 (c) tiles with every operand streamed by TMA
 //                      in the 128-byte-swizzled K-major layout (no conversion in shared
-//                      memory): per 32-deep K-block 96 KiB of TMA writes and 144 KiB of MMA
-//                      reads for 128 x 256 x 32 x 3 products, against 192 KiB + 96 KiB for
-//                      twice the 128-column tiles.  Warp 0 TMA, warp 1 MMA issuer (N = 256),
-//                      warps 2-17 epilogue (four per TMEM lane quarter, 64 columns each).
-constexpr int BN2 = 256, STAGES2 = 2;
-constexpr int A2_BYTES = BM * BK * 4;                   // 16 KiB
-constexpr int B2_BYTES = BN2 * BK * 4;                  // 32 KiB
+//                      memory): per 32 of K 96 KiB of TMA writes and 144 KiB of MMA reads for
+//                      128 x 256 x 32 x 3 products, against 192 KiB + 96 KiB for twice the
+//                      128-column tiles.  K-blocks of 16 in the 64-byte swizzle: 48 KiB
+//                      stages, four of them in flight.  Warp 0 TMA, warp 1 MMA issuer
+//                      (N = 256), warps 2-17 epilogue (four per TMEM lane quarter, 64 columns each).
+constexpr int BN2 = 256, BK2 = 16, STAGES2 = 4;        // K-blocks of 16 (one 64-byte swizzle row)
+constexpr int A2_BYTES = BM * BK2 * 4;                  // 8 KiB
+constexpr int B2_BYTES = BN2 * BK2 * 4;                 // 16 KiB
 constexpr int STAGE2_BYTES = 2 * A2_BYTES + 2 * B2_BYTES;
 constexpr int NEPI2 = 16;
 constexpr int THREADS2 = 64 + 32 * NEPI2;
@@ -540,6 +541,18 @@ __global__ void __launch_bounds__(256) qdht_split_kernel(const float* __restrict
         XhT[(size_t)c * nr + j] = hi;
         XlT[(size_t)c * nr + j] = tf32_rna(v - hi);
     }
+}
+
+// shared-memory matrix descriptor for K-major tiles in the 64-byte swizzle: rows of 16 FP32,
+// 8-row groups 512 B apart
+__device__ __forceinline__ uint64_t make_desc64(uint32_t saddr) {
+    uint64_t d = 0;
+    d |= (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)1 << 16;                 // leading byte offset (unused for swizzled K-major)
+    d |= (uint64_t)(512 >> 4) << 32;        // stride byte offset: next 8-row group
+    d |= (uint64_t)1 << 46;                 // descriptor version (sm_100 family)
+    d |= (uint64_t)4 << 61;                 // SWIZZLE_64B
+    return d;
 }
 
 __host__ __device__ constexpr uint32_t make_idesc_n(int n) {
@@ -596,7 +609,7 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int MT = a.nr / BM;
     const int ntiles = MT * (a.ncols / BN2);
-    const int nk = a.nr / BK;
+    const int nk = a.nr / BK2;
     const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
 
     if (threadIdx.x == 0) {
@@ -639,10 +652,10 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
                     if (*abort_flag) break;
                     unsigned char* st = smem + s * STAGE2_BYTES;
                     mbar_expect_tx(&full[s], STAGE2_BYTES);
-                    tma_load_2d(st, &map_hi, kb * BK, m0, &full[s]);
-                    tma_load_2d(st + A2_BYTES, &map_lo, kb * BK, m0, &full[s]);
-                    tma_load_2d(st + 2 * A2_BYTES, &map_bh, kb * BK, c0, &full[s]);
-                    tma_load_2d(st + 2 * A2_BYTES + B2_BYTES, &map_bl, kb * BK, c0, &full[s]);
+                    tma_load_2d(st, &map_hi, kb * BK2, m0, &full[s]);
+                    tma_load_2d(st + A2_BYTES, &map_lo, kb * BK2, m0, &full[s]);
+                    tma_load_2d(st + 2 * A2_BYTES, &map_bh, kb * BK2, c0, &full[s]);
+                    tma_load_2d(st + 2 * A2_BYTES + B2_BYTES, &map_bl, kb * BK2, c0, &full[s]);
                     issued = g + 1;
                 }
             }
@@ -677,12 +690,12 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
                     const uint32_t ah = smem_u32(st), al = ah + A2_BYTES;
                     const uint32_t bh = ah + 2 * A2_BYTES, bl = bh + B2_BYTES;
 #pragma unroll
-                    for (int kk = 0; kk < BK / 8; kk++) {
+                    for (int kk = 0; kk < BK2 / 8; kk++) {
                         const uint32_t off = kk * 32;   // 8 TF32 = 32 bytes along K inside the swizzle row
-                        mma_tf32(tmem, make_desc(al + off), make_desc(bh + off), idesc, acc);
+                        mma_tf32(tmem, make_desc64(al + off), make_desc64(bh + off), idesc, acc);
                         acc = 1;
-                        mma_tf32(tmem, make_desc(ah + off), make_desc(bl + off), idesc, 1);
-                        mma_tf32(tmem, make_desc(ah + off), make_desc(bh + off), idesc, 1);
+                        mma_tf32(tmem, make_desc64(ah + off), make_desc64(bl + off), idesc, 1);
+                        mma_tf32(tmem, make_desc64(ah + off), make_desc64(bh + off), idesc, 1);
                     }
                     mma_commit(&empty[s]);
                 }
@@ -752,7 +765,7 @@ struct QdhtTc {
     // wide-tile path (2 n_t a multiple of 256): X split once into K-major TF32 hi / lo parts
     bool wide = false;
     float *xhT = nullptr, *xlT = nullptr;   // [2 n_t][n_r]
-    CUtensorMap map_bh, map_bl;
+    CUtensorMap map_bh, map_bl, map_hi64, map_lo64;   // 16-float boxes in the 64-byte swizzle
     // tensor maps of the X operands seen so far (the handle's few state arrays)
     std::vector<std::pair<const float*, CUtensorMap>> xmaps;
 };
@@ -827,10 +840,19 @@ QdhtTc* qdht_tc_create(int nr, int nt, cudaStream_t st, std::string* msg) {
             // [2 n_t rows c][n_r floats j]: boxes of 32 j (128 B, swizzled) x 256 c
             cuuint64_t gdim[2] = {(cuuint64_t)nr, (cuuint64_t)ncols};
             cuuint64_t gstride[1] = {(cuuint64_t)nr * 4};
-            cuuint32_t box[2] = {(cuuint32_t)tc::BK, (cuuint32_t)tc::BN2};
+            cuuint32_t box[2] = {(cuuint32_t)tc::BK2, (cuuint32_t)tc::BN2};
             cuuint32_t estr[2] = {1, 1};
             okw = enc(w ? &q->map_bl : &q->map_bh, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, w ? (void*)q->xlT : (void*)q->xhT,
-                      gdim, gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                      gdim, gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+        }
+        for (int w = 0; okw && w < 2; w++) {   // H hi / lo in 16-float boxes of 128 rows
+            cuuint64_t gdim[2] = {(cuuint64_t)nr, (cuuint64_t)nr};
+            cuuint64_t gstride[1] = {(cuuint64_t)nr * 4};
+            cuuint32_t box[2] = {(cuuint32_t)tc::BK2, (cuuint32_t)tc::BM};
+            cuuint32_t estr[2] = {1, 1};
+            okw = enc(w ? &q->map_lo64 : &q->map_hi64, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, w ? (void*)q->hl : (void*)q->hh,
+                      gdim, gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
         }
         if (!okw) {
@@ -934,7 +956,7 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
         (*nlaunch)++;
         const int nt2 = (q->nr / tc::BM) * (a.ncols / tc::BN2);
         const unsigned g2 = (unsigned)(nt2 < q->sms ? nt2 : q->sms);
-        tc::qdht_tc2_kernel<<<g2, tc::THREADS2, tc::SMEM2_BYTES, q->st>>>(q->map_hi, q->map_lo, q->map_bh, q->map_bl, a);
+        tc::qdht_tc2_kernel<<<g2, tc::THREADS2, tc::SMEM2_BYTES, q->st>>>(q->map_hi64, q->map_lo64, q->map_bh, q->map_bl, a);
         (*nlaunch)++;
         return cudaGetLastError();
     }
