@@ -141,12 +141,14 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
 
     // phase A: W_t and the avalanche prefactor g_t = AV/(U + P I_t) * I_t (t >= 1)
     const bool gas = a.gas != 0;
+    bool anyw = false;
     for (int t = tid; t < N; t += nthr) {
         Rl W = 0, g = 0;
         if (t > 0) {
             T2 e = E[t];
             Rl I = e.x * e.x + e.y * e.y;
             W = photo_rate<Rl>(I, a.rate, a.err);
+            anyw = anyw || W > (Rl)0;
             g = AV / (U + Pc * I) * I;
             if (gas) W = gas_rate_slot<Rl>(t, I, W);
         } else if (gas) {
@@ -154,7 +156,9 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
         }
         U1[t] = T2{W, g};
     }
-    __syncthreads();
+    // no sample with W > 0 and rho starting at 0: every step adds exactly 0, the density
+    // stays 0 along the row and the recurrence below is skipped
+    const bool ion = __syncthreads_or(anyw ? 1 : 0) != 0 || a.k.rho0 != (Rl)0;
 
     // phase B: the Heun recurrence by multiple shooting.  Thread c owns the L consecutive
     // steps nt in [c L, c L + L); its start value s_c = rho_{cL-1} is refined by Newton
@@ -217,7 +221,7 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
     // stop when the starts move less than tol (relative): Newton converges quadratically, so
     // the starts then carry ~tol^2 + rounding; far below the parity bars (1e-10 / 1e-5)
     const Rl tol = sizeof(Rl) == 8 ? (Rl)1e-13 : (Rl)1e-5;
-    for (int it = 0; it < 16; it++) {
+    for (int it = 0; it < (ion ? 16 : 0); it++) {
         Rl A = 1, B = 0, sc = 0;
         if (c < P) {
             sc = s_start[c];
@@ -274,15 +278,16 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
         __syncthreads();
         if (s_done) break;
     }
-    if (c < P) run_chunk(s_start[c], true, nullptr);
+    if (ion && c < P) run_chunk(s_start[c], true, nullptr);
     __syncthreads();
 
-    if (a.density_only) return;
-
     // phase C: loss[t] (uses W_t, I_t, rho_t at step t+1), rho*E, intensity terms
+    if (a.density_only && !ion)
+        for (int t = tid; t < N; t += nthr) U2[t] = T2{0, 0};
+    if (a.density_only) return;
     for (int t = tid; t < N; t += nthr) {
         T2 e = E[t];
-        Rl rho = U2[t].x;
+        const Rl rho = ion ? U2[t].x : (Rl)0;
         T2 w = U1[t];
         T2 loss = T2{0, 0};
         if (gas) {
