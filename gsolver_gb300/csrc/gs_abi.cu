@@ -197,6 +197,8 @@ int gs_create(const gs_params* prm, gs_handle** out) {
     if (e == cudaSuccess) e = h->fp64 ? fft_set_smem<double>(h->M, nt) : fft_set_smem<float>(h->M, nt);
     h->fused = h->P == 1 && (h->fp64 ? nl_fused_supported<double>(nt) : nl_fused_supported<float>(nt));
     if (e == cudaSuccess && h->fused) e = h->fp64 ? nl_fused_setup<double>(nt) : nl_fused_setup<float>(nt);
+    h->pair = !h->fused && h->P == 2 && (h->fp64 ? nl_pair_supported<double>(nt) : nl_pair_supported<float>(nt));
+    if (e == cudaSuccess && h->pair) e = h->fp64 ? nl_pair_setup<double>(nt) : nl_pair_setup<float>(nt);
     if (e == cudaSuccess) {
         double k[20], b = 1.0;
         for (int n = 1; n <= 20; n++) { b *= (0.5 - (n - 1)) / n; k[n - 1] = b; }
@@ -508,6 +510,21 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
     // without Kerr the Raman response is never used: the fused stage applies
     const bool fused = h->fused && (raman_scan || !raman || !kerr_on);
     if (tape && !fused) return fail(h, GS_ERR_UNSUPPORTED, "recording the RK4 stages needs rows that fit one CTA");
+    if (h->pair && !tape && (raman_scan || !raman || !kerr_on)) {   // rows over two CTAs (gs_nl_pair.cu)
+        pa.row_ion = h->row_ion;
+        sa.row_ion = h->row_ion;
+        for (int s = 0; s < 4; s++) {
+            FftArgs<Rl> f1 = fa;
+            f1.rows = nr; f1.kp = KP;
+            f1.cdz = (Rl)((s == 0) ? 0.0 : (s < 3 ? dz * 0.5 : dz));
+            f1.track_max = (s == 0);
+            CK(h, launch_nl_pair_front<Rl>(f1, pa, A, nr, h->st, &h->launches));
+            SpecArgs<Rl> s2 = sa;
+            s2.stage = s;
+            CK(h, launch_nl_pair_back<Rl>(fa, s2, nr, h->st, &h->launches));
+        }
+        return GS_OK;
+    }
     if (fused) {
         pa.row_ion = h->row_ion;   // written by each front launch, read by its back launch
         sa.row_ion = h->row_ion;

@@ -23,6 +23,7 @@ struct gs_handle {
     int nr = 0, nt = 0, P = 1, M = 0, logM = 0;
     bool fp64 = true;
     bool fused = false;        // one-CTA rows: the fused front/back kernels per RK4 stage
+    bool pair = false;         // rows over two CTAs (P = 2: FP32 32768, FP64 16384), gs_nl_pair.cu
     int nl_threads = 0;        // fused kernels' threads per row (0: default; gs_autotune sets it)
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;

@@ -146,6 +146,16 @@ cudaError_t launch_nl_front(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2
 template <typename Rl>
 cudaError_t launch_nl_back(FftArgs<Rl> f, SpecArgs<Rl> s, int rows, cudaStream_t st, long long* nl);
 
+// ---- one RK4 stage over two CTAs per row (gs_nl_pair.cu): rows of N = 2H stored in the
+// P = 2 position order, FP32 N = 32768 / FP64 N = 16384
+template <typename Rl> bool nl_pair_supported(int N);
+template <typename Rl> cudaError_t nl_pair_setup(int N);
+template <typename Rl>
+cudaError_t launch_nl_pair_front(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2<Rl>::T* A, int rows,
+                                 cudaStream_t st, long long* nl);
+template <typename Rl>
+cudaError_t launch_nl_pair_back(FftArgs<Rl> f, SpecArgs<Rl> s, int rows, cudaStream_t st, long long* nl);
+
 // ---- dump reductions (gs_dumps.cu)
 template <typename Rl>
 cudaError_t launch_row_intensity(const typename Vec2<Rl>::T* E, int rows, int N, double tstep, double* maxI,
