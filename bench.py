@@ -337,7 +337,7 @@ def argon_leg(args, lrank):
            "pulses": n, "n_r": 512, "n_t": 32768, "points_per_zstep": pts, "precision": "mixed",
            "dz_m": float(dz[0]), "setup_s_device": t_setup, "value": pts * args.argon_steps / (ms / 1e3),
            "unit": UNIT, "ms_per_zstep": ms / args.argon_steps, "steps": args.argon_steps,
-           "path": "staged kernels (rows of 32768 exceed one CTA's shared memory)"}
+           "path": "pair kernels (each row of 32768 over two CTAs)"}
     B.close()
     for p in P:
         p.close()

@@ -1,6 +1,6 @@
 """The gas build on the GPU against the oracle: single-level PPT ionization with neutral
 depletion and the third harmonic (FP64 1e-10; mixed 2e-5), on the fused path (rows in one
-CTA) and the staged path (FP64 N_T = 16384: radix-2 cross pass + 8192-point rows)."""
+CTA) and the pair path (FP64 N_T = 16384: each row over two CTAs, 8192 points each)."""
 import tempfile
 
 import numpy as np

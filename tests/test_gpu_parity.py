@@ -91,7 +91,7 @@ def test_nl_step_no_raman_no_kerr():
 
 
 def test_nl_step_two_level_fft():
-    """N_T = 16384 exceeds one CTA's FP64 shared-memory row: radix-2 cross pass + 8192-point rows."""
+    """N_T = 16384 exceeds one CTA's FP64 shared-memory row: each RK4 stage over two CTAs per row."""
     T = hot_setup(n_r=4, n_t=16384, window=1.6e-12)
     O = oracle.Oracle(T)
     dz = tables.init_zstep_kerr(T, T["field"])
