@@ -538,6 +538,7 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
                 ps.tape_e = (T2*)tape->e[s];
                 ps.tape_rho = (Rl*)tape->rho[s];
                 ps.tape_q = (Rl*)tape->q[s];
+                ps.row_ion = tape->ion[s];   // the stage's row flags are kept for the adjoint
             }
             const bool tm = h->time_nl && !tape;
             if (tm) CK(h, cudaEventRecord(h->nl_ev[3 * s], h->st));
@@ -545,6 +546,7 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
             if (tm) CK(h, cudaEventRecord(h->nl_ev[3 * s + 1], h->st));
             SpecArgs<Rl> s2 = sa;
             s2.stage = s;
+            if (tape) s2.row_ion = tape->ion[s];
             CK(h, launch_nl_back<Rl>(fa, s2, nr, h->st, &h->launches));
             if (tm) CK(h, cudaEventRecord(h->nl_ev[3 * s + 2], h->st));
         }

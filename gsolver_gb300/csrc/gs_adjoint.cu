@@ -38,7 +38,9 @@ struct AdjLayout {
     int K, nck;
     size_t work_bytes() const { return 6 * nel * esz; }
     size_t ck_bytes() const { return (size_t)(nck > 1 ? nck - 1 : 0) * 2 * nel * esz; }   // the last segment is recorded
-    size_t tape_step_bytes() const { return 4 * nel * (esz + 2 * rsz); }
+    int nr;
+    size_t ion_bytes() const { return ((size_t)nr * 4 + 255) & ~(size_t)255; }
+    size_t tape_step_bytes() const { return 4 * (nel * (esz + 2 * rsz) + ion_bytes()); }
     size_t total() const { return work_bytes() + ck_bytes() + (size_t)K * tape_step_bytes(); }
 };
 
@@ -80,6 +82,8 @@ GsTape tape_of(const AdjLayout& L, char* base, int slot) {
         s += L.nel * L.rsz;
         t.q[k] = s;
         s += L.nel * L.rsz;
+        t.ion[k] = (int*)s;
+        s += L.ion_bytes();
     }
     return t;
 }
@@ -181,6 +185,7 @@ int stage_vjps(gs_handle* h, const AdjPtrs& P, const GsTape& tp, double dz) {
         a.tape_e = (const T2*)tp.e[s];
         a.tape_rho = (const Rl*)tp.rho[s];
         a.tape_q = (const Rl*)tp.q[s];
+        a.tape_ion = tp.ion[s];
         a.ab_add = s != 3;
         a.kb_out = (s > 0) ? (T2*)P.KB : nullptr;
         a.cR = cR_next[s];
@@ -296,6 +301,7 @@ int gs_gradient(gs_handle* h, const double* field_in, int n_steps, const double*
     CK(h, cudaSetDevice(h->p.device));
     AdjLayout L;
     L.nel = (size_t)h->nr * h->nt;
+    L.nr = h->nr;
     L.esz = h->esz;
     L.rsz = h->esz / 2;
     L.K = checkpoint_stride > 0 ? checkpoint_stride : (int)std::ceil(std::sqrt((double)n_steps));
@@ -367,6 +373,7 @@ int gs_adjoint_step(gs_handle* h, double dz_rk, double dz_lin, double* field_bar
     CK(h, cudaSetDevice(h->p.device));
     AdjLayout L;
     L.nel = (size_t)h->nr * h->nt;
+    L.nr = h->nr;
     L.esz = h->esz;
     L.rsz = h->esz / 2;
     L.K = 1;

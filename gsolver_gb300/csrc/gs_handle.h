@@ -16,6 +16,7 @@ struct GsTape {
     void* e[4];
     void* rho[4];
     void* q[4];
+    int* ion[4];   // per row: the stage's row ionizes (0: rho stays 0 and W = dW = 0 along it)
 };
 
 struct gs_handle {

@@ -81,6 +81,8 @@ template <typename Rl> struct VjpArgs {
     double kb_scale;
     const typename Vec2<Rl>::T* tape_e;   // the stage's E/N, rho, Q (natural time order)
     const Rl *tape_rho, *tape_q;
+    const int* tape_ion;                  // per row: the stage's row ionizes (0: loss, plasma and
+                                          // density terms of the adjoint are exactly 0), or null
     const typename Vec2<Rl>::T* pf;       // PLASMA_FUNC (position order)
     const Rl* kerr;                       // KERR_PROFILE (position order)
     const Rl* rate;                       // IONIZATION_RATE_LN

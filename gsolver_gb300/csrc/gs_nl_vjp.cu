@@ -136,6 +136,11 @@ __global__ void __launch_bounds__(512) nl_vjp_kernel(VjpArgs<Rl> v) {
     const Rl U = (Rl)v.ionization_potential, Pc = (Rl)v.ponderomotive, AV = (Rl)v.avalanche_cs;
     const Rl invND = (Rl)1 / ND, invTAU = (Rl)1 / (Rl)v.recombination_tau;
 
+    // A row that did not ionize in this stage (no sample above the rate table: W = dW = 0,
+    // rho = 0) has s = ds = 0 in the loss term, rho E = 0 and d rho / d I = 0: the loss, plasma
+    // and density-adjoint passes below add exact zeros there and are skipped.
+    const bool ion = v.tape_ion ? v.tape_ion[blockIdx.x] != 0 : true;
+    if (ion) {
     // ---- loss: l = IFFT(kb); loss_t = s(I_t) E_t for 0 < t < N-1 above the (log) threshold
     for (int p = tid; p < N; p += nthr) {
         const T2 k = kb[p];
@@ -241,6 +246,7 @@ __global__ void __launch_bounds__(512) nl_vjp_kernel(VjpArgs<Rl> v) {
         if (c + 1 < nthr) Ib[pad32(t0 + L - 1)] += bnd[c + 1];
     }
     __syncthreads();
+    }   // ion
 
     // ---- ybar = FFT(E_bar + 2 I_bar E) / N, then the RK4 bookkeeping
     for (int t = tid; t < N; t += nthr) {
