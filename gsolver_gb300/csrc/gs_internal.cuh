@@ -37,6 +37,17 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, doub
     atomicMax(addr, (unsigned long long)__double_as_longlong(v));
 }
 
+// Asynchronous prefetch of a row into L2 (cp.async.bulk.prefetch): lanes 0..3 of the calling
+// warp each request a quarter (other lane values request nothing).  p 16-byte aligned, bytes
+// a multiple of 64.
+__device__ __forceinline__ void prefetch_row_l2(const void* p, size_t bytes, int lane) {
+    if (lane >= 0 && lane < 4) {
+        const size_t q = bytes / 4;
+        const char* a = static_cast<const char*>(p) + lane * q;
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((unsigned)q) : "memory");
+    }
+}
+
 // ------------------------------------------------------------------ register DFTs --
 // Constant 16th roots of unity, cos / sin(2*pi*j/16) for j = 0..7.
 __device__ __forceinline__ double root16c(int j) {

@@ -22,6 +22,8 @@ template <typename Rl> struct FftArgs {
     const typename Vec2<Rl>::T* e;           // time-domain field (TPOST_DIVN_MULE)
     int threads;                             // fused kernels: threads per row (0: N/16, capped)
     const typename Vec2<Rl>::T* twb;         // per-stage base twiddles (tw_base_offset) or null
+    int ahead;                               // fused kernels: rows resident at once; each CTA
+                                             // prefetches into L2 the inputs of row + ahead
 };
 
 template <typename Rl> struct PlasmaArgs {

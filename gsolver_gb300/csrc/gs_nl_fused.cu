@@ -101,6 +101,12 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
         if ((tid & 31) == 0) atomic_max_nonneg(f.max_out, (double)lmax);
     }
     __syncthreads();
+    // the row that takes this SM's next slot: its inputs travel to L2 while this row computes
+    if (tid < 32 && f.ahead > 0 && (int)blockIdx.x + f.ahead < f.rows) {
+        const size_t nbase = base + (size_t)f.ahead * N;
+        prefetch_row_l2(A + nbase, (size_t)N * sizeof(T2), tid);
+        if (f.cdz != 0) prefetch_row_l2(f.kp + nbase, (size_t)N * sizeof(T2), tid - 4);
+    }
     const TwTab<Rl> tw{twh, twl, f.twb};
     if constexpr (LOGN > 0) smem_fft_ct<+1, Rl, LOGN>(E, tw, 1, tid, nthr);
     else smem_fft<+1, Rl>(E, N, f.logM, tw, 1, tid, nthr);
@@ -371,6 +377,19 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_back_kernel(F
                 for (int q = tid; q < N; q += nthr) buf[pad16((q % nthr) * L + q / nthr)] = in[base + q];
             }
             __syncthreads();
+            if (src == first && tid < 32 && f.ahead > 0 && (int)blockIdx.x + f.ahead < f.rows) {
+                // the next row of this SM: its sources and RK4 sums travel to L2 meanwhile
+                const int nr2 = blockIdx.x + f.ahead;
+                const size_t nbase = (size_t)nr2 * N, rb = (size_t)N * sizeof(T2);
+                const bool nion = s.row_ion ? s.row_ion[nr2] != 0 : true;
+                if (s.kerr_on) prefetch_row_l2(s.u3 + nbase, rb, tid);
+                if (s.stage > 0) prefetch_row_l2(s.nb + nbase, rb, tid - 4);
+                if (nion) {
+                    prefetch_row_l2(s.u1 + nbase, rb, tid - 8);
+                    prefetch_row_l2(s.u2 + nbase, rb, tid - 12);
+                    prefetch_row_l2(acc + nbase, rb, tid - 16);
+                }
+            }
             if constexpr (LOGN > 0) smem_fft_ct<-1, Rl, LOGN>(buf, tw, 1, tid, nthr);
             else smem_fft<-1, Rl>(buf, N, f.logM, tw, 1, tid, nthr);
         }
@@ -469,22 +488,46 @@ template <typename Rl> cudaError_t nl_fused_setup(int N) {
     return e;
 }
 
+// CTAs of a kernel resident on the device at once (the prefetch distance of the fused
+// kernels); the last query per kernel is kept, since the shapes rarely change
+template <typename K> static int resident_ctas(K kern, int nthr, size_t smem) {
+    struct Last { const void* k; int nthr; size_t smem; int dev; int ctas; };
+    static thread_local Last last{nullptr, 0, 0, -1, 0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (last.k == (const void*)kern && last.nthr == nthr && last.smem == smem && last.dev == dev) return last.ctas;
+    int per = 0, sms = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, nthr, smem) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return 0;
+    }
+    last = Last{(const void*)kern, nthr, smem, dev, per * sms};
+    return last.ctas;
+}
+
 template <typename Rl>
 cudaError_t launch_nl_front(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2<Rl>::T* A, int rows, cudaStream_t st,
                             long long* nl) {
     const int nthr = f.threads > 0 ? f.threads : fused_threads<Rl>(f.N);
     const size_t sm = FrontSmem<Rl>::bytes(f.N, nthr);
+    f.rows = rows;
     bool done = false;
     if constexpr (sizeof(Rl) == 4) {
         if (f.N == 16384 && nthr == 1024) {
+            f.ahead = resident_ctas(nl_front_kernel<Rl, 14, 16>, nthr, sm);
             nl_front_kernel<Rl, 14, 16><<<rows, nthr, sm, st>>>(f, a, A);
             done = true;
         } else if (f.N == 16384) {
+            f.ahead = resident_ctas(nl_front_kernel<Rl, 14>, nthr, sm);
             nl_front_kernel<Rl, 14><<<rows, nthr, sm, st>>>(f, a, A);
             done = true;
         }
     }
-    if (!done) nl_front_kernel<Rl><<<rows, nthr, sm, st>>>(f, a, A);
+    if (!done) {
+        f.ahead = resident_ctas(nl_front_kernel<Rl>, nthr, sm);
+        nl_front_kernel<Rl><<<rows, nthr, sm, st>>>(f, a, A);
+    }
     (*nl)++;
     return cudaGetLastError();
 }
@@ -493,14 +536,19 @@ template <typename Rl>
 cudaError_t launch_nl_back(FftArgs<Rl> f, SpecArgs<Rl> s, int rows, cudaStream_t st, long long* nl) {
     const int nthr = f.threads > 0 ? f.threads : fused_threads<Rl>(f.N);
     const size_t bb = ((size_t)padded_len(f.N) + f.N / 64 + 64) * sizeof(typename Vec2<Rl>::T);
+    f.rows = rows;
     bool done = false;
     if constexpr (sizeof(Rl) == 4) {
         if (f.N == 16384) {
+            f.ahead = resident_ctas(nl_back_kernel<Rl, 14>, nthr, bb);
             nl_back_kernel<Rl, 14><<<rows, nthr, bb, st>>>(f, s);
             done = true;
         }
     }
-    if (!done) nl_back_kernel<Rl><<<rows, nthr, bb, st>>>(f, s);
+    if (!done) {
+        f.ahead = resident_ctas(nl_back_kernel<Rl>, nthr, bb);
+        nl_back_kernel<Rl><<<rows, nthr, bb, st>>>(f, s);
+    }
     (*nl)++;
     return cudaGetLastError();
 }
