@@ -67,6 +67,10 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
     Rl lmax = 0;
     const Rl cdz = (Rl)f.cdz;
     const int per = N / nthr;
+    // rows of 2^k points take the 1/N of the inverse transform on the input: scaling by a power
+    // of two is exact and commutes with every rounding of the FFT, so IFFT(X/N) = IFFT(X)/N
+    const bool pow2 = (N & (N - 1)) == 0;
+    const Rl sc = pow2 ? (Rl)1 / (Rl)N : (Rl)1;
     if (per == 16) {
         T2 v[16];
 #pragma unroll
@@ -83,7 +87,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
             for (int u = 0; u < 16; u++) { v[u].x = v[u].x + cdz * k[u].x; v[u].y = v[u].y + cdz * k[u].y; }
         }
 #pragma unroll
-        for (int u = 0; u < 16; u++) E[pad16(tid + u * nthr)] = v[u];
+        for (int u = 0; u < 16; u++) E[pad16(tid + u * nthr)] = T2{v[u].x * sc, v[u].y * sc};
     } else {
         for (int i = tid; i < N; i += nthr) {
             T2 v = A[base + i];
@@ -93,7 +97,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
                 v.x = v.x + cdz * k.x;
                 v.y = v.y + cdz * k.y;
             }
-            E[pad16(i)] = v;
+            E[pad16(i)] = T2{v.x * sc, v.y * sc};
         }
     }
     if (f.track_max) {
@@ -113,50 +117,6 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
     const Rl rn = (Rl)N;
     const Rl ND = a.k.ND, tstep = a.k.tstep, U = a.k.U, Pc = a.k.Pc, AV = a.k.AV;
     const Rl invND = a.k.invND, invTAU = a.k.invTAU;
-    // E /= N and the rates W_t (the first sample is treated as E_0 = 0: W_0 = g_0 = 0)
-    // in batches of 8 samples per thread so that the table reads (L2: the carve-out leaves
-    // little L1) are in flight together
-    const bool gas = a.gas != 0;
-    bool anyw = false;   // some sample of this thread is above the rate table's threshold
-    for (int tb = tid; tb < N; tb += 8 * nthr) {
-        int n[8];
-        Rl dl[8], Iv[8];
-#pragma unroll
-        for (int u = 0; u < 8; u++) {
-            const int t = tb + u * nthr;
-            n[u] = -1;
-            dl[u] = 0;
-            Iv[u] = 0;
-            if (t < N) {
-                T2 e = E[pad16(t)];
-                e.x = e.x / rn;
-                e.y = e.y / rn;
-                E[pad16(t)] = e;
-                Iv[u] = e.x * e.x + e.y * e.y;
-                if (t > 0) n[u] = photo_index<Rl>(Iv[u], &dl[u], a.err);
-            }
-        }
-        Rl w0[8], w1[8];
-#pragma unroll
-        for (int u = 0; u < 8; u++) {
-            w0[u] = n[u] >= 0 ? __ldg(&a.rate[n[u]]) : (Rl)0;
-            w1[u] = n[u] >= 0 ? __ldg(&a.rate[n[u] + 1]) : (Rl)0;
-        }
-#pragma unroll
-        for (int u = 0; u < 8; u++) {
-            const int t = tb + u * nthr;
-            if (t < N) {
-                const Rl W = n[u] >= 0 ? photo_rate_from<Rl>(w0[u], w1[u], dl[u]) : (Rl)0;
-                Wb[pad32(t)] = gas ? gas_rate_slot<Rl>(t, Iv[u], W) : W;
-                anyw = anyw || n[u] >= 0;
-            }
-        }
-    }
-    // W > 0 somewhere (exp of the table is positive above its threshold) or rho starting above
-    // 0: otherwise every Heun / gas step adds exactly 0 and the density stays 0 along the row
-    const bool ion = __syncthreads_or(anyw ? 1 : 0) != 0 || a.k.rho0 != (Rl)0;
-    if (tid == 0 && a.row_ion) a.row_ion[blockIdx.x] = ion ? 1 : 0;
-
     auto g_of = [&](int t) -> Rl {
         if (t == 0) return (Rl)0;
         const T2 e = E[pad16(t)];
@@ -171,6 +131,88 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
     const Rl* Wc = Wb + pad32(t0);
     auto e_at = [&](int i) -> T2 { return LC == 16 ? Ec[i] : E[pad16(t0 + i)]; };
     auto w_at = [&](int i) -> Rl { return LC == 16 ? Wc[i] : Wb[pad32(t0 + i)]; };
+    // ---- one pass over this thread's chunk: E /= N (rows whose length is not a power of two),
+    // the rates W_t (the first sample is treated as E_0 = 0: W_0 = g_0 = 0) and the Raman
+    // chunk sum z_t = a z_{t-1} + I_t.  Samples go in groups of 8; a warp computes rates only
+    // when one of its samples is at or above the table threshold (or NaN, which the rate
+    // function reports), and then issues the group's table reads together.
+    const bool gas = a.gas != 0;
+    const bool rscan = a.raman_scan != 0;
+    const T2 ra = T2{a.k.a_re, a.k.a_im};
+    bool anyw = false;   // some sample of this thread is above the rate table's threshold
+    T2 zl = T2{0, 0}, aL = T2{1, 0};
+    for (int g = 0; g < L; g += 8) {
+        Rl Iv[8];
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            Iv[u] = 0;
+            if (g + u >= L) continue;   // chunks of 2 or 4 samples (short rows)
+            T2 e = e_at(g + u);
+            if (!pow2) {
+                e.x = e.x / rn;
+                e.y = e.y / rn;
+                if (LC == 16) E[pad16(t0) + g + u] = e;
+                else E[pad16(t0 + g + u)] = e;
+            }
+            Iv[u] = e.x * e.x + e.y * e.y;
+            if (rscan) {
+                zl = cmul(ra, zl);
+                zl.x += Iv[u];
+                aL = cmul(aL, ra);
+            }
+        }
+        bool above = false;
+#pragma unroll
+        for (int u = 0; u < 8; u++) above = above || (g + u < L && t0 + g + u > 0 && !(Iv[u] < (Rl)(1e13 / 1e16)));
+        Rl W[8];
+        if (__any_sync(0xffffffffu, above)) {
+            int n[8];
+            Rl dl[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                dl[u] = 0;
+                n[u] = (g + u < L && t0 + g + u > 0) ? photo_index<Rl>(Iv[u], &dl[u], a.err) : -1;
+            }
+            Rl w0[8], w1[8];
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                w0[u] = n[u] >= 0 ? __ldg(&a.rate[n[u]]) : (Rl)0;
+                w1[u] = n[u] >= 0 ? __ldg(&a.rate[n[u] + 1]) : (Rl)0;
+            }
+#pragma unroll
+            for (int u = 0; u < 8; u++) {
+                W[u] = n[u] >= 0 ? photo_rate_from<Rl>(w0[u], w1[u], dl[u]) : (Rl)0;
+                anyw = anyw || n[u] >= 0;
+            }
+        } else {
+#pragma unroll
+            for (int u = 0; u < 8; u++) W[u] = 0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; u++) {
+            const int t = t0 + g + u;
+            if (g + u >= L) continue;
+            const Rl w = gas ? gas_rate_slot<Rl>(t, Iv[u], W[u]) : W[u];
+            if (LC == 16) Wb[pad32(t0) + g + u] = w;
+            else Wb[pad32(t)] = w;
+        }
+    }
+    // W > 0 somewhere (exp of the table is positive above its threshold) or rho starting above
+    // 0: otherwise every Heun / gas step adds exactly 0 and the density stays 0 along the row
+    const bool ion = __syncthreads_or(anyw ? 1 : 0) != 0 || a.k.rho0 != (Rl)0;
+    // Raman: an exclusive scan of the chunk sums gives each chunk's start
+    T2 zs = T2{0, 0}, zN = T2{0, 0};
+    if (rscan) {
+        if (c == 0) cend_aL[0] = aL;                   // a^L, common to all chunks
+        T2 Am = aL, Bm = zl;
+        block_affine_scan<T2>(Am, Bm, T2{1, 0}, T2{0, 0}, scA, scB);
+        cend[c] = Bm;                                   // z at the end of chunk c
+        __syncthreads();
+        zs = (c == 0) ? T2{0, 0} : cend[c - 1];
+        zN = cend[nthr - 1];
+    }
+    if (tid == 0 && a.row_ion) a.row_ion[blockIdx.x] = ion ? 1 : 0;
+
     // the exact recurrence over this thread's chunk from start value s (rho_{t0-1})
     auto run_chunk = [&](Rl s, Rl* dout) -> Rl {
         Rl ro = s, d = (Rl)1;
@@ -237,28 +279,6 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
         __syncthreads();
         if (*flag) break;
         __syncthreads();
-    }
-
-    // ---- Raman: z_t = a z_{t-1} + I_t, chunk sums then an exclusive scan of chunk starts
-    const bool rscan = a.raman_scan != 0;
-    const T2 ra = T2{a.k.a_re, a.k.a_im};
-    T2 zs = T2{0, 0}, zN = T2{0, 0};
-    if (rscan) {
-        T2 zl = T2{0, 0}, aL = T2{1, 0};
-#pragma unroll 4
-        for (int i = 0; i < L; i++) {
-            const T2 e = e_at(i);
-            zl = cmul(ra, zl);
-            zl.x += e.x * e.x + e.y * e.y;
-            aL = cmul(aL, ra);
-        }
-        if (c == 0) cend_aL[0] = aL;                   // a^L, common to all chunks
-        T2 Am = aL, Bm = zl;
-        block_affine_scan<T2>(Am, Bm, T2{1, 0}, T2{0, 0}, scA, scB);
-        cend[c] = Bm;                                   // z at the end of chunk c
-        __syncthreads();
-        zs = (c == 0) ? T2{0, 0} : cend[c - 1];
-        zN = cend[nthr - 1];
     }
 
     // ---- final pass: density, Raman Q and the three source rows
