@@ -469,7 +469,7 @@ def main():
     ms = e0.elapsed_time(e1)
     launches = P.launch_count() - n0
     q_ms, q_n = P.qdht_timing(enable=False)
-    nf_ms, nb_ms, n_st = P.nl_timing(enable=False)
+    st_ms, n_st = P.nl_timing(enable=False)
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -487,28 +487,28 @@ def main():
             "peak_kind": f"{pk_kind} cuBLAS bf16 burst", "launch_ms": per_launch_ms,
             "qdht_share_of_step": (q_ms / ms) if ms else None,
             "note": "algorithmic flop (8 N_r per field-point step); 3xTF32 executes 3x; TF32 tensor peak is half the bf16 peak"}
-    # the dominant kernel: nl_back (three FFTs of the stage's sources, spectral combination, RK4
-    # sum), HBM-bound by design; its algorithmic bytes per launch are its own input and output
-    # once each: the three source rows (24 B per field point), the RK4 sum read in stages 1-3
-    # and written (6 + 8 B on average), k written in stages 0-2 (6 B on average)
+    # the dominant kernel: nl_stage (one RK4 stage per launch: inverse FFT, plasma and Raman
+    # recurrences, forward FFT of the sources, spectral combination, RK4 sums); its algorithmic
+    # bytes per launch are its one-pass input and output: A (8 B per field point), k of the
+    # previous stage and the RK4 sum read in stages 1-3 (6 + 6 B on average), k written in
+    # stages 0-2 (6 B on average) and the RK4 sum written (8 B): 34 B in complex64
     esz = 8 if prec == gs.PREC_MIXED else 16
-    nb_launch_ms = nb_ms / n_st if n_st else None
-    nb_bytes = (44 if esz == 8 else 88) * nr * nt
-    nb_ach = nb_bytes / (nb_launch_ms / 1e3) / 1e9 if nb_launch_ms else None
-    nl_step_ms = (nf_ms + nb_ms) / n_st * 4 if n_st else None
+    st_launch_ms = st_ms / n_st if n_st else None
+    st_bytes = (34 if esz == 8 else 68) * nr * nt
+    st_ach = st_bytes / (st_launch_ms / 1e3) / 1e9 if st_launch_ms else None
+    nl_step_ms = st_ms / n_st * 4 if n_st else None
     nl_ach = (16 if esz == 8 else 32) * nr * nt / (nl_step_ms / 1e3) / 1e9 if nl_step_ms else None
-    roof = {"bound": "hbm", "kernel": "nl_back_kernel" if n_st else "staged NL kernels (not timed)",
-            "achieved": nb_ach, "peak": hbm, "unit": "GB/s", "frac": (nb_ach / hbm) if nb_ach and hbm else None,
+    roof = {"bound": "hbm", "kernel": "nl_stage_kernel" if n_st else "staged NL kernels (not timed)",
+            "achieved": st_ach, "peak": hbm, "unit": "GB/s", "frac": (st_ach / hbm) if st_ach and hbm else None,
             "traffic": read_profile_traffic("nl_fused_silica_256x16384.md") if prec == gs.PREC_MIXED else None,
-            "peak_kind": f"{pk_kind} HBM copy", "launch_ms": nb_launch_ms,
-            "algorithmic_bytes_per_launch": nb_bytes,
-            "share_of_step": (nb_ms / ms) if ms and n_st else None,
-            "front_launch_ms": (nf_ms / n_st) if n_st else None,
+            "peak_kind": f"{pk_kind} HBM copy", "launch_ms": st_launch_ms,
+            "algorithmic_bytes_per_launch": st_bytes,
+            "share_of_step": (st_ms / ms) if ms and n_st else None,
             "note": "CUDA events around each launch on the handle's stream; traffic = ncu DRAM bytes per launch of a "
                     "256-row capture scaled by rows (writes still in L2 when the kernel ends are not counted)"}
     roof_nl = {"bound": "hbm", "unit": "GB/s", "peak": hbm, "achieved": nl_ach,
                "frac": (nl_ach / hbm) if nl_ach and hbm else None, "step_ms": nl_step_ms,
-               "note": "the whole NL increment (4 RK4 stages, 8 launches) against its one-pass minimum: read A and "
+               "note": "the whole NL increment (4 RK4 stages, 4 launches) against its one-pass minimum: read A and "
                        "write the NL increment once, 16 B per field point in complex64"}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -343,12 +343,11 @@ int gsi::run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz) {
     return GS_OK;
 }
 
-int gs_nl_timing(gs_handle* h, int enable, double* ms_front, double* ms_back, int* stages) {
+int gs_nl_timing(gs_handle* h, int enable, double* ms, int* stages) {
     if (!h) return GS_ERR_ARG;
-    if (ms_front) *ms_front = h->nl_ms_front;
-    if (ms_back) *ms_back = h->nl_ms_back;
+    if (ms) *ms = h->nl_ms;
     if (stages) *stages = h->nl_stages_timed;
-    h->nl_ms_front = h->nl_ms_back = 0;
+    h->nl_ms = 0;
     h->nl_stages_timed = 0;
     h->nl_ev_pending = false;
     if (enable && !h->nl_ev[0]) {
@@ -526,8 +525,7 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
         return GS_OK;
     }
     if (fused) {
-        pa.row_ion = h->row_ion;   // written by each front launch, read by its back launch
-        sa.row_ion = h->row_ion;
+        pa.row_ion = h->row_ion;   // the row flags of the last stage (the adjoint keeps its own)
         for (int s = 0; s < 4; s++) {
             FftArgs<Rl> f1 = fa;
             f1.rows = nr; f1.kp = KP;
@@ -541,14 +539,11 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
                 ps.row_ion = tape->ion[s];   // the stage's row flags are kept for the adjoint
             }
             const bool tm = h->time_nl && !tape;
-            if (tm) CK(h, cudaEventRecord(h->nl_ev[3 * s], h->st));
-            CK(h, launch_nl_front<Rl>(f1, ps, A, nr, h->st, &h->launches));
-            if (tm) CK(h, cudaEventRecord(h->nl_ev[3 * s + 1], h->st));
             SpecArgs<Rl> s2 = sa;
             s2.stage = s;
-            if (tape) s2.row_ion = tape->ion[s];
-            CK(h, launch_nl_back<Rl>(fa, s2, nr, h->st, &h->launches));
-            if (tm) CK(h, cudaEventRecord(h->nl_ev[3 * s + 2], h->st));
+            if (tm) CK(h, cudaEventRecord(h->nl_ev[2 * s], h->st));
+            CK(h, launch_nl_stage<Rl>(f1, ps, A, s2, nr, h->st, &h->launches));
+            if (tm) CK(h, cudaEventRecord(h->nl_ev[2 * s + 1], h->st));
         }
         if (h->time_nl && !tape) h->nl_ev_pending = true;
         return GS_OK;
@@ -598,11 +593,9 @@ static int nl_step(gs_handle* h, double dz, double* max_a2, double* max_nl2) {
     CK(h, cudaStreamSynchronize(h->st));
     if (h->nl_ev_pending) {   // fold the stage kernels' event times into the gs_nl_timing totals
         for (int s = 0; s < 4; s++) {
-            float f = 0, b = 0;
-            CK(h, cudaEventElapsedTime(&f, h->nl_ev[3 * s], h->nl_ev[3 * s + 1]));
-            CK(h, cudaEventElapsedTime(&b, h->nl_ev[3 * s + 1], h->nl_ev[3 * s + 2]));
-            h->nl_ms_front += f;
-            h->nl_ms_back += b;
+            float f = 0;
+            CK(h, cudaEventElapsedTime(&f, h->nl_ev[2 * s], h->nl_ev[2 * s + 1]));
+            h->nl_ms += f;
         }
         h->nl_stages_timed += 4;
         h->nl_ev_pending = false;

@@ -48,8 +48,8 @@ struct gs_handle {
     // gs_nl_timing: events around each fused front / back launch of one NL step (start, mid,
     // end per RK4 stage), folded into the totals after the step's own synchronisation
     bool time_nl = false, nl_ev_pending = false;
-    cudaEvent_t nl_ev[12] = {};
-    double nl_ms_front = 0, nl_ms_back = 0;
+    cudaEvent_t nl_ev[8] = {};   // before / after each RK4-stage launch
+    double nl_ms = 0;
     int nl_stages_timed = 0;
     double* dump_dev = nullptr;   // 3 n_r + 2 n_t doubles of reduction output, r weights
     void* twb = nullptr;          // per-stage base twiddles of the M-point row FFTs (tw_base_offset)

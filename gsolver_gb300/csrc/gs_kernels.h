@@ -144,11 +144,12 @@ template <typename Rl> bool nl_fused_supported(int N);
 template <typename Rl> bool nl_fused_threads_ok(int N, int threads);
 template <typename Rl> int nl_fused_default_threads(int N);
 template <typename Rl> cudaError_t nl_fused_setup(int N);
+// one RK4 stage per launch: f the stage input (cdz, kp = k of the previous stage), a the
+// plasma / Raman parameters and the optional tape, s the spectral combination (kp = k of this
+// stage, written over the previous one row by row; nb the RK4 sum; u1..u3 scratch rows)
 template <typename Rl>
-cudaError_t launch_nl_front(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2<Rl>::T* A, int rows,
-                            cudaStream_t st, long long* nl);
-template <typename Rl>
-cudaError_t launch_nl_back(FftArgs<Rl> f, SpecArgs<Rl> s, int rows, cudaStream_t st, long long* nl);
+cudaError_t launch_nl_stage(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2<Rl>::T* A, SpecArgs<Rl> s,
+                            int rows, cudaStream_t st, long long* nl);
 
 // ---- one RK4 stage over two CTAs per row (gs_nl_pair.cu): rows of N = 2H stored in the
 // P = 2 position order, FP32 N = 32768 / FP64 N = 16384

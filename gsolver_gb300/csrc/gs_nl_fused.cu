@@ -1,17 +1,19 @@
-// gs_nl_fused.cu -- one RK4 stage of calculate_NLstep in two kernels per row, for rows that
-// fit one CTA's shared memory (N_t <= 16384 complex float / 8192 complex double).
+// gs_nl_fused.cu -- one RK4 stage of calculate_NLstep in one kernel, one CTA per row, for rows
+// that fit one CTA's shared memory (N_t <= 16384 complex float / 8192 complex double).
 //
-//   nl_front_kernel  stage input X = A + c dz k_prev, E = IFFT(X)/N_t (shared memory),
-//                    then with E resident: photoionization rates, the Heun carrier-density
-//                    recurrence by multiple shooting (ionization.cpp:9-95), the Raman
-//                    response as an exact one-pole recurrence (solver_main.cpp:401-413,
-//                    propagator.cu:697-705), and the three source rows
-//                    loss(t), rho(t) E(t), Q(t) E(t) written once.
-//   nl_back_kernel   FFT of the three sources in turn, N = FFT(loss) + PLASMA_FUNC FFT(rho E)
-//                    - j KERR_PROFILE FFT(Q E) (propagator.cu:679-710), and the RK4
-//                    accumulation of calculate_NLstep (propagator.cu:386-421) with max |N|^2.
-// Versus the separate kernels this removes the E round trip and every pass of the
-// recurrences over global memory: per stage ~88 B per field point of HBM traffic.
+//   nl_stage_kernel  first half: stage input X = A + c dz k_prev, E = IFFT(X)/N_t (shared
+//                    memory), then with E resident: photoionization rates, the Heun
+//                    carrier-density recurrence by multiple shooting (ionization.cpp:9-95), the
+//                    Raman response as an exact one-pole recurrence (solver_main.cpp:401-413,
+//                    propagator.cu:697-705), and the sources loss(t), rho(t) E(t), Q(t) E(t);
+//                    second half: N = FFT(loss) + PLASMA_FUNC FFT(rho E) - j KERR_PROFILE
+//                    FFT(Q E) (propagator.cu:679-710) and the RK4 accumulation of
+//                    calculate_NLstep (propagator.cu:386-421) with max |N|^2.
+// The Kerr source replaces E in shared memory and is transformed there; the loss and plasma
+// sources exist only on rows that ionize, which store them and read them back.  Per stage a
+// row without ionization reads A, k_prev and the RK4 sum and writes k and the RK4 sum.
+#include <type_traits>
+
 #include "gs_internal.cuh"
 #include "gs_kernels.h"
 #include "gs_plasma.cuh"
@@ -41,8 +43,9 @@ template <> __device__ __forceinline__ float qdiv<float>(float a, float b) { ret
 // thread's chunk is 16 consecutive samples starting at a multiple of 16 and its shared-memory
 // slots are at constant offsets (pad16(t0 + i) = pad16(t0) + i, pad32(t0 + i) = pad32(t0) + i).
 template <typename Rl, int LOGN = 0, int LC = 0>
-__global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(FftArgs<Rl> f, PlasmaArgs<Rl> a,
-                                                                              const typename Vec2<Rl>::T* __restrict__ A) {
+__global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(FftArgs<Rl> f, PlasmaArgs<Rl> a,
+                                                                              const typename Vec2<Rl>::T* __restrict__ A,
+                                                                              SpecArgs<Rl> sp) {
     using T2 = C2<Rl>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int N = LOGN > 0 ? (1 << LOGN) : f.N;
@@ -110,6 +113,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
         const size_t nbase = base + (size_t)f.ahead * N;
         prefetch_row_l2(A + nbase, (size_t)N * sizeof(T2), tid);
         if (f.cdz != 0) prefetch_row_l2(f.kp + nbase, (size_t)N * sizeof(T2), tid - 4);
+        if (sp.stage > 0) prefetch_row_l2(sp.nb + nbase, (size_t)N * sizeof(T2), tid - 8);
     }
     const TwTab<Rl> tw{twh, twl, f.twb};
     if constexpr (LOGN > 0) smem_fft_ct<+1, Rl, LOGN>(E, tw, 1, tid, nthr);
@@ -285,6 +289,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
     {
         Rl ro = s_start[c], d = 1;
         Rl W0 = (t0 > 0) ? Wb[pad32(t0 - 1)] : (Rl)0, g0 = (t0 > 0) ? g_of(t0 - 1) : (Rl)0;
+        __syncthreads();   // every chunk has read its left neighbour's last sample: E is rewritten below
         T2 z = zs;
         T2 pw = T2{0, 0};
         if (rscan) {
@@ -343,14 +348,16 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
                 src3.x += h.x;
                 src3.y += h.y;
             }
-            // source rows in chunk-interleaved order (sample c L + i at i nthr + c): the warp's
-            // stores are coalesced; nl_back undoes the order when it stages the row
-            const size_t q = base + (size_t)i * nthr + c;
-            if (ion || !a.row_ion) {   // zero rows are not written: nl_back skips their FFTs
+            // loss and plasma source rows in chunk-interleaved order (sample c L + i at i nthr + c):
+            // the warp's stores are coalesced, and the order is undone when they are staged below;
+            // rows without ionization have neither.  The Kerr source takes E's place.
+            if (ion) {
+                const size_t q = base + (size_t)i * nthr + c;
                 a.u1[q] = loss;
                 a.u2[q] = T2{ro * e.x, ro * e.y};
             }
-            a.u3[q] = src3;
+            if (LC == 16) E[pad16(t0) + i] = src3;
+            else E[pad16(t)] = src3;
             if (a.tape_e) {   // what the adjoint of this stage reads back
                 a.tape_e[base + t] = e;
                 a.tape_rho[base + t] = ro;
@@ -358,115 +365,96 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_front_kernel(
             }
         }
     }
-}
 
-// shared memory of nl_back_kernel: padded row + twiddles
-template <typename Rl, int LOGN = 0>
-__global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_back_kernel(FftArgs<Rl> f, SpecArgs<Rl> s) {
-    using T2 = C2<Rl>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const int N = LOGN > 0 ? (1 << LOGN) : f.N;
-    const int tid = threadIdx.x, nthr = blockDim.x;
-    T2* buf = reinterpret_cast<T2*>(smem_raw);
-    T2* twh = buf + padded_len(N);
-    T2* twl = twh + N / 64;
-    const size_t base = (size_t)blockIdx.x * N;
-    load_twiddles<Rl>(twh, twl, f.tw, N, tid, nthr);
-    const TwTab<Rl> tw{twh, twl, f.twb};
-    T2* acc = s.kp;   // the new k doubles as the accumulator of the three spectra
-    Rl lmax = 0;
-    // a row without ionization has loss = rho E = 0: only the Kerr source (FFT(0) = 0 adds
-    // nothing), or, with Kerr off, no source at all (k = 0: one pass with a zero spectrum)
-    const bool ion = s.row_ion ? s.row_ion[blockIdx.x] != 0 : true;
-    const int lastsrc = s.kerr_on ? 2 : 1;
-    const int first = ion ? 0 : lastsrc;
-    const bool zero_src = !ion && !s.kerr_on;
-    for (int src = first; src <= lastsrc; src++) {
-        const T2* in = src == 0 ? s.u1 : (src == 1 ? s.u2 : s.u3);
-        if (!zero_src) {
-            // the rows arrive in nl_front's chunk-interleaved order: position u nthr + c holds
-            // sample c L + u (L = N / nthr; the same launch shape runs both kernels)
-            const int L = N / nthr;
-            if (L == 16) {
-                T2 v[16];
+    // ---- second half: the spectra of the sources, their combination and the RK4 sums
+    __syncthreads();   // the Kerr source is complete in E
+    T2* acc = sp.kp;   // k of this stage; on rows that ionize first FFT(loss)
+    const bool kerr = sp.kerr_on != 0;
+    auto fwd = [&]() {
+        if constexpr (LOGN > 0) smem_fft_ct<-1, Rl, LOGN>(E, tw, 1, tid, nthr);
+        else smem_fft<-1, Rl>(E, N, f.logM, tw, 1, tid, nthr);
+    };
+    auto stage_row = [&](const T2* in) {   // a source row in chunk-interleaved order into E
+        if (L == 16) {
+            T2 v[16];
 #pragma unroll
-                for (int u = 0; u < 16; u++) v[u] = in[base + tid + u * nthr];
+            for (int u = 0; u < 16; u++) v[u] = in[base + tid + u * nthr];
 #pragma unroll
-                for (int u = 0; u < 16; u++) buf[pad16(tid * 16 + u)] = v[u];
-            } else {
-                for (int q = tid; q < N; q += nthr) buf[pad16((q % nthr) * L + q / nthr)] = in[base + q];
-            }
-            __syncthreads();
-            if (src == first && tid < 32 && f.ahead > 0 && (int)blockIdx.x + f.ahead < f.rows) {
-                // the next row of this SM: its sources and RK4 sums travel to L2 meanwhile
-                const int nr2 = blockIdx.x + f.ahead;
-                const size_t nbase = (size_t)nr2 * N, rb = (size_t)N * sizeof(T2);
-                const bool nion = s.row_ion ? s.row_ion[nr2] != 0 : true;
-                if (s.kerr_on) prefetch_row_l2(s.u3 + nbase, rb, tid);
-                if (s.stage > 0) prefetch_row_l2(s.nb + nbase, rb, tid - 4);
-                if (nion) {
-                    prefetch_row_l2(s.u1 + nbase, rb, tid - 8);
-                    prefetch_row_l2(s.u2 + nbase, rb, tid - 12);
-                    prefetch_row_l2(acc + nbase, rb, tid - 16);
-                }
-            }
-            if constexpr (LOGN > 0) smem_fft_ct<-1, Rl, LOGN>(buf, tw, 1, tid, nthr);
-            else smem_fft<-1, Rl>(buf, N, f.logM, tw, 1, tid, nthr);
+            for (int u = 0; u < 16; u++) E[pad16(tid * 16 + u)] = v[u];
+        } else {
+            for (int q = tid; q < N; q += nthr) E[pad16((q % nthr) * L + q / nthr)] = in[base + q];
         }
-        const bool last = src == lastsrc;
-        // batches of SB points per thread: every global read of a batch is issued before use
-        constexpr int SB = 4;
+        __syncthreads();
+    };
+    // source j = 0: Q E (in E already), 1: loss, 2: rho E (rows that ionize only).  On those
+    // rows FFT(Q E) waits in U3 and FFT(loss) in k while the next source uses the row; the
+    // last spectrum stays in E for the combination
+    for (int j = 0; j < 3; j++) {
+        if (!(j == 0 ? kerr : ion)) continue;
+        if (j > 0) stage_row(j == 1 ? sp.u1 : sp.u2);
+        fwd();
+        if (ion && j < 2) {
+            T2* keep = (j == 0) ? sp.u3 : acc;
+            for (int p = tid; p < N; p += nthr) keep[base + p] = E[pad16(p)];
+            __syncthreads();
+        }
+    }
+    // N = FFT(loss) + PLASMA_FUNC FFT(rho E) - j KERR_PROFILE FFT(Q E), then RK4:
+    // (k1 + 2 k2 + 2 k3 + k4) / 6 accumulated in that order (propagator.cu:412).  Batches of
+    // SB points per thread: every global read of a batch is issued before use.
+    Rl nmax = 0;
+    auto combine = [&](auto ion_c) {
+        constexpr bool ION = decltype(ion_c)::value;
+        constexpr int SB = ION ? 2 : 4;
         for (int pb = tid; pb < N; pb += SB * nthr) {
-            T2 v[SB], ac[SB], o[SB], c[SB];
+            T2 v[SB], ac[SB], pf[SB], q[SB], o[SB];
+            Rl kc[SB];
 #pragma unroll
             for (int u = 0; u < SB; u++) {
                 const int p = pb + u * nthr;
                 const bool in = p < N;
-                v[u] = (in && !zero_src) ? buf[pad16(p)] : T2{0, 0};
-                ac[u] = (in && src > first) ? acc[base + p] : T2{0, 0};
-                // the spectral coefficient: PLASMA_FUNC for FFT(rho E), -j KERR_PROFILE for FFT(Q E)
-                if (src == 1) c[u] = in ? s.pf[p] : T2{0, 0};
-                else if (src == 2) c[u] = T2{(Rl)0, in ? -s.kerr[p] : (Rl)0};
-                else c[u] = T2{(Rl)1, (Rl)0};
-                o[u] = (in && last && s.stage > 0) ? s.nb[base + p] : T2{0, 0};
+                v[u] = (in && (ION || kerr)) ? E[pad16(p)] : T2{0, 0};
+                if constexpr (ION) {
+                    ac[u] = in ? acc[base + p] : T2{0, 0};
+                    pf[u] = in ? sp.pf[p] : T2{0, 0};
+                    q[u] = (in && kerr) ? sp.u3[base + p] : T2{0, 0};
+                }
+                kc[u] = (in && kerr) ? -sp.kerr[p] : (Rl)0;
+                o[u] = (in && sp.stage > 0) ? sp.nb[base + p] : T2{0, 0};
             }
 #pragma unroll
             for (int u = 0; u < SB; u++) {
                 const int p = pb + u * nthr;
                 if (p >= N) continue;
-                T2 k;
-                if (src == 0) {
-                    k = v[u];
-                } else if (src == 1) {
-                    k = cadd(ac[u], cmul(v[u], c[u]));        // FFT(loss) + FFT(rho E) PLASMA_FUNC
-                } else {
-                    k = ac[u];                                 // += -j KERR_PROFILE FFT(Q E)
-                    k.x += -c[u].y * v[u].y;
-                    k.y += c[u].y * v[u].x;
+                T2 k = T2{0, 0};
+                T2 qs = v[u];
+                if constexpr (ION) {
+                    k = cadd(ac[u], cmul(v[u], pf[u]));   // FFT(loss) + FFT(rho E) PLASMA_FUNC
+                    qs = q[u];
                 }
-                if (!last) {
-                    acc[base + p] = k;
-                    continue;
+                if (kerr) {                                 // += -j KERR_PROFILE FFT(Q E)
+                    k.x += -kc[u] * qs.y;
+                    k.y += kc[u] * qs.x;
                 }
-                // RK4: (k1 + 2 k2 + 2 k3 + k4) / 6 accumulated in that order (propagator.cu:412)
                 T2 nb;
-                if (s.stage == 0) {
+                if (sp.stage == 0) {
                     nb = k;
-                } else if (s.stage < 3) {
+                } else if (sp.stage < 3) {
                     nb = T2{o[u].x + (Rl)2 * k.x, o[u].y + (Rl)2 * k.y};
                 } else {
                     nb = T2{(o[u].x + k.x) / (Rl)6, (o[u].y + k.y) / (Rl)6};
-                    lmax = fmax(lmax, nb.x * nb.x + nb.y * nb.y);
+                    nmax = fmax(nmax, nb.x * nb.x + nb.y * nb.y);
                 }
-                s.nb[base + p] = nb;
-                if (s.stage < 3) acc[base + p] = k;
+                sp.nb[base + p] = nb;
+                if (sp.stage < 3) acc[base + p] = k;
             }
         }
-        __syncthreads();
-    }
-    if (s.stage == 3) {
-        for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
-        if ((tid & 31) == 0) atomic_max_nonneg(s.max_out, (double)lmax);
+    };
+    if (ion) combine(std::true_type{});
+    else combine(std::false_type{});
+    if (sp.stage == 3) {
+        for (int o = 16; o > 0; o >>= 1) nmax = fmax(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
+        if ((tid & 31) == 0) atomic_max_nonneg(sp.max_out, (double)nmax);
     }
 }
 
@@ -494,16 +482,12 @@ template <typename Rl> cudaError_t nl_fused_setup(int N) {
     // the attribute is a per-kernel ceiling shared by every handle of the process: set the
     // device maximum so that a handle on a smaller grid never lowers it for a larger one
     (void)N;
-    cudaError_t e = cudaFuncSetAttribute(nl_front_kernel<Rl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-    if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(nl_back_kernel<Rl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    cudaError_t e = cudaFuncSetAttribute(nl_stage_kernel<Rl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if constexpr (sizeof(Rl) == 4) {   // the FP32 rows of 16384
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(nl_front_kernel<Rl, 14, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+            e = cudaFuncSetAttribute(nl_stage_kernel<Rl, 14, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(nl_front_kernel<Rl, 14>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(nl_back_kernel<Rl, 14>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+            e = cudaFuncSetAttribute(nl_stage_kernel<Rl, 14>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     }
     return e;
 }
@@ -527,47 +511,26 @@ template <typename K> static int resident_ctas(K kern, int nthr, size_t smem) {
 }
 
 template <typename Rl>
-cudaError_t launch_nl_front(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2<Rl>::T* A, int rows, cudaStream_t st,
-                            long long* nl) {
+cudaError_t launch_nl_stage(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2<Rl>::T* A, SpecArgs<Rl> s, int rows,
+                            cudaStream_t st, long long* nl) {
     const int nthr = f.threads > 0 ? f.threads : fused_threads<Rl>(f.N);
     const size_t sm = FrontSmem<Rl>::bytes(f.N, nthr);
     f.rows = rows;
     bool done = false;
     if constexpr (sizeof(Rl) == 4) {
         if (f.N == 16384 && nthr == 1024) {
-            f.ahead = resident_ctas(nl_front_kernel<Rl, 14, 16>, nthr, sm);
-            nl_front_kernel<Rl, 14, 16><<<rows, nthr, sm, st>>>(f, a, A);
+            f.ahead = resident_ctas(nl_stage_kernel<Rl, 14, 16>, nthr, sm);
+            nl_stage_kernel<Rl, 14, 16><<<rows, nthr, sm, st>>>(f, a, A, s);
             done = true;
         } else if (f.N == 16384) {
-            f.ahead = resident_ctas(nl_front_kernel<Rl, 14>, nthr, sm);
-            nl_front_kernel<Rl, 14><<<rows, nthr, sm, st>>>(f, a, A);
+            f.ahead = resident_ctas(nl_stage_kernel<Rl, 14>, nthr, sm);
+            nl_stage_kernel<Rl, 14><<<rows, nthr, sm, st>>>(f, a, A, s);
             done = true;
         }
     }
     if (!done) {
-        f.ahead = resident_ctas(nl_front_kernel<Rl>, nthr, sm);
-        nl_front_kernel<Rl><<<rows, nthr, sm, st>>>(f, a, A);
-    }
-    (*nl)++;
-    return cudaGetLastError();
-}
-
-template <typename Rl>
-cudaError_t launch_nl_back(FftArgs<Rl> f, SpecArgs<Rl> s, int rows, cudaStream_t st, long long* nl) {
-    const int nthr = f.threads > 0 ? f.threads : fused_threads<Rl>(f.N);
-    const size_t bb = ((size_t)padded_len(f.N) + f.N / 64 + 64) * sizeof(typename Vec2<Rl>::T);
-    f.rows = rows;
-    bool done = false;
-    if constexpr (sizeof(Rl) == 4) {
-        if (f.N == 16384) {
-            f.ahead = resident_ctas(nl_back_kernel<Rl, 14>, nthr, bb);
-            nl_back_kernel<Rl, 14><<<rows, nthr, bb, st>>>(f, s);
-            done = true;
-        }
-    }
-    if (!done) {
-        f.ahead = resident_ctas(nl_back_kernel<Rl>, nthr, bb);
-        nl_back_kernel<Rl><<<rows, nthr, bb, st>>>(f, s);
+        f.ahead = resident_ctas(nl_stage_kernel<Rl>, nthr, sm);
+        nl_stage_kernel<Rl><<<rows, nthr, sm, st>>>(f, a, A, s);
     }
     (*nl)++;
     return cudaGetLastError();
@@ -576,9 +539,8 @@ cudaError_t launch_nl_back(FftArgs<Rl> f, SpecArgs<Rl> s, int rows, cudaStream_t
 #define GS_FUSED_INST(Rl)                                                                                         \
     template bool nl_fused_supported<Rl>(int);                                                                    \
     template cudaError_t nl_fused_setup<Rl>(int);                                                                 \
-    template cudaError_t launch_nl_front<Rl>(FftArgs<Rl>, PlasmaArgs<Rl>, const typename Vec2<Rl>::T*, int,        \
-                                             cudaStream_t, long long*);                                           \
-    template cudaError_t launch_nl_back<Rl>(FftArgs<Rl>, SpecArgs<Rl>, int, cudaStream_t, long long*);     \
+    template cudaError_t launch_nl_stage<Rl>(FftArgs<Rl>, PlasmaArgs<Rl>, const typename Vec2<Rl>::T*, SpecArgs<Rl>, \
+                                             int, cudaStream_t, long long*);                                      \
     template bool nl_fused_threads_ok<Rl>(int, int);                                                             \
     template int nl_fused_default_threads<Rl>(int);
 GS_FUSED_INST(double)
