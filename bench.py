@@ -359,8 +359,8 @@ def argon_leg(args, lrank):
 def adjoint_leg(args, lrank):
     """The adjoint workload: fused silica 256 x 4096, 2 mm in 1000 fixed 2 um steps, seeded
     degree-6 spectral phase on the input, J = energy in the 500-600 nm band (average_spectrum
-    radial weights).  Times gs_forward_fixed and gs_gradient (forward + sqrt(N)-checkpointed
-    adjoint) on the mixed path, both through the C ABI with host fields, and checks the
+    radial weights).  Times gs_forward_fixed and gs_gradient (forward + checkpointed adjoint,
+    the default stride: every step recorded when it fits in memory) on the mixed path, both through the C ABI with host fields, and checks the
     gradient on the first `adjoint_check_steps` steps against the FP64 adjoint and fourth-order
     central differences of the FP64 forward along one seeded direction."""
     import gsolver_gb300 as gs
@@ -386,7 +386,7 @@ def adjoint_leg(args, lrank):
     tg, (Jg, gm) = timed(lambda: Pm.gradient(A0, rk, lin, w))
     out = {"workload": "fused_silica_256x4096_adjoint", "n_r": 256, "n_t": 4096, "steps": n, "dz_m": 2e-6,
            "objective": "band energy 500-600 nm, average_spectrum radial weights",
-           "checkpoint_stride": int(np.ceil(np.sqrt(n))), "precision": "mixed",
+           "checkpoint_stride": Pm.adjoint_stride(), "precision": "mixed",
            "nl_threads_per_row": tuned[0] if tuned else "default",
            "forward_ms": tf, "gradient_ms": tg, "cost_ratio": tg / tf,
            "note": "gradient_ms = forward + adjoint (one gs_gradient call); cost_ratio = gradient / forward"}

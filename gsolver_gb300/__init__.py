@@ -37,7 +37,7 @@ ABI_FUNCTIONS = (
     "gs_setup_tables", "gs_setup_field", "gs_setup_znet", "gs_setup_destroy",
     "gs_run_config", "gs_run_last_error", "gs_dump_reductions", "gs_get_time_field",
     "gs_plasma_max_noalloc", "gs_noalloc_max_samples", "gs_noalloc_last_error",
-    "gs_forward_fixed", "gs_gradient", "gs_adjoint_step",
+    "gs_forward_fixed", "gs_gradient", "gs_adjoint_step", "gs_adjoint_stride",
     "gs_batch_create", "gs_batch_step", "gs_batch_stream", "gs_batch_launch_count", "gs_batch_last_error",
     "gs_batch_destroy", "gs_autotune", "gs_set_nl_threads", "gs_get_nl_threads", "gs_batch_autotune",
     "gs_set_apertures", "gs_setup_apertures", "gs_setup_from_config_dev",
@@ -118,6 +118,7 @@ def load_library(path: str | None = None):
     L.gs_forward_fixed.argtypes = [V, V, I, V, V, V, PD, V]
     L.gs_gradient.argtypes = [V, V, I, V, V, V, I, PD, V]
     L.gs_adjoint_step.argtypes = [V, D, D, V, V]
+    L.gs_adjoint_stride.argtypes = [V, C.POINTER(C.c_int)]
     L.gs_batch_create.argtypes = [I, C.POINTER(V), C.POINTER(V)]
     L.gs_batch_step.argtypes = [V, I, V, I]
     L.gs_batch_stream.argtypes = [V]
@@ -333,6 +334,12 @@ class Propagator:
         self._check(self.L.gs_gradient(self.h, _ptr(f), len(a), _ptr(a), _ptr(b), _ptr(w), int(checkpoint_stride),
                                        C.byref(J), _ptr(g)))
         return J.value, g
+
+    def adjoint_stride(self):
+        """Checkpoint stride of the last gradient() call (0 before the first)."""
+        k = C.c_int()
+        self._check(self.L.gs_adjoint_stride(self.h, C.byref(k)))
+        return k.value
 
     def adjoint_step(self, dz_rk, dz_lin, field_bar, spec_bar):
         """Run one step forward from the current state and map the cotangents of (FIELD,

@@ -14,14 +14,18 @@
 // Finally A_bar += H^T S_bar (BIGBUFFER2 starts as QDHT(FIELD)).  H^T is the QDHT with
 // 1/m1 in place of m1.
 //
-// Memory: sqrt(N) checkpointing.  The forward stores (FIELD, BIGBUFFER2) every K steps
-// (K = ceil(sqrt(n_steps)) unless given) and records the four RK4 stages of every step of
-// the last segment (E/N, rho, Q per sample); the backward sweep walks that segment back,
-// then re-runs each earlier segment from its checkpoint, recording its stages, and walks it
-// back.  Device memory: 6 work arrays, 2 per checkpoint and 4 (E, rho, Q) triples per step
-// of a segment.  The forward is thus run about twice in all.
+// Memory: checkpointing.  The forward stores (FIELD, BIGBUFFER2) every K steps and records
+// the four RK4 stages of every step of the last segment (E/N, rho, Q per sample); the
+// backward sweep walks that segment back, then re-runs each earlier segment from its
+// checkpoint, recording its stages, and walks it back.  Device memory: 6 work arrays, 2 per
+// checkpoint and 4 (E, rho, Q) triples per step of a segment.  The n - K steps before the
+// last segment run twice, so K is as large as memory allows: unless given, every step is
+// recorded during the forward when that fits in half of the device memory that is free (the
+// handle's own adjoint arrays counted as free), else the largest K that fits, and at least
+// ceil(sqrt(n)) (the forward then runs about twice in all).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -70,6 +74,27 @@ int ensure_adj(gs_handle* h, const AdjLayout& L, AdjPtrs* P) {
     P->ck = b + L.work_bytes();
     P->tape = P->ck + L.ck_bytes();
     return GS_OK;
+}
+
+// the checkpoint stride for n steps when none is given (see the memory note above)
+int auto_stride(gs_handle* h, AdjLayout L, int n) {
+    const int ks = (int)std::ceil(std::sqrt((double)n));
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        cudaGetLastError();
+        return ks;
+    }
+    const size_t budget = (fr + h->adj_bytes) / 2;
+    int K = n;
+    for (int it = 0; it < 64 && K > ks; it++) {
+        L.K = K;
+        L.nck = (n + K - 1) / K;
+        if (L.total() <= budget) return K;
+        const size_t fixed = L.work_bytes() + L.ck_bytes();
+        const long long fit = budget > fixed ? (long long)((budget - fixed) / L.tape_step_bytes()) : 0;
+        K = (int)std::max<long long>(ks, std::min<long long>(K - 1, fit));
+    }
+    return std::max(K, ks);
 }
 
 GsTape tape_of(const AdjLayout& L, char* base, int slot) {
@@ -304,8 +329,9 @@ int gs_gradient(gs_handle* h, const double* field_in, int n_steps, const double*
     L.nr = h->nr;
     L.esz = h->esz;
     L.rsz = h->esz / 2;
-    L.K = checkpoint_stride > 0 ? checkpoint_stride : (int)std::ceil(std::sqrt((double)n_steps));
+    L.K = checkpoint_stride > 0 ? checkpoint_stride : auto_stride(h, L, n_steps);
     if (L.K > n_steps) L.K = n_steps;
+    h->adj_stride = L.K;
     L.nck = (n_steps + L.K - 1) / L.K;
     AdjPtrs P;
     rc = ensure_adj(h, L, &P);
@@ -362,6 +388,12 @@ int gs_gradient(gs_handle* h, const double* field_in, int n_steps, const double*
     if (rc) return rc;
     if (objective_out) *objective_out = J;
     return gsi::permute_out(h, P.Ab, grad_field);
+}
+
+int gs_adjoint_stride(gs_handle* h, int* stride) {
+    if (!h || !stride) return GS_ERR_ARG;
+    *stride = h->adj_stride;
+    return GS_OK;
 }
 
 int gs_adjoint_step(gs_handle* h, double dz_rk, double dz_lin, double* field_bar, double* spec_bar) {

@@ -50,6 +50,7 @@ struct gs_handle {
     bool time_nl = false, nl_ev_pending = false;
     cudaEvent_t nl_ev[8] = {};   // before / after each RK4-stage launch
     double nl_ms = 0;
+    int adj_stride = 0;   // checkpoint stride of the last gs_gradient
     int nl_stages_timed = 0;
     double* dump_dev = nullptr;   // 3 n_r + 2 n_t doubles of reduction output, r weights
     void* twb = nullptr;          // per-stage base twiddles of the M-point row FFTs (tw_base_offset)

@@ -186,11 +186,16 @@ int gs_get_nl_threads(const gs_handle* h);
 int gs_forward_fixed(gs_handle* h, const double* field_in, int n_steps, const double* dz_rk, const double* dz_lin,
                      const double* weights, double* objective, double* field_out);
 /* J as above and grad_field = dJ/dRe(FIELD_0) + i dJ/dIm(FIELD_0) by the hand-written adjoint,
- * with checkpoints every checkpoint_stride steps (0: ceil(sqrt(n_steps))) and the steps of
- * each segment re-run from its checkpoint.  Needs rows that fit one CTA (n_t <= 8192 mixed,
+ * with checkpoints every checkpoint_stride steps and the steps of each segment but the last
+ * re-run from its checkpoint.  checkpoint_stride 0: every step recorded during the forward
+ * (no re-run) when the record fits in half of the free device memory, else the largest
+ * stride that fits, at least ceil(sqrt(n_steps)); gs_adjoint_stride reports the one used.  Needs rows that fit one CTA (n_t <= 8192 mixed,
  * <= 4096 FP64) and, with Raman on, the oscillator parameters (raman_tau, raman_omega). */
 int gs_gradient(gs_handle* h, const double* field_in, int n_steps, const double* dz_rk, const double* dz_lin,
                 const double* weights, int checkpoint_stride, double* objective, double* grad_field);
+/* The checkpoint stride of the last gs_gradient call on the handle (0 before the first; no
+ * counterpart in the reference). */
+int gs_adjoint_stride(gs_handle* h, int* stride);
 /* One step of the adjoint from the handle's current state (FIELD_n, BIGBUFFER2_n): the step
  * is run forward (the handle then holds state n+1) and the cotangents of FIELD (r,omega) and
  * BIGBUFFER2 (k,omega) after it, field_bar and spec_bar, are replaced by those before it. */

@@ -6,7 +6,8 @@ gs_adjoint_step).
 * FP64 gradient vs central differences of the GPU FP64 forward along seeded directions.
 * Mixed (3xTF32 QDHT, FP32 NL) gradient: directional derivatives within 1e-4 relative of
   the FP64 central differences.
-* sqrt(N) checkpointing: every checkpoint stride gives the bit-identical gradient.
+* checkpointing: every checkpoint stride gives the bit-identical gradient; the default
+  records every step during the forward when it fits in memory.
 * A torch.autograd.Function over the C ABI (ctypes) whose backward is gs_gradient.
 """
 import tempfile
@@ -81,8 +82,9 @@ def test_checkpoint_strides_give_identical_gradients():
     w = np.random.default_rng(1).random((T["n_r"], T["n_t"]))
     P = gs.Propagator(T, precision=gs.PREC_FP64)
     ref = None
-    for k in (0, 1, 2, 7):   # 0: ceil(sqrt(7)) = 3
+    for k in (0, 1, 2, 3, 7):   # 0: every step recorded in the forward (a few MB here)
         J, g = P.gradient(T["field"], dz_rk, dz_lin, w, checkpoint_stride=k)
+        assert P.adjoint_stride() == (k if k else 7)
         if ref is None:
             ref = (J, g)
         assert J == ref[0] and np.array_equal(g, ref[1])
