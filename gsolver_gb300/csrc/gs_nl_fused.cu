@@ -358,9 +358,9 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(
             }
             if (LC == 16) E[pad16(t0) + i] = src3;
             else E[pad16(t)] = src3;
-            if (a.tape_e) {   // what the adjoint of this stage reads back
+            if (a.tape_e) {   // what the adjoint of this stage reads back (rho only where it ionizes)
                 a.tape_e[base + t] = e;
-                a.tape_rho[base + t] = ro;
+                if (ion) a.tape_rho[base + t] = ro;
                 a.tape_q[base + t] = Q;
             }
         }

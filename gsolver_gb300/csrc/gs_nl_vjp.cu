@@ -67,24 +67,57 @@ __global__ void __launch_bounds__(512) nl_vjp_kernel(VjpArgs<Rl> v) {
     const TwTab<Rl> tw{twh, twl, v.twb};
     const int L = N / nthr;
 
+    // A row that did not ionize in this stage (no sample above the rate table: W = dW = 0,
+    // rho = 0) has s = ds = 0 in the loss term, rho E = 0 and d rho / d I = 0: the loss, plasma
+    // and density-adjoint passes below add exact zeros there and are skipped, and its E_bar
+    // (= Q q) is formed again from q, still in the row buffer, instead of kept in EBAR.
+    const bool ion = v.tape_ion ? v.tape_ion[blockIdx.x] != 0 : true;
+    // the loops over the row take SB points per thread, every global read of a batch issued
+    // before its use
+    constexpr int SB = 4;
+
     // ---- Kerr: q = IFFT(j K kb)
     if (v.kerr_on) {
-        for (int p = tid; p < N; p += nthr) {
-            const T2 k = kb[p];
-            const Rl K = v.kerr[p] * ks;
-            buf[pad16(p)] = T2{-K * k.y, K * k.x};
+        for (int pb = tid; pb < N; pb += SB * nthr) {
+            T2 k[SB];
+            Rl K[SB];
+#pragma unroll
+            for (int u = 0; u < SB; u++) {
+                const int p = pb + u * nthr;
+                k[u] = p < N ? kb[p] : T2{0, 0};
+                K[u] = p < N ? v.kerr[p] : (Rl)0;
+            }
+#pragma unroll
+            for (int u = 0; u < SB; u++) {
+                const int p = pb + u * nthr;
+                const Rl Kp = K[u] * ks;
+                if (p < N) buf[pad16(p)] = T2{-Kp * k[u].y, Kp * k[u].x};
+            }
         }
         __syncthreads();
         smem_fft<+1, Rl>(buf, N, v.logM, tw, 1, tid, nthr);
-        for (int t = tid; t < N; t += nthr) {
-            const T2 q = buf[pad16(t)], e = te[t];
-            const Rl Q = tq[t];
-            Eb[t] = T2{Q * q.x, Q * q.y};
-            Xr[pad32(t)] = e.x * q.x + e.y * q.y;
+        for (int tb = tid; tb < N; tb += SB * nthr) {
+            T2 q[SB], e[SB];
+            Rl Q[SB];
+#pragma unroll
+            for (int u = 0; u < SB; u++) {
+                const int t = tb + u * nthr;
+                const bool in = t < N;
+                q[u] = in ? buf[pad16(t)] : T2{0, 0};
+                e[u] = in ? te[t] : T2{0, 0};
+                Q[u] = (in && ion) ? tq[t] : (Rl)0;
+            }
+#pragma unroll
+            for (int u = 0; u < SB; u++) {
+                const int t = tb + u * nthr;
+                if (t >= N) continue;
+                if (ion) Eb[t] = T2{Q[u] * q[u].x, Q[u] * q[u].y};
+                Xr[pad32(t)] = e[u].x * q[u].x + e[u].y * q[u].y;
+            }
         }
     } else {
         for (int t = tid; t < N; t += nthr) {
-            Eb[t] = T2{0, 0};
+            if (ion) Eb[t] = T2{0, 0};
             Xr[pad32(t)] = 0;
         }
     }
@@ -136,10 +169,6 @@ __global__ void __launch_bounds__(512) nl_vjp_kernel(VjpArgs<Rl> v) {
     const Rl U = (Rl)v.ionization_potential, Pc = (Rl)v.ponderomotive, AV = (Rl)v.avalanche_cs;
     const Rl invND = (Rl)1 / ND, invTAU = (Rl)1 / (Rl)v.recombination_tau;
 
-    // A row that did not ionize in this stage (no sample above the rate table: W = dW = 0,
-    // rho = 0) has s = ds = 0 in the loss term, rho E = 0 and d rho / d I = 0: the loss, plasma
-    // and density-adjoint passes below add exact zeros there and are skipped.
-    const bool ion = v.tape_ion ? v.tape_ion[blockIdx.x] != 0 : true;
     if (ion) {
     // ---- loss: l = IFFT(kb); loss_t = s(I_t) E_t for 0 < t < N-1 above the (log) threshold
     for (int p = tid; p < N; p += nthr) {
@@ -249,27 +278,54 @@ __global__ void __launch_bounds__(512) nl_vjp_kernel(VjpArgs<Rl> v) {
     }   // ion
 
     // ---- ybar = FFT(E_bar + 2 I_bar E) / N, then the RK4 bookkeeping
-    for (int t = tid; t < N; t += nthr) {
-        const T2 e = te[t], eb = Eb[t];
-        const Rl i2 = 2 * Ib[pad32(t)];
-        buf[pad16(t)] = T2{eb.x + i2 * e.x, eb.y + i2 * e.y};
+    for (int tb = tid; tb < N; tb += SB * nthr) {
+        T2 e[SB], eb[SB];
+        Rl Q[SB];
+#pragma unroll
+        for (int u = 0; u < SB; u++) {
+            const int t = tb + u * nthr;
+            const bool in = t < N;
+            e[u] = in ? te[t] : T2{0, 0};
+            eb[u] = (in && ion) ? Eb[t] : T2{0, 0};
+            Q[u] = (in && !ion && v.kerr_on) ? tq[t] : (Rl)0;
+        }
+#pragma unroll
+        for (int u = 0; u < SB; u++) {
+            const int t = tb + u * nthr;
+            if (t >= N) continue;
+            if (!ion && v.kerr_on) {   // E_bar = Q q, q still in the row buffer
+                const T2 q = buf[pad16(t)];
+                eb[u] = T2{Q[u] * q.x, Q[u] * q.y};
+            }
+            const Rl i2 = 2 * Ib[pad32(t)];
+            buf[pad16(t)] = T2{eb[u].x + i2 * e[u].x, eb[u].y + i2 * e[u].y};
+        }
     }
     __syncthreads();
     smem_fft<-1, Rl>(buf, N, v.logM, tw, 1, tid, nthr);
     const Rl rn = (Rl)N, cR = (Rl)v.cR, cdz = (Rl)v.cdz;
-    for (int p = tid; p < N; p += nthr) {
-        const T2 y = buf[pad16(p)];
-        const T2 yb = T2{y.x / rn, y.y / rn};
-        T2 a = yb;
-        if (v.ab_add) {
-            const T2 o = v.ab[base + p];
-            a.x += o.x;
-            a.y += o.y;
+    for (int pb = tid; pb < N; pb += SB * nthr) {
+        T2 o[SB], r[SB];
+#pragma unroll
+        for (int u = 0; u < SB; u++) {
+            const int p = pb + u * nthr;
+            const bool in = p < N;
+            o[u] = (in && v.ab_add) ? v.ab[base + p] : T2{0, 0};
+            r[u] = (in && v.kb_out) ? v.rbar[base + p] : T2{0, 0};
         }
-        v.ab[base + p] = a;
-        if (v.kb_out) {
-            const T2 r = v.rbar[base + p];
-            v.kb_out[base + p] = T2{cR * r.x + cdz * yb.x, cR * r.y + cdz * yb.y};
+#pragma unroll
+        for (int u = 0; u < SB; u++) {
+            const int p = pb + u * nthr;
+            if (p >= N) continue;
+            const T2 y = buf[pad16(p)];
+            const T2 yb = T2{y.x / rn, y.y / rn};
+            T2 a = yb;
+            if (v.ab_add) {
+                a.x += o[u].x;
+                a.y += o[u].y;
+            }
+            v.ab[base + p] = a;
+            if (v.kb_out) v.kb_out[base + p] = T2{cR * r[u].x + cdz * yb.x, cR * r[u].y + cdz * yb.y};
         }
     }
 }
