@@ -526,9 +526,12 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
     }
     if (fused) {
         pa.row_ion = h->row_ion;   // the row flags of the last stage (the adjoint keeps its own)
+        // k of stages 0, 1, 2 in KP, E (free on this path) and NB; stage 3 reads all three and
+        // writes the RK4 sum over NB row by row
+        T2* kst[3] = {KP, E, NB};
         for (int s = 0; s < 4; s++) {
             FftArgs<Rl> f1 = fa;
-            f1.rows = nr; f1.kp = KP;
+            f1.rows = nr; f1.kp = s > 0 ? kst[s - 1] : KP;
             f1.cdz = (s == 0) ? 0.0 : (s < 3 ? dz * 0.5 : dz);
             f1.track_max = (s == 0);
             PlasmaArgs<Rl> ps = pa;
@@ -541,6 +544,7 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
             const bool tm = h->time_nl && !tape;
             SpecArgs<Rl> s2 = sa;
             s2.stage = s;
+            for (int j = 0; j < 3; j++) s2.kst[j] = kst[j];
             if (tm) CK(h, cudaEventRecord(h->nl_ev[2 * s], h->st));
             CK(h, launch_nl_stage<Rl>(f1, ps, A, s2, nr, h->st, &h->launches));
             if (tm) CK(h, cudaEventRecord(h->nl_ev[2 * s + 1], h->st));

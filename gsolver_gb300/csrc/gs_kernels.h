@@ -122,6 +122,9 @@ template <typename Rl> struct SpecArgs {
     typename Vec2<Rl>::T *nb, *kp;
     unsigned long long* max_out;
     const int* row_ion;   // fused back kernel: rows flagged 0 have only the Kerr source (or none)
+    // the fused stage kernel: k of stages 0..2, each in its own array (k of stage s is written
+    // to kst[s]; stage 3 forms the RK4 sum from them and writes nb, which may be kst[2])
+    typename Vec2<Rl>::T* kst[3];
 };
 
 template <typename Rl>

@@ -113,7 +113,10 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(
         const size_t nbase = base + (size_t)f.ahead * N;
         prefetch_row_l2(A + nbase, (size_t)N * sizeof(T2), tid);
         if (f.cdz != 0) prefetch_row_l2(f.kp + nbase, (size_t)N * sizeof(T2), tid - 4);
-        if (sp.stage > 0) prefetch_row_l2(sp.nb + nbase, (size_t)N * sizeof(T2), tid - 8);
+        if (sp.stage == 3) {
+            prefetch_row_l2(sp.kst[0] + nbase, (size_t)N * sizeof(T2), tid - 8);
+            prefetch_row_l2(sp.kst[1] + nbase, (size_t)N * sizeof(T2), tid - 12);
+        }
     }
     const TwTab<Rl> tw{twh, twl, f.twb};
     if constexpr (LOGN > 0) smem_fft_ct<+1, Rl, LOGN>(E, tw, 1, tid, nthr);
@@ -368,7 +371,6 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(
 
     // ---- second half: the spectra of the sources, their combination and the RK4 sums
     __syncthreads();   // the Kerr source is complete in E
-    T2* acc = sp.kp;   // k of this stage; on rows that ionize first FFT(loss)
     const bool kerr = sp.kerr_on != 0;
     auto fwd = [&]() {
         if constexpr (LOGN > 0) smem_fft_ct<-1, Rl, LOGN>(E, tw, 1, tid, nthr);
@@ -387,27 +389,30 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(
         __syncthreads();
     };
     // source j = 0: Q E (in E already), 1: loss, 2: rho E (rows that ionize only).  On those
-    // rows FFT(Q E) waits in U3 and FFT(loss) in k while the next source uses the row; the
-    // last spectrum stays in E for the combination
+    // rows FFT(Q E) waits in U3 and FFT(loss) in U1 (staged already) while the next source
+    // uses the row; the last spectrum stays in E for the combination
     for (int j = 0; j < 3; j++) {
         if (!(j == 0 ? kerr : ion)) continue;
         if (j > 0) stage_row(j == 1 ? sp.u1 : sp.u2);
         fwd();
         if (ion && j < 2) {
-            T2* keep = (j == 0) ? sp.u3 : acc;
+            T2* keep = (j == 0) ? sp.u3 : sp.u1;
             for (int p = tid; p < N; p += nthr) keep[base + p] = E[pad16(p)];
             __syncthreads();
         }
     }
-    // N = FFT(loss) + PLASMA_FUNC FFT(rho E) - j KERR_PROFILE FFT(Q E), then RK4:
-    // (k1 + 2 k2 + 2 k3 + k4) / 6 accumulated in that order (propagator.cu:412).  Batches of
-    // SB points per thread: every global read of a batch is issued before use.
+    // N = FFT(loss) + PLASMA_FUNC FFT(rho E) - j KERR_PROFILE FFT(Q E).  Stages 0..2 write
+    // their k; stage 3 forms (k1 + 2 k2 + 2 k3 + k4) / 6, accumulated in that order
+    // (propagator.cu:412).  Batches of SB points per thread: every global read of a batch is
+    // issued before use.
     Rl nmax = 0;
-    auto combine = [&](auto ion_c) {
+    T2* const kout = sp.stage == 0 ? sp.kst[0] : (sp.stage == 1 ? sp.kst[1] : sp.kst[2]);
+    auto combine = [&](auto ion_c, auto last_c) {
         constexpr bool ION = decltype(ion_c)::value;
+        constexpr bool last = decltype(last_c)::value;
         constexpr int SB = ION ? 2 : 4;
         for (int pb = tid; pb < N; pb += SB * nthr) {
-            T2 v[SB], ac[SB], pf[SB], q[SB], o[SB];
+            T2 v[SB], ac[SB], pf[SB], q[SB], k1[SB], k2[SB], k3[SB];
             Rl kc[SB];
 #pragma unroll
             for (int u = 0; u < SB; u++) {
@@ -415,12 +420,16 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(
                 const bool in = p < N;
                 v[u] = (in && (ION || kerr)) ? E[pad16(p)] : T2{0, 0};
                 if constexpr (ION) {
-                    ac[u] = in ? acc[base + p] : T2{0, 0};
+                    ac[u] = in ? sp.u1[base + p] : T2{0, 0};
                     pf[u] = in ? sp.pf[p] : T2{0, 0};
                     q[u] = (in && kerr) ? sp.u3[base + p] : T2{0, 0};
                 }
                 kc[u] = (in && kerr) ? -sp.kerr[p] : (Rl)0;
-                o[u] = (in && sp.stage > 0) ? sp.nb[base + p] : T2{0, 0};
+                if constexpr (last) {
+                    k1[u] = in ? sp.kst[0][base + p] : T2{0, 0};
+                    k2[u] = in ? sp.kst[1][base + p] : T2{0, 0};
+                    k3[u] = in ? sp.kst[2][base + p] : T2{0, 0};
+                }
             }
 #pragma unroll
             for (int u = 0; u < SB; u++) {
@@ -436,22 +445,26 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(
                     k.x += -kc[u] * qs.y;
                     k.y += kc[u] * qs.x;
                 }
-                T2 nb;
-                if (sp.stage == 0) {
-                    nb = k;
-                } else if (sp.stage < 3) {
-                    nb = T2{o[u].x + (Rl)2 * k.x, o[u].y + (Rl)2 * k.y};
-                } else {
-                    nb = T2{(o[u].x + k.x) / (Rl)6, (o[u].y + k.y) / (Rl)6};
-                    nmax = fmax(nmax, nb.x * nb.x + nb.y * nb.y);
+                if constexpr (!last) {
+                    kout[base + p] = k;
+                    continue;
                 }
+                T2 s = k1[u];
+                s = T2{s.x + (Rl)2 * k2[u].x, s.y + (Rl)2 * k2[u].y};
+                s = T2{s.x + (Rl)2 * k3[u].x, s.y + (Rl)2 * k3[u].y};
+                const T2 nb = T2{(s.x + k.x) / (Rl)6, (s.y + k.y) / (Rl)6};
+                nmax = fmax(nmax, nb.x * nb.x + nb.y * nb.y);
                 sp.nb[base + p] = nb;
-                if (sp.stage < 3) acc[base + p] = k;
             }
         }
     };
-    if (ion) combine(std::true_type{});
-    else combine(std::false_type{});
+    if (sp.stage == 3) {
+        if (ion) combine(std::true_type{}, std::true_type{});
+        else combine(std::false_type{}, std::true_type{});
+    } else {
+        if (ion) combine(std::true_type{}, std::false_type{});
+        else combine(std::false_type{}, std::false_type{});
+    }
     if (sp.stage == 3) {
         for (int o = 16; o > 0; o >>= 1) nmax = fmax(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
         if ((tid & 31) == 0) atomic_max_nonneg(sp.max_out, (double)nmax);
