@@ -486,7 +486,8 @@ def main():
             "frac": (achieved / bf16) if achieved else None, "traffic": read_profile_traffic() if prec == gs.PREC_MIXED else None,
             "peak_kind": f"{pk_kind} cuBLAS bf16 burst", "launch_ms": per_launch_ms,
             "qdht_share_of_step": (q_ms / ms) if ms else None,
-            "note": "algorithmic flop (8 N_r per field-point step); 3xTF32 executes 3x; TF32 tensor peak is half the bf16 peak"}
+            "note": "algorithmic flop (8 N_r per field-point step); the split FP16 operands execute 3 products "
+                    "(Hh Xh + Hh Xl + Hl Xh) at the FP16 rate, which equals the bf16 rate of the peak"}
     # the dominant kernel: nl_stage (one RK4 stage per launch: inverse FFT, plasma and Raman
     # recurrences, forward FFT of the sources, spectral combination, RK4 sums); its algorithmic
     # bytes per launch are its one-pass input and output: A (8 B per field point), k of the
@@ -513,7 +514,7 @@ def main():
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32+3xtf32" if prec == gs.PREC_MIXED else "f64",
+            "vs_baseline": None, "dtype": "f32+fp16x2" if prec == gs.PREC_MIXED else "f64",
             "data": "synthetic (seeded Gaussian pulse + 1e-4 complex noise; no dataset)",
             "config": dict(conf, precision="mixed" if prec == gs.PREC_MIXED else "fp64",
                            parallelism=f"replicas{world}", l2="inputs larger than L2 (state ~1 GB per pulse)",

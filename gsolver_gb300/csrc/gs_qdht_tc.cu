@@ -3,8 +3,10 @@
 // ht_run (qdht_plan::run_many, fhatha.cpp:218-230) is the real GEMM
 //   Y[i][c] = sum_j H(i,j) X[j][c],  H(i,j) = m1_i C(i,j) / m1_j   (folded in FP64 at set-up)
 // over the 2*n_t interleaved (re, im) float columns of a [n_r][n_t] complex array.
-// It runs as 3xTF32 with FP32 accumulation: H = Hh + Hl and X = Xh + Xl split into
-// round-to-nearest TF32 parts, D = Hh Xh + Hh Xl + Hl Xh (relative error ~2^-21).
+// It runs with split operands and FP32 accumulation, D = Hh Xh + Hh Xl + Hl Xh: on grids with
+// 2 n_t a multiple of 256 as FP16 pairs with power-of-two row / column scales (the wide-tile
+// path below), otherwise as 3xTF32 (round-to-nearest TF32 parts, relative error ~2^-21) in
+// the kernel described here.
 //
 // Persistent: one CTA per SM walks 128 (i) x 128 (c) output tiles (tile T = row tile T % MT
 // of column tile T / MT, so the row tiles of a column block run side by side and share X in
@@ -27,7 +29,9 @@
 // issued, frees TMEM and returns.
 #include <cuda.h>
 #include <cudaTypedefs.h>
+#include <cuda_fp16.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -62,6 +66,9 @@ struct TcArgs {
     const float* kt2;
     const int* kmax;
     unsigned* err;
+    // FP16 operands: Y[i][c] = hscale[i] xscale[c] (H' X')[i][c] (powers of two)
+    const float* hscale;
+    const float* xscale;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -500,50 +507,88 @@ __global__ void lstep_adj_kernel(const float2* __restrict__ fb, float2* __restri
 
 
 // ======================================================================= wide-tile path --
-// For grids with 2 n_t a multiple of 256 the X operand is split once, outside the GEMM:
-//   qdht_split_kernel  X [n_r][2 n_t] -> XhT, XlT [2 n_t][n_r] (TF32 hi / lo parts, K-major:
-//                      the row index j contiguous), with the inverse transform's window mask
-//                      applied; a 32 x 32 shared-memory transpose, coalesced both ways.
-//   qdht_tc2_kernel    the GEMM on 128 (i) x 256 (c) tiles with every operand streamed by TMA
-//                      in the 128-byte-swizzled K-major layout (no conversion in shared
-//                      memory): per 32 of K 96 KiB of TMA writes and 144 KiB of MMA reads for
-//                      128 x 256 x 32 x 3 products, against 192 KiB + 96 KiB for twice the
-//                      128-column tiles.  K-blocks of 16 in the 64-byte swizzle: 48 KiB
-//                      stages, four of them in flight.  Warp 0 TMA, warp 1 MMA issuer
-//                      (N = 256), warps 2-17 epilogue (four per TMEM lane quarter, 64 columns each).
-constexpr int BN2 = 256, BK2 = 16, STAGES2 = 4;        // K-blocks of 16 (one 64-byte swizzle row)
-constexpr int A2_BYTES = BM * BK2 * 4;                  // 8 KiB
-constexpr int B2_BYTES = BN2 * BK2 * 4;                 // 16 KiB
+// For grids with 2 n_t a multiple of 256 the operands are FP16 pairs with power-of-two scales:
+// H[i][j] = hscale[i] (Hh + Hl) (split once at set-up) and X[j][c] = xscale[c] (Xh + Xl), so
+//   Y[i][c] = hscale[i] xscale[c] (Hh Xh + Hh Xl + Hl Xh)   (FP32 accumulation)
+// with ~22 significant bits per operand, three products at the FP16 tensor rate (twice the
+// TF32 rate) and half the operand bytes of TF32 parts.
+//   qdht_split16_kernel  X [n_r][2 n_t] -> xscale and XhT, XlT [2 n_t][n_r] (K-major: the row
+//                        index j contiguous), the inverse transform's window mask applied.
+//   qdht_tc2_kernel      the GEMM on 128 (i) x 256 (c) tiles with every operand streamed by
+//                        TMA in the K-major layout with the 64-byte swizzle (no conversion in
+//                        shared memory): K-blocks of 32 (one 64-byte row), 48 KiB stages, four
+//                        in flight; tcgen05.mma.kind::f16 M = 128, N = 256, K = 16.  Warp 0
+//                        TMA, warp 1 MMA issuer, warps 2-17 epilogue (four per TMEM lane
+//                        quarter, 64 columns each), which also undoes the scales.
+constexpr int BN2 = 256, BK2 = 32, STAGES2 = 4;        // K-blocks of 32 FP16 (one 64-byte swizzle row)
+constexpr int A2_BYTES = BM * BK2 * 2;                  // 8 KiB
+constexpr int B2_BYTES = BN2 * BK2 * 2;                 // 16 KiB
 constexpr int STAGE2_BYTES = 2 * A2_BYTES + 2 * B2_BYTES;
 constexpr int NEPI2 = 16;
 constexpr int THREADS2 = 64 + 32 * NEPI2;
 constexpr int SMEM2_BYTES = STAGES2 * STAGE2_BYTES + 1024 + 256;
 
-__global__ void __launch_bounds__(256) qdht_split_kernel(const float* __restrict__ X, float* __restrict__ XhT,
-                                                         float* __restrict__ XlT, int nr, int ncols,
-                                                         const int* __restrict__ kmax) {
+// Per column c a power of two xscale[c] > max_j |X[j][c]| (1 for a zero column), then
+// X / xscale[c] = Xh + Xl in round-to-nearest FP16 parts, written K-major.  One CTA owns 32 columns: the first pass over its strip finds the column maxima,
+// the second (from L2) writes the parts through a 32 x 32 transpose.  Relative error of the
+// parts ~2^-22 of each value, or 2^-25 of its column's maximum where Xl falls below the
+// FP16 normal range.
+__global__ void __launch_bounds__(256) qdht_split16_kernel(const float* __restrict__ X, __half* __restrict__ XhT,
+                                                           __half* __restrict__ XlT, float* __restrict__ xscale,
+                                                           int nr, int ncols, const int* __restrict__ kmax) {
     __shared__ float t[32][33];
+    __shared__ float cm[8][32];
     const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
-    const int c0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        const int j = j0 + ty + 8 * k, c = c0 + tx;
-        float v = X[(size_t)j * ncols + c];
-        if (kmax && j > kmax[c >> 1]) v = 0.f;   // outside the spectral window
-        t[ty + 8 * k][tx] = v;
+    const int c0 = blockIdx.x * 32;
+    const int c = c0 + tx;
+    const int km = kmax ? kmax[c >> 1] : nr;
+    float m = 0.f;
+    for (int j = ty; j < nr; j += 8) {
+        const float v = j > km ? 0.f : X[(size_t)j * ncols + c];
+        m = fmaxf(m, fabsf(v));
+    }
+    cm[ty][tx] = m;
+    __syncthreads();
+    if (ty == 0) {
+        for (int w = 1; w < 8; w++) m = fmaxf(m, cm[w][tx]);
+        int e = 0;
+        if (m > 0.f) frexpf(m, &e);   // m = f 2^e, f in [0.5, 1): |X / 2^e| < 1
+        t[0][tx] = ldexpf(1.f, e);
+        xscale[c] = ldexpf(1.f, e);
     }
     __syncthreads();
+    float inv[4];
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-        const int c = c0 + ty + 8 * k, j = j0 + tx;
-        const float v = t[tx][ty + 8 * k];
-        const float hi = tf32_rna(v);
-        XhT[(size_t)c * nr + j] = hi;
-        XlT[(size_t)c * nr + j] = tf32_rna(v - hi);
+    for (int k = 0; k < 4; k++) inv[k] = 1.f / t[0][ty + 8 * k];   // exact: powers of two
+    __syncthreads();
+    for (int j0 = 0; j0 < nr; j0 += 32) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int j = j0 + ty + 8 * k;
+            t[ty + 8 * k][tx] = j > km ? 0.f : X[(size_t)j * ncols + c];
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            const int cc = c0 + ty + 8 * k, j = j0 + tx;
+            const float v = t[tx][ty + 8 * k] * inv[k];
+            const __half hi = __float2half_rn(v);
+            XhT[(size_t)cc * nr + j] = hi;
+            XlT[(size_t)cc * nr + j] = __float2half_rn(v - __half2float(hi));
+        }
+        __syncthreads();
     }
 }
 
-// shared-memory matrix descriptor for K-major tiles in the 64-byte swizzle: rows of 16 FP32,
+__device__ __forceinline__ void mma_f16(uint32_t tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+            tmem),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc)
+        : "memory");
+}
+
+// shared-memory matrix descriptor for K-major tiles in the 64-byte swizzle: rows of 32 FP16,
 // 8-row groups 512 B apart
 __device__ __forceinline__ uint64_t make_desc64(uint32_t saddr) {
     uint64_t d = 0;
@@ -555,14 +600,26 @@ __device__ __forceinline__ uint64_t make_desc64(uint32_t saddr) {
     return d;
 }
 
-__host__ __device__ constexpr uint32_t make_idesc_n(int n) {
-    return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+// instruction descriptor: kind::f16, D = F32, A = B = F16 (format code 0), both K-major, M = 128
+__host__ __device__ constexpr uint32_t make_idesc_f16(int n) {
+    return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 }
 
 // 32 accumulator columns of row i starting at output column cg: a plain store or the fused
 // calculate_Lstep update of BIGBUFFER2 (propagator.cu:570-625)
-__device__ __forceinline__ void epilogue_cols(const TcArgs& a, const float* v, int i, int cg, float kt2i) {
+__device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, int cg, float kt2i) {
     float* yrow = a.Y + (size_t)i * a.ncols + cg;
+    if (a.xscale) {   // FP16 operands: undo the row and column scales (exact: powers of two)
+        const float si = a.hscale[i];
+#pragma unroll
+        for (int k = 0; k < 32; k += 4) {
+            const float4 xs = *reinterpret_cast<const float4*>(a.xscale + cg + k);
+            v[k] *= si * xs.x;
+            v[k + 1] *= si * xs.y;
+            v[k + 2] *= si * xs.z;
+            v[k + 3] *= si * xs.w;
+        }
+    }
     if (a.mode != QDHT_LSTEP) {
 #pragma unroll
         for (int k = 0; k < 32; k += 4)
@@ -666,7 +723,7 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer
         if (lane == 0) {
-            constexpr uint32_t idesc = make_idesc_n(BN2);
+            constexpr uint32_t idesc = make_idesc_f16(BN2);
             for (int it = 0; it < my_tiles && !*abort_flag; it++) {
                 if (it >= 1 && !mbar_wait(acc_empty, (it - 1) & 1)) {
                     record_stall(a.err, 4096u, 0, warp);
@@ -690,12 +747,12 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
                     const uint32_t ah = smem_u32(st), al = ah + A2_BYTES;
                     const uint32_t bh = ah + 2 * A2_BYTES, bl = bh + B2_BYTES;
 #pragma unroll
-                    for (int kk = 0; kk < BK2 / 8; kk++) {
-                        const uint32_t off = kk * 32;   // 8 TF32 = 32 bytes along K inside the swizzle row
-                        mma_tf32(tmem, make_desc64(al + off), make_desc64(bh + off), idesc, acc);
+                    for (int kk = 0; kk < BK2 / 16; kk++) {
+                        const uint32_t off = kk * 32;   // 16 FP16 = 32 bytes along K inside the swizzle row
+                        mma_f16(tmem, make_desc64(al + off), make_desc64(bh + off), idesc, acc);
                         acc = 1;
-                        mma_tf32(tmem, make_desc64(ah + off), make_desc64(bl + off), idesc, 1);
-                        mma_tf32(tmem, make_desc64(ah + off), make_desc64(bh + off), idesc, 1);
+                        mma_f16(tmem, make_desc64(ah + off), make_desc64(bl + off), idesc, 1);
+                        mma_f16(tmem, make_desc64(ah + off), make_desc64(bh + off), idesc, 1);
                     }
                     mma_commit(&empty[s]);
                 }
@@ -762,10 +819,13 @@ struct QdhtTc {
     unsigned* err = nullptr;
     CUtensorMap map_hi, map_lo;
     bool have_lstep = false;
-    // wide-tile path (2 n_t a multiple of 256): X split once into K-major TF32 hi / lo parts
+    // wide-tile path (2 n_t a multiple of 256): X split once into K-major FP16 hi / lo parts
+    // of X / xscale[c], H held as FP16 hi / lo parts of H[i][j] / hscale[i]
     bool wide = false;
-    float *xhT = nullptr, *xlT = nullptr;   // [2 n_t][n_r]
-    CUtensorMap map_bh, map_bl, map_hi64, map_lo64;   // 16-float boxes in the 64-byte swizzle
+    float *xhT = nullptr, *xlT = nullptr;   // [2 n_t][n_r] halves
+    __half *hh16 = nullptr, *hl16 = nullptr;
+    float *hs = nullptr, *xs = nullptr;     // hscale[n_r], xscale[2 n_t]
+    CUtensorMap map_bh, map_bl, map_hi64, map_lo64;   // 32-half boxes in the 64-byte swizzle
     // tensor maps of the X operands seen so far (the handle's few state arrays)
     std::vector<std::pair<const float*, CUtensorMap>> xmaps;
 };
@@ -833,27 +893,31 @@ QdhtTc* qdht_tc_create(int nr, int nt, cudaStream_t st, std::string* msg) {
     q->wide = (2 * nt) % tc::BN2 == 0;
     if (q->wide) {
         const size_t ncols = 2 * (size_t)nt;
-        bool okw = cudaMalloc(&q->xhT, ncols * nr * 4) == cudaSuccess && cudaMalloc(&q->xlT, ncols * nr * 4) == cudaSuccess &&
+        bool okw = cudaMalloc(&q->xhT, ncols * nr * 2) == cudaSuccess && cudaMalloc(&q->xlT, ncols * nr * 2) == cudaSuccess &&
+                   cudaMalloc(&q->hh16, (size_t)nr * nr * 2) == cudaSuccess &&
+                   cudaMalloc(&q->hl16, (size_t)nr * nr * 2) == cudaSuccess && cudaMalloc(&q->hs, nr * 4) == cudaSuccess &&
+                   cudaMalloc(&q->xs, ncols * 4) == cudaSuccess &&
                    cudaFuncSetAttribute(tc::qdht_tc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         tc::SMEM2_BYTES) == cudaSuccess;
         for (int w = 0; okw && w < 2; w++) {
-            // [2 n_t rows c][n_r floats j]: boxes of 32 j (128 B, swizzled) x 256 c
+            // [2 n_t rows c][n_r halves j]: boxes of 32 j (64 B, swizzled) x 256 c
             cuuint64_t gdim[2] = {(cuuint64_t)nr, (cuuint64_t)ncols};
-            cuuint64_t gstride[1] = {(cuuint64_t)nr * 4};
+            cuuint64_t gstride[1] = {(cuuint64_t)nr * 2};
             cuuint32_t box[2] = {(cuuint32_t)tc::BK2, (cuuint32_t)tc::BN2};
             cuuint32_t estr[2] = {1, 1};
-            okw = enc(w ? &q->map_bl : &q->map_bh, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, w ? (void*)q->xlT : (void*)q->xhT,
+            okw = enc(w ? &q->map_bl : &q->map_bh, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2, w ? (void*)q->xlT : (void*)q->xhT,
                       gdim, gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
                       CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
         }
-        for (int w = 0; okw && w < 2; w++) {   // H hi / lo in 16-float boxes of 128 rows
+        for (int w = 0; okw && w < 2; w++) {   // H hi / lo in 32-half boxes of 128 rows
             cuuint64_t gdim[2] = {(cuuint64_t)nr, (cuuint64_t)nr};
-            cuuint64_t gstride[1] = {(cuuint64_t)nr * 4};
+            cuuint64_t gstride[1] = {(cuuint64_t)nr * 2};
             cuuint32_t box[2] = {(cuuint32_t)tc::BK2, (cuuint32_t)tc::BM};
             cuuint32_t estr[2] = {1, 1};
-            okw = enc(w ? &q->map_lo64 : &q->map_hi64, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, w ? (void*)q->hl : (void*)q->hh,
-                      gdim, gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
-                      CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+            okw = enc(w ? &q->map_lo64 : &q->map_hi64, CU_TENSOR_MAP_DATA_TYPE_FLOAT16, 2,
+                      w ? (void*)q->hl16 : (void*)q->hh16, gdim, gstride, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                      CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
         }
         if (!okw) {
             if (msg) *msg = "wide-tile QDHT set-up failed";
@@ -892,6 +956,32 @@ int qdht_tc_set_matrix(QdhtTc* q, const double* C, const double* m1, std::string
         cudaMemcpy(q->hl, hl.data(), hl.size() * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
         if (msg) *msg = "matrix upload failed";
         return 1;
+    }
+    if (q->wide) {
+        // FP16 parts of H[i][j] / hscale[i], hscale[i] the power of two above the row's largest
+        // |H|: Hh round-to-nearest, Hl the rounded remainder (computed in FP64)
+        std::vector<__half> h16((size_t)nr * nr), l16((size_t)nr * nr);
+        std::vector<float> hs(nr);
+        for (int i = 0; i < nr; i++) {
+            double m = 0;
+            for (int j = 0; j < nr; j++) m = std::max(m, std::fabs(m1[i] * C[(size_t)i + (size_t)nr * j] / m1[j]));
+            int e = 0;
+            if (m > 0) std::frexp(m, &e);
+            const double sc = std::ldexp(1.0, e);
+            hs[i] = (float)sc;
+            for (int j = 0; j < nr; j++) {
+                const double h = m1[i] * C[(size_t)i + (size_t)nr * j] / m1[j] / sc;
+                const __half hi = __float2half_rn((float)h);
+                h16[(size_t)i * nr + j] = hi;
+                l16[(size_t)i * nr + j] = __float2half_rn((float)(h - (double)__half2float(hi)));
+            }
+        }
+        if (cudaMemcpy(q->hh16, h16.data(), h16.size() * 2, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(q->hl16, l16.data(), l16.size() * 2, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(q->hs, hs.data(), nr * 4, cudaMemcpyHostToDevice) != cudaSuccess) {
+            if (msg) *msg = "matrix upload failed";
+            return 1;
+        }
     }
     return 0;
 }
@@ -947,13 +1037,16 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
     a.kt2 = q->kt2;
     a.kmax = q->kmax;
     a.err = q->err;
+    a.hscale = nullptr;
+    a.xscale = nullptr;
     if (q->wide) {
-        // split X into the K-major hi / lo operands (the window mask of the inverse applied), then
-        // the GEMM on 128 x 256 tiles
-        dim3 sg((unsigned)(a.ncols / 32), (unsigned)(q->nr / 32));
-        tc::qdht_split_kernel<<<sg, 256, 0, q->st>>>(X, q->xhT, q->xlT, q->nr, a.ncols,
-                                                     mode == QDHT_MASKED ? q->kmax : nullptr);
+        // split X into the K-major FP16 hi / lo operands and the column scales (the window mask
+        // of the inverse applied), then the GEMM on 128 x 256 tiles
+        tc::qdht_split16_kernel<<<(unsigned)(a.ncols / 32), 256, 0, q->st>>>(
+            X, (__half*)q->xhT, (__half*)q->xlT, q->xs, q->nr, a.ncols, mode == QDHT_MASKED ? q->kmax : nullptr);
         (*nlaunch)++;
+        a.hscale = q->hs;
+        a.xscale = q->xs;
         const int nt2 = (q->nr / tc::BM) * (a.ncols / tc::BN2);
         const unsigned g2 = (unsigned)(nt2 < q->sms ? nt2 : q->sms);
         tc::qdht_tc2_kernel<<<g2, tc::THREADS2, tc::SMEM2_BYTES, q->st>>>(q->map_hi64, q->map_lo64, q->map_bh, q->map_bl, a);
@@ -1013,7 +1106,7 @@ int qdht_tc_check(QdhtTc* q, std::string* msg) {
 
 void qdht_tc_destroy(QdhtTc* q) {
     if (!q) return;
-    void* ptrs[] = {q->hh, q->hl, q->kr, q->ki, q->ho, q->kt2, q->kmax, q->err, q->xhT, q->xlT};
+    void* ptrs[] = {q->hh, q->hl, q->kr, q->ki, q->ho, q->kt2, q->kmax, q->err, q->xhT, q->xlT, q->hh16, q->hl16, q->hs, q->xs};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete q;

@@ -1,4 +1,5 @@
-// gs_qdht_tc.h -- mixed-precision QDHT on the tcgen05 tensor cores (3xTF32, FP32 accumulate).
+// gs_qdht_tc.h -- mixed-precision QDHT on the tcgen05 tensor cores (split FP16 or TF32 operands,
+// FP32 accumulate).
 #pragma once
 #include <cuda_runtime.h>
 

@@ -1,7 +1,9 @@
-"""Mixed-precision path (FP32 elementwise/FFT + tcgen05 3xTF32 QDHT) vs the FP64 oracle.
+"""Mixed-precision path (FP32 elementwise/FFT + tcgen05 QDHT with split operands) vs the FP64
+oracle.
 
-Tolerances are stated per quantity: the 3xTF32 QDHT carries ~2^-21 relative error per
-product, the FP32 FFTs ~1e-7 per pass, so one transform / step is expected near 1e-6.
+Tolerances are stated per quantity: the QDHT's split operands (FP16 pairs with power-of-two
+row / column scales where 2 n_t is a multiple of 256, 3xTF32 otherwise) carry ~2^-21 relative
+error per product, the FP32 FFTs ~1e-7 per pass, so one transform / step is expected near 1e-6.
 """
 import tempfile
 
@@ -14,7 +16,7 @@ from oracle import oracle, tables
 
 pytestmark = pytest.mark.gpu
 
-QDHT_TOL = 1e-5     # one 3xTF32 transform, relative L2
+QDHT_TOL = 1e-5     # one transform, relative L2
 STEP_TOL = 1e-5     # one NL increment / one full step, relative L2
 
 
@@ -42,6 +44,30 @@ def test_qdht_tensor_cores(n_r, n_t):
     # every output tile is exercised: per-row errors stay small too
     assert max(rel(y[i], ref[i]) for i in range(0, n_r, max(1, n_r // 16))) < 10 * QDHT_TOL
     assert np.array_equal(P.qdht(x), y)   # the transform is deterministic
+
+
+@pytest.mark.parametrize("n_r,n_t", [(256, 512), (1024, 256)])
+def test_qdht_fp16_scales(n_r, n_t):
+    """The FP16 operands with their scales: columns spread over 60 decades, a zero column, a
+    column with one tiny entry, and a beam-like radial profile (large at small r, where the
+    rows of H are small): each nonzero column within the transform tolerance of the FP64
+    oracle, the zero column exactly zero."""
+    T = hot_setup(n_r=n_r, n_t=n_t)
+    rng = np.random.default_rng(5)
+    r = np.arange(n_r)[:, None] / n_r
+    x = (rng.standard_normal((n_r, n_t)) + 1j * rng.standard_normal((n_r, n_t))) * np.exp(-(r / 0.05) ** 2)
+    x += 1e-6 * (rng.standard_normal((n_r, n_t)) + 1j * rng.standard_normal((n_r, n_t)))
+    x *= 10.0 ** rng.uniform(-30, 30, n_t)[None, :]
+    x[:, 3] = 0
+    x[:, 5] = 0
+    x[n_r // 2, 5] = 1e-35
+    ref = oracle.Oracle(T).qdht(x)
+    P = gs.Propagator(T, precision=gs.PREC_MIXED)
+    y = P.qdht(x)
+    assert np.all(y[:, 3] == 0)
+    for c in range(n_t):
+        if c != 3:
+            assert rel(y[:, c], ref[:, c]) < QDHT_TOL, c
 
 
 def test_nl_step_mixed():
