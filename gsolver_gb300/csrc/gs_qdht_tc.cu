@@ -529,54 +529,78 @@ constexpr int THREADS2 = 64 + 32 * NEPI2;
 constexpr int SMEM2_BYTES = STAGES2 * STAGE2_BYTES + 1024 + 256;
 
 // Per column c a power of two xscale[c] > max_j |X[j][c]| (1 for a zero column), then
-// X / xscale[c] = Xh + Xl in round-to-nearest FP16 parts, written K-major.  One CTA owns 32 columns: the first pass over its strip finds the column maxima,
-// the second (from L2) writes the parts through a 32 x 32 transpose.  Relative error of the
-// parts ~2^-22 of each value, or 2^-25 of its column's maximum where Xl falls below the
-// FP16 normal range.
-__global__ void __launch_bounds__(256) qdht_split16_kernel(const float* __restrict__ X, __half* __restrict__ XhT,
-                                                           __half* __restrict__ XlT, float* __restrict__ xscale,
-                                                           int nr, int ncols, const int* __restrict__ kmax) {
-    __shared__ float t[32][33];
-    __shared__ float cm[8][32];
-    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;   // 32 x 8
-    const int c0 = blockIdx.x * 32;
-    const int c = c0 + tx;
-    const int km = kmax ? kmax[c >> 1] : nr;
-    float m = 0.f;
-    for (int j = ty; j < nr; j += 8) {
-        const float v = j > km ? 0.f : X[(size_t)j * ncols + c];
-        m = fmaxf(m, fabsf(v));
+// X / xscale[c] = Xh + Xl in round-to-nearest FP16 parts, written K-major.  One CTA owns a
+// strip of 16 columns: it reads the strip once into shared memory (rows of 17 floats), finds
+// the column maxima there and writes the parts as pairs of halves along j.  Relative error
+// of the parts ~2^-22 of each value, or 2^-25 of its column's maximum where Xl falls below the
+// FP16 normal range.  Dynamic shared memory: nr * 17 floats.
+constexpr int SPLIT_COLS = 16, SPLIT_THREADS = 256;
+__global__ void __launch_bounds__(SPLIT_THREADS) qdht_split16_kernel(const float* __restrict__ X,
+                                                                     __half* __restrict__ XhT,
+                                                                     __half* __restrict__ XlT,
+                                                                     float* __restrict__ xscale, int nr, int ncols,
+                                                                     const int* __restrict__ kmax) {
+    extern __shared__ float strip[];   // [nr][17]
+    __shared__ float part[SPLIT_THREADS / SPLIT_COLS][SPLIT_COLS];
+    __shared__ float inv[SPLIT_COLS];
+    const int tid = threadIdx.x;
+    const int c0 = blockIdx.x * SPLIT_COLS;
+    // load: a thread takes 4 columns (one float4) of a row, 64 rows per pass
+    {
+        const int q = tid & 3, r0 = tid >> 2;
+        const int ca = c0 + 4 * q;
+        const int k0 = kmax ? kmax[ca >> 1] : nr, k1 = kmax ? kmax[(ca >> 1) + 1] : nr;
+        constexpr int RS = SPLIT_THREADS / 4, LB = 8;   // rows per pass; loads in flight per thread
+        for (int jb = r0; jb < nr; jb += LB * RS) {
+            float4 v[LB];
+#pragma unroll
+            for (int u = 0; u < LB; u++) {
+                const int j = jb + u * RS;
+                v[u] = j < nr ? *reinterpret_cast<const float4*>(X + (size_t)j * ncols + ca) : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+            for (int u = 0; u < LB; u++) {
+                const int j = jb + u * RS;
+                if (j >= nr) break;
+                if (j > k0) { v[u].x = 0.f; v[u].y = 0.f; }   // outside the spectral window
+                if (j > k1) { v[u].z = 0.f; v[u].w = 0.f; }
+                float* d = strip + j * 17 + 4 * q;
+                d[0] = v[u].x;
+                d[1] = v[u].y;
+                d[2] = v[u].z;
+                d[3] = v[u].w;
+            }
+        }
     }
-    cm[ty][tx] = m;
     __syncthreads();
-    if (ty == 0) {
-        for (int w = 1; w < 8; w++) m = fmaxf(m, cm[w][tx]);
+    {
+        const int c = tid & (SPLIT_COLS - 1), p = tid / SPLIT_COLS;
+        float m = 0.f;
+        for (int j = p; j < nr; j += SPLIT_THREADS / SPLIT_COLS) m = fmaxf(m, fabsf(strip[j * 17 + c]));
+        part[p][c] = m;
+    }
+    __syncthreads();
+    if (tid < SPLIT_COLS) {
+        float m = 0.f;
+        for (int p = 0; p < SPLIT_THREADS / SPLIT_COLS; p++) m = fmaxf(m, part[p][tid]);
         int e = 0;
         if (m > 0.f) frexpf(m, &e);   // m = f 2^e, f in [0.5, 1): |X / 2^e| < 1
-        t[0][tx] = ldexpf(1.f, e);
-        xscale[c] = ldexpf(1.f, e);
+        const float sc = ldexpf(1.f, e);
+        xscale[c0 + tid] = sc;
+        inv[tid] = ldexpf(1.f, -e);   // exact
     }
     __syncthreads();
-    float inv[4];
-#pragma unroll
-    for (int k = 0; k < 4; k++) inv[k] = 1.f / t[0][ty + 8 * k];   // exact: powers of two
-    __syncthreads();
-    for (int j0 = 0; j0 < nr; j0 += 32) {
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const int j = j0 + ty + 8 * k;
-            t[ty + 8 * k][tx] = j > km ? 0.f : X[(size_t)j * ncols + c];
-        }
-        __syncthreads();
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            const int cc = c0 + ty + 8 * k, j = j0 + tx;
-            const float v = t[tx][ty + 8 * k] * inv[k];
-            const __half hi = __float2half_rn(v);
-            XhT[(size_t)cc * nr + j] = hi;
-            XlT[(size_t)cc * nr + j] = __float2half_rn(v - __half2float(hi));
-        }
-        __syncthreads();
+    // write: pairs (j, j + 1) of column c as half2, consecutive threads along j
+    const int half_rows = nr >> 1;
+    for (int idx = tid; idx < SPLIT_COLS * half_rows; idx += SPLIT_THREADS) {
+        const int c = idx / half_rows, jp = idx - c * half_rows;
+        const float s = inv[c];
+        const float v0 = strip[(2 * jp) * 17 + c] * s, v1 = strip[(2 * jp + 1) * 17 + c] * s;
+        const __half h0 = __float2half_rn(v0), h1 = __float2half_rn(v1);
+        const size_t o = (size_t)(c0 + c) * nr + 2 * jp;
+        *reinterpret_cast<__half2*>(XhT + o) = __halves2half2(h0, h1);
+        *reinterpret_cast<__half2*>(XlT + o) =
+            __halves2half2(__float2half_rn(v0 - __half2float(h0)), __float2half_rn(v1 - __half2float(h1)));
     }
 }
 
@@ -898,7 +922,10 @@ QdhtTc* qdht_tc_create(int nr, int nt, cudaStream_t st, std::string* msg) {
                    cudaMalloc(&q->hl16, (size_t)nr * nr * 2) == cudaSuccess && cudaMalloc(&q->hs, nr * 4) == cudaSuccess &&
                    cudaMalloc(&q->xs, ncols * 4) == cudaSuccess &&
                    cudaFuncSetAttribute(tc::qdht_tc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        tc::SMEM2_BYTES) == cudaSuccess;
+                                        tc::SMEM2_BYTES) == cudaSuccess &&
+                   (size_t)nr * 17 * 4 <= 227 * 1024 &&
+                   cudaFuncSetAttribute(tc::qdht_split16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                        nr * 17 * 4) == cudaSuccess;
         for (int w = 0; okw && w < 2; w++) {
             // [2 n_t rows c][n_r halves j]: boxes of 32 j (64 B, swizzled) x 256 c
             cuuint64_t gdim[2] = {(cuuint64_t)nr, (cuuint64_t)ncols};
@@ -1042,7 +1069,7 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
     if (q->wide) {
         // split X into the K-major FP16 hi / lo operands and the column scales (the window mask
         // of the inverse applied), then the GEMM on 128 x 256 tiles
-        tc::qdht_split16_kernel<<<(unsigned)(a.ncols / 32), 256, 0, q->st>>>(
+        tc::qdht_split16_kernel<<<(unsigned)(a.ncols / tc::SPLIT_COLS), tc::SPLIT_THREADS, (size_t)q->nr * 17 * 4, q->st>>>(
             X, (__half*)q->xhT, (__half*)q->xlT, q->xs, q->nr, a.ncols, mode == QDHT_MASKED ? q->kmax : nullptr);
         (*nlaunch)++;
         a.hscale = q->hs;
