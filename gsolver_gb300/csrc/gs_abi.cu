@@ -7,6 +7,7 @@
 // stage, U = three scratch rows per radial point (loss, rho*E, Kerr source).
 // FP64 handles hold double2, mixed handles float2 (their QDHT tables stay FP64 at
 // set-up and are split for the tensor cores).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -97,7 +98,8 @@ void* gs_stream(const gs_handle* h) { return h ? (void*)h->st : nullptr; }
 static void free_all(gs_handle* h) {
     void* ptrs[] = {h->A, h->S, h->NB, h->KP, h->E, h->U, h->tw, h->pf, h->rm, h->kerr, h->rate,
                     h->omega, h->ho, h->kt2, h->Cm, h->m1, h->wavenum, h->staging, h->perm_dev,
-                    h->err_dev, h->max_dev, h->dump_dev, h->m1inv, h->adj, h->adj_w, h->th, h->twb, h->row_ion};
+                    h->iperm_dev, h->err_dev, h->max_dev, h->dump_dev, h->m1inv, h->adj, h->adj_w, h->th, h->twb,
+                    h->row_ion};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (h->tc) gs::qdht_tc_destroy(h->tc);
     if (h->tcT) gs::qdht_tc_destroy(h->tcT);
@@ -142,7 +144,8 @@ int gs_create(const gs_params* prm, gs_handle** out) {
          al((void**)&h->omega, nt * 8) && al((void**)&h->ho, nt * 8) && al((void**)&h->kt2, nr * 8) &&
          al((void**)&h->Cm, (size_t)nr * nr * 8) && al((void**)&h->m1, nr * 8) &&
          al((void**)&h->wavenum, nt * 16) && al((void**)&h->staging, nel * 16) &&
-         al((void**)&h->perm_dev, nt * 4) && al((void**)&h->err_dev, 4) && al((void**)&h->max_dev, 16) &&
+         al((void**)&h->perm_dev, nt * 4) && al((void**)&h->iperm_dev, nt * 4) && al((void**)&h->err_dev, 4) &&
+         al((void**)&h->max_dev, 16) &&
          al((void**)&h->row_ion, (size_t)nr * 4);
     if (!ok) {
         cudaGetLastError();
@@ -152,6 +155,12 @@ int gs_create(const gs_params* prm, gs_handle** out) {
     }
     h->perm = fft_position_map(nt, h->P, h->M, h->logM);
     e = cudaMemcpy(h->perm_dev, h->perm.data(), nt * 4, cudaMemcpyHostToDevice);
+    {
+        std::vector<int> ip(nt);
+        for (int p = 0; p < nt; p++) ip[h->perm[p]] = p;
+        if (e == cudaSuccess) e = cudaMemcpy(h->iperm_dev, ip.data(), nt * 4, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->p.device);
+    }
     // twiddles exp(-2 pi i j / N)
     std::vector<double> tw(2 * (size_t)nt);
     for (int j = 0; j < nt; j++) {
@@ -385,8 +394,46 @@ static int collect_qdht_time(gs_handle* h) {
     return GS_OK;
 }
 
+// The device address of a pinned host buffer when all of [host, host + bytes) lies in one
+// pinned allocation (the driver's record of it), 16-byte aligned; else null (the copy then
+// goes through the staging buffer).
+static void* pinned_device_ptr(const void* host, size_t bytes) {
+    if (((uintptr_t)host & 15) != 0) return nullptr;
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, host) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer) return nullptr;
+    // the driver's cuPointerGetAttribute, looked up at run time (the library links no driver symbol)
+    using GetAttr = CUresult (*)(void*, CUpointer_attribute, CUdeviceptr);
+    static GetAttr get_attr = [] {
+        void* fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &fn, 4000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            fn = nullptr;
+        return (GetAttr)fn;
+    }();
+    if (!get_attr) return nullptr;
+    CUdeviceptr start = 0;
+    size_t size = 0;
+    const CUdeviceptr d = (CUdeviceptr)(uintptr_t)at.devicePointer;
+    if (get_attr(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, d) != CUDA_SUCCESS ||
+        get_attr(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, d) != CUDA_SUCCESS)
+        return nullptr;
+    if (d < start || d - start > size || size - (d - start) < bytes) return nullptr;
+    return at.devicePointer;
+}
+
 int gsi::permute_in(gs_handle* h, const double* host, void* dst) {
     const size_t nel = (size_t)h->nr * h->nt;
+    if (void* dp = pinned_device_ptr(host, nel * 16)) {   // read over the host link, no staging copy
+        cudaError_t e = h->fp64 ? launch_permute_host<double>(+1, dp, dst, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches)
+                                : launch_permute_host<float>(+1, dp, dst, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches);
+        CK(h, e);
+        return GS_OK;
+    }
     CK(h, cudaMemcpyAsync(h->staging, host, nel * 16, cudaMemcpyHostToDevice, h->st));
     cudaError_t e = h->fp64 ? launch_permute<double>(+1, h->staging, dst, h->perm_dev, h->nt, nel, h->st, &h->launches)
                             : launch_permute<float>(+1, h->staging, dst, h->perm_dev, h->nt, nel, h->st, &h->launches);
@@ -395,6 +442,13 @@ int gsi::permute_in(gs_handle* h, const double* host, void* dst) {
 }
 int gsi::permute_out(gs_handle* h, const void* src, double* host) {
     const size_t nel = (size_t)h->nr * h->nt;
+    if (void* dp = pinned_device_ptr(host, nel * 16)) {   // written over the host link
+        cudaError_t e = h->fp64 ? launch_permute_host<double>(-1, src, dp, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches)
+                                : launch_permute_host<float>(-1, src, dp, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches);
+        CK(h, e);
+        CK(h, cudaStreamSynchronize(h->st));
+        return GS_OK;
+    }
     cudaError_t e = h->fp64 ? launch_permute<double>(-1, src, h->staging, h->perm_dev, h->nt, nel, h->st, &h->launches)
                             : launch_permute<float>(-1, src, h->staging, h->perm_dev, h->nt, nel, h->st, &h->launches);
     CK(h, e);

@@ -36,6 +36,8 @@ struct gs_handle {
     double2* wavenum = nullptr;
     double2* staging = nullptr;
     int* perm_dev = nullptr;
+    int* iperm_dev = nullptr;   // natural index -> position
+    int sms = 0;
     unsigned* err_dev = nullptr;
     unsigned long long* max_dev = nullptr;
     std::vector<int> perm;

@@ -140,6 +140,10 @@ cudaError_t launch_zero_nl(const typename Vec2<Rl>::T* A, typename Vec2<Rl>::T* 
 template <typename Rl>
 cudaError_t launch_permute(int dir, const void* src, void* dst, const int* perm, int N, size_t total,
                            cudaStream_t st, long long* nlaunch);
+// the same with the FP64 side a device-mapped pinned host buffer (iperm: natural -> position)
+template <typename Rl>
+cudaError_t launch_permute_host(int dir, const void* src, void* dst, const int* iperm, int N, size_t total, int sms,
+                                cudaStream_t st, long long* nlaunch);
 
 // ---- fused RK4 stage (gs_nl_fused.cu), rows that fit one CTA's shared memory
 template <typename Rl> bool nl_fused_supported(int N);

@@ -496,6 +496,52 @@ __global__ void permute_out_kernel(const C2<Rl>* __restrict__ src, double2* __re
     }
 }
 
+// The same maps with the FP64 side in pinned host memory, read or written by the kernel over
+// the host link: that side goes in natural order (consecutive threads, consecutive 16-byte
+// elements), iperm[q] the position of natural index q; four elements in flight per thread.
+template <typename Rl>
+__global__ void permute_in_host_kernel(const double2* __restrict__ src, C2<Rl>* __restrict__ dst,
+                                       const int* __restrict__ iperm, int N, size_t total) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < total; i0 += 4 * stride) {
+        double2 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const size_t i = i0 + u * stride;
+            v[u] = i < total ? src[i] : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const size_t i = i0 + u * stride;
+            if (i >= total) break;
+            const size_t row = i / N;
+            const int q = (int)(i - row * N);
+            dst[row * N + iperm[q]] = C2<Rl>{(Rl)v[u].x, (Rl)v[u].y};
+        }
+    }
+}
+template <typename Rl>
+__global__ void permute_out_host_kernel(const C2<Rl>* __restrict__ src, double2* __restrict__ dst,
+                                        const int* __restrict__ iperm, int N, size_t total) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < total; i0 += 4 * stride) {
+        C2<Rl> v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const size_t i = i0 + u * stride;
+            if (i < total) {
+                const size_t row = i / N;
+                v[u] = src[row * N + iperm[(int)(i - row * N)]];
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const size_t i = i0 + u * stride;
+            if (i < total) dst[i] = make_double2((double)v[u].x, (double)v[u].y);
+        }
+    }
+}
+
 // ------------------------------------------------------------------ launchers --
 template <typename Rl>
 static int fft_threads(int M) {
@@ -604,6 +650,18 @@ cudaError_t launch_permute(int dir, const void* src, void* dst, const int* perm,
     return cudaGetLastError();
 }
 
+template <typename Rl>
+cudaError_t launch_permute_host(int dir, const void* src, void* dst, const int* iperm, int N, size_t total, int sms,
+                                cudaStream_t st, long long* nlaunch) {
+    const unsigned g = (unsigned)(sms > 0 ? 8 * sms : 1024);
+    if (dir > 0)
+        permute_in_host_kernel<Rl><<<g, 256, 0, st>>>((const double2*)src, (C2<Rl>*)dst, iperm, N, total);
+    else
+        permute_out_host_kernel<Rl><<<g, 256, 0, st>>>((const C2<Rl>*)src, (double2*)dst, iperm, N, total);
+    (*nlaunch)++;
+    return cudaGetLastError();
+}
+
 #define GS_INST(Rl)                                                                                          \
     template cudaError_t launch_fft<Rl>(int, const C2<Rl>*, C2<Rl>*, FftArgs<Rl>, cudaStream_t, long long*); \
     template cudaError_t fft_set_smem<Rl>(int, int);                                                              \
@@ -613,7 +671,9 @@ cudaError_t launch_permute(int dir, const void* src, void* dst, const int* perm,
     template cudaError_t launch_zero_nl<Rl>(const C2<Rl>*, C2<Rl>*, size_t, unsigned long long*,             \
                                             cudaStream_t, long long*);                                       \
     template cudaError_t launch_permute<Rl>(int, const void*, void*, const int*, int, size_t, cudaStream_t,  \
-                                            long long*);
+                                            long long*);                                                     \
+    template cudaError_t launch_permute_host<Rl>(int, const void*, void*, const int*, int, size_t, int,      \
+                                                 cudaStream_t, long long*);
 GS_INST(double)
 GS_INST(float)
 

@@ -1,0 +1,79 @@
+"""gs_set_field / gs_get_field with pinned host buffers (read and written by the permutation
+kernels over the host link) against pageable ones (through the staging copy): the device
+state and the fields read back are bit-identical, in both precisions, also for a field that
+starts inside a larger pinned block."""
+import tempfile
+
+import numpy as np
+import pytest
+
+import gsolver_gb300 as gs
+from gsolver_gb300 import configs
+from oracle import tables
+
+pytestmark = pytest.mark.gpu
+DZ = 2e-8   # one fixed step (m)
+torch = pytest.importorskip("torch")
+
+
+def setup(n_r=128, n_t=1024):
+    d = tempfile.mkdtemp(prefix="gs_io_")
+    p = configs.hot_solid(d, n_r=n_r, n_t=n_t, power_cr=20.0, tol=1e-2)
+    return tables.build(tables.Config.from_file(p), noise_seed=3, noise_sigma=1e-4)
+
+
+def pinned_like(a):
+    t = torch.empty(a.shape, dtype=torch.complex128, pin_memory=True)
+    t.numpy()[...] = a
+    return t
+
+
+@pytest.mark.parametrize("prec", [gs.PREC_MIXED, gs.PREC_FP64])
+def test_pinned_and_pageable_agree(prec):
+    T = setup()
+    rng = np.random.default_rng(1)
+    f = T["field"]
+    s = rng.standard_normal(f.shape) + 1j * rng.standard_normal(f.shape)
+    P = gs.Propagator(T, precision=prec)
+    # pageable in, pageable out
+    P.set_field(f, spec=s)
+    P.nl_step(DZ)
+    P.lstep(DZ)
+    f_ref, s_ref = P.get_field(want_spec=True)
+    # pinned in, pinned out
+    fp, sp = pinned_like(f), pinned_like(s)
+    P.set_field_ptr(fp.data_ptr(), sp.data_ptr())
+    P.nl_step(DZ)
+    P.lstep(DZ)
+    fo = torch.zeros(f.shape, dtype=torch.complex128, pin_memory=True)
+    so = torch.zeros(f.shape, dtype=torch.complex128, pin_memory=True)
+    P.get_field_ptr(fo.data_ptr(), so.data_ptr())
+    assert np.array_equal(fo.numpy(), f_ref)
+    assert np.array_equal(so.numpy(), s_ref)
+    # pinned in, pageable out and the reverse
+    P.set_field_ptr(fp.data_ptr(), sp.data_ptr())
+    a, b = P.get_field(want_spec=True)
+    assert np.array_equal(a, f.astype(np.complex64).astype(np.complex128) if prec == gs.PREC_MIXED else f)
+    P.set_field(f, spec=s)
+    fo.zero_()
+    P.get_field_ptr(fo.data_ptr(), None)
+    assert np.array_equal(fo.numpy(), a)
+
+
+def test_pinned_pointer_inside_a_larger_allocation():
+    """A field that starts inside a larger pinned block (the second half of it): the range
+    check measures from the pointer, the kernels read and write only the field's bytes."""
+    T = setup(n_r=128, n_t=512)
+    P = gs.Propagator(T, precision=gs.PREC_FP64)
+    f = T["field"]
+    P.set_field(f)
+    ref = P.get_field(want_spec=False)
+    n = f.shape[0]
+    big = torch.zeros((2 * n, f.shape[1]), dtype=torch.complex128, pin_memory=True)
+    big.numpy()[n:] = f
+    P.set_field_ptr(big[n:].data_ptr(), None)
+    assert np.array_equal(P.get_field(want_spec=False), ref)
+    big.zero_()
+    P.get_field_ptr(big[n:].data_ptr(), None)
+    assert np.array_equal(big.numpy()[n:], ref)
+    assert not big.numpy()[:n].any()   # nothing written before the pointer
