@@ -12,8 +12,8 @@ Synthetic: the pulse is generated (seeded 1e-4 complex Gaussian noise), no datas
           copies FIELD and BIGBUFFER2 in and out (the host globals propagator() works on)
   fp64    the plain FP64 GPU path on the same workload, and the mixed path's relative L2
           error against it after the same fixed-dz steps from the same start
-  roofline  the dominant kernel, nl_back (HBM-bound): its one-pass input and output (44 B per
-          field point in complex64) over its CUDA-event launch time; roofline_nl_step the
+  roofline  the dominant kernel, nl_stage (one RK4 stage): its one-pass input and output (34 B
+          per field point in complex64) over its CUDA-event launch time; roofline_nl_step the
           whole NL increment against its 16 B per field point minimum; roofline_qdht the
           tensor-core QDHT, algorithmic 8 N_r flop per field-point step
   adjoint the gradient workload (256 x 4096, 1000 steps): forward vs forward+adjoint time
@@ -501,7 +501,7 @@ def main():
     nl_ach = (16 if esz == 8 else 32) * nr * nt / (nl_step_ms / 1e3) / 1e9 if nl_step_ms else None
     roof = {"bound": "hbm", "kernel": "nl_stage_kernel" if n_st else "staged NL kernels (not timed)",
             "achieved": st_ach, "peak": hbm, "unit": "GB/s", "frac": (st_ach / hbm) if st_ach and hbm else None,
-            "traffic": read_profile_traffic("nl_fused_silica_256x16384.md") if prec == gs.PREC_MIXED else None,
+            "traffic": read_profile_traffic("nl_stage_silica_256x16384.md") if prec == gs.PREC_MIXED else None,
             "peak_kind": f"{pk_kind} HBM copy", "launch_ms": st_launch_ms,
             "algorithmic_bytes_per_launch": st_bytes,
             "share_of_step": (st_ms / ms) if ms and n_st else None,
