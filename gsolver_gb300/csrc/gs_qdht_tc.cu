@@ -530,17 +530,20 @@ constexpr int SMEM2_BYTES = STAGES2 * STAGE2_BYTES + 1024 + 256;
 
 // Per column c a power of two xscale[c] > max_j |X[j][c]| (1 for a zero column), then
 // X / xscale[c] = Xh + Xl in round-to-nearest FP16 parts, written K-major.  One CTA owns a
-// strip of 16 columns: it reads the strip once into shared memory (rows of 17 floats), finds
-// the column maxima there and writes the parts as pairs of halves along j.  Relative error
-// of the parts ~2^-22 of each value, or 2^-25 of its column's maximum where Xl falls below the
-// FP16 normal range.  Dynamic shared memory: nr * 17 floats.
+// strip of 16 columns: it reads the strip once into shared memory, finds the column maxima
+// there and writes the parts as pairs of halves along j.  In shared memory rows j and j + 1
+// (j even) share a line of 33 floats (element (j, c) at (j / 2) 33 + (j % 2) 16 + c), so the
+// row-wise stores, the column scans and the pair-wise reads are all free of bank conflicts.
+// Relative error of the parts ~2^-22 of each value, or 2^-25 of its column's maximum where Xl
+// falls below the FP16 normal range.  Dynamic shared memory: (nr / 2) * 33 floats.
 constexpr int SPLIT_COLS = 16, SPLIT_THREADS = 256;
 __global__ void __launch_bounds__(SPLIT_THREADS) qdht_split16_kernel(const float* __restrict__ X,
                                                                      __half* __restrict__ XhT,
                                                                      __half* __restrict__ XlT,
                                                                      float* __restrict__ xscale, int nr, int ncols,
                                                                      const int* __restrict__ kmax) {
-    extern __shared__ float strip[];   // [nr][17]
+    extern __shared__ float strip[];   // [nr / 2][33]
+    auto at = [](int j, int c) { return (j >> 1) * 33 + (j & 1) * 16 + c; };
     __shared__ float part[SPLIT_THREADS / SPLIT_COLS][SPLIT_COLS];
     __shared__ float inv[SPLIT_COLS];
     const int tid = threadIdx.x;
@@ -564,7 +567,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS) qdht_split16_kernel(const float
                 if (j >= nr) break;
                 if (j > k0) { v[u].x = 0.f; v[u].y = 0.f; }   // outside the spectral window
                 if (j > k1) { v[u].z = 0.f; v[u].w = 0.f; }
-                float* d = strip + j * 17 + 4 * q;
+                float* d = strip + at(j, 4 * q);
                 d[0] = v[u].x;
                 d[1] = v[u].y;
                 d[2] = v[u].z;
@@ -576,7 +579,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS) qdht_split16_kernel(const float
     {
         const int c = tid & (SPLIT_COLS - 1), p = tid / SPLIT_COLS;
         float m = 0.f;
-        for (int j = p; j < nr; j += SPLIT_THREADS / SPLIT_COLS) m = fmaxf(m, fabsf(strip[j * 17 + c]));
+        for (int j = p; j < nr; j += SPLIT_THREADS / SPLIT_COLS) m = fmaxf(m, fabsf(strip[at(j, c)]));
         part[p][c] = m;
     }
     __syncthreads();
@@ -595,7 +598,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS) qdht_split16_kernel(const float
     for (int idx = tid; idx < SPLIT_COLS * half_rows; idx += SPLIT_THREADS) {
         const int c = idx / half_rows, jp = idx - c * half_rows;
         const float s = inv[c];
-        const float v0 = strip[(2 * jp) * 17 + c] * s, v1 = strip[(2 * jp + 1) * 17 + c] * s;
+        const float v0 = strip[jp * 33 + c] * s, v1 = strip[jp * 33 + 16 + c] * s;
         const __half h0 = __float2half_rn(v0), h1 = __float2half_rn(v1);
         const size_t o = (size_t)(c0 + c) * nr + 2 * jp;
         *reinterpret_cast<__half2*>(XhT + o) = __halves2half2(h0, h1);
@@ -923,9 +926,9 @@ QdhtTc* qdht_tc_create(int nr, int nt, cudaStream_t st, std::string* msg) {
                    cudaMalloc(&q->xs, ncols * 4) == cudaSuccess &&
                    cudaFuncSetAttribute(tc::qdht_tc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         tc::SMEM2_BYTES) == cudaSuccess &&
-                   (size_t)nr * 17 * 4 <= 227 * 1024 &&
+                   (size_t)(nr / 2) * 33 * 4 <= 227 * 1024 &&
                    cudaFuncSetAttribute(tc::qdht_split16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        nr * 17 * 4) == cudaSuccess;
+                                        (nr / 2) * 33 * 4) == cudaSuccess;
         for (int w = 0; okw && w < 2; w++) {
             // [2 n_t rows c][n_r halves j]: boxes of 32 j (64 B, swizzled) x 256 c
             cuuint64_t gdim[2] = {(cuuint64_t)nr, (cuuint64_t)ncols};
@@ -1069,7 +1072,7 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
     if (q->wide) {
         // split X into the K-major FP16 hi / lo operands and the column scales (the window mask
         // of the inverse applied), then the GEMM on 128 x 256 tiles
-        tc::qdht_split16_kernel<<<(unsigned)(a.ncols / tc::SPLIT_COLS), tc::SPLIT_THREADS, (size_t)q->nr * 17 * 4, q->st>>>(
+        tc::qdht_split16_kernel<<<(unsigned)(a.ncols / tc::SPLIT_COLS), tc::SPLIT_THREADS, (size_t)(q->nr / 2) * 33 * 4, q->st>>>(
             X, (__half*)q->xhT, (__half*)q->xlT, q->xs, q->nr, a.ncols, mode == QDHT_MASKED ? q->kmax : nullptr);
         (*nlaunch)++;
         a.hscale = q->hs;
