@@ -69,6 +69,10 @@ struct TcArgs {
     // FP16 operands: Y[i][c] = hscale[i] xscale[c] (H' X')[i][c] (powers of two)
     const float* hscale;
     const float* xscale;
+    // wide path: nc operand columns, compact column c' holding column cmap[c'] of X and Y
+    // (-1: padding), or cmap null and nc = ncols
+    int nc;
+    const int* cmap;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -541,37 +545,37 @@ __global__ void __launch_bounds__(SPLIT_THREADS) qdht_split16_kernel(const float
                                                                      __half* __restrict__ XhT,
                                                                      __half* __restrict__ XlT,
                                                                      float* __restrict__ xscale, int nr, int ncols,
-                                                                     const int* __restrict__ kmax) {
+                                                                     const int* __restrict__ kmax,
+                                                                     const int* __restrict__ cmap) {
     extern __shared__ float strip[];   // [nr / 2][33]
     auto at = [](int j, int c) { return (j >> 1) * 33 + (j & 1) * 16 + c; };
     __shared__ float part[SPLIT_THREADS / SPLIT_COLS][SPLIT_COLS];
     __shared__ float inv[SPLIT_COLS];
     const int tid = threadIdx.x;
     const int c0 = blockIdx.x * SPLIT_COLS;
-    // load: a thread takes 4 columns (one float4) of a row, 64 rows per pass
+    // load: a thread takes one (re, im) column pair (a float2) of a row, 32 rows per pass;
+    // compact column pairs map to pairs of X's columns (cmap[2q] even, -1: padding, zeros)
     {
-        const int q = tid & 3, r0 = tid >> 2;
-        const int ca = c0 + 4 * q;
-        const int k0 = kmax ? kmax[ca >> 1] : nr, k1 = kmax ? kmax[(ca >> 1) + 1] : nr;
-        constexpr int RS = SPLIT_THREADS / 4, LB = 8;   // rows per pass; loads in flight per thread
+        const int q = tid & 7, r0 = tid >> 3;
+        const int ca = cmap ? cmap[c0 + 2 * q] : c0 + 2 * q;
+        const int k0 = ca < 0 ? -1 : (kmax ? kmax[ca >> 1] : nr);
+        constexpr int RS = SPLIT_THREADS / 8, LB = 8;   // rows per pass; loads in flight per thread
         for (int jb = r0; jb < nr; jb += LB * RS) {
-            float4 v[LB];
+            float2 v[LB];
 #pragma unroll
             for (int u = 0; u < LB; u++) {
                 const int j = jb + u * RS;
-                v[u] = j < nr ? *reinterpret_cast<const float4*>(X + (size_t)j * ncols + ca) : make_float4(0.f, 0.f, 0.f, 0.f);
+                // rows past the window (and padding) are zero and not read
+                v[u] = (j < nr && j <= k0) ? *reinterpret_cast<const float2*>(X + (size_t)j * ncols + ca)
+                                           : make_float2(0.f, 0.f);
             }
 #pragma unroll
             for (int u = 0; u < LB; u++) {
                 const int j = jb + u * RS;
                 if (j >= nr) break;
-                if (j > k0) { v[u].x = 0.f; v[u].y = 0.f; }   // outside the spectral window
-                if (j > k1) { v[u].z = 0.f; v[u].w = 0.f; }
-                float* d = strip + at(j, 4 * q);
+                float* d = strip + at(j, 2 * q);
                 d[0] = v[u].x;
                 d[1] = v[u].y;
-                d[2] = v[u].z;
-                d[3] = v[u].w;
             }
         }
     }
@@ -648,19 +652,30 @@ __device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, 
         }
     }
     if (a.mode != QDHT_LSTEP) {
+        if (a.cmap) {   // compact columns: pairs scattered back to their columns
+            float* y = a.Y + (size_t)i * a.ncols;
+#pragma unroll
+            for (int k = 0; k < 32; k += 2) {
+                const int rc = a.cmap[cg + k];
+                if (rc >= 0) *reinterpret_cast<float2*>(y + rc) = make_float2(v[k], v[k + 1]);
+            }
+            return;
+        }
 #pragma unroll
         for (int k = 0; k < 32; k += 4)
             *reinterpret_cast<float4*>(yrow + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
         return;
     }
-    const int p0 = cg >> 1;
 #pragma unroll
     for (int e = 0; e < 16; e++) {
-        const int p = p0 + e;
+        const int rc = a.cmap ? a.cmap[cg + 2 * e] : cg + 2 * e;
+        if (rc < 0) continue;               // padding
+        const int p = rc >> 1;
         if (i > a.kmax[p]) continue;        // outside the window: BIGBUFFER2 untouched
+        float2* y2 = reinterpret_cast<float2*>(a.Y + (size_t)i * a.ncols + rc);
         const float k1 = a.kr[p], k2 = a.ki[p];
         const float sq = sqrt_ho_f(-kt2i / k1 / k1);
-        float2 b2 = *reinterpret_cast<float2*>(yrow + 2 * e);
+        float2 b2 = *y2;
         const float inv = 1.f / (1.f + sq);
         b2.x += a.dz * v[2 * e] * inv;
         b2.y += a.dz * v[2 * e + 1] * inv;
@@ -671,7 +686,18 @@ __device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, 
         float2 f;
         f.x = b2.x * pr - b2.y * pi;
         f.y = b2.x * pi + b2.y * pr;
-        *reinterpret_cast<float2*>(yrow + 2 * e) = f;
+        *y2 = f;
+    }
+}
+
+// Zeros of the masked inverse outside the spectral window: Y[i][2 p], Y[i][2 p + 1] = 0 for
+// the positions p in zpos[nz] (their whole column of the operand is masked)
+__global__ void qdht_zero_cols_kernel(float* __restrict__ Y, int ncols, int nr, const int* __restrict__ zpos, int nz) {
+    const size_t total = (size_t)nr * nz;
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = idx / nz;
+        const int z = (int)(idx - i * nz);
+        *reinterpret_cast<float2*>(Y + i * ncols + 2 * zpos[z]) = make_float2(0.f, 0.f);
     }
 }
 
@@ -692,7 +718,7 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int MT = a.nr / BM;
-    const int ntiles = MT * (a.ncols / BN2);
+    const int ntiles = MT * (a.nc / BN2);
     const int nk = a.nr / BK2;
     const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
 
@@ -852,6 +878,10 @@ struct QdhtTc {
     float *xhT = nullptr, *xlT = nullptr;   // [2 n_t][n_r] halves
     __half *hh16 = nullptr, *hl16 = nullptr;
     float *hs = nullptr, *xs = nullptr;     // hscale[n_r], xscale[2 n_t]
+    // the spectral window's columns (kmax >= 0) for the linear-step and masked transforms:
+    // cmap[nc_act] (padded with -1 to a multiple of 256) and the positions outside, zpos[nz]
+    int *cmap = nullptr, *zpos = nullptr;
+    int nc_act = 0, nz = 0;
     CUtensorMap map_bh, map_bl, map_hi64, map_lo64;   // 32-half boxes in the 64-byte swizzle
     // tensor maps of the X operands seen so far (the handle's few state arrays)
     std::vector<std::pair<const float*, CUtensorMap>> xmaps;
@@ -1044,6 +1074,32 @@ int qdht_tc_set_lstep(QdhtTc* q, const double* omega, const double* wavenum, con
         if (msg) *msg = "linear-step table upload failed";
         return 1;
     }
+    if (q->wide) {
+        // compact column list of the window (pairs of real columns), padded to whole tiles
+        std::vector<int> cm, zp;
+        for (int p = 0; p < nt; p++) {
+            if (kmax[p] >= 0) {
+                cm.push_back(2 * p);
+                cm.push_back(2 * p + 1);
+            } else {
+                zp.push_back(p);
+            }
+        }
+        while (cm.size() % tc::BN2) cm.push_back(-1);
+        if (q->cmap) cudaFree(q->cmap);
+        if (q->zpos) cudaFree(q->zpos);
+        q->cmap = q->zpos = nullptr;
+        q->nc_act = (int)cm.size();
+        q->nz = (int)zp.size();
+        bool okc = (cm.empty() || (cudaMalloc(&q->cmap, cm.size() * 4) == cudaSuccess &&
+                                   cudaMemcpy(q->cmap, cm.data(), cm.size() * 4, cudaMemcpyHostToDevice) == cudaSuccess)) &&
+                   (zp.empty() || (cudaMalloc(&q->zpos, zp.size() * 4) == cudaSuccess &&
+                                   cudaMemcpy(q->zpos, zp.data(), zp.size() * 4, cudaMemcpyHostToDevice) == cudaSuccess));
+        if (!okc) {
+            if (msg) *msg = "window column list upload failed";
+            return 1;
+        }
+    }
     q->have_lstep = true;
     return 0;
 }
@@ -1069,15 +1125,33 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
     a.err = q->err;
     a.hscale = nullptr;
     a.xscale = nullptr;
+    a.nc = a.ncols;
+    a.cmap = nullptr;
     if (q->wide) {
+        // The linear step leaves BIGBUFFER2 untouched outside the spectral window and the masked
+        // inverse transforms a zero column there: both run on the window's columns only (the
+        // compact list), the masked one writing the zeros of the other columns directly.
+        const bool compact = mode != QDHT_PLAIN;
+        if (compact) {
+            a.nc = q->nc_act;
+            a.cmap = q->cmap;
+            if (mode == QDHT_MASKED && q->nz > 0) {
+                const size_t tot = (size_t)q->nr * q->nz;
+                const unsigned gz = (unsigned)std::min<size_t>((tot + 255) / 256, (size_t)q->sms * 16);
+                tc::qdht_zero_cols_kernel<<<gz, 256, 0, q->st>>>(Y, a.ncols, q->nr, q->zpos, q->nz);
+                (*nlaunch)++;
+            }
+        }
+        if (a.nc == 0) return cudaGetLastError();
         // split X into the K-major FP16 hi / lo operands and the column scales (the window mask
         // of the inverse applied), then the GEMM on 128 x 256 tiles
-        tc::qdht_split16_kernel<<<(unsigned)(a.ncols / tc::SPLIT_COLS), tc::SPLIT_THREADS, (size_t)(q->nr / 2) * 33 * 4, q->st>>>(
-            X, (__half*)q->xhT, (__half*)q->xlT, q->xs, q->nr, a.ncols, mode == QDHT_MASKED ? q->kmax : nullptr);
+        tc::qdht_split16_kernel<<<(unsigned)(a.nc / tc::SPLIT_COLS), tc::SPLIT_THREADS, (size_t)(q->nr / 2) * 33 * 4,
+                                  q->st>>>(X, (__half*)q->xhT, (__half*)q->xlT, q->xs, q->nr, a.ncols,
+                                           mode == QDHT_MASKED ? q->kmax : nullptr, a.cmap);
         (*nlaunch)++;
         a.hscale = q->hs;
         a.xscale = q->xs;
-        const int nt2 = (q->nr / tc::BM) * (a.ncols / tc::BN2);
+        const int nt2 = (q->nr / tc::BM) * (a.nc / tc::BN2);
         const unsigned g2 = (unsigned)(nt2 < q->sms ? nt2 : q->sms);
         tc::qdht_tc2_kernel<<<g2, tc::THREADS2, tc::SMEM2_BYTES, q->st>>>(q->map_hi64, q->map_lo64, q->map_bh, q->map_bl, a);
         (*nlaunch)++;
@@ -1136,7 +1210,8 @@ int qdht_tc_check(QdhtTc* q, std::string* msg) {
 
 void qdht_tc_destroy(QdhtTc* q) {
     if (!q) return;
-    void* ptrs[] = {q->hh, q->hl, q->kr, q->ki, q->ho, q->kt2, q->kmax, q->err, q->xhT, q->xlT, q->hh16, q->hl16, q->hs, q->xs};
+    void* ptrs[] = {q->hh, q->hl, q->kr, q->ki, q->ho, q->kt2, q->kmax, q->err, q->xhT, q->xlT, q->hh16, q->hl16, q->hs, q->xs,
+                    q->cmap, q->zpos};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete q;
