@@ -176,6 +176,17 @@ def read_profile_traffic(name="qdht_tc_fused_silica_512x16384.md"):
         return None
 
 
+def window_columns(S):
+    """Real columns (2 per omega) inside calculate_Lstep's window: omega in [min, max] and some
+    kt^2 <= Re(k^2) / 4 -- the columns the tensor-core QDHT transforms (propagator.cu:570-625)."""
+    om = np.asarray(S["omega"])
+    k = np.asarray(S["wavenum"])
+    kt2 = np.asarray(S["kt2"])
+    inwin = ~((om < S["omega_min"]) | (om > S["omega_max"]))
+    lim = 0.25 * (k.real ** 2 - k.imag ** 2)
+    return int(2 * np.count_nonzero(inwin & (kt2.min() <= lim)))
+
+
 def peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -476,9 +487,12 @@ def main():
         ms = float(t.item())
     value = nr * nt * args.steps * world / (ms / 1e3)
 
-    # roofline: the QDHT pair (forward + fused linear step, inverse), 2*N_r^2*(2 N_t) flop each
+    # roofline: the QDHT (forward + fused linear step, inverse), 2 N_r^2 flop per real column
+    # of the spectral window each: outside it the linear step leaves BIGBUFFER2 untouched and
+    # the masked inverse transforms zero columns, so neither is computed there
     hbm, bf16, bf16s, pk_kind = peaks()
-    flop_launch = 2.0 * nr * nr * 2 * nt
+    ncol_win = window_columns(S)
+    flop_launch = 2.0 * nr * nr * ncol_win
     per_launch_ms = q_ms / max(q_n, 1)
     achieved = flop_launch / (per_launch_ms / 1e3) / 1e12 if q_n else None
     roof_q = {"bound": "tensor", "kernel": "qdht_tc" if prec == gs.PREC_MIXED else "qdht64 (FP64 CUDA cores)",
@@ -486,8 +500,10 @@ def main():
             "frac": (achieved / bf16) if achieved else None, "traffic": read_profile_traffic() if prec == gs.PREC_MIXED else None,
             "peak_kind": f"{pk_kind} cuBLAS bf16 burst", "launch_ms": per_launch_ms,
             "qdht_share_of_step": (q_ms / ms) if ms else None,
-            "note": "algorithmic flop (8 N_r per field-point step); the split FP16 operands execute 3 products "
-                    "(Hh Xh + Hh Xl + Hl Xh) at the FP16 rate, which equals the bf16 rate of the peak"}
+            "window_columns": ncol_win, "columns": 2 * nt,
+            "note": "algorithmic flop 2 N_r^2 per real column of the spectral window per transform (launch_ms is "
+                    "one transform, split + GEMM); the split FP16 operands execute 3 products (Hh Xh + Hh Xl + "
+                    "Hl Xh) at the FP16 rate, which equals the bf16 rate of the peak"}
     # the dominant kernel: nl_stage (one RK4 stage per launch: inverse FFT, plasma and Raman
     # recurrences, forward FFT of the sources, spectral combination, RK4 sums); its algorithmic
     # bytes per launch are its one-pass input and output: A (8 B per field point), k of the
