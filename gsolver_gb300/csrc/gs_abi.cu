@@ -99,7 +99,7 @@ static void free_all(gs_handle* h) {
     void* ptrs[] = {h->A, h->S, h->NB, h->KP, h->E, h->U, h->tw, h->pf, h->rm, h->kerr, h->rate,
                     h->omega, h->ho, h->kt2, h->Cm, h->m1, h->wavenum, h->staging, h->perm_dev,
                     h->iperm_dev, h->err_dev, h->max_dev, h->dump_dev, h->m1inv, h->adj, h->adj_w, h->th, h->twb,
-                    h->row_ion};
+                    h->row_ion, h->win64, h->zpos64};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (h->tc) gs::qdht_tc_destroy(h->tc);
     if (h->tcT) gs::qdht_tc_destroy(h->tcT);
@@ -299,6 +299,43 @@ int gs_upload_tables(gs_handle* h, const gs_tables* t) {
             }
         }
     }
+    if (h->fp64) {
+        // calculate_Lstep's window per position (omega in [min, max], some kt^2 <= Re(k^2) / 4):
+        // the FP64 linear-step and masked transforms take these columns only
+        std::vector<int> cm, zp;
+        double kt2min = t->kt2[0];
+        for (int k = 1; k < nr; k++) kt2min = std::min(kt2min, t->kt2[k]);
+        for (int p = 0; p < nt; p++) {
+            const double w = om[p], kr = wn[2 * p], ki = wn[2 * p + 1];
+            const bool in = !(w < h->p.omega_min || w > h->p.omega_max) && !(kt2min > 0.25 * (kr * kr - ki * ki));
+            if (in) {
+                cm.push_back(2 * p);
+                cm.push_back(2 * p + 1);
+            } else {
+                zp.push_back(p);
+            }
+        }
+        while (cm.size() % 64) cm.push_back(-1);
+        if (h->win64) cudaFree(h->win64);
+        if (h->zpos64) cudaFree(h->zpos64);
+        h->win64 = h->zpos64 = nullptr;
+        h->nwin64 = (int)cm.size();
+        h->nz64 = (int)zp.size();
+        if (!cm.empty()) {
+            CK(h, cudaMalloc((void**)&h->win64, cm.size() * 4));
+            CK(h, up(h->win64, cm.data(), cm.size() * 4));
+        }
+        if (!zp.empty()) {
+            CK(h, cudaMalloc((void**)&h->zpos64, zp.size() * 4));
+            CK(h, up(h->zpos64, zp.data(), zp.size() * 4));
+        }
+        if (cm.empty()) {   // no column in the window: keep one padding tile so the list is non-null
+            std::vector<int> pad(64, -1);
+            CK(h, cudaMalloc((void**)&h->win64, 64 * 4));
+            CK(h, up(h->win64, pad.data(), 64 * 4));
+            h->nwin64 = 64;
+        }
+    }
     if (h->tc) {
         std::string m;
         if (gs::qdht_tc_set_matrix(h->tc, t->qdht_c, t->qdht_m1, &m)) return fail(h, GS_ERR_CUDA, "mixed QDHT matrix: " + m);
@@ -343,7 +380,9 @@ static LstepArgs lstep_args(gs_handle* h, double dz) {
 int gsi::run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz) {
     LstepArgs L = lstep_args(h, dz);
     if (h->fp64) {
-        CK(h, launch_qdht64(mode, h->Cm, h->m1, (const double*)X, (double*)Y, h->nr, 2 * h->nt, L, h->st, &h->launches));
+        const bool win = mode != QDHT_PLAIN && h->win64;
+        CK(h, launch_qdht64(mode, h->Cm, h->m1, (const double*)X, (double*)Y, h->nr, 2 * h->nt, L, h->st, &h->launches,
+                            win ? h->win64 : nullptr, h->nwin64, h->zpos64, h->nz64));
     } else {
         std::string m;
         cudaError_t e = gs::qdht_tc_run(h->tc, mode, (const float*)X, (float*)Y, L, &h->launches, &m);

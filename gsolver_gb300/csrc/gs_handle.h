@@ -53,6 +53,9 @@ struct gs_handle {
     cudaEvent_t nl_ev[8] = {};   // before / after each RK4-stage launch
     double nl_ms = 0;
     int adj_stride = 0;   // checkpoint stride of the last gs_gradient
+    // FP64 QDHT: the spectral window's columns (padded to 64 with -1) and the positions outside
+    int *win64 = nullptr, *zpos64 = nullptr;
+    int nwin64 = 0, nz64 = 0;
     int nl_stages_timed = 0;
     double* dump_dev = nullptr;   // 3 n_r + 2 n_t doubles of reduction output, r weights
     void* twb = nullptr;          // per-stage base twiddles of the M-point row FFTs (tw_base_offset)

@@ -189,8 +189,11 @@ struct LstepArgs {
     double omega_min, omega_max;
 };
 enum { QDHT_PLAIN = 0, QDHT_LSTEP = 1, QDHT_MASKED = 2 };
+// cmap[nc] / zpos[nz]: the spectral window's columns (padded to 64 with -1) and the positions
+// outside it; the linear-step and masked transforms then run on the window only (null: all)
 cudaError_t launch_qdht64(int mode, const double* C, const double* m1, const double* X, double* Y, int nr,
-                          int ncols, const LstepArgs& L, cudaStream_t st, long long* nlaunch);
+                          int ncols, const LstepArgs& L, cudaStream_t st, long long* nlaunch, const int* cmap = nullptr,
+                          int nc = 0, const int* zpos = nullptr, int nz = 0);
 cudaError_t qdht_set_sqrt_ho(const double* coeffs20);
 // adjoint of the linear step (gs_qdht64.cu): fb = cotangent of FIELD (k,omega) after the
 // step, sb of BIGBUFFER2 (in: after, out: before), b1b out: of BIGBUFFER1 (k,omega)

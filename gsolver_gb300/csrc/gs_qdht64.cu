@@ -12,6 +12,8 @@
 //                window  B2 += dz*N/(1+s);  B2 *= exp(dz*(-j(D + k_r s) + k_i)).
 //   QDHT_MASKED  X = BIGBUFFER2 read as FIELD: zero outside the window (what
 //                calculate_Lstep writes into FIELD there), Y = FIELD (r,omega).
+#include <algorithm>
+
 #include "gs_kernels.h"
 #include "gs_internal.cuh"
 
@@ -36,10 +38,14 @@ __device__ __forceinline__ bool in_window(const LstepArgs& L, int k, int p) {
 
 constexpr int BM = 64, BN = 64, BK = 16;
 
+// cmap (or null: column c itself): the real column of X / Y that operand column c stands for
+// (-1: padding).  The linear-step and masked transforms take the spectral window's columns
+// only: outside it the linear step leaves BIGBUFFER2 untouched and the masked inverse's
+// columns are zero (written by qdht64_zero_kernel).
 template <int MODE>
 __global__ void __launch_bounds__(256) qdht64_kernel(const double* __restrict__ C, const double* __restrict__ m1,
                                                      const double* __restrict__ X, double* __restrict__ Y, int nr,
-                                                     int ncols, LstepArgs L) {
+                                                     int ncols, LstepArgs L, const int* __restrict__ cmap) {
     __shared__ double As[2][BK][BM];
     __shared__ __align__(16) double Bs[2][BK][BN];
     const int tid = threadIdx.x;
@@ -56,10 +62,10 @@ __global__ void __launch_bounds__(256) qdht64_kernel(const double* __restrict__ 
     auto load = [&](int k0) {
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-            const int k = lk + 4 * u, j = k0 + k, i = i0 + lm, c = c0 + lm;
+            const int k = lk + 4 * u, j = k0 + k, i = i0 + lm, c = cmap ? cmap[c0 + lm] : c0 + lm;
             ra[u] = (i < nr && j < nr) ? C[(size_t)i + (size_t)nr * j] : 0.0;
             double v = 0.0;
-            if (j < nr) {
+            if (j < nr && c >= 0) {
                 v = X[(size_t)j * ncols + c];
                 if (MODE == QDHT_MASKED && !in_window(L, j, c >> 1)) v = 0.0;
                 v = v / m1[j];
@@ -103,20 +109,24 @@ __global__ void __launch_bounds__(256) qdht64_kernel(const double* __restrict__ 
         const int i = i0 + ty * 4 + u;
         if (i >= nr) continue;
         const double mi = m1[i];
-        const size_t rowo = (size_t)i * ncols + c0 + tx * 4;
+        // the two (re, im) pairs of this thread's four operand columns
+        const int rc0 = cmap ? cmap[c0 + tx * 4] : c0 + tx * 4, rc1 = cmap ? cmap[c0 + tx * 4 + 2] : c0 + tx * 4 + 2;
         if (MODE != QDHT_LSTEP) {
-            *reinterpret_cast<double2*>(&Y[rowo]) = make_double2(acc[u][0] * mi, acc[u][1] * mi);
-            *reinterpret_cast<double2*>(&Y[rowo + 2]) = make_double2(acc[u][2] * mi, acc[u][3] * mi);
+            if (rc0 >= 0) *reinterpret_cast<double2*>(&Y[(size_t)i * ncols + rc0]) = make_double2(acc[u][0] * mi, acc[u][1] * mi);
+            if (rc1 >= 0) *reinterpret_cast<double2*>(&Y[(size_t)i * ncols + rc1]) = make_double2(acc[u][2] * mi, acc[u][3] * mi);
         } else {
 #pragma unroll
             for (int e = 0; e < 2; e++) {
-                const int p = (c0 + tx * 4) / 2 + e;
+                const int rc = e ? rc1 : rc0;
+                if (rc < 0) continue;
+                const int p = rc >> 1;
+                double* y2 = &Y[(size_t)i * ncols + rc];
                 if (!in_window(L, i, p)) continue;   // FIELD = 0 there; BIGBUFFER2 untouched
                 const double vr = acc[u][2 * e] * mi, vi = acc[u][2 * e + 1] * mi;
                 const double2 kk = L.wavenum[p];
                 const double k1 = kk.x, k2 = kk.y;
                 const double sq = sqrt_ho(-L.kt2[i] / k1 / k1);
-                double2 b2 = *reinterpret_cast<const double2*>(&Y[rowo + 2 * e]);
+                double2 b2 = *reinterpret_cast<const double2*>(y2);
                 b2.x += L.dz * vr / (1 + sq);
                 b2.y += L.dz * vi / (1 + sq);
                 const double er = L.dz * k2, ei = L.dz * (-L.ho[p] - sq * k1);
@@ -127,19 +137,36 @@ __global__ void __launch_bounds__(256) qdht64_kernel(const double* __restrict__ 
                 double2 f;
                 f.x = b2.x * pr - b2.y * pi;
                 f.y = b2.x * pi + b2.y * pr;
-                *reinterpret_cast<double2*>(&Y[rowo + 2 * e]) = f;
+                *reinterpret_cast<double2*>(y2) = f;
             }
         }
     }
 }
 
+__global__ void qdht64_zero_kernel(double* __restrict__ Y, int ncols, int nr, const int* __restrict__ zpos, int nz) {
+    const size_t total = (size_t)nr * nz;
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = idx / nz;
+        const int z = (int)(idx - i * nz);
+        *reinterpret_cast<double2*>(Y + i * ncols + 2 * zpos[z]) = make_double2(0.0, 0.0);
+    }
+}
+
 cudaError_t launch_qdht64(int mode, const double* C, const double* m1, const double* X, double* Y, int nr,
-                          int ncols, const LstepArgs& L, cudaStream_t st, long long* nlaunch) {
-    dim3 grid(ncols / BN, (nr + BM - 1) / BM);
+                          int ncols, const LstepArgs& L, cudaStream_t st, long long* nlaunch, const int* cmap, int nc,
+                          const int* zpos, int nz) {
+    if (!cmap) nc = ncols;
+    if (mode == QDHT_MASKED && cmap && nz > 0) {
+        const size_t tot = (size_t)nr * nz;
+        qdht64_zero_kernel<<<(unsigned)std::min<size_t>((tot + 255) / 256, 4096), 256, 0, st>>>(Y, ncols, nr, zpos, nz);
+        (*nlaunch)++;
+    }
+    if (nc == 0) return cudaGetLastError();
+    dim3 grid(nc / BN, (nr + BM - 1) / BM);
     switch (mode) {
-        case QDHT_PLAIN: qdht64_kernel<QDHT_PLAIN><<<grid, 256, 0, st>>>(C, m1, X, Y, nr, ncols, L); break;
-        case QDHT_LSTEP: qdht64_kernel<QDHT_LSTEP><<<grid, 256, 0, st>>>(C, m1, X, Y, nr, ncols, L); break;
-        case QDHT_MASKED: qdht64_kernel<QDHT_MASKED><<<grid, 256, 0, st>>>(C, m1, X, Y, nr, ncols, L); break;
+        case QDHT_PLAIN: qdht64_kernel<QDHT_PLAIN><<<grid, 256, 0, st>>>(C, m1, X, Y, nr, ncols, L, nullptr); break;
+        case QDHT_LSTEP: qdht64_kernel<QDHT_LSTEP><<<grid, 256, 0, st>>>(C, m1, X, Y, nr, ncols, L, cmap); break;
+        case QDHT_MASKED: qdht64_kernel<QDHT_MASKED><<<grid, 256, 0, st>>>(C, m1, X, Y, nr, ncols, L, cmap); break;
         default: return cudaErrorInvalidValue;
     }
     (*nlaunch)++;
