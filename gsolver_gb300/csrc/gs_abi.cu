@@ -377,7 +377,7 @@ static LstepArgs lstep_args(gs_handle* h, double dz) {
 }
 
 // QDHT of device array X -> Y (mode: plain / fused linear step / masked input).
-int gsi::run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz) {
+int gsi::run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz, bool x_compact) {
     LstepArgs L = lstep_args(h, dz);
     if (h->fp64) {
         const bool win = mode != QDHT_PLAIN && h->win64;
@@ -385,7 +385,7 @@ int gsi::run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz) {
                             win ? h->win64 : nullptr, h->nwin64, h->zpos64, h->nz64));
     } else {
         std::string m;
-        cudaError_t e = gs::qdht_tc_run(h->tc, mode, (const float*)X, (float*)Y, L, &h->launches, &m);
+        cudaError_t e = gs::qdht_tc_run(h->tc, mode, (const float*)X, (float*)Y, L, &h->launches, &m, x_compact);
         if (e != cudaSuccess) return fail(h, GS_ERR_CUDA, "mixed QDHT: " + m + " " + cudaGetErrorString(e));
     }
     return GS_OK;
@@ -580,6 +580,7 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
     T2* U1 = (T2*)h->U;
     T2* U2 = U1 + nel;
     T2* U3 = U2 + nel;
+    h->nbc_valid = false;   // set again below when the fused stages also write NB's compact columns
     if (!h->p.nonlinear) {
         CK(h, launch_zero_nl<Rl>(A, NB, nel, h->max_dev, h->st, &h->launches));
         return GS_OK;
@@ -620,8 +621,12 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
     if (fused) {
         pa.row_ion = h->row_ion;   // the row flags of the last stage (the adjoint keeps its own)
         // k of stages 0, 1, 2 in KP, E (free on this path) and NB; stage 3 reads all three and
-        // writes the RK4 sum over NB row by row
+        // writes the RK4 sum over NB row by row, and (mixed) its window columns compactly for
+        // the linear-step transform
         T2* kst[3] = {KP, E, NB};
+        const int* cinv = nullptr;
+        int ncw = 0;
+        float* nbc = (!h->fp64 && h->tc) ? gs::qdht_tc_compact_x(h->tc, &cinv, &ncw) : nullptr;
         for (int s = 0; s < 4; s++) {
             FftArgs<Rl> f1 = fa;
             f1.rows = nr; f1.kp = s > 0 ? kst[s - 1] : KP;
@@ -638,11 +643,15 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
             SpecArgs<Rl> s2 = sa;
             s2.stage = s;
             for (int j = 0; j < 3; j++) s2.kst[j] = kst[j];
+            s2.nbc = nbc;
+            s2.cinv = cinv;
+            s2.ncw = ncw;
             if (tm) CK(h, cudaEventRecord(h->nl_ev[2 * s], h->st));
             CK(h, launch_nl_stage<Rl>(f1, ps, A, s2, nr, h->st, &h->launches));
             if (tm) CK(h, cudaEventRecord(h->nl_ev[2 * s + 1], h->st));
         }
         if (h->time_nl && !tape) h->nl_ev_pending = true;
+        h->nbc_valid = nbc != nullptr;
         return GS_OK;
     }
     for (int s = 0; s < 4; s++) {
@@ -717,7 +726,7 @@ int gs_nl_step(gs_handle* h, double zstep, double* max_a2, double* max_nl2) {
 
 int gsi::lstep(gs_handle* h, double dz) {
     if (h->time_qdht) CK(h, cudaEventRecord(h->ev0, h->st));
-    int rc = run_qdht(h, QDHT_LSTEP, h->NB, h->S, dz);
+    int rc = run_qdht(h, QDHT_LSTEP, h->NB, h->S, dz, h->nbc_valid);
     if (rc) return rc;
     rc = run_qdht(h, QDHT_MASKED, h->S, h->A, dz);
     if (rc) return rc;

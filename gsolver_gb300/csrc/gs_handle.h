@@ -53,6 +53,7 @@ struct gs_handle {
     cudaEvent_t nl_ev[8] = {};   // before / after each RK4-stage launch
     double nl_ms = 0;
     int adj_stride = 0;   // checkpoint stride of the last gs_gradient
+    bool nbc_valid = false;   // the last NL step also wrote NB's window columns compactly (mixed)
     // FP64 QDHT: the spectral window's columns (padded to 64 with -1) and the positions outside
     int *win64 = nullptr, *zpos64 = nullptr;
     int nwin64 = 0, nz64 = 0;
@@ -78,7 +79,8 @@ namespace gsi {
 int fail(gs_handle* h, int code, const std::string& msg);
 int cuda_fail(gs_handle* h, cudaError_t e, const char* where);
 // QDHT of device array X -> Y (gs::QDHT_PLAIN / _LSTEP / _MASKED)
-int run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz);
+// x_compact: the linear-step transform reads the compact window columns its producer wrote
+int run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz, bool x_compact = false);
 // calculate_NLstep's four RK4 stages: NB = RK4 increment of A (no host sync); with a tape
 // the stages are recorded (fused rows only)
 int nl_stages(gs_handle* h, double dz, const GsTape* tape);

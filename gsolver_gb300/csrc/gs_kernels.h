@@ -125,6 +125,11 @@ template <typename Rl> struct SpecArgs {
     // the fused stage kernel: k of stages 0..2, each in its own array (k of stage s is written
     // to kst[s]; stage 3 forms the RK4 sum from them and writes nb, which may be kst[2])
     typename Vec2<Rl>::T* kst[3];
+    // optional (FP32): stage 3 also writes the RK4 sum of the spectral window's positions into
+    // this compact [rows][ncw] array, nbc[row][cinv[p]] (cinv[p] >= 0), the linear-step input
+    float* nbc;
+    const int* cinv;
+    int ncw;
 };
 
 template <typename Rl>

@@ -455,6 +455,12 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(
                 const T2 nb = T2{(s.x + k.x) / (Rl)6, (s.y + k.y) / (Rl)6};
                 nmax = fmax(nmax, nb.x * nb.x + nb.y * nb.y);
                 sp.nb[base + p] = nb;
+                if constexpr (sizeof(Rl) == 4) {
+                    if (sp.nbc) {
+                        const int c = __ldg(sp.cinv + p);
+                        if (c >= 0) *reinterpret_cast<float2*>(sp.nbc + (size_t)blockIdx.x * sp.ncw + c) = make_float2(nb.x, nb.y);
+                    }
+                }
             }
         }
     };

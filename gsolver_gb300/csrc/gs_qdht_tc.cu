@@ -73,6 +73,7 @@ struct TcArgs {
     // (-1: padding), or cmap null and nc = ncols
     int nc;
     const int* cmap;
+    float* yc;   // non-null: the output goes to this [nr][nc] compact array instead of Y
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -546,7 +547,7 @@ __global__ void __launch_bounds__(SPLIT_THREADS) qdht_split16_kernel(const float
                                                                      __half* __restrict__ XlT,
                                                                      float* __restrict__ xscale, int nr, int ncols,
                                                                      const int* __restrict__ kmax,
-                                                                     const int* __restrict__ cmap) {
+                                                                     const int* __restrict__ cmap, int xcompact) {
     extern __shared__ float strip[];   // [nr / 2][33]
     auto at = [](int j, int c) { return (j >> 1) * 33 + (j & 1) * 16 + c; };
     __shared__ float part[SPLIT_THREADS / SPLIT_COLS][SPLIT_COLS];
@@ -557,8 +558,9 @@ __global__ void __launch_bounds__(SPLIT_THREADS) qdht_split16_kernel(const float
     // compact column pairs map to pairs of X's columns (cmap[2q] even, -1: padding, zeros)
     {
         const int q = tid & 7, r0 = tid >> 3;
-        const int ca = cmap ? cmap[c0 + 2 * q] : c0 + 2 * q;
-        const int k0 = ca < 0 ? -1 : (kmax ? kmax[ca >> 1] : nr);
+        const int cm = cmap ? cmap[c0 + 2 * q] : c0 + 2 * q;   // the column (position pair) it stands for
+        const int k0 = cm < 0 ? -1 : (kmax ? kmax[cm >> 1] : nr);
+        const int ca = xcompact ? c0 + 2 * q : cm;               // where it is read: X is [nr][ncols]
         constexpr int RS = SPLIT_THREADS / 8, LB = 8;   // rows per pass; loads in flight per thread
         for (int jb = r0; jb < nr; jb += LB * RS) {
             float2 v[LB];
@@ -652,6 +654,13 @@ __device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, 
         }
     }
     if (a.mode != QDHT_LSTEP) {
+        if (a.yc) {   // the compact output array, expanded by qdht_expand_kernel
+            float* y = a.yc + (size_t)i * a.nc + cg;
+#pragma unroll
+            for (int k = 0; k < 32; k += 4)
+                *reinterpret_cast<float4*>(y + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+            return;
+        }
         if (a.cmap) {   // compact columns: pairs scattered back to their columns
             float* y = a.Y + (size_t)i * a.ncols;
 #pragma unroll
@@ -687,6 +696,20 @@ __device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, 
         f.x = b2.x * pr - b2.y * pi;
         f.y = b2.x * pi + b2.y * pr;
         *y2 = f;
+    }
+}
+
+// The masked inverse's result from its compact array: row i of Y (all n_t positions, coalesced)
+// takes the pair cinv[p] of yc where p is inside the spectral window and zeros elsewhere.
+__global__ void qdht_expand_kernel(const float* __restrict__ yc, float* __restrict__ Y, int nr, int nt, int nc,
+                                   const int* __restrict__ cinv) {
+    const size_t total = (size_t)nr * nt;
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = idx / nt;
+        const int p = (int)(idx - i * nt);
+        const int c = cinv[p];
+        const float2 v = c >= 0 ? *reinterpret_cast<const float2*>(yc + i * nc + c) : make_float2(0.f, 0.f);
+        *reinterpret_cast<float2*>(Y + 2 * idx) = v;
     }
 }
 
@@ -882,6 +905,9 @@ struct QdhtTc {
     // cmap[nc_act] (padded with -1 to a multiple of 256) and the positions outside, zpos[nz]
     int *cmap = nullptr, *zpos = nullptr;
     int nc_act = 0, nz = 0;
+    int* cinv = nullptr;      // [n_t]: compact column of position p's pair (even), or -1
+    float* yc = nullptr;      // [n_r][nc_act]: the masked inverse's compact result
+    float* xc = nullptr;      // [n_r][nc_act]: a compact linear-step input written by its producer
     CUtensorMap map_bh, map_bl, map_hi64, map_lo64;   // 32-half boxes in the 64-byte swizzle
     // tensor maps of the X operands seen so far (the handle's few state arrays)
     std::vector<std::pair<const float*, CUtensorMap>> xmaps;
@@ -1086,15 +1112,27 @@ int qdht_tc_set_lstep(QdhtTc* q, const double* omega, const double* wavenum, con
             }
         }
         while (cm.size() % tc::BN2) cm.push_back(-1);
+        std::vector<int> ci(nt, -1);
+        for (size_t c = 0; c < cm.size(); c += 2)
+            if (cm[c] >= 0) ci[cm[c] >> 1] = (int)c;
         if (q->cmap) cudaFree(q->cmap);
         if (q->zpos) cudaFree(q->zpos);
-        q->cmap = q->zpos = nullptr;
+        if (q->cinv) cudaFree(q->cinv);
+        if (q->yc) cudaFree(q->yc);
+        if (q->xc) cudaFree(q->xc);
+        q->cmap = q->zpos = q->cinv = nullptr;
+        q->yc = q->xc = nullptr;
         q->nc_act = (int)cm.size();
         q->nz = (int)zp.size();
         bool okc = (cm.empty() || (cudaMalloc(&q->cmap, cm.size() * 4) == cudaSuccess &&
                                    cudaMemcpy(q->cmap, cm.data(), cm.size() * 4, cudaMemcpyHostToDevice) == cudaSuccess)) &&
                    (zp.empty() || (cudaMalloc(&q->zpos, zp.size() * 4) == cudaSuccess &&
-                                   cudaMemcpy(q->zpos, zp.data(), zp.size() * 4, cudaMemcpyHostToDevice) == cudaSuccess));
+                                   cudaMemcpy(q->zpos, zp.data(), zp.size() * 4, cudaMemcpyHostToDevice) == cudaSuccess)) &&
+                   cudaMalloc(&q->cinv, (size_t)nt * 4) == cudaSuccess &&
+                   cudaMemcpy(q->cinv, ci.data(), (size_t)nt * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
+                   (cm.empty() || (cudaMalloc(&q->yc, (size_t)nr * cm.size() * 4) == cudaSuccess &&
+                                   cudaMalloc(&q->xc, (size_t)nr * cm.size() * 4) == cudaSuccess &&
+                                   cudaMemset(q->xc, 0, (size_t)nr * cm.size() * 4) == cudaSuccess));
         if (!okc) {
             if (msg) *msg = "window column list upload failed";
             return 1;
@@ -1105,7 +1143,7 @@ int qdht_tc_set_lstep(QdhtTc* q, const double* omega, const double* wavenum, con
 }
 
 cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const LstepArgs& L, long long* nlaunch,
-                        std::string* msg) {
+                        std::string* msg, bool x_compact) {
     if (mode != QDHT_PLAIN && !q->have_lstep) {
         if (msg) *msg = "linear-step tables not set";
         return cudaErrorInvalidValue;
@@ -1127,6 +1165,7 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
     a.xscale = nullptr;
     a.nc = a.ncols;
     a.cmap = nullptr;
+    a.yc = nullptr;
     if (q->wide) {
         // The linear step leaves BIGBUFFER2 untouched outside the spectral window and the masked
         // inverse transforms a zero column there: both run on the window's columns only (the
@@ -1135,7 +1174,8 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
         if (compact) {
             a.nc = q->nc_act;
             a.cmap = q->cmap;
-            if (mode == QDHT_MASKED && q->nz > 0) {
+            if (mode == QDHT_MASKED && a.nc > 0) a.yc = q->yc;   // expanded into Y below
+            if (mode == QDHT_MASKED && a.nc == 0 && q->nz > 0) {
                 const size_t tot = (size_t)q->nr * q->nz;
                 const unsigned gz = (unsigned)std::min<size_t>((tot + 255) / 256, (size_t)q->sms * 16);
                 tc::qdht_zero_cols_kernel<<<gz, 256, 0, q->st>>>(Y, a.ncols, q->nr, q->zpos, q->nz);
@@ -1143,11 +1183,12 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
             }
         }
         if (a.nc == 0) return cudaGetLastError();
+        const bool xc = compact && x_compact && mode == QDHT_LSTEP;   // X already compact in q->xc
         // split X into the K-major FP16 hi / lo operands and the column scales (the window mask
         // of the inverse applied), then the GEMM on 128 x 256 tiles
         tc::qdht_split16_kernel<<<(unsigned)(a.nc / tc::SPLIT_COLS), tc::SPLIT_THREADS, (size_t)(q->nr / 2) * 33 * 4,
-                                  q->st>>>(X, (__half*)q->xhT, (__half*)q->xlT, q->xs, q->nr, a.ncols,
-                                           mode == QDHT_MASKED ? q->kmax : nullptr, a.cmap);
+                                  q->st>>>(xc ? q->xc : X, (__half*)q->xhT, (__half*)q->xlT, q->xs, q->nr,
+                                           xc ? a.nc : a.ncols, mode == QDHT_MASKED ? q->kmax : nullptr, a.cmap, xc);
         (*nlaunch)++;
         a.hscale = q->hs;
         a.xscale = q->xs;
@@ -1155,6 +1196,12 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
         const unsigned g2 = (unsigned)(nt2 < q->sms ? nt2 : q->sms);
         tc::qdht_tc2_kernel<<<g2, tc::THREADS2, tc::SMEM2_BYTES, q->st>>>(q->map_hi64, q->map_lo64, q->map_bh, q->map_bl, a);
         (*nlaunch)++;
+        if (a.yc) {
+            const size_t tot = (size_t)q->nr * q->nt;
+            tc::qdht_expand_kernel<<<(unsigned)std::min<size_t>((tot + 255) / 256, (size_t)q->sms * 16), 256, 0, q->st>>>(
+                a.yc, Y, q->nr, q->nt, a.nc, q->cinv);
+            (*nlaunch)++;
+        }
         return cudaGetLastError();
     }
     const int ntiles = (q->nr / tc::BM) * (a.ncols / tc::BN);
@@ -1194,6 +1241,13 @@ cudaError_t qdht_tc_lstep_adj(QdhtTc* q, const float* fb, float* sb, float* b1b,
     return cudaGetLastError();
 }
 
+float* qdht_tc_compact_x(QdhtTc* q, const int** cinv, int* nc) {
+    if (!q || !q->wide || !q->xc) return nullptr;
+    if (cinv) *cinv = q->cinv;
+    if (nc) *nc = q->nc_act;
+    return q->xc;
+}
+
 int qdht_tc_check(QdhtTc* q, std::string* msg) {
     unsigned e[2] = {0, 0};
     if (cudaMemcpy(e, q->err, 8, cudaMemcpyDeviceToHost) != cudaSuccess) return 1;
@@ -1211,7 +1265,7 @@ int qdht_tc_check(QdhtTc* q, std::string* msg) {
 void qdht_tc_destroy(QdhtTc* q) {
     if (!q) return;
     void* ptrs[] = {q->hh, q->hl, q->kr, q->ki, q->ho, q->kt2, q->kmax, q->err, q->xhT, q->xlT, q->hh16, q->hl16, q->hs, q->xs,
-                    q->cmap, q->zpos};
+                    q->cmap, q->zpos, q->cinv, q->yc, q->xc};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete q;

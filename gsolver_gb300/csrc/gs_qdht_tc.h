@@ -21,9 +21,15 @@ int qdht_tc_set_lstep(QdhtTc* q, const double* omega, const double* wavenum, con
                       double omega_min, double omega_max, std::string* msg);
 // Nonzero (with a message) if a kernel recorded an expired wait since the last check.
 int qdht_tc_check(QdhtTc* q, std::string* msg);
-// Y = QDHT(X) with the given mode (QDHT_PLAIN / QDHT_LSTEP / QDHT_MASKED).
+// Y = QDHT(X) with the given mode (QDHT_PLAIN / QDHT_LSTEP / QDHT_MASKED).  x_compact: for the
+// linear-step transform, X's spectral-window columns are already in the compact array of
+// qdht_tc_compact_x (X itself is not read).
 cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const LstepArgs& L, long long* nlaunch,
-                        std::string* msg);
+                        std::string* msg, bool x_compact = false);
+// The compact [n_r][nc] input array of the linear-step transform and its position map (cinv[p]:
+// the column of position p's (re, im) pair, or -1 outside the spectral window); null when the
+// plan has no window columns (set_lstep not called, or a width outside the wide-tile path).
+float* qdht_tc_compact_x(QdhtTc* q, const int** cinv, int* nc);
 // Adjoint of the QDHT_LSTEP epilogue's linear step, elementwise over [n_r][n_t] (FP32, the
 // epilogue's tables): fb = cotangent of FIELD (k,omega), sb of BIGBUFFER2 (in: after the
 // step, out: before), b1b out: of BIGBUFFER1 (k,omega).
