@@ -701,15 +701,31 @@ __device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, 
 
 // The masked inverse's result from its compact array: row i of Y (all n_t positions, coalesced)
 // takes the pair cinv[p] of yc where p is inside the spectral window and zeros elsewhere.
+// Two positions per thread (one 16-byte store), four stores in flight per thread.
 __global__ void qdht_expand_kernel(const float* __restrict__ yc, float* __restrict__ Y, int nr, int nt, int nc,
                                    const int* __restrict__ cinv) {
-    const size_t total = (size_t)nr * nt;
-    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
-        const size_t i = idx / nt;
-        const int p = (int)(idx - i * nt);
-        const int c = cinv[p];
-        const float2 v = c >= 0 ? *reinterpret_cast<const float2*>(yc + i * nc + c) : make_float2(0.f, 0.f);
-        *reinterpret_cast<float2*>(Y + 2 * idx) = v;
+    const size_t total = (size_t)nr * nt / 2;   // position pairs (n_t even)
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    for (size_t q0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q0 < total; q0 += 4 * stride) {
+        float4 v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const size_t q = q0 + u * stride;
+            v[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (q < total) {
+                const size_t idx = 2 * q, i = idx / nt;
+                const int p = (int)(idx - i * nt);
+                const int2 c = *reinterpret_cast<const int2*>(cinv + p);
+                const float* row = yc + i * nc;
+                if (c.x >= 0) { const float2 a = *reinterpret_cast<const float2*>(row + c.x); v[u].x = a.x; v[u].y = a.y; }
+                if (c.y >= 0) { const float2 b = *reinterpret_cast<const float2*>(row + c.y); v[u].z = b.x; v[u].w = b.y; }
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const size_t q = q0 + u * stride;
+            if (q < total) *reinterpret_cast<float4*>(Y + 4 * q) = v[u];
+        }
     }
 }
 
@@ -1197,8 +1213,8 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
         tc::qdht_tc2_kernel<<<g2, tc::THREADS2, tc::SMEM2_BYTES, q->st>>>(q->map_hi64, q->map_lo64, q->map_bh, q->map_bl, a);
         (*nlaunch)++;
         if (a.yc) {
-            const size_t tot = (size_t)q->nr * q->nt;
-            tc::qdht_expand_kernel<<<(unsigned)std::min<size_t>((tot + 255) / 256, (size_t)q->sms * 16), 256, 0, q->st>>>(
+            const size_t tot = (size_t)q->nr * q->nt / 2;
+            tc::qdht_expand_kernel<<<(unsigned)std::min<size_t>((tot + 1023) / 1024, (size_t)q->sms * 8), 256, 0, q->st>>>(
                 a.yc, Y, q->nr, q->nt, a.nc, q->cinv);
             (*nlaunch)++;
         }
