@@ -338,6 +338,12 @@ int gs_upload_tables(gs_handle* h, const gs_tables* t) {
     }
     if (h->tc) {
         std::string m;
+        // the plan's compact copies are rebuilt: BIGBUFFER2 takes its window columns back first
+        if (h->s_compact) {
+            const int rc = gsi::spec_sync(h);
+            if (rc) return rc;
+            gsi::spec_written(h);
+        }
         if (gs::qdht_tc_set_matrix(h->tc, t->qdht_c, t->qdht_m1, &m)) return fail(h, GS_ERR_CUDA, "mixed QDHT matrix: " + m);
         if (gs::qdht_tc_set_lstep(h->tc, om.data(), wn.data(), ho.data(), t->kt2, h->p.omega_min, h->p.omega_max, &m))
             return fail(h, GS_ERR_CUDA, "mixed QDHT: " + m);
@@ -377,7 +383,8 @@ static LstepArgs lstep_args(gs_handle* h, double dz) {
 }
 
 // QDHT of device array X -> Y (mode: plain / fused linear step / masked input).
-int gsi::run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz, bool x_compact) {
+int gsi::run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz, int flags) {
+    if (Y == h->S && mode == QDHT_PLAIN) spec_written(h);
     LstepArgs L = lstep_args(h, dz);
     if (h->fp64) {
         const bool win = mode != QDHT_PLAIN && h->win64;
@@ -385,7 +392,7 @@ int gsi::run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz, boo
                             win ? h->win64 : nullptr, h->nwin64, h->zpos64, h->nz64));
     } else {
         std::string m;
-        cudaError_t e = gs::qdht_tc_run(h->tc, mode, (const float*)X, (float*)Y, L, &h->launches, &m, x_compact);
+        cudaError_t e = gs::qdht_tc_run(h->tc, mode, (const float*)X, (float*)Y, L, &h->launches, &m, flags);
         if (e != cudaSuccess) return fail(h, GS_ERR_CUDA, "mixed QDHT: " + m + " " + cudaGetErrorString(e));
     }
     return GS_OK;
@@ -467,6 +474,7 @@ static void* pinned_device_ptr(const void* host, size_t bytes) {
 
 int gsi::permute_in(gs_handle* h, const double* host, void* dst) {
     const size_t nel = (size_t)h->nr * h->nt;
+    if (dst == h->S) spec_written(h);
     if (void* dp = pinned_device_ptr(host, nel * 16)) {   // read over the host link, no staging copy
         cudaError_t e = h->fp64 ? launch_permute_host<double>(+1, dp, dst, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches)
                                 : launch_permute_host<float>(+1, dp, dst, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches);
@@ -481,6 +489,10 @@ int gsi::permute_in(gs_handle* h, const double* host, void* dst) {
 }
 int gsi::permute_out(gs_handle* h, const void* src, double* host) {
     const size_t nel = (size_t)h->nr * h->nt;
+    if (src == h->S) {
+        const int rc = spec_sync(h);
+        if (rc) return rc;
+    }
     if (void* dp = pinned_device_ptr(host, nel * 16)) {   // written over the host link
         cudaError_t e = h->fp64 ? launch_permute_host<double>(-1, src, dp, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches)
                                 : launch_permute_host<float>(-1, src, dp, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches);
@@ -724,11 +736,30 @@ int gs_nl_step(gs_handle* h, double zstep, double* max_a2, double* max_nl2) {
     return nl_step(h, zstep, max_a2, max_nl2);
 }
 
+int gsi::spec_sync(gs_handle* h) {
+    if (!h->s_compact) return GS_OK;
+    CK(h, gs::qdht_tc_spec_copy(h->tc, (float*)h->S, 0, &h->launches));   // S stays current, the copy too
+    return GS_OK;
+}
+
+void gsi::spec_written(gs_handle* h) { h->s_compact = false; }
+
+int gsi::spec_prepare(gs_handle* h) {
+    if (h->s_compact || h->fp64 || !h->tc || !gs::qdht_tc_has_compact(h->tc)) return GS_OK;
+    CK(h, gs::qdht_tc_spec_copy(h->tc, (float*)h->S, 1, &h->launches));
+    h->s_compact = true;
+    return GS_OK;
+}
+
 int gsi::lstep(gs_handle* h, double dz) {
-    if (h->time_qdht) CK(h, cudaEventRecord(h->ev0, h->st));
-    int rc = run_qdht(h, QDHT_LSTEP, h->NB, h->S, dz, h->nbc_valid);
+    // mixed wide plans keep BIGBUFFER2's window columns compact from step to step
+    int rc = spec_prepare(h);
     if (rc) return rc;
-    rc = run_qdht(h, QDHT_MASKED, h->S, h->A, dz);
+    const int fs = h->s_compact ? gs::QTC_S_COMPACT : 0;
+    if (h->time_qdht) CK(h, cudaEventRecord(h->ev0, h->st));
+    rc = run_qdht(h, QDHT_LSTEP, h->NB, h->S, dz, fs | (h->nbc_valid ? gs::QTC_X_COMPACT : 0));
+    if (rc) return rc;
+    rc = run_qdht(h, QDHT_MASKED, h->S, h->A, dz, fs);
     if (rc) return rc;
     if (h->time_qdht) {
         CK(h, cudaEventRecord(h->ev1, h->st));

@@ -350,6 +350,8 @@ int gs_gradient(gs_handle* h, const double* field_in, int n_steps, const double*
         if (n % L.K == 0 && n < last0) {
             char* ck = P.ck + (size_t)(n / L.K) * 2 * arr;
             CK(h, cudaMemcpyAsync(ck, h->A, arr, cudaMemcpyDeviceToDevice, h->st));
+            rc = gsi::spec_sync(h);
+            if (rc) return rc;
             CK(h, cudaMemcpyAsync(ck + arr, h->S, arr, cudaMemcpyDeviceToDevice, h->st));
         }
         const bool rec = h->p.nonlinear && n >= last0;
@@ -370,6 +372,7 @@ int gs_gradient(gs_handle* h, const double* field_in, int n_steps, const double*
             const char* ck = P.ck + (size_t)seg * 2 * arr;
             CK(h, cudaMemcpyAsync(h->A, ck, arr, cudaMemcpyDeviceToDevice, h->st));
             CK(h, cudaMemcpyAsync(h->S, ck + arr, arr, cudaMemcpyDeviceToDevice, h->st));
+            gsi::spec_written(h);
             for (int m = n0; m < n1 && !rc; m++) {
                 const GsTape tp = tape_of(L, P.tape, m - n0);
                 rc = gsi::nl_stages(h, dz_rk[m], h->p.nonlinear ? &tp : nullptr);

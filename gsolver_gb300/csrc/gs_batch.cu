@@ -125,6 +125,9 @@ int gs_batch_step(gs_batch* b, int n_steps, const double* dz, int use_graph) {
     }
     BCK(b, cudaSetDevice(b->device));
     for (gs_handle* h : b->h) BCK(b, cudaMemsetAsync(h->err_dev, 0, 4, h->st));
+    // the compact copies of BIGBUFFER2 are taken now, outside any graph capture
+    for (size_t i = 0; i < b->h.size(); i++)
+        if (gsi::spec_prepare(b->h[i])) return bfail(b, GS_ERR_CUDA, "pulse " + std::to_string(i) + ": " + b->h[i]->err);
     // the pulses' streams may hold earlier work: the batch stream waits for all of it
     for (size_t i = 0; i < b->h.size(); i++) {
         BCK(b, cudaEventRecord(b->join[i], b->h[i]->st));
@@ -211,10 +214,12 @@ int gs_batch_autotune(gs_batch* b, const double* dz, double* ms_default, double*
             char* st = snap[i];
             if (!restore) {
                 BCK(b, cudaMemcpyAsync(st, h->A, bytes, cudaMemcpyDeviceToDevice, h->st));
+                if (gsi::spec_sync(h)) return bfail(b, GS_ERR_CUDA, "pulse " + std::to_string(i) + ": " + h->err);
                 BCK(b, cudaMemcpyAsync(st + bytes, h->S, bytes, cudaMemcpyDeviceToDevice, h->st));
             } else {
                 BCK(b, cudaMemcpyAsync(h->A, st, bytes, cudaMemcpyDeviceToDevice, h->st));
                 BCK(b, cudaMemcpyAsync(h->S, st + bytes, bytes, cudaMemcpyDeviceToDevice, h->st));
+                gsi::spec_written(h);
             }
         }
         return GS_OK;

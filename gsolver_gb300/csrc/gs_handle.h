@@ -54,6 +54,7 @@ struct gs_handle {
     double nl_ms = 0;
     int adj_stride = 0;   // checkpoint stride of the last gs_gradient
     bool nbc_valid = false;   // the last NL step also wrote NB's window columns compactly (mixed)
+    bool s_compact = false;   // BIGBUFFER2's window columns are current only in the plan's compact copy
     // FP64 QDHT: the spectral window's columns (padded to 64 with -1) and the positions outside
     int *win64 = nullptr, *zpos64 = nullptr;
     int nwin64 = 0, nz64 = 0;
@@ -79,8 +80,15 @@ namespace gsi {
 int fail(gs_handle* h, int code, const std::string& msg);
 int cuda_fail(gs_handle* h, cudaError_t e, const char* where);
 // QDHT of device array X -> Y (gs::QDHT_PLAIN / _LSTEP / _MASKED)
-// x_compact: the linear-step transform reads the compact window columns its producer wrote
-int run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz, bool x_compact = false);
+// flags: the tensor-core plan's QTC_* flags (gs_qdht_tc.h; 0 for the FP64 path)
+int run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz, int flags = 0);
+// BIGBUFFER2 kept compact by the mixed plan between steps (window columns): spec_sync writes
+// them back into S before S is read outside the steps; spec_written marks S as rewritten
+// (the copy is taken again at the next step); spec_prepare takes the copy now (before a
+// CUDA-graph capture of steps, which must not contain it)
+int spec_sync(gs_handle* h);
+void spec_written(gs_handle* h);
+int spec_prepare(gs_handle* h);
 // calculate_NLstep's four RK4 stages: NB = RK4 increment of A (no host sync); with a tape
 // the stages are recorded (fused rows only)
 int nl_stages(gs_handle* h, double dz, const GsTape* tape);

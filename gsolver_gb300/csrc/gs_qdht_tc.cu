@@ -74,6 +74,7 @@ struct TcArgs {
     int nc;
     const int* cmap;
     float* yc;   // non-null: the output goes to this [nr][nc] compact array instead of Y
+    int ycompact;   // linear step: Y is the compact [nr][nc] copy of BIGBUFFER2's window columns
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -681,7 +682,8 @@ __device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, 
         if (rc < 0) continue;               // padding
         const int p = rc >> 1;
         if (i > a.kmax[p]) continue;        // outside the window: BIGBUFFER2 untouched
-        float2* y2 = reinterpret_cast<float2*>(a.Y + (size_t)i * a.ncols + rc);
+        float2* y2 = reinterpret_cast<float2*>(a.ycompact ? a.Y + (size_t)i * a.nc + cg + 2 * e
+                                                          : a.Y + (size_t)i * a.ncols + rc);
         const float k1 = a.kr[p], k2 = a.ki[p];
         const float sq = sqrt_ho_f(-kt2i / k1 / k1);
         float2 b2 = *y2;
@@ -725,6 +727,24 @@ __global__ void qdht_expand_kernel(const float* __restrict__ yc, float* __restri
         for (int u = 0; u < 4; u++) {
             const size_t q = q0 + u * stride;
             if (q < total) *reinterpret_cast<float4*>(Y + 4 * q) = v[u];
+        }
+    }
+}
+
+// BIGBUFFER2's window columns to / from their compact copy: dir > 0 S -> sc (padding columns
+// zero), dir < 0 sc -> S.  One (re, im) pair per thread.
+__global__ void qdht_spec_copy_kernel(float* __restrict__ S, float* __restrict__ sc, int nr, int ncols, int nc,
+                                      const int* __restrict__ cmap, int dir) {
+    const size_t total = (size_t)nr * (nc / 2);
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = idx / (nc / 2);
+        const int c = 2 * (int)(idx - i * (nc / 2));
+        const int rc = cmap[c];
+        float2* cpt = reinterpret_cast<float2*>(sc + i * nc + c);
+        if (dir > 0) {
+            *cpt = rc >= 0 ? *reinterpret_cast<const float2*>(S + i * ncols + rc) : make_float2(0.f, 0.f);
+        } else if (rc >= 0) {
+            *reinterpret_cast<float2*>(S + i * ncols + rc) = *cpt;
         }
     }
 }
@@ -924,6 +944,7 @@ struct QdhtTc {
     int* cinv = nullptr;      // [n_t]: compact column of position p's pair (even), or -1
     float* yc = nullptr;      // [n_r][nc_act]: the masked inverse's compact result
     float* xc = nullptr;      // [n_r][nc_act]: a compact linear-step input written by its producer
+    float* sc = nullptr;      // [n_r][nc_act]: BIGBUFFER2's window columns kept compact between steps
     CUtensorMap map_bh, map_bl, map_hi64, map_lo64;   // 32-half boxes in the 64-byte swizzle
     // tensor maps of the X operands seen so far (the handle's few state arrays)
     std::vector<std::pair<const float*, CUtensorMap>> xmaps;
@@ -1136,8 +1157,9 @@ int qdht_tc_set_lstep(QdhtTc* q, const double* omega, const double* wavenum, con
         if (q->cinv) cudaFree(q->cinv);
         if (q->yc) cudaFree(q->yc);
         if (q->xc) cudaFree(q->xc);
+        if (q->sc) cudaFree(q->sc);
         q->cmap = q->zpos = q->cinv = nullptr;
-        q->yc = q->xc = nullptr;
+        q->yc = q->xc = q->sc = nullptr;
         q->nc_act = (int)cm.size();
         q->nz = (int)zp.size();
         bool okc = (cm.empty() || (cudaMalloc(&q->cmap, cm.size() * 4) == cudaSuccess &&
@@ -1148,6 +1170,7 @@ int qdht_tc_set_lstep(QdhtTc* q, const double* omega, const double* wavenum, con
                    cudaMemcpy(q->cinv, ci.data(), (size_t)nt * 4, cudaMemcpyHostToDevice) == cudaSuccess &&
                    (cm.empty() || (cudaMalloc(&q->yc, (size_t)nr * cm.size() * 4) == cudaSuccess &&
                                    cudaMalloc(&q->xc, (size_t)nr * cm.size() * 4) == cudaSuccess &&
+                                   cudaMalloc(&q->sc, (size_t)nr * cm.size() * 4) == cudaSuccess &&
                                    cudaMemset(q->xc, 0, (size_t)nr * cm.size() * 4) == cudaSuccess));
         if (!okc) {
             if (msg) *msg = "window column list upload failed";
@@ -1159,7 +1182,7 @@ int qdht_tc_set_lstep(QdhtTc* q, const double* omega, const double* wavenum, con
 }
 
 cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const LstepArgs& L, long long* nlaunch,
-                        std::string* msg, bool x_compact) {
+                        std::string* msg, int flags) {
     if (mode != QDHT_PLAIN && !q->have_lstep) {
         if (msg) *msg = "linear-step tables not set";
         return cudaErrorInvalidValue;
@@ -1182,6 +1205,7 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
     a.nc = a.ncols;
     a.cmap = nullptr;
     a.yc = nullptr;
+    a.ycompact = 0;
     if (q->wide) {
         // The linear step leaves BIGBUFFER2 untouched outside the spectral window and the masked
         // inverse transforms a zero column there: both run on the window's columns only (the
@@ -1199,11 +1223,22 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
             }
         }
         if (a.nc == 0) return cudaGetLastError();
-        const bool xc = compact && x_compact && mode == QDHT_LSTEP;   // X already compact in q->xc
+        const bool s_comp = compact && (flags & QTC_S_COMPACT) && q->sc;
+        // where the split reads a compact X: BIGBUFFER1's window columns (linear step) or
+        // BIGBUFFER2's compact copy (masked inverse)
+        const float* xsrc = nullptr;
+        if (mode == QDHT_LSTEP && (flags & QTC_X_COMPACT)) xsrc = q->xc;
+        if (mode == QDHT_MASKED && s_comp) xsrc = q->sc;
+        const bool xc = xsrc != nullptr;
+        if (mode == QDHT_LSTEP && s_comp) {   // the epilogue updates the compact copy
+            Y = q->sc;
+            a.Y = q->sc;
+            a.ycompact = 1;
+        }
         // split X into the K-major FP16 hi / lo operands and the column scales (the window mask
         // of the inverse applied), then the GEMM on 128 x 256 tiles
         tc::qdht_split16_kernel<<<(unsigned)(a.nc / tc::SPLIT_COLS), tc::SPLIT_THREADS, (size_t)(q->nr / 2) * 33 * 4,
-                                  q->st>>>(xc ? q->xc : X, (__half*)q->xhT, (__half*)q->xlT, q->xs, q->nr,
+                                  q->st>>>(xc ? xsrc : X, (__half*)q->xhT, (__half*)q->xlT, q->xs, q->nr,
                                            xc ? a.nc : a.ncols, mode == QDHT_MASKED ? q->kmax : nullptr, a.cmap, xc);
         (*nlaunch)++;
         a.hscale = q->hs;
@@ -1257,6 +1292,17 @@ cudaError_t qdht_tc_lstep_adj(QdhtTc* q, const float* fb, float* sb, float* b1b,
     return cudaGetLastError();
 }
 
+bool qdht_tc_has_compact(const QdhtTc* q) { return q && q->wide && q->sc != nullptr; }
+
+cudaError_t qdht_tc_spec_copy(QdhtTc* q, float* S, int to_compact, long long* nlaunch) {
+    if (!qdht_tc_has_compact(q)) return cudaErrorInvalidValue;
+    const size_t tot = (size_t)q->nr * (q->nc_act / 2);
+    tc::qdht_spec_copy_kernel<<<(unsigned)std::min<size_t>((tot + 255) / 256, (size_t)q->sms * 16), 256, 0, q->st>>>(
+        S, q->sc, q->nr, 2 * q->nt, q->nc_act, q->cmap, to_compact ? 1 : -1);
+    (*nlaunch)++;
+    return cudaGetLastError();
+}
+
 float* qdht_tc_compact_x(QdhtTc* q, const int** cinv, int* nc) {
     if (!q || !q->wide || !q->xc) return nullptr;
     if (cinv) *cinv = q->cinv;
@@ -1281,7 +1327,7 @@ int qdht_tc_check(QdhtTc* q, std::string* msg) {
 void qdht_tc_destroy(QdhtTc* q) {
     if (!q) return;
     void* ptrs[] = {q->hh, q->hl, q->kr, q->ki, q->ho, q->kt2, q->kmax, q->err, q->xhT, q->xlT, q->hh16, q->hl16, q->hs, q->xs,
-                    q->cmap, q->zpos, q->cinv, q->yc, q->xc};
+                    q->cmap, q->zpos, q->cinv, q->yc, q->xc, q->sc};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete q;

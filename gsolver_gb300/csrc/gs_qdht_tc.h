@@ -21,11 +21,19 @@ int qdht_tc_set_lstep(QdhtTc* q, const double* omega, const double* wavenum, con
                       double omega_min, double omega_max, std::string* msg);
 // Nonzero (with a message) if a kernel recorded an expired wait since the last check.
 int qdht_tc_check(QdhtTc* q, std::string* msg);
-// Y = QDHT(X) with the given mode (QDHT_PLAIN / QDHT_LSTEP / QDHT_MASKED).  x_compact: for the
-// linear-step transform, X's spectral-window columns are already in the compact array of
-// qdht_tc_compact_x (X itself is not read).
+// Y = QDHT(X) with the given mode (QDHT_PLAIN / QDHT_LSTEP / QDHT_MASKED).  Flags:
+//   QTC_X_COMPACT  linear step: X's spectral-window columns are already in the compact array
+//                  of qdht_tc_compact_x (X itself is not read);
+//   QTC_S_COMPACT  BIGBUFFER2's window columns live in the plan's compact copy: the linear
+//                  step updates it (Y is not touched) and the masked inverse reads it (X is
+//                  not read); see qdht_tc_spec_copy.
+enum { QTC_X_COMPACT = 1, QTC_S_COMPACT = 2 };
 cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const LstepArgs& L, long long* nlaunch,
-                        std::string* msg, bool x_compact = false);
+                        std::string* msg, int flags = 0);
+// The plan keeps compact copies of the window's columns (wide-tile plans with linear-step tables).
+bool qdht_tc_has_compact(const QdhtTc* q);
+// Copy BIGBUFFER2 S's window columns into the compact copy (to_compact != 0) or back into S.
+cudaError_t qdht_tc_spec_copy(QdhtTc* q, float* S, int to_compact, long long* nlaunch);
 // The compact [n_r][nc] input array of the linear-step transform and its position map (cinv[p]:
 // the column of position p's (re, im) pair, or -1 outside the spectral window); null when the
 // plan has no window columns (set_lstep not called, or a width outside the wide-tile path).
