@@ -77,3 +77,35 @@ def test_pinned_pointer_inside_a_larger_allocation():
     P.get_field_ptr(big[n:].data_ptr(), None)
     assert np.array_equal(big.numpy()[n:], ref)
     assert not big.numpy()[:n].any()   # nothing written before the pointer
+
+
+def test_compact_spectrum_state_transitions():
+    """BIGBUFFER2's window columns live in the mixed plan's compact copy between steps: reading
+    the state after every step, replacing it mid-run, or reading it only at the end gives
+    bit-identical fields and spectra."""
+    T = setup(n_r=128, n_t=1024)
+    f0 = T["field"]
+    a = gs.Propagator(T, precision=gs.PREC_MIXED)
+    b = gs.Propagator(T, precision=gs.PREC_MIXED)
+    a.set_field(f0)
+    b.set_field(f0)
+    for _ in range(3):
+        for P in (a, b):
+            P.nl_step(DZ)
+            P.lstep(DZ)
+        fa, sa = a.get_field(want_spec=True)   # a is read back after every step
+    fb, sb = b.get_field(want_spec=True)
+    assert np.array_equal(fa, fb) and np.array_equal(sa, sb)
+    # replace the state mid-run on one handle; a fresh handle started there agrees
+    rng = np.random.default_rng(2)
+    s_new = sb * (1 + 1e-3 * rng.standard_normal(sb.shape))
+    b.set_field(fb, spec=s_new)
+    c = gs.Propagator(T, precision=gs.PREC_MIXED)
+    c.set_field(fb, spec=s_new)
+    for P in (b, c):
+        for _ in range(2):
+            P.nl_step(DZ)
+            P.lstep(DZ)
+    fb2, sb2 = b.get_field(want_spec=True)
+    fc2, sc2 = c.get_field(want_spec=True)
+    assert np.array_equal(fb2, fc2) and np.array_equal(sb2, sc2)
