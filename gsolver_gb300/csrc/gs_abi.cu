@@ -639,6 +639,40 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
         const int* cinv = nullptr;
         int ncw = 0;
         float* nbc = (!h->fp64 && h->tc) ? gs::qdht_tc_compact_x(h->tc, &cinv, &ncw) : nullptr;
+        if (h->all_stages_thr != h->nl_threads) {   // decided once per launch shape
+            h->all_stages = nl_stage_all_preferred<Rl>(nt, h->nl_threads, nr) ? 1 : 0;
+            h->all_stages_thr = h->nl_threads;
+        }
+        if (h->all_stages == 1) {   // the four stages of each row in one launch
+            FftArgs<Rl> f1 = fa;
+            f1.rows = nr; f1.kp = KP;
+            f1.all_stages = 1;
+            f1.dzs = dz;
+            PlasmaArgs<Rl> ps = pa;
+            if (tape) {   // stage s's record at a constant stride from stage 0's
+                ps.tape_e = (T2*)tape->e[0];
+                ps.tape_rho = (Rl*)tape->rho[0];
+                ps.tape_q = (Rl*)tape->q[0];
+                ps.row_ion = tape->ion[0];
+                ps.tape_stride = (size_t)((char*)tape->e[1] - (char*)tape->e[0]);
+            }
+            SpecArgs<Rl> s2 = sa;
+            s2.stage = 0;
+            for (int j = 0; j < 3; j++) s2.kst[j] = kst[j];
+            s2.nbc = nbc;
+            s2.cinv = cinv;
+            s2.ncw = ncw;
+            const bool tm = h->time_nl && !tape;
+            if (tm) CK(h, cudaEventRecord(h->nl_ev[0], h->st));
+            CK(h, launch_nl_stage<Rl>(f1, ps, A, s2, nr, h->st, &h->launches));
+            if (tm) {
+                CK(h, cudaEventRecord(h->nl_ev[1], h->st));
+                h->nl_ev_pending = true;
+                h->nl_ev_one = true;
+            }
+            h->nbc_valid = nbc != nullptr;
+            return GS_OK;
+        }
         for (int s = 0; s < 4; s++) {
             FftArgs<Rl> f1 = fa;
             f1.rows = nr; f1.kp = s > 0 ? kst[s - 1] : KP;
@@ -710,11 +744,12 @@ static int nl_step(gs_handle* h, double dz, double* max_a2, double* max_nl2) {
     CK(h, cudaMemcpyAsync(&err, h->err_dev, 4, cudaMemcpyDeviceToHost, h->st));
     CK(h, cudaStreamSynchronize(h->st));
     if (h->nl_ev_pending) {   // fold the stage kernels' event times into the gs_nl_timing totals
-        for (int s = 0; s < 4; s++) {
+        for (int s = 0; s < (h->nl_ev_one ? 1 : 4); s++) {
             float f = 0;
             CK(h, cudaEventElapsedTime(&f, h->nl_ev[2 * s], h->nl_ev[2 * s + 1]));
             h->nl_ms += f;
         }
+        h->nl_ev_one = false;
         h->nl_stages_timed += 4;
         h->nl_ev_pending = false;
     }

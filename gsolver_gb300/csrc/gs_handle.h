@@ -52,6 +52,9 @@ struct gs_handle {
     bool time_nl = false, nl_ev_pending = false;
     cudaEvent_t nl_ev[8] = {};   // before / after each RK4-stage launch
     double nl_ms = 0;
+    bool nl_ev_one = false;   // the pending events bracket one launch of all four stages
+    int all_stages = -1;      // fused path: all four stages per launch (1) or one per stage (0)
+    int all_stages_thr = -1;  // ... decided for this nl_threads value
     int adj_stride = 0;   // checkpoint stride of the last gs_gradient
     bool nbc_valid = false;   // the last NL step also wrote NB's window columns compactly (mixed)
     bool s_compact = false;   // BIGBUFFER2's window columns are current only in the plan's compact copy

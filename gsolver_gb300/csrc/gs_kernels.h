@@ -24,6 +24,8 @@ template <typename Rl> struct FftArgs {
     const typename Vec2<Rl>::T* twb;         // per-stage base twiddles (tw_base_offset) or null
     int ahead;                               // fused kernels: rows resident at once; each CTA
                                              // prefetches into L2 the inputs of row + ahead
+    int all_stages;                          // fused stage kernel: all four RK4 stages per launch
+    double dzs;                              // ... with this step size (c dz per stage inside)
 };
 
 template <typename Rl> struct PlasmaArgs {
@@ -42,6 +44,8 @@ template <typename Rl> struct PlasmaArgs {
     // optional record of the stage for the adjoint (fused kernel only): E/N, rho, Q per sample
     typename Vec2<Rl>::T* tape_e;
     Rl *tape_rho, *tape_q;
+    size_t tape_stride;   // all four stages per launch: bytes from stage s's tape arrays and row
+                          // flags to stage s + 1's
     // gas build: single-level PPT ionization with neutral depletion (no avalanche, no
     // recombination) and, when th is set, the third-harmonic source th[t] E_t^3 added to the
     // Kerr source (th[t] = (KERR_TH/KERR) exp(j phi_t), natural time order)
@@ -162,6 +166,8 @@ template <typename Rl> cudaError_t nl_fused_setup(int N);
 template <typename Rl>
 cudaError_t launch_nl_stage(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2<Rl>::T* A, SpecArgs<Rl> s,
                             int rows, cudaStream_t st, long long* nl);
+// whether one launch of all four stages (f.all_stages) suits a grid of this many rows
+template <typename Rl> bool nl_stage_all_preferred(int N, int threads, int rows);
 
 // ---- one RK4 stage over two CTAs per row (gs_nl_pair.cu): rows of N = 2H stored in the
 // P = 2 position order, FP32 N = 32768 / FP64 N = 16384

@@ -42,10 +42,20 @@ template <> __device__ __forceinline__ float qdiv<float>(float a, float b) { ret
 // else inlined); LOGN = 0: any fused row length.  LC = 16: launched with N/16 threads, so each
 // thread's chunk is 16 consecutive samples starting at a multiple of 16 and its shared-memory
 // slots are at constant offsets (pad16(t0 + i) = pad16(t0) + i, pad32(t0 + i) = pad32(t0) + i).
-template <typename Rl, int LOGN = 0, int LC = 0>
-__global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(FftArgs<Rl> f, PlasmaArgs<Rl> a,
-                                                                              const typename Vec2<Rl>::T* __restrict__ A,
-                                                                              SpecArgs<Rl> sp) {
+// the per-stage values of one RK4 stage of a row (the rest comes from the launch's arguments)
+template <typename Rl> struct StageOv {
+    Rl cdz;
+    const typename Vec2<Rl>::T* kp;
+    int track_max, ahead, stage;
+    typename Vec2<Rl>::T* tape_e;
+    Rl *tape_rho, *tape_q;
+    int* row_ion;
+};
+
+template <typename Rl, int LOGN, int LC>
+__device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaArgs<Rl>& a,
+                                             const typename Vec2<Rl>::T* __restrict__ A, const SpecArgs<Rl>& sp,
+                                             const StageOv<Rl>& ov) {
     using T2 = C2<Rl>;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int N = LOGN > 0 ? (1 << LOGN) : f.N;
@@ -68,7 +78,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(
     load_twiddles<Rl>(twh, twl, f.tw, N, tid, nthr);
     // N / nthr = 16 elements per thread (2 when N < 512): loads issued together
     Rl lmax = 0;
-    const Rl cdz = (Rl)f.cdz;
+    const Rl cdz = (Rl)ov.cdz;
     const int per = N / nthr;
     // rows of 2^k points take the 1/N of the inverse transform on the input: scaling by a power
     // of two is exact and commutes with every rounding of the FFT, so IFFT(X/N) = IFFT(X)/N
@@ -78,14 +88,14 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(
         T2 v[16];
 #pragma unroll
         for (int u = 0; u < 16; u++) v[u] = A[base + tid + u * nthr];
-        if (f.track_max) {
+        if (ov.track_max) {
 #pragma unroll
             for (int u = 0; u < 16; u++) lmax = fmax(lmax, v[u].x * v[u].x + v[u].y * v[u].y);
         }
-        if (f.cdz != 0) {
+        if (ov.cdz != 0) {
             T2 k[16];
 #pragma unroll
-            for (int u = 0; u < 16; u++) k[u] = f.kp[base + tid + u * nthr];
+            for (int u = 0; u < 16; u++) k[u] = ov.kp[base + tid + u * nthr];
 #pragma unroll
             for (int u = 0; u < 16; u++) { v[u].x = v[u].x + cdz * k[u].x; v[u].y = v[u].y + cdz * k[u].y; }
         }
@@ -94,26 +104,26 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(
     } else {
         for (int i = tid; i < N; i += nthr) {
             T2 v = A[base + i];
-            if (f.track_max) lmax = fmax(lmax, v.x * v.x + v.y * v.y);
-            if (f.cdz != 0) {
-                const T2 k = f.kp[base + i];
+            if (ov.track_max) lmax = fmax(lmax, v.x * v.x + v.y * v.y);
+            if (ov.cdz != 0) {
+                const T2 k = ov.kp[base + i];
                 v.x = v.x + cdz * k.x;
                 v.y = v.y + cdz * k.y;
             }
             E[pad16(i)] = T2{v.x * sc, v.y * sc};
         }
     }
-    if (f.track_max) {
+    if (ov.track_max) {
         for (int o = 16; o > 0; o >>= 1) lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
         if ((tid & 31) == 0) atomic_max_nonneg(f.max_out, (double)lmax);
     }
     __syncthreads();
     // the row that takes this SM's next slot: its inputs travel to L2 while this row computes
-    if (tid < 32 && f.ahead > 0 && (int)blockIdx.x + f.ahead < f.rows) {
-        const size_t nbase = base + (size_t)f.ahead * N;
+    if (tid < 32 && ov.ahead > 0 && (int)blockIdx.x + ov.ahead < f.rows) {
+        const size_t nbase = base + (size_t)ov.ahead * N;
         prefetch_row_l2(A + nbase, (size_t)N * sizeof(T2), tid);
-        if (f.cdz != 0) prefetch_row_l2(f.kp + nbase, (size_t)N * sizeof(T2), tid - 4);
-        if (sp.stage == 3) {
+        if (ov.cdz != 0) prefetch_row_l2(ov.kp + nbase, (size_t)N * sizeof(T2), tid - 4);
+        if (ov.stage == 3) {
             prefetch_row_l2(sp.kst[0] + nbase, (size_t)N * sizeof(T2), tid - 8);
             prefetch_row_l2(sp.kst[1] + nbase, (size_t)N * sizeof(T2), tid - 12);
         }
@@ -218,7 +228,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(
         zs = (c == 0) ? T2{0, 0} : cend[c - 1];
         zN = cend[nthr - 1];
     }
-    if (tid == 0 && a.row_ion) a.row_ion[blockIdx.x] = ion ? 1 : 0;
+    if (tid == 0 && ov.row_ion) ov.row_ion[blockIdx.x] = ion ? 1 : 0;
 
     // the exact recurrence over this thread's chunk from start value s (rho_{t0-1})
     auto run_chunk = [&](Rl s, Rl* dout) -> Rl {
@@ -361,10 +371,10 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(
             }
             if (LC == 16) E[pad16(t0) + i] = src3;
             else E[pad16(t)] = src3;
-            if (a.tape_e) {   // what the adjoint of this stage reads back (rho only where it ionizes)
-                a.tape_e[base + t] = e;
-                if (ion) a.tape_rho[base + t] = ro;
-                a.tape_q[base + t] = Q;
+            if (ov.tape_e) {   // what the adjoint of this stage reads back (rho only where it ionizes)
+                ov.tape_e[base + t] = e;
+                if (ion) ov.tape_rho[base + t] = ro;
+                ov.tape_q[base + t] = Q;
             }
         }
     }
@@ -406,7 +416,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(
     // (propagator.cu:412).  Batches of SB points per thread: every global read of a batch is
     // issued before use.
     Rl nmax = 0;
-    T2* const kout = sp.stage == 0 ? sp.kst[0] : (sp.stage == 1 ? sp.kst[1] : sp.kst[2]);
+    T2* const kout = ov.stage == 0 ? sp.kst[0] : (ov.stage == 1 ? sp.kst[1] : sp.kst[2]);
     auto combine = [&](auto ion_c, auto last_c) {
         constexpr bool ION = decltype(ion_c)::value;
         constexpr bool last = decltype(last_c)::value;
@@ -464,16 +474,48 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(
             }
         }
     };
-    if (sp.stage == 3) {
+    if (ov.stage == 3) {
         if (ion) combine(std::true_type{}, std::true_type{});
         else combine(std::false_type{}, std::true_type{});
     } else {
         if (ion) combine(std::true_type{}, std::false_type{});
         else combine(std::false_type{}, std::false_type{});
     }
-    if (sp.stage == 3) {
+    if (ov.stage == 3) {
         for (int o = 16; o > 0; o >>= 1) nmax = fmax(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
         if ((tid & 31) == 0) atomic_max_nonneg(sp.max_out, (double)nmax);
+    }
+}
+
+// One RK4 stage (sp.stage) of every row.
+template <typename Rl, int LOGN = 0, int LC = 0>
+__global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(FftArgs<Rl> f, PlasmaArgs<Rl> a,
+                                                                              const typename Vec2<Rl>::T* __restrict__ A,
+                                                                              SpecArgs<Rl> sp) {
+    const StageOv<Rl> ov{f.cdz, f.kp, f.track_max, f.ahead, sp.stage, a.tape_e, a.tape_rho, a.tape_q, a.row_ion};
+    nl_stage_row<Rl, LOGN, LC>(f, a, A, sp, ov);
+}
+
+// All four RK4 stages of every row in turn (step size f.dzs): stage s reads A and the k of
+// stage s - 1 that the same CTA has just written (L2-resident), so between steps a row's state
+// crosses HBM once.  A separate kernel, so that each keeps one inlined copy of the row body.
+template <typename Rl, int LOGN = 0, int LC = 0>
+__global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage4_kernel(FftArgs<Rl> f, PlasmaArgs<Rl> a,
+                                                                               const typename Vec2<Rl>::T* __restrict__ A,
+                                                                               SpecArgs<Rl> sp) {
+    for (int s = 0; s < 4; s++) {
+        StageOv<Rl> ov{(Rl)(s == 0 ? 0.0 : (s < 3 ? f.dzs * 0.5 : f.dzs)),   // as the per-stage launches round it
+                       s > 0 ? sp.kst[s - 1] : f.kp, s == 0, s == 0 ? f.ahead : 0, s,
+                       a.tape_e, a.tape_rho, a.tape_q, a.row_ion};
+        if (a.tape_e) {   // stage s's record for the adjoint
+            const size_t o = (size_t)s * a.tape_stride;
+            ov.tape_e = reinterpret_cast<typename Vec2<Rl>::T*>(reinterpret_cast<char*>(a.tape_e) + o);
+            ov.tape_rho = reinterpret_cast<Rl*>(reinterpret_cast<char*>(a.tape_rho) + o);
+            ov.tape_q = reinterpret_cast<Rl*>(reinterpret_cast<char*>(a.tape_q) + o);
+            ov.row_ion = reinterpret_cast<int*>(reinterpret_cast<char*>(a.row_ion) + o);
+        }
+        if (s > 0) __syncthreads();   // k of stage s - 1 written by every thread of the CTA
+        nl_stage_row<Rl, LOGN, LC>(f, a, A, sp, ov);
     }
 }
 
@@ -502,11 +544,17 @@ template <typename Rl> cudaError_t nl_fused_setup(int N) {
     // device maximum so that a handle on a smaller grid never lowers it for a larger one
     (void)N;
     cudaError_t e = cudaFuncSetAttribute(nl_stage_kernel<Rl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(nl_stage4_kernel<Rl>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     if constexpr (sizeof(Rl) == 4) {   // the FP32 rows of 16384
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(nl_stage_kernel<Rl, 14, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(nl_stage_kernel<Rl, 14>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(nl_stage4_kernel<Rl, 14, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(nl_stage4_kernel<Rl, 14>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     }
     return e;
 }
@@ -530,27 +578,48 @@ template <typename K> static int resident_ctas(K kern, int nthr, size_t smem) {
 }
 
 template <typename Rl>
+bool nl_stage_all_preferred(int N, int threads, int rows) {
+    const int nthr = threads > 0 ? threads : fused_threads<Rl>(N);
+    const size_t sm = FrontSmem<Rl>::bytes(N, nthr);
+    int res = 0;
+    if constexpr (sizeof(Rl) == 4) {
+        if (N == 16384 && nthr == 1024) res = resident_ctas(nl_stage_kernel<Rl, 14, 16>, nthr, sm);
+        else if (N == 16384) res = resident_ctas(nl_stage_kernel<Rl, 14>, nthr, sm);
+    }
+    if (res == 0) res = resident_ctas(nl_stage_kernel<Rl>, nthr, sm);
+    // a row's four stages in one CTA pay off when the grid has several waves: each CTA then
+    // reads the k it just wrote from L2; with fewer rows the per-stage launches keep more
+    // rows in flight
+    return res > 0 && rows >= 4 * res;
+}
+
+template <typename Rl>
 cudaError_t launch_nl_stage(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2<Rl>::T* A, SpecArgs<Rl> s, int rows,
                             cudaStream_t st, long long* nl) {
     const int nthr = f.threads > 0 ? f.threads : fused_threads<Rl>(f.N);
     const size_t sm = FrontSmem<Rl>::bytes(f.N, nthr);
     f.rows = rows;
+    // the instantiation for the launch shape, one stage or all four
+    auto go = [&](auto k1, auto k4) {
+        if (f.all_stages) {
+            f.ahead = resident_ctas(k4, nthr, sm);
+            k4<<<rows, nthr, sm, st>>>(f, a, A, s);
+        } else {
+            f.ahead = resident_ctas(k1, nthr, sm);
+            k1<<<rows, nthr, sm, st>>>(f, a, A, s);
+        }
+    };
     bool done = false;
     if constexpr (sizeof(Rl) == 4) {
         if (f.N == 16384 && nthr == 1024) {
-            f.ahead = resident_ctas(nl_stage_kernel<Rl, 14, 16>, nthr, sm);
-            nl_stage_kernel<Rl, 14, 16><<<rows, nthr, sm, st>>>(f, a, A, s);
+            go(nl_stage_kernel<Rl, 14, 16>, nl_stage4_kernel<Rl, 14, 16>);
             done = true;
         } else if (f.N == 16384) {
-            f.ahead = resident_ctas(nl_stage_kernel<Rl, 14>, nthr, sm);
-            nl_stage_kernel<Rl, 14><<<rows, nthr, sm, st>>>(f, a, A, s);
+            go(nl_stage_kernel<Rl, 14>, nl_stage4_kernel<Rl, 14>);
             done = true;
         }
     }
-    if (!done) {
-        f.ahead = resident_ctas(nl_stage_kernel<Rl>, nthr, sm);
-        nl_stage_kernel<Rl><<<rows, nthr, sm, st>>>(f, a, A, s);
-    }
+    if (!done) go(nl_stage_kernel<Rl>, nl_stage4_kernel<Rl>);
     (*nl)++;
     return cudaGetLastError();
 }
@@ -560,6 +629,7 @@ cudaError_t launch_nl_stage(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2
     template cudaError_t nl_fused_setup<Rl>(int);                                                                 \
     template cudaError_t launch_nl_stage<Rl>(FftArgs<Rl>, PlasmaArgs<Rl>, const typename Vec2<Rl>::T*, SpecArgs<Rl>, \
                                              int, cudaStream_t, long long*);                                      \
+    template bool nl_stage_all_preferred<Rl>(int, int, int);                                                     \
     template bool nl_fused_threads_ok<Rl>(int, int);                                                             \
     template int nl_fused_default_threads<Rl>(int);
 GS_FUSED_INST(double)
