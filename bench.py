@@ -480,7 +480,7 @@ def main():
     ms = e0.elapsed_time(e1)
     launches = P.launch_count() - n0
     q_ms, q_n = P.qdht_timing(enable=False)
-    st_ms, n_st = P.nl_timing(enable=False)
+    st_ms, n_st, n_launch = P.nl_timing(enable=False)
     if world > 1:
         t = torch.tensor([ms], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
@@ -515,14 +515,15 @@ def main():
     st_ach = st_bytes / (st_launch_ms / 1e3) / 1e9 if st_launch_ms else None
     nl_step_ms = st_ms / n_st * 4 if n_st else None
     nl_ach = (16 if esz == 8 else 32) * nr * nt / (nl_step_ms / 1e3) / 1e9 if nl_step_ms else None
-    roof = {"bound": "hbm", "kernel": "nl_stage_kernel" if n_st else "staged NL kernels (not timed)",
+    roof = {"bound": "hbm", "kernel": ("nl_stage4_kernel (four RK4 stages per launch; per-stage figures)"
+                                       if n_launch < n_st else "nl_stage_kernel") if n_st else "staged NL kernels (not timed)",
             "achieved": st_ach, "peak": hbm, "unit": "GB/s", "frac": (st_ach / hbm) if st_ach and hbm else None,
-            "traffic": read_profile_traffic("nl_stage_silica_256x16384.md") if prec == gs.PREC_MIXED else None,
+            "traffic": read_profile_traffic("nl_stage4_silica_1024x16384.md") if prec == gs.PREC_MIXED else None,
             "peak_kind": f"{pk_kind} HBM copy", "launch_ms": st_launch_ms,
             "algorithmic_bytes_per_launch": st_bytes,
             "share_of_step": (st_ms / ms) if ms and n_st else None,
-            "note": "CUDA events around each launch on the handle's stream; traffic = ncu DRAM bytes per launch of a "
-                    "256-row capture scaled by rows (writes still in L2 when the kernel ends are not counted)"}
+            "note": "CUDA events around each launch on the handle's stream, per RK4 stage; traffic = a quarter of "
+                    "the ncu DRAM bytes of one four-stage launch of this workload"}
     roof_nl = {"bound": "hbm", "unit": "GB/s", "peak": hbm, "achieved": nl_ach,
                "frac": (nl_ach / hbm) if nl_ach and hbm else None, "step_ms": nl_step_ms,
                "note": "the whole NL increment (4 RK4 stages, 4 launches) against its one-pass minimum: read A and "

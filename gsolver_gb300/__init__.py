@@ -104,7 +104,7 @@ def load_library(path: str | None = None):
     L.gs_launch_count.argtypes = [V]
     L.gs_launch_count.restype = C.c_longlong
     L.gs_qdht_timing.argtypes = [V, I, PD, C.POINTER(C.c_int)]
-    L.gs_nl_timing.argtypes = [V, I, PD, C.POINTER(C.c_int)]
+    L.gs_nl_timing.argtypes = [V, I, PD, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     L.gs_destroy.argtypes = [V]
     L.gs_last_error.argtypes = [V]
     L.gs_last_error.restype = C.c_char_p
@@ -278,11 +278,11 @@ class Propagator:
         return ms.value, n.value
 
     def nl_timing(self, enable=True):
-        """CUDA-event time of the fused RK4-stage kernel since the previous call:
-        (ms of the stage launches, RK4 stages timed)."""
-        f, n = C.c_double(), C.c_int()
-        self._check(self.L.gs_nl_timing(self.h, int(enable), C.byref(f), C.byref(n)))
-        return f.value, n.value
+        """CUDA-event time of the fused RK4-stage kernels since the previous call:
+        (ms of their launches, RK4 stages timed, launches timed)."""
+        f, n, k = C.c_double(), C.c_int(), C.c_int()
+        self._check(self.L.gs_nl_timing(self.h, int(enable), C.byref(f), C.byref(n), C.byref(k)))
+        return f.value, n.value, k.value
 
     def set_apertures(self, z, r, qdht_x, r_max):
         """Apertures in the reference's array order (the last entry is applied first); gs_step

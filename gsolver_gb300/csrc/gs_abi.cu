@@ -398,10 +398,12 @@ int gsi::run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz, int
     return GS_OK;
 }
 
-int gs_nl_timing(gs_handle* h, int enable, double* ms, int* stages) {
+int gs_nl_timing(gs_handle* h, int enable, double* ms, int* stages, int* launches) {
     if (!h) return GS_ERR_ARG;
     if (ms) *ms = h->nl_ms;
     if (stages) *stages = h->nl_stages_timed;
+    if (launches) *launches = h->nl_launches_timed;
+    h->nl_launches_timed = 0;
     h->nl_ms = 0;
     h->nl_stages_timed = 0;
     h->nl_ev_pending = false;
@@ -749,8 +751,9 @@ static int nl_step(gs_handle* h, double dz, double* max_a2, double* max_nl2) {
             CK(h, cudaEventElapsedTime(&f, h->nl_ev[2 * s], h->nl_ev[2 * s + 1]));
             h->nl_ms += f;
         }
-        h->nl_ev_one = false;
         h->nl_stages_timed += 4;
+        h->nl_launches_timed += h->nl_ev_one ? 1 : 4;
+        h->nl_ev_one = false;
         h->nl_ev_pending = false;
     }
     double a2, n2;

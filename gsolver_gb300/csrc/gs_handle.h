@@ -61,7 +61,7 @@ struct gs_handle {
     // FP64 QDHT: the spectral window's columns (padded to 64 with -1) and the positions outside
     int *win64 = nullptr, *zpos64 = nullptr;
     int nwin64 = 0, nz64 = 0;
-    int nl_stages_timed = 0;
+    int nl_stages_timed = 0, nl_launches_timed = 0;
     double* dump_dev = nullptr;   // 3 n_r + 2 n_t doubles of reduction output, r weights
     void* twb = nullptr;          // per-stage base twiddles of the M-point row FFTs (tw_base_offset)
     int* row_ion = nullptr;       // [n_r] fused NL kernels: row ionizes in the current RK4 stage

@@ -144,11 +144,12 @@ long long gs_launch_count(const gs_handle* h);
  * timing on.  No extra synchronisation: the step's own final sync is reused. */
 int gs_qdht_timing(gs_handle* h, int enable, double* ms_total, int* launches);
 
-/* The same for the fused RK4-stage kernel of gs_nl_step / gs_step (rows that fit one CTA;
- * no counterpart in the reference, which has no kernels to time): milliseconds of the stage
- * launches and the number of RK4 stages timed since the previous call, by CUDA events around
- * each launch on the handle's stream; enable != 0 keeps timing on. */
-int gs_nl_timing(gs_handle* h, int enable, double* ms, int* stages);
+/* The same for the fused RK4-stage kernels of gs_nl_step / gs_step (rows that fit one CTA;
+ * no counterpart in the reference, which has no kernels to time): milliseconds of their
+ * launches, the number of RK4 stages and of launches timed since the previous call (a launch
+ * runs one stage, or all four on large grids), by CUDA events around each launch on the
+ * handle's stream; enable != 0 keeps timing on.  Any output may be NULL. */
+int gs_nl_timing(gs_handle* h, int enable, double* ms, int* stages, int* launches);
 
 /* Reductions of the current FIELD behind the reference's .udf dumps (dump_types.cpp,
  * FILTER_TYPE NO), computed on the device; any output may be NULL:
