@@ -317,8 +317,24 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
         const T2 oma = T2{a.k.oma_re, a.k.oma_im};
         const Rl fRM = a.k.fRM, omf = a.k.omf;
         if (gas && t0 == 0) W0 = (Rl)-1;
+        // the common row (no ionization, solid, Raman recurrence, no record): the Kerr source
+        // only, the same arithmetic as the general loop below
+        const bool plain = !ion && !gas && rscan && !a.th && !ov.tape_e;
 #pragma unroll 4
-        for (int i = 0; i < L; i++) {
+        for (int i = 0; i < (plain ? L : 0); i++) {
+            const T2 e = e_at(i);
+            const Rl I = e.x * e.x + e.y * e.y;
+            z = cmul(ra, z);
+            z.x += I;
+            const T2 v = cadd(cmul(oma, z), cmul(pw, zN));
+            const Rl Q = omf * I + fRM * v.y;
+            pw = cmul(pw, ra);
+            const T2 src3 = T2{Q * e.x, Q * e.y};
+            if (LC == 16) E[pad16(t0) + i] = src3;
+            else E[pad16(t0 + i)] = src3;
+        }
+#pragma unroll 4
+        for (int i = 0; i < (plain ? 0 : L); i++) {
             const int t = t0 + i;
             const T2 e = e_at(i);
             const Rl I = e.x * e.x + e.y * e.y;
