@@ -50,6 +50,8 @@ template <typename Rl> struct StageOv {
     typename Vec2<Rl>::T* tape_e;
     Rl *tape_rho, *tape_q;
     int* row_ion;
+    Rl next_cdz;     // != 0: this stage also leaves the next stage's input (A + next_cdz k) / N in E
+    int preloaded;   // E holds this stage's input already
 };
 
 template <typename Rl, int LOGN, int LC>
@@ -84,7 +86,9 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
     // of two is exact and commutes with every rounding of the FFT, so IFFT(X/N) = IFFT(X)/N
     const bool pow2 = (N & (N - 1)) == 0;
     const Rl sc = pow2 ? (Rl)1 / (Rl)N : (Rl)1;
-    if (per == 16) {
+    if (ov.preloaded) {
+        // the previous stage of this CTA left (A + c dz k) / N in E (four stages per launch)
+    } else if (per == 16) {
         T2 v[16];
 #pragma unroll
         for (int u = 0; u < 16; u++) v[u] = A[base + tid + u * nthr];
@@ -438,7 +442,7 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
         constexpr bool last = decltype(last_c)::value;
         constexpr int SB = ION ? 2 : 4;
         for (int pb = tid; pb < N; pb += SB * nthr) {
-            T2 v[SB], ac[SB], pf[SB], q[SB], k1[SB], k2[SB], k3[SB];
+            T2 v[SB], ac[SB], pf[SB], q[SB], k1[SB], k2[SB], k3[SB], an[SB];
             Rl kc[SB];
 #pragma unroll
             for (int u = 0; u < SB; u++) {
@@ -455,6 +459,8 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
                     k1[u] = in ? sp.kst[0][base + p] : T2{0, 0};
                     k2[u] = in ? sp.kst[1][base + p] : T2{0, 0};
                     k3[u] = in ? sp.kst[2][base + p] : T2{0, 0};
+                } else {
+                    an[u] = (in && ov.next_cdz != 0) ? A[base + p] : T2{0, 0};
                 }
             }
 #pragma unroll
@@ -473,6 +479,13 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
                 }
                 if constexpr (!last) {
                     kout[base + p] = k;
+                    if (ov.next_cdz != 0) {   // the next stage's input, as its load would form it
+                        const Rl nc = ov.next_cdz;
+                        T2 x = an[u];
+                        x.x = x.x + nc * k.x;
+                        x.y = x.y + nc * k.y;
+                        E[pad16(p)] = T2{x.x * sc, x.y * sc};
+                    }
                     continue;
                 }
                 T2 s = k1[u];
@@ -508,7 +521,8 @@ template <typename Rl, int LOGN = 0, int LC = 0>
 __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(FftArgs<Rl> f, PlasmaArgs<Rl> a,
                                                                               const typename Vec2<Rl>::T* __restrict__ A,
                                                                               SpecArgs<Rl> sp) {
-    const StageOv<Rl> ov{f.cdz, f.kp, f.track_max, f.ahead, sp.stage, a.tape_e, a.tape_rho, a.tape_q, a.row_ion};
+    const StageOv<Rl> ov{f.cdz, f.kp, f.track_max, f.ahead, sp.stage, a.tape_e, a.tape_rho, a.tape_q, a.row_ion,
+                         (Rl)0, 0};
     nl_stage_row<Rl, LOGN, LC>(f, a, A, sp, ov);
 }
 
@@ -522,7 +536,9 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage4_kernel
     for (int s = 0; s < 4; s++) {
         StageOv<Rl> ov{(Rl)(s == 0 ? 0.0 : (s < 3 ? f.dzs * 0.5 : f.dzs)),   // as the per-stage launches round it
                        s > 0 ? sp.kst[s - 1] : f.kp, s == 0, s == 0 ? f.ahead : 0, s,
-                       a.tape_e, a.tape_rho, a.tape_q, a.row_ion};
+                       a.tape_e, a.tape_rho, a.tape_q, a.row_ion,
+                       (Rl)(s < 3 ? (s + 1 < 3 ? f.dzs * 0.5 : f.dzs) : 0.0),   // stage s + 1's c dz
+                       s > 0};
         if (a.tape_e) {   // stage s's record for the adjoint
             const size_t o = (size_t)s * a.tape_stride;
             ov.tape_e = reinterpret_cast<typename Vec2<Rl>::T*>(reinterpret_cast<char*>(a.tape_e) + o);
