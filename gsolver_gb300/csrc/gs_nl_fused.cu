@@ -38,10 +38,37 @@ template <typename Rl> struct FrontSmem {
 template <typename Rl> __device__ __forceinline__ Rl qdiv(Rl a, Rl b) { return a / b; }
 template <> __device__ __forceinline__ float qdiv<float>(float a, float b) { return __fdividef(a, b); }
 
-// LOGN > 0: rows of exactly 2^LOGN points (the row FFT with compile-time sizes and nothing
-// else inlined); LOGN = 0: any fused row length.  LC = 16: launched with N/16 threads, so each
-// thread's chunk is 16 consecutive samples starting at a multiple of 16 and its shared-memory
-// slots are at constant offsets (pad16(t0 + i) = pad16(t0) + i, pad32(t0 + i) = pad32(t0) + i).
+// Tensor-memory access of the RK4 sum (four-stage launches of 16384-point FP32 rows): a
+// warp's lane quarter, NC consecutive 32-bit columns per thread; each access waits for itself.
+template <int NC> __device__ __forceinline__ void tm_ld(uint32_t ta, float* v);
+template <> __device__ __forceinline__ void tm_ld<4>(uint32_t ta, float* v) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];\n"
+                 "tcgen05.wait::ld.sync.aligned;"
+                 : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3])
+                 : "r"(ta)
+                 : "memory");
+}
+template <> __device__ __forceinline__ void tm_ld<8>(uint32_t ta, float* v) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
+                 "tcgen05.wait::ld.sync.aligned;"
+                 : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
+                 : "r"(ta)
+                 : "memory");
+}
+template <int NC> __device__ __forceinline__ void tm_st(uint32_t ta, const float* v);
+template <> __device__ __forceinline__ void tm_st<4>(uint32_t ta, const float* v) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};\n"
+                 "tcgen05.wait::st.sync.aligned;" ::"r"(ta),
+                 "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3])
+                 : "memory");
+}
+template <> __device__ __forceinline__ void tm_st<8>(uint32_t ta, const float* v) {
+    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};\n"
+                 "tcgen05.wait::st.sync.aligned;" ::"r"(ta),
+                 "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7])
+                 : "memory");
+}
+
 // the per-stage values of one RK4 stage of a row (the rest comes from the launch's arguments)
 template <typename Rl> struct StageOv {
     Rl cdz;
@@ -52,9 +79,15 @@ template <typename Rl> struct StageOv {
     int* row_ion;
     Rl next_cdz;     // != 0: this stage also leaves the next stage's input (A + next_cdz k) / N in E
     int preloaded;   // E holds this stage's input already
+    uint32_t tmem;   // != 0: the RK4 sum k1 + 2 k2 + 2 k3 lives in tensor memory at this address
 };
 
-template <typename Rl, int LOGN, int LC>
+// LOGN > 0: rows of exactly 2^LOGN points (the row FFT with compile-time sizes and nothing
+// else inlined); LOGN = 0: any fused row length.  LC = 16: launched with N/16 threads, so each
+// thread's chunk is 16 consecutive samples starting at a multiple of 16 and its shared-memory
+// slots are at constant offsets (pad16(t0 + i) = pad16(t0) + i, pad32(t0 + i) = pad32(t0) + i).
+// TMA: ov.tmem holds the RK4 sum (k of stages 0-2 is never stored).
+template <typename Rl, int LOGN, int LC, bool TMA = false>
 __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaArgs<Rl>& a,
                                              const typename Vec2<Rl>::T* __restrict__ A, const SpecArgs<Rl>& sp,
                                              const StageOv<Rl>& ov) {
@@ -444,6 +477,14 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
         for (int pb = tid; pb < N; pb += SB * nthr) {
             T2 v[SB], ac[SB], pf[SB], q[SB], k1[SB], k2[SB], k3[SB], an[SB];
             Rl kc[SB];
+            // the RK4 sum in tensor memory: this thread's points pb + u nthr are its points
+            // (pb - tid) / nthr + u of 16, at columns 32 (warp / 4) + 2 (point) (re, im) of its
+            // lane in the warp's lane quarter
+            float tv[2 * SB];
+            constexpr bool tacc = TMA;
+            const uint32_t ta = ov.tmem + ((uint32_t)(32 * ((tid >> 5) & 3)) << 16) +
+                                (uint32_t)(32 * (tid >> 7) + 2 * ((pb - tid) / nthr));
+            if constexpr (tacc && last) tm_ld<2 * SB>(ta, tv);
 #pragma unroll
             for (int u = 0; u < SB; u++) {
                 const int p = pb + u * nthr;
@@ -456,9 +497,9 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
                 }
                 kc[u] = (in && kerr) ? -sp.kerr[p] : (Rl)0;
                 if constexpr (last) {
-                    k1[u] = in ? sp.kst[0][base + p] : T2{0, 0};
-                    k2[u] = in ? sp.kst[1][base + p] : T2{0, 0};
-                    k3[u] = in ? sp.kst[2][base + p] : T2{0, 0};
+                    k1[u] = (in && !tacc) ? sp.kst[0][base + p] : T2{0, 0};
+                    k2[u] = (in && !tacc) ? sp.kst[1][base + p] : T2{0, 0};
+                    k3[u] = (in && !tacc) ? sp.kst[2][base + p] : T2{0, 0};
                 } else {
                     an[u] = (in && ov.next_cdz != 0) ? A[base + p] : T2{0, 0};
                 }
@@ -478,7 +519,12 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
                     k.y += kc[u] * qs.x;
                 }
                 if constexpr (!last) {
-                    kout[base + p] = k;
+                    if constexpr (!tacc) {
+                        kout[base + p] = k;
+                    } else {
+                        tv[2 * u] = k.x;
+                        tv[2 * u + 1] = k.y;
+                    }
                     if (ov.next_cdz != 0) {   // the next stage's input, as its load would form it
                         const Rl nc = ov.next_cdz;
                         T2 x = an[u];
@@ -491,6 +537,7 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
                 T2 s = k1[u];
                 s = T2{s.x + (Rl)2 * k2[u].x, s.y + (Rl)2 * k2[u].y};
                 s = T2{s.x + (Rl)2 * k3[u].x, s.y + (Rl)2 * k3[u].y};
+                if constexpr (tacc) s = T2{tv[2 * u], tv[2 * u + 1]};
                 const T2 nb = T2{(s.x + k.x) / (Rl)6, (s.y + k.y) / (Rl)6};
                 nmax = fmax(nmax, nb.x * nb.x + nb.y * nb.y);
                 sp.nb[base + p] = nb;
@@ -500,6 +547,15 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
                         if (c >= 0) *reinterpret_cast<float2*>(sp.nbc + (size_t)blockIdx.x * sp.ncw + c) = make_float2(nb.x, nb.y);
                     }
                 }
+            }
+            if constexpr (tacc && !last) {   // k1, then + 2 k2, + 2 k3 in that order
+                if (ov.stage > 0) {
+                    float o[2 * SB];
+                    tm_ld<2 * SB>(ta, o);
+#pragma unroll
+                    for (int i = 0; i < 2 * SB; i++) tv[i] = o[i] + 2.0f * tv[i];
+                }
+                tm_st<2 * SB>(ta, tv);
             }
         }
     };
@@ -522,7 +578,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(
                                                                               const typename Vec2<Rl>::T* __restrict__ A,
                                                                               SpecArgs<Rl> sp) {
     const StageOv<Rl> ov{f.cdz, f.kp, f.track_max, f.ahead, sp.stage, a.tape_e, a.tape_rho, a.tape_q, a.row_ion,
-                         (Rl)0, 0};
+                         (Rl)0, 0, 0u};
     nl_stage_row<Rl, LOGN, LC>(f, a, A, sp, ov);
 }
 
@@ -533,12 +589,29 @@ template <typename Rl, int LOGN = 0, int LC = 0>
 __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage4_kernel(FftArgs<Rl> f, PlasmaArgs<Rl> a,
                                                                                const typename Vec2<Rl>::T* __restrict__ A,
                                                                                SpecArgs<Rl> sp) {
+    // 16384-point FP32 rows at 1024 threads keep the RK4 sum in tensor memory (256 columns:
+    // 16 complex per thread), so k of stages 0-2 is never stored; one CTA per SM holds it
+    constexpr bool TM = sizeof(Rl) == 4 && LOGN == 14 && LC == 16;
+    __shared__ uint32_t tslot;
+    uint32_t tmem = 0;
+    if constexpr (TM) {
+        if (threadIdx.x < 32) {
+            asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                             (uint32_t)__cvta_generic_to_shared(&tslot)),
+                         "r"(256));
+            asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+        }
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        tmem = tslot;
+    }
     for (int s = 0; s < 4; s++) {
         StageOv<Rl> ov{(Rl)(s == 0 ? 0.0 : (s < 3 ? f.dzs * 0.5 : f.dzs)),   // as the per-stage launches round it
                        s > 0 ? sp.kst[s - 1] : f.kp, s == 0, s == 0 ? f.ahead : 0, s,
                        a.tape_e, a.tape_rho, a.tape_q, a.row_ion,
                        (Rl)(s < 3 ? (s + 1 < 3 ? f.dzs * 0.5 : f.dzs) : 0.0),   // stage s + 1's c dz
-                       s > 0};
+                       s > 0, tmem};
         if (a.tape_e) {   // stage s's record for the adjoint
             const size_t o = (size_t)s * a.tape_stride;
             ov.tape_e = reinterpret_cast<typename Vec2<Rl>::T*>(reinterpret_cast<char*>(a.tape_e) + o);
@@ -547,7 +620,15 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage4_kernel
             ov.row_ion = reinterpret_cast<int*>(reinterpret_cast<char*>(a.row_ion) + o);
         }
         if (s > 0) __syncthreads();   // k of stage s - 1 written by every thread of the CTA
-        nl_stage_row<Rl, LOGN, LC>(f, a, A, sp, ov);
+        nl_stage_row<Rl, LOGN, LC, TM>(f, a, A, sp, ov);
+    }
+    if constexpr (TM) {
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256));
+        }
     }
 }
 
@@ -584,7 +665,8 @@ template <typename Rl> cudaError_t nl_fused_setup(int N) {
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(nl_stage_kernel<Rl, 14>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(nl_stage4_kernel<Rl, 14, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+            e = cudaFuncSetAttribute(nl_stage4_kernel<Rl, 14, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     227 * 1024 - 1024);   // its static tensor-memory slot counts too
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(nl_stage4_kernel<Rl, 14>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
     }
