@@ -385,6 +385,16 @@ static LstepArgs lstep_args(gs_handle* h, double dz) {
 // QDHT of device array X -> Y (mode: plain / fused linear step / masked input).
 int gsi::run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz, int flags) {
     if (Y == h->S && mode == QDHT_PLAIN) spec_written(h);
+    if (X == h->A) {
+        const int rs = field_sync(h);
+        if (rs) return rs;
+    }
+    if (Y == h->A) field_written(h);
+    // the masked inverse leaves FIELD compact only on plans that keep a compact result
+    int nyc = 0;
+    const bool lazy = (flags & gs::QTC_Y_LAZY) && mode == QDHT_MASKED && Y == h->A && !h->fp64 && h->tc &&
+                      gs::qdht_tc_compact_y(h->tc, &nyc) && nyc > 0;
+    if (!lazy) flags &= ~gs::QTC_Y_LAZY;
     LstepArgs L = lstep_args(h, dz);
     if (h->fp64) {
         const bool win = mode != QDHT_PLAIN && h->win64;
@@ -394,6 +404,7 @@ int gsi::run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz, int
         std::string m;
         cudaError_t e = gs::qdht_tc_run(h->tc, mode, (const float*)X, (float*)Y, L, &h->launches, &m, flags);
         if (e != cudaSuccess) return fail(h, GS_ERR_CUDA, "mixed QDHT: " + m + " " + cudaGetErrorString(e));
+        if (lazy) h->a_compact = true;   // A itself is not written
     }
     return GS_OK;
 }
@@ -477,6 +488,7 @@ static void* pinned_device_ptr(const void* host, size_t bytes) {
 int gsi::permute_in(gs_handle* h, const double* host, void* dst) {
     const size_t nel = (size_t)h->nr * h->nt;
     if (dst == h->S) spec_written(h);
+    if (dst == h->A) field_written(h);
     if (void* dp = pinned_device_ptr(host, nel * 16)) {   // read over the host link, no staging copy
         cudaError_t e = h->fp64 ? launch_permute_host<double>(+1, dp, dst, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches)
                                 : launch_permute_host<float>(+1, dp, dst, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches);
@@ -493,6 +505,10 @@ int gsi::permute_out(gs_handle* h, const void* src, double* host) {
     const size_t nel = (size_t)h->nr * h->nt;
     if (src == h->S) {
         const int rc = spec_sync(h);
+        if (rc) return rc;
+    }
+    if (src == h->A) {
+        const int rc = field_sync(h);
         if (rc) return rc;
     }
     if (void* dp = pinned_device_ptr(host, nel * 16)) {   // written over the host link
@@ -595,14 +611,32 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
     T2* U2 = U1 + nel;
     T2* U3 = U2 + nel;
     h->nbc_valid = false;   // set again below when the fused stages also write NB's compact columns
-    if (!h->p.nonlinear) {
-        CK(h, launch_zero_nl<Rl>(A, NB, nel, h->max_dev, h->st, &h->launches));
-        return GS_OK;
-    }
     const bool raman = h->p.raman_fraction > 0.001;
     const bool kerr_on = h->p.n2 != 0;
     // the oscillator recurrence replaces the RAMAN_FUNCTION FFT pair when its parameters are known
     const bool raman_scan = raman && kerr_on && h->p.raman_tau > 0 && h->p.raman_omega > 0;
+    // without Kerr the Raman response is never used: the fused stage applies
+    const bool fused = h->fused && (raman_scan || !raman || !kerr_on);
+    {
+        // the four-stage kernel of 16384-point FP32 rows reads FIELD compactly where the masked
+        // inverse left it so; every other path reads A
+        if (fused && h->all_stages_thr != h->nl_threads) {   // decided once per launch shape
+            h->all_stages = nl_stage_all_preferred<Rl>(nt, h->nl_threads, nr) ? 1 : 0;
+            h->all_stages_thr = h->nl_threads;
+        }
+        int nyc = 0;
+        h->nl_compact = h->p.nonlinear && fused && !h->pair && h->all_stages == 1 && !h->fp64 && h->tc &&
+                        nl_stage_reads_compact<Rl>(nt, h->nl_threads) && gs::qdht_tc_compact_y(h->tc, &nyc) &&
+                        gs::qdht_tc_compact_x(h->tc, nullptr, nullptr) && nyc > 0;
+        if (!h->nl_compact) {
+            const int rs = gsi::field_sync(h);
+            if (rs) return rs;
+        }
+    }
+    if (!h->p.nonlinear) {
+        CK(h, launch_zero_nl<Rl>(A, NB, nel, h->max_dev, h->st, &h->launches));
+        return GS_OK;
+    }
     FftArgs<Rl> fa{};
     fa.N = nt; fa.M = h->M; fa.P = h->P; fa.logM = h->logM;
     fa.tw = (const T2*)h->tw;
@@ -614,8 +648,6 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
     sa.N = nt; sa.rows = nr; sa.u1 = U1; sa.u2 = U2; sa.u3 = U3;
     sa.pf = (const T2*)h->pf; sa.rm = (const T2*)h->rm; sa.kerr = (const Rl*)h->kerr;
     sa.raman = raman && !raman_scan; sa.kerr_on = kerr_on; sa.nb = NB; sa.kp = KP; sa.max_out = h->max_dev + 1;
-    // without Kerr the Raman response is never used: the fused stage applies
-    const bool fused = h->fused && (raman_scan || !raman || !kerr_on);
     if (tape && !fused) return fail(h, GS_ERR_UNSUPPORTED, "recording the RK4 stages needs rows that fit one CTA");
     if (h->pair && !tape && (raman_scan || !raman || !kerr_on)) {   // rows over two CTAs (gs_nl_pair.cu)
         pa.row_ion = h->row_ion;
@@ -641,10 +673,6 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
         const int* cinv = nullptr;
         int ncw = 0;
         float* nbc = (!h->fp64 && h->tc) ? gs::qdht_tc_compact_x(h->tc, &cinv, &ncw) : nullptr;
-        if (h->all_stages_thr != h->nl_threads) {   // decided once per launch shape
-            h->all_stages = nl_stage_all_preferred<Rl>(nt, h->nl_threads, nr) ? 1 : 0;
-            h->all_stages_thr = h->nl_threads;
-        }
         if (h->all_stages == 1) {   // the four stages of each row in one launch
             FftArgs<Rl> f1 = fa;
             f1.rows = nr; f1.kp = KP;
@@ -664,6 +692,7 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
             s2.nbc = nbc;
             s2.cinv = cinv;
             s2.ncw = ncw;
+            if (h->a_compact) s2.ac = gs::qdht_tc_compact_y(h->tc, nullptr, &s2.cmap);   // nl_compact holds
             const bool tm = h->time_nl && !tape;
             if (tm) CK(h, cudaEventRecord(h->nl_ev[0], h->st));
             CK(h, launch_nl_stage<Rl>(f1, ps, A, s2, nr, h->st, &h->launches));
@@ -782,6 +811,15 @@ int gsi::spec_sync(gs_handle* h) {
 
 void gsi::spec_written(gs_handle* h) { h->s_compact = false; }
 
+int gsi::field_sync(gs_handle* h) {
+    if (!h->a_compact) return GS_OK;
+    h->a_compact = false;
+    CK(h, gs::qdht_tc_expand(h->tc, (float*)h->A, &h->launches));
+    return GS_OK;
+}
+
+void gsi::field_written(gs_handle* h) { h->a_compact = false; }
+
 int gsi::spec_prepare(gs_handle* h) {
     if (h->s_compact || h->fp64 || !h->tc || !gs::qdht_tc_has_compact(h->tc)) return GS_OK;
     CK(h, gs::qdht_tc_spec_copy(h->tc, (float*)h->S, 1, &h->launches));
@@ -797,7 +835,8 @@ int gsi::lstep(gs_handle* h, double dz) {
     if (h->time_qdht) CK(h, cudaEventRecord(h->ev0, h->st));
     rc = run_qdht(h, QDHT_LSTEP, h->NB, h->S, dz, fs | (h->nbc_valid ? gs::QTC_X_COMPACT : 0));
     if (rc) return rc;
-    rc = run_qdht(h, QDHT_MASKED, h->S, h->A, dz, fs);
+    // FIELD stays compact when the next NL step reads it so
+    rc = run_qdht(h, QDHT_MASKED, h->S, h->A, dz, fs | ((h->a_lazy_ok && h->nl_compact) ? gs::QTC_Y_LAZY : 0));
     if (rc) return rc;
     if (h->time_qdht) {
         CK(h, cudaEventRecord(h->ev1, h->st));
@@ -863,6 +902,8 @@ int gs_step(gs_handle* h, double current_z, double znet_cur, double znet_prev, d
             // apertures (propagator.cu:232-261), with CURRENT_Z the z before this step
             if (!h->ap_z.empty() && current_z >= h->ap_z.back()) {
                 const int k0 = h->ap_row0.back();
+                rc = gsi::field_sync(h);
+                if (rc) return rc;
                 if (k0 < h->nr)
                     CK(h, cudaMemsetAsync((char*)h->A + (size_t)k0 * h->nt * h->esz, 0,
                                           (size_t)(h->nr - k0) * h->nt * h->esz, h->st));
@@ -980,6 +1021,10 @@ static int dump_impl(gs_handle* h, const double* qdht_x, double r_max, double* m
     f.N = nt; f.M = h->M; f.P = h->P; f.logM = h->logM; f.rows = nr;
     f.tw = (const T2*)h->tw; f.tpost = 1;
     f.twb = (const T2*)h->twb;
+    {
+        const int rs = gsi::field_sync(h);
+        if (rs) return rs;
+    }
     CK(h, launch_fft<Rl>(+1, (const T2*)h->A, (T2*)h->E, f, h->st, &h->launches));
     if (max_I || flux) CK(h, launch_row_intensity<Rl>((const T2*)h->E, nr, nt, h->p.tstep, d_maxI, d_flux, h->st, &h->launches));
     if (plasma_max) {
@@ -1037,6 +1082,10 @@ int gs_get_time_field(gs_handle* h, double* e_r_t) {
     if (!h->tables_ok || !h->field_ok) return fail(h, GS_ERR_STATE, "tables / field not set");
     CK(h, cudaSetDevice(h->p.device));
     const size_t nel = (size_t)h->nr * h->nt;
+    {
+        const int rs = gsi::field_sync(h);
+        if (rs) return rs;
+    }
     cudaError_t e;
     if (h->fp64) {
         FftArgs<double> f{};

@@ -267,6 +267,8 @@ int objective(gs_handle* h, const AdjPtrs* P, double* J) {
     double* part = h->adj_w + nel;
     double* jd = part + nb;
     void* ab = P ? P->Ab : h->KP;   // the forward alone: A_bar lands in scratch
+    const int rs = gsi::field_sync(h);
+    if (rs) return rs;
     if (h->fp64)
         CK(h, launch_adj_seed<double>((const double2*)h->A, h->adj_w, (double2*)ab, nel, part, nb, jd, h->st,
                                       &h->launches));
@@ -349,6 +351,8 @@ int gs_gradient(gs_handle* h, const double* field_in, int n_steps, const double*
     for (int n = 0; n < n_steps && !rc; n++) {
         if (n % L.K == 0 && n < last0) {
             char* ck = P.ck + (size_t)(n / L.K) * 2 * arr;
+            rc = gsi::field_sync(h);
+            if (rc) return rc;
             CK(h, cudaMemcpyAsync(ck, h->A, arr, cudaMemcpyDeviceToDevice, h->st));
             rc = gsi::spec_sync(h);
             if (rc) return rc;
@@ -373,6 +377,7 @@ int gs_gradient(gs_handle* h, const double* field_in, int n_steps, const double*
             CK(h, cudaMemcpyAsync(h->A, ck, arr, cudaMemcpyDeviceToDevice, h->st));
             CK(h, cudaMemcpyAsync(h->S, ck + arr, arr, cudaMemcpyDeviceToDevice, h->st));
             gsi::spec_written(h);
+            gsi::field_written(h);
             for (int m = n0; m < n1 && !rc; m++) {
                 const GsTape tp = tape_of(L, P.tape, m - n0);
                 rc = gsi::nl_stages(h, dz_rk[m], h->p.nonlinear ? &tp : nullptr);

@@ -126,8 +126,12 @@ int gs_batch_step(gs_batch* b, int n_steps, const double* dz, int use_graph) {
     BCK(b, cudaSetDevice(b->device));
     for (gs_handle* h : b->h) BCK(b, cudaMemsetAsync(h->err_dev, 0, 4, h->st));
     // the compact copies of BIGBUFFER2 are taken now, outside any graph capture
-    for (size_t i = 0; i < b->h.size(); i++)
-        if (gsi::spec_prepare(b->h[i])) return bfail(b, GS_ERR_CUDA, "pulse " + std::to_string(i) + ": " + b->h[i]->err);
+    // and FIELD is kept expanded (a captured step must not depend on the state it starts from)
+    for (size_t i = 0; i < b->h.size(); i++) {
+        b->h[i]->a_lazy_ok = false;
+        if (gsi::spec_prepare(b->h[i]) || gsi::field_sync(b->h[i]))
+            return bfail(b, GS_ERR_CUDA, "pulse " + std::to_string(i) + ": " + b->h[i]->err);
+    }
     // the pulses' streams may hold earlier work: the batch stream waits for all of it
     for (size_t i = 0; i < b->h.size(); i++) {
         BCK(b, cudaEventRecord(b->join[i], b->h[i]->st));
@@ -213,6 +217,7 @@ int gs_batch_autotune(gs_batch* b, const double* dz, double* ms_default, double*
             const size_t bytes = (size_t)h->nr * h->nt * h->esz;
             char* st = snap[i];
             if (!restore) {
+                if (gsi::field_sync(h)) return bfail(b, GS_ERR_CUDA, "pulse " + std::to_string(i) + ": " + h->err);
                 BCK(b, cudaMemcpyAsync(st, h->A, bytes, cudaMemcpyDeviceToDevice, h->st));
                 if (gsi::spec_sync(h)) return bfail(b, GS_ERR_CUDA, "pulse " + std::to_string(i) + ": " + h->err);
                 BCK(b, cudaMemcpyAsync(st + bytes, h->S, bytes, cudaMemcpyDeviceToDevice, h->st));
@@ -220,6 +225,7 @@ int gs_batch_autotune(gs_batch* b, const double* dz, double* ms_default, double*
                 BCK(b, cudaMemcpyAsync(h->A, st, bytes, cudaMemcpyDeviceToDevice, h->st));
                 BCK(b, cudaMemcpyAsync(h->S, st + bytes, bytes, cudaMemcpyDeviceToDevice, h->st));
                 gsi::spec_written(h);
+                gsi::field_written(h);
             }
         }
         return GS_OK;

@@ -58,6 +58,9 @@ struct gs_handle {
     int adj_stride = 0;   // checkpoint stride of the last gs_gradient
     bool nbc_valid = false;   // the last NL step also wrote NB's window columns compactly (mixed)
     bool s_compact = false;   // BIGBUFFER2's window columns are current only in the plan's compact copy
+    bool a_compact = false;   // FIELD is current only as the masked inverse's compact result
+    bool a_lazy_ok = true;    // the masked inverse may leave FIELD compact (not in captured graphs)
+    bool nl_compact = false;  // the last NL step ran the kernel that reads a compact FIELD
     // FP64 QDHT: the spectral window's columns (padded to 64 with -1) and the positions outside
     int *win64 = nullptr, *zpos64 = nullptr;
     int nwin64 = 0, nz64 = 0;
@@ -92,6 +95,10 @@ int run_qdht(gs_handle* h, int mode, const void* X, void* Y, double dz, int flag
 int spec_sync(gs_handle* h);
 void spec_written(gs_handle* h);
 int spec_prepare(gs_handle* h);
+// FIELD left compact by the masked inverse (the next NL step reads it so): field_sync expands
+// it into A before A is read by anything else; field_written marks A as rewritten
+int field_sync(gs_handle* h);
+void field_written(gs_handle* h);
 // calculate_NLstep's four RK4 stages: NB = RK4 increment of A (no host sync); with a tape
 // the stages are recorded (fused rows only)
 int nl_stages(gs_handle* h, double dz, const GsTape* tape);

@@ -134,6 +134,12 @@ template <typename Rl> struct SpecArgs {
     float* nbc;
     const int* cinv;
     int ncw;
+    // != nullptr: FIELD (the stage input A) as the masked inverse's compact [rows][ncw] array
+    // at the same columns, zero outside the window; read by the four-stage kernel of
+    // 16384-point FP32 rows at 1024 threads (nl_stage_reads_compact) instead of A.  cmap[c]:
+    // the real column of compact column c (-1 in the padding)
+    const float* ac;
+    const int* cmap;
 };
 
 template <typename Rl>
@@ -168,6 +174,8 @@ cudaError_t launch_nl_stage(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2
                             int rows, cudaStream_t st, long long* nl);
 // whether one launch of all four stages (f.all_stages) suits a grid of this many rows
 template <typename Rl> bool nl_stage_all_preferred(int N, int threads, int rows);
+// whether the four-stage launch of this shape can read FIELD compactly (SpecArgs::ac)
+template <typename Rl> bool nl_stage_reads_compact(int N, int threads);
 
 // ---- one RK4 stage over two CTAs per row (gs_nl_pair.cu): rows of N = 2H stored in the
 // P = 2 position order, FP32 N = 32768 / FP64 N = 16384

@@ -109,6 +109,13 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
     T2* cend_aL = reinterpret_cast<T2*>(reinterpret_cast<unsigned char*>(flag) + 16);   // a^L (flag area is 64 B)
     const size_t base = (size_t)blockIdx.x * N;
 
+    // FIELD's compact row, where the masked inverse left it so (zero outside the spectral
+    // window, as its expansion writes)
+    const float* acr = nullptr;
+    if constexpr (TMA) {
+        if (sp.ac) acr = sp.ac + (size_t)blockIdx.x * sp.ncw;
+    }
+
     // ---- stage input and inverse FFT (propagator.cu:386-396, 640-641)
     load_twiddles<Rl>(twh, twl, f.tw, N, tid, nthr);
     // N / nthr = 16 elements per thread (2 when N < 512): loads issued together
@@ -123,8 +130,33 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
         // the previous stage of this CTA left (A + c dz k) / N in E (four stages per launch)
     } else if (per == 16) {
         T2 v[16];
+        if (acr) {   // compact FIELD: zero the row, place the window's columns, read it back
 #pragma unroll
-        for (int u = 0; u < 16; u++) v[u] = A[base + tid + u * nthr];
+            for (int u = 0; u < 16; u++) E[pad16(tid + u * nthr)] = T2{0, 0};
+            __syncthreads();
+            for (int c = 2 * tid; c < sp.ncw; c += 2 * nthr) {
+                const int rc = __ldg(sp.cmap + c);
+                if (rc >= 0) E[pad16(rc >> 1)] = *reinterpret_cast<const T2*>(acr + c);
+            }
+            __syncthreads();
+#pragma unroll
+            for (int u = 0; u < 16; u++) v[u] = E[pad16(tid + u * nthr)];
+        } else {
+#pragma unroll
+            for (int u = 0; u < 16; u++) v[u] = A[base + tid + u * nthr];
+        }
+        if constexpr (TMA) {   // the row's A stays in tensor memory for the next stages' inputs
+#pragma unroll
+            for (int g = 0; g < 4; g++) {
+                float w[8];
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    w[2 * i] = v[4 * g + i].x;
+                    w[2 * i + 1] = v[4 * g + i].y;
+                }
+                tm_st<8>(ov.tmem + ((uint32_t)(32 * ((tid >> 5) & 3)) << 16) + (uint32_t)(256 + 32 * (tid >> 7) + 8 * g), w);
+            }
+        }
         if (ov.track_max) {
 #pragma unroll
             for (int u = 0; u < 16; u++) lmax = fmax(lmax, v[u].x * v[u].x + v[u].y * v[u].y);
@@ -158,7 +190,8 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
     // the row that takes this SM's next slot: its inputs travel to L2 while this row computes
     if (tid < 32 && ov.ahead > 0 && (int)blockIdx.x + ov.ahead < f.rows) {
         const size_t nbase = base + (size_t)ov.ahead * N;
-        prefetch_row_l2(A + nbase, (size_t)N * sizeof(T2), tid);
+        if (acr) prefetch_row_l2(acr + (size_t)ov.ahead * sp.ncw, (size_t)sp.ncw * sizeof(float), tid);
+        else prefetch_row_l2(A + nbase, (size_t)N * sizeof(T2), tid);
         if (ov.cdz != 0) prefetch_row_l2(ov.kp + nbase, (size_t)N * sizeof(T2), tid - 4);
         if (ov.stage == 3) {
             prefetch_row_l2(sp.kst[0] + nbase, (size_t)N * sizeof(T2), tid - 8);
@@ -485,6 +518,8 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
             const uint32_t ta = ov.tmem + ((uint32_t)(32 * ((tid >> 5) & 3)) << 16) +
                                 (uint32_t)(32 * (tid >> 7) + 2 * ((pb - tid) / nthr));
             if constexpr (tacc && last) tm_ld<2 * SB>(ta, tv);
+            float ta_a[2 * SB];   // A at these points (tensor memory, from the stage-0 load)
+            if constexpr (tacc && !last) tm_ld<2 * SB>(ta + 256, ta_a);
 #pragma unroll
             for (int u = 0; u < SB; u++) {
                 const int p = pb + u * nthr;
@@ -501,7 +536,8 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
                     k2[u] = (in && !tacc) ? sp.kst[1][base + p] : T2{0, 0};
                     k3[u] = (in && !tacc) ? sp.kst[2][base + p] : T2{0, 0};
                 } else {
-                    an[u] = (in && ov.next_cdz != 0) ? A[base + p] : T2{0, 0};
+                    if constexpr (tacc) an[u] = T2{ta_a[2 * u], ta_a[2 * u + 1]};
+                    else an[u] = (in && ov.next_cdz != 0) ? A[base + p] : T2{0, 0};
                 }
             }
 #pragma unroll
@@ -589,8 +625,9 @@ template <typename Rl, int LOGN = 0, int LC = 0>
 __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage4_kernel(FftArgs<Rl> f, PlasmaArgs<Rl> a,
                                                                                const typename Vec2<Rl>::T* __restrict__ A,
                                                                                SpecArgs<Rl> sp) {
-    // 16384-point FP32 rows at 1024 threads keep the RK4 sum in tensor memory (256 columns:
-    // 16 complex per thread), so k of stages 0-2 is never stored; one CTA per SM holds it
+    // 16384-point FP32 rows at 1024 threads keep the RK4 sum (columns 0-255: 16 complex per
+    // thread) and the row's A (columns 256-511) in tensor memory, so k of stages 0-2 is never
+    // stored and A is read once per step; one CTA per SM holds all 512 columns
     constexpr bool TM = sizeof(Rl) == 4 && LOGN == 14 && LC == 16;
     __shared__ uint32_t tslot;
     uint32_t tmem = 0;
@@ -598,7 +635,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage4_kernel
         if (threadIdx.x < 32) {
             asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                              (uint32_t)__cvta_generic_to_shared(&tslot)),
-                         "r"(256));
+                         "r"(512));
             asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -627,7 +664,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage4_kernel
         __syncthreads();
         if (threadIdx.x < 32) {
             asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(256));
+            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
         }
     }
 }
@@ -648,6 +685,11 @@ template <typename Rl> bool nl_fused_supported(int N) {
 template <typename Rl> bool nl_fused_threads_ok(int N, int t) {
     const int maxt = sizeof(Rl) == 8 ? 512 : 1024;
     return t >= 32 && t <= maxt && t % 32 == 0 && N % t == 0 && FrontSmem<Rl>::bytes(N, t) <= 227 * 1024;
+}
+
+template <typename Rl> bool nl_stage_reads_compact(int N, int threads) {
+    const int nthr = threads > 0 ? threads : fused_threads<Rl>(N);
+    return sizeof(Rl) == 4 && N == 16384 && nthr == 1024;   // nl_stage4_kernel<float, 14, 16>
 }
 
 template <typename Rl> int nl_fused_default_threads(int N) { return fused_threads<Rl>(N); }
@@ -723,6 +765,7 @@ cudaError_t launch_nl_stage(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2
             k1<<<rows, nthr, sm, st>>>(f, a, A, s);
         }
     };
+    if (s.ac && !(f.all_stages && nl_stage_reads_compact<Rl>(f.N, nthr))) return cudaErrorInvalidValue;
     bool done = false;
     if constexpr (sizeof(Rl) == 4) {
         if (f.N == 16384 && nthr == 1024) {
@@ -744,6 +787,7 @@ cudaError_t launch_nl_stage(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2
     template cudaError_t launch_nl_stage<Rl>(FftArgs<Rl>, PlasmaArgs<Rl>, const typename Vec2<Rl>::T*, SpecArgs<Rl>, \
                                              int, cudaStream_t, long long*);                                      \
     template bool nl_stage_all_preferred<Rl>(int, int, int);                                                     \
+    template bool nl_stage_reads_compact<Rl>(int, int);                                                          \
     template bool nl_fused_threads_ok<Rl>(int, int);                                                             \
     template int nl_fused_default_threads<Rl>(int);
 GS_FUSED_INST(double)

@@ -1247,12 +1247,7 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
         const unsigned g2 = (unsigned)(nt2 < q->sms ? nt2 : q->sms);
         tc::qdht_tc2_kernel<<<g2, tc::THREADS2, tc::SMEM2_BYTES, q->st>>>(q->map_hi64, q->map_lo64, q->map_bh, q->map_bl, a);
         (*nlaunch)++;
-        if (a.yc) {
-            const size_t tot = (size_t)q->nr * q->nt / 2;
-            tc::qdht_expand_kernel<<<(unsigned)std::min<size_t>((tot + 1023) / 1024, (size_t)q->sms * 8), 256, 0, q->st>>>(
-                a.yc, Y, q->nr, q->nt, a.nc, q->cinv);
-            (*nlaunch)++;
-        }
+        if (a.yc && !(flags & QTC_Y_LAZY)) return qdht_tc_expand(q, Y, nlaunch);
         return cudaGetLastError();
     }
     const int ntiles = (q->nr / tc::BM) * (a.ncols / tc::BN);
@@ -1299,6 +1294,22 @@ cudaError_t qdht_tc_spec_copy(QdhtTc* q, float* S, int to_compact, long long* nl
     const size_t tot = (size_t)q->nr * (q->nc_act / 2);
     tc::qdht_spec_copy_kernel<<<(unsigned)std::min<size_t>((tot + 255) / 256, (size_t)q->sms * 16), 256, 0, q->st>>>(
         S, q->sc, q->nr, 2 * q->nt, q->nc_act, q->cmap, to_compact ? 1 : -1);
+    (*nlaunch)++;
+    return cudaGetLastError();
+}
+
+const float* qdht_tc_compact_y(QdhtTc* q, int* nc, const int** cmap) {
+    if (!q || !q->wide || !q->yc) return nullptr;
+    if (nc) *nc = q->nc_act;
+    if (cmap) *cmap = q->cmap;
+    return q->yc;
+}
+
+cudaError_t qdht_tc_expand(QdhtTc* q, float* Y, long long* nlaunch) {
+    if (!q || !q->yc || q->nc_act == 0) return cudaErrorInvalidValue;
+    const size_t tot = (size_t)q->nr * q->nt / 2;
+    tc::qdht_expand_kernel<<<(unsigned)std::min<size_t>((tot + 1023) / 1024, (size_t)q->sms * 8), 256, 0, q->st>>>(
+        q->yc, Y, q->nr, q->nt, q->nc_act, q->cinv);
     (*nlaunch)++;
     return cudaGetLastError();
 }

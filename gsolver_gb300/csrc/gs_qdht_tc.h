@@ -27,7 +27,9 @@ int qdht_tc_check(QdhtTc* q, std::string* msg);
 //   QTC_S_COMPACT  BIGBUFFER2's window columns live in the plan's compact copy: the linear
 //                  step updates it (Y is not touched) and the masked inverse reads it (X is
 //                  not read); see qdht_tc_spec_copy.
-enum { QTC_X_COMPACT = 1, QTC_S_COMPACT = 2 };
+//   QTC_Y_LAZY     masked inverse: leave the result in the compact array of qdht_tc_compact_y
+//                  (Y is not written; qdht_tc_expand writes it when it is wanted).
+enum { QTC_X_COMPACT = 1, QTC_S_COMPACT = 2, QTC_Y_LAZY = 4 };
 cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const LstepArgs& L, long long* nlaunch,
                         std::string* msg, int flags = 0);
 // The plan keeps compact copies of the window's columns (wide-tile plans with linear-step tables).
@@ -38,6 +40,11 @@ cudaError_t qdht_tc_spec_copy(QdhtTc* q, float* S, int to_compact, long long* nl
 // the column of position p's (re, im) pair, or -1 outside the spectral window); null when the
 // plan has no window columns (set_lstep not called, or a width outside the wide-tile path).
 float* qdht_tc_compact_x(QdhtTc* q, const int** cinv, int* nc);
+// The masked inverse's compact [n_r][nc] result array (same columns and position map as
+// qdht_tc_compact_x; cmap[c]: the real column of compact column c, -1 in the padding), and
+// its expansion into Y (zeros outside the spectral window).
+const float* qdht_tc_compact_y(QdhtTc* q, int* nc, const int** cmap = nullptr);
+cudaError_t qdht_tc_expand(QdhtTc* q, float* Y, long long* nlaunch);
 // Adjoint of the QDHT_LSTEP epilogue's linear step, elementwise over [n_r][n_t] (FP32, the
 // epilogue's tables): fb = cotangent of FIELD (k,omega), sb of BIGBUFFER2 (in: after the
 // step, out: before), b1b out: of BIGBUFFER1 (k,omega).
