@@ -139,3 +139,28 @@ def test_compact_field_state_transitions():
     fb2, sb2 = b.get_field(want_spec=True)
     fc2, sc2 = c.get_field(want_spec=True)
     assert np.array_equal(fb2, fc2) and np.array_equal(sb2, sc2)
+
+
+def test_compact_field_read_by_dumps_and_time_field():
+    """The dump reductions and the time-domain field read FIELD itself: on a handle whose FIELD
+    is compact they expand it first, and give what they give after an explicit read-back."""
+    T = setup(n_r=640, n_t=16384)
+    f0 = T["field"]
+    a = gs.Propagator(T, precision=gs.PREC_MIXED)
+    b = gs.Propagator(T, precision=gs.PREC_MIXED)
+    a.set_field(f0)
+    b.set_field(f0)
+    for _ in range(2):
+        for P in (a, b):
+            P.nl_step(DZ)
+            P.lstep(DZ)
+    a.get_field(want_spec=False)   # a's FIELD expanded by the read-back
+    da = a.dumps(T["qdht_x"], T["r_max"])
+    db = b.dumps(T["qdht_x"], T["r_max"])   # b's expanded by the dump itself
+    for k in da:
+        assert np.array_equal(da[k], db[k]), k
+    # both continue identically; the time-domain field agrees as well
+    for P in (a, b):
+        P.nl_step(DZ)
+        P.lstep(DZ)
+    assert np.array_equal(a.time_field(), b.time_field())
