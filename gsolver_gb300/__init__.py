@@ -170,6 +170,13 @@ class Propagator:
         if rc:
             raise GsError(rc, self.L.gs_last_error(None).decode())
         self.h = h
+        self.upload_tables(setup)
+        if len(setup.get("aperture_z", ())) > 0:   # apertures of the config (propagator.cu:232-261)
+            self.set_apertures(setup["aperture_z"], setup["aperture_r"], setup["qdht_x"], setup["r_max"])
+
+    def upload_tables(self, setup: dict):
+        """gs_upload_tables: the per-omega / per-k tables, the rate table and the QDHT matrix
+        (cuda_load_const); may be called again on a live handle to replace them."""
         self._keep = {}
         t = Tables()
         for k, dt in (("rate_ln", np.float64), ("plasma_func", np.complex128), ("raman_func", np.complex128),
@@ -182,8 +189,6 @@ class Propagator:
         self._keep["qdht_c"] = cm
         t.qdht_c = cm.ctypes.data
         self._check(self.L.gs_upload_tables(self.h, C.byref(t)))
-        if len(setup.get("aperture_z", ())) > 0:   # apertures of the config (propagator.cu:232-261)
-            self.set_apertures(setup["aperture_z"], setup["aperture_r"], setup["qdht_x"], setup["r_max"])
 
     def _check(self, rc):
         if rc:

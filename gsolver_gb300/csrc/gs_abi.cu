@@ -338,7 +338,12 @@ int gs_upload_tables(gs_handle* h, const gs_tables* t) {
     }
     if (h->tc) {
         std::string m;
-        // the plan's compact copies are rebuilt: BIGBUFFER2 takes its window columns back first
+        // the plan's compact copies are rebuilt: FIELD (left compact by the masked inverse) and
+        // BIGBUFFER2 take their window columns back first, through the old column lists
+        {
+            const int rc = gsi::field_sync(h);
+            if (rc) return rc;
+        }
         if (h->s_compact) {
             const int rc = gsi::spec_sync(h);
             if (rc) return rc;

@@ -21,15 +21,12 @@ namespace {
 // 16 MiB: a 256-byte error word, then 2 x rows x n_t x 16 bytes of recurrence scratch
 constexpr size_t kScratchBytes = 16u << 20;
 constexpr size_t kErrBytes = 256;
-constexpr int kMaxDevices = 64;
 
 // Every GPU that loads this library holds this array until the process exits.  In host code
 // its name is only a host-side stand-in for the symbol, not a device address: kernels get the
 // address that cudaGetSymbolAddress returns for the current device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-// Device address of the array, looked up once per device with that device current.
-void* g_scratch_dev[kMaxDevices] = {};
 std::string g_noalloc_err;
 
 int fail(int code, const std::string& m) {
@@ -54,19 +51,14 @@ extern "C" int gs_plasma_max_noalloc(const gs_params* p, const double* rate_ln_d
         return fail(GS_ERR_ARG, "gs_plasma_max_noalloc: rows * n_t = " + std::to_string(samples) +
                                     " exceeds the fixed scratch of " + std::to_string(gs_noalloc_max_samples()) +
                                     " samples (16 MiB); split the rows into several calls");
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return fail(GS_ERR_CUDA, cudaGetErrorString(e));
-    if (dev < 0 || dev >= kMaxDevices) return fail(GS_ERR_ARG, "gs_plasma_max_noalloc: device ordinal out of range");
-    if (!g_scratch_dev[dev]) {
-        // first call on this device: resolve the array's device address (the device is current).
-        // Make this first call before any stream capture begins on the device.
-        void* ptr = nullptr;
-        e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-        if (e != cudaSuccess || !ptr) return fail(GS_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
-        g_scratch_dev[dev] = ptr;
-    }
-    unsigned char* base = (unsigned char*)g_scratch_dev[dev];
+    // The array's device address on the current device, looked up on every call: the lookup
+    // allocates nothing, and a cached address would go stale after cudaDeviceReset or a new
+    // primary context.  The first call on a device also loads this library's device code
+    // there, so make that first call before any stream capture begins on the device.
+    void* ptr = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess || !ptr) return fail(GS_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+    unsigned char* base = (unsigned char*)ptr;
     unsigned* err_dev = (unsigned*)base;
     double2* u1 = (double2*)(base + kErrBytes);
     double2* u2 = u1 + samples;

@@ -52,7 +52,9 @@ enum gs_status {
 
 enum gs_precision {
     GS_PREC_FP64 = 0,       /* plain FP64 GPU path: the parity path against the FP64 reference */
-    GS_PREC_MIXED = 1       /* FP32 elementwise/FFT + tcgen05 3xTF32 QDHT with FP32 accumulation */
+    GS_PREC_MIXED = 1       /* FP32 elementwise/FFT; QDHT on tcgen05 with FP32 accumulation over split
+                               operands: FP16 hi/lo pairs of power-of-two-scaled values where
+                               2 n_t is a multiple of 256, 3xTF32 hi/lo parts for other widths */
 };
 
 /* Scalars of the hot path, in the reference's scaled units
@@ -227,19 +229,20 @@ int gs_batch_destroy(gs_batch* b);
 /* Carrier-density maxima without any device allocation.  No counterpart in the reference:
  * it is an addition for host code that cannot allocate device memory where it needs this
  * result (for example an application whose own allocator has reserved the GPU's memory and
- * refuses further cudaMalloc calls from the libraries it links).  It runs the FP64 plasma
- * recurrence of calculate_plasmadensity_losses_small on caller-owned device buffers:
+ * refuses further cudaMalloc calls from the libraries it links).  It runs the FP64 Heun
+ * recurrence of the carrier density (photoionization from the rate table, avalanche,
+ * recombination), then takes each row's maximum over time, on caller-owned device buffers:
  *   e_r_t_dev[rows][n_t]  complex time-domain field (interleaved doubles)
- *   rate_ln_dev[8192]     IONIZATION_RATE_LN
+ *   rate_ln_dev[8192]     the log photoionization-rate table
  *   plasma_max_dev[rows]  output: max over t of the carrier density per row
  * with the scalars of *params (n_t and the plasma constants), on `stream` (a cudaStream_t,
  * NULL for the default stream); it synchronises that stream before returning.  Its scratch
  * is one fixed 16 MiB array inside the library, held on every GPU that loads the library
  * until the process exits; rows * n_t may not exceed gs_noalloc_max_samples() (524,280) —
- * larger requests are refused with GS_ERR_ARG.  The first call on a device does a one-time
- * set-up (it looks up the array's device address with that device current); make that first
- * call before any stream capture begins.  All calls share the array, so calls that overlap on
- * the GPU (other streams, other host threads) race. */
+ * larger requests are refused with GS_ERR_ARG.  Each call looks up the array's device address
+ * on the current device (no allocation); the first call on a device also loads the library's
+ * device code there, so make that first call before any stream capture begins.  All calls
+ * share the array, so calls that overlap on the GPU (other streams, other host threads) race. */
 int gs_plasma_max_noalloc(const gs_params* params, const double* rate_ln_dev, const double* e_r_t_dev, int rows,
                           double* plasma_max_dev, void* stream);
 /* Largest rows * n_t accepted by gs_plasma_max_noalloc. */
