@@ -520,27 +520,35 @@ __global__ void lstep_adj_kernel(const float2* __restrict__ fb, float2* __restri
 // TF32 rate) and half the operand bytes of TF32 parts.
 //   qdht_split16_kernel  X [n_r][2 n_t] -> xscale and XhT, XlT [2 n_t][n_r] (K-major: the row
 //                        index j contiguous), the inverse transform's window mask applied.
-//   qdht_tc2_kernel      the GEMM on 128 (i) x 256 (c) tiles with every operand streamed by
+//   qdht_tc2_kernel      the GEMM on 128 (i) x 128 (c) tiles with every operand streamed by
 //                        TMA in the K-major layout with the 64-byte swizzle (no conversion in
-//                        shared memory): K-blocks of 32 (one 64-byte row), 48 KiB stages, four
-//                        in flight; tcgen05.mma.kind::f16 M = 128, N = 256, K = 16.  Warp 0
+//                        shared memory): K-blocks of 32 (one 64-byte row), 32 KiB stages, six
+//                        in flight; tcgen05.mma.kind::f16 M = 128, N = 128, K = 16, summed in
+//                        chunks of 64 of K into two alternating TMEM accumulators.  Warp 0
 //                        TMA, warp 1 MMA issuer, warps 2-17 epilogue (four per TMEM lane
-//                        quarter, 64 columns each), which also undoes the scales.
-constexpr int BN2 = 256, BK2 = 32, STAGES2 = 4;        // K-blocks of 32 FP16 (one 64-byte swizzle row)
+//                        quarter, 32 columns each): each chunk is added into FP32 registers,
+//                        then the scales are undone and the tile stored / updated.
+constexpr int WIDE_COLS = 256;                         // the path takes grids with 2 n_t a multiple of this
+constexpr int BN2 = 128, BK2 = 32, STAGES2 = 6;        // K-blocks of 32 FP16 (one 64-byte swizzle row)
+constexpr int KCHUNK2 = 2;                              // K-blocks per accumulation chunk (64 of K)
 constexpr int A2_BYTES = BM * BK2 * 2;                  // 8 KiB
-constexpr int B2_BYTES = BN2 * BK2 * 2;                 // 16 KiB
+constexpr int B2_BYTES = BN2 * BK2 * 2;                 // 8 KiB
 constexpr int STAGE2_BYTES = 2 * A2_BYTES + 2 * B2_BYTES;
 constexpr int NEPI2 = 16;
 constexpr int THREADS2 = 64 + 32 * NEPI2;
 constexpr int SMEM2_BYTES = STAGES2 * STAGE2_BYTES + 1024 + 256;
+// Operand parts are scaled so that the row / column maximum lies in [2^13, 2^14): the low
+// parts then stay in FP16's normal range down to 2^-17 of the maximum (scaled to at most 1
+// they would fall below it at 2^-3).  Products stay below 2^28 and K-sums below 2^38.
+constexpr int OPERAND_EXP = 14;
 
-// Per column c a power of two xscale[c] > max_j |X[j][c]| (1 for a zero column), then
-// X / xscale[c] = Xh + Xl in round-to-nearest FP16 parts, written K-major.  One CTA owns a
+// Per column c a power of two xscale[c] > 2^-14 max_j |X[j][c]|, then X / xscale[c] = Xh + Xl
+// in round-to-nearest FP16 parts, written K-major.  One CTA owns a
 // strip of 16 columns: it reads the strip once into shared memory, finds the column maxima
 // there and writes the parts as pairs of halves along j.  In shared memory rows j and j + 1
 // (j even) share a line of 33 floats (element (j, c) at (j / 2) 33 + (j % 2) 16 + c), so the
 // row-wise stores, the column scans and the pair-wise reads are all free of bank conflicts.
-// Relative error of the parts ~2^-22 of each value, or 2^-25 of its column's maximum where Xl
+// Relative error of the parts ~2^-22 of each value, or 2^-39 of its column's maximum where Xl
 // falls below the FP16 normal range.  Dynamic shared memory: (nr / 2) * 33 floats.
 constexpr int SPLIT_COLS = 16, SPLIT_THREADS = 256;
 __global__ void __launch_bounds__(SPLIT_THREADS) qdht_split16_kernel(const float* __restrict__ X,
@@ -594,10 +602,10 @@ __global__ void __launch_bounds__(SPLIT_THREADS) qdht_split16_kernel(const float
         float m = 0.f;
         for (int p = 0; p < SPLIT_THREADS / SPLIT_COLS; p++) m = fmaxf(m, part[p][tid]);
         int e = 0;
-        if (m > 0.f) frexpf(m, &e);   // m = f 2^e, f in [0.5, 1): |X / 2^e| < 1
-        const float sc = ldexpf(1.f, e);
-        xscale[c0 + tid] = sc;
-        inv[tid] = ldexpf(1.f, -e);   // exact
+        if (m > 0.f) frexpf(m, &e);   // m = f 2^e, f in [0.5, 1): |X 2^(14 - e)| < 2^14
+        e = max(e, -108);             // keeps both powers of two below inside FP32's normal range
+        xscale[c0 + tid] = ldexpf(1.f, e - OPERAND_EXP);
+        inv[tid] = ldexpf(1.f, OPERAND_EXP - e);   // exact
     }
     __syncthreads();
     // write: pairs (j, j + 1) of column c as half2, consecutive threads along j
@@ -643,15 +651,16 @@ __host__ __device__ constexpr uint32_t make_idesc_f16(int n) {
 // calculate_Lstep update of BIGBUFFER2 (propagator.cu:570-625)
 __device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, int cg, float kt2i) {
     float* yrow = a.Y + (size_t)i * a.ncols + cg;
-    if (a.xscale) {   // FP16 operands: undo the row and column scales (exact: powers of two)
+    if (a.xscale) {   // FP16 operands: undo the row and column scales (exact: powers of two,
+                      // applied one at a time so that their product cannot underflow)
         const float si = a.hscale[i];
 #pragma unroll
         for (int k = 0; k < 32; k += 4) {
             const float4 xs = *reinterpret_cast<const float4*>(a.xscale + cg + k);
-            v[k] *= si * xs.x;
-            v[k + 1] *= si * xs.y;
-            v[k + 2] *= si * xs.z;
-            v[k + 3] *= si * xs.w;
+            v[k] = (v[k] * si) * xs.x;
+            v[k + 1] = (v[k + 1] * si) * xs.y;
+            v[k + 2] = (v[k + 2] * si) * xs.z;
+            v[k + 3] = (v[k + 3] * si) * xs.w;
         }
     }
     if (a.mode != QDHT_LSTEP) {
@@ -769,9 +778,9 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
     uint64_t* bars = (uint64_t*)(smem + STAGES2 * STAGE2_BYTES);
     uint64_t* full = bars;                    // [STAGES2] TMA tx
     uint64_t* empty = bars + STAGES2;         // [STAGES2] MMA commit
-    uint64_t* acc_full = bars + 2 * STAGES2;  // MMA commit: accumulator ready
-    uint64_t* acc_empty = acc_full + 1;       // NEPI2 epilogue warps: read out
-    uint64_t* done = acc_empty + 1;           // every MMA of this CTA complete
+    uint64_t* acc_full = bars + 2 * STAGES2;  // [2] MMA commit: a chunk's accumulator ready
+    uint64_t* acc_empty = acc_full + 2;       // [2] NEPI2 epilogue warps: read out
+    uint64_t* done = acc_empty + 2;           // every MMA of this CTA complete
     uint32_t* tmem_slot = (uint32_t*)(done + 1);
     volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
@@ -779,6 +788,7 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
     const int MT = a.nr / BM;
     const int ntiles = MT * (a.nc / BN2);
     const int nk = a.nr / BK2;
+    const int nch = nk / KCHUNK2;             // accumulation chunks per tile
     const int my_tiles = blockIdx.x < ntiles ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
 
     if (threadIdx.x == 0) {
@@ -786,8 +796,10 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        mbar_init(acc_full, 1);
-        mbar_init(acc_empty, NEPI2);
+        for (int b = 0; b < 2; b++) {
+            mbar_init(&acc_full[b], 1);
+            mbar_init(&acc_empty[b], NEPI2);
+        }
         mbar_init(done, 1);
         *abort_flag = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -795,7 +807,7 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
     __syncwarp();
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(BN2));
+                     "r"(2 * BN2));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -834,75 +846,113 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
         __syncwarp();
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer
+        // Each chunk of KCHUNK2 K-blocks is summed afresh into accumulator buffer u % 2 (u the
+        // CTA's running chunk count), the correction products Hh Xl + Hl Xh of the chunk first
+        // and its main products Hh Xh last; the epilogue adds the chunks in FP32 registers.
+        // The tensor core's accumulation truncates: with a fresh, small accumulator per chunk
+        // and the small terms summed first, its error stays ~2^-22 of the result instead of
+        // growing with the whole K = n_r sum.
         if (lane == 0) {
             constexpr uint32_t idesc = make_idesc_f16(BN2);
-            for (int it = 0; it < my_tiles && !*abort_flag; it++) {
-                if (it >= 1 && !mbar_wait(acc_empty, (it - 1) & 1)) {
-                    record_stall(a.err, 4096u, 0, warp);
-                    *abort_flag = 1;
-                    break;
-                }
-                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                uint32_t acc = 0;
-                bool ok = true;
-                for (int kb = 0; kb < nk; kb++) {
-                    const int g = it * nk + kb;
-                    const int s = g % STAGES2;
-                    if (!mbar_wait(&full[s], (g / STAGES2) & 1)) {
-                        record_stall(a.err, 8u, kb, warp);
+            bool ok = true;
+            for (int it = 0; it < my_tiles && ok && !*abort_flag; it++) {
+                for (int c = 0; c < nch; c++) {
+                    const int u = it * nch + c, b = u & 1;
+                    if (u >= 2 && !mbar_wait(&acc_empty[b], ((u >> 1) - 1) & 1)) {
+                        record_stall(a.err, 4096u, c, warp);
                         ok = false;
                         break;
                     }
-                    if (*abort_flag) { ok = false; break; }
                     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-                    unsigned char* st = smem + s * STAGE2_BYTES;
-                    const uint32_t ah = smem_u32(st), al = ah + A2_BYTES;
-                    const uint32_t bh = ah + 2 * A2_BYTES, bl = bh + B2_BYTES;
-#pragma unroll
-                    for (int kk = 0; kk < BK2 / 16; kk++) {
-                        const uint32_t off = kk * 32;   // 16 FP16 = 32 bytes along K inside the swizzle row
-                        mma_f16(tmem, make_desc64(al + off), make_desc64(bh + off), idesc, acc);
-                        acc = 1;
-                        mma_f16(tmem, make_desc64(ah + off), make_desc64(bl + off), idesc, 1);
-                        mma_f16(tmem, make_desc64(ah + off), make_desc64(bh + off), idesc, 1);
+                    uint32_t st_addr[KCHUNK2];
+                    int st_idx[KCHUNK2];
+                    for (int j = 0; j < KCHUNK2 && ok; j++) {
+                        const int g = it * nk + c * KCHUNK2 + j;
+                        const int s = g % STAGES2;
+                        if (!mbar_wait(&full[s], (g / STAGES2) & 1)) {
+                            record_stall(a.err, 8u, c * KCHUNK2 + j, warp);
+                            ok = false;
+                        }
+                        st_idx[j] = s;
+                        st_addr[j] = smem_u32(smem + s * STAGE2_BYTES);
                     }
-                    mma_commit(&empty[s]);
+                    if (!ok || *abort_flag) {
+                        ok = false;
+                        break;
+                    }
+                    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                    const uint32_t d = tmem + (uint32_t)(b * BN2);
+                    uint32_t acc = 0;
+#pragma unroll
+                    for (int j = 0; j < KCHUNK2; j++) {
+                        const uint32_t ah = st_addr[j], al = ah + A2_BYTES;
+                        const uint32_t bh = ah + 2 * A2_BYTES, bl = bh + B2_BYTES;
+#pragma unroll
+                        for (int kk = 0; kk < BK2 / 16; kk++) {
+                            const uint32_t off = kk * 32;   // 16 FP16 = 32 bytes along K inside the swizzle row
+                            mma_f16(d, make_desc64(al + off), make_desc64(bh + off), idesc, acc);
+                            acc = 1;
+                            mma_f16(d, make_desc64(ah + off), make_desc64(bl + off), idesc, 1);
+                        }
+                    }
+#pragma unroll
+                    for (int j = 0; j < KCHUNK2; j++) {
+                        const uint32_t ah = st_addr[j], bh = ah + 2 * A2_BYTES;
+#pragma unroll
+                        for (int kk = 0; kk < BK2 / 16; kk++) {
+                            const uint32_t off = kk * 32;
+                            mma_f16(d, make_desc64(ah + off), make_desc64(bh + off), idesc, 1);
+                        }
+                    }
+                    for (int j = 0; j < KCHUNK2; j++) mma_commit(&empty[st_idx[j]]);
+                    mma_commit(&acc_full[b]);
                 }
-                if (!ok) {
-                    *abort_flag = 1;
-                    break;
-                }
-                mma_commit(acc_full);
             }
+            if (!ok) *abort_flag = 1;
             mma_commit(done);
         }
         __syncwarp();
     } else {
-        // ------------------------------------------------ epilogue: each warp reads its 64
-        // accumulator columns out, hands tensor memory back, then stores / updates
+        // ------------------------------------------------ epilogue: each warp reads its 32
+        // accumulator columns of every chunk, hands the buffer back, adds the chunk to its
+        // running sums (round-to-nearest FP32), and after the last chunk stores / updates
         const int q = warp & 3;                 // TMEM lane quarter this warp may read
-        const int part = (warp - 2) >> 2;       // which 64 columns (0..3)
-        for (int it = 0; it < my_tiles; it++) {
-            const bool ok = __all_sync(0xffffffffu, mbar_wait(acc_full, it & 1) ? 1 : 0) != 0;
-            if (!ok) {
-                if (lane == 0) record_stall(a.err, 32u, it, warp);
-                *abort_flag = 1;
-                break;
-            }
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            if (__any_sync(0xffffffffu, *abort_flag)) break;   // warp-uniform: tcgen05.ld is .sync.aligned
+        const int part = (warp - 2) >> 2;       // which 32 columns (0..3)
+        bool ok = true;
+        for (int it = 0; it < my_tiles && ok; it++) {
             const int T = blockIdx.x + it * gridDim.x;
             const int m0 = (T % MT) * BM, c0 = (T / MT) * BN2;
             const int i = m0 + 32 * q + lane;
+            float sum[32];
+            for (int c = 0; c < nch; c++) {
+                const int u = it * nch + c, b = u & 1;
+                ok = __all_sync(0xffffffffu, mbar_wait(&acc_full[b], (u >> 1) & 1) ? 1 : 0) != 0;
+                if (!ok) {
+                    if (lane == 0) record_stall(a.err, 32u, c, warp);
+                    *abort_flag = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                if (__any_sync(0xffffffffu, *abort_flag)) {   // warp-uniform: tcgen05.ld is .sync.aligned
+                    ok = false;
+                    break;
+                }
+                float v[32];
+                tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(b * BN2 + 32 * part), v);
+                asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+                __syncwarp();
+                if (lane == 0) mbar_arrive(&acc_empty[b]);
+                if (c == 0) {
+#pragma unroll
+                    for (int k = 0; k < 32; k++) sum[k] = v[k];
+                } else {
+#pragma unroll
+                    for (int k = 0; k < 32; k++) sum[k] = __fadd_rn(sum[k], v[k]);
+                }
+            }
+            if (!ok) break;
             const float kt2i = a.kt2 ? a.kt2[i] : 0.f;
-            float accv[64];
-            tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * part), accv);
-            tmem_ld32(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(64 * part + 32), accv + 32);
-            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-            __syncwarp();
-            if (lane == 0) mbar_arrive(acc_empty);
-            epilogue_cols(a, accv, i, c0 + 64 * part, kt2i);
-            epilogue_cols(a, accv + 32, i, c0 + 64 * part + 32, kt2i);
+            epilogue_cols(a, sum, i, c0 + 32 * part, kt2i);
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     }
@@ -915,7 +965,7 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(BN2));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN2));
     }
 }
 
@@ -960,6 +1010,14 @@ static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
             fn = (PFN_cuTensorMapEncodeTiled_v12000)p;
     }
     return fn;
+}
+
+static cudaError_t split_smem_ceiling() {
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, tc::qdht_split16_kernel);
+    if (e != cudaSuccess) return e;
+    return cudaFuncSetAttribute(tc::qdht_split16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)(227 * 1024 - fa.sharedSizeBytes));
 }
 
 QdhtTc* qdht_tc_create(int nr, int nt, cudaStream_t st, std::string* msg) {
@@ -1010,7 +1068,7 @@ QdhtTc* qdht_tc_create(int nr, int nt, cudaStream_t st, std::string* msg) {
             return nullptr;
         }
     }
-    q->wide = (2 * nt) % tc::BN2 == 0;
+    q->wide = (2 * nt) % tc::WIDE_COLS == 0;
     if (q->wide) {
         const size_t ncols = 2 * (size_t)nt;
         bool okw = cudaMalloc(&q->xhT, ncols * nr * 2) == cudaSuccess && cudaMalloc(&q->xlT, ncols * nr * 2) == cudaSuccess &&
@@ -1020,8 +1078,10 @@ QdhtTc* qdht_tc_create(int nr, int nt, cudaStream_t st, std::string* msg) {
                    cudaFuncSetAttribute(tc::qdht_tc2_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                         tc::SMEM2_BYTES) == cudaSuccess &&
                    (size_t)(nr / 2) * 33 * 4 <= 227 * 1024 &&
-                   cudaFuncSetAttribute(tc::qdht_split16_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                        (nr / 2) * 33 * 4) == cudaSuccess;
+                   // a per-kernel ceiling shared by every plan of the process: the device maximum
+                   // less the kernel's static shared memory, so that a plan for fewer rows never
+                   // lowers it below a larger plan's need
+                   split_smem_ceiling() == cudaSuccess;
         for (int w = 0; okw && w < 2; w++) {
             // [2 n_t rows c][n_r halves j]: boxes of 32 j (64 B, swizzled) x 256 c
             cuuint64_t gdim[2] = {(cuuint64_t)nr, (cuuint64_t)ncols};
@@ -1081,8 +1141,8 @@ int qdht_tc_set_matrix(QdhtTc* q, const double* C, const double* m1, std::string
         return 1;
     }
     if (q->wide) {
-        // FP16 parts of H[i][j] / hscale[i], hscale[i] the power of two above the row's largest
-        // |H|: Hh round-to-nearest, Hl the rounded remainder (computed in FP64)
+        // FP16 parts of H[i][j] / hscale[i], hscale[i] the power of two above 2^-14 of the row's
+        // largest |H|: Hh round-to-nearest, Hl the rounded remainder (computed in FP64)
         std::vector<__half> h16((size_t)nr * nr), l16((size_t)nr * nr);
         std::vector<float> hs(nr);
         for (int i = 0; i < nr; i++) {
@@ -1090,7 +1150,8 @@ int qdht_tc_set_matrix(QdhtTc* q, const double* C, const double* m1, std::string
             for (int j = 0; j < nr; j++) m = std::max(m, std::fabs(m1[i] * C[(size_t)i + (size_t)nr * j] / m1[j]));
             int e = 0;
             if (m > 0) std::frexp(m, &e);
-            const double sc = std::ldexp(1.0, e);
+            e = std::max(e, -108);
+            const double sc = std::ldexp(1.0, e - tc::OPERAND_EXP);   // |H / sc| < 2^14
             hs[i] = (float)sc;
             for (int j = 0; j < nr; j++) {
                 const double h = m1[i] * C[(size_t)i + (size_t)nr * j] / m1[j] / sc;
