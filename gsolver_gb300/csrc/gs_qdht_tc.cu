@@ -75,6 +75,10 @@ struct TcArgs {
     const int* cmap;
     float* yc;   // non-null: the output goes to this [nr][nc] compact array instead of Y
     int ycompact;   // linear step: Y is the compact [nr][nc] copy of BIGBUFFER2's window columns
+    // linear step on compact columns: double-float factors of this dz and 1 / (1 + s), both
+    // [nr][nc / 2] by compact column pair (null: the factor is evaluated in FP32 per element)
+    const float4* fac;
+    const float* inv1ps;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -647,6 +651,94 @@ __host__ __device__ constexpr uint32_t make_idesc_f16(int n) {
     return (1u << 4) | ((uint32_t)(n >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
 }
 
+// ---- double-float arithmetic (Dekker's pairs: a value hi + lo, |lo| <= ulp(hi) / 2, built on
+// Knuth's TwoSum and the FMA product error), ~48 significant bits on the FP32 pipe ----
+struct ff2 {
+    float h, l;
+};
+__device__ __forceinline__ ff2 ff_fast_sum(float a, float b) {   // |a| >= |b|
+    const float s = a + b;
+    return {s, b - (s - a)};
+}
+__device__ __forceinline__ ff2 ff_add(ff2 a, ff2 b) {
+    const float s = a.h + b.h;
+    const float bb = s - a.h;
+    const float e = (a.h - (s - bb)) + (b.h - bb) + a.l + b.l;
+    return ff_fast_sum(s, e);
+}
+__device__ __forceinline__ ff2 ff_mul(ff2 a, ff2 b) {
+    const float p = a.h * b.h;
+    float e = fmaf(a.h, b.h, -p);
+    e = fmaf(a.h, b.l, fmaf(a.l, b.h, e));
+    return ff_fast_sum(p, e);
+}
+__device__ __forceinline__ ff2 ff_mul_f(ff2 a, float b) {
+    const float p = a.h * b;
+    const float e = fmaf(a.h, b, -p) + a.l * b;
+    return ff_fast_sum(p, e);
+}
+__device__ __forceinline__ ff2 ff_neg(ff2 a) { return {-a.h, -a.l}; }
+__host__ __device__ constexpr float ff_hi(double d) { return (float)d; }
+__host__ __device__ constexpr float ff_lo(double d) { return (float)(d - (double)(float)d); }
+
+// exp(z) of a complex double-float z = x + i y: the linear step's propagator factor
+// exp(dz (k_i + i theta)).  Phase: y reduced by the nearest multiple of pi/2 (Cody and Waite's
+// additive reduction with a double-float pi/2), then sin and cos of |r| <= pi/4 from their
+// Taylor series (the two leading terms of each in double-float, the rest in FP32: below 2^-46
+// absolute); amplitude: exp(x) from its Taylor series for |x| < 2^-6, else the FP32 exponential
+// (x is dz times the absorbing layer's k_i, zero inside the medium's window).
+__device__ __forceinline__ void ff_cexp(ff2 x, ff2 y, ff2* re, ff2* im) {
+    constexpr double PIO2 = 1.57079632679489661923132169163975144;
+    const float k = rintf(y.h * (float)(1.0 / PIO2));
+    const ff2 r = ff_add(y, ff_neg(ff_mul_f(ff2{ff_hi(PIO2), ff_lo(PIO2)}, k)));
+    const ff2 r2 = ff_mul(r, r);
+    const float u = r2.h;
+    // sin r = r + r^3 (-1/6 + u/120 + u^2 Ts(u)),  cos r = 1 - u/2 + u^2 (1/24 - u/720 + u^2 Tc(u))
+    const float ts = u * (u * (u * (u * (u * (-1.0f / 1307674368000.0f) + 1.0f / 6227020800.0f) - 1.0f / 39916800.0f) +
+                               1.0f / 362880.0f) -
+                          1.0f / 5040.0f);
+    const float tc = u * (u * (u * (u * (u * (1.0f / 20922789888000.0f) - 1.0f / 87178291200.0f) + 1.0f / 479001600.0f) -
+                               1.0f / 3628800.0f) +
+                          1.0f / 40320.0f);
+    const ff2 s_poly = ff_add(ff2{ff_hi(-1.0 / 6), ff_lo(-1.0 / 6)},
+                              ff_mul(r2, ff_add(ff2{ff_hi(1.0 / 120), ff_lo(1.0 / 120)}, ff2{ts, 0.f})));
+    const ff2 sn = ff_add(r, ff_mul(ff_mul(r, r2), s_poly));
+    const ff2 c_poly = ff_add(ff2{ff_hi(1.0 / 24), ff_lo(1.0 / 24)},
+                              ff_mul(r2, ff_add(ff2{ff_hi(-1.0 / 720), ff_lo(-1.0 / 720)}, ff2{tc, 0.f})));
+    const ff2 cs = ff_add(ff2{1.f, 0.f}, ff_add(ff_mul_f(r2, -0.5f), ff_mul(ff_mul(r2, r2), c_poly)));
+    const int q = ((int)k) & 3;
+    ff2 c = cs, sv = sn;
+    if (q == 1) { c = ff_neg(sn); sv = cs; }
+    else if (q == 2) { c = ff_neg(cs); sv = ff_neg(sn); }
+    else if (q == 3) { c = sn; sv = ff_neg(cs); }
+    ff2 a;
+    if (fabsf(x.h) < 0.015625f) {   // 1 + x + x^2/2 + x^3 (1/6 + x/24 + ...)
+        const float t3 = x.h * x.h * x.h * (1.0f / 6 + x.h * (1.0f / 24 + x.h * (1.0f / 120 + x.h * (1.0f / 720))));
+        a = ff_add(ff2{1.f, 0.f}, ff_add(x, ff_add(ff_mul_f(ff_mul(x, x), 0.5f), ff2{t3, 0.f})));
+    } else {
+        a = ff2{expf(x.h), 0.f};
+    }
+    *re = ff_mul(a, c);
+    *im = ff_mul(a, sv);
+}
+
+// The linear step's factors for one dz over the spectral window's compact columns:
+// fac[i][c/2] = (P_hi, P_lo), P = exp(dz (k_i + i theta(i, p))) of calculate_Lstep
+// (propagator.cu:614-616) with theta(i, p) = -HO(p) - sqrtHO(-kt2_i / k_r^2) k_r(p) tabulated
+// in FP64 at set-up as a double-float pair; elements outside the window are left unused.
+__global__ void qdht_factor_kernel(const float2* __restrict__ theta, const float2* __restrict__ kiff,
+                                   float4* __restrict__ fac, int nr, int npair, float dz_h, float dz_l) {
+    const size_t total = (size_t)nr * npair;
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+        const int c2 = (int)(idx % npair);
+        const float2 t = theta[idx], kk = kiff[c2];
+        const ff2 dz{dz_h, dz_l};
+        ff2 re, im;
+        ff_cexp(ff_mul(dz, ff2{kk.x, kk.y}), ff_mul(dz, ff2{t.x, t.y}), &re, &im);
+        fac[idx] = make_float4(re.h, im.h, re.l, im.l);
+    }
+}
+
 // 32 accumulator columns of row i starting at output column cg: a plain store or the fused
 // calculate_Lstep update of BIGBUFFER2 (propagator.cu:570-625)
 __device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, int cg, float kt2i) {
@@ -683,6 +775,29 @@ __device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, 
 #pragma unroll
         for (int k = 0; k < 32; k += 4)
             *reinterpret_cast<float4*>(yrow + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
+        return;
+    }
+    if (a.fac) {   // compact columns with the double-float factor table of this dz
+        const size_t t0 = (size_t)i * (a.nc >> 1) + (cg >> 1);
+#pragma unroll
+        for (int e = 0; e < 16; e++) {
+            const int rc = a.cmap[cg + 2 * e];
+            if (rc < 0) continue;               // padding
+            if (i > a.kmax[rc >> 1]) continue;  // outside the window: BIGBUFFER2 untouched
+            float2* y2 = reinterpret_cast<float2*>(a.ycompact ? a.Y + (size_t)i * a.nc + cg + 2 * e
+                                                              : a.Y + (size_t)i * a.ncols + rc);
+            const float inv = a.inv1ps[t0 + e];
+            const float4 P = a.fac[t0 + e];   // (P_hi re, im, P_lo re, im)
+            float2 b2 = *y2;
+            b2.x += a.dz * v[2 * e] * inv;
+            b2.y += a.dz * v[2 * e + 1] * inv;
+            // b2 (P_hi + P_lo): the low part's product first, then the two high-part FMAs
+            const float lr = b2.x * P.z - b2.y * P.w, li = b2.x * P.w + b2.y * P.z;
+            float2 f;
+            f.x = fmaf(b2.x, P.x, fmaf(-b2.y, P.y, lr));
+            f.y = fmaf(b2.x, P.y, fmaf(b2.y, P.x, li));
+            *y2 = f;
+        }
         return;
     }
 #pragma unroll
@@ -995,6 +1110,14 @@ struct QdhtTc {
     float* yc = nullptr;      // [n_r][nc_act]: the masked inverse's compact result
     float* xc = nullptr;      // [n_r][nc_act]: a compact linear-step input written by its producer
     float* sc = nullptr;      // [n_r][nc_act]: BIGBUFFER2's window columns kept compact between steps
+    // the linear step's factors on the compact columns, per pair c / 2 of row i ([n_r][nc_act / 2]):
+    // theta = -HO - sqrtHO(-kt2 / k_r^2) k_r and k_i (per pair) as double-float pairs, 1 / (1 + s),
+    // and exp(dz (k_i + i theta)) as (hi, lo) for the dz in fac_dz (NaN: not built)
+    float2* theta = nullptr;
+    float2* kiff = nullptr;
+    float* inv1ps = nullptr;
+    float4* fac = nullptr;
+    double fac_dz = NAN;
     CUtensorMap map_bh, map_bl, map_hi64, map_lo64;   // 32-half boxes in the 64-byte swizzle
     // tensor maps of the X operands seen so far (the handle's few state arrays)
     std::vector<std::pair<const float*, CUtensorMap>> xmaps;
@@ -1237,6 +1360,51 @@ int qdht_tc_set_lstep(QdhtTc* q, const double* omega, const double* wavenum, con
             if (msg) *msg = "window column list upload failed";
             return 1;
         }
+        // theta and 1 / (1 + s) per row and compact pair in FP64 (calculate_Lstep,
+        // propagator.cu:614-616, with the reference's 20-term sqrtHO, extmath.h:245-256)
+        double hk[20], bc = 1.0;
+        for (int n = 1; n <= 20; n++) { bc *= (0.5 - (n - 1)) / n; hk[n - 1] = bc; }
+        const size_t npair = cm.size() / 2;
+        std::vector<float2> th((size_t)nr * npair, make_float2(0.f, 0.f)), kf(npair, make_float2(0.f, 0.f));
+        std::vector<float> iv((size_t)nr * npair, 0.f);
+        for (size_t c2 = 0; c2 < npair; c2++) {
+            const int rc = cm[2 * c2];
+            if (rc < 0) continue;
+            const int pp = rc >> 1;
+            const double k1 = wavenum[2 * pp], k2 = wavenum[2 * pp + 1];
+            kf[c2] = make_float2((float)k2, (float)(k2 - (double)(float)k2));
+            for (int i = 0; i <= kmax[pp]; i++) {
+                const double x = -kt2[i] / k1 / k1;
+                double sq = 0, xn = x;
+                for (int j = 0; j < 20; j++) { sq += hk[j] * xn; xn *= x; }
+                const double t = -ho[pp] - sq * k1;
+                th[(size_t)i * npair + c2] = make_float2((float)t, (float)(t - (double)(float)t));
+                iv[(size_t)i * npair + c2] = (float)(1.0 / (1.0 + sq));
+            }
+        }
+        if (q->theta) cudaFree(q->theta);
+        if (q->kiff) cudaFree(q->kiff);
+        if (q->inv1ps) cudaFree(q->inv1ps);
+        if (q->fac) cudaFree(q->fac);
+        q->theta = nullptr;
+        q->kiff = nullptr;
+        q->inv1ps = nullptr;
+        q->fac = nullptr;
+        q->fac_dz = NAN;
+        if (npair > 0) {
+            const size_t ne = (size_t)nr * npair;
+            const bool okf = cudaMalloc(&q->theta, ne * sizeof(float2)) == cudaSuccess &&
+                             cudaMalloc(&q->kiff, npair * sizeof(float2)) == cudaSuccess &&
+                             cudaMalloc(&q->inv1ps, ne * sizeof(float)) == cudaSuccess &&
+                             cudaMalloc(&q->fac, ne * sizeof(float4)) == cudaSuccess &&
+                             cudaMemcpy(q->theta, th.data(), ne * sizeof(float2), cudaMemcpyHostToDevice) == cudaSuccess &&
+                             cudaMemcpy(q->kiff, kf.data(), npair * sizeof(float2), cudaMemcpyHostToDevice) == cudaSuccess &&
+                             cudaMemcpy(q->inv1ps, iv.data(), ne * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
+            if (!okf) {
+                if (msg) *msg = "linear-step factor tables: allocation or upload failed";
+                return 1;
+            }
+        }
     }
     q->have_lstep = true;
     return 0;
@@ -1267,6 +1435,8 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
     a.cmap = nullptr;
     a.yc = nullptr;
     a.ycompact = 0;
+    a.fac = nullptr;
+    a.inv1ps = nullptr;
     if (q->wide) {
         // The linear step leaves BIGBUFFER2 untouched outside the spectral window and the masked
         // inverse transforms a zero column there: both run on the window's columns only (the
@@ -1295,6 +1465,25 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
             Y = q->sc;
             a.Y = q->sc;
             a.ycompact = 1;
+        }
+        if (mode == QDHT_LSTEP && q->fac) {
+            // the double-float factors of this dz: rebuilt when dz changes, and always recorded
+            // into a graph under capture (a replay must not depend on the table's last dz)
+            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+            cudaError_t ce = cudaStreamIsCapturing(q->st, &cs);
+            if (ce != cudaSuccess) return ce;
+            const bool capturing = cs != cudaStreamCaptureStatusNone;
+            if (capturing || !(L.dz == q->fac_dz)) {
+                const int npair = a.nc / 2;
+                const size_t total = (size_t)q->nr * npair;
+                const unsigned gf = (unsigned)std::min<size_t>((total + 255) / 256, (size_t)q->sms * 8);
+                const float dzh = (float)L.dz, dzl = (float)(L.dz - (double)dzh);
+                tc::qdht_factor_kernel<<<gf, 256, 0, q->st>>>(q->theta, q->kiff, q->fac, q->nr, npair, dzh, dzl);
+                (*nlaunch)++;
+                q->fac_dz = capturing ? NAN : L.dz;
+            }
+            a.fac = q->fac;
+            a.inv1ps = q->inv1ps;
         }
         // split X into the K-major FP16 hi / lo operands and the column scales (the window mask
         // of the inverse applied), then the GEMM on 128 x 256 tiles
@@ -1399,7 +1588,7 @@ int qdht_tc_check(QdhtTc* q, std::string* msg) {
 void qdht_tc_destroy(QdhtTc* q) {
     if (!q) return;
     void* ptrs[] = {q->hh, q->hl, q->kr, q->ki, q->ho, q->kt2, q->kmax, q->err, q->xhT, q->xlT, q->hh16, q->hl16, q->hs, q->xs,
-                    q->cmap, q->zpos, q->cinv, q->yc, q->xc, q->sc};
+                    q->cmap, q->zpos, q->cinv, q->yc, q->xc, q->sc, q->theta, q->kiff, q->inv1ps, q->fac};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete q;
