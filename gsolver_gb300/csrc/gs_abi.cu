@@ -344,14 +344,26 @@ int gs_upload_tables(gs_handle* h, const gs_tables* t) {
             const int rc = gsi::field_sync(h);
             if (rc) return rc;
         }
-        if (h->s_compact) {
+        // BIGBUFFER2's double-float window columns are kept across the rebuild in FP64 (staging,
+        // natural order) and split again over the new column list
+        const bool keep_spec = h->s_compact;
+        if (keep_spec) {
             const int rc = gsi::spec_sync(h);
             if (rc) return rc;
+            const size_t nel = (size_t)nr * nt;
+            CK(h, launch_permute<float>(-1, h->S, h->staging, h->perm_dev, nt, nel, h->st, &h->launches));
+            CK(h, gs::qdht_tc_spec_ff(h->tc, (double*)h->staging, h->perm_dev, 0, &h->launches));
+            CK(h, cudaStreamSynchronize(h->st));
             gsi::spec_written(h);
         }
         if (gs::qdht_tc_set_matrix(h->tc, t->qdht_c, t->qdht_m1, &m)) return fail(h, GS_ERR_CUDA, "mixed QDHT matrix: " + m);
         if (gs::qdht_tc_set_lstep(h->tc, om.data(), wn.data(), ho.data(), t->kt2, h->p.omega_min, h->p.omega_max, &m))
             return fail(h, GS_ERR_CUDA, "mixed QDHT: " + m);
+        if (keep_spec && gs::qdht_tc_has_compact(h->tc)) {
+            CK(h, gs::qdht_tc_spec_ff(h->tc, (double*)h->staging, h->perm_dev, 1, &h->launches));
+            CK(h, cudaStreamSynchronize(h->st));
+            h->s_compact = true;
+        }
     }
     if (h->p.gas && h->p.th_coeff != 0) {
         // third harmonic (propagator.cu:712-720): th_coeff exp(j phi_t), phi_t =
@@ -494,16 +506,28 @@ int gsi::permute_in(gs_handle* h, const double* host, void* dst) {
     const size_t nel = (size_t)h->nr * h->nt;
     if (dst == h->S) spec_written(h);
     if (dst == h->A) field_written(h);
+    // mixed plans keep BIGBUFFER2's window columns as a double-float pair: an FP64 spectrum
+    // given here is split into its high and low parts there, so that a state read back by
+    // gs_get_field and set again continues exactly
+    const bool spec_ff = dst == h->S && !h->fp64 && h->tc && gs::qdht_tc_has_compact(h->tc);
     if (void* dp = pinned_device_ptr(host, nel * 16)) {   // read over the host link, no staging copy
         cudaError_t e = h->fp64 ? launch_permute_host<double>(+1, dp, dst, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches)
                                 : launch_permute_host<float>(+1, dp, dst, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches);
         CK(h, e);
+        if (spec_ff) {
+            CK(h, gs::qdht_tc_spec_ff(h->tc, (double*)dp, h->perm_dev, 1, &h->launches));
+            h->s_compact = true;
+        }
         return GS_OK;
     }
     CK(h, cudaMemcpyAsync(h->staging, host, nel * 16, cudaMemcpyHostToDevice, h->st));
     cudaError_t e = h->fp64 ? launch_permute<double>(+1, h->staging, dst, h->perm_dev, h->nt, nel, h->st, &h->launches)
                             : launch_permute<float>(+1, h->staging, dst, h->perm_dev, h->nt, nel, h->st, &h->launches);
     CK(h, e);
+    if (spec_ff) {
+        CK(h, gs::qdht_tc_spec_ff(h->tc, (double*)h->staging, h->perm_dev, 1, &h->launches));
+        h->s_compact = true;
+    }
     return GS_OK;
 }
 int gsi::permute_out(gs_handle* h, const void* src, double* host) {
@@ -516,16 +540,20 @@ int gsi::permute_out(gs_handle* h, const void* src, double* host) {
         const int rc = field_sync(h);
         if (rc) return rc;
     }
+    // BIGBUFFER2's window columns leave as their double-float value (high + low parts)
+    const bool spec_ff = src == h->S && h->s_compact && !h->fp64;
     if (void* dp = pinned_device_ptr(host, nel * 16)) {   // written over the host link
         cudaError_t e = h->fp64 ? launch_permute_host<double>(-1, src, dp, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches)
                                 : launch_permute_host<float>(-1, src, dp, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches);
         CK(h, e);
+        if (spec_ff) CK(h, gs::qdht_tc_spec_ff(h->tc, (double*)dp, h->perm_dev, 0, &h->launches));
         CK(h, cudaStreamSynchronize(h->st));
         return GS_OK;
     }
     cudaError_t e = h->fp64 ? launch_permute<double>(-1, src, h->staging, h->perm_dev, h->nt, nel, h->st, &h->launches)
                             : launch_permute<float>(-1, src, h->staging, h->perm_dev, h->nt, nel, h->st, &h->launches);
     CK(h, e);
+    if (spec_ff) CK(h, gs::qdht_tc_spec_ff(h->tc, (double*)h->staging, h->perm_dev, 0, &h->launches));
     CK(h, cudaMemcpyAsync(host, h->staging, nel * 16, cudaMemcpyDeviceToHost, h->st));
     CK(h, cudaStreamSynchronize(h->st));
     return GS_OK;

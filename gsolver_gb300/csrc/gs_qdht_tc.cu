@@ -79,6 +79,7 @@ struct TcArgs {
     // [nr][nc / 2] by compact column pair (null: the factor is evaluated in FP32 per element)
     const float4* fac;
     const float* inv1ps;
+    float* ylo;     // with ycompact and fac: the low parts of Y (BIGBUFFER2's double-float compact copy)
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -660,11 +661,19 @@ __device__ __forceinline__ ff2 ff_fast_sum(float a, float b) {   // |a| >= |b|
     const float s = a + b;
     return {s, b - (s - a)};
 }
+__device__ __forceinline__ ff2 ff_two_sum(float a, float b) {   // any magnitudes
+    const float s = a + b;
+    const float bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+// the sum renormalised by a full TwoSum: under cancellation the error term can exceed the high
+// sum, and every stored pair stays canonical (hi = RN(hi + lo)), so a state written out as
+// hi + lo in FP64 and split again continues bit for bit
 __device__ __forceinline__ ff2 ff_add(ff2 a, ff2 b) {
     const float s = a.h + b.h;
     const float bb = s - a.h;
     const float e = (a.h - (s - bb)) + (b.h - bb) + a.l + b.l;
-    return ff_fast_sum(s, e);
+    return ff_two_sum(s, e);
 }
 __device__ __forceinline__ ff2 ff_mul(ff2 a, ff2 b) {
     const float p = a.h * b.h;
@@ -788,6 +797,22 @@ __device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, 
                                                               : a.Y + (size_t)i * a.ncols + rc);
             const float inv = a.inv1ps[t0 + e];
             const float4 P = a.fac[t0 + e];   // (P_hi re, im, P_lo re, im)
+            if (a.ylo) {
+                // BIGBUFFER2 carried as a double-float pair: (B2 + dz N / (1 + s)) P with ~48
+                // significant bits, so that factors within 2^-24 of 1 (small k_t near omega0,
+                // where the step's phase is tiny) still turn the state instead of being lost to
+                // FP32 rounding
+                float2* y2l = reinterpret_cast<float2*>(a.ylo + (size_t)i * a.nc + cg + 2 * e);
+                const float2 bh = *y2, bl = *y2l;
+                const ff2 br = ff_add(ff2{bh.x, bl.x}, ff2{a.dz * v[2 * e] * inv, 0.f});
+                const ff2 bi = ff_add(ff2{bh.y, bl.y}, ff2{a.dz * v[2 * e + 1] * inv, 0.f});
+                const ff2 pr{P.x, P.z}, pi{P.y, P.w};
+                const ff2 fr = ff_add(ff_mul(br, pr), ff_neg(ff_mul(bi, pi)));
+                const ff2 fi = ff_add(ff_mul(br, pi), ff_mul(bi, pr));
+                *y2 = make_float2(fr.h, fi.h);
+                *y2l = make_float2(fr.l, fi.l);
+                continue;
+            }
             float2 b2 = *y2;
             b2.x += a.dz * v[2 * e] * inv;
             b2.y += a.dz * v[2 * e + 1] * inv;
@@ -855,20 +880,60 @@ __global__ void qdht_expand_kernel(const float* __restrict__ yc, float* __restri
     }
 }
 
-// BIGBUFFER2's window columns to / from their compact copy: dir > 0 S -> sc (padding columns
-// zero), dir < 0 sc -> S.  One (re, im) pair per thread.
-__global__ void qdht_spec_copy_kernel(float* __restrict__ S, float* __restrict__ sc, int nr, int ncols, int nc,
-                                      const int* __restrict__ cmap, int dir) {
+// BIGBUFFER2's window columns to / from their compact double-float copy sc + sl: dir > 0
+// S -> sc, sl = 0 (padding columns zero), dir < 0 sc -> S.  One (re, im) pair per thread.
+__global__ void qdht_spec_copy_kernel(float* __restrict__ S, float* __restrict__ sc, float* __restrict__ sl, int nr,
+                                      int ncols, int nc, const int* __restrict__ cmap, int dir) {
     const size_t total = (size_t)nr * (nc / 2);
     for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
         const size_t i = idx / (nc / 2);
         const int c = 2 * (int)(idx - i * (nc / 2));
         const int rc = cmap[c];
         float2* cpt = reinterpret_cast<float2*>(sc + i * nc + c);
-        if (dir > 0) {
+        if (dir > 0) {   // a fresh copy: its low parts are zero
             *cpt = rc >= 0 ? *reinterpret_cast<const float2*>(S + i * ncols + rc) : make_float2(0.f, 0.f);
-        } else if (rc >= 0) {
+            *reinterpret_cast<float2*>(sl + i * nc + c) = make_float2(0.f, 0.f);
+        } else if (rc >= 0) {   // S takes the high parts (the double-float value rounded to FP32)
             *reinterpret_cast<float2*>(S + i * ncols + rc) = *cpt;
+        }
+    }
+}
+
+// BIGBUFFER2's compact double-float copy from / into an FP64 array X [nr][nt] complex whose
+// column q holds position p with q = perm[p] (perm null: q = p): take (dir > 0) sets
+// sc = fl32(X), sl = fl32(X - sc) at the window's pairs (zeros in the padding); add (dir < 0)
+// adds sl into X at the window's pairs, so that X = sc + sl exactly where X already holds sc.
+// X may be pinned host memory reached over the host link.  One pair per thread.
+__global__ void qdht_spec_ff_kernel(double2* __restrict__ X, float* __restrict__ sc, float* __restrict__ sl, int nr,
+                                    int nt, int nc, const int* __restrict__ cmap, const int* __restrict__ perm,
+                                    int dir) {
+    const size_t total = (size_t)nr * (nc / 2);
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = idx / (nc / 2);
+        const int c = 2 * (int)(idx - i * (nc / 2));
+        const int rc = cmap[c];
+        float2* hp = reinterpret_cast<float2*>(sc + i * nc + c);
+        float2* lp = reinterpret_cast<float2*>(sl + i * nc + c);
+        if (rc < 0) {
+            if (dir > 0) {
+                *hp = make_float2(0.f, 0.f);
+                *lp = make_float2(0.f, 0.f);
+            }
+            continue;
+        }
+        const int pp = rc >> 1;
+        double2* x = X + i * (size_t)nt + (perm ? perm[pp] : pp);
+        if (dir > 0) {
+            const double2 v = *x;
+            const float hx = (float)v.x, hy = (float)v.y;
+            *hp = make_float2(hx, hy);
+            *lp = make_float2((float)(v.x - (double)hx), (float)(v.y - (double)hy));
+        } else {
+            const float2 l = *lp;
+            double2 v = *x;
+            v.x += (double)l.x;
+            v.y += (double)l.y;
+            *x = v;
         }
     }
 }
@@ -1110,6 +1175,7 @@ struct QdhtTc {
     float* yc = nullptr;      // [n_r][nc_act]: the masked inverse's compact result
     float* xc = nullptr;      // [n_r][nc_act]: a compact linear-step input written by its producer
     float* sc = nullptr;      // [n_r][nc_act]: BIGBUFFER2's window columns kept compact between steps
+    float* sl = nullptr;      // [n_r][nc_act]: their low parts (the compact copy is the double-float sc + sl)
     // the linear step's factors on the compact columns, per pair c / 2 of row i ([n_r][nc_act / 2]):
     // theta = -HO - sqrtHO(-kt2 / k_r^2) k_r and k_i (per pair) as double-float pairs, 1 / (1 + s),
     // and exp(dz (k_i + i theta)) as (hi, lo) for the dz in fac_dz (NaN: not built)
@@ -1342,6 +1408,8 @@ int qdht_tc_set_lstep(QdhtTc* q, const double* omega, const double* wavenum, con
         if (q->yc) cudaFree(q->yc);
         if (q->xc) cudaFree(q->xc);
         if (q->sc) cudaFree(q->sc);
+        if (q->sl) cudaFree(q->sl);
+        q->sl = nullptr;
         q->cmap = q->zpos = q->cinv = nullptr;
         q->yc = q->xc = q->sc = nullptr;
         q->nc_act = (int)cm.size();
@@ -1355,6 +1423,8 @@ int qdht_tc_set_lstep(QdhtTc* q, const double* omega, const double* wavenum, con
                    (cm.empty() || (cudaMalloc(&q->yc, (size_t)nr * cm.size() * 4) == cudaSuccess &&
                                    cudaMalloc(&q->xc, (size_t)nr * cm.size() * 4) == cudaSuccess &&
                                    cudaMalloc(&q->sc, (size_t)nr * cm.size() * 4) == cudaSuccess &&
+                                   cudaMalloc(&q->sl, (size_t)nr * cm.size() * 4) == cudaSuccess &&
+                                   cudaMemset(q->sl, 0, (size_t)nr * cm.size() * 4) == cudaSuccess &&
                                    cudaMemset(q->xc, 0, (size_t)nr * cm.size() * 4) == cudaSuccess));
         if (!okc) {
             if (msg) *msg = "window column list upload failed";
@@ -1437,6 +1507,7 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
     a.ycompact = 0;
     a.fac = nullptr;
     a.inv1ps = nullptr;
+    a.ylo = nullptr;
     if (q->wide) {
         // The linear step leaves BIGBUFFER2 untouched outside the spectral window and the masked
         // inverse transforms a zero column there: both run on the window's columns only (the
@@ -1464,6 +1535,7 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
         if (mode == QDHT_LSTEP && s_comp) {   // the epilogue updates the compact copy
             Y = q->sc;
             a.Y = q->sc;
+            a.ylo = q->sl;
             a.ycompact = 1;
         }
         if (mode == QDHT_LSTEP && q->fac) {
@@ -1543,7 +1615,16 @@ cudaError_t qdht_tc_spec_copy(QdhtTc* q, float* S, int to_compact, long long* nl
     if (!qdht_tc_has_compact(q)) return cudaErrorInvalidValue;
     const size_t tot = (size_t)q->nr * (q->nc_act / 2);
     tc::qdht_spec_copy_kernel<<<(unsigned)std::min<size_t>((tot + 255) / 256, (size_t)q->sms * 16), 256, 0, q->st>>>(
-        S, q->sc, q->nr, 2 * q->nt, q->nc_act, q->cmap, to_compact ? 1 : -1);
+        S, q->sc, q->sl, q->nr, 2 * q->nt, q->nc_act, q->cmap, to_compact ? 1 : -1);
+    (*nlaunch)++;
+    return cudaGetLastError();
+}
+
+cudaError_t qdht_tc_spec_ff(QdhtTc* q, double* X, const int* perm, int take, long long* nlaunch) {
+    if (!qdht_tc_has_compact(q)) return cudaErrorInvalidValue;
+    const size_t tot = (size_t)q->nr * (q->nc_act / 2);
+    tc::qdht_spec_ff_kernel<<<(unsigned)std::min<size_t>((tot + 255) / 256, (size_t)q->sms * 16), 256, 0, q->st>>>(
+        reinterpret_cast<double2*>(X), q->sc, q->sl, q->nr, q->nt, q->nc_act, q->cmap, perm, take ? 1 : -1);
     (*nlaunch)++;
     return cudaGetLastError();
 }
@@ -1588,7 +1669,7 @@ int qdht_tc_check(QdhtTc* q, std::string* msg) {
 void qdht_tc_destroy(QdhtTc* q) {
     if (!q) return;
     void* ptrs[] = {q->hh, q->hl, q->kr, q->ki, q->ho, q->kt2, q->kmax, q->err, q->xhT, q->xlT, q->hh16, q->hl16, q->hs, q->xs,
-                    q->cmap, q->zpos, q->cinv, q->yc, q->xc, q->sc, q->theta, q->kiff, q->inv1ps, q->fac};
+                    q->cmap, q->zpos, q->cinv, q->yc, q->xc, q->sc, q->sl, q->theta, q->kiff, q->inv1ps, q->fac};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete q;

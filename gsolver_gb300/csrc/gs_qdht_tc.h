@@ -34,8 +34,15 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
                         std::string* msg, int flags = 0);
 // The plan keeps compact copies of the window's columns (wide-tile plans with linear-step tables).
 bool qdht_tc_has_compact(const QdhtTc* q);
-// Copy BIGBUFFER2 S's window columns into the compact copy (to_compact != 0) or back into S.
+// Copy BIGBUFFER2 S's window columns into the compact copy (to_compact != 0; its low parts
+// zero) or back into S (the high parts).  The compact copy is a double-float pair (high, low):
+// the linear step updates it with ~48 significant bits.
 cudaError_t qdht_tc_spec_copy(QdhtTc* q, float* S, int to_compact, long long* nlaunch);
+// The compact copy from / into an FP64 [n_r][n_t] complex array X (device or pinned host
+// memory) whose column perm[p] holds position p (perm null: position order): take != 0 splits
+// X's window pairs into high and low parts; take == 0 adds the low parts into X, which must
+// already hold the high parts there.
+cudaError_t qdht_tc_spec_ff(QdhtTc* q, double* X, const int* perm, int take, long long* nlaunch);
 // The compact [n_r][nc] input array of the linear-step transform and its position map (cinv[p]:
 // the column of position p's (re, im) pair, or -1 outside the spectral window); null when the
 // plan has no window columns (set_lstep not called, or a width outside the wide-tile path).

@@ -7,6 +7,9 @@
 * One propagator() call of the 1024 x 16384 workload on the FP64 GPU path against the oracle
   within 1e-10 (the full-size grid: window-compacted FP64 transforms, the FP64 row kernels of
   16384 points over two CTAs).
+* The mixed path's error against the FP64 path on the 1024 x 16384 workload does not grow with
+  the number of steps (200 fixed steps): the QDHT's chunked accumulation, the double-float
+  propagator factors and BIGBUFFER2's double-float window columns leave no error that builds up.
 """
 import tempfile
 
@@ -86,3 +89,26 @@ def test_fused_silica_1024x16384_one_step_fp64():
     assert rel(dg["f"], dr["f"]) < FP64_TOL
     assert rel(on_axis_plasma(O, f), on_axis_plasma(O, st["field"])) < FP64_TOL
     P.close()
+
+
+def test_fused_silica_1024x16384_mixed_error_does_not_grow():
+    d = tempfile.mkdtemp(prefix="gs_c2_err_")
+    S = gs.Setup(configs.fused_silica_c2(d), noise_seed=1234, noise_sigma=1e-4).as_dict()
+    dz = float(S["init_zstep"])
+    P64 = gs.Propagator(S, precision=gs.PREC_FP64)
+    Pm = gs.Propagator(S, precision=gs.PREC_MIXED)
+    errs = []
+    done = 0
+    for P in (P64, Pm):
+        P.set_field(S["field"])
+    for n in (20, 200):
+        for P in (P64, Pm):
+            for _ in range(n - done):
+                P.nl_step(dz)
+                P.lstep(dz)
+        done = n
+        errs.append(rel(Pm.get_field(want_spec=False), P64.get_field(want_spec=False)))
+    assert errs[1] < 1e-6, errs
+    assert errs[1] < 1.5 * errs[0], errs
+    P64.close()
+    Pm.close()

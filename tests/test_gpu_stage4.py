@@ -130,8 +130,9 @@ def test_stage4_agrees_with_per_stage_launches(hot16k):
 def test_table_reupload_expands_compact_field(hot16k):
     """Re-uploading the tables on a handle whose FIELD is held compactly (after a step of the
     four-stage grid) first expands FIELD through the old column lists: the field read after the
-    re-upload is the one read before it, and stepping on agrees bit for bit with a handle that
-    was never re-uploaded."""
+    re-upload is the one read before it, and stepping on agrees with a handle that was never
+    re-uploaded: the field bit for bit, BIGBUFFER2 (kept as double-float pairs across the
+    rebuild) to below FP32 resolution."""
     T, _ = hot16k
     dz = 2e-8
     a = gs.Propagator(T, precision=gs.PREC_MIXED)
@@ -152,6 +153,7 @@ def test_table_reupload_expands_compact_field(hot16k):
         P.lstep(dz)
     fa, sa = a.get_field(want_spec=True)
     fb, sb = b.get_field(want_spec=True)
-    assert np.array_equal(fa, fb) and np.array_equal(sa, sb)
+    assert np.array_equal(fa, fb)
+    assert np.all(np.abs(sa - sb) <= 2.0 ** -30 * np.abs(sb))
     a.close()
     b.close()
