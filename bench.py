@@ -11,11 +11,13 @@ Synthetic: the pulse is generated (seeded 1e-4 complex Gaussian noise), no datas
   e2e     the same metric through the public C ABI with pinned host buffers: every step
           copies FIELD and BIGBUFFER2 in and out (the host globals propagator() works on)
   fp64    the plain FP64 GPU path on the same workload, and the mixed path's relative L2
-          error against it after the same fixed-dz steps from the same start
-  roofline  the dominant kernel, nl_stage (one RK4 stage): its one-pass input and output (34 B
-          per field point in complex64) over its CUDA-event launch time; roofline_nl_step the
-          whole NL increment against its 16 B per field point minimum; roofline_qdht the
-          tensor-core QDHT, algorithmic 8 N_r flop per field-point step
+          error against it after 5, 100, 1000 and 2000 fixed-dz steps from the same start
+  roofline  the dominant kernel, nl_stage4_kernel (the four RK4 stages of every row in one
+          launch): the NL increment's algorithmic bytes, 16 B per field point (read FIELD,
+          write BIGBUFFER1, complex64), over its CUDA-event launch time; its DRAM traffic and
+          instruction counts from an ncu capture of one launch of this workload (the kernel
+          is bound by SM instruction issue, not by HBM); roofline_qdht the tensor-core QDHT,
+          algorithmic 8 N_r flop per field-point step
   adjoint the gradient workload (256 x 4096, 1000 steps): forward vs forward+adjoint time
           and the gradient's accuracy (see adjoint_leg)
   batch   64 pulses with uneven grids, one CUDA graph launch per z-step (see batch_leg)
@@ -31,7 +33,6 @@ from __future__ import annotations
 import argparse
 import json
 import os
-import re
 import subprocess
 import sys
 import tempfile
@@ -57,6 +58,8 @@ def parse():
     ap.add_argument("--only", default=None, choices=["adjoint", "batch", "argon"],
                     help="run one leg alone and print its JSON object (profiling captures)")
     ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--err-steps", default="5,100,1000,2000",
+                    help="step counts at which the mixed path's error against FP64 is recorded")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
@@ -164,16 +167,14 @@ def new_state(S):
     return {"z": float(S["znet"][0]), "n_z": 0, "zstep": float(S["init_zstep"]), "step_n": 0}
 
 
-def read_profile_traffic(name="qdht_tc_fused_silica_512x16384.md"):
-    """Per-launch DRAM bytes of a kernel from its committed ncu summary (a smaller capture
-    scaled to the 1024-row launch by the rows it processes)."""
-    p = os.path.join(ROOT, "profiles", name)
-    try:
-        with open(p) as f:
-            m = re.search(r"traffic_bytes_per_launch:\s*([0-9.eE+]+)", f.read())
-        return float(m.group(1)) if m else None
-    except OSError:
-        return None
+# Per field point of one launch on the 1024 x 16384 workload, from ncu captures of that
+# workload (dram__bytes_read.sum + dram__bytes_write.sum, smsp__inst_executed.sum and
+# sm__inst_issued.avg.pct_of_peak_sustained_active of one launch, divided by its n_r n_t field
+# points); they are fixed properties of the kernels, re-measured whenever a kernel changes.
+NCU_PER_POINT = {
+    "nl_stage4": {"dram_bytes": 14.70, "warp_instructions": 41.4, "issue_active": 0.598},
+    "qdht_pair": {"dram_bytes": None},
+}
 
 
 def window_columns(S):
@@ -231,7 +232,8 @@ def cpu_sample(T, nthreads=None):
     Oq.qdht(d1)
     t_cols = time.perf_counter() - t0
     t_step = t_rows * nr / len(rows) + t_cols * nt / cols
-    desc = (f"oracle (C port of the reference z-step, OpenMP {cores} threads, radix-2 FFT): RK4 NL step + "
+    desc = (f"oracle (C port of the reference z-step, agreeing with the reference solver itself to 1e-12 on every "
+            f"hot-path function; OpenMP {cores} threads, radix-2 FFT): RK4 NL step + "
             f"linear step on {len(rows)} of {nr} rows, forward+inverse QDHT on {cols} of {nt} omega columns, "
             f"extrapolated to one {nr}x{nt} step ({t_step:.2f} s)")
     return nr * nt / t_step, desc, cores
@@ -495,39 +497,38 @@ def main():
     flop_launch = 2.0 * nr * nr * ncol_win
     per_launch_ms = q_ms / max(q_n, 1)
     achieved = flop_launch / (per_launch_ms / 1e3) / 1e12 if q_n else None
-    roof_q = {"bound": "tensor", "kernel": "qdht_tc" if prec == gs.PREC_MIXED else "qdht64 (FP64 CUDA cores)",
-            "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
-            "frac": (achieved / bf16) if achieved else None, "traffic": read_profile_traffic() if prec == gs.PREC_MIXED else None,
-            "peak_kind": f"{pk_kind} cuBLAS bf16 burst", "launch_ms": per_launch_ms,
-            "qdht_share_of_step": (q_ms / ms) if ms else None,
-            "window_columns": ncol_win, "columns": 2 * nt,
-            "note": "algorithmic flop 2 N_r^2 per real column of the spectral window per transform (launch_ms is "
-                    "one transform, split + GEMM); the split FP16 operands execute 3 products (Hh Xh + Hh Xl + "
-                    "Hl Xh) at the FP16 rate, which equals the bf16 rate of the peak"}
-    # the dominant kernel: nl_stage (one RK4 stage per launch: inverse FFT, plasma and Raman
-    # recurrences, forward FFT of the sources, spectral combination, RK4 sums); its algorithmic
-    # bytes per launch are its one-pass input and output: A (8 B per field point), k of the
-    # previous stage and the RK4 sum read in stages 1-3 (6 + 6 B on average), k written in
-    # stages 0-2 (6 B on average) and the RK4 sum written (8 B): 34 B in complex64
+    qt = NCU_PER_POINT["qdht_pair"]["dram_bytes"]
+    roof_q = {"bound": "tensor", "kernel": "qdht_tc2 (split + GEMM)" if prec == gs.PREC_MIXED else "qdht64 (FP64 CUDA cores)",
+              "achieved": achieved, "peak": bf16, "unit": "TFLOP/s",
+              "frac": (achieved / bf16) if achieved else None,
+              "traffic": (qt * nr * nt / 2) if (qt and prec == gs.PREC_MIXED) else None,
+              "peak_kind": f"{pk_kind} cuBLAS bf16 burst", "launch_ms": per_launch_ms,
+              "qdht_share_of_step": (q_ms / ms) if ms else None,
+              "window_columns": ncol_win, "columns": 2 * nt,
+              "note": "algorithmic flop 2 N_r^2 per real column of the spectral window per transform (launch_ms is "
+                      "one transform: split, factor table when dz changes, GEMM); the split FP16 operands execute 3 "
+                      "products (Hh Xh + Hh Xl + Hl Xh) at the FP16 rate, which equals the bf16 rate of the peak"}
+    # the dominant kernel: nl_stage4_kernel, one launch per NL step (all four RK4 stages of a row
+    # in one CTA), or nl_stage_kernel once per stage on smaller grids; algorithmic bytes per step
+    # 16 per field point (read FIELD, write the NL increment BIGBUFFER1, complex64)
     esz = 8 if prec == gs.PREC_MIXED else 16
-    st_launch_ms = st_ms / n_st if n_st else None
-    st_bytes = (34 if esz == 8 else 68) * nr * nt
-    st_ach = st_bytes / (st_launch_ms / 1e3) / 1e9 if st_launch_ms else None
-    nl_step_ms = st_ms / n_st * 4 if n_st else None
-    nl_ach = (16 if esz == 8 else 32) * nr * nt / (nl_step_ms / 1e3) / 1e9 if nl_step_ms else None
-    roof = {"bound": "hbm", "kernel": ("nl_stage4_kernel (four RK4 stages per launch; per-stage figures)"
-                                       if n_launch < n_st else "nl_stage_kernel") if n_st else "staged NL kernels (not timed)",
-            "achieved": st_ach, "peak": hbm, "unit": "GB/s", "frac": (st_ach / hbm) if st_ach and hbm else None,
-            "traffic": read_profile_traffic("nl_stage4_silica_1024x16384.md") if prec == gs.PREC_MIXED else None,
-            "peak_kind": f"{pk_kind} HBM copy", "launch_ms": st_launch_ms,
-            "algorithmic_bytes_per_launch": st_bytes,
+    four = n_st and n_launch < n_st
+    step_ms_nl = st_ms / n_st * 4 if n_st else None
+    nl_bytes = 2 * esz * nr * nt
+    nl_ach = nl_bytes / (step_ms_nl / 1e3) / 1e9 if step_ms_nl else None
+    ncu4 = NCU_PER_POINT["nl_stage4"]
+    roof = {"bound": "hbm", "kernel": ("nl_stage4_kernel" if four else "nl_stage_kernel") if n_st else "staged NL kernels (not timed)",
+            "achieved": nl_ach, "peak": hbm, "unit": "GB/s", "frac": (nl_ach / hbm) if nl_ach and hbm else None,
+            "traffic": (ncu4["dram_bytes"] * nr * nt) if (four and prec == gs.PREC_MIXED) else None,
+            "peak_kind": f"{pk_kind} HBM copy", "launch_ms": step_ms_nl,
+            "algorithmic_bytes_per_launch": nl_bytes,
             "share_of_step": (st_ms / ms) if ms and n_st else None,
-            "note": "CUDA events around each launch on the handle's stream, per RK4 stage; traffic = a quarter of "
-                    "the ncu DRAM bytes of one four-stage launch of this workload"}
-    roof_nl = {"bound": "hbm", "unit": "GB/s", "peak": hbm, "achieved": nl_ach,
-               "frac": (nl_ach / hbm) if nl_ach and hbm else None, "step_ms": nl_step_ms,
-               "note": "the whole NL increment (4 RK4 stages, 4 launches) against its one-pass minimum: read A and "
-                       "write the NL increment once, 16 B per field point in complex64"}
+            "limiter": ({"kind": "SM instruction issue",
+                         "warp_instructions_per_field_point": ncu4["warp_instructions"],
+                         "issue_active_frac": ncu4["issue_active"]} if (four and prec == gs.PREC_MIXED) else None),
+            "note": "per NL step (one launch of all four RK4 stages), CUDA events around each launch on the handle's "
+                    "stream; algorithmic bytes 16 per field point (FIELD in, BIGBUFFER1 out, complex64); traffic and "
+                    "the limiter figures from an ncu capture of one launch of this workload"}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -537,7 +538,7 @@ def main():
                            parallelism=f"replicas{world}", l2="inputs larger than L2 (state ~1 GB per pulse)",
                            z_reached_m=state["z"], dz_last_m=state["zstep"],
                            nl_threads_per_row=tuned[0] if tuned else "default"),
-            "gpu_launches": launches, "roofline": roof, "roofline_nl_step": roof_nl, "roofline_qdht": roof_q,
+            "gpu_launches": launches, "roofline": roof, "roofline_qdht": roof_q,
             "clocks": clk.summary()}
 
     # e2e through the public API with pinned host buffers
@@ -570,20 +571,28 @@ def main():
         a1.synchronize()
         ms64 = a0.elapsed_time(a1)
         v64 = nr * nt * args.fp64_steps / (ms64 / 1e3)
-        # accuracy: both paths from the start field, fixed dz = first ZSTEP
-        nerr = 5
+        # accuracy: both paths from the start field, fixed dz = first ZSTEP, the mixed path's
+        # relative L2 error of FIELD and BIGBUFFER2 against the FP64 path after each count of steps
         dz = float(S["init_zstep"])
+        counts = sorted(int(c) for c in args.err_steps.split(",") if c)
+        curve = []
+        done = 0
         for Q in (P, P64):
             Q.set_field(S["field"])
-            for _ in range(nerr):
-                Q.nl_step(dz)
-                Q.lstep(dz)
-        fm = P.get_field(want_spec=False)
-        fd = P64.get_field(want_spec=False)
-        err = float(np.linalg.norm(fm - fd) / np.linalg.norm(fd))
+        for c in counts:
+            for Q in (P, P64):
+                for _ in range(c - done):
+                    Q.nl_step(dz)
+                    Q.lstep(dz)
+            done = c
+            fm, sm = P.get_field(want_spec=True)
+            fd, sd = P64.get_field(want_spec=True)
+            curve.append({"steps": c, "field": float(np.linalg.norm(fm - fd) / np.linalg.norm(fd)),
+                          "bigbuffer2": float(np.linalg.norm(sm - sd) / np.linalg.norm(sd))})
         line["fp64"] = {"value": v64, "unit": UNIT, "ms_per_step": ms64 / args.fp64_steps, "steps": args.fp64_steps,
                         "mixed_speedup": value / world / v64,
-                        "mixed_rel_l2_field_err": err, "err_steps": nerr, "err_dz_m": dz}
+                        "mixed_rel_l2_field_err": curve[-1]["field"] if curve else None,
+                        "err_steps": done, "err_dz_m": dz, "error_curve": curve}
         P64.close()
 
     if prec == gs.PREC_MIXED and not args.no_adjoint and args.workload == "c2":

@@ -511,11 +511,13 @@ int gsi::permute_in(gs_handle* h, const double* host, void* dst) {
     // gs_get_field and set again continues exactly
     const bool spec_ff = dst == h->S && !h->fp64 && h->tc && gs::qdht_tc_has_compact(h->tc);
     if (void* dp = pinned_device_ptr(host, nel * 16)) {   // read over the host link, no staging copy
+        // (the low parts go to the free staging buffer, in position order, on the same pass)
         cudaError_t e = h->fp64 ? launch_permute_host<double>(+1, dp, dst, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches)
-                                : launch_permute_host<float>(+1, dp, dst, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches);
+                                : launch_permute_host<float>(+1, dp, dst, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches,
+                                                             spec_ff ? h->staging : nullptr);
         CK(h, e);
         if (spec_ff) {
-            CK(h, gs::qdht_tc_spec_ff(h->tc, (double*)dp, h->perm_dev, 1, &h->launches));
+            CK(h, gs::qdht_tc_spec_dev(h->tc, (float*)h->S, (float*)h->staging, 1, &h->launches));
             h->s_compact = true;
         }
         return GS_OK;
@@ -543,10 +545,12 @@ int gsi::permute_out(gs_handle* h, const void* src, double* host) {
     // BIGBUFFER2's window columns leave as their double-float value (high + low parts)
     const bool spec_ff = src == h->S && h->s_compact && !h->fp64;
     if (void* dp = pinned_device_ptr(host, nel * 16)) {   // written over the host link
+        // (the compact low parts scattered into the free staging buffer first, then added on the pass)
+        if (spec_ff) CK(h, gs::qdht_tc_spec_dev(h->tc, nullptr, (float*)h->staging, 0, &h->launches));
         cudaError_t e = h->fp64 ? launch_permute_host<double>(-1, src, dp, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches)
-                                : launch_permute_host<float>(-1, src, dp, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches);
+                                : launch_permute_host<float>(-1, src, dp, h->iperm_dev, h->nt, nel, h->sms, h->st, &h->launches,
+                                                             spec_ff ? h->staging : nullptr);
         CK(h, e);
-        if (spec_ff) CK(h, gs::qdht_tc_spec_ff(h->tc, (double*)dp, h->perm_dev, 0, &h->launches));
         CK(h, cudaStreamSynchronize(h->st));
         return GS_OK;
     }

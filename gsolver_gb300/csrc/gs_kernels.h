@@ -155,10 +155,12 @@ cudaError_t launch_zero_nl(const typename Vec2<Rl>::T* A, typename Vec2<Rl>::T* 
 template <typename Rl>
 cudaError_t launch_permute(int dir, const void* src, void* dst, const int* perm, int N, size_t total,
                            cudaStream_t st, long long* nlaunch);
-// the same with the FP64 side a device-mapped pinned host buffer (iperm: natural -> position)
+// the same with the FP64 side a device-mapped pinned host buffer (iperm: natural -> position);
+// lo (optional, position order like the device side): dir > 0 writes the remainders of the FP64
+// values after rounding (the low parts of double-float values), dir < 0 adds them to the output
 template <typename Rl>
 cudaError_t launch_permute_host(int dir, const void* src, void* dst, const int* iperm, int N, size_t total, int sms,
-                                cudaStream_t st, long long* nlaunch);
+                                cudaStream_t st, long long* nlaunch, void* lo = nullptr);
 
 // ---- fused RK4 stage (gs_nl_fused.cu), rows that fit one CTA's shared memory
 template <typename Rl> bool nl_fused_supported(int N);

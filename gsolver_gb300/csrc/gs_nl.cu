@@ -501,7 +501,7 @@ __global__ void permute_out_kernel(const C2<Rl>* __restrict__ src, double2* __re
 // elements), iperm[q] the position of natural index q; four elements in flight per thread.
 template <typename Rl>
 __global__ void permute_in_host_kernel(const double2* __restrict__ src, C2<Rl>* __restrict__ dst,
-                                       const int* __restrict__ iperm, int N, size_t total) {
+                                       C2<Rl>* __restrict__ lo, const int* __restrict__ iperm, int N, size_t total) {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < total; i0 += 4 * stride) {
         double2 v[4];
@@ -516,28 +516,39 @@ __global__ void permute_in_host_kernel(const double2* __restrict__ src, C2<Rl>* 
             if (i >= total) break;
             const size_t row = i / N;
             const int q = (int)(i - row * N);
-            dst[row * N + iperm[q]] = C2<Rl>{(Rl)v[u].x, (Rl)v[u].y};
+            const C2<Rl> h{(Rl)v[u].x, (Rl)v[u].y};
+            dst[row * N + iperm[q]] = h;
+            // the remainder v - h (zero in FP64): the low parts of a double-float value
+            if (lo) lo[row * N + iperm[q]] = C2<Rl>{(Rl)(v[u].x - (double)h.x), (Rl)(v[u].y - (double)h.y)};
         }
     }
 }
 template <typename Rl>
-__global__ void permute_out_host_kernel(const C2<Rl>* __restrict__ src, double2* __restrict__ dst,
-                                        const int* __restrict__ iperm, int N, size_t total) {
+__global__ void permute_out_host_kernel(const C2<Rl>* __restrict__ src, const C2<Rl>* __restrict__ lo,
+                                        double2* __restrict__ dst, const int* __restrict__ iperm, int N,
+                                        size_t total) {
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t i0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < total; i0 += 4 * stride) {
-        C2<Rl> v[4];
+        double2 v[4];
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             const size_t i = i0 + u * stride;
             if (i < total) {
                 const size_t row = i / N;
-                v[u] = src[row * N + iperm[(int)(i - row * N)]];
+                const size_t pos = row * N + iperm[(int)(i - row * N)];
+                const C2<Rl> h = src[pos];
+                v[u] = make_double2((double)h.x, (double)h.y);
+                if (lo) {   // high + low parts, exact in FP64
+                    const C2<Rl> l = lo[pos];
+                    v[u].x += (double)l.x;
+                    v[u].y += (double)l.y;
+                }
             }
         }
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             const size_t i = i0 + u * stride;
-            if (i < total) dst[i] = make_double2((double)v[u].x, (double)v[u].y);
+            if (i < total) dst[i] = v[u];
         }
     }
 }
@@ -652,12 +663,13 @@ cudaError_t launch_permute(int dir, const void* src, void* dst, const int* perm,
 
 template <typename Rl>
 cudaError_t launch_permute_host(int dir, const void* src, void* dst, const int* iperm, int N, size_t total, int sms,
-                                cudaStream_t st, long long* nlaunch) {
+                                cudaStream_t st, long long* nlaunch, void* lo) {
     const unsigned g = (unsigned)(sms > 0 ? 8 * sms : 1024);
     if (dir > 0)
-        permute_in_host_kernel<Rl><<<g, 256, 0, st>>>((const double2*)src, (C2<Rl>*)dst, iperm, N, total);
+        permute_in_host_kernel<Rl><<<g, 256, 0, st>>>((const double2*)src, (C2<Rl>*)dst, (C2<Rl>*)lo, iperm, N, total);
     else
-        permute_out_host_kernel<Rl><<<g, 256, 0, st>>>((const C2<Rl>*)src, (double2*)dst, iperm, N, total);
+        permute_out_host_kernel<Rl><<<g, 256, 0, st>>>((const C2<Rl>*)src, (const C2<Rl>*)lo, (double2*)dst, iperm, N,
+                                                       total);
     (*nlaunch)++;
     return cudaGetLastError();
 }
@@ -673,7 +685,7 @@ cudaError_t launch_permute_host(int dir, const void* src, void* dst, const int* 
     template cudaError_t launch_permute<Rl>(int, const void*, void*, const int*, int, size_t, cudaStream_t,  \
                                             long long*);                                                     \
     template cudaError_t launch_permute_host<Rl>(int, const void*, void*, const int*, int, size_t, int,      \
-                                                 cudaStream_t, long long*);
+                                                 cudaStream_t, long long*, void*);
 GS_INST(double)
 GS_INST(float)
 

@@ -75,11 +75,14 @@ struct TcArgs {
     const int* cmap;
     float* yc;   // non-null: the output goes to this [nr][nc] compact array instead of Y
     int ycompact;   // linear step: Y is the compact [nr][nc] copy of BIGBUFFER2's window columns
-    // linear step on compact columns: double-float factors of this dz and 1 / (1 + s), both
-    // [nr][nc / 2] by compact column pair (null: the factor is evaluated in FP32 per element)
-    const float4* fac;
+    // linear step on BIGBUFFER2's double-float compact copy (Y = its high parts, ylo its low
+    // parts): theta per [pair][row] and k_i per pair as double-float pairs, 1 / (1 + s) per
+    // [pair][row] (0 outside the window and in the padding), dz as a double-float pair
+    const float2* theta;
+    const float2* kiff;
     const float* inv1ps;
-    float* ylo;     // with ycompact and fac: the low parts of Y (BIGBUFFER2's double-float compact copy)
+    float* ylo;
+    float dz_lo;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -699,7 +702,7 @@ __host__ __device__ constexpr float ff_lo(double d) { return (float)(d - (double
 __device__ __forceinline__ void ff_cexp(ff2 x, ff2 y, ff2* re, ff2* im) {
     constexpr double PIO2 = 1.57079632679489661923132169163975144;
     const float k = rintf(y.h * (float)(1.0 / PIO2));
-    const ff2 r = ff_add(y, ff_neg(ff_mul_f(ff2{ff_hi(PIO2), ff_lo(PIO2)}, k)));
+    const ff2 r = k == 0.f ? y : ff_add(y, ff_neg(ff_mul_f(ff2{ff_hi(PIO2), ff_lo(PIO2)}, k)));
     const ff2 r2 = ff_mul(r, r);
     const float u = r2.h;
     // sin r = r + r^3 (-1/6 + u/120 + u^2 Ts(u)),  cos r = 1 - u/2 + u^2 (1/24 - u/720 + u^2 Tc(u))
@@ -720,6 +723,11 @@ __device__ __forceinline__ void ff_cexp(ff2 x, ff2 y, ff2* re, ff2* im) {
     if (q == 1) { c = ff_neg(sn); sv = cs; }
     else if (q == 2) { c = ff_neg(cs); sv = ff_neg(sn); }
     else if (q == 3) { c = sn; sv = ff_neg(cs); }
+    if (x.h == 0.f && x.l == 0.f) {   // no absorption (k_i = 0 inside the medium's window)
+        *re = c;
+        *im = sv;
+        return;
+    }
     ff2 a;
     if (fabsf(x.h) < 0.015625f) {   // 1 + x + x^2/2 + x^3 (1/6 + x/24 + ...)
         const float t3 = x.h * x.h * x.h * (1.0f / 6 + x.h * (1.0f / 24 + x.h * (1.0f / 120 + x.h * (1.0f / 720))));
@@ -729,23 +737,6 @@ __device__ __forceinline__ void ff_cexp(ff2 x, ff2 y, ff2* re, ff2* im) {
     }
     *re = ff_mul(a, c);
     *im = ff_mul(a, sv);
-}
-
-// The linear step's factors for one dz over the spectral window's compact columns:
-// fac[i][c/2] = (P_hi, P_lo), P = exp(dz (k_i + i theta(i, p))) of calculate_Lstep
-// (propagator.cu:614-616) with theta(i, p) = -HO(p) - sqrtHO(-kt2_i / k_r^2) k_r(p) tabulated
-// in FP64 at set-up as a double-float pair; elements outside the window are left unused.
-__global__ void qdht_factor_kernel(const float2* __restrict__ theta, const float2* __restrict__ kiff,
-                                   float4* __restrict__ fac, int nr, int npair, float dz_h, float dz_l) {
-    const size_t total = (size_t)nr * npair;
-    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
-        const int c2 = (int)(idx % npair);
-        const float2 t = theta[idx], kk = kiff[c2];
-        const ff2 dz{dz_h, dz_l};
-        ff2 re, im;
-        ff_cexp(ff_mul(dz, ff2{kk.x, kk.y}), ff_mul(dz, ff2{t.x, t.y}), &re, &im);
-        fac[idx] = make_float4(re.h, im.h, re.l, im.l);
-    }
 }
 
 // 32 accumulator columns of row i starting at output column cg: a plain store or the fused
@@ -786,42 +777,62 @@ __device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, 
             *reinterpret_cast<float4*>(yrow + k) = make_float4(v[k], v[k + 1], v[k + 2], v[k + 3]);
         return;
     }
-    if (a.fac) {   // compact columns with the double-float factor table of this dz
-        const size_t t0 = (size_t)i * (a.nc >> 1) + (cg >> 1);
+    if (a.ylo) {
+        // BIGBUFFER2's compact copy as double-float pairs, (B2 + dz N / (1 + s)) P with ~48
+        // significant bits, so that factors within 2^-24 of 1 (small k_t near omega0, where the
+        // step's phase is tiny) still turn the state instead of being lost to FP32 rounding.
+        // P = exp(dz (k_i + i theta)) is formed here in double-float arithmetic from the FP64
+        // theta table (ff_cexp); outside the window and in the padding (1 / (1 + s) = 0) P = 1, so
+        // every element is handled alike and those stay unchanged.  The tables are [pair][row] (a
+        // warp's lanes are consecutive rows: coalesced); the loads of four positions are issued
+        // before their arithmetic.
+        const size_t nr = (size_t)a.nr;
+        const size_t t0 = (size_t)(cg >> 1) * nr + i;
+        const ff2 dz{a.dz, a.dz_lo};
+        float* yh = a.Y + (size_t)i * a.nc + cg;
+        float* yl = a.ylo + (size_t)i * a.nc + cg;
 #pragma unroll
-        for (int e = 0; e < 16; e++) {
-            const int rc = a.cmap[cg + 2 * e];
-            if (rc < 0) continue;               // padding
-            if (i > a.kmax[rc >> 1]) continue;  // outside the window: BIGBUFFER2 untouched
-            float2* y2 = reinterpret_cast<float2*>(a.ycompact ? a.Y + (size_t)i * a.nc + cg + 2 * e
-                                                              : a.Y + (size_t)i * a.ncols + rc);
-            const float inv = a.inv1ps[t0 + e];
-            const float4 P = a.fac[t0 + e];   // (P_hi re, im, P_lo re, im)
-            if (a.ylo) {
-                // BIGBUFFER2 carried as a double-float pair: (B2 + dz N / (1 + s)) P with ~48
-                // significant bits, so that factors within 2^-24 of 1 (small k_t near omega0,
-                // where the step's phase is tiny) still turn the state instead of being lost to
-                // FP32 rounding
-                float2* y2l = reinterpret_cast<float2*>(a.ylo + (size_t)i * a.nc + cg + 2 * e);
-                const float2 bh = *y2, bl = *y2l;
-                const ff2 br = ff_add(ff2{bh.x, bl.x}, ff2{a.dz * v[2 * e] * inv, 0.f});
-                const ff2 bi = ff_add(ff2{bh.y, bl.y}, ff2{a.dz * v[2 * e + 1] * inv, 0.f});
-                const ff2 pr{P.x, P.z}, pi{P.y, P.w};
+        for (int e0 = 0; e0 < 16; e0 += 4) {
+            float2 th[4], kk[4];
+            float inv[4];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                th[u] = a.theta[t0 + (size_t)(e0 + u) * nr];
+                inv[u] = a.inv1ps[t0 + (size_t)(e0 + u) * nr];
+                kk[u] = a.kiff[(cg >> 1) + e0 + u];
+            }
+            const float4 h0 = *reinterpret_cast<const float4*>(yh + 2 * e0);
+            const float4 h1 = *reinterpret_cast<const float4*>(yh + 2 * e0 + 4);
+            const float4 l0 = *reinterpret_cast<const float4*>(yl + 2 * e0);
+            const float4 l1 = *reinterpret_cast<const float4*>(yl + 2 * e0 + 4);
+            const float bh[8] = {h0.x, h0.y, h0.z, h0.w, h1.x, h1.y, h1.z, h1.w};
+            const float bl[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
+            float oh[8], ol[8];
+#pragma unroll
+            for (int u = 0; u < 4; u++) {
+                const int e = e0 + u;
+                if (inv[u] == 0.f) {   // P = 1, nothing added: the pair stays as it is
+                    oh[2 * u] = bh[2 * u];
+                    oh[2 * u + 1] = bh[2 * u + 1];
+                    ol[2 * u] = bl[2 * u];
+                    ol[2 * u + 1] = bl[2 * u + 1];
+                    continue;
+                }
+                ff2 pr, pi;
+                ff_cexp(ff_mul(dz, ff2{kk[u].x, kk[u].y}), ff_mul(dz, ff2{th[u].x, th[u].y}), &pr, &pi);
+                const ff2 br = ff_add(ff2{bh[2 * u], bl[2 * u]}, ff2{a.dz * v[2 * e] * inv[u], 0.f});
+                const ff2 bi = ff_add(ff2{bh[2 * u + 1], bl[2 * u + 1]}, ff2{a.dz * v[2 * e + 1] * inv[u], 0.f});
                 const ff2 fr = ff_add(ff_mul(br, pr), ff_neg(ff_mul(bi, pi)));
                 const ff2 fi = ff_add(ff_mul(br, pi), ff_mul(bi, pr));
-                *y2 = make_float2(fr.h, fi.h);
-                *y2l = make_float2(fr.l, fi.l);
-                continue;
+                oh[2 * u] = fr.h;
+                oh[2 * u + 1] = fi.h;
+                ol[2 * u] = fr.l;
+                ol[2 * u + 1] = fi.l;
             }
-            float2 b2 = *y2;
-            b2.x += a.dz * v[2 * e] * inv;
-            b2.y += a.dz * v[2 * e + 1] * inv;
-            // b2 (P_hi + P_lo): the low part's product first, then the two high-part FMAs
-            const float lr = b2.x * P.z - b2.y * P.w, li = b2.x * P.w + b2.y * P.z;
-            float2 f;
-            f.x = fmaf(b2.x, P.x, fmaf(-b2.y, P.y, lr));
-            f.y = fmaf(b2.x, P.y, fmaf(b2.y, P.x, li));
-            *y2 = f;
+            *reinterpret_cast<float4*>(yh + 2 * e0) = make_float4(oh[0], oh[1], oh[2], oh[3]);
+            *reinterpret_cast<float4*>(yh + 2 * e0 + 4) = make_float4(oh[4], oh[5], oh[6], oh[7]);
+            *reinterpret_cast<float4*>(yl + 2 * e0) = make_float4(ol[0], ol[1], ol[2], ol[3]);
+            *reinterpret_cast<float4*>(yl + 2 * e0 + 4) = make_float4(ol[4], ol[5], ol[6], ol[7]);
         }
         return;
     }
@@ -935,6 +946,39 @@ __global__ void qdht_spec_ff_kernel(double2* __restrict__ X, float* __restrict__
             v.y += (double)l.y;
             *x = v;
         }
+    }
+}
+
+// The compact double-float copy from device arrays in position order, S (high parts) and lo
+// (low parts), both [nr][ncols] floats: take (dir > 0) sets sc, sl at the window's pairs (zeros
+// in the padding); scatter (dir < 0) writes lo over all of [nr][ncols]: sl at the window's pairs,
+// zeros elsewhere (cinv[p]: the compact column of position p, or -1).
+__global__ void qdht_spec_dev_kernel(const float* __restrict__ S, float* __restrict__ lo, float* __restrict__ sc,
+                                     float* __restrict__ sl, int nr, int ncols, int nc, const int* __restrict__ cmap,
+                                     const int* __restrict__ cinv, int dir) {
+    if (dir > 0) {
+        const size_t total = (size_t)nr * (nc / 2);
+        for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+            const size_t i = idx / (nc / 2);
+            const int c = 2 * (int)(idx - i * (nc / 2));
+            const int rc = cmap[c];
+            float2 h = make_float2(0.f, 0.f), l = make_float2(0.f, 0.f);
+            if (rc >= 0) {
+                h = *reinterpret_cast<const float2*>(S + i * ncols + rc);
+                l = *reinterpret_cast<const float2*>(lo + i * ncols + rc);
+            }
+            *reinterpret_cast<float2*>(sc + i * nc + c) = h;
+            *reinterpret_cast<float2*>(sl + i * nc + c) = l;
+        }
+        return;
+    }
+    const size_t total = (size_t)nr * (ncols / 2);
+    for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+        const size_t i = idx / (ncols / 2);
+        const int p = (int)(idx - i * (ncols / 2));
+        const int c = cinv[p];
+        *reinterpret_cast<float2*>(lo + i * ncols + 2 * p) =
+            c >= 0 ? *reinterpret_cast<const float2*>(sl + i * nc + c) : make_float2(0.f, 0.f);
     }
 }
 
@@ -1176,14 +1220,11 @@ struct QdhtTc {
     float* xc = nullptr;      // [n_r][nc_act]: a compact linear-step input written by its producer
     float* sc = nullptr;      // [n_r][nc_act]: BIGBUFFER2's window columns kept compact between steps
     float* sl = nullptr;      // [n_r][nc_act]: their low parts (the compact copy is the double-float sc + sl)
-    // the linear step's factors on the compact columns, per pair c / 2 of row i ([n_r][nc_act / 2]):
-    // theta = -HO - sqrtHO(-kt2 / k_r^2) k_r and k_i (per pair) as double-float pairs, 1 / (1 + s),
-    // and exp(dz (k_i + i theta)) as (hi, lo) for the dz in fac_dz (NaN: not built)
+    // the linear step's factors on the compact columns, per pair c / 2 and row i ([nc_act / 2][n_r]):
+    // theta = -HO - sqrtHO(-kt2 / k_r^2) k_r and k_i (per pair) as double-float pairs, 1 / (1 + s)
     float2* theta = nullptr;
     float2* kiff = nullptr;
     float* inv1ps = nullptr;
-    float4* fac = nullptr;
-    double fac_dz = NAN;
     CUtensorMap map_bh, map_bl, map_hi64, map_lo64;   // 32-half boxes in the 64-byte swizzle
     // tensor maps of the X operands seen so far (the handle's few state arrays)
     std::vector<std::pair<const float*, CUtensorMap>> xmaps;
@@ -1430,8 +1471,10 @@ int qdht_tc_set_lstep(QdhtTc* q, const double* omega, const double* wavenum, con
             if (msg) *msg = "window column list upload failed";
             return 1;
         }
-        // theta and 1 / (1 + s) per row and compact pair in FP64 (calculate_Lstep,
-        // propagator.cu:614-616, with the reference's 20-term sqrtHO, extmath.h:245-256)
+        // theta and 1 / (1 + s) per compact pair and row ([pair][row]: the epilogue's lanes are rows)
+        // in FP64 (calculate_Lstep, propagator.cu:614-616, with the reference's 20-term sqrtHO,
+        // extmath.h:245-256); 1 / (1 + s) = 0 marks elements outside the window and padding, whose
+        // factor is exactly 1 so that the linear step leaves them unchanged
         double hk[20], bc = 1.0;
         for (int n = 1; n <= 20; n++) { bc *= (0.5 - (n - 1)) / n; hk[n - 1] = bc; }
         const size_t npair = cm.size() / 2;
@@ -1448,25 +1491,21 @@ int qdht_tc_set_lstep(QdhtTc* q, const double* omega, const double* wavenum, con
                 double sq = 0, xn = x;
                 for (int j = 0; j < 20; j++) { sq += hk[j] * xn; xn *= x; }
                 const double t = -ho[pp] - sq * k1;
-                th[(size_t)i * npair + c2] = make_float2((float)t, (float)(t - (double)(float)t));
-                iv[(size_t)i * npair + c2] = (float)(1.0 / (1.0 + sq));
+                th[c2 * (size_t)nr + i] = make_float2((float)t, (float)(t - (double)(float)t));
+                iv[c2 * (size_t)nr + i] = (float)(1.0 / (1.0 + sq));
             }
         }
         if (q->theta) cudaFree(q->theta);
         if (q->kiff) cudaFree(q->kiff);
         if (q->inv1ps) cudaFree(q->inv1ps);
-        if (q->fac) cudaFree(q->fac);
         q->theta = nullptr;
         q->kiff = nullptr;
         q->inv1ps = nullptr;
-        q->fac = nullptr;
-        q->fac_dz = NAN;
         if (npair > 0) {
             const size_t ne = (size_t)nr * npair;
             const bool okf = cudaMalloc(&q->theta, ne * sizeof(float2)) == cudaSuccess &&
                              cudaMalloc(&q->kiff, npair * sizeof(float2)) == cudaSuccess &&
                              cudaMalloc(&q->inv1ps, ne * sizeof(float)) == cudaSuccess &&
-                             cudaMalloc(&q->fac, ne * sizeof(float4)) == cudaSuccess &&
                              cudaMemcpy(q->theta, th.data(), ne * sizeof(float2), cudaMemcpyHostToDevice) == cudaSuccess &&
                              cudaMemcpy(q->kiff, kf.data(), npair * sizeof(float2), cudaMemcpyHostToDevice) == cudaSuccess &&
                              cudaMemcpy(q->inv1ps, iv.data(), ne * sizeof(float), cudaMemcpyHostToDevice) == cudaSuccess;
@@ -1505,9 +1544,11 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
     a.cmap = nullptr;
     a.yc = nullptr;
     a.ycompact = 0;
-    a.fac = nullptr;
+    a.theta = nullptr;
+    a.kiff = nullptr;
     a.inv1ps = nullptr;
     a.ylo = nullptr;
+    a.dz_lo = (float)(L.dz - (double)(float)L.dz);
     if (q->wide) {
         // The linear step leaves BIGBUFFER2 untouched outside the spectral window and the masked
         // inverse transforms a zero column there: both run on the window's columns only (the
@@ -1532,31 +1573,18 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
         if (mode == QDHT_LSTEP && (flags & QTC_X_COMPACT)) xsrc = q->xc;
         if (mode == QDHT_MASKED && s_comp) xsrc = q->sc;
         const bool xc = xsrc != nullptr;
-        if (mode == QDHT_LSTEP && s_comp) {   // the epilogue updates the compact copy
+        if (mode == QDHT_LSTEP && s_comp) {   // the epilogue updates the compact double-float copy
             Y = q->sc;
             a.Y = q->sc;
-            a.ylo = q->sl;
             a.ycompact = 1;
-        }
-        if (mode == QDHT_LSTEP && q->fac) {
-            // the double-float factors of this dz: rebuilt when dz changes, and always recorded
-            // into a graph under capture (a replay must not depend on the table's last dz)
-            cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-            cudaError_t ce = cudaStreamIsCapturing(q->st, &cs);
-            if (ce != cudaSuccess) return ce;
-            const bool capturing = cs != cudaStreamCaptureStatusNone;
-            if (capturing || !(L.dz == q->fac_dz)) {
-                const int npair = a.nc / 2;
-                const size_t total = (size_t)q->nr * npair;
-                const unsigned gf = (unsigned)std::min<size_t>((total + 255) / 256, (size_t)q->sms * 8);
-                const float dzh = (float)L.dz, dzl = (float)(L.dz - (double)dzh);
-                tc::qdht_factor_kernel<<<gf, 256, 0, q->st>>>(q->theta, q->kiff, q->fac, q->nr, npair, dzh, dzl);
-                (*nlaunch)++;
-                q->fac_dz = capturing ? NAN : L.dz;
+            if (q->theta) {
+                a.ylo = q->sl;
+                a.theta = q->theta;
+                a.kiff = q->kiff;
+                a.inv1ps = q->inv1ps;
             }
-            a.fac = q->fac;
-            a.inv1ps = q->inv1ps;
         }
+
         // split X into the K-major FP16 hi / lo operands and the column scales (the window mask
         // of the inverse applied), then the GEMM on 128 x 256 tiles
         tc::qdht_split16_kernel<<<(unsigned)(a.nc / tc::SPLIT_COLS), tc::SPLIT_THREADS, (size_t)(q->nr / 2) * 33 * 4,
@@ -1629,6 +1657,15 @@ cudaError_t qdht_tc_spec_ff(QdhtTc* q, double* X, const int* perm, int take, lon
     return cudaGetLastError();
 }
 
+cudaError_t qdht_tc_spec_dev(QdhtTc* q, float* S, float* lo, int take, long long* nlaunch) {
+    if (!qdht_tc_has_compact(q)) return cudaErrorInvalidValue;
+    const size_t tot = take ? (size_t)q->nr * (q->nc_act / 2) : (size_t)q->nr * q->nt;
+    tc::qdht_spec_dev_kernel<<<(unsigned)std::min<size_t>((tot + 255) / 256, (size_t)q->sms * 16), 256, 0, q->st>>>(
+        S, lo, q->sc, q->sl, q->nr, 2 * q->nt, q->nc_act, q->cmap, q->cinv, take ? 1 : -1);
+    (*nlaunch)++;
+    return cudaGetLastError();
+}
+
 const float* qdht_tc_compact_y(QdhtTc* q, int* nc, const int** cmap) {
     if (!q || !q->wide || !q->yc) return nullptr;
     if (nc) *nc = q->nc_act;
@@ -1669,7 +1706,7 @@ int qdht_tc_check(QdhtTc* q, std::string* msg) {
 void qdht_tc_destroy(QdhtTc* q) {
     if (!q) return;
     void* ptrs[] = {q->hh, q->hl, q->kr, q->ki, q->ho, q->kt2, q->kmax, q->err, q->xhT, q->xlT, q->hh16, q->hl16, q->hs, q->xs,
-                    q->cmap, q->zpos, q->cinv, q->yc, q->xc, q->sc, q->sl, q->theta, q->kiff, q->inv1ps, q->fac};
+                    q->cmap, q->zpos, q->cinv, q->yc, q->xc, q->sc, q->sl, q->theta, q->kiff, q->inv1ps};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete q;

@@ -43,6 +43,10 @@ cudaError_t qdht_tc_spec_copy(QdhtTc* q, float* S, int to_compact, long long* nl
 // X's window pairs into high and low parts; take == 0 adds the low parts into X, which must
 // already hold the high parts there.
 cudaError_t qdht_tc_spec_ff(QdhtTc* q, double* X, const int* perm, int take, long long* nlaunch);
+// The same from / into device arrays in position order: S (high parts) and lo (low parts), both
+// [n_r][2 n_t] floats; take != 0 sets the compact copy from them, take == 0 writes lo over the
+// whole array (the compact low parts at the window's pairs, zeros elsewhere).
+cudaError_t qdht_tc_spec_dev(QdhtTc* q, float* S, float* lo, int take, long long* nlaunch);
 // The compact [n_r][nc] input array of the linear-step transform and its position map (cinv[p]:
 // the column of position p's (re, im) pair, or -1 outside the spectral window); null when the
 // plan has no window columns (set_lstep not called, or a width outside the wide-tile path).
