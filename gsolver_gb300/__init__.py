@@ -41,6 +41,7 @@ ABI_FUNCTIONS = (
     "gs_batch_create", "gs_batch_step", "gs_batch_stream", "gs_batch_launch_count", "gs_batch_last_error",
     "gs_batch_destroy", "gs_autotune", "gs_set_nl_threads", "gs_get_nl_threads", "gs_batch_autotune",
     "gs_set_apertures", "gs_setup_apertures", "gs_setup_from_config_dev",
+    "gs_energy", "gs_set_energy_tolerance", "gs_energy_stats", "gs_checkpoint_save", "gs_checkpoint_load",
 )
 
 
@@ -134,6 +135,11 @@ def load_library(path: str | None = None):
     L.gs_batch_autotune.argtypes = [V, V, PD, PD, C.POINTER(C.c_int)]
     L.gs_set_apertures.argtypes = [V, I, V, V, V, D]
     L.gs_setup_apertures.argtypes = [V, C.POINTER(C.c_int), V, V]
+    L.gs_energy.argtypes = [V, V, D, PD, PD]
+    L.gs_set_energy_tolerance.argtypes = [V, D, V, D]
+    L.gs_energy_stats.argtypes = [V, PD, C.POINTER(C.c_longlong)]
+    L.gs_checkpoint_save.argtypes = [V, C.c_char_p, D, D, I, C.c_uint]
+    L.gs_checkpoint_load.argtypes = [V, C.c_char_p, PD, PD, C.POINTER(C.c_int), C.POINTER(C.c_uint)]
     _lib = L
     return L
 
@@ -296,6 +302,36 @@ class Propagator:
         r = np.ascontiguousarray(r, dtype=np.float64)
         x = np.ascontiguousarray(qdht_x, dtype=np.float64)
         self._check(self.L.gs_set_apertures(self.h, len(z), _ptr(z), _ptr(r), _ptr(x), float(r_max)))
+
+    def energy(self, qdht_x, r_max):
+        """(energy, photon number) of FIELD: the sum of the average spectrum and of it over omega
+        (gs_energy, FP64 on the device)."""
+        x = np.ascontiguousarray(qdht_x, dtype=np.float64)
+        e, n = C.c_double(), C.c_double()
+        self._check(self.L.gs_energy(self.h, _ptr(x), float(r_max), C.byref(e), C.byref(n)))
+        return e.value, n.value
+
+    def set_energy_tolerance(self, tol, qdht_x=None, r_max=0.0):
+        """The photon-number check of step() (gs_set_energy_tolerance); 0 turns it off."""
+        x = np.ascontiguousarray(qdht_x, dtype=np.float64) if qdht_x is not None else None
+        self._check(self.L.gs_set_energy_tolerance(self.h, float(tol), _ptr(x), float(r_max)))
+
+    def energy_stats(self):
+        """(|N1/N0 - 1| of the last accepted step, rejections so far)."""
+        r, k = C.c_double(), C.c_longlong()
+        self._check(self.L.gs_energy_stats(self.h, C.byref(r), C.byref(k)))
+        return r.value, k.value
+
+    def checkpoint_save(self, path, current_z=0.0, zstep=0.0, n_z=0, step_n=0):
+        self._check(self.L.gs_checkpoint_save(self.h, str(path).encode(), float(current_z), float(zstep), int(n_z),
+                                              int(step_n)))
+
+    def checkpoint_load(self, path):
+        """Restore a saved state; returns the z-loop state {z, zstep, n_z, step_n}."""
+        z, dz, nz, sn = C.c_double(), C.c_double(), C.c_int(), C.c_uint()
+        self._check(self.L.gs_checkpoint_load(self.h, str(path).encode(), C.byref(z), C.byref(dz), C.byref(nz),
+                                              C.byref(sn)))
+        return {"z": z.value, "zstep": dz.value, "n_z": nz.value, "step_n": sn.value}
 
     def nl_threads(self, threads=None):
         """Read, or set (0: default), the fused kernels' threads per row."""

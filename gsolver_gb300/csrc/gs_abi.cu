@@ -99,7 +99,7 @@ static void free_all(gs_handle* h) {
     void* ptrs[] = {h->A, h->S, h->NB, h->KP, h->E, h->U, h->tw, h->pf, h->rm, h->kerr, h->rate,
                     h->omega, h->ho, h->kt2, h->Cm, h->m1, h->wavenum, h->staging, h->perm_dev,
                     h->iperm_dev, h->err_dev, h->max_dev, h->dump_dev, h->m1inv, h->adj, h->adj_w, h->th, h->twb,
-                    h->row_ion, h->win64, h->zpos64};
+                    h->row_ion, h->win64, h->zpos64, h->en_dev, h->en_save};
     for (void* q : ptrs) if (q) cudaFree(q);
     if (h->tc) gs::qdht_tc_destroy(h->tc);
     if (h->tcT) gs::qdht_tc_destroy(h->tcT);
@@ -577,6 +577,7 @@ int gs_set_field(gs_handle* h, const double* field, const double* spec) {
     if (rc) return rc;
     CK(h, cudaStreamSynchronize(h->st));
     h->field_ok = true;
+    h->en_prev = 0;
     return GS_OK;
 }
 
@@ -933,8 +934,13 @@ int gs_step(gs_handle* h, double current_z, double znet_cur, double znet_prev, d
         if (max_a2_out) *max_a2_out = max_a2;
         if (max_nl2_out) *max_nl2_out = max_nl2;
         if (!repeat) {
-            *zstep_inout = zstep;
-            rc = lstep(h, zstep);
+            if (h->en_tol > 0) {   // the optional photon-number check (gs_set_energy_tolerance)
+                rc = gsi::lstep_checked(h, &zstep, 1e-10 * (znet_cur - znet_prev));
+                *zstep_inout = zstep;
+            } else {
+                *zstep_inout = zstep;
+                rc = lstep(h, zstep);
+            }
             if (rc) return rc;
             // apertures (propagator.cu:232-261), with CURRENT_Z the z before this step
             if (!h->ap_z.empty() && current_z >= h->ap_z.back()) {
@@ -946,6 +952,7 @@ int gs_step(gs_handle* h, double current_z, double znet_cur, double znet_prev, d
                                           (size_t)(h->nr - k0) * h->nt * h->esz, h->st));
                 rc = run_qdht(h, QDHT_PLAIN, h->A, h->S, 0.0);
                 if (rc) return rc;
+                h->en_prev = 0;   // the photon number of the field the aperture left is taken anew
                 h->ap_z.pop_back();
                 h->ap_row0.pop_back();
             }

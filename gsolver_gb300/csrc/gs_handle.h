@@ -80,6 +80,17 @@ struct gs_handle {
     size_t adj_bytes = 0;
     double* adj_w = nullptr;                   // objective weights (position order) + partial sums
     size_t adj_w_bytes = 0;
+    // energy / photon number (gs_state.cu): radial weights of the average spectrum, the reduction's
+    // partial sums, the optional photon-number check of gs_step and its state
+    double* en_dev = nullptr;                  // [n_r] weights, then partial sums and the two results
+    double en_scale = 0;                       // R_MAX^2 / 2
+    bool en_weights = false;
+    double en_tol = 0;                         // 0: no check (the reference's controller alone)
+    double en_prev = 0;                        // photon number of FIELD after the last accepted step (0: unknown)
+    double en_last = 0;                        // |N1 / N0 - 1| of the last accepted step
+    long long en_rejects = 0;
+    void* en_save = nullptr;                   // BIGBUFFER2 before the linear step, for a rejected one
+    size_t en_save_bytes = 0;
 };
 
 namespace gsi {
@@ -111,6 +122,9 @@ template <typename Rl> gs::PlasmaArgs<Rl> plasma_args(gs_handle* h, bool raman, 
 bool raman_scan_on(const gs_handle* h);
 // position -> omega index of the device FFT of rows N = P M (M = 2^logM per CTA)
 std::vector<int> position_map(int N, int P, int M, int logM);
+// the linear step with the photon-number check of gs_set_energy_tolerance (gs_state.cu): repeated
+// with half the step while |N1 / N0 - 1| exceeds the tolerance; dz_inout the step taken
+int lstep_checked(gs_handle* h, double* dz_inout, double dz_min);
 }  // namespace gsi
 
 #define CK(h, expr)                                                    \

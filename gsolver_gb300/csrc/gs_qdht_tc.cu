@@ -1666,6 +1666,13 @@ cudaError_t qdht_tc_spec_dev(QdhtTc* q, float* S, float* lo, int take, long long
     return cudaGetLastError();
 }
 
+void qdht_tc_spec_pairs(QdhtTc* q, float** sc, float** sl, int* nc) {
+    const bool has = qdht_tc_has_compact(q);
+    if (sc) *sc = has ? q->sc : nullptr;
+    if (sl) *sl = has ? q->sl : nullptr;
+    if (nc) *nc = has ? q->nc_act : 0;
+}
+
 const float* qdht_tc_compact_y(QdhtTc* q, int* nc, const int** cmap) {
     if (!q || !q->wide || !q->yc) return nullptr;
     if (nc) *nc = q->nc_act;

@@ -47,6 +47,9 @@ cudaError_t qdht_tc_spec_ff(QdhtTc* q, double* X, const int* perm, int take, lon
 // [n_r][2 n_t] floats; take != 0 sets the compact copy from them, take == 0 writes lo over the
 // whole array (the compact low parts at the window's pairs, zeros elsewhere).
 cudaError_t qdht_tc_spec_dev(QdhtTc* q, float* S, float* lo, int take, long long* nlaunch);
+// BIGBUFFER2's compact double-float copy itself: high and low parts, each [n_r][nc] floats
+// (null when the plan keeps none)
+void qdht_tc_spec_pairs(QdhtTc* q, float** sc, float** sl, int* nc);
 // The compact [n_r][nc] input array of the linear-step transform and its position map (cinv[p]:
 // the column of position p's (re, im) pair, or -1 outside the spectral window); null when the
 // plan has no window columns (set_lstep not called, or a width outside the wide-tile path).

@@ -24,6 +24,9 @@
  *   gs_step                       <- propagator() (solver.h:269, propagator.cu:125-266)
  *   gs_destroy                    <- destroy_variables()/cuda_free_const()
  *                                    (solver_main.cpp:415-440)
+ *   gs_energy                     <- dump_type_average_spectrum_class (dump_types.cpp:427-457)
+ *   gs_checkpoint_save / _load    <- dump_type_full_class (dump_types.cpp:77-97) and the
+ *                                    DUMP_FINAL_FIELD restart (solver_main.cpp:226-229)
  */
 #ifndef GS_ABI_H
 #define GS_ABI_H
@@ -249,6 +252,32 @@ int gs_plasma_max_noalloc(const gs_params* params, const double* rate_ln_dev, co
 size_t gs_noalloc_max_samples(void);
 /* Message of the last failed gs_plasma_max_noalloc call. */
 const char* gs_noalloc_last_error(void);
+
+/* Energy and photon number of FIELD, FP64 reductions on the device: energy is the sum over
+ * omega of the reference's average spectrum (dump_type_average_spectrum_class,
+ * dump_types.cpp:427-457: R_MAX^2/2 sum_r w_r |FIELD(r, omega)|^2, w_0 = x_0 (x_1 - x_0),
+ * w_r = x_r (x_r - x_{r-1}), x the QDHT points qdht_x[n_r]); photons weights each omega > 0 by
+ * 1 / omega.  Units are the reference's scaled field units.  Either output may be NULL. */
+int gs_energy(gs_handle* h, const double* qdht_x, double r_max, double* energy, double* photons);
+/* Optional photon-number check of gs_step (no counterpart in the reference, whose controller is
+ * the max-ratio rule of propagator.cu:147-150; 0, the default, keeps it that way): after each
+ * accepted attempt's linear step, while |N_after / N_before - 1| > tol (N the photon number of
+ * gs_energy) BIGBUFFER2 is restored and the linear step repeated with half the step (the NL
+ * increment, taken with the previous step size as propagator() does, is reused); the step taken
+ * is returned in zstep_inout.  A step below 1e-10 of the ZNET interval fails with
+ * GS_ERR_COLLAPSE.  Plasma absorption and the absorbing layer remove photons; Kerr, Raman and
+ * dispersion conserve them, so the check bounds the loss per step. */
+int gs_set_energy_tolerance(gs_handle* h, double tol, const double* qdht_x, double r_max);
+/* |N_after / N_before - 1| of the last step accepted by the check, and the rejections so far. */
+int gs_energy_stats(const gs_handle* h, double* last_rel_change, long long* rejections);
+
+/* Checkpoints of a handle's state (the reference restarts from its full-field dump,
+ * dump_type_full_class, dump_types.cpp:77-97, and DUMP_FINAL_FIELD, solver_main.cpp:226-229):
+ * FIELD, BIGBUFFER2 (with the mixed plan's double-float window columns) as stored on the device,
+ * and the z-loop's CURRENT_Z, ZSTEP, n_Z and STEP_N, in a binary file.  Loading into a handle of
+ * the same grid, precision and tables continues exactly where the saved one was. */
+int gs_checkpoint_save(gs_handle* h, const char* path, double current_z, double zstep, int n_z, unsigned step_n);
+int gs_checkpoint_load(gs_handle* h, const char* path, double* current_z, double* zstep, int* n_z, unsigned* step_n);
 
 /* Apertures (propagator.cu:232-261, process_input.cpp:176-179): n entries in the reference's
  * array order (z[n-1], r[n-1] is the first applied).  gs_step then applies them as
