@@ -42,6 +42,7 @@ ABI_FUNCTIONS = (
     "gs_batch_destroy", "gs_autotune", "gs_set_nl_threads", "gs_get_nl_threads", "gs_batch_autotune",
     "gs_set_apertures", "gs_setup_apertures", "gs_setup_from_config_dev",
     "gs_energy", "gs_set_energy_tolerance", "gs_energy_stats", "gs_checkpoint_save", "gs_checkpoint_load",
+    "gs_selftest_bounded_wait",
 )
 
 
@@ -136,6 +137,7 @@ def load_library(path: str | None = None):
     L.gs_set_apertures.argtypes = [V, I, V, V, V, D]
     L.gs_setup_apertures.argtypes = [V, C.POINTER(C.c_int), V, V]
     L.gs_energy.argtypes = [V, V, D, PD, PD]
+    L.gs_selftest_bounded_wait.argtypes = [V, D]
     L.gs_set_energy_tolerance.argtypes = [V, D, V, D]
     L.gs_energy_stats.argtypes = [V, PD, C.POINTER(C.c_longlong)]
     L.gs_checkpoint_save.argtypes = [V, C.c_char_p, D, D, I, C.c_uint]
@@ -332,6 +334,11 @@ class Propagator:
         self._check(self.L.gs_checkpoint_load(self.h, str(path).encode(), C.byref(z), C.byref(dz), C.byref(nz),
                                               C.byref(sn)))
         return {"z": z.value, "zstep": dz.value, "n_z": nz.value, "step_n": sn.value}
+
+    def selftest_bounded_wait(self, limit_s=1e-3):
+        """gs_selftest_bounded_wait: raises GsError (GS_ERR_CUDA, 'wait expired') when the bounded
+        waits report as they should."""
+        self._check(self.L.gs_selftest_bounded_wait(self.h, float(limit_s)))
 
     def nl_threads(self, threads=None):
         """Read, or set (0: default), the fused kernels' threads per row."""

@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -122,6 +123,10 @@ int gs_create(const gs_params* prm, gs_handle** out) {
                     "gas build: the third harmonic with Raman needs the Raman oscillator parameters");
     gs_handle* h = new gs_handle();
     h->p = *prm;
+    {
+        const char* ex = std::getenv("GS_TEST_SHOOTING_EXHAUST");
+        h->shoot_exhaust = (ex && ex[0] == '1') ? 1 : 0;
+    }
     h->nr = nr;
     h->nt = nt;
     h->fp64 = prm->precision == GS_PREC_FP64;
@@ -610,6 +615,7 @@ PlasmaArgs<Rl> gsi::plasma_args(gs_handle* h, bool raman, bool raman_scan) {
     pa.ionization_potential = h->p.ionization_potential; pa.ponderomotive = h->p.ponderomotive;
     pa.avalanche_cs = h->p.avalanche_cs; pa.recombination_tau = h->p.recombination_tau;
     pa.raman_scan = raman_scan;
+    pa.shoot_exhaust = h->shoot_exhaust;
     pa.gas = h->p.gas;
     pa.th = (h->p.gas && h->p.th_coeff != 0) ? (const T2*)h->th : nullptr;
     if (raman_scan) {
@@ -960,6 +966,16 @@ int gs_step(gs_handle* h, double current_z, double znet_cur, double znet_prev, d
             return collect_qdht_time(h);
         }
     }
+}
+
+int gs_selftest_bounded_wait(gs_handle* h, double limit_s) {
+    if (!h || !(limit_s > 0) || limit_s > 1.0) return fail(h, GS_ERR_ARG, "gs_selftest_bounded_wait: 0 < limit <= 1 s");
+    if (!h->tc) return fail(h, GS_ERR_UNSUPPORTED, "gs_selftest_bounded_wait: mixed handles only");
+    CK(h, cudaSetDevice(h->p.device));
+    CK(h, gs::qdht_tc_wait_probe(h->tc, limit_s, &h->launches));
+    std::string m;
+    if (gs::qdht_tc_check(h->tc, &m)) return fail(h, GS_ERR_CUDA, m);
+    return GS_OK;
 }
 
 int gs_set_apertures(gs_handle* h, int n, const double* z, const double* r, const double* qdht_x, double r_max) {

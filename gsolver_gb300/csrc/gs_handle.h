@@ -26,6 +26,8 @@ struct gs_handle {
     bool fused = false;        // one-CTA rows: the fused front/back kernels per RK4 stage
     bool pair = false;         // rows over two CTAs (P = 2: FP32 32768, FP64 16384), gs_nl_pair.cu
     int nl_threads = 0;        // fused kernels' threads per row (0: default; gs_autotune sets it)
+    int shoot_exhaust = 0;     // test hook (GS_TEST_SHOOTING_EXHAUST=1 at gs_create): no early stop
+                               // of the carrier-density shooting
     cudaStream_t st = nullptr;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     size_t esz = 16;           // bytes per complex element

@@ -37,6 +37,9 @@ template <typename Rl> struct PlasmaArgs {
     int raman;        // 1: U3 = |E|^2 for the FFT convolution; 0: U3 = |E|^2 E (Raman off)
     int raman_scan;   // 1: U3 = Q E with Q from the one-pole recurrence below
     int density_only; // 1: stop after the recurrence, rho left in U2.x (the plasma dumps)
+    int shoot_exhaust; // test hook: the carrier-density shooting ignores its stopping test and runs
+                       // its full bound of iterations (one more than the chunks), which reproduces
+                       // the sequential recurrence exactly
     double tstep_scaled, neutral_density, rho0, ionization_potential, ponderomotive;
     double avalanche_cs, recombination_tau;
     // Raman oscillator h_k = fRM Im(a^k), a = exp(dt (-1/tau + i Omega)); circular wrap a^N

@@ -219,9 +219,11 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
     if (tid == 0) s_done = 0;
     __syncthreads();
     // stop when the starts move less than tol (relative): Newton converges quadratically, so
-    // the starts then carry ~tol^2 + rounding; far below the parity bars (1e-10 / 1e-5)
+    // the starts then carry ~tol^2 + rounding; far below the parity bars (1e-10 / 1e-5).  After
+    // k iterations the starts of chunks 0..k equal the sequential recurrence's (each computed
+    // from an exact predecessor), so P + 1 iterations bound the loop with an exact result
     const Rl tol = sizeof(Rl) == 8 ? (Rl)1e-13 : (Rl)1e-5;
-    for (int it = 0; it < (ion ? 16 : 0); it++) {
+    for (int it = 0; it < (ion ? P + 1 : 0); it++) {
         Rl A = 1, B = 0, sc = 0;
         if (c < P) {
             sc = s_start[c];
@@ -273,7 +275,7 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
         if (tid == 0) {
             Rl cm = 0, mm = 0;
             for (int w = 0; w < (nthr >> 5); w++) { cm = fmax(cm, red[w]); mm = fmax(mm, red[16 + w]); }
-            s_done = (cm <= tol * mm) ? 1 : 0;
+            s_done = (cm <= tol * mm && !a.shoot_exhaust) ? 1 : 0;
         }
         __syncthreads();
         if (s_done) break;

@@ -336,9 +336,12 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
     if (tid == 0) *flag = 0;
     __syncthreads();
     // relative change of the starts at which Newton stops (quadratic convergence: the
-    // starts then carry ~tol^2 + rounding)
+    // starts then carry ~tol^2 + rounding).  Newton on a forward recurrence also ends in finitely
+    // many steps: after k iterations the starts of chunks 0..k are those of the sequential
+    // recurrence (each computed from an exact predecessor), so nthr + 1 iterations give the
+    // sequential result whatever the stopping test does; typical rows stop after a few
     const Rl tol = sizeof(Rl) == 8 ? (Rl)1e-13 : (Rl)1e-5;
-    for (int it = 0; it < (ion ? 16 : 0); it++) {   // no ionization: the starts stay 0
+    for (int it = 0; it < (ion ? nthr + 1 : 0); it++) {   // no ionization: the starts stay 0
         const Rl sc = s_start[c];
         Rl D;
         const Rl e = run_chunk(sc, &D);
@@ -361,7 +364,7 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
         if (tid == 0) {
             Rl cm = 0, mm = 0;
             for (int w = 0; w < (nthr >> 5); w++) { cm = fmax(cm, rA[w]); mm = fmax(mm, rB[w]); }
-            *flag = (cm <= tol * mm) ? 1 : 0;
+            *flag = (cm <= tol * mm && !a.shoot_exhaust) ? 1 : 0;
         }
         __syncthreads();
         if (*flag) break;

@@ -264,8 +264,10 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape<Rl>::THREA
     // Both CTAs take the same number of iterations (and cluster barriers).
     s_start[c] = (h == 0 && c == 0) ? a.k.rho0 : (Rl)0;
     __syncthreads();
+    // after k iterations the starts of the pair's first k + 1 chunks equal the sequential
+    // recurrence's, so 2 nthr + 1 iterations bound the loop with an exact result
     const Rl tol = sizeof(Rl) == 8 ? (Rl)1e-13 : (Rl)1e-5;
-    for (int it = 0; it < (ion ? 16 : 0); it++) {
+    for (int it = 0; it < (ion ? 2 * nthr + 1 : 0); it++) {
         const int par = it & 1;
         const Rl sc = s_start[c];
         Rl D;
@@ -306,7 +308,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape<Rl>::THREA
         cl.sync();   // both CTAs' maxima are in place: the same decision on both sides
         const Rl cm = fmax(xr[XR_CM + par], xr[XR_PCM + par]);
         const Rl mm = fmax(xr[XR_MM + par], xr[XR_PMM + par]);
-        if (cm <= tol * mm) break;
+        if (cm <= tol * mm && !a.shoot_exhaust) break;
     }
 
     // ---- Raman: z_t = a z_{t-1} + I_t; chunk sums, a scan per CTA, the carry across the seam

@@ -110,16 +110,17 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
     return t;
 }
 
-// wall-clock bounded wait: false when WAIT_NS expired
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) {
+// wall-clock bounded wait: false when limit_ns expired
+__device__ __forceinline__ bool mbar_wait_ns(uint64_t* bar, unsigned parity, unsigned long long limit_ns) {
     if (mbar_try(bar, parity)) return true;
     const unsigned long long t0 = globaltimer_ns();
     for (;;) {
         if (mbar_try(bar, parity)) return true;
-        if (globaltimer_ns() - t0 > WAIT_NS) return false;
+        if (globaltimer_ns() - t0 > limit_ns) return false;
         __nanosleep(64);
     }
 }
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) { return mbar_wait_ns(bar, parity, WAIT_NS); }
 
 // first expired wait of a launch: code | k-block << 8 | warp << 20, kept for the host
 __device__ __forceinline__ void record_stall(unsigned* err, unsigned code, int kb, int warp) {
@@ -982,6 +983,19 @@ __global__ void qdht_spec_dev_kernel(const float* __restrict__ S, float* __restr
     }
 }
 
+// Self-test of the bounded waits: one thread waits on a shared-memory mbarrier that nothing
+// arrives at, with the same helper as the GEMM's waits (limit_ns instead of WAIT_NS), records the
+// expiry in the plan's error words as they do and returns.  No copy is in flight, so returning is
+// safe; the host reads the record through qdht_tc_check, as after a GEMM.
+__global__ void wait_probe_kernel(unsigned* err, unsigned long long limit_ns) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        if (!mbar_wait_ns(&bar, 0, limit_ns)) record_stall(err, 256u, 0, 0);
+    }
+}
+
 // Zeros of the masked inverse outside the spectral window: Y[i][2 p], Y[i][2 p + 1] = 0 for
 // the positions p in zpos[nz] (their whole column of the operand is masked)
 __global__ void qdht_zero_cols_kernel(float* __restrict__ Y, int ncols, int nr, const int* __restrict__ zpos, int nz) {
@@ -1694,6 +1708,14 @@ float* qdht_tc_compact_x(QdhtTc* q, const int** cinv, int* nc) {
     if (cinv) *cinv = q->cinv;
     if (nc) *nc = q->nc_act;
     return q->xc;
+}
+
+cudaError_t qdht_tc_wait_probe(QdhtTc* q, double limit_s, long long* nlaunch) {
+    tc::wait_probe_kernel<<<1, 32, 0, q->st>>>(q->err, (unsigned long long)(limit_s * 1e9));
+    (*nlaunch)++;
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(q->st);
+    return e;
 }
 
 int qdht_tc_check(QdhtTc* q, std::string* msg) {

@@ -21,6 +21,9 @@ int qdht_tc_set_lstep(QdhtTc* q, const double* omega, const double* wavenum, con
                       double omega_min, double omega_max, std::string* msg);
 // Nonzero (with a message) if a kernel recorded an expired wait since the last check.
 int qdht_tc_check(QdhtTc* q, std::string* msg);
+// Self-test of the bounded waits: a kernel waits limit_s on an mbarrier nothing arrives at,
+// records the expiry as the GEMM's waits do and returns (synchronises the plan's stream).
+cudaError_t qdht_tc_wait_probe(QdhtTc* q, double limit_s, long long* nlaunch);
 // Y = QDHT(X) with the given mode (QDHT_PLAIN / QDHT_LSTEP / QDHT_MASKED).  Flags:
 //   QTC_X_COMPACT  linear step: X's spectral-window columns are already in the compact array
 //                  of qdht_tc_compact_x (X itself is not read);

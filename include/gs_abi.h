@@ -279,6 +279,13 @@ int gs_energy_stats(const gs_handle* h, double* last_rel_change, long long* reje
 int gs_checkpoint_save(gs_handle* h, const char* path, double current_z, double zstep, int n_z, unsigned step_n);
 int gs_checkpoint_load(gs_handle* h, const char* path, double* current_z, double* zstep, int* n_z, unsigned* step_n);
 
+/* Self-test of the tensor-core kernels' bounded waits (no counterpart in the reference): a
+ * kernel waits limit_s (at most 1 s) on a barrier that nothing completes, using the same bounded
+ * wait and expiry record as the QDHT GEMM, and returns; the call then reports the record as a
+ * GEMM's expired wait is reported: GS_ERR_CUDA with "wait expired" in gs_last_error.  The handle
+ * stays usable.  Mixed handles only. */
+int gs_selftest_bounded_wait(gs_handle* h, double limit_s);
+
 /* Apertures (propagator.cu:232-261, process_input.cpp:176-179): n entries in the reference's
  * array order (z[n-1], r[n-1] is the first applied).  gs_step then applies them as
  * propagator() does: after an accepted step, when current_z (the z before the step) has
