@@ -181,6 +181,13 @@ cudaError_t launch_nl_stage(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2
 template <typename Rl> bool nl_stage_all_preferred(int N, int threads, int rows);
 // whether the four-stage launch of this shape can read FIELD compactly (SpecArgs::ac)
 template <typename Rl> bool nl_stage_reads_compact(int N, int threads);
+// ---- the four RK4 stages of 16384-point FP32 rows, 1024 threads each (gs_nl_row16k.cu):
+// the four-stage launch of that shape without a stage record
+bool nl_row16k_applies(int N, int threads);
+cudaError_t nl_row16k_setup();
+cudaError_t launch_nl_row16k(FftArgs<float> f, PlasmaArgs<float> a, const float2* A, SpecArgs<float> s, int rows,
+                             int ahead, cudaStream_t st, long long* nl);
+int nl_row16k_resident(int* ctas);   // CTAs resident on the device at once (cudaError_t)
 
 // ---- one RK4 stage over two CTAs per row (gs_nl_pair.cu): rows of N = 2H stored in the
 // P = 2 position order, FP32 N = 32768 / FP64 N = 16384

@@ -38,37 +38,6 @@ template <typename Rl> struct FrontSmem {
 template <typename Rl> __device__ __forceinline__ Rl qdiv(Rl a, Rl b) { return a / b; }
 template <> __device__ __forceinline__ float qdiv<float>(float a, float b) { return __fdividef(a, b); }
 
-// Tensor-memory access of the RK4 sum (four-stage launches of 16384-point FP32 rows): a
-// warp's lane quarter, NC consecutive 32-bit columns per thread; each access waits for itself.
-template <int NC> __device__ __forceinline__ void tm_ld(uint32_t ta, float* v);
-template <> __device__ __forceinline__ void tm_ld<4>(uint32_t ta, float* v) {
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];\n"
-                 "tcgen05.wait::ld.sync.aligned;"
-                 : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3])
-                 : "r"(ta)
-                 : "memory");
-}
-template <> __device__ __forceinline__ void tm_ld<8>(uint32_t ta, float* v) {
-    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];\n"
-                 "tcgen05.wait::ld.sync.aligned;"
-                 : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]), "=f"(v[7])
-                 : "r"(ta)
-                 : "memory");
-}
-template <int NC> __device__ __forceinline__ void tm_st(uint32_t ta, const float* v);
-template <> __device__ __forceinline__ void tm_st<4>(uint32_t ta, const float* v) {
-    asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};\n"
-                 "tcgen05.wait::st.sync.aligned;" ::"r"(ta),
-                 "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3])
-                 : "memory");
-}
-template <> __device__ __forceinline__ void tm_st<8>(uint32_t ta, const float* v) {
-    asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};\n"
-                 "tcgen05.wait::st.sync.aligned;" ::"r"(ta),
-                 "f"(v[0]), "f"(v[1]), "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7])
-                 : "memory");
-}
-
 // the per-stage values of one RK4 stage of a row (the rest comes from the launch's arguments)
 template <typename Rl> struct StageOv {
     Rl cdz;
@@ -79,15 +48,13 @@ template <typename Rl> struct StageOv {
     int* row_ion;
     Rl next_cdz;     // != 0: this stage also leaves the next stage's input (A + next_cdz k) / N in E
     int preloaded;   // E holds this stage's input already
-    uint32_t tmem;   // != 0: the RK4 sum k1 + 2 k2 + 2 k3 lives in tensor memory at this address
 };
 
 // LOGN > 0: rows of exactly 2^LOGN points (the row FFT with compile-time sizes and nothing
 // else inlined); LOGN = 0: any fused row length.  LC = 16: launched with N/16 threads, so each
 // thread's chunk is 16 consecutive samples starting at a multiple of 16 and its shared-memory
 // slots are at constant offsets (pad16(t0 + i) = pad16(t0) + i, pad32(t0 + i) = pad32(t0) + i).
-// TMA: ov.tmem holds the RK4 sum (k of stages 0-2 is never stored).
-template <typename Rl, int LOGN, int LC, bool TMA = false>
+template <typename Rl, int LOGN, int LC>
 __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaArgs<Rl>& a,
                                              const typename Vec2<Rl>::T* __restrict__ A, const SpecArgs<Rl>& sp,
                                              const StageOv<Rl>& ov) {
@@ -109,13 +76,6 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
     T2* cend_aL = reinterpret_cast<T2*>(reinterpret_cast<unsigned char*>(flag) + 16);   // a^L (flag area is 64 B)
     const size_t base = (size_t)blockIdx.x * N;
 
-    // FIELD's compact row, where the masked inverse left it so (zero outside the spectral
-    // window, as its expansion writes)
-    const float* acr = nullptr;
-    if constexpr (TMA) {
-        if (sp.ac) acr = sp.ac + (size_t)blockIdx.x * sp.ncw;
-    }
-
     // ---- stage input and inverse FFT (propagator.cu:386-396, 640-641)
     load_twiddles<Rl>(twh, twl, f.tw, N, tid, nthr);
     // N / nthr = 16 elements per thread (2 when N < 512): loads issued together
@@ -130,33 +90,8 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
         // the previous stage of this CTA left (A + c dz k) / N in E (four stages per launch)
     } else if (per == 16) {
         T2 v[16];
-        if (acr) {   // compact FIELD: zero the row, place the window's columns, read it back
 #pragma unroll
-            for (int u = 0; u < 16; u++) E[pad16(tid + u * nthr)] = T2{0, 0};
-            __syncthreads();
-            for (int c = 2 * tid; c < sp.ncw; c += 2 * nthr) {
-                const int rc = __ldg(sp.cmap + c);
-                if (rc >= 0) E[pad16(rc >> 1)] = *reinterpret_cast<const T2*>(acr + c);
-            }
-            __syncthreads();
-#pragma unroll
-            for (int u = 0; u < 16; u++) v[u] = E[pad16(tid + u * nthr)];
-        } else {
-#pragma unroll
-            for (int u = 0; u < 16; u++) v[u] = A[base + tid + u * nthr];
-        }
-        if constexpr (TMA) {   // the row's A stays in tensor memory for the next stages' inputs
-#pragma unroll
-            for (int g = 0; g < 4; g++) {
-                float w[8];
-#pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    w[2 * i] = v[4 * g + i].x;
-                    w[2 * i + 1] = v[4 * g + i].y;
-                }
-                tm_st<8>(ov.tmem + ((uint32_t)(32 * ((tid >> 5) & 3)) << 16) + (uint32_t)(256 + 32 * (tid >> 7) + 8 * g), w);
-            }
-        }
+        for (int u = 0; u < 16; u++) v[u] = A[base + tid + u * nthr];
         if (ov.track_max) {
 #pragma unroll
             for (int u = 0; u < 16; u++) lmax = fmax(lmax, v[u].x * v[u].x + v[u].y * v[u].y);
@@ -190,8 +125,7 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
     // the row that takes this SM's next slot: its inputs travel to L2 while this row computes
     if (tid < 32 && ov.ahead > 0 && (int)blockIdx.x + ov.ahead < f.rows) {
         const size_t nbase = base + (size_t)ov.ahead * N;
-        if (acr) prefetch_row_l2(acr + (size_t)ov.ahead * sp.ncw, (size_t)sp.ncw * sizeof(float), tid);
-        else prefetch_row_l2(A + nbase, (size_t)N * sizeof(T2), tid);
+        prefetch_row_l2(A + nbase, (size_t)N * sizeof(T2), tid);
         if (ov.cdz != 0) prefetch_row_l2(ov.kp + nbase, (size_t)N * sizeof(T2), tid - 4);
         if (ov.stage == 3) {
             prefetch_row_l2(sp.kst[0] + nbase, (size_t)N * sizeof(T2), tid - 8);
@@ -513,16 +447,6 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
         for (int pb = tid; pb < N; pb += SB * nthr) {
             T2 v[SB], ac[SB], pf[SB], q[SB], k1[SB], k2[SB], k3[SB], an[SB];
             Rl kc[SB];
-            // the RK4 sum in tensor memory: this thread's points pb + u nthr are its points
-            // (pb - tid) / nthr + u of 16, at columns 32 (warp / 4) + 2 (point) (re, im) of its
-            // lane in the warp's lane quarter
-            float tv[2 * SB];
-            constexpr bool tacc = TMA;
-            const uint32_t ta = ov.tmem + ((uint32_t)(32 * ((tid >> 5) & 3)) << 16) +
-                                (uint32_t)(32 * (tid >> 7) + 2 * ((pb - tid) / nthr));
-            if constexpr (tacc && last) tm_ld<2 * SB>(ta, tv);
-            float ta_a[2 * SB];   // A at these points (tensor memory, from the stage-0 load)
-            if constexpr (tacc && !last) tm_ld<2 * SB>(ta + 256, ta_a);
 #pragma unroll
             for (int u = 0; u < SB; u++) {
                 const int p = pb + u * nthr;
@@ -535,12 +459,11 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
                 }
                 kc[u] = (in && kerr) ? -sp.kerr[p] : (Rl)0;
                 if constexpr (last) {
-                    k1[u] = (in && !tacc) ? sp.kst[0][base + p] : T2{0, 0};
-                    k2[u] = (in && !tacc) ? sp.kst[1][base + p] : T2{0, 0};
-                    k3[u] = (in && !tacc) ? sp.kst[2][base + p] : T2{0, 0};
+                    k1[u] = in ? sp.kst[0][base + p] : T2{0, 0};
+                    k2[u] = in ? sp.kst[1][base + p] : T2{0, 0};
+                    k3[u] = in ? sp.kst[2][base + p] : T2{0, 0};
                 } else {
-                    if constexpr (tacc) an[u] = T2{ta_a[2 * u], ta_a[2 * u + 1]};
-                    else an[u] = (in && ov.next_cdz != 0) ? A[base + p] : T2{0, 0};
+                    an[u] = (in && ov.next_cdz != 0) ? A[base + p] : T2{0, 0};
                 }
             }
 #pragma unroll
@@ -558,12 +481,7 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
                     k.y += kc[u] * qs.x;
                 }
                 if constexpr (!last) {
-                    if constexpr (!tacc) {
-                        kout[base + p] = k;
-                    } else {
-                        tv[2 * u] = k.x;
-                        tv[2 * u + 1] = k.y;
-                    }
+                    kout[base + p] = k;
                     if (ov.next_cdz != 0) {   // the next stage's input, as its load would form it
                         const Rl nc = ov.next_cdz;
                         T2 x = an[u];
@@ -576,7 +494,6 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
                 T2 s = k1[u];
                 s = T2{s.x + (Rl)2 * k2[u].x, s.y + (Rl)2 * k2[u].y};
                 s = T2{s.x + (Rl)2 * k3[u].x, s.y + (Rl)2 * k3[u].y};
-                if constexpr (tacc) s = T2{tv[2 * u], tv[2 * u + 1]};
                 const T2 nb = T2{(s.x + k.x) / (Rl)6, (s.y + k.y) / (Rl)6};
                 nmax = fmax(nmax, nb.x * nb.x + nb.y * nb.y);
                 sp.nb[base + p] = nb;
@@ -586,15 +503,6 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
                         if (c >= 0) *reinterpret_cast<float2*>(sp.nbc + (size_t)blockIdx.x * sp.ncw + c) = make_float2(nb.x, nb.y);
                     }
                 }
-            }
-            if constexpr (tacc && !last) {   // k1, then + 2 k2, + 2 k3 in that order
-                if (ov.stage > 0) {
-                    float o[2 * SB];
-                    tm_ld<2 * SB>(ta, o);
-#pragma unroll
-                    for (int i = 0; i < 2 * SB; i++) tv[i] = o[i] + 2.0f * tv[i];
-                }
-                tm_st<2 * SB>(ta, tv);
             }
         }
     };
@@ -617,41 +525,25 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(
                                                                               const typename Vec2<Rl>::T* __restrict__ A,
                                                                               SpecArgs<Rl> sp) {
     const StageOv<Rl> ov{f.cdz, f.kp, f.track_max, f.ahead, sp.stage, a.tape_e, a.tape_rho, a.tape_q, a.row_ion,
-                         (Rl)0, 0, 0u};
+                         (Rl)0, 0};
     nl_stage_row<Rl, LOGN, LC>(f, a, A, sp, ov);
 }
 
 // All four RK4 stages of every row in turn (step size f.dzs): stage s reads A and the k of
 // stage s - 1 that the same CTA has just written (L2-resident), so between steps a row's state
 // crosses HBM once.  A separate kernel, so that each keeps one inlined copy of the row body.
+// (Rows of 16384 FP32 points at 1024 threads without a stage record take nl_row16k_kernel,
+// gs_nl_row16k.cu, instead.)
 template <typename Rl, int LOGN = 0, int LC = 0>
 __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage4_kernel(FftArgs<Rl> f, PlasmaArgs<Rl> a,
                                                                                const typename Vec2<Rl>::T* __restrict__ A,
                                                                                SpecArgs<Rl> sp) {
-    // 16384-point FP32 rows at 1024 threads keep the RK4 sum (columns 0-255: 16 complex per
-    // thread) and the row's A (columns 256-511) in tensor memory, so k of stages 0-2 is never
-    // stored and A is read once per step; one CTA per SM holds all 512 columns
-    constexpr bool TM = sizeof(Rl) == 4 && LOGN == 14 && LC == 16;
-    __shared__ uint32_t tslot;
-    uint32_t tmem = 0;
-    if constexpr (TM) {
-        if (threadIdx.x < 32) {
-            asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
-                             (uint32_t)__cvta_generic_to_shared(&tslot)),
-                         "r"(512));
-            asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
-        }
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        tmem = tslot;
-    }
     for (int s = 0; s < 4; s++) {
         StageOv<Rl> ov{(Rl)(s == 0 ? 0.0 : (s < 3 ? f.dzs * 0.5 : f.dzs)),   // as the per-stage launches round it
                        s > 0 ? sp.kst[s - 1] : f.kp, s == 0, s == 0 ? f.ahead : 0, s,
                        a.tape_e, a.tape_rho, a.tape_q, a.row_ion,
                        (Rl)(s < 3 ? (s + 1 < 3 ? f.dzs * 0.5 : f.dzs) : 0.0),   // stage s + 1's c dz
-                       s > 0, tmem};
+                       s > 0};
         if (a.tape_e) {   // stage s's record for the adjoint
             const size_t o = (size_t)s * a.tape_stride;
             ov.tape_e = reinterpret_cast<typename Vec2<Rl>::T*>(reinterpret_cast<char*>(a.tape_e) + o);
@@ -660,15 +552,7 @@ __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage4_kernel
             ov.row_ion = reinterpret_cast<int*>(reinterpret_cast<char*>(a.row_ion) + o);
         }
         if (s > 0) __syncthreads();   // k of stage s - 1 written by every thread of the CTA
-        nl_stage_row<Rl, LOGN, LC, TM>(f, a, A, sp, ov);
-    }
-    if constexpr (TM) {
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        if (threadIdx.x < 32) {
-            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-            asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
-        }
+        nl_stage_row<Rl, LOGN, LC>(f, a, A, sp, ov);
     }
 }
 
@@ -692,7 +576,7 @@ template <typename Rl> bool nl_fused_threads_ok(int N, int t) {
 
 template <typename Rl> bool nl_stage_reads_compact(int N, int threads) {
     const int nthr = threads > 0 ? threads : fused_threads<Rl>(N);
-    return sizeof(Rl) == 4 && N == 16384 && nthr == 1024;   // nl_stage4_kernel<float, 14, 16>
+    return sizeof(Rl) == 4 && nl_row16k_applies(N, nthr);   // nl_row16k_kernel
 }
 
 template <typename Rl> int nl_fused_default_threads(int N) { return fused_threads<Rl>(N); }
@@ -710,10 +594,10 @@ template <typename Rl> cudaError_t nl_fused_setup(int N) {
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(nl_stage_kernel<Rl, 14>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(nl_stage4_kernel<Rl, 14, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     227 * 1024 - 1024);   // its static tensor-memory slot counts too
+            e = cudaFuncSetAttribute(nl_stage4_kernel<Rl, 14, 16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(nl_stage4_kernel<Rl, 14>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        if (e == cudaSuccess) e = nl_row16k_setup();
     }
     return e;
 }
@@ -768,10 +652,18 @@ cudaError_t launch_nl_stage(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2
             k1<<<rows, nthr, sm, st>>>(f, a, A, s);
         }
     };
-    if (s.ac && !(f.all_stages && nl_stage_reads_compact<Rl>(f.N, nthr))) return cudaErrorInvalidValue;
+    // a compact FIELD is read by nl_row16k_kernel only (its four-stage launch, no stage record)
+    if (s.ac && !(f.all_stages && !a.tape_e && nl_stage_reads_compact<Rl>(f.N, nthr))) return cudaErrorInvalidValue;
     bool done = false;
     if constexpr (sizeof(Rl) == 4) {
-        if (f.N == 16384 && nthr == 1024) {
+        if (f.all_stages && !a.tape_e && nl_row16k_applies(f.N, nthr)) {   // gs_nl_row16k.cu
+            static thread_local int ctas = -1;
+            if (ctas < 0 && nl_row16k_resident(&ctas) != 0) {
+                (void)cudaGetLastError();
+                ctas = 0;
+            }
+            return launch_nl_row16k(f, a, A, s, rows, ctas, st, nl);
+        } else if (f.N == 16384 && nthr == 1024) {
             go(nl_stage_kernel<Rl, 14, 16>, nl_stage4_kernel<Rl, 14, 16>);
             done = true;
         } else if (f.N == 16384) {

@@ -1,7 +1,7 @@
 """The four-stage NL kernel of 16384-point FP32 rows against the FP64 oracle.
 
-nl_stage4_kernel<float, 14, 16> runs all four RK4 stages of a row in one CTA, keeps the RK4 sum
-and the row's spectrum in tensor memory, and on steps after the first reads FIELD from the
+nl_row16k_kernel (gs_nl_row16k.cu) runs all four RK4 stages of a row in one CTA, keeps the RK4
+sum and the row's spectrum in tensor memory, and on steps after the first reads FIELD from the
 masked inverse's compact window columns.  It is chosen for mixed handles with n_t = 16384,
 1024 threads per row and at least four waves of rows (n_r >= 4 x resident CTAs: 608 rows on
 152 SMs), which is the 1024 x 16384 fused-silica workload's kernel.  These tests run it on 640
@@ -61,7 +61,7 @@ def test_stage4_nl_step_vs_oracle(hot16k):
     P.nl_timing(enable=True)
     ga2, gn2 = P.nl_step(dz)
     _, stages, launches = P.nl_timing(enable=False)
-    assert (stages, launches) == (4, 1)   # the four stages in one launch: nl_stage4_kernel
+    assert (stages, launches) == (4, 1)   # the four stages in one launch: nl_row16k_kernel
     g = P.get_nl()
     assert rel(g, bb1) < MIXED_TOL
     assert abs(ga2 - a2) / a2 < 1e-6
