@@ -12,7 +12,7 @@ Synthetic: the pulse is generated (seeded 1e-4 complex Gaussian noise), no datas
           copies FIELD and BIGBUFFER2 in and out (the host globals propagator() works on)
   fp64    the plain FP64 GPU path on the same workload, and the mixed path's relative L2
           error against it after 5, 100, 1000 and 2000 fixed-dz steps from the same start
-  roofline  the dominant kernel, nl_stage4_kernel (the four RK4 stages of every row in one
+  roofline  the dominant kernel, nl_row16k_kernel (the four RK4 stages of every row in one
           launch): the NL increment's algorithmic bytes, 16 B per field point (read FIELD,
           write BIGBUFFER1, complex64), over its CUDA-event launch time; its DRAM traffic and
           instruction counts from an ncu capture of one launch of this workload (the kernel
@@ -172,7 +172,7 @@ def new_state(S):
 # sm__inst_issued.avg.pct_of_peak_sustained_active of one launch, divided by its n_r n_t field
 # points); they are fixed properties of the kernels, re-measured whenever a kernel changes.
 NCU_PER_POINT = {
-    "nl_stage4": {"dram_bytes": 14.70, "warp_instructions": 41.4, "issue_active": 0.598},
+    "nl_row16k": {"dram_bytes": 11.44, "warp_instructions": 33.4, "issue_active": 0.623},
     "qdht_pair": {"dram_bytes": None},
 }
 
@@ -508,24 +508,27 @@ def main():
               "note": "algorithmic flop 2 N_r^2 per real column of the spectral window per transform (launch_ms is "
                       "one transform: split, factor table when dz changes, GEMM); the split FP16 operands execute 3 "
                       "products (Hh Xh + Hh Xl + Hl Xh) at the FP16 rate, which equals the bf16 rate of the peak"}
-    # the dominant kernel: nl_stage4_kernel, one launch per NL step (all four RK4 stages of a row
-    # in one CTA), or nl_stage_kernel once per stage on smaller grids; algorithmic bytes per step
+    # the dominant kernel: nl_row16k_kernel (16384-point FP32 rows) or nl_stage4_kernel, one launch
+    # per NL step (all four RK4 stages of a row in one CTA), or nl_stage_kernel once per stage on
+    # smaller grids; algorithmic bytes per step
     # 16 per field point (read FIELD, write the NL increment BIGBUFFER1, complex64)
     esz = 8 if prec == gs.PREC_MIXED else 16
     four = n_st and n_launch < n_st
     step_ms_nl = st_ms / n_st * 4 if n_st else None
     nl_bytes = 2 * esz * nr * nt
     nl_ach = nl_bytes / (step_ms_nl / 1e3) / 1e9 if step_ms_nl else None
-    ncu4 = NCU_PER_POINT["nl_stage4"]
-    roof = {"bound": "hbm", "kernel": ("nl_stage4_kernel" if four else "nl_stage_kernel") if n_st else "staged NL kernels (not timed)",
+    ncu4 = NCU_PER_POINT["nl_row16k"]
+    r16 = four and nt == 16384 and prec == gs.PREC_MIXED   # the shape the ncu figures describe
+    kname = ("nl_row16k_kernel" if r16 else "nl_stage4_kernel") if four else "nl_stage_kernel"
+    roof = {"bound": "hbm", "kernel": kname if n_st else "staged NL kernels (not timed)",
             "achieved": nl_ach, "peak": hbm, "unit": "GB/s", "frac": (nl_ach / hbm) if nl_ach and hbm else None,
-            "traffic": (ncu4["dram_bytes"] * nr * nt) if (four and prec == gs.PREC_MIXED) else None,
+            "traffic": (ncu4["dram_bytes"] * nr * nt) if r16 else None,
             "peak_kind": f"{pk_kind} HBM copy", "launch_ms": step_ms_nl,
             "algorithmic_bytes_per_launch": nl_bytes,
             "share_of_step": (st_ms / ms) if ms and n_st else None,
             "limiter": ({"kind": "SM instruction issue",
                          "warp_instructions_per_field_point": ncu4["warp_instructions"],
-                         "issue_active_frac": ncu4["issue_active"]} if (four and prec == gs.PREC_MIXED) else None),
+                         "issue_active_frac": ncu4["issue_active"]} if r16 else None),
             "note": "per NL step (one launch of all four RK4 stages), CUDA events around each launch on the handle's "
                     "stream; algorithmic bytes 16 per field point (FIELD in, BIGBUFFER1 out, complex64); traffic and "
                     "the limiter figures from an ncu capture of one launch of this workload"}

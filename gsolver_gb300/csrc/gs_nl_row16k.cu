@@ -38,7 +38,7 @@ constexpr int LOGN = 14;
 static_assert(N == NT * L, "one chunk of 16 per thread");
 
 // shared memory (bytes): E row (padded), rates W_t (padded), chunk starts of the density,
-// a^{16 j} (j < 1024), Raman warp totals and prefixes, density scan scratch, flag
+// a^{16 j} (j < 1024), Raman warp totals and prefixes, density scan scratch, warp maxima, flag
 constexpr int OFF_E = 0;
 constexpr int OFF_W = OFF_E + (N + N / 16) * 8;
 constexpr int OFF_S = OFF_W + ((N + N / 32 + 1 + 3) & ~3) * 4;
@@ -47,7 +47,8 @@ constexpr int OFF_WTOT = OFF_APW + NT * 8;
 constexpr int OFF_WPRE = OFF_WTOT + 32 * 8;
 constexpr int OFF_RA = OFF_WPRE + 32 * 8;
 constexpr int OFF_RB = OFF_RA + 32 * 4;
-constexpr int OFF_FLAG = OFF_RB + 32 * 4;
+constexpr int OFF_MX = OFF_RB + 32 * 4;
+constexpr int OFF_FLAG = OFF_MX + 32 * 4;
 constexpr int SMEM = OFF_FLAG + 16;
 static_assert(SMEM + 16 <= 227 * 1024, "fits one CTA");
 
@@ -149,6 +150,7 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
     float2* const wpre = reinterpret_cast<float2*>(smem_raw + OFF_WPRE);
     float* const rA = reinterpret_cast<float*>(smem_raw + OFF_RA);
     float* const rB = reinterpret_cast<float*>(smem_raw + OFF_RB);
+    float* const wmx = reinterpret_cast<float*>(smem_raw + OFF_MX);
     int* const flag = reinterpret_cast<int*>(smem_raw + OFF_FLAG);
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     const int row = blockIdx.x;
@@ -191,17 +193,19 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
     {
         float2 x[L];
         const float* acr = sp.ac ? sp.ac + (size_t)row * sp.ncw : nullptr;
-        if (acr) {   // zero the row, place the window's column pairs, read the thread's positions
+        if (acr) {   // the thread's positions from their window column pairs (zero outside)
+            int cc[L];
 #pragma unroll
-            for (int i = 0; i < L; i++) Ec[i] = make_float2(0.f, 0.f);
-            __syncthreads();
-            for (int c = 2 * t; c < sp.ncw; c += 2 * NT) {
-                const int rc = __ldg(sp.cmap + c);
-                if (rc >= 0) E[pad16(rc >> 1)] = *reinterpret_cast<const float2*>(acr + c);
+            for (int h = 0; h < L / 4; h++) {
+                const int4 v = __ldg(reinterpret_cast<const int4*>(sp.cinv + t0) + h);
+                cc[4 * h] = v.x;
+                cc[4 * h + 1] = v.y;
+                cc[4 * h + 2] = v.z;
+                cc[4 * h + 3] = v.w;
             }
-            __syncthreads();
 #pragma unroll
-            for (int i = 0; i < L; i++) x[i] = Ec[i];
+            for (int i = 0; i < L; i++)
+                x[i] = cc[i] >= 0 ? *reinterpret_cast<const float2*>(acr + cc[i]) : make_float2(0.f, 0.f);
         } else {
             const float4* a4 = reinterpret_cast<const float4*>(A + base + t0);
 #pragma unroll
@@ -217,7 +221,7 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
 #pragma unroll
         for (int i = 0; i < L; i++) amax = fmaxf(amax, x[i].x * x[i].x + x[i].y * x[i].y);
         for (int o = 16; o > 0; o >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, o));
-        if (lane == 0) atomic_max_nonneg(f.max_out, (double)amax);
+        if (lane == 0) wmx[w] = amax;   // one atomic per row, after the next barrier
         // the row that takes this SM's next slot: its input travels to L2 meanwhile
         if (t < 32 && f.ahead > 0 && row + f.ahead < f.rows) {
             if (acr) prefetch_row_l2(acr + (size_t)f.ahead * sp.ncw, (size_t)sp.ncw * sizeof(float), t);
@@ -307,6 +311,11 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
         // W > 0 somewhere (exp of the table is positive above its threshold) or rho starting
         // above 0: otherwise every Heun / gas step adds exactly 0 and the density stays 0
         const bool ion = __syncthreads_or(anyw ? 1 : 0) != 0 || a.k.rho0 != 0.f;
+        if (s == 0 && w == 0) {   // max |A|^2 of the row (the warps' maxima are in wmx since stage 0's input)
+            float m = wmx[lane];
+            for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+            if (lane == 0) atomic_max_nonneg(f.max_out, (double)m);
+        }
         float2 zs = make_float2(0.f, 0.f), zN = zs;
         if (rscan) {   // warp totals scanned by warp 0 (multiplier a^{512 o}); chunk starts
             if (w == 0) {
@@ -511,6 +520,10 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
         // the RK4 sum and leave the next stage's input, through its radix-4 pass, in E; stage 3
         // writes (k1 + 2 k2 + 2 k3 + k4) / 6, accumulated in that order (propagator.cu:412)
         const float cnext = (s < 2) ? c_half : c_full;
+        float4 kq[4];   // KERR_PROFILE at the thread's positions, its reads issued first
+#pragma unroll
+        for (int g = 0; g < 4; g++)
+            kq[g] = kerr ? __ldg(reinterpret_cast<const float4*>(sp.kerr + t0) + g) : make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
         for (int g = 0; g < 4; g++) {
             const int p0 = t0 + 4 * g;
@@ -523,11 +536,7 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
 #pragma unroll
                 for (int i = 0; i < 4; i++) v[i] = make_float2(0.f, 0.f);
             }
-            float kc[4] = {0.f, 0.f, 0.f, 0.f};
-            if (kerr) {
-                const float4 k4 = __ldg(reinterpret_cast<const float4*>(sp.kerr + p0));
-                kc[0] = -k4.x; kc[1] = -k4.y; kc[2] = -k4.z; kc[3] = -k4.w;
-            }
+            const float kc[4] = {-kq[g].x, -kq[g].y, -kq[g].z, -kq[g].w};
             float2 k[4], qs[4];
             if (ion) {
                 const float4* u1q = reinterpret_cast<const float4*>(sp.u1 + base) + 2 * (g * NT + t);
@@ -596,33 +605,42 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
             } else {
                 tld8(tm + 8 * g, sum);
                 tld_wait(sum);
-                float2 nb[4];
 #pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    nb[i] = make_float2((sum[2 * i] + k[i].x) / 6.0f, (sum[2 * i + 1] + k[i].y) / 6.0f);
-                    nmax = fmaxf(nmax, nb[i].x * nb[i].x + nb[i].y * nb[i].y);
-                }
-                float4* o4 = reinterpret_cast<float4*>(sp.nb + base + p0);
-                o4[0] = make_float4(nb[0].x, nb[0].y, nb[1].x, nb[1].y);
-                o4[1] = make_float4(nb[2].x, nb[2].y, nb[3].x, nb[3].y);
-                if (sp.nbc) {   // the spectral window's positions, compactly (the linear step's input)
-                    const int4 c4 = __ldg(reinterpret_cast<const int4*>(sp.cinv + p0));
-                    const int cc[4] = {c4.x, c4.y, c4.z, c4.w};
-                    float* nbr = sp.nbc + (size_t)row * sp.ncw;
-#pragma unroll
-                    for (int i = 0; i < 4; i++)
-                        if (cc[i] >= 0) *reinterpret_cast<float2*>(nbr + cc[i]) = nb[i];
+                for (int i = 0; i < 4; i++) {   // to E: the warp stores its 512 positions below
+                    const float2 nb = make_float2((sum[2 * i] + k[i].x) / 6.0f, (sum[2 * i + 1] + k[i].y) / 6.0f);
+                    nmax = fmaxf(nmax, nb.x * nb.x + nb.y * nb.y);
+                    Ec[4 * g + i] = nb;
                 }
             }
         }
         if (s < 3) tst_wait();
     }
+    // ---- BIGBUFFER1 and (sp.nbc) its spectral-window positions compactly, the linear step's
+    // input: each warp's 512 consecutive positions, two per lane per 16-byte store
+    __syncwarp();
+    {
+        float* const nbr = sp.nbc ? sp.nbc + (size_t)row * sp.ncw : nullptr;
+#pragma unroll 4
+        for (int r = 0; r < 8; r++) {
+            const int p = 512 * w + 64 * r + 2 * lane;
+            const float2 y0 = E[pad16(p)], y1 = E[pad16(p) + 1];
+            *reinterpret_cast<float4*>(sp.nb + base + p) = make_float4(y0.x, y0.y, y1.x, y1.y);
+            if (nbr) {
+                const int2 c2 = __ldg(reinterpret_cast<const int2*>(sp.cinv + p));
+                if (c2.x >= 0) *reinterpret_cast<float2*>(nbr + c2.x) = y0;
+                if (c2.y >= 0) *reinterpret_cast<float2*>(nbr + c2.y) = y1;
+            }
+        }
+    }
     for (int o = 16; o > 0; o >>= 1) nmax = fmaxf(nmax, __shfl_xor_sync(0xffffffffu, nmax, o));
-    if (lane == 0) atomic_max_nonneg(sp.max_out, (double)nmax);
+    if (lane == 0) wmx[w] = nmax;
 
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (w == 0) {
+        float m = wmx[lane];
+        for (int o = 16; o > 0; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (lane == 0) atomic_max_nonneg(sp.max_out, (double)m);
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tslot), "r"(512));
     }
@@ -638,7 +656,7 @@ cudaError_t nl_row16k_setup() {
 
 cudaError_t launch_nl_row16k(FftArgs<float> f, PlasmaArgs<float> a, const float2* A, SpecArgs<float> s, int rows,
                              int ahead, cudaStream_t st, long long* nl) {
-    if (f.N != r16k::N || !f.twb || a.tape_e) return cudaErrorInvalidValue;
+    if (f.N != r16k::N || !f.twb || a.tape_e || (s.ac && !s.cinv) || (s.nbc && !s.cinv)) return cudaErrorInvalidValue;
     f.rows = rows;
     f.ahead = ahead;
     r16k::nl_row16k_kernel<<<rows, r16k::NT, r16k::SMEM, st>>>(f, a, A, s);
