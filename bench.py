@@ -72,6 +72,8 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=10)
     ap.add_argument("--adjoint-steps", type=int, default=1000)
     ap.add_argument("--adjoint-check-steps", type=int, default=100)
+    ap.add_argument("--adjoint-dirs", type=int, default=2,
+                    help="seeded random directions of the finite-difference check (the full check: 32 over 1000 steps)")
     return ap.parse_args()
 
 
@@ -375,7 +377,8 @@ def adjoint_leg(args, lrank):
     radial weights).  Times gs_forward_fixed and gs_gradient (forward + checkpointed adjoint,
     the default stride: every step recorded when it fits in memory) on the mixed path, both through the C ABI with host fields, and checks the
     gradient on the first `adjoint_check_steps` steps against the FP64 adjoint and fourth-order
-    central differences of the FP64 forward along one seeded direction."""
+    central differences of the FP64 forward along the FP64 gradient and `adjoint_dirs` seeded
+    random directions (max and median relative errors over those)."""
     import gsolver_gb300 as gs
     from gsolver_gb300 import configs
     d = tempfile.mkdtemp(prefix="gs_bench_adj_")
@@ -397,12 +400,18 @@ def adjoint_leg(args, lrank):
 
     tf, (J, _) = timed(lambda: Pm.forward_fixed(A0, rk, lin, w))
     tg, (Jg, gm) = timed(lambda: Pm.gradient(A0, rk, lin, w))
+    stride = Pm.adjoint_stride()
+    ks = int(np.ceil(np.sqrt(n)))   # the sqrt(N) checkpointing: segments re-run from checkpoints
+    tk, (_, gk) = timed(lambda: Pm.gradient(A0, rk, lin, w, checkpoint_stride=ks), reps=1)
     out = {"workload": "fused_silica_256x4096_adjoint", "n_r": 256, "n_t": 4096, "steps": n, "dz_m": 2e-6,
            "objective": "band energy 500-600 nm, average_spectrum radial weights",
-           "checkpoint_stride": Pm.adjoint_stride(), "precision": "mixed",
+           "checkpoint_stride": stride, "precision": "mixed",
            "nl_threads_per_row": tuned[0] if tuned else "default",
            "forward_ms": tf, "gradient_ms": tg, "cost_ratio": tg / tf,
-           "note": "gradient_ms = forward + adjoint (one gs_gradient call); cost_ratio = gradient / forward"}
+           "sqrt_stride": {"checkpoint_stride": ks, "gradient_ms": tk, "cost_ratio": tk / tf,
+                           "max_abs_diff_vs_default": float(np.abs(gk - gm).max() / np.abs(gm).max())},
+           "note": "gradient_ms = forward + adjoint (one gs_gradient call); cost_ratio = gradient / forward; "
+                   "sqrt_stride: the same gradient with checkpoints every ceil(sqrt(steps)) steps"}
     m = args.adjoint_check_steps
     if m > 0:
         P64 = gs.Propagator(S, precision=gs.PREC_FP64, device=lrank)
@@ -412,9 +421,9 @@ def adjoint_leg(args, lrank):
         Jf = lambda A: P64.forward_fixed(A, rk[:m], lin[:m], w)[0]
         chk = {"steps": m, "grad_rel_l2_mixed_vs_fp64": float(np.linalg.norm(gmm - g64) / np.linalg.norm(g64)),
                "fd": "fourth-order central differences of the FP64 forward, h = 1e-5, along the FP64 gradient "
-                     "(well conditioned) and along one seeded random direction"}
-        rnd = np.random.default_rng(11).standard_normal(A0.shape) + 1j * np.random.default_rng(12).standard_normal(A0.shape)
-        for name, v in (("gradient_dir", g64), ("random_dir", rnd)):
+                     "(well conditioned) and along seeded random directions (complex Gaussian, seeds 11 + k)"}
+
+        def fd_check(v):
             v = v * (np.linalg.norm(A0) / np.linalg.norm(v))
             fd = (-Jf(A0 + 2 * h * v) + 8 * Jf(A0 + h * v) - 8 * Jf(A0 - h * v) + Jf(A0 - 2 * h * v)) / (12 * h)
             d64 = float(np.sum((np.conj(g64) * v).real))
@@ -422,8 +431,19 @@ def adjoint_leg(args, lrank):
             # conditioning |g||v| / |<g, v>|: a gradient error e (relative L2) moves the
             # directional derivative by up to e times this
             cond = float(np.linalg.norm(g64) * np.linalg.norm(v) / abs(d64))
-            chk[name] = {"fd_rel_err_fp64": abs(d64 - fd) / abs(fd), "fd_rel_err_mixed": abs(dm - fd) / abs(fd),
-                         "conditioning": cond}
+            return abs(d64 - fd) / abs(fd), abs(dm - fd) / abs(fd), cond
+
+        e64, em, cd = fd_check(g64)
+        chk["gradient_dir"] = {"fd_rel_err_fp64": e64, "fd_rel_err_mixed": em, "conditioning": cd}
+        res = []
+        for k in range(args.adjoint_dirs):
+            r = np.random.default_rng(11 + k)
+            res.append(fd_check(r.standard_normal(A0.shape) + 1j * r.standard_normal(A0.shape)))
+        if res:
+            a = np.asarray(res)
+            stat = lambda x: {"max": float(np.max(x)), "median": float(np.median(x))}
+            chk["random_dirs"] = {"n": len(res), "fd_rel_err_fp64": stat(a[:, 0]), "fd_rel_err_mixed": stat(a[:, 1]),
+                                  "conditioning": stat(a[:, 2])}
         out["check"] = chk
         P64.close()
     Pm.close()

@@ -17,7 +17,7 @@
 // Memory: checkpointing.  The forward stores (FIELD, BIGBUFFER2) every K steps and records
 // the four RK4 stages of every step of the last segment (E/N, rho, Q per sample); the
 // backward sweep walks that segment back, then re-runs each earlier segment from its
-// checkpoint, recording its stages, and walks it back.  Device memory: 6 work arrays, 2 per
+// checkpoint, recording its stages, and walks it back.  Device memory: 7 work arrays, 2 per
 // checkpoint and 4 (E, rho, Q) triples per step of a segment.  The n - K steps before the
 // last segment run twice, so K is as large as memory allows: unless given, every step is
 // recorded during the forward when that fits in half of the device memory that is free (the
@@ -40,8 +40,11 @@ namespace {
 struct AdjLayout {
     size_t nel, esz, rsz;
     int K, nck;
-    size_t work_bytes() const { return 6 * nel * esz; }
-    size_t ck_bytes() const { return (size_t)(nck > 1 ? nck - 1 : 0) * 2 * nel * esz; }   // the last segment is recorded
+    size_t work_bytes() const { return 7 * nel * esz; }
+    // per checkpoint: FIELD, BIGBUFFER2 and (mixed) its window columns as double-float pairs
+    size_t spec_bytes = 0;
+    size_t ck_slot() const { return 2 * nel * esz + spec_bytes; }
+    size_t ck_bytes() const { return (size_t)(nck > 1 ? nck - 1 : 0) * ck_slot(); }   // the last segment is recorded
     int nr;
     size_t ion_bytes() const { return ((size_t)nr * 4 + 255) & ~(size_t)255; }
     size_t tape_step_bytes() const { return 4 * (nel * (esz + 2 * rsz) + ion_bytes()); }
@@ -50,6 +53,7 @@ struct AdjLayout {
 
 struct AdjPtrs {
     void *Ab, *Sb, *Rb, *KB, *Eb, *Fb;
+    void* Sl;   // mixed: the low parts of BIGBUFFER2's cotangent (double-float pairs Sb + Sl)
     char* ck;
     char* tape;
 };
@@ -71,6 +75,7 @@ int ensure_adj(gs_handle* h, const AdjLayout& L, AdjPtrs* P) {
     char* b = (char*)h->adj;
     const size_t a = L.nel * L.esz;
     P->Ab = b; P->Sb = b + a; P->Rb = b + 2 * a; P->KB = b + 3 * a; P->Eb = b + 4 * a; P->Fb = b + 5 * a;
+    P->Sl = b + 6 * a;
     P->ck = b + L.work_bytes();
     P->tape = P->ck + L.ck_bytes();
     return GS_OK;
@@ -236,8 +241,9 @@ int adjoint_step(gs_handle* h, const AdjPtrs& P, const GsTape& tp, double dz_rk,
     if (h->fp64)
         CK(h, launch_lstep_adj<double>((const double2*)P.Fb, (double2*)P.Sb, (double2*)P.KB, h->nr, h->nt, L, h->st,
                                        &h->launches));
-    else   // the FP32 arithmetic of the mixed forward's fused epilogue
-        CK(h, gs::qdht_tc_lstep_adj(h->tc, (const float*)P.Fb, (float*)P.Sb, (float*)P.KB, dz_lin, &h->launches));
+    else   // the arithmetic of the mixed forward's fused epilogue (double-float where it is)
+        CK(h, gs::qdht_tc_lstep_adj(h->tc, (const float*)P.Fb, (float*)P.Sb, (float*)P.Sl, (float*)P.KB, dz_lin,
+                                    &h->launches));
     if (!h->p.nonlinear) {   // N = 0: FIELD enters the step only through the NL response
         CK(h, cudaMemsetAsync(P.Ab, 0, nel * h->esz, h->st));
         return GS_OK;
@@ -331,6 +337,11 @@ int gs_gradient(gs_handle* h, const double* field_in, int n_steps, const double*
     L.nr = h->nr;
     L.esz = h->esz;
     L.rsz = h->esz / 2;
+    float *spc = nullptr, *spl = nullptr;   // BIGBUFFER2's compact double-float columns (mixed)
+    int spn = 0;
+    if (!h->fp64 && h->tc) gs::qdht_tc_spec_pairs(h->tc, &spc, &spl, &spn);
+    const size_t spb = (size_t)h->nr * spn * sizeof(float);
+    L.spec_bytes = spc ? 2 * spb : 0;
     L.K = checkpoint_stride > 0 ? checkpoint_stride : auto_stride(h, L, n_steps);
     if (L.K > n_steps) L.K = n_steps;
     h->adj_stride = L.K;
@@ -345,18 +356,24 @@ int gs_gradient(gs_handle* h, const double* field_in, int n_steps, const double*
     // forward, storing a checkpoint every K steps; the last segment records its stages now,
     // so the backward sweep starts without re-running it
     const int last0 = (L.nck - 1) * L.K;
+    std::vector<char> ck_pairs((size_t)L.nck, 0);   // whether checkpoint k holds the compact pairs
     rc = gsi::permute_in(h, field_in, h->A);
     if (!rc) rc = gsi::run_qdht(h, QDHT_PLAIN, h->A, h->S, 0.0);
     h->field_ok = rc == GS_OK;
     for (int n = 0; n < n_steps && !rc; n++) {
         if (n % L.K == 0 && n < last0) {
-            char* ck = P.ck + (size_t)(n / L.K) * 2 * arr;
+            char* ck = P.ck + (size_t)(n / L.K) * L.ck_slot();
             rc = gsi::field_sync(h);
             if (rc) return rc;
             CK(h, cudaMemcpyAsync(ck, h->A, arr, cudaMemcpyDeviceToDevice, h->st));
             rc = gsi::spec_sync(h);
             if (rc) return rc;
             CK(h, cudaMemcpyAsync(ck + arr, h->S, arr, cudaMemcpyDeviceToDevice, h->st));
+            if (spc && h->s_compact) {   // the low parts too: a re-run segment repeats the forward exactly
+                CK(h, cudaMemcpyAsync(ck + 2 * arr, spc, spb, cudaMemcpyDeviceToDevice, h->st));
+                CK(h, cudaMemcpyAsync(ck + 2 * arr + spb, spl, spb, cudaMemcpyDeviceToDevice, h->st));
+                ck_pairs[n / L.K] = 1;
+            }
         }
         const bool rec = h->p.nonlinear && n >= last0;
         const GsTape tp = tape_of(L, P.tape, rec ? n - last0 : 0);
@@ -368,16 +385,22 @@ int gs_gradient(gs_handle* h, const double* field_in, int n_steps, const double*
     rc = objective(h, &P, &J);   // A_bar = 2 w FIELD_N
     if (rc) return rc;
     CK(h, cudaMemsetAsync(P.Sb, 0, arr, h->st));
+    CK(h, cudaMemsetAsync(P.Sl, 0, arr, h->st));
 
     // backward, one checkpoint segment at a time
     for (int seg = L.nck - 1; seg >= 0 && !rc; seg--) {
         const int n0 = seg * L.K, n1 = std::min(n_steps, n0 + L.K);
         if (seg < L.nck - 1) {   // re-run the segment from its checkpoint, recording its stages
-            const char* ck = P.ck + (size_t)seg * 2 * arr;
-            CK(h, cudaMemcpyAsync(h->A, ck, arr, cudaMemcpyDeviceToDevice, h->st));
-            CK(h, cudaMemcpyAsync(h->S, ck + arr, arr, cudaMemcpyDeviceToDevice, h->st));
+            const char* ck = P.ck + (size_t)seg * L.ck_slot();
             gsi::spec_written(h);
             gsi::field_written(h);
+            CK(h, cudaMemcpyAsync(h->A, ck, arr, cudaMemcpyDeviceToDevice, h->st));
+            CK(h, cudaMemcpyAsync(h->S, ck + arr, arr, cudaMemcpyDeviceToDevice, h->st));
+            if (ck_pairs[seg]) {
+                CK(h, cudaMemcpyAsync(spc, ck + 2 * arr, spb, cudaMemcpyDeviceToDevice, h->st));
+                CK(h, cudaMemcpyAsync(spl, ck + 2 * arr + spb, spb, cudaMemcpyDeviceToDevice, h->st));
+                h->s_compact = true;
+            }
             for (int m = n0; m < n1 && !rc; m++) {
                 const GsTape tp = tape_of(L, P.tape, m - n0);
                 rc = gsi::nl_stages(h, dz_rk[m], h->p.nonlinear ? &tp : nullptr);
@@ -427,6 +450,7 @@ int gs_adjoint_step(gs_handle* h, double dz_rk, double dz_lin, double* field_bar
     if (!rc) rc = gsi::lstep(h, dz_lin);
     if (!rc) rc = gsi::permute_in(h, field_bar, P.Ab);
     if (!rc) rc = gsi::permute_in(h, spec_bar, P.Sb);
+    if (!rc) CK(h, cudaMemsetAsync(P.Sl, 0, L.nel * L.esz, h->st));
     if (!rc) rc = adjoint_step(h, P, tp, dz_rk, dz_lin);
     if (!rc) rc = read_err(h);
     if (!rc) rc = gsi::permute_out(h, P.Ab, field_bar);

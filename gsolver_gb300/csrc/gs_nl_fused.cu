@@ -324,9 +324,10 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
         const T2 oma = T2{a.k.oma_re, a.k.oma_im};
         const Rl fRM = a.k.fRM, omf = a.k.omf;
         if (gas && t0 == 0) W0 = (Rl)-1;
-        // the common row (no ionization, solid, Raman recurrence, no record): the Kerr source
-        // only, the same arithmetic as the general loop below
-        const bool plain = !ion && !gas && rscan && !a.th && !ov.tape_e;
+        // the common row (no ionization, solid, Raman recurrence): the Kerr source only.  It
+        // takes this loop whether or not the stage is recorded, so that a recorded step (the
+        // adjoint's re-run of a checkpoint segment) repeats an unrecorded one bit for bit
+        const bool plain = !ion && !gas && rscan && !a.th;
 #pragma unroll 4
         for (int i = 0; i < (plain ? L : 0); i++) {
             const T2 e = e_at(i);
@@ -339,6 +340,10 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
             const T2 src3 = T2{Q * e.x, Q * e.y};
             if (LC == 16) E[pad16(t0) + i] = src3;
             else E[pad16(t0 + i)] = src3;
+            if (ov.tape_e) {   // what the adjoint of this stage reads back (no density: no ionization)
+                ov.tape_e[base + t0 + i] = e;
+                ov.tape_q[base + t0 + i] = Q;
+            }
         }
 #pragma unroll 4
         for (int i = 0; i < (plain ? 0 : L); i++) {

@@ -862,6 +862,42 @@ __device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, 
     }
 }
 
+// Adjoint of the double-float linear step (epilogue_cols with a.ylo) on [n_r][n_t] cotangents:
+// T_bar = FIELD_bar + B2_bar, B2_bar = conj(P) T_bar, N_bar = dz T_bar conj(P) / (1 + s), where
+// P = exp(dz (k_i + i theta)) comes from the same [pair][row] tables (position p's pair
+// cinv[p] / 2) and ff_cexp as the forward's, and B2_bar is carried as double-float pairs
+// (sb + sbl) across steps, as the forward carries BIGBUFFER2: factors within 2^-24 of 1 and
+// their rounding repeated over many steps would otherwise build up in an FP32 cotangent.
+// Outside the window (cinv[p] < 0, or 1 / (1 + s) = 0) B2_bar passes unchanged and N_bar = 0.
+__global__ void lstep_adj_ff_kernel(const float2* __restrict__ fb, float2* __restrict__ sb, float2* __restrict__ sbl,
+                                    float2* __restrict__ b1b, int nr, int nt, float dzh, float dzl,
+                                    const int* __restrict__ cinv, const float2* __restrict__ theta,
+                                    const float2* __restrict__ kiff, const float* __restrict__ inv1ps) {
+    const size_t total = (size_t)nr * nt;
+    const size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= total) return;
+    const int i = (int)(idx / nt), p = (int)(idx % nt);
+    const int c = cinv[p];
+    const size_t tq = c >= 0 ? (size_t)(c >> 1) * nr + i : 0;
+    const float inv = c >= 0 ? inv1ps[tq] : 0.f;
+    if (inv == 0.f) {
+        b1b[idx] = make_float2(0.f, 0.f);
+        return;
+    }
+    const ff2 dz{dzh, dzl};
+    const float2 th = theta[tq], kk = kiff[c >> 1];
+    ff2 cr, ci;   // conj(P)
+    ff_cexp(ff_mul(dz, ff2{kk.x, kk.y}), ff_neg(ff_mul(dz, ff2{th.x, th.y})), &cr, &ci);
+    const float2 f = fb[idx], bh = sb[idx], bl = sbl[idx];
+    const ff2 tr = ff_add(ff2{bh.x, bl.x}, ff2{f.x, 0.f});
+    const ff2 ti = ff_add(ff2{bh.y, bl.y}, ff2{f.y, 0.f});
+    const ff2 rr = ff_add(ff_mul(cr, tr), ff_neg(ff_mul(ci, ti)));
+    const ff2 ri = ff_add(ff_mul(cr, ti), ff_mul(ci, tr));
+    sb[idx] = make_float2(rr.h, ri.h);
+    sbl[idx] = make_float2(rr.l, ri.l);
+    b1b[idx] = make_float2(dzh * rr.h * inv, dzh * ri.h * inv);
+}
+
 // The masked inverse's result from its compact array: row i of Y (all n_t positions, coalesced)
 // takes the pair cinv[p] of yc where p is inside the spectral window and zeros elsewhere.
 // Two positions per thread (one 16-byte store), four stores in flight per thread.
@@ -1642,13 +1678,25 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
     return cudaGetLastError();
 }
 
-cudaError_t qdht_tc_lstep_adj(QdhtTc* q, const float* fb, float* sb, float* b1b, double dz, long long* nlaunch) {
+cudaError_t qdht_tc_lstep_adj(QdhtTc* q, const float* fb, float* sb, float* sbl, float* b1b, double dz,
+                              long long* nlaunch) {
     if (!q->have_lstep) return cudaErrorInvalidValue;
     const size_t total = (size_t)q->nr * q->nt;
-    tc::lstep_adj_kernel<<<(unsigned)((total + 255) / 256), 256, 0, q->st>>>(
-        (const float2*)fb, (float2*)sb, (float2*)b1b, q->nt, total, (float)dz, q->kr, q->ki, q->ho, q->kt2, q->kmax);
+    if (sbl && qdht_tc_lstep_adj_ff(q)) {   // the double-float forward's adjoint
+        const float dzh = (float)dz, dzl = (float)(dz - (double)dzh);
+        tc::lstep_adj_ff_kernel<<<(unsigned)((total + 255) / 256), 256, 0, q->st>>>(
+            (const float2*)fb, (float2*)sb, (float2*)sbl, (float2*)b1b, q->nr, q->nt, dzh, dzl, q->cinv, q->theta,
+            q->kiff, q->inv1ps);
+    } else {
+        tc::lstep_adj_kernel<<<(unsigned)((total + 255) / 256), 256, 0, q->st>>>(
+            (const float2*)fb, (float2*)sb, (float2*)b1b, q->nt, total, (float)dz, q->kr, q->ki, q->ho, q->kt2, q->kmax);
+    }
     (*nlaunch)++;
     return cudaGetLastError();
+}
+
+bool qdht_tc_lstep_adj_ff(const QdhtTc* q) {
+    return q && q->wide && q->cinv && q->theta && q->kiff && q->inv1ps;
 }
 
 bool qdht_tc_has_compact(const QdhtTc* q) { return q && q->wide && q->sc != nullptr; }

@@ -62,10 +62,15 @@ float* qdht_tc_compact_x(QdhtTc* q, const int** cinv, int* nc);
 // its expansion into Y (zeros outside the spectral window).
 const float* qdht_tc_compact_y(QdhtTc* q, int* nc, const int** cmap = nullptr);
 cudaError_t qdht_tc_expand(QdhtTc* q, float* Y, long long* nlaunch);
-// Adjoint of the QDHT_LSTEP epilogue's linear step, elementwise over [n_r][n_t] (FP32, the
-// epilogue's tables): fb = cotangent of FIELD (k,omega), sb of BIGBUFFER2 (in: after the
-// step, out: before), b1b out: of BIGBUFFER1 (k,omega).
-cudaError_t qdht_tc_lstep_adj(QdhtTc* q, const float* fb, float* sb, float* b1b, double dz, long long* nlaunch);
+// Adjoint of the QDHT_LSTEP epilogue's linear step, elementwise over [n_r][n_t]: fb = cotangent
+// of FIELD (k,omega), sb of BIGBUFFER2 (in: after the step, out: before), b1b out: of
+// BIGBUFFER1 (k,omega).  When the plan forms the forward's factors in double-float
+// (qdht_tc_lstep_adj_ff) and sbl is given, the adjoint does the same and sb + sbl is
+// BIGBUFFER2's cotangent as double-float pairs (sbl: their low parts, zero to start);
+// otherwise FP32 with the epilogue's FP32 tables.
+cudaError_t qdht_tc_lstep_adj(QdhtTc* q, const float* fb, float* sb, float* sbl, float* b1b, double dz,
+                              long long* nlaunch);
+bool qdht_tc_lstep_adj_ff(const QdhtTc* q);
 void qdht_tc_destroy(QdhtTc* q);
 
 }  // namespace gs

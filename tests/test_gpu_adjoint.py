@@ -4,10 +4,11 @@ gs_adjoint_step).
 * FP64 gradient vs the oracle's FP64 adjoint (which is itself checked against central
   differences of the oracle forward): <= 1e-9 relative L2.
 * FP64 gradient vs central differences of the GPU FP64 forward along seeded directions.
-* Mixed (3xTF32 QDHT, FP32 NL) gradient: directional derivatives within 1e-4 relative of
-  the FP64 central differences.
-* checkpointing: every checkpoint stride gives the bit-identical gradient; the default
-  records every step during the forward when it fits in memory.
+* Mixed (split-FP16 QDHT, the linear step and BIGBUFFER2's cotangent in double-float as in the
+  forward, FP32 NL) gradient: directional derivatives within 1e-4 relative of the FP64 central
+  differences.
+* checkpointing: every checkpoint stride gives the bit-identical gradient (both precisions);
+  the default records every step during the forward when it fits in memory.
 * A torch.autograd.Function over the C ABI (ctypes) whose backward is gs_gradient.
 """
 import tempfile
@@ -76,11 +77,14 @@ def test_adjoint_step_matches_oracle():
     assert rel(s, s_ref) < 1e-12
 
 
-def test_checkpoint_strides_give_identical_gradients():
-    T = hot(n_r=32, n_t=1024, power_cr=30.0)
+@pytest.mark.parametrize("prec,n_r", [(gs.PREC_FP64, 32), (gs.PREC_MIXED, 128)])
+def test_checkpoint_strides_give_identical_gradients(prec, n_r):
+    """Re-run segments repeat the forward exactly: the mixed path's checkpoints hold BIGBUFFER2's
+    double-float window columns too (128 rows: the tensor-core QDHT with its compact state)."""
+    T = hot(n_r=n_r, n_t=1024, power_cr=30.0)
     dz_rk, dz_lin = schedule(T, 7)
     w = np.random.default_rng(1).random((T["n_r"], T["n_t"]))
-    P = gs.Propagator(T, precision=gs.PREC_FP64)
+    P = gs.Propagator(T, precision=prec)
     ref = None
     for k in (0, 1, 2, 3, 7):   # 0: every step recorded in the forward (a few MB here)
         J, g = P.gradient(T["field"], dz_rk, dz_lin, w, checkpoint_stride=k)
@@ -116,7 +120,7 @@ def test_gradients_vs_central_differences_fp64_and_mixed():
     Pm = gs.Propagator(T, precision=gs.PREC_MIXED)
     Jm, gm = Pm.gradient(A0, dz_rk, dz_lin, w)
     assert abs(Jm - J) <= 1e-4 * J
-    assert rel(gm, g64) < 1e-4
+    assert rel(gm, g64) < 5e-5   # 2.0e-5 measured (10 steps of a strongly ionizing pulse)
     rng = np.random.default_rng(4)
     scale = np.linalg.norm(A0)
     # fourth-order central differences at h = 1e-5 (the h^2 term of the two-point rule is
