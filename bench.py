@@ -153,16 +153,20 @@ class Clocks:
 
 
 def run_z_steps(P, S, state, k):
-    """k accepted propagator() calls continuing the z-loop (solver_main.cpp:202-225)."""
+    """k accepted propagator() calls continuing the z-loop (solver_main.cpp:202-225), through
+    gs_advance: the step controller on the device, no host round trip per call (the workload's
+    kernels read their step sizes from device memory; gs_step gives the same results bit for
+    bit, tests/test_gpu_advance.py)."""
     znet = S["znet"]
-    for _ in range(k):
+    while k > 0:
         cz, n_z, zstep, step_n = state["z"], state["n_z"], state["zstep"], state["step_n"]
         if cz >= znet[n_z]:
             if n_z == len(znet) - 1:
                 raise RuntimeError("workload ran past its last ZNET point")
             n_z += 1
-        zstep, step_n, _, _ = P.step(cz, znet[n_z], znet[n_z - 1], zstep, step_n)
-        state.update(z=cz + zstep, n_z=n_z, zstep=zstep, step_n=step_n + 1)
+        cz, zstep, step_n, calls, _ = P.advance(znet, n_z, cz, zstep, step_n, k)
+        state.update(z=cz, n_z=n_z, zstep=zstep, step_n=step_n)
+        k -= calls
 
 
 def new_state(S):

@@ -29,7 +29,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 # every function declared in include/gs_abi.h
 ABI_FUNCTIONS = (
     "gs_create", "gs_upload_tables", "gs_set_field", "gs_get_field", "gs_nl_step", "gs_get_nl",
-    "gs_lstep", "gs_qdht", "gs_step", "gs_stream", "gs_launch_count", "gs_qdht_timing", "gs_nl_timing",
+    "gs_lstep", "gs_qdht", "gs_step", "gs_advance", "gs_stream", "gs_launch_count", "gs_qdht_timing", "gs_nl_timing",
     "gs_destroy",
     "gs_last_error", "gs_status_string",
     # include/gs_setup.h
@@ -101,6 +101,8 @@ def load_library(path: str | None = None):
     L.gs_lstep.argtypes = [V, D]
     L.gs_qdht.argtypes = [V, V]
     L.gs_step.argtypes = [V, D, D, D, PD, C.POINTER(C.c_uint), PD, PD]
+    L.gs_advance.argtypes = [V, V, C.c_int, C.c_int, PD, PD, C.POINTER(C.c_uint), C.c_int, C.POINTER(C.c_int),
+                             C.POINTER(C.c_int)]
     L.gs_stream.argtypes = [V]
     L.gs_stream.restype = V
     L.gs_launch_count.argtypes = [V]
@@ -256,6 +258,16 @@ class Propagator:
                                    C.byref(dz), C.byref(sn), C.byref(a2), C.byref(n2)))
         return dz.value, sn.value, a2.value, n2.value
 
+    def advance(self, znet, n_z, current_z, zstep, step_n=0, max_calls=1 << 30):
+        """gs_advance: up to max_calls propagator() calls from CURRENT_Z below ZNET[n_z], the step
+        controller on the device.  Returns (CURRENT_Z, ZSTEP, STEP_N, calls, reached ZNET[n_z])."""
+        zn = np.ascontiguousarray(znet, dtype=np.float64)
+        cz, dz, sn = C.c_double(current_z), C.c_double(zstep), C.c_uint(step_n)
+        calls, reached = C.c_int(), C.c_int()
+        self._check(self.L.gs_advance(self.h, _ptr(zn), len(zn), int(n_z), C.byref(cz), C.byref(dz), C.byref(sn),
+                                      int(max_calls), C.byref(calls), C.byref(reached)))
+        return cz.value, dz.value, sn.value, calls.value, bool(reached.value)
+
     def stream_ptr(self):
         return int(self.L.gs_stream(self.h) or 0)
 
@@ -397,9 +409,10 @@ class Propagator:
         self._check(self.L.gs_adjoint_step(self.h, float(dz_rk), float(dz_lin), _ptr(fb), _ptr(sb)))
         return fb, sb
 
-    def run(self, znet, dz0, steps=None, on_dump=None):
+    def run(self, znet, dz0, steps=None, on_dump=None, device=False):
         """The z-loop of solver_main.cpp:202-225 over ZNET; on_dump(n_z, self) at each
-        ZNET point.  Returns (final z, zstep, STEP_N, propagator calls)."""
+        ZNET point.  Returns (final z, zstep, STEP_N, propagator calls).  device=True runs the
+        calls between ZNET points through gs_advance (the step controller on the device)."""
         cz = float(znet[0]); n_z = 0; step_n = 0; zstep = float(dz0); calls = 0
         nz = len(znet)
         while True:
@@ -411,6 +424,11 @@ class Propagator:
                 n_z += 1
             if steps is not None and calls >= steps:
                 break
+            if device:
+                left = (1 << 30) if steps is None else steps - calls
+                cz, zstep, step_n, k, _ = self.advance(znet, n_z, cz, zstep, step_n, left)
+                calls += k
+                continue
             zstep, step_n, _, _ = self.step(cz, znet[n_z], znet[n_z - 1], zstep, step_n)
             step_n += 1
             calls += 1

@@ -393,8 +393,12 @@ int gs_upload_tables(gs_handle* h, const gs_tables* t) {
 }
 
 static LstepArgs lstep_args(gs_handle* h, double dz) {
-    LstepArgs L;
+    LstepArgs L{};
     L.dz = dz;
+    if (h->ctl) {   // gs_advance: the accepted attempt's size, and no work for a rejected one
+        L.dz_dev = &h->ctl->dz_lin;
+        L.run = &h->ctl->accept;
+    }
     L.omega = h->omega;
     L.wavenum = h->wavenum;
     L.ho = h->ho;
@@ -687,6 +691,11 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
     fa.twb = (const T2*)h->twb;
     fa.max_out = h->max_dev;
     fa.threads = h->nl_threads;
+    if (h->ctl) {   // gs_advance: the attempt's size and the stop flag from the device
+        fa.dz_dev = &h->ctl->zstep;
+        fa.halt = &h->ctl->stop;
+        fa.ac_on = &h->ctl->field_compact;
+    }
     PlasmaArgs<Rl> pa = plasma_args<Rl>(h, raman, raman_scan);
     SpecArgs<Rl> sa{};
     sa.N = nt; sa.rows = nr; sa.u1 = U1; sa.u2 = U2; sa.u3 = U3;
@@ -736,7 +745,8 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
             s2.nbc = nbc;
             s2.cinv = cinv;
             s2.ncw = ncw;
-            if (h->a_compact) s2.ac = gs::qdht_tc_compact_y(h->tc, nullptr, &s2.cmap);   // nl_compact holds
+            // nl_compact holds; under gs_advance the device flag ac_on tells whether it is current
+            if (h->a_compact || (h->ctl && h->nl_compact)) s2.ac = gs::qdht_tc_compact_y(h->tc, nullptr, &s2.cmap);
             const bool tm = h->time_nl && !tape;
             if (tm) CK(h, cudaEventRecord(h->nl_ev[0], h->st));
             CK(h, launch_nl_stage<Rl>(f1, ps, A, s2, nr, h->st, &h->launches));

@@ -58,6 +58,13 @@ struct gs_handle {
     int all_stages = -1;      // fused path: all four stages per launch (1) or one per stage (0)
     int all_stages_thr = -1;  // ... decided for this nl_threads value
     int adj_stride = 0;   // checkpoint stride of the last gs_gradient
+    // gs_advance: the device-side z-loop state while its attempts are enqueued (null otherwise:
+    // the kernels then take the host's step sizes), ZNET on the device, per-attempt timing events
+    gs::DevCtl* ctl = nullptr;
+    gs::DevCtl* ctl_dev = nullptr;
+    double* znet_dev = nullptr;
+    int znet_cap = 0;
+    std::vector<cudaEvent_t> adv_ev;
     bool nbc_valid = false;   // the last NL step also wrote NB's window columns compactly (mixed)
     bool s_compact = false;   // BIGBUFFER2's window columns are current only in the plan's compact copy
     bool a_compact = false;   // FIELD is current only as the masked inverse's compact result

@@ -26,6 +26,12 @@ template <typename Rl> struct FftArgs {
                                              // prefetches into L2 the inputs of row + ahead
     int all_stages;                          // fused stage kernel: all four RK4 stages per launch
     double dzs;                              // ... with this step size (c dz per stage inside)
+    // steps controlled on the device (gs_advance, nl_row16k_kernel): the step size is *dz_dev
+    // instead of dzs, the launch does nothing while *halt != 0, and FIELD is read compactly
+    // (SpecArgs::ac) only while *ac_on != 0
+    const double* dz_dev;
+    const int* halt;
+    const int* ac_on;
 };
 
 template <typename Rl> struct PlasmaArgs {
@@ -218,7 +224,31 @@ struct LstepArgs {
     const double* ho;         // position order
     const double* kt2;        // [n_r]
     double omega_min, omega_max;
+    // steps controlled on the device (gs_advance, mixed wide plans): the linear step's size is
+    // *dz_dev instead of dz, and the transform does nothing while *run == 0 (a rejected attempt)
+    const double* dz_dev;
+    const int* run;
 };
+
+// The z-loop's state on the device (gs_advance): propagator()'s step-size controller
+// (propagator.cu:139-164) and the z-loop's bookkeeping (solver_main.cpp:202-225) run in a
+// one-thread kernel between each attempt's NL step and its linear step.
+struct DevCtl {
+    double z;            // CURRENT_Z
+    double zstep;        // ZSTEP: the next attempt's NL step size; after it, the new proposal
+    double dz_lin;       // the accepted attempt's linear-step size
+    unsigned step_n;     // STEP_N
+    int n_z;             // ZNET index of the next dump point
+    int calls, max_calls;   // accepted propagator() calls so far / at most
+    int stop;            // 0 running, 1 CURRENT_Z reached ZNET[n_z], 2 max_calls, 3 collapse, 4 NL error
+    int accept;          // the attempt in flight is accepted: its linear step runs
+    int field_compact;   // FIELD is the masked inverse's compact result
+    unsigned err;        // the NL error bits that stopped the loop
+    int iter;            // attempts of the current batch that ran
+    int acc_log[64];     // per attempt of the batch: accepted (its linear step ran)
+};
+cudaError_t launch_step_ctl(DevCtl* c, const double* znet, unsigned long long* max_dev, unsigned* err, double tol,
+                            int slot, cudaStream_t st, long long* nl);
 enum { QDHT_PLAIN = 0, QDHT_LSTEP = 1, QDHT_MASKED = 2 };
 // cmap[nc] / zpos[nz]: the spectral window's columns (padded to 64 with -1) and the positions
 // outside it; the linear-step and masked transforms then run on the window only (null: all)

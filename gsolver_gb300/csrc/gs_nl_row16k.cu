@@ -152,6 +152,7 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
     float* const rB = reinterpret_cast<float*>(smem_raw + OFF_RB);
     float* const wmx = reinterpret_cast<float*>(smem_raw + OFF_MX);
     int* const flag = reinterpret_cast<int*>(smem_raw + OFF_FLAG);
+    if (f.halt && *f.halt) return;   // gs_advance: the z-loop stopped (the whole CTA returns)
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
     const int row = blockIdx.x;
     const size_t base = (size_t)row * N;
@@ -187,12 +188,13 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
     const uint32_t tm = tslot + ((uint32_t)(32 * (w & 3)) << 16) + (uint32_t)(64 * (w >> 2));
 
     const float sc = 1.0f / (float)N;   // the inverse transform's 1/N, exact on 2^14 points
-    const float c_half = (float)(f.dzs * 0.5), c_full = (float)f.dzs;
+    const double dzs = f.dz_dev ? *f.dz_dev : f.dzs;
+    const float c_half = (float)(dzs * 0.5), c_full = (float)dzs;
 
     // ---- stage 0's input: FIELD (compact window columns or the full row) into tensor memory
     {
         float2 x[L];
-        const float* acr = sp.ac ? sp.ac + (size_t)row * sp.ncw : nullptr;
+        const float* acr = (sp.ac && !(f.ac_on && *f.ac_on == 0)) ? sp.ac + (size_t)row * sp.ncw : nullptr;
         if (acr) {   // the thread's positions from their window column pairs (zero outside)
             int cc[L];
 #pragma unroll

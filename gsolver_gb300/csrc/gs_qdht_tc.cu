@@ -83,6 +83,9 @@ struct TcArgs {
     const float* inv1ps;
     float* ylo;
     float dz_lo;
+    // gs_advance: the step size *dz_dev (instead of dz, dz_lo) and no work while *run == 0
+    const double* dz_dev;
+    const int* run;
 };
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -565,7 +568,9 @@ __global__ void __launch_bounds__(SPLIT_THREADS) qdht_split16_kernel(const float
                                                                      __half* __restrict__ XlT,
                                                                      float* __restrict__ xscale, int nr, int ncols,
                                                                      const int* __restrict__ kmax,
-                                                                     const int* __restrict__ cmap, int xcompact) {
+                                                                     const int* __restrict__ cmap, int xcompact,
+                                                                     const int* __restrict__ run) {
+    if (run && *run == 0) return;   // gs_advance: a rejected attempt
     extern __shared__ float strip[];   // [nr / 2][33]
     auto at = [](int j, int c) { return (j >> 1) * 33 + (j & 1) * 16 + c; };
     __shared__ float part[SPLIT_THREADS / SPLIT_COLS][SPLIT_COLS];
@@ -742,7 +747,8 @@ __device__ __forceinline__ void ff_cexp(ff2 x, ff2 y, ff2* re, ff2* im) {
 
 // 32 accumulator columns of row i starting at output column cg: a plain store or the fused
 // calculate_Lstep update of BIGBUFFER2 (propagator.cu:570-625)
-__device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, int cg, float kt2i) {
+__device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, int cg, float kt2i, float dzh,
+                                              float dzl) {
     float* yrow = a.Y + (size_t)i * a.ncols + cg;
     if (a.xscale) {   // FP16 operands: undo the row and column scales (exact: powers of two,
                       // applied one at a time so that their product cannot underflow)
@@ -789,7 +795,7 @@ __device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, 
         // before their arithmetic.
         const size_t nr = (size_t)a.nr;
         const size_t t0 = (size_t)(cg >> 1) * nr + i;
-        const ff2 dz{a.dz, a.dz_lo};
+        const ff2 dz{dzh, dzl};
         float* yh = a.Y + (size_t)i * a.nc + cg;
         float* yl = a.ylo + (size_t)i * a.nc + cg;
 #pragma unroll
@@ -821,8 +827,8 @@ __device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, 
                 }
                 ff2 pr, pi;
                 ff_cexp(ff_mul(dz, ff2{kk[u].x, kk[u].y}), ff_mul(dz, ff2{th[u].x, th[u].y}), &pr, &pi);
-                const ff2 br = ff_add(ff2{bh[2 * u], bl[2 * u]}, ff2{a.dz * v[2 * e] * inv[u], 0.f});
-                const ff2 bi = ff_add(ff2{bh[2 * u + 1], bl[2 * u + 1]}, ff2{a.dz * v[2 * e + 1] * inv[u], 0.f});
+                const ff2 br = ff_add(ff2{bh[2 * u], bl[2 * u]}, ff2{dzh * v[2 * e] * inv[u], 0.f});
+                const ff2 bi = ff_add(ff2{bh[2 * u + 1], bl[2 * u + 1]}, ff2{dzh * v[2 * e + 1] * inv[u], 0.f});
                 const ff2 fr = ff_add(ff_mul(br, pr), ff_neg(ff_mul(bi, pi)));
                 const ff2 fi = ff_add(ff_mul(br, pi), ff_mul(bi, pr));
                 oh[2 * u] = fr.h;
@@ -849,11 +855,11 @@ __device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, 
         const float sq = sqrt_ho_f(-kt2i / k1 / k1);
         float2 b2 = *y2;
         const float inv = 1.f / (1.f + sq);
-        b2.x += a.dz * v[2 * e] * inv;
-        b2.y += a.dz * v[2 * e + 1] * inv;
+        b2.x += dzh * v[2 * e] * inv;
+        b2.y += dzh * v[2 * e + 1] * inv;
         float sn, cs;
-        sincosf(a.dz * (-a.ho[p] - sq * k1), &sn, &cs);
-        const float m = expf(a.dz * k2);
+        sincosf(dzh * (-a.ho[p] - sq * k1), &sn, &cs);
+        const float m = expf(dzh * k2);
         const float pr = m * cs, pi = m * sn;
         float2 f;
         f.x = b2.x * pr - b2.y * pi;
@@ -1047,6 +1053,13 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
                                                                const __grid_constant__ CUtensorMap map_lo,
                                                                const __grid_constant__ CUtensorMap map_bh,
                                                                const __grid_constant__ CUtensorMap map_bl, TcArgs a) {
+    if (a.run && *a.run == 0) return;   // gs_advance: a rejected attempt (before any set-up)
+    float dzh = a.dz, dzl = a.dz_lo;
+    if (a.dz_dev) {
+        const double d = *a.dz_dev;
+        dzh = (float)d;
+        dzl = (float)(d - (double)dzh);
+    }
     extern __shared__ unsigned char smem_raw[];
     unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     uint64_t* bars = (uint64_t*)(smem + STAGES2 * STAGE2_BYTES);
@@ -1226,7 +1239,7 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
             }
             if (!ok) break;
             const float kt2i = a.kt2 ? a.kt2[i] : 0.f;
-            epilogue_cols(a, sum, i, c0 + 32 * part, kt2i);
+            epilogue_cols(a, sum, i, c0 + 32 * part, kt2i, dzh, dzl);
         }
         asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     }
@@ -1599,6 +1612,8 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
     a.inv1ps = nullptr;
     a.ylo = nullptr;
     a.dz_lo = (float)(L.dz - (double)(float)L.dz);
+    a.dz_dev = L.dz_dev;
+    a.run = L.run;
     if (q->wide) {
         // The linear step leaves BIGBUFFER2 untouched outside the spectral window and the masked
         // inverse transforms a zero column there: both run on the window's columns only (the
@@ -1639,7 +1654,8 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
         // of the inverse applied), then the GEMM on 128 x 256 tiles
         tc::qdht_split16_kernel<<<(unsigned)(a.nc / tc::SPLIT_COLS), tc::SPLIT_THREADS, (size_t)(q->nr / 2) * 33 * 4,
                                   q->st>>>(xc ? xsrc : X, (__half*)q->xhT, (__half*)q->xlT, q->xs, q->nr,
-                                           xc ? a.nc : a.ncols, mode == QDHT_MASKED ? q->kmax : nullptr, a.cmap, xc);
+                                           xc ? a.nc : a.ncols, mode == QDHT_MASKED ? q->kmax : nullptr, a.cmap, xc,
+                                           L.run);
         (*nlaunch)++;
         a.hscale = q->hs;
         a.xscale = q->xs;

@@ -137,6 +137,20 @@ int gs_qdht(gs_handle* h, double* data_r_omega);
 int gs_step(gs_handle* h, double current_z, double znet_cur, double znet_prev,
             double* zstep_inout, unsigned* step_n_inout, double* max_a2, double* max_nl2);
 
+/* The z-loop of solver_main.cpp:202-225 advanced by up to max_calls propagator() calls without
+ * a host round trip per call: each attempt's controller (propagator.cu:147-164: the error test,
+ * the new ZSTEP, the collapse and ZNET-clamp rules) and the loop's STEP_N / CURRENT_Z update run
+ * in a one-thread kernel between the NL step and the linear step, which take their step sizes
+ * from device memory.  Starts from CURRENT_Z = *current_z below ZNET[n_z] (the caller has done the
+ * dump test at the loop's top), ZSTEP = *zstep, STEP_N = *step_n; stops after the call that brings
+ * CURRENT_Z to ZNET[n_z] or beyond (*reached = 1: the caller dumps, advances n_z, calls again), or
+ * after max_calls calls (*reached = 0).  Results are those of the same calls through gs_step, bit
+ * for bit.  Grids whose NL step or linear step needs the host (other than the 16384-point FP32
+ * rows with the compact tensor-core plan; a photon-number tolerance; apertures) take gs_step call
+ * by call.  *calls_done = accepted calls; on GS_ERR_COLLAPSE *zstep is the collapsed proposal. */
+int gs_advance(gs_handle* h, const double* znet, int nz, int n_z, double* current_z, double* zstep,
+               unsigned* step_n, int max_calls, int* calls_done, int* reached);
+
 /* The handle's CUDA stream (a cudaStream_t), for callers that time or order work on it. */
 void* gs_stream(const gs_handle* h);
 
