@@ -195,12 +195,14 @@ int gs_advance(gs_handle* h, const double* znet, int nz, int n_z, double* curren
         dz = c.zstep;
         sn = c.step_n;
         done += c.calls;
+        // the state after the last accepted call (and, on a collapse, the collapsed proposal)
+        *current_z = cz;
+        *zstep = dz;
+        *step_n = sn;
+        if (calls_done) *calls_done = done;
         std::string m;
         if (gs::qdht_tc_check(h->tc, &m)) return gsi::fail(h, GS_ERR_CUDA, m);
-        if (c.stop == 3) {
-            *zstep = dz;
-            return gsi::fail(h, GS_ERR_COLLAPSE, gs_status_string(GS_ERR_COLLAPSE));
-        }
+        if (c.stop == 3) return gsi::fail(h, GS_ERR_COLLAPSE, gs_status_string(GS_ERR_COLLAPSE));
         if (c.stop == 4) {
             if (c.err & 1u) return gsi::fail(h, GS_ERR_BLAST, gs_status_string(GS_ERR_BLAST));
             return gsi::fail(h, GS_ERR_NAN, gs_status_string(GS_ERR_NAN));

@@ -7,6 +7,7 @@
 // Supported dump types (FILTER_TYPE NO): flux, maxI, field_axis, plasma_max,
 // average_spectrum, full (with NZ_DENOM).  DUMP_FILENAMEi may hold one %s, replaced by
 // DUMP_FILENAME_MOD (default empty) as the reference does.
+#include <algorithm>
 #include <chrono>
 #include <cstdio>
 #include <cstdlib>
@@ -195,11 +196,14 @@ extern "C" int gs_run_config(const char* config_path, const char* out_dir, int n
             n_z++;
         }
         if (max_calls >= 0 && calls >= max_calls) break;
-        rc = gs_step(h, cz, znet[n_z], znet[n_z - 1], &dz, &step_n, nullptr, nullptr);
+        // the calls up to the next ZNET point (or the call budget), the step controller on the
+        // device where the grid allows (gs_advance; else gs_step per call, the same results)
+        const long long left = max_calls >= 0 ? max_calls - calls : (1LL << 30);
+        int done = 0, reached = 0;
+        rc = gs_advance(h, znet.data(), nz, n_z, &cz, &dz, &step_n, (int)std::min<long long>(left, 1 << 30), &done,
+                        &reached);
+        calls += done;
         if (rc) { g_run_err = gs_last_error(h); break; }
-        step_n++;
-        calls++;
-        cz += dz;
     }
     const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     if (stats) {
