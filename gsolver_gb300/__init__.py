@@ -63,6 +63,7 @@ class Params(C.Structure):
         ("raman_fraction", C.c_double), ("n2", C.c_double),
         ("omega_min", C.c_double), ("omega_max", C.c_double), ("max_tolerance", C.c_double),
         ("raman_tau", C.c_double), ("raman_omega", C.c_double), ("th_coeff", C.c_double),
+        ("ion_levels", C.c_int), ("ion_potentials", C.c_double * 8),
     ]
 
 
@@ -174,6 +175,12 @@ class Propagator:
         p.raman_omega = float(setup.get("raman_omega", 0.0))
         p.gas = int(setup.get("gas", 0))
         p.th_coeff = float(setup.get("th_coeff", 0.0))
+        lv = int(setup.get("ion_levels", 1)) if p.gas else 1
+        p.ion_levels = lv
+        if lv > 1:
+            pots = np.asarray(setup["ion_potentials"], dtype=np.float64)
+            for i in range(lv):
+                p.ion_potentials[i] = float(pots[i])
         self.params = p
         h = C.c_void_p()
         rc = self.L.gs_create(C.byref(p), C.byref(h))
@@ -494,9 +501,11 @@ class Setup:
         def grab(ptr, n, dt=np.float64):
             return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(C.c_double)), shape=(n,)).copy().view(dt)
         d = {k: getattr(p, k) for k in PARAM_KEYS}
+        lv = max(1, p.ion_levels) if p.gas else 1
+        pots = np.array(list(p.ion_potentials)[:lv]) if lv > 1 else np.array([p.ionization_potential])
         d.update(n_r=nr, n_t=nt, rho0=p.rho0, raman_tau=p.raman_tau, raman_omega=p.raman_omega,
-                 gas=p.gas, th_coeff=p.th_coeff, ion_levels=1, ion_potentials=np.array([p.ionization_potential]))
-        d["rate_ln"] = grab(t.rate_ln, 8192)
+                 gas=p.gas, th_coeff=p.th_coeff, ion_levels=lv, ion_potentials=pots)
+        d["rate_ln"] = grab(t.rate_ln, 8192 * lv).reshape(lv, 8192) if lv > 1 else grab(t.rate_ln, 8192)
         d["plasma_func"] = grab(t.plasma_func, 2 * nt, np.complex128)
         d["raman_func"] = grab(t.raman_func, 2 * nt, np.complex128)
         d["kerr"] = grab(t.kerr, nt)

@@ -37,6 +37,7 @@ using gsi::permute_in;
 using gsi::permute_out;
 using gsi::lstep;
 using gsi::plasma_args;
+using gsi::ion_levels;
 
 int gsi::fail(gs_handle* h, int code, const std::string& msg) {
     if (h) h->err = msg; else g_create_error = msg;
@@ -117,6 +118,8 @@ int gs_create(const gs_params* prm, gs_handle** out) {
     const int nr = prm->n_r, nt = prm->n_t;
     if (nr < 1 || nt < 64 || (nt & (nt - 1))) return fail(nullptr, GS_ERR_UNSUPPORTED, "n_t must be a power of two >= 64, n_r >= 1");
     if (prm->precision != GS_PREC_FP64 && prm->precision != GS_PREC_MIXED) return fail(nullptr, GS_ERR_ARG, "precision");
+    if (prm->gas && (prm->ion_levels < 0 || prm->ion_levels > GS_MAX_ION_LEVELS))
+        return fail(nullptr, GS_ERR_ARG, "ion_levels out of range (0..8)");
     if (prm->gas && prm->th_coeff != 0 && prm->n2 != 0 && prm->raman_fraction > 0.001 &&
         !(prm->raman_tau > 0 && prm->raman_omega > 0))
         return fail(nullptr, GS_ERR_UNSUPPORTED,
@@ -145,7 +148,7 @@ int gs_create(const gs_params* prm, gs_handle** out) {
     ok = ok && al(&h->A, nel * h->esz) && al(&h->S, nel * h->esz) && al(&h->NB, nel * h->esz) &&
          al(&h->KP, nel * h->esz) && al(&h->E, nel * h->esz) && al(&h->U, 3 * nel * h->esz) &&
          al(&h->tw, (size_t)nt * h->esz) && al(&h->pf, (size_t)nt * h->esz) && al(&h->rm, (size_t)nt * h->esz) &&
-         al(&h->kerr, (size_t)nt * h->esz / 2) && al(&h->rate, 8192 * h->esz / 2) &&
+         al(&h->kerr, (size_t)nt * h->esz / 2) && al(&h->rate, 8192 * (size_t)ion_levels(h) * h->esz / 2) &&
          al((void**)&h->omega, nt * 8) && al((void**)&h->ho, nt * 8) && al((void**)&h->kt2, nr * 8) &&
          al((void**)&h->Cm, (size_t)nr * nr * 8) && al((void**)&h->m1, nr * 8) &&
          al((void**)&h->wavenum, nt * 16) && al((void**)&h->staging, nel * 16) &&
@@ -269,16 +272,16 @@ int gs_upload_tables(gs_handle* h, const gs_tables* t) {
         CK(h, up(h->pf, pf.data(), nt * 16));
         CK(h, up(h->rm, rm.data(), nt * 16));
         CK(h, up(h->kerr, ke.data(), nt * 8));
-        CK(h, up(h->rate, t->rate_ln, 8192 * 8));
+        CK(h, up(h->rate, t->rate_ln, 8192 * (size_t)ion_levels(h) * 8));
     } else {
         auto pf = permuted<float>(t->plasma_func, h->perm, 2);
         auto rm = permuted<float>(t->raman_func, h->perm, 2);
         auto ke = permuted<float>(t->kerr, h->perm, 1);
-        std::vector<float> rate(t->rate_ln, t->rate_ln + 8192);
+        std::vector<float> rate(t->rate_ln, t->rate_ln + 8192 * (size_t)ion_levels(h));
         CK(h, up(h->pf, pf.data(), nt * 8));
         CK(h, up(h->rm, rm.data(), nt * 8));
         CK(h, up(h->kerr, ke.data(), nt * 4));
-        CK(h, up(h->rate, rate.data(), 8192 * 4));
+        CK(h, up(h->rate, rate.data(), rate.size() * 4));
     }
     auto om = permuted<double>(t->omega, h->perm, 1);
     auto wn = permuted<double>(t->wavenum, h->perm, 2);
@@ -621,6 +624,8 @@ PlasmaArgs<Rl> gsi::plasma_args(gs_handle* h, bool raman, bool raman_scan) {
     pa.raman_scan = raman_scan;
     pa.shoot_exhaust = h->shoot_exhaust;
     pa.gas = h->p.gas;
+    pa.levels = ion_levels(h);
+    for (int n = 0; n < pa.levels && pa.levels > 1; n++) pa.pot[n] = h->p.ion_potentials[n];
     pa.th = (h->p.gas && h->p.th_coeff != 0) ? (const T2*)h->th : nullptr;
     if (raman_scan) {
         const double dt = h->p.tstep, tau = h->p.raman_tau, om = h->p.raman_omega;
@@ -663,8 +668,10 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
     const bool kerr_on = h->p.n2 != 0;
     // the oscillator recurrence replaces the RAMAN_FUNCTION FFT pair when its parameters are known
     const bool raman_scan = raman && kerr_on && h->p.raman_tau > 0 && h->p.raman_omega > 0;
-    // without Kerr the Raman response is never used: the fused stage applies
-    const bool fused = h->fused && (raman_scan || !raman || !kerr_on);
+    // without Kerr the Raman response is never used: the fused stage applies.  Several
+    // ionization levels take the staged kernels (plasma_kernel's level-by-level recurrence)
+    const bool multi = ion_levels(h) > 1;
+    const bool fused = h->fused && (raman_scan || !raman || !kerr_on) && !multi;
     {
         // the four-stage kernel of 16384-point FP32 rows reads FIELD compactly where the masked
         // inverse left it so; every other path reads A
@@ -702,7 +709,7 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
     sa.pf = (const T2*)h->pf; sa.rm = (const T2*)h->rm; sa.kerr = (const Rl*)h->kerr;
     sa.raman = raman && !raman_scan; sa.kerr_on = kerr_on; sa.nb = NB; sa.kp = KP; sa.max_out = h->max_dev + 1;
     if (tape && !fused) return fail(h, GS_ERR_UNSUPPORTED, "recording the RK4 stages needs rows that fit one CTA");
-    if (h->pair && !tape && (raman_scan || !raman || !kerr_on)) {   // rows over two CTAs (gs_nl_pair.cu)
+    if (h->pair && !tape && !multi && (raman_scan || !raman || !kerr_on)) {   // rows over two CTAs (gs_nl_pair.cu)
         pa.row_ion = h->row_ion;
         sa.row_ion = h->row_ion;
         for (int s = 0; s < 4; s++) {

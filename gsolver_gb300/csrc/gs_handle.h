@@ -125,6 +125,8 @@ int nl_stages(gs_handle* h, double dz, const GsTape* tape);
 // QDHT(NB) with the linear step into S, then A = QDHT(window S) (no host sync)
 int lstep(gs_handle* h, double dz);
 int permute_in(gs_handle* h, const double* host, void* dst);
+// ionization levels of the rate table (the gas build's IONIZATION_LEVEL_N; 1 otherwise)
+inline int ion_levels(const gs_handle* h) { return (h->p.gas && h->p.ion_levels > 1) ? h->p.ion_levels : 1; }
 int permute_out(gs_handle* h, const void* src, double* host);
 template <typename Rl> gs::PlasmaArgs<Rl> plasma_args(gs_handle* h, bool raman, bool raman_scan);
 // the Raman recurrence applies (oscillator parameters known, Kerr on)

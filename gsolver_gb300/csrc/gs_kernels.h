@@ -60,6 +60,10 @@ template <typename Rl> struct PlasmaArgs {
     // Kerr source (th[t] = (KERR_TH/KERR) exp(j phi_t), natural time order)
     int gas;
     const typename Vec2<Rl>::T* th;
+    // several ionization levels (the gas build's MULTI_LEVEL_IONIZATION, ionization.cpp:45-84):
+    // rate holds [levels][8192] rows, pot the levels' potentials (scaled as ionization_potential)
+    int levels;
+    double pot[8];
     // fused front kernel: per row, whether any sample ionizes (some W_t > 0) or rho starts
     // above 0; where not, the density stays exactly 0, loss and rho E are 0 and are not written
     int* row_ion;
@@ -67,6 +71,7 @@ template <typename Rl> struct PlasmaArgs {
     // converting a double on the device runs on the FP64 pipe, which is slow on this GPU
     struct Consts {
         Rl ND, invND, tstep, U, Pc, AV, invTAU, rho0, a_re, a_im, oma_re, oma_im, fRM, omf;
+        Rl pot[8];
     } k;
 };
 
@@ -86,6 +91,7 @@ template <typename Rl> inline void plasma_consts(PlasmaArgs<Rl>& pa) {
     pa.k.oma_im = (Rl)(-pa.aN_im);
     pa.k.fRM = (Rl)pa.fRM;
     pa.k.omf = (Rl)pa.one_minus_fR;
+    for (int n = 0; n < 8; n++) pa.k.pot[n] = (Rl)pa.pot[n];
 }
 
 // ---- adjoint of one RK4 stage's NL response (gs_nl_vjp.cu), rows that fit one CTA

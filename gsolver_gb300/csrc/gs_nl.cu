@@ -122,6 +122,168 @@ __global__ void __launch_bounds__(256) fft_cross_kernel(const C2<Rl>* __restrict
 }
 
 // ------------------------------------------------------------------- plasma ----
+// The gas build's MULTI_LEVEL_IONIZATION branch of calculate_plasmadensity_losses_small
+// (ionization.cpp:19-24, 45-84) for one row per CTA: per sample nt >= 1 whose predecessor is
+// above IONIZATION_MIN_I, level 0 takes a Heun step towards the neutral density and level n >= 1
+// one towards level n - 1 (already stepped), each clamped by what it moves towards; the density
+// is the levels' sum, the loss factor at sample nt - 1 sums -k1_n / 2 / dt (U_n + P I) / I over
+// the levels.  Level n's recurrence is scalar once level n - 1 is known along the row, so the
+// levels are solved in turn, each by the multiple shooting of the single-level recurrence
+// (Newton on the chunk starts, exact after chunks + 1 iterations).  Scratch per sample: U1 =
+// (table index or -1, ln-intensity offset), U3 = (level n's rate or -1, level n - 1's density);
+// U2 accumulates (loss factor, density).  Leaves U1 = loss E, U2 = density E (density in U2.x
+// when a.density_only).
+template <typename Rl>
+__device__ void plasma_levels(const PlasmaArgs<Rl>& a) {
+    using T2 = C2<Rl>;
+    __shared__ Rl s_start[256], sA[256], sB[256], red[64];
+    __shared__ int s_done;
+    const int N = a.N;
+    const size_t base = (size_t)blockIdx.x * N;
+    const T2* E = a.e + base;
+    T2* U1 = a.u1 + base;
+    T2* U2 = a.u2 + base;
+    T2* U3 = a.u3 + base;
+    Rl* u1 = reinterpret_cast<Rl*>(U1);   // scalar views: the x / y halves written apart
+    Rl* u2 = reinterpret_cast<Rl*>(U2);
+    Rl* u3 = reinterpret_cast<Rl*>(U3);
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const Rl ND = a.k.ND, tstep = a.k.tstep, Pc = a.k.Pc;
+    const Rl thr = (Rl)(1e13 / 1e16);
+    bool any = false;
+    for (int t = tid; t < N; t += nthr) {
+        Rl nn = -1, dl = 0;
+        if (t > 0) {
+            const T2 e = E[t];
+            const Rl I = e.x * e.x + e.y * e.y;
+            Rl d = 0;
+            const int n = photo_index<Rl>(I, &d, a.err);
+            if (n >= 0 && I > thr) {   // as the single-level slot: a step is taken from this sample
+                nn = (Rl)n;
+                dl = d;
+                any = true;
+            }
+        }
+        U1[t] = T2{nn, dl};
+        U2[t] = T2{(Rl)0, (Rl)0};
+        u3[2 * t + 1] = ND;   // level 0 moves towards the neutral density
+    }
+    const bool ion = __syncthreads_or(any ? 1 : 0) != 0;
+    const int P = min(nthr, N);
+    const int L = N / P;
+    const int c = tid;
+    const int lane = tid & 31, wid = tid >> 5;
+    const Rl tol = sizeof(Rl) == 8 ? (Rl)1e-13 : (Rl)1e-5;
+    for (int lv = 0; lv < (ion ? a.levels : 0); lv++) {
+        const Rl* tab = a.rate + (size_t)lv * 8192;
+        const Rl pot = a.k.pot[lv];
+        for (int t = tid; t < N; t += nthr) {   // level lv's rate per sample (-1: no step from it)
+            const Rl nn = u1[2 * t];
+            Rl W = -1;
+            if (nn >= 0) {
+                const int n = (int)nn;
+                W = photo_rate_from<Rl>(__ldg(&tab[n]), __ldg(&tab[n + 1]), u1[2 * t + 1]);
+            }
+            u3[2 * t] = W;
+        }
+        __syncthreads();
+        // the chunk of steps [c L, c L + L) from start s; write: the final pass (density,
+        // loss factor, this level's density as the next level's target)
+        auto run_chunk = [&](Rl s, bool write, Rl* dout) -> Rl {
+            Rl ro = s, d = 1;
+            const int nt0 = c * L;
+            Rl W0 = nt0 > 0 ? u3[2 * (nt0 - 1)] : (Rl)-1;
+            for (int i = 0; i < L; i++) {
+                const int nt = nt0 + i;
+                const Rl W1 = u3[2 * nt];
+                if (nt > 0) {
+                    const Rl src = u3[2 * nt + 1];
+                    const Rl r0 = ro;
+                    ro = gas_step<Rl>(ro, W0, W1, tstep, src, &d);
+                    if (write) {
+                        if (W0 >= 0) {   // k1 of this level's step: the loss at sample nt - 1
+                            Rl k1 = tstep * W0 * (src - r0);
+                            if (k1 < 0) k1 = 0;
+                            const T2 e = E[nt - 1];
+                            const Rl I0 = e.x * e.x + e.y * e.y;
+                            u2[2 * (nt - 1)] -= (Rl)0.5 * k1 / tstep * (pot + Pc * I0) / I0;
+                        }
+                        u2[2 * nt + 1] += ro;
+                        u3[2 * nt + 1] = ro;
+                    }
+                }
+                W0 = W1;
+            }
+            if (dout) *dout = d;
+            return ro;
+        };
+        if (c < P) s_start[c] = 0;
+        if (tid == 0) s_done = 0;
+        __syncthreads();
+        for (int it = 0; it < P + 1; it++) {
+            Rl A = 1, B = 0;
+            if (c < P) {
+                const Rl sc = s_start[c];
+                Rl D;
+                const Rl e = run_chunk(sc, false, &D);
+                A = D;
+                B = e - D * sc;
+            }
+            for (int o = 1; o < 32; o <<= 1) {
+                const Rl pa = __shfl_up_sync(0xffffffffu, A, o), pb = __shfl_up_sync(0xffffffffu, B, o);
+                if (lane >= o) { B = A * pb + B; A = A * pa; }
+            }
+            if (lane == 31) { sA[wid] = A; sB[wid] = B; }
+            __syncthreads();
+            if (wid == 0) {
+                const int nw = nthr >> 5;
+                Rl wa = lane < nw ? sA[lane] : (Rl)1, wb = lane < nw ? sB[lane] : (Rl)0;
+                for (int o = 1; o < 32; o <<= 1) {
+                    const Rl pa = __shfl_up_sync(0xffffffffu, wa, o), pb = __shfl_up_sync(0xffffffffu, wb, o);
+                    if (lane >= o) { wb = wa * pb + wb; wa = wa * pa; }
+                }
+                if (lane < nw) { sA[lane] = wa; sB[lane] = wb; }
+            }
+            __syncthreads();
+            if (wid > 0) {
+                const Rl pa = sA[wid - 1], pb = sB[wid - 1];
+                B = A * pb + B;
+                A = A * pa;
+            }
+            const Rl next = A * s_start[0] + B;   // the start of chunk c + 1
+            __syncthreads();
+            Rl change = 0, mag = 0;
+            if (c + 1 < P) {
+                change = fabs(next - s_start[c + 1]);
+                mag = fabs(next);
+                s_start[c + 1] = next;
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                change = fmax(change, __shfl_xor_sync(0xffffffffu, change, o));
+                mag = fmax(mag, __shfl_xor_sync(0xffffffffu, mag, o));
+            }
+            if (lane == 0) { red[wid] = change; red[32 + wid] = mag; }
+            __syncthreads();
+            if (tid == 0) {
+                Rl cm = 0, mm = 0;
+                for (int w = 0; w < (nthr >> 5); w++) { cm = fmax(cm, red[w]); mm = fmax(mm, red[32 + w]); }
+                s_done = (cm <= tol * mm && !a.shoot_exhaust) ? 1 : 0;
+            }
+            __syncthreads();
+            if (s_done) break;
+        }
+        if (c < P) run_chunk(s_start[c], true, nullptr);
+        __syncthreads();
+    }
+    for (int t = tid; t < N; t += nthr) {
+        const T2 e = E[t];
+        const Rl tl = ion ? u2[2 * t] : (Rl)0, rho = ion ? u2[2 * t + 1] : (Rl)0;
+        U1[t] = t < N - 1 ? T2{tl * e.x, tl * e.y} : T2{0, 0};
+        U2[t] = a.density_only ? T2{rho, (Rl)0} : T2{rho * e.x, rho * e.y};
+    }
+    __syncthreads();
+}
+
 // calculate_plasmadensity_losses_small (ionization.cpp:9-95), single-level branch, for
 // one row per CTA.  Inputs: E (time row).  Outputs: U1 = loss, U2 = rho*E,
 // U3 = |E|^2 (Raman on) or |E|^2 * E (Raman off).  The first recurrence step sees
@@ -138,11 +300,18 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
     T2* U3 = a.u3 + base;
     const int tid = threadIdx.x, nthr = blockDim.x;
     const Rl ND = a.k.ND, tstep = a.k.tstep, U = a.k.U, Pc = a.k.Pc, AV = a.k.AV;
+    // several ionization levels: density and loss by plasma_levels (U1 = loss E, U2 = rho E);
+    // the Kerr / Raman source below is common
+    const bool ml = a.levels > 1;
+    if (ml) {
+        plasma_levels<Rl>(a);
+        if (a.density_only) return;
+    }
 
     // phase A: W_t and the avalanche prefactor g_t = AV/(U + P I_t) * I_t (t >= 1)
     const bool gas = a.gas != 0;
     bool anyw = false;
-    for (int t = tid; t < N; t += nthr) {
+    for (int t = tid; t < N && !ml; t += nthr) {
         Rl W = 0, g = 0;
         if (t > 0) {
             T2 e = E[t];
@@ -158,7 +327,7 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
     }
     // no sample with W > 0 and rho starting at 0: every step adds exactly 0, the density
     // stays 0 along the row and the recurrence below is skipped
-    const bool ion = __syncthreads_or(anyw ? 1 : 0) != 0 || a.k.rho0 != (Rl)0;
+    const bool ion = (__syncthreads_or(anyw ? 1 : 0) != 0 || a.k.rho0 != (Rl)0) && !ml;
 
     // phase B: the Heun recurrence by multiple shooting.  Thread c owns the L consecutive
     // steps nt in [c L, c L + L); its start value s_c = rho_{cL-1} is refined by Newton
@@ -290,9 +459,11 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
     for (int t = tid; t < N; t += nthr) {
         T2 e = E[t];
         const Rl rho = ion ? U2[t].x : (Rl)0;
-        T2 w = U1[t];
+        T2 w = ml ? T2{0, 0} : U1[t];
         T2 loss = T2{0, 0};
-        if (gas) {
+        if (ml) {
+            // U1, U2 written by plasma_levels
+        } else if (gas) {
             // loss[t] = tl E_t (ionization.cpp:60-81), where sample t is above the threshold
             if (t < N - 1 && w.x >= 0) {
                 const Rl I0 = e.x * e.x + e.y * e.y;
@@ -308,8 +479,10 @@ __global__ void __launch_bounds__(256) plasma_kernel(PlasmaArgs<Rl> a) {
                 loss = T2{s * e.x, s * e.y};
             }
         }
-        U1[t] = loss;
-        U2[t] = T2{rho * e.x, rho * e.y};
+        if (!ml) {
+            U1[t] = loss;
+            U2[t] = T2{rho * e.x, rho * e.y};
+        }
         Rl I = e.x * e.x + e.y * e.y;
         if (!a.raman_scan) {
             T2 src = a.raman ? T2{I, (Rl)0} : T2{I * e.x - (Rl)0 * e.y, I * e.y + (Rl)0 * e.x};

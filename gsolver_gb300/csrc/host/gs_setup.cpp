@@ -289,9 +289,16 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
         if (cfg.f("NONLIN_REFRINDEX4", 0) != 0) throw std::string("NONLIN_REFRINDEX4 != 0 is not supported");
         if (cfg.s("TH_PROFILE", "NO") != "NO" || cfg.s("KERR_PROFILE", "NO") != "NO")
             throw std::string("KERR_PROFILE / TH_PROFILE files are not supported");
-        if ((int)cfg.f("IONIZATION_LEVEL_N", 1) != 1)
-            throw std::string("IONIZATION_LEVEL_N > 1 is not supported on the GPU path");
         th_coeff = (1 - cfg.f("RAMAN_FRACTION")) / 3.0 * cfg.f("TH_FACTOR", 1);
+    }
+    // MULTI_LEVEL_IONIZATION (ionization.cpp:45-84): IONIZATION_LEVEL_N levels, level n's
+    // potential by load_namednumfloat("IONIZATION_POTENTIAL", n + 1) (NAMEn, then NAME)
+    const int levels = gas ? (int)cfg.f("IONIZATION_LEVEL_N", 1) : 1;
+    if (levels < 1 || levels > GS_MAX_ION_LEVELS) throw std::string("IONIZATION_LEVEL_N out of range (1..8)");
+    std::vector<double> pots(levels);
+    for (int n = 0; n < levels; n++) {
+        const std::string k = "IONIZATION_POTENTIAL" + std::to_string(n + 1);
+        pots[n] = (cfg.raw(k.c_str()) ? cfg.f(k.c_str()) : cfg.f("IONIZATION_POTENTIAL")) * kE;
     }
     // load_namednumfloat("IONIZATION_POTENTIAL", 1) for the gas build: NAME1, then NAME
     const double Ui = (gas && cfg.raw("IONIZATION_POTENTIAL1") ? cfg.f("IONIZATION_POTENTIAL1")
@@ -334,8 +341,17 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
     // Keldysh table (top entry left at zero as in the reference)
     // entries are independent: spread them over the host's cores (each is computed exactly
     // as it would be alone)
-    std::vector<double> rate(8192, 0.0);
-    if (dev >= 0) {
+    std::vector<double> rate(8192 * (size_t)levels, 0.0);
+    if (levels > 1) {   // level 0 with PPT_Z, level n >= 1 with Z = n + 1 (ionization.cpp:313-331)
+        const int l = (int)cfg.f("PPT_L", 0);
+        for (int n = 0; n < levels; n++) {
+            const double Z = n == 0 ? cfg.f("PPT_Z", 1) : (double)(n + 1);
+            double* row = rate.data() + 8192 * (size_t)n;
+            parallel_for(8191, [&](int i, unsigned) {
+                row[i] = ppt_rate_ln(kMinLn + kTol * i, pots[n], Z, l, k0r, w0, vg) - kIonDenomGasLn;
+            });
+        }
+    } else if (dev >= 0) {
         if (gsi_dev_rate_table(dev, gas ? 1 : 0, k0r, Ui, w0, vg, mred, cfg.f("PPT_Z", 1), (int)cfg.f("PPT_L", 0),
                                gas ? kIonDenomGasLn : kIonDenomLn, kMinLn, kTol, rate.data(), &derr))
             throw "device set-up: " + derr;
@@ -457,6 +473,8 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
     p.ionrate_denom = ion_denom;
     p.gas = gas ? 1 : 0;
     p.th_coeff = th_coeff;
+    p.ion_levels = levels;
+    for (int n = 0; n < levels && levels > 1; n++) p.ion_potentials[n] = pots[n] * (ion_denom / kIntDenom);
     p.neutral_density = rho_n;
     p.rho0 = 0.0;   // AMBIENT_CARRIERS*2*frand() with AMBIENT_CARRIERS = 0
     p.ionization_potential = Ui * (ion_denom / kIntDenom);

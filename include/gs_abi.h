@@ -69,8 +69,9 @@ typedef struct gs_params {
     int device;                   /* CUDA device ordinal */
     int gas;                      /* 0: the solid build (gsolver_solid_qdht: Keldysh, avalanche,
                                      recombination); 1: the gas build (gsolver_gas_qdht,
-                                     Makefile:19: PPT rate table, single-level ionization with
-                                     neutral depletion, third harmonic, IONRATE_DENOM 1e10) */
+                                     Makefile:19: PPT rate tables, ionization with neutral
+                                     depletion over ion_levels levels, third harmonic,
+                                     IONRATE_DENOM 1e10) */
     double tstep, tmin, tmax, omega0;
     double ionrate_denom;         /* IONRATE_DENOM (1e20 for the solid build) */
     double neutral_density;       /* NEUTRAL_DENSITY */
@@ -88,11 +89,19 @@ typedef struct gs_params {
                                       recurrence instead of the RAMAN_FUNCTION FFT pair */
     double th_coeff;              /* gas build: KERR_TH_PROFILE / KERR_PROFILE = (1 - fR)/3
                                      TH_FACTOR (process_input.cpp:1020); 0: no third harmonic */
+    int ion_levels;               /* gas build: IONIZATION_LEVEL_N (0 or 1: one level, with
+                                     ionization_potential; up to GS_MAX_ION_LEVELS: the
+                                     MULTI_LEVEL_IONIZATION branch, ionization.cpp:45-84) */
+    double ion_potentials[8];     /* gas build with ion_levels > 1: IONIZATION_POTENTIALn of level
+                                     n - 1, scaled as ionization_potential */
 } gs_params;
+
+#define GS_MAX_ION_LEVELS 8
 
 /* Per-omega / per-k tables (host pointers, FP64, reference omega order). */
 typedef struct gs_tables {
-    const double* rate_ln;        /* IONIZATION_RATE_LN[8192] */
+    const double* rate_ln;        /* IONIZATION_RATE_LN[8192]; gas build with ion_levels > 1:
+                                     [ion_levels][8192], level n's row (ionization.cpp:313-331) */
     const double* plasma_func;    /* PLASMA_FUNC, complex [n_t] */
     const double* raman_func;     /* RAMAN_FUNCTION, complex [n_t] */
     const double* kerr;           /* KERR_PROFILE [n_t] */

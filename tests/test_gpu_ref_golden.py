@@ -80,3 +80,18 @@ def test_gas_single_level_matches_reference_golden():
     assert rel(P.get_nl(), g["l1_bb1"]) < TOL
     _check_run(P, S, g, "l1_", 3)
     P.close()
+
+
+def test_gas_two_levels_matches_reference_golden():
+    """IONIZATION_LEVEL_N 2 (MULTI_LEVEL_IONIZATION, ionization.cpp:45-84): the reference's own
+    NL step and three propagator() calls, on the staged kernels' level-by-level recurrence."""
+    g = np.load(os.path.join(HERE, "golden", "ref_argon_gas.npz"))
+    S = gs.Setup(_config(g["l2_config"], "argon")).as_dict()
+    assert S["gas"] == 1 and S["ion_levels"] == 2
+    P = gs.Propagator(S, precision=gs.PREC_FP64)
+    P.set_field(g["field0"])
+    a2, n2 = P.nl_step(float(g["l2_dz0"]))
+    assert rel(P.get_nl(), g["l2_bb1"]) < TOL
+    assert abs(n2 / float(g["l2_max_nl2"]) - 1) < TOL
+    _check_run(P, S, g, "l2_", 3)
+    P.close()

@@ -59,6 +59,23 @@ def test_product_setup_matches_oracle_gas_build():
     assert T["ionrate_denom"] == 1e10
 
 
+def test_product_setup_matches_oracle_with_three_levels():
+    """IONIZATION_LEVEL_N 3: the product's set-up builds one PPT row per level (level 0 with
+    PPT_Z, level n with Z = n + 1) and the levels' potentials as the oracle does."""
+    p, _ = _argon()
+    with open(p, "a") as fh:
+        fh.write("IONIZATION_LEVEL_N 3\nIONIZATION_POTENTIAL1 15.76\nIONIZATION_POTENTIAL2 27.63\n"
+                 "IONIZATION_POTENTIAL3 40.74\n")
+    T = tables.build(tables.Config.from_file(p), noise_seed=1, noise_sigma=1e-4)
+    S = gs.Setup(p, noise_seed=1, noise_sigma=1e-4).as_dict()
+    assert S["ion_levels"] == T["ion_levels"] == 3
+    rel = lambda a, b: float(np.linalg.norm(np.asarray(a) - b) / np.linalg.norm(b))
+    assert np.asarray(S["rate_ln"]).shape == (3, 8192)
+    for n in range(3):
+        assert rel(S["rate_ln"][n], T["rate_ln"][n]) < 1e-10, n
+    assert rel(S["ion_potentials"], T["ion_potentials"]) < 1e-15
+
+
 def test_third_harmonic_generates_the_third_harmonic():
     """A Kerr-only gas pulse: with the third-harmonic term the NL response has power near
     3 omega0 (inside the grid), without it none beyond the rounding floor."""
