@@ -826,6 +826,7 @@ int gsi::nl_stages(gs_handle* h, double dz, const GsTape* tape) {
 }
 
 static int nl_step(gs_handle* h, double dz, double* max_a2, double* max_nl2) {
+    gsi::Range r("gs nl_step");
     CK(h, cudaMemsetAsync(h->max_dev, 0, 16, h->st));
     CK(h, cudaMemsetAsync(h->err_dev, 0, 4, h->st));
     int rc = h->fp64 ? nl_step_impl<double>(h, dz) : nl_step_impl<float>(h, dz);
@@ -889,6 +890,7 @@ int gsi::spec_prepare(gs_handle* h) {
 }
 
 int gsi::lstep(gs_handle* h, double dz) {
+    gsi::Range r("gs lstep");
     // mixed wide plans keep BIGBUFFER2's window columns compact from step to step
     int rc = spec_prepare(h);
     if (rc) return rc;
@@ -935,6 +937,7 @@ int gs_step(gs_handle* h, double current_z, double znet_cur, double znet_prev, d
     if (!h || !zstep_inout) return GS_ERR_ARG;
     if (!h->tables_ok || !h->field_ok) return fail(h, GS_ERR_STATE, "tables / field not set");
     CK(h, cudaSetDevice(h->p.device));
+    gsi::Range r("gs_step");
     const double tol = h->p.max_tolerance;
     double zstep = *zstep_inout;
     for (;;) {

@@ -227,6 +227,7 @@ int stage_vjps(gs_handle* h, const AdjPtrs& P, const GsTape& tp, double dz) {
 
 // cotangents (A_bar, S_bar) after step -> before it; tp = the step's recorded stages
 int adjoint_step(gs_handle* h, const AdjPtrs& P, const GsTape& tp, double dz_rk, double dz_lin) {
+    gsi::Range r("gs adjoint_step");
     const size_t nel = (size_t)h->nr * h->nt;
     int rc = run_qdht_t(h, P.Ab, P.Fb);
     if (rc) return rc;

@@ -90,6 +90,7 @@ int gs_advance(gs_handle* h, const double* znet, int nz, int n_z, double* curren
     if (nz < 2 || n_z < 1 || n_z >= nz || max_calls < 0) return gsi::fail(h, GS_ERR_ARG, "gs_advance: bad ZNET index or call count");
     if (!h->tables_ok || !h->field_ok) return gsi::fail(h, GS_ERR_STATE, "tables / field not set");
     CK(h, cudaSetDevice(h->p.device));
+    gsi::Range range("gs_advance");
     int done = 0;
     if (calls_done) *calls_done = 0;
     if (reached) *reached = 0;

@@ -2,6 +2,7 @@
 // gs_abi.cu (forward) and gs_adjoint.cu (adjoint) share.  Private to the library.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <string>
 #include <vector>
@@ -125,6 +126,13 @@ int nl_stages(gs_handle* h, double dz, const GsTape* tape);
 // QDHT(NB) with the linear step into S, then A = QDHT(window S) (no host sync)
 int lstep(gs_handle* h, double dz);
 int permute_in(gs_handle* h, const double* host, void* dst);
+// an NVTX range over a scope (named phases in Nsight timelines; a no-op without a tool attached)
+struct Range {
+    explicit Range(const char* name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+    Range(const Range&) = delete;
+    Range& operator=(const Range&) = delete;
+};
 // ionization levels of the rate table (the gas build's IONIZATION_LEVEL_N; 1 otherwise)
 inline int ion_levels(const gs_handle* h) { return (h->p.gas && h->p.ion_levels > 1) ? h->p.ion_levels : 1; }
 int permute_out(gs_handle* h, const void* src, double* host);

@@ -55,6 +55,77 @@ __global__ void gg_time_kernel(double2* __restrict__ buf, const double* __restri
     }
 }
 
+// The per-omega tables, one thread per grid point i (the host build's formulas, gs_setup.cpp):
+// omega_i, n(omega_i) from the RAW table (the first bracketing interval, linear in |omega|),
+// k = conj(n) omega / c with the absorbing layer, HO dispersion with its two filters, the
+// plasma function, the Kerr profile, and the Raman function in closed form: the DFT of
+// h_m = fR M e^{-m dt / tau} sin(Omega m dt), m < N, is the geometric sum
+//     fR M / (2 j) [(1 - a^N) / (1 - a w^i) - (1 - conj(a)^N) / (1 - conj(a) w^i)],
+// a = e^{dt (-1 / tau + j Omega)}, w = e^{-2 pi j / N}, plus 1 - fR.
+__global__ void omega_tables_kernel(OmDevArgs a, const double* __restrict__ rw, const double* __restrict__ rn, int nraw,
+                                    double* __restrict__ wn, double* __restrict__ ho, double* __restrict__ pf,
+                                    double* __restrict__ rm, double* __restrict__ kerr) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nt) return;
+    const double om = i < a.nt / 2 ? a.w0 + a.wstep * i : a.w0 - a.wstep * (a.nt - i);
+    // refr_index: lower_bound of om in the sorted RAW frequencies
+    double nre = 1, nim = 0;
+    {
+        int lo = 0, hi = nraw;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (rw[mid] < om) lo = mid + 1;
+            else hi = mid;
+        }
+        int j = lo == 0 ? 1 : lo;
+        if (j < nraw && !((rw[j - 1] - om) * (rw[j] - om) > 0)) {
+            const double ren_ = a.P * (rn[2 * j - 2] - 1) + 1, imn_ = a.P * rn[2 * j - 1];
+            const double ren = a.P * (rn[2 * j] - 1) + 1, imn = a.P * rn[2 * j + 1];
+            nre = ren_ + (ren - ren_) * (fabs(om) - rw[j - 1]) / (rw[j] - rw[j - 1]);
+            nim = imn_ + (imn - imn_) * (fabs(om) - rw[j - 1]) / (rw[j] - rw[j - 1]);
+        }
+    }
+    double kr = nre * om / a.c, ki = -nim * om / a.c;
+    const double d = (om / a.wmax_grid - 1 - a.layer_w) / a.layer_w;
+    if (d > 0) ki = ki + (-kr) * (exp(a.layer_b) * d * d);
+    wn[2 * i] = kr;
+    wn[2 * i + 1] = ki;
+    const double h = (om / a.c) * (nre - a.ngr);
+    const double dh = (om / a.omax - 1) / a.layer_w;
+    const double hf = dh < 0 ? 1.0 : exp(-a.layer_b * dh * dh);
+    const double dl = om * (1 - a.layer_w) / a.omin - 1;
+    const double lf = dl > 0 ? 1.0 : exp(-a.layer_b * dl * dl);
+    ho[i] = h * (lf * hf);
+    // plasma function -(a / (1 + j a)) / 2 / k_r e^2 / m mu0, a = tau_c omega
+    {
+        const double x = a.tau_c * om, den = 1 + x * x;
+        const double s = 1.0 / 2.0 / kr * a.e * a.e / a.m * a.mu0;
+        pf[2 * i] = -(x / den) * s;
+        pf[2 * i + 1] = -(-x * x / den) * s;
+    }
+    kerr[i] = a.n2s * om / a.c / kr * om / a.c;
+    {
+        const double m1 = exp(-a.tstep / a.tauR), mN = exp(-(double)a.nt * a.tstep / a.tauR);
+        double s1, c1, sN, cN, sw, cw;
+        sincos(a.omR * a.tstep, &s1, &c1);
+        sincos(a.omR * a.tstep * a.nt, &sN, &cN);
+        sincospi(-2.0 * i / a.nt, &sw, &cw);
+        const double2 q = make_double2(m1 * c1, m1 * s1), qN = make_double2(mN * cN, mN * sN);
+        // (1 - q^N) / (1 - q w) and its conjugate-q twin
+        auto term = [&](double2 p, double2 pN) {
+            const double2 num = make_double2(1 - pN.x, -pN.y);
+            const double2 den = make_double2(1 - (p.x * cw - p.y * sw), -(p.x * sw + p.y * cw));
+            const double dd = den.x * den.x + den.y * den.y;
+            return make_double2((num.x * den.x + num.y * den.y) / dd, (num.y * den.x - num.x * den.y) / dd);
+        };
+        const double2 t1 = term(q, qN), t2 = term(make_double2(q.x, -q.y), make_double2(qN.x, -qN.y));
+        const double2 df = make_double2(t1.x - t2.x, t1.y - t2.y);
+        const double g = a.fR * a.M / 2;   // (1 / (2 j)) (x + j y) = (y - j x) / 2
+        rm[2 * i] = g * df.y + (1 - a.fR);
+        rm[2 * i + 1] = -g * df.x;
+    }
+}
+
 // FIELD = row(omega) exp(j ph) / FIELD_DENOM, ph = R^2 k_r / (2 f) - Cw (omega - omega0)^2 / 2
 __global__ void gg_phase_kernel(double2* __restrict__ field, const double2* __restrict__ row, const double* __restrict__ x,
                                 const double* __restrict__ kr, const double* __restrict__ om, GgDevArgs g) {
@@ -122,6 +193,28 @@ int gsi_dev_rate_table(int device, int gas, double k0, double U, double w0, doub
     gs::rate_table_kernel<<<(8191 + 127) / 128, 128>>>((double*)d.p, gas, k0, U, w0, vg, mred, Z, l, denom_ln, min_ln, tol);
     DCK(cudaGetLastError());
     DCK(cudaMemcpy(out8192, d.p, 8192 * sizeof(double), cudaMemcpyDeviceToHost));
+    return 0;
+}
+
+int gsi_dev_omega_tables(int device, const OmDevArgs& a, const double* raw_w, const double* raw_n, int nraw,
+                         double* wn, double* ho, double* pf, double* rm, double* kerr, std::string* err) {
+    DCK(cudaSetDevice(device));
+    const size_t nt = (size_t)a.nt;
+    DevBuf dout, draw;
+    DCK(cudaMalloc(&dout.p, nt * 8 * 8));   // wn (2), pf (2), rm (2), ho, kerr
+    DCK(cudaMalloc(&draw.p, (size_t)nraw * 3 * 8));
+    double* o = (double*)dout.p;
+    double* rw = (double*)draw.p;
+    DCK(cudaMemcpy(rw, raw_w, (size_t)nraw * 8, cudaMemcpyHostToDevice));
+    DCK(cudaMemcpy(rw + nraw, raw_n, (size_t)nraw * 16, cudaMemcpyHostToDevice));
+    gs::omega_tables_kernel<<<(unsigned)((nt + 255) / 256), 256>>>(a, rw, rw + nraw, nraw, o, o + 2 * nt, o + 3 * nt,
+                                                                  o + 5 * nt, o + 7 * nt);
+    DCK(cudaGetLastError());
+    DCK(cudaMemcpy(wn, o, nt * 16, cudaMemcpyDeviceToHost));
+    DCK(cudaMemcpy(ho, o + 2 * nt, nt * 8, cudaMemcpyDeviceToHost));
+    DCK(cudaMemcpy(pf, o + 3 * nt, nt * 16, cudaMemcpyDeviceToHost));
+    DCK(cudaMemcpy(rm, o + 5 * nt, nt * 16, cudaMemcpyDeviceToHost));
+    DCK(cudaMemcpy(kerr, o + 7 * nt, nt * 8, cudaMemcpyDeviceToHost));
     return 0;
 }
 

@@ -230,28 +230,34 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
     if (df[0] != '/') df = cfg.dir + "/" + df;
     const RawDisp rd = read_rawdisp(df);
     double omax = *std::max_element(rd.w.begin(), rd.w.end()), omin = *std::min_element(rd.w.begin(), rd.w.end());
-    // calculate_wavenumber
+    // calculate_wavenumber (the per-omega tables on the GPU when dev >= 0: below)
     std::vector<cd> n(nt), k(nt);
     const double wmax_grid = *std::max_element(om.begin(), om.end());
-    for (int i = 0; i < nt; i++) {
-        n[i] = refr_index(rd, om[i], P);
-        k[i] = std::conj(n[i]) * om[i] / kC;
-        const double d = (om[i] / wmax_grid - 1 - kLayerW) / kLayerW;
-        if (d > 0) k[i] = cd(k[i].real(), k[i].imag() + (-k[i].real()) * (std::exp(kLayerB) * d * d));
+    const double omax_raw = omax, omin_raw = omin;
+    if (dev < 0) {
+        for (int i = 0; i < nt; i++) {
+            n[i] = refr_index(rd, om[i], P);
+            k[i] = std::conj(n[i]) * om[i] / kC;
+            const double d = (om[i] / wmax_grid - 1 - kLayerW) / kLayerW;
+            if (d > 0) k[i] = cd(k[i].real(), k[i].imag() + (-k[i].real()) * (std::exp(kLayerB) * d * d));
+        }
     }
     const cd k0 = std::conj(refr_index(rd, w0, P)) * w0 / kC;
-    // calculate_HOdispersion (OMEGA0 == OMEGA[0])
-    const double n0 = n[0].real();
-    const double dndw = (n[1] - n[nt - 1]).real() / (om[1] - om[nt - 1]);
+    // calculate_HOdispersion (OMEGA0 == OMEGA[0]): the group index from n at OMEGA[0], OMEGA[1]
+    // and OMEGA[N_T - 1]
+    const double n0 = refr_index(rd, om[0], P).real();
+    const double dndw = (refr_index(rd, om[1], P) - refr_index(rd, om[nt - 1], P)).real() / (om[1] - om[nt - 1]);
     const double ngr = n0 + w0 * dndw;
     std::vector<double> ho(nt);
-    for (int i = 0; i < nt; i++) {
-        double h = (om[i] / kC) * (n[i].real() - ngr);
-        double dh = (om[i] / omax - 1) / kLayerW;
-        const double hf = dh < 0 ? 1.0 : std::exp(-kLayerB * dh * dh);
-        double dl = om[i] * (1 - kLayerW) / omin - 1;
-        const double lf = dl > 0 ? 1.0 : std::exp(-kLayerB * dl * dl);
-        ho[i] = h * (lf * hf);
+    if (dev < 0) {
+        for (int i = 0; i < nt; i++) {
+            double h = (om[i] / kC) * (n[i].real() - ngr);
+            double dh = (om[i] / omax - 1) / kLayerW;
+            const double hf = dh < 0 ? 1.0 : std::exp(-kLayerB * dh * dh);
+            double dl = om[i] * (1 - kLayerW) / omin - 1;
+            const double lf = dl > 0 ? 1.0 : std::exp(-kLayerB * dl * dl);
+            ho[i] = h * (lf * hf);
+        }
     }
     const double vg = kC / ngr;
     omax = std::min(omax, (1 - kLayerW) * om[nt / 2 - 1]);
@@ -330,7 +336,20 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
     const double aval = IBS * w0 * tau_c / (1 + w0 * tau_c * w0 * tau_c);
     const double pond = IBS / 2.0 / k0r / vg / (1.0 + 1.0 / (w0 * tau_c));
     std::vector<double> pf(2 * (size_t)nt), rm(2 * (size_t)nt), kerr(nt), wn(2 * (size_t)nt);
-    for (int i = 0; i < nt; i++) {
+    const double n2s = n2 * kIntDenom;
+    const double Mr = tstep * (1 + omR * omR * tauR * tauR) / tauR / (omR * tauR);
+    if (dev >= 0) {   // k, HO dispersion, plasma function, Raman function, Kerr profile on the GPU
+        OmDevArgs oa{};
+        oa.nt = nt; oa.w0 = w0; oa.wstep = wstep; oa.P = P; oa.wmax_grid = wmax_grid;
+        oa.omax = omax_raw; oa.omin = omin_raw; oa.ngr = ngr; oa.c = kC; oa.layer_w = kLayerW; oa.layer_b = kLayerB;
+        oa.tau_c = tau_c; oa.e = kE; oa.m = m; oa.mu0 = kMu0; oa.n2s = n2s;
+        oa.fR = fR; oa.M = Mr; oa.tauR = tauR; oa.omR = omR; oa.tstep = tstep;
+        if (gsi_dev_omega_tables(dev, oa, rd.w.data(), rd.n.data(), (int)rd.w.size(), wn.data(), ho.data(), pf.data(),
+                                 rm.data(), kerr.data(), &derr))
+            throw "device set-up: " + derr;
+        for (int i = 0; i < nt; i++) k[i] = cd(wn[2 * i], wn[2 * i + 1]);
+    }
+    for (int i = 0; i < nt && dev < 0; i++) {
         const double a = tau_c * om[i];
         const cd v = -(a / cd(1.0, a) / 2.0 / k[i].real() * kE * kE / m * kMu0);
         pf[2 * i] = v.real();
@@ -367,8 +386,8 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
         });
     }
     // Raman response
-    {
-        const double M = tstep * (1 + omR * omR * tauR * tauR) / tauR / (omR * tauR);
+    if (dev < 0) {
+        const double M = Mr;
         std::vector<cd> h(nt);
         for (int t = 0; t < nt; t++) {
             const double tt = tstep * t;
@@ -380,8 +399,7 @@ static void build(gs_setup* s, const Cfg& cfg, unsigned long long seed, double s
             rm[2 * i + 1] = h[i].imag();
         }
     }
-    const double n2s = n2 * kIntDenom;
-    for (int i = 0; i < nt; i++) kerr[i] = n2s * om[i] / kC / k[i].real() * om[i] / kC;
+    for (int i = 0; i < nt && dev < 0; i++) kerr[i] = n2s * om[i] / kC / k[i].real() * om[i] / kC;
 
     // create_gg
     double tau_fwhm = cfg.f("DURATION_FWHM", -1);

@@ -1,5 +1,6 @@
-"""Device-side set-up (gs_setup_from_config_dev: rate table, QDHT matrix and start field
-built on the GPU in FP64) against the host set-up and the oracle."""
+"""Device-side set-up (gs_setup_from_config_dev: rate table, QDHT matrix, the per-omega tables
+(wavenumber, HO dispersion, plasma function, Kerr profile, Raman function in closed form) and
+the start field built on the GPU in FP64) against the host set-up and the oracle."""
 import tempfile
 
 import numpy as np
@@ -33,8 +34,12 @@ def test_device_setup_matches_host(kind):
     assert rel(D["qdht_c"], H["qdht_c"]) < 5e-12
     assert rel(D["field"], H["field"]) < 1e-13
     assert abs(D["init_zstep"] - H["init_zstep"]) <= 1e-12 * H["init_zstep"]
-    for k in ("omega", "wavenum", "kerr", "plasma_func", "ho_disp", "kt2", "qdht_m1"):
+    for k in ("omega", "kt2", "qdht_m1"):   # host arithmetic on both paths
         assert np.array_equal(D[k], H[k]), k
+    # the per-omega tables: the same formulas with CUDA's exp and the Raman function's DFT as
+    # its geometric-sum closed form (the host takes an FFT of the response)
+    for k in ("wavenum", "kerr", "plasma_func", "ho_disp", "raman_func"):
+        assert rel(D[k], H[k]) < 1e-13, k
     if kind == "silica_c1":   # and the oracle
         T = tables.build(tables.Config.from_file(p), noise_seed=5, noise_sigma=1e-4)
         assert rel(D["field"], T["field"]) < 1e-13 and rel(D["rate_ln"], T["rate_ln"]) < 1e-12
