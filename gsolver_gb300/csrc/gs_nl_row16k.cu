@@ -38,7 +38,8 @@ constexpr int LOGN = 14;
 static_assert(N == NT * L, "one chunk of 16 per thread");
 
 // shared memory (bytes): E row (padded), rates W_t (padded), chunk starts of the density,
-// a^{16 j} (j < 1024), Raman warp totals and prefixes, density scan scratch, warp maxima, flag
+// a^{16 j} (j < 1024), Raman warp totals and prefixes, density scan scratch, warp maxima, the
+// twiddles of radix-16 pass 2, flag
 constexpr int OFF_E = 0;
 constexpr int OFF_W = OFF_E + (N + N / 16) * 8;
 constexpr int OFF_S = OFF_W + ((N + N / 32 + 1 + 3) & ~3) * 4;
@@ -48,7 +49,8 @@ constexpr int OFF_WPRE = OFF_WTOT + 32 * 8;
 constexpr int OFF_RA = OFF_WPRE + 32 * 8;
 constexpr int OFF_RB = OFF_RA + 32 * 4;
 constexpr int OFF_MX = OFF_RB + 32 * 4;
-constexpr int OFF_FLAG = OFF_MX + 32 * 4;
+constexpr int OFF_TW2 = OFF_MX + 32 * 4;   // w_64^{q r}, q = 1..3, r = 1..15 (45 complex)
+constexpr int OFF_FLAG = OFF_TW2 + 48 * 8;
 constexpr int SMEM = OFF_FLAG + 16;
 static_assert(SMEM + 16 <= 227 * 1024, "fits one CTA");
 
@@ -85,19 +87,38 @@ __device__ __forceinline__ void bar_group(int t) {
     asm volatile("bar.sync %0, 128;" ::"r"(1 + (t >> 7)) : "memory");
 }
 
+// x[r] *= w_64^{SIGN-sign q r}, r = 1..15, from the shared table of pass 2 (q = 1..3: a warp
+// reads four addresses, broadcast; forward values, conjugated for the inverse)
+template <int SIGN>
+__device__ __forceinline__ void tw64(float2* x, const float2* tw2, int q) {
+#pragma unroll
+    for (int r = 1; r < 16; r++) {
+        float2 w = tw2[(q - 1) * 15 + r - 1];
+        if (SIGN > 0) w.y = -w.y;
+        x[r] = cmul(x[r], w);
+    }
+}
+
 // One radix-16 pass of the 16384-point FFT, butterfly t of sub-problems of size S (the
-// fft_stage_ct butterfly: the same loads, twiddles from the stage's base rows, DFT and stores).
+// fft_stage_ct butterfly: the same loads, twiddles from the stage's base rows, DFT and stores);
+// the sub-problems of 64 (q < 4) take their twiddles from the shared table tw2.
 template <int SIGN, int S>
-__device__ __forceinline__ void pass16(float2* E, const float2* __restrict__ stb, int t) {
+__device__ __forceinline__ void pass16(float2* E, const float2* __restrict__ stb, int t, const float2* tw2 = nullptr) {
     constexpr int sub = S / 16;
     const int q = t & (sub - 1);
     float2* p = E + pad16((t / sub) * S + q);
     float2 x[16];
 #pragma unroll
     for (int r = 0; r < 16; r++) x[r] = p[pad16(sub * r)];
-    if (SIGN > 0 && q != 0) apply_tw16<SIGN, float>(x, stb, sub, q);
+    if (SIGN > 0 && q != 0) {
+        if constexpr (S == 64) tw64<SIGN>(x, tw2, q);
+        else apply_tw16<SIGN, float>(x, stb, sub, q);
+    }
     RegDFT<16, SIGN, float, float2>::run(x);
-    if (SIGN < 0 && q != 0) apply_tw16<SIGN, float>(x, stb, sub, q);
+    if (SIGN < 0 && q != 0) {
+        if constexpr (S == 64) tw64<SIGN>(x, tw2, q);
+        else apply_tw16<SIGN, float>(x, stb, sub, q);
+    }
 #pragma unroll
     for (int r = 0; r < 16; r++) p[pad16(sub * r)] = x[r];
 }
@@ -106,9 +127,9 @@ __device__ __forceinline__ void pass16(float2* E, const float2* __restrict__ stb
 __device__ __forceinline__ const float2* stage_base(const float2* twb, int j) { return twb + tw_base_offset(LOGN, j); }
 
 // inverse transform after the radix-4 pass: every thread has written its 16 positions
-__device__ __forceinline__ void inverse_rest(float2* E, const float2* __restrict__ twb, int t) {
+__device__ __forceinline__ void inverse_rest(float2* E, const float2* __restrict__ twb, int t, const float2* tw2) {
     __syncwarp();                                  // pass 2 reads the quad's positions
-    pass16<+1, 64>(E, stage_base(twb, 2), t);
+    pass16<+1, 64>(E, stage_base(twb, 2), t, tw2);
     bar_group(t);                                  // pass 1 reads the 4-warp group's
     pass16<+1, 1024>(E, stage_base(twb, 1), t);
     __syncthreads();                               // pass 0 reads the whole row
@@ -117,12 +138,12 @@ __device__ __forceinline__ void inverse_rest(float2* E, const float2* __restrict
 }
 
 // forward transform up to the radix-4 pass (the caller synchronised the row before)
-__device__ __forceinline__ void forward_head(float2* E, const float2* __restrict__ twb, int t) {
+__device__ __forceinline__ void forward_head(float2* E, const float2* __restrict__ twb, int t, const float2* tw2) {
     pass16<-1, 16384>(E, stage_base(twb, 0), t);
     __syncthreads();
     pass16<-1, 1024>(E, stage_base(twb, 1), t);
     bar_group(t);
-    pass16<-1, 64>(E, stage_base(twb, 2), t);
+    pass16<-1, 64>(E, stage_base(twb, 2), t, tw2);
     __syncwarp();                                  // the radix-4 pass reads the quad's positions
 }
 
@@ -151,6 +172,7 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
     float* const rA = reinterpret_cast<float*>(smem_raw + OFF_RA);
     float* const rB = reinterpret_cast<float*>(smem_raw + OFF_RB);
     float* const wmx = reinterpret_cast<float*>(smem_raw + OFF_MX);
+    float2* const tw2 = reinterpret_cast<float2*>(smem_raw + OFF_TW2);
     int* const flag = reinterpret_cast<int*>(smem_raw + OFF_FLAG);
     if (f.halt && *f.halt) return;   // gs_advance: the z-loop stopped (the whole CTA returns)
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -181,6 +203,12 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
             b = cmul(b, b);
         }
         apw[t] = pr;
+    }
+    if (t < 45) {   // w_64^{q r} = exp(-2 pi i q r / 64), rounded once from FP64
+        const int q = 1 + t / 15, r = 1 + t % 15;
+        double sn, cs;
+        sincospi(-2.0 * (double)(q * r) / 64.0, &sn, &cs);
+        tw2[t] = make_float2((float)cs, (float)sn);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -251,7 +279,7 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
 #pragma unroll 1
     for (int s = 0; s < 4; s++) {
         // ---- E = IFFT(stage input) / N (propagator.cu:386-396, 640-641)
-        inverse_rest(E, twb, t);
+        inverse_rest(E, twb, t, tw2);
 
         // ---- one pass over the thread's samples: rates W_t (the first sample is taken as
         // E_0 = 0: W_0 = 0) and the Raman chunk sum; groups of 8 samples, whose table reads are
@@ -502,7 +530,7 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
                 for (int i = 0; i < L; i++) Ec[i] = y[i];
                 __syncthreads();
             }
-            forward_head(E, twb, t);
+            forward_head(E, twb, t, tw2);
             if (j != lastj) {
                 float4* keep = reinterpret_cast<float4*>((j == 0 ? sp.u3 : sp.u1) + base);
 #pragma unroll
