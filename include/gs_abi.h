@@ -22,6 +22,8 @@
  *   gs_qdht                       <- ht_run(f_complex*, f_complex*) (solver.h:337-346)
  *                                    -> qdht_plan::run_many (fhatha.cpp:218-230)
  *   gs_step                       <- propagator() (solver.h:269, propagator.cu:125-266)
+ *   gs_advance                    <- the z-loop's propagator() calls between ZNET points
+ *                                    (solver_main.cpp:202-225), the controller on the device
  *   gs_destroy                    <- destroy_variables()/cuda_free_const()
  *                                    (solver_main.cpp:415-440)
  *   gs_energy                     <- dump_type_average_spectrum_class (dump_types.cpp:427-457)
@@ -37,7 +39,7 @@
 extern "C" {
 #endif
 
-#define GS_ABI_VERSION 1
+#define GS_ABI_VERSION 2   /* 2: gs_params gained ion_levels / ion_potentials */
 
 typedef struct gs_handle gs_handle;
 
