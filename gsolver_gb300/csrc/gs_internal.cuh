@@ -78,6 +78,24 @@ __device__ __forceinline__ T2 twc(T2 v, int k) {
     return r;
 }
 
+// The butterfly (e + t, e - t).  For FP32 pairs each is one packed instruction (add / sub
+// .rn.f32x2): the same two correctly rounded results as the scalar form, half the issue slots.
+template <typename T2> __device__ __forceinline__ void bfly(T2& a, T2& b, T2 e, T2 t) {
+    a = cadd(e, t);
+    b = csub(e, t);
+}
+#if defined(__CUDA_ARCH__)
+template <> __device__ __forceinline__ void bfly<float2>(float2& a, float2& b, float2 e, float2 t) {
+    unsigned long long re, rt, ra, rb;
+    re = (unsigned long long)__float_as_uint(e.x) | ((unsigned long long)__float_as_uint(e.y) << 32);
+    rt = (unsigned long long)__float_as_uint(t.x) | ((unsigned long long)__float_as_uint(t.y) << 32);
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(ra) : "l"(re), "l"(rt));
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rb) : "l"(re), "l"(rt));
+    a = make_float2(__uint_as_float((unsigned)ra), __uint_as_float((unsigned)(ra >> 32)));
+    b = make_float2(__uint_as_float((unsigned)rb), __uint_as_float((unsigned)(rb >> 32)));
+}
+#endif
+
 // In-register radix-2 decimation-in-time DFT of size R (1,2,4,8,16), natural order in/out.
 template <int R, int SIGN, typename Rl, typename T2> struct RegDFT {
     static __device__ __forceinline__ void run(T2* x) {
@@ -87,11 +105,7 @@ template <int R, int SIGN, typename Rl, typename T2> struct RegDFT {
         RegDFT<R / 2, SIGN, Rl, T2>::run(e);
         RegDFT<R / 2, SIGN, Rl, T2>::run(o);
 #pragma unroll
-        for (int k = 0; k < R / 2; k++) {
-            T2 t = twc<R, SIGN, Rl>(o[k], k);
-            x[k] = cadd(e[k], t);
-            x[k + R / 2] = csub(e[k], t);
-        }
+        for (int k = 0; k < R / 2; k++) bfly(x[k], x[k + R / 2], e[k], twc<R, SIGN, Rl>(o[k], k));
     }
 };
 template <int SIGN, typename Rl, typename T2> struct RegDFT<1, SIGN, Rl, T2> {

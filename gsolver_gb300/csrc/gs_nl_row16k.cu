@@ -13,8 +13,10 @@
 //     thread's own samples, as in the general fused kernel (gs_nl_fused.cu).
 // The RK4 sum k1 + 2 k2 + 2 k3 and the row's A (FIELD at the step's start) live in tensor
 // memory (tcgen05.st / ld), 32 columns each per thread: k of stages 0-2 never leaves the SM.
-// The FFT arithmetic (radix-16 butterflies, per-stage twiddle bases, radix-4 butterflies)
-// is that of the shared-memory FFT in gs_internal.cuh; only the work assignment differs.
+// The FFT arithmetic (radix-16 butterflies, radix-4 butterflies) is that of the shared-memory
+// FFT in gs_internal.cuh; the twiddles of pass 0 come from its per-stage base rows, those of
+// passes 1 and 2 (w_1024^{q r}, w_64^{q r}: 960 and 45 values) from tables in shared memory,
+// each value rounded once from FP64.
 //
 // The Raman response (solver_main.cpp:401-413, propagator.cu:694-705) is the one-pole
 // recurrence z_t = a z_{t-1} + I_t; the Kerr factor needs Im(v_t) for
@@ -39,7 +41,7 @@ static_assert(N == NT * L, "one chunk of 16 per thread");
 
 // shared memory (bytes): E row (padded), rates W_t (padded), chunk starts of the density,
 // a^{16 j} (j < 1024), Raman warp totals and prefixes, density scan scratch, warp maxima, the
-// twiddles of radix-16 pass 2, flag
+// twiddles of radix-16 passes 2 and 1, flag
 constexpr int OFF_E = 0;
 constexpr int OFF_W = OFF_E + (N + N / 16) * 8;
 constexpr int OFF_S = OFF_W + ((N + N / 32 + 1 + 3) & ~3) * 4;
@@ -50,7 +52,8 @@ constexpr int OFF_RA = OFF_WPRE + 32 * 8;
 constexpr int OFF_RB = OFF_RA + 32 * 4;
 constexpr int OFF_MX = OFF_RB + 32 * 4;
 constexpr int OFF_TW2 = OFF_MX + 32 * 4;   // w_64^{q r}, q = 1..3, r = 1..15 (45 complex)
-constexpr int OFF_FLAG = OFF_TW2 + 48 * 8;
+constexpr int OFF_TW1 = OFF_TW2 + 48 * 8;  // w_1024^{q r}, r = 1..15, q = 0..63 ([r - 1][q])
+constexpr int OFF_FLAG = OFF_TW1 + 15 * 64 * 8;
 constexpr int SMEM = OFF_FLAG + 16;
 static_assert(SMEM + 16 <= 227 * 1024, "fits one CTA");
 
@@ -99,11 +102,24 @@ __device__ __forceinline__ void tw64(float2* x, const float2* tw2, int q) {
     }
 }
 
+// x[r] *= w_1024^{SIGN-sign q r}, r = 1..15, from the shared table of pass 1 (a warp reads 32
+// consecutive entries per r)
+template <int SIGN>
+__device__ __forceinline__ void tw1024(float2* x, const float2* tw1, int q) {
+#pragma unroll
+    for (int r = 1; r < 16; r++) {
+        float2 w = tw1[(r - 1) * 64 + q];
+        if (SIGN > 0) w.y = -w.y;
+        x[r] = cmul(x[r], w);
+    }
+}
+
 // One radix-16 pass of the 16384-point FFT, butterfly t of sub-problems of size S (the
 // fft_stage_ct butterfly: the same loads, twiddles from the stage's base rows, DFT and stores);
-// the sub-problems of 64 (q < 4) take their twiddles from the shared table tw2.
+// the sub-problems of 64 (q < 4) and of 1024 (q < 64) take their twiddles from the shared
+// tables tws (tw2, tw1).
 template <int SIGN, int S>
-__device__ __forceinline__ void pass16(float2* E, const float2* __restrict__ stb, int t, const float2* tw2 = nullptr) {
+__device__ __forceinline__ void pass16(float2* E, const float2* __restrict__ stb, int t, const float2* tws = nullptr) {
     constexpr int sub = S / 16;
     const int q = t & (sub - 1);
     float2* p = E + pad16((t / sub) * S + q);
@@ -111,12 +127,14 @@ __device__ __forceinline__ void pass16(float2* E, const float2* __restrict__ stb
 #pragma unroll
     for (int r = 0; r < 16; r++) x[r] = p[pad16(sub * r)];
     if (SIGN > 0 && q != 0) {
-        if constexpr (S == 64) tw64<SIGN>(x, tw2, q);
+        if constexpr (S == 64) tw64<SIGN>(x, tws, q);
+        else if constexpr (S == 1024) tw1024<SIGN>(x, tws, q);
         else apply_tw16<SIGN, float>(x, stb, sub, q);
     }
     RegDFT<16, SIGN, float, float2>::run(x);
     if (SIGN < 0 && q != 0) {
-        if constexpr (S == 64) tw64<SIGN>(x, tw2, q);
+        if constexpr (S == 64) tw64<SIGN>(x, tws, q);
+        else if constexpr (S == 1024) tw1024<SIGN>(x, tws, q);
         else apply_tw16<SIGN, float>(x, stb, sub, q);
     }
 #pragma unroll
@@ -127,23 +145,25 @@ __device__ __forceinline__ void pass16(float2* E, const float2* __restrict__ stb
 __device__ __forceinline__ const float2* stage_base(const float2* twb, int j) { return twb + tw_base_offset(LOGN, j); }
 
 // inverse transform after the radix-4 pass: every thread has written its 16 positions
-__device__ __forceinline__ void inverse_rest(float2* E, const float2* __restrict__ twb, int t, const float2* tw2) {
+__device__ __forceinline__ void inverse_rest(float2* E, const float2* __restrict__ twb, int t, const float2* tw2,
+                                             const float2* tw1) {
     __syncwarp();                                  // pass 2 reads the quad's positions
-    pass16<+1, 64>(E, stage_base(twb, 2), t, tw2);
+    pass16<+1, 64>(E, nullptr, t, tw2);
     bar_group(t);                                  // pass 1 reads the 4-warp group's
-    pass16<+1, 1024>(E, stage_base(twb, 1), t);
+    pass16<+1, 1024>(E, nullptr, t, tw1);
     __syncthreads();                               // pass 0 reads the whole row
     pass16<+1, 16384>(E, stage_base(twb, 0), t);
     __syncthreads();
 }
 
 // forward transform up to the radix-4 pass (the caller synchronised the row before)
-__device__ __forceinline__ void forward_head(float2* E, const float2* __restrict__ twb, int t, const float2* tw2) {
+__device__ __forceinline__ void forward_head(float2* E, const float2* __restrict__ twb, int t, const float2* tw2,
+                                             const float2* tw1) {
     pass16<-1, 16384>(E, stage_base(twb, 0), t);
     __syncthreads();
-    pass16<-1, 1024>(E, stage_base(twb, 1), t);
+    pass16<-1, 1024>(E, nullptr, t, tw1);
     bar_group(t);
-    pass16<-1, 64>(E, stage_base(twb, 2), t, tw2);
+    pass16<-1, 64>(E, nullptr, t, tw2);
     __syncwarp();                                  // the radix-4 pass reads the quad's positions
 }
 
@@ -173,6 +193,7 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
     float* const rB = reinterpret_cast<float*>(smem_raw + OFF_RB);
     float* const wmx = reinterpret_cast<float*>(smem_raw + OFF_MX);
     float2* const tw2 = reinterpret_cast<float2*>(smem_raw + OFF_TW2);
+    float2* const tw1 = reinterpret_cast<float2*>(smem_raw + OFF_TW1);
     int* const flag = reinterpret_cast<int*>(smem_raw + OFF_FLAG);
     if (f.halt && *f.halt) return;   // gs_advance: the z-loop stopped (the whole CTA returns)
     const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -209,6 +230,10 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
         double sn, cs;
         sincospi(-2.0 * (double)(q * r) / 64.0, &sn, &cs);
         tw2[t] = make_float2((float)cs, (float)sn);
+    }
+    if (t < 15 * 64) {   // w_1024^{q r} = w_16384^{16 q r} from the row's table (16 q r < 16384)
+        const int q = t & 63, r = 1 + (t >> 6);
+        tw1[t] = __ldg(f.tw + 16 * q * r);
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -279,7 +304,7 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
 #pragma unroll 1
     for (int s = 0; s < 4; s++) {
         // ---- E = IFFT(stage input) / N (propagator.cu:386-396, 640-641)
-        inverse_rest(E, twb, t, tw2);
+        inverse_rest(E, twb, t, tw2, tw1);
 
         // ---- one pass over the thread's samples: rates W_t (the first sample is taken as
         // E_0 = 0: W_0 = 0) and the Raman chunk sum; groups of 8 samples, whose table reads are
@@ -530,7 +555,7 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
                 for (int i = 0; i < L; i++) Ec[i] = y[i];
                 __syncthreads();
             }
-            forward_head(E, twb, t, tw2);
+            forward_head(E, twb, t, tw2, tw1);
             if (j != lastj) {
                 float4* keep = reinterpret_cast<float4*>((j == 0 ? sp.u3 : sp.u1) + base);
 #pragma unroll
@@ -618,17 +643,21 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
                     tv[2 * i] = k[i].x;
                     tv[2 * i + 1] = k[i].y;
                 }
-                if (s > 0) {   // k1, then + 2 k2, + 2 k3 in that order
+                if (s > 0) {   // k1, then + 2 k2, + 2 k3 in that order (2 tv exact: one rounding)
 #pragma unroll
-                    for (int i = 0; i < 8; i++) tv[i] = sum[i] + 2.0f * tv[i];
+                    for (int i = 0; i < 4; i++) {
+                        const float2 r = __ffma2_rn(make_float2(2.0f, 2.0f), make_float2(tv[2 * i], tv[2 * i + 1]),
+                                                    make_float2(sum[2 * i], sum[2 * i + 1]));
+                        tv[2 * i] = r.x;
+                        tv[2 * i + 1] = r.y;
+                    }
                 }
                 tst8(tm + 8 * g, tv);
                 float2 x[4];   // the next stage's input (A + c dz k) / N, as a stage load forms it
 #pragma unroll
-                for (int i = 0; i < 4; i++) {
-                    float xr = av[2 * i] + cnext * k[i].x, xi = av[2 * i + 1] + cnext * k[i].y;
-                    x[i] = make_float2(xr * sc, xi * sc);
-                }
+                for (int i = 0; i < 4; i++)
+                    x[i] = __fmul2_rn(__ffma2_rn(make_float2(cnext, cnext), k[i], make_float2(av[2 * i], av[2 * i + 1])),
+                                      make_float2(sc, sc));
                 radix4<+1>(x);
 #pragma unroll
                 for (int i = 0; i < 4; i++) Ec[4 * g + i] = x[i];
@@ -686,7 +715,7 @@ cudaError_t nl_row16k_setup() {
 
 cudaError_t launch_nl_row16k(FftArgs<float> f, PlasmaArgs<float> a, const float2* A, SpecArgs<float> s, int rows,
                              int ahead, cudaStream_t st, long long* nl) {
-    if (f.N != r16k::N || !f.twb || a.tape_e || (s.ac && !s.cinv) || (s.nbc && !s.cinv)) return cudaErrorInvalidValue;
+    if (f.N != r16k::N || !f.twb || !f.tw || a.tape_e || (s.ac && !s.cinv) || (s.nbc && !s.cinv)) return cudaErrorInvalidValue;
     f.rows = rows;
     f.ahead = ahead;
     r16k::nl_row16k_kernel<<<rows, r16k::NT, r16k::SMEM, st>>>(f, a, A, s);
