@@ -175,11 +175,11 @@ def new_state(S):
 
 # Per field point of one launch on the 1024 x 16384 workload, from ncu captures of that
 # workload (dram__bytes_read.sum + dram__bytes_write.sum, smsp__inst_executed.sum and
-# sm__inst_issued.avg.pct_of_peak_sustained_active of one launch, divided by its n_r n_t field
+# smsp__issue_active.avg.pct_of_peak_sustained_active of one launch, divided by its n_r n_t field
 # points); they are fixed properties of the kernels, re-measured whenever a kernel changes.
 NCU_PER_POINT = {
-    "nl_row16k": {"dram_bytes": 11.44, "warp_instructions": 33.4, "issue_active": 0.623},
-    "qdht_pair": {"dram_bytes": None},
+    "nl_row16k": {"dram_bytes": 10.61, "warp_instructions": 30.2, "issue_active": 0.589},
+    "qdht_pair": {"dram_bytes": 9.13},
 }
 
 
