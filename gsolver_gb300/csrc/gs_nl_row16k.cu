@@ -225,11 +225,9 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
         }
         apw[t] = pr;
     }
-    if (t < 45) {   // w_64^{q r} = exp(-2 pi i q r / 64), rounded once from FP64
+    if (t < 45) {   // w_64^{q r} = w_16384^{256 q r} from the row's table (256 q r < 16384)
         const int q = 1 + t / 15, r = 1 + t % 15;
-        double sn, cs;
-        sincospi(-2.0 * (double)(q * r) / 64.0, &sn, &cs);
-        tw2[t] = make_float2((float)cs, (float)sn);
+        tw2[t] = __ldg(f.tw + 256 * q * r);
     }
     if (t < 15 * 64) {   // w_1024^{q r} = w_16384^{16 q r} from the row's table (16 q r < 16384)
         const int q = t & 63, r = 1 + (t >> 6);
