@@ -9,7 +9,8 @@ Synthetic: the pulse is generated (seeded 1e-4 complex Gaussian noise), no datas
 
   value   device throughput (inputs resident in HBM), CUDA events on the handle's stream
   e2e     the same metric through the public C ABI with pinned host buffers: every step
-          copies FIELD and BIGBUFFER2 in and out (the host globals propagator() works on)
+          copies FIELD and BIGBUFFER2 in and out (the host globals propagator() works on),
+          gs_step_host (BIGBUFFER2's copy in overlapping the NL attempt)
   fp64    the plain FP64 GPU path on the same workload, and the mixed path's relative L2
           error against it after 5, 100, 1000 and 2000 fixed-dz steps from the same start
   roofline  the dominant kernel, nl_row16k_kernel (the four RK4 stages of every row in one
@@ -568,21 +569,42 @@ def main():
             "gpu_launches": launches, "roofline": roof, "roofline_qdht": roof_q,
             "clocks": clk.summary()}
 
-    # e2e through the public API with pinned host buffers
+    # e2e through the public API with pinned host buffers: propagator() on host-resident FIELD
+    # and BIGBUFFER2 (gs_step_host: both in, one call's attempts, both out); also the same
+    # through three calls (gs_set_field + gs_advance + gs_get_field), without the overlap
     if not args.no_e2e:
         f_h = torch.empty((nr, nt), dtype=torch.complex128, pin_memory=True)
         s_h = torch.empty((nr, nt), dtype=torch.complex128, pin_memory=True)
         P.get_field_ptr(f_h.data_ptr(), s_h.data_ptr())
         ke = max(2, min(args.steps, 10))
+        znet = S["znet"]
+
+        def host_call():
+            if state["z"] >= znet[state["n_z"]]:
+                if state["n_z"] == len(znet) - 1:
+                    raise RuntimeError("workload ran past its last ZNET point")
+                state["n_z"] += 1
+            n_z = state["n_z"]
+            zstep, step_n = P.step_host(f_h.data_ptr(), s_h.data_ptr(), state["z"], znet[n_z], znet[n_z - 1],
+                                        state["zstep"], state["step_n"])
+            state.update(z=state["z"] + zstep, zstep=zstep, step_n=step_n + 1)
+
         t0 = time.perf_counter()
+        for _ in range(ke):
+            host_call()
+        te = time.perf_counter() - t0
+        t1 = time.perf_counter()
         for _ in range(ke):
             P.set_field_ptr(f_h.data_ptr(), s_h.data_ptr())
             run_z_steps(P, S, state, 1)
             P.get_field_ptr(f_h.data_ptr(), s_h.data_ptr())
-        te = time.perf_counter() - t0
+        t3 = time.perf_counter() - t1
         line["e2e"] = {"value": nr * nt * ke / te, "unit": UNIT, "h2d_bytes_per_step": 2 * nr * nt * 16,
                        "d2h_bytes_per_step": 2 * nr * nt * 16, "steps": ke,
-                       "api": "gs_set_field(FIELD, BIGBUFFER2) + gs_step + gs_get_field(FIELD, BIGBUFFER2)"}
+                       "api": "gs_step_host (propagator() on host FIELD and BIGBUFFER2: both copied in and out "
+                              "every call, pinned)",
+                       "three_calls_value": nr * nt * ke / t3,
+                       "three_calls_api": "gs_set_field + gs_advance (one call) + gs_get_field"}
 
     # FP64 path on the same workload + mixed-vs-FP64 field error after the same fixed-dz steps
     if prec == gs.PREC_MIXED and args.fp64_steps > 0:

@@ -29,7 +29,7 @@ PREC_FP64, PREC_MIXED = 0, 1
 # every function declared in include/gs_abi.h
 ABI_FUNCTIONS = (
     "gs_create", "gs_upload_tables", "gs_set_field", "gs_get_field", "gs_nl_step", "gs_get_nl",
-    "gs_lstep", "gs_qdht", "gs_step", "gs_advance", "gs_stream", "gs_launch_count", "gs_qdht_timing", "gs_nl_timing",
+    "gs_lstep", "gs_qdht", "gs_step", "gs_step_host", "gs_advance", "gs_stream", "gs_launch_count", "gs_qdht_timing", "gs_nl_timing",
     "gs_destroy",
     "gs_last_error", "gs_status_string",
     # include/gs_setup.h
@@ -102,6 +102,7 @@ def load_library(path: str | None = None):
     L.gs_lstep.argtypes = [V, D]
     L.gs_qdht.argtypes = [V, V]
     L.gs_step.argtypes = [V, D, D, D, PD, C.POINTER(C.c_uint), PD, PD]
+    L.gs_step_host.argtypes = [V, V, V, D, D, D, PD, C.POINTER(C.c_uint), PD, PD]
     L.gs_advance.argtypes = [V, V, C.c_int, C.c_int, PD, PD, C.POINTER(C.c_uint), C.c_int, C.POINTER(C.c_int),
                              C.POINTER(C.c_int)]
     L.gs_stream.argtypes = [V]
@@ -264,6 +265,15 @@ class Propagator:
         self._check(self.L.gs_step(self.h, float(current_z), float(znet_cur), float(znet_prev),
                                    C.byref(dz), C.byref(sn), C.byref(a2), C.byref(n2)))
         return dz.value, sn.value, a2.value, n2.value
+
+    def step_host(self, field_ptr, spec_ptr, current_z, znet_cur, znet_prev, zstep, step_n=0):
+        """gs_step_host: one propagator() call on host FIELD / BIGBUFFER2 buffers (raw pointers to
+        [n_r][n_t] complex128, e.g. pinned), taken in and given back.  Returns (ZSTEP, STEP_N)."""
+        dz = C.c_double(zstep)
+        sn = C.c_uint(step_n)
+        self._check(self.L.gs_step_host(self.h, C.c_void_p(field_ptr), C.c_void_p(spec_ptr), float(current_z),
+                                        float(znet_cur), float(znet_prev), C.byref(dz), C.byref(sn), None, None))
+        return dz.value, sn.value
 
     def advance(self, znet, n_z, current_z, zstep, step_n=0, max_calls=1 << 30):
         """gs_advance: up to max_calls propagator() calls from CURRENT_Z below ZNET[n_z], the step

@@ -110,6 +110,9 @@ static void free_all(gs_handle* h) {
     if (h->st) cudaStreamDestroy(h->st);
     for (cudaEvent_t e : h->nl_ev)
         if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : h->io_ev)
+        if (e) cudaEventDestroy(e);
+    if (h->io_st) cudaStreamDestroy(h->io_st);
 }
 
 int gs_create(const gs_params* prm, gs_handle** out) {
@@ -516,6 +519,7 @@ static void* pinned_device_ptr(const void* host, size_t bytes) {
 
 int gsi::permute_in(gs_handle* h, const double* host, void* dst) {
     const size_t nel = (size_t)h->nr * h->nt;
+    if (const int rc = spec_in_finish(h)) return rc;   // the staging buffer is free again
     if (dst == h->S) spec_written(h);
     if (dst == h->A) field_written(h);
     // mixed plans keep BIGBUFFER2's window columns as a double-float pair: an FP64 spectrum
@@ -546,6 +550,7 @@ int gsi::permute_in(gs_handle* h, const double* host, void* dst) {
 }
 int gsi::permute_out(gs_handle* h, const void* src, double* host) {
     const size_t nel = (size_t)h->nr * h->nt;
+    if (const int rc = spec_in_finish(h)) return rc;
     if (src == h->S) {
         const int rc = spec_sync(h);
         if (rc) return rc;
@@ -866,6 +871,7 @@ int gs_nl_step(gs_handle* h, double zstep, double* max_a2, double* max_nl2) {
 }
 
 int gsi::spec_sync(gs_handle* h) {
+    if (const int rc = spec_in_finish(h)) return rc;
     if (!h->s_compact) return GS_OK;
     CK(h, gs::qdht_tc_spec_copy(h->tc, (float*)h->S, 0, &h->launches));   // S stays current, the copy too
     return GS_OK;
@@ -882,7 +888,26 @@ int gsi::field_sync(gs_handle* h) {
 
 void gsi::field_written(gs_handle* h) { h->a_compact = false; }
 
+// BIGBUFFER2 of gs_step_host: the handle's stream waits for its copy into the staging buffer,
+// then takes it as permute_in does for a staged copy (position order, and the double-float
+// window columns of a mixed plan)
+int gsi::spec_in_finish(gs_handle* h) {
+    if (!h->spec_in_pending) return GS_OK;
+    h->spec_in_pending = false;
+    const size_t nel = (size_t)h->nr * h->nt;
+    CK(h, cudaStreamWaitEvent(h->st, h->io_ev[1], 0));
+    cudaError_t e = h->fp64 ? launch_permute<double>(+1, h->staging, h->S, h->perm_dev, h->nt, nel, h->st, &h->launches)
+                            : launch_permute<float>(+1, h->staging, h->S, h->perm_dev, h->nt, nel, h->st, &h->launches);
+    CK(h, e);
+    if (!h->fp64 && h->tc && gs::qdht_tc_has_compact(h->tc)) {
+        CK(h, gs::qdht_tc_spec_ff(h->tc, (double*)h->staging, h->perm_dev, 1, &h->launches));
+        h->s_compact = true;
+    }
+    return GS_OK;
+}
+
 int gsi::spec_prepare(gs_handle* h) {
+    if (const int rc = spec_in_finish(h)) return rc;
     if (h->s_compact || h->fp64 || !h->tc || !gs::qdht_tc_has_compact(h->tc)) return GS_OK;
     CK(h, gs::qdht_tc_spec_copy(h->tc, (float*)h->S, 1, &h->launches));
     h->s_compact = true;
@@ -986,6 +1011,37 @@ int gs_step(gs_handle* h, double current_z, double znet_cur, double znet_prev, d
             return collect_qdht_time(h);
         }
     }
+}
+
+int gs_step_host(gs_handle* h, double* field, double* spec, double current_z, double znet_cur, double znet_prev,
+                 double* zstep_inout, unsigned* step_n_inout, double* max_a2, double* max_nl2) {
+    if (!h || !field || !spec || !zstep_inout) return fail(h, GS_ERR_ARG, "null argument");
+    if (!h->tables_ok) return fail(h, GS_ERR_STATE, "tables not uploaded");
+    CK(h, cudaSetDevice(h->p.device));
+    gsi::Range r("gs_step_host");
+    if (!h->io_st) {
+        CK(h, cudaStreamCreateWithFlags(&h->io_st, cudaStreamNonBlocking));
+        for (cudaEvent_t& e : h->io_ev) CK(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    }
+    // FIELD first (the NL attempt reads nothing else), then BIGBUFFER2 on the copy stream into
+    // the staging buffer while the attempt runs; the linear step takes it (spec_in_finish)
+    int rc = gsi::permute_in(h, field, h->A);
+    if (rc) return rc;
+    gsi::spec_written(h);
+    CK(h, cudaEventRecord(h->io_ev[0], h->st));
+    CK(h, cudaStreamWaitEvent(h->io_st, h->io_ev[0], 0));
+    CK(h, cudaMemcpyAsync(h->staging, spec, (size_t)h->nr * h->nt * 16, cudaMemcpyHostToDevice, h->io_st));
+    CK(h, cudaEventRecord(h->io_ev[1], h->io_st));
+    h->spec_in_pending = true;
+    h->field_ok = true;
+    h->en_prev = 0;
+    rc = gs_step(h, current_z, znet_cur, znet_prev, zstep_inout, step_n_inout, max_a2, max_nl2);
+    const int rf = gsi::spec_in_finish(h);   // a failed call still leaves BIGBUFFER2 installed
+    if (rc) return rc;
+    if (rf) return rf;
+    rc = gsi::permute_out(h, h->S, spec);
+    if (!rc) rc = gsi::permute_out(h, h->A, field);
+    return rc;
 }
 
 int gs_selftest_bounded_wait(gs_handle* h, double limit_s) {

@@ -22,6 +22,8 @@
  *   gs_qdht                       <- ht_run(f_complex*, f_complex*) (solver.h:337-346)
  *                                    -> qdht_plan::run_many (fhatha.cpp:218-230)
  *   gs_step                       <- propagator() (solver.h:269, propagator.cu:125-266)
+ *   gs_step_host                  <- propagator() on the host FIELD / BIGBUFFER2 globals (the copies in
+ *                                    and out the call makes, overlapped with its first NL attempt)
  *   gs_advance                    <- the z-loop's propagator() calls between ZNET points
  *                                    (solver_main.cpp:202-225), the controller on the device
  *   gs_destroy                    <- destroy_variables()/cuda_free_const()
@@ -147,6 +149,15 @@ int gs_qdht(gs_handle* h, double* data_r_omega);
  * reference does); max_a2 / max_nl2 (may be NULL) of the accepted attempt. */
 int gs_step(gs_handle* h, double current_z, double znet_cur, double znet_prev,
             double* zstep_inout, unsigned* step_n_inout, double* max_a2, double* max_nl2);
+
+/* gs_step on host-resident state: the reference's propagator() works on the host globals FIELD
+ * and BIGBUFFER2 (solver.h:169), so a drop-in call takes them in, steps, and gives them back.
+ * Equivalent to gs_set_field(field, spec) + gs_step(...) + gs_get_field(field, spec), bit for
+ * bit; FIELD goes in first and BIGBUFFER2's copy in (on a copy stream) overlaps the first NL
+ * attempt, which reads FIELD only.  field / spec: [n_r][n_t] complex, in and out (pinned
+ * memory for the full host-link rate). */
+int gs_step_host(gs_handle* h, double* field_r_omega, double* spec_k_omega, double current_z, double znet_cur,
+                 double znet_prev, double* zstep_inout, unsigned* step_n_inout, double* max_a2, double* max_nl2);
 
 /* The z-loop of solver_main.cpp:202-225 advanced by up to max_calls propagator() calls without
  * a host round trip per call: each attempt's controller (propagator.cu:147-164: the error test,
