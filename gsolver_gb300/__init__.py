@@ -20,7 +20,8 @@ import os
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "_build", "libgsolver_gb300.so")
+# GS_CHECK=1 in the environment at import: the GS_CHECK build (python -m gsolver_gb300.build --check)
+LIB_PATH = os.path.join(HERE, "_build_check" if os.environ.get("GS_CHECK") == "1" else "_build", "libgsolver_gb300.so")
 
 GS_OK, GS_ERR_ARG, GS_ERR_CUDA, GS_ERR_BLAST, GS_ERR_NAN, GS_ERR_COLLAPSE = 0, 1, 2, 3, 4, 5
 GS_ERR_STATE, GS_ERR_UNSUPPORTED, GS_ERR_NOMEM = 6, 7, 8
@@ -42,7 +43,7 @@ ABI_FUNCTIONS = (
     "gs_batch_destroy", "gs_autotune", "gs_set_nl_threads", "gs_get_nl_threads", "gs_batch_autotune",
     "gs_set_apertures", "gs_setup_apertures", "gs_setup_from_config_dev",
     "gs_energy", "gs_set_energy_tolerance", "gs_energy_stats", "gs_checkpoint_save", "gs_checkpoint_load",
-    "gs_selftest_bounded_wait",
+    "gs_selftest_bounded_wait", "gs_check_build", "gs_selftest_bounds",
 )
 
 
@@ -142,6 +143,8 @@ def load_library(path: str | None = None):
     L.gs_setup_apertures.argtypes = [V, C.POINTER(C.c_int), V, V]
     L.gs_energy.argtypes = [V, V, D, PD, PD]
     L.gs_selftest_bounded_wait.argtypes = [V, D]
+    L.gs_check_build.argtypes = []
+    L.gs_selftest_bounds.argtypes = [V]
     L.gs_set_energy_tolerance.argtypes = [V, D, V, D]
     L.gs_energy_stats.argtypes = [V, PD, C.POINTER(C.c_longlong)]
     L.gs_checkpoint_save.argtypes = [V, C.c_char_p, D, D, I, C.c_uint]
@@ -368,6 +371,11 @@ class Propagator:
         """gs_selftest_bounded_wait: raises GsError (GS_ERR_CUDA, 'wait expired') when the bounded
         waits report as they should."""
         self._check(self.L.gs_selftest_bounded_wait(self.h, float(limit_s)))
+
+    def selftest_bounds(self):
+        """gs_selftest_bounds: raises GsError (GS_ERR_CUDA, 'index out of bounds') in a GS_CHECK
+        build whose index test reports as it should (GS_ERR_UNSUPPORTED in other builds)."""
+        self._check(self.L.gs_selftest_bounds(self.h))
 
     def nl_threads(self, threads=None):
         """Read, or set (0: default), the fused kernels' threads per row."""

@@ -858,6 +858,7 @@ static int nl_step(gs_handle* h, double dz, double* max_a2, double* max_nl2) {
     if (max_a2) *max_a2 = a2;
     if (max_nl2) *max_nl2 = n2;
     // an overflowing stage input can turn into NaN in later RK4 stages: the blast comes first
+    if (err & gs::GS_ERRBIT_BOUNDS) return fail(h, GS_ERR_CUDA, gs::GS_BOUNDS_MSG);
     if (err & 1u) return fail(h, GS_ERR_BLAST, gs_status_string(GS_ERR_BLAST));
     if (err & 2u) return fail(h, GS_ERR_NAN, gs_status_string(GS_ERR_NAN));
     return GS_OK;
@@ -1044,6 +1045,35 @@ int gs_step_host(gs_handle* h, double* field, double* spec, double current_z, do
     return rc;
 }
 
+#if GS_CHECK
+// buf has more than len + 1 elements: the tested index len is inside the allocation
+__global__ void bounds_probe_kernel(float* buf, int len, unsigned* err) {
+    const int idx = len;
+    if (gs::in_bounds(idx < len, err)) buf[idx] = 1.f;
+}
+#endif
+
+int gs_check_build(void) { return GS_CHECK ? 1 : 0; }
+
+int gs_selftest_bounds(gs_handle* h) {
+    if (!h) return GS_ERR_ARG;
+#if GS_CHECK
+    CK(h, cudaSetDevice(h->p.device));
+    CK(h, cudaMemsetAsync(h->err_dev, 0, 4, h->st));
+    bounds_probe_kernel<<<1, 1, 0, h->st>>>(reinterpret_cast<float*>(h->staging), 1, h->err_dev);
+    h->launches++;
+    CK(h, cudaGetLastError());
+    unsigned err = 0;
+    CK(h, cudaMemcpyAsync(&err, h->err_dev, 4, cudaMemcpyDeviceToHost, h->st));
+    CK(h, cudaStreamSynchronize(h->st));
+    CK(h, cudaMemsetAsync(h->err_dev, 0, 4, h->st));
+    if (err & gs::GS_ERRBIT_BOUNDS) return fail(h, GS_ERR_CUDA, gs::GS_BOUNDS_MSG);
+    return fail(h, GS_ERR_STATE, "gs_selftest_bounds: the index test did not report");
+#else
+    return fail(h, GS_ERR_UNSUPPORTED, "gs_selftest_bounds: built without GS_CHECK");
+#endif
+}
+
 int gs_selftest_bounded_wait(gs_handle* h, double limit_s) {
     if (!h || !(limit_s > 0) || limit_s > 1.0) return fail(h, GS_ERR_ARG, "gs_selftest_bounded_wait: 0 < limit <= 1 s");
     if (!h->tc) return fail(h, GS_ERR_UNSUPPORTED, "gs_selftest_bounded_wait: mixed handles only");
@@ -1199,6 +1229,7 @@ static int dump_impl(gs_handle* h, const double* qdht_x, double r_max, double* m
     }
     if (avg_spectrum)
         for (int p = 0; p < nt; p++) avg_spectrum[h->perm[p]] = spec_pos[p];
+    if (err & gs::GS_ERRBIT_BOUNDS) return fail(h, GS_ERR_CUDA, gs::GS_BOUNDS_MSG);
     if (err & 1u) return fail(h, GS_ERR_BLAST, gs_status_string(GS_ERR_BLAST));
     if (err & 2u) return fail(h, GS_ERR_NAN, gs_status_string(GS_ERR_NAN));
     return GS_OK;

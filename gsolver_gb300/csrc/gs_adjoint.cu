@@ -263,6 +263,7 @@ int read_err(gs_handle* h) {
         if (h->tc && gs::qdht_tc_check(h->tc, &m)) return gsi::fail(h, GS_ERR_CUDA, m);
         if (h->tcT && gs::qdht_tc_check(h->tcT, &m)) return gsi::fail(h, GS_ERR_CUDA, m);
     }
+    if (err & GS_ERRBIT_BOUNDS) return gsi::fail(h, GS_ERR_CUDA, GS_BOUNDS_MSG);
     if (err & 1u) return gsi::fail(h, GS_ERR_BLAST, gs_status_string(GS_ERR_BLAST));
     if (err & 2u) return gsi::fail(h, GS_ERR_NAN, gs_status_string(GS_ERR_NAN));
     return GS_OK;

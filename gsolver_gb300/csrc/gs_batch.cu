@@ -178,6 +178,7 @@ int gs_batch_step(gs_batch* b, int n_steps, const double* dz, int use_graph) {
             std::string m;
             if (gs::qdht_tc_check(h->tc, &m)) return bfail(b, GS_ERR_CUDA, "pulse " + std::to_string(i) + ": " + m);
         }
+        if (err & gs::GS_ERRBIT_BOUNDS) return bfail(b, GS_ERR_CUDA, "pulse " + std::to_string(i) + ": " + gs::GS_BOUNDS_MSG);
         if (err & 1u) return bfail(b, GS_ERR_BLAST, "pulse " + std::to_string(i) + ": " + gs_status_string(GS_ERR_BLAST));
         if (err & 2u) return bfail(b, GS_ERR_NAN, "pulse " + std::to_string(i) + ": " + gs_status_string(GS_ERR_NAN));
     }

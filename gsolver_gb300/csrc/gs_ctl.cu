@@ -205,6 +205,7 @@ int gs_advance(gs_handle* h, const double* znet, int nz, int n_z, double* curren
         if (gs::qdht_tc_check(h->tc, &m)) return gsi::fail(h, GS_ERR_CUDA, m);
         if (c.stop == 3) return gsi::fail(h, GS_ERR_COLLAPSE, gs_status_string(GS_ERR_COLLAPSE));
         if (c.stop == 4) {
+            if (c.err & GS_ERRBIT_BOUNDS) return gsi::fail(h, GS_ERR_CUDA, GS_BOUNDS_MSG);
             if (c.err & 1u) return gsi::fail(h, GS_ERR_BLAST, gs_status_string(GS_ERR_BLAST));
             return gsi::fail(h, GS_ERR_NAN, gs_status_string(GS_ERR_NAN));
         }

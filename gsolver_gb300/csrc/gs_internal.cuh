@@ -29,8 +29,30 @@ template <typename T2> __device__ __forceinline__ T2 cmul(T2 a, T2 b) {
 }
 template <typename T2> __device__ __forceinline__ T2 cconj(T2 a) { a.y = -a.y; return a; }
 
-// error word bits written by kernels (host maps them to the reference's exceptions)
+// error word bits written by kernels (host maps them to the reference's exceptions; a
+// GS_CHECK build's failed index test sets GS_ERRBIT_BOUNDS, gs_kernels.h)
 enum : unsigned { ERRBIT_BLAST = 1u, ERRBIT_NAN = 2u };
+
+// GS_CHECK builds (`python -m gsolver_gb300.build --check`: -DGS_CHECK=1, a library of its own
+// under _build_check/) test the indices the hot kernels take from index tables (compact-column
+// maps, rate-table rows) before each access: a failed test sets ERRBIT_BOUNDS in the error word
+// and the access is skipped (no trap), and the call returns GS_ERR_CUDA "index out of bounds".
+// Other builds compile the test away.
+#ifndef GS_CHECK
+#define GS_CHECK 0
+#endif
+__device__ __forceinline__ bool in_bounds(bool ok, unsigned* err) {
+#if GS_CHECK
+    if (!ok) {
+        if (err) atomicOr(err, GS_ERRBIT_BOUNDS);
+        return false;
+    }
+#else
+    (void)ok;
+    (void)err;
+#endif
+    return true;
+}
 
 // Non-negative doubles order like their bit patterns: max-reduce through 64-bit atomics.
 __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {

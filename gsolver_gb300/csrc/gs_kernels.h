@@ -236,6 +236,10 @@ struct LstepArgs {
     const int* run;
 };
 
+// the error word's bit for a failed index test of a GS_CHECK build (gs_internal.cuh in_bounds)
+constexpr unsigned GS_ERRBIT_BOUNDS = 1u << 16;
+constexpr const char* GS_BOUNDS_MSG = "index out of bounds (GS_CHECK build)";
+
 // The z-loop's state on the device (gs_advance): propagator()'s step-size controller
 // (propagator.cu:139-164) and the z-loop's bookkeeping (solver_main.cpp:202-225) run in a
 // one-thread kernel between each attempt's NL step and its linear step.

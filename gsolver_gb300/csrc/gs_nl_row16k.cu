@@ -258,7 +258,9 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
             }
 #pragma unroll
             for (int i = 0; i < L; i++)
-                x[i] = cc[i] >= 0 ? *reinterpret_cast<const float2*>(acr + cc[i]) : make_float2(0.f, 0.f);
+                x[i] = (cc[i] >= 0 && in_bounds(cc[i] + 2 <= sp.ncw, a.err))
+                           ? *reinterpret_cast<const float2*>(acr + cc[i])
+                           : make_float2(0.f, 0.f);
         } else {
             const float4* a4 = reinterpret_cast<const float4*>(A + base + t0);
 #pragma unroll
@@ -332,6 +334,7 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
                 for (int u = 0; u < 8; u++) {
                     dl[u] = 0.f;
                     n[u] = (t0 + g + u > 0) ? photo_index<float>(Iv[u], &dl[u], a.err) : -1;
+                    if (n[u] >= 0 && !in_bounds(n[u] + 1 < 8192, a.err)) n[u] = -1;
                 }
                 float w0[8], w1[8];
 #pragma unroll
@@ -684,8 +687,8 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
             *reinterpret_cast<float4*>(sp.nb + base + p) = make_float4(y0.x, y0.y, y1.x, y1.y);
             if (nbr) {
                 const int2 c2 = __ldg(reinterpret_cast<const int2*>(sp.cinv + p));
-                if (c2.x >= 0) *reinterpret_cast<float2*>(nbr + c2.x) = y0;
-                if (c2.y >= 0) *reinterpret_cast<float2*>(nbr + c2.y) = y1;
+                if (c2.x >= 0 && in_bounds(c2.x + 2 <= sp.ncw, a.err)) *reinterpret_cast<float2*>(nbr + c2.x) = y0;
+                if (c2.y >= 0 && in_bounds(c2.y + 2 <= sp.ncw, a.err)) *reinterpret_cast<float2*>(nbr + c2.y) = y1;
             }
         }
     }

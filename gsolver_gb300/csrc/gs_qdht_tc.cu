@@ -562,7 +562,7 @@ constexpr int OPERAND_EXP = 14;
 // row-wise stores, the column scans and the pair-wise reads are all free of bank conflicts.
 // Relative error of the parts ~2^-22 of each value, or 2^-39 of its column's maximum where Xl
 // falls below the FP16 normal range.  Dynamic shared memory: (nr / 2) * 33 floats.
-constexpr int SPLIT_COLS = 16, SPLIT_THREADS = 256;
+constexpr int SPLIT_COLS = 16, SPLIT_THREADS = 512;
 __global__ void __launch_bounds__(SPLIT_THREADS) qdht_split16_kernel(const float* __restrict__ X,
                                                                      __half* __restrict__ XhT,
                                                                      __half* __restrict__ XlT,
@@ -775,7 +775,8 @@ __device__ __forceinline__ void epilogue_cols(const TcArgs& a, float* v, int i, 
 #pragma unroll
             for (int k = 0; k < 32; k += 2) {
                 const int rc = a.cmap[cg + k];
-                if (rc >= 0) *reinterpret_cast<float2*>(y + rc) = make_float2(v[k], v[k + 1]);
+                if (rc >= 0 && in_bounds(rc + 2 <= a.ncols, a.err))
+                    *reinterpret_cast<float2*>(y + rc) = make_float2(v[k], v[k + 1]);
             }
             return;
         }
@@ -1785,6 +1786,11 @@ cudaError_t qdht_tc_wait_probe(QdhtTc* q, double limit_s, long long* nlaunch) {
 int qdht_tc_check(QdhtTc* q, std::string* msg) {
     unsigned e[2] = {0, 0};
     if (cudaMemcpy(e, q->err, 8, cudaMemcpyDeviceToHost) != cudaSuccess) return 1;
+    if (e[0] & GS_ERRBIT_BOUNDS) {
+        if (msg) *msg = GS_BOUNDS_MSG;
+        cudaMemset(q->err, 0, 8);
+        return 1;
+    }
     if (e[0]) {
         if (msg)
             *msg = "tensor-core QDHT wait expired (codes " + std::to_string(e[0]) + ", first: code " +

@@ -322,6 +322,19 @@ int gs_checkpoint_load(gs_handle* h, const char* path, double* current_z, double
  * stays usable.  Mixed handles only. */
 int gs_selftest_bounded_wait(gs_handle* h, double limit_s);
 
+/* 1 when the library was built with GS_CHECK (`python -m gsolver_gb300.build --check`): the hot
+ * kernels test the indices they take from index tables (compact-column maps, rate-table rows)
+ * before each access, skip a failing access and report it as GS_ERR_CUDA "index out of bounds
+ * (GS_CHECK build)" from the call; else 0. */
+int gs_check_build(void);
+
+/* Self-test of the GS_CHECK index test (no counterpart in the reference): a kernel tests an index
+ * one past the length it declares for a buffer that is larger (so the access could not fault
+ * either way); the test fails, the access is skipped, and the call returns GS_ERR_CUDA with the
+ * bounds message, the handle usable.  Builds without GS_CHECK return GS_ERR_UNSUPPORTED and
+ * launch nothing. */
+int gs_selftest_bounds(gs_handle* h);
+
 /* Apertures (propagator.cu:232-261, process_input.cpp:176-179): n entries in the reference's
  * array order (z[n-1], r[n-1] is the first applied).  gs_step then applies them as
  * propagator() does: after an accepted step, when current_z (the z before the step) has

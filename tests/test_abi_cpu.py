@@ -35,6 +35,12 @@ def test_library_exports_every_declared_symbol():
     assert set(gs.ABI_FUNCTIONS) == names
 
 
+def test_the_default_build_is_not_the_checked_one():
+    # GS_CHECK index tests live in their own library (_build_check/), loaded only under GS_CHECK=1
+    assert gs.load_library().gs_check_build() == 0
+    assert gs.LIB_PATH.endswith(os.path.join("_build", "libgsolver_gb300.so"))
+
+
 def test_status_strings_are_the_reference_messages():
     L = gs.load_library()
     assert L.gs_status_string(gs.GS_ERR_BLAST).decode() == \
