@@ -204,6 +204,34 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
     float* const Wc = Wb + pad32(t0);
     const float2* const twb = f.twb;
 
+    // ---- stage 0's input: FIELD (compact window columns or the full row); the loads are issued
+    // before the set-up below so that their latency overlaps it
+    float2 x[L];
+    const float* acr = (sp.ac && !(f.ac_on && *f.ac_on == 0)) ? sp.ac + (size_t)row * sp.ncw : nullptr;
+    if (acr) {   // the thread's positions from their window column pairs (zero outside)
+        int cc[L];
+#pragma unroll
+        for (int h = 0; h < L / 4; h++) {
+            const int4 v = __ldg(reinterpret_cast<const int4*>(sp.cinv + t0) + h);
+            cc[4 * h] = v.x;
+            cc[4 * h + 1] = v.y;
+            cc[4 * h + 2] = v.z;
+            cc[4 * h + 3] = v.w;
+        }
+#pragma unroll
+        for (int i = 0; i < L; i++)
+            x[i] = (cc[i] >= 0 && in_bounds(cc[i] + 2 <= sp.ncw, a.err)) ? *reinterpret_cast<const float2*>(acr + cc[i])
+                                                                       : make_float2(0.f, 0.f);
+    } else {
+        const float4* a4 = reinterpret_cast<const float4*>(A + base + t0);
+#pragma unroll
+        for (int h = 0; h < L / 2; h++) {
+            const float4 v = a4[h];
+            x[2 * h] = make_float2(v.x, v.y);
+            x[2 * h + 1] = make_float2(v.z, v.w);
+        }
+    }
+
     // tensor memory: per thread 32 columns of the RK4 sum, then 32 of A, in its warp's lanes
     if (w == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
@@ -242,34 +270,8 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
     const double dzs = f.dz_dev ? *f.dz_dev : f.dzs;
     const float c_half = (float)(dzs * 0.5), c_full = (float)dzs;
 
-    // ---- stage 0's input: FIELD (compact window columns or the full row) into tensor memory
+    // ---- stage 0's input into tensor memory (loaded above)
     {
-        float2 x[L];
-        const float* acr = (sp.ac && !(f.ac_on && *f.ac_on == 0)) ? sp.ac + (size_t)row * sp.ncw : nullptr;
-        if (acr) {   // the thread's positions from their window column pairs (zero outside)
-            int cc[L];
-#pragma unroll
-            for (int h = 0; h < L / 4; h++) {
-                const int4 v = __ldg(reinterpret_cast<const int4*>(sp.cinv + t0) + h);
-                cc[4 * h] = v.x;
-                cc[4 * h + 1] = v.y;
-                cc[4 * h + 2] = v.z;
-                cc[4 * h + 3] = v.w;
-            }
-#pragma unroll
-            for (int i = 0; i < L; i++)
-                x[i] = (cc[i] >= 0 && in_bounds(cc[i] + 2 <= sp.ncw, a.err))
-                           ? *reinterpret_cast<const float2*>(acr + cc[i])
-                           : make_float2(0.f, 0.f);
-        } else {
-            const float4* a4 = reinterpret_cast<const float4*>(A + base + t0);
-#pragma unroll
-            for (int h = 0; h < L / 2; h++) {
-                const float4 v = a4[h];
-                x[2 * h] = make_float2(v.x, v.y);
-                x[2 * h + 1] = make_float2(v.z, v.w);
-            }
-        }
 #pragma unroll
         for (int g = 0; g < 4; g++) tst8(tm + 32 + 8 * g, reinterpret_cast<const float*>(&x[4 * g]));
         float amax = 0.f;

@@ -536,13 +536,16 @@ __global__ void lstep_adj_kernel(const float2* __restrict__ fb, float2* __restri
 //                        TMA in the K-major layout with the 64-byte swizzle (no conversion in
 //                        shared memory): K-blocks of 32 (one 64-byte row), 32 KiB stages, six
 //                        in flight; tcgen05.mma.kind::f16 M = 128, N = 128, K = 16, summed in
-//                        chunks of 64 of K into two alternating TMEM accumulators.  Warp 0
+//                        chunks of 64 of K into three rotating TMEM accumulators.  Warp 0
 //                        TMA, warp 1 MMA issuer, warps 2-17 epilogue (four per TMEM lane
 //                        quarter, 32 columns each): each chunk is added into FP32 registers,
 //                        then the scales are undone and the tile stored / updated.
 constexpr int WIDE_COLS = 256;                         // the path takes grids with 2 n_t a multiple of this
 constexpr int BN2 = 128, BK2 = 32, STAGES2 = 6;        // K-blocks of 32 FP16 (one 64-byte swizzle row)
 constexpr int KCHUNK2 = 2;                              // K-blocks per accumulation chunk (64 of K)
+constexpr int NACC2 = 3;                                // TMEM accumulators: the MMA runs NACC2 - 1 chunks ahead
+constexpr int TMEM_COLS2 = NACC2 * BN2 <= 256 ? 256 : 512;   // the allocation (a power of two)
+static_assert(NACC2 * BN2 <= 512, "accumulators fit tensor memory");
 constexpr int A2_BYTES = BM * BK2 * 2;                  // 8 KiB
 constexpr int B2_BYTES = BN2 * BK2 * 2;                 // 8 KiB
 constexpr int STAGE2_BYTES = 2 * A2_BYTES + 2 * B2_BYTES;
@@ -1066,9 +1069,9 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
     uint64_t* bars = (uint64_t*)(smem + STAGES2 * STAGE2_BYTES);
     uint64_t* full = bars;                    // [STAGES2] TMA tx
     uint64_t* empty = bars + STAGES2;         // [STAGES2] MMA commit
-    uint64_t* acc_full = bars + 2 * STAGES2;  // [2] MMA commit: a chunk's accumulator ready
-    uint64_t* acc_empty = acc_full + 2;       // [2] NEPI2 epilogue warps: read out
-    uint64_t* done = acc_empty + 2;           // every MMA of this CTA complete
+    uint64_t* acc_full = bars + 2 * STAGES2;  // [NACC2] MMA commit: a chunk's accumulator ready
+    uint64_t* acc_empty = acc_full + NACC2;   // [NACC2] NEPI2 epilogue warps: read out
+    uint64_t* done = acc_empty + NACC2;       // every MMA of this CTA complete
     uint32_t* tmem_slot = (uint32_t*)(done + 1);
     volatile int* abort_flag = (volatile int*)(tmem_slot + 1);
 
@@ -1084,7 +1087,7 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
             mbar_init(&full[s], 1);
             mbar_init(&empty[s], 1);
         }
-        for (int b = 0; b < 2; b++) {
+        for (int b = 0; b < NACC2; b++) {
             mbar_init(&acc_full[b], 1);
             mbar_init(&acc_empty[b], NEPI2);
         }
@@ -1095,7 +1098,7 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
     __syncwarp();
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                     "r"(2 * BN2));
+                     "r"(TMEM_COLS2));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -1134,7 +1137,7 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
         __syncwarp();
     } else if (warp == 1) {
         // ------------------------------------------------ MMA issuer
-        // Each chunk of KCHUNK2 K-blocks is summed afresh into accumulator buffer u % 2 (u the
+        // Each chunk of KCHUNK2 K-blocks is summed afresh into accumulator buffer u % NACC2 (u the
         // CTA's running chunk count), the correction products Hh Xl + Hl Xh of the chunk first
         // and its main products Hh Xh last; the epilogue adds the chunks in FP32 registers.
         // The tensor core's accumulation truncates: with a fresh, small accumulator per chunk
@@ -1145,8 +1148,8 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
             bool ok = true;
             for (int it = 0; it < my_tiles && ok && !*abort_flag; it++) {
                 for (int c = 0; c < nch; c++) {
-                    const int u = it * nch + c, b = u & 1;
-                    if (u >= 2 && !mbar_wait(&acc_empty[b], ((u >> 1) - 1) & 1)) {
+                    const int u = it * nch + c, b = u % NACC2;
+                    if (u >= NACC2 && !mbar_wait(&acc_empty[b], ((u / NACC2) - 1) & 1)) {
                         record_stall(a.err, 4096u, c, warp);
                         ok = false;
                         break;
@@ -1213,8 +1216,8 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
             const int i = m0 + 32 * q + lane;
             float sum[32];
             for (int c = 0; c < nch; c++) {
-                const int u = it * nch + c, b = u & 1;
-                ok = __all_sync(0xffffffffu, mbar_wait(&acc_full[b], (u >> 1) & 1) ? 1 : 0) != 0;
+                const int u = it * nch + c, b = u % NACC2;
+                ok = __all_sync(0xffffffffu, mbar_wait(&acc_full[b], (u / NACC2) & 1) ? 1 : 0) != 0;
                 if (!ok) {
                     if (lane == 0) record_stall(a.err, 32u, c, warp);
                     *abort_flag = 1;
@@ -1253,7 +1256,7 @@ __global__ void __launch_bounds__(THREADS2, 1) qdht_tc2_kernel(const __grid_cons
     __syncthreads();
     if (warp == 0) {
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * BN2));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TMEM_COLS2));
     }
 }
 
@@ -1652,7 +1655,7 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
         }
 
         // split X into the K-major FP16 hi / lo operands and the column scales (the window mask
-        // of the inverse applied), then the GEMM on 128 x 256 tiles
+        // of the inverse applied), then the GEMM on 128 x 128 tiles
         tc::qdht_split16_kernel<<<(unsigned)(a.nc / tc::SPLIT_COLS), tc::SPLIT_THREADS, (size_t)(q->nr / 2) * 33 * 4,
                                   q->st>>>(xc ? xsrc : X, (__half*)q->xhT, (__half*)q->xlT, q->xs, q->nr,
                                            xc ? a.nc : a.ncols, mode == QDHT_MASKED ? q->kmax : nullptr, a.cmap, xc,
