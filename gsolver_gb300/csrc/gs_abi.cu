@@ -1017,6 +1017,9 @@ int gs_step(gs_handle* h, double current_z, double znet_cur, double znet_prev, d
 int gs_step_host(gs_handle* h, double* field, double* spec, double current_z, double znet_cur, double znet_prev,
                  double* zstep_inout, unsigned* step_n_inout, double* max_a2, double* max_nl2) {
     if (!h || !field || !spec || !zstep_inout) return fail(h, GS_ERR_ARG, "null argument");
+    const size_t bytes = (size_t)h->nr * h->nt * 16;
+    if ((const char*)field < (const char*)spec + bytes && (const char*)spec < (const char*)field + bytes)
+        return fail(h, GS_ERR_ARG, "gs_step_host: FIELD and BIGBUFFER2 overlap");
     if (!h->tables_ok) return fail(h, GS_ERR_STATE, "tables not uploaded");
     CK(h, cudaSetDevice(h->p.device));
     gsi::Range r("gs_step_host");

@@ -7,8 +7,9 @@
 // batch's stream, so pulses of different grids run concurrently and fill the GPU together.
 // The whole z-step is captured once into a CUDA graph and replayed, so the host issues one
 // launch per z-step instead of ~10 per pulse.  Step sizes are fixed per pulse (the graph
-// holds them; a new set of sizes captures a new graph); the adaptive controller needs a
-// host decision per step and stays with gs_step.
+// holds them; a new set of sizes captures a new graph).  The adaptive controller stays with
+// gs_step / gs_advance: the fused stage kernels of these grids take their step size from the
+// host, so a captured attempt could not follow a controller kernel's decision.
 #include <cuda_runtime.h>
 
 #include <algorithm>

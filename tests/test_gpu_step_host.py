@@ -28,10 +28,13 @@ def host_bufs(T, pinned):
     return f, s, f.ctypes.data, s.ctypes.data, f, s
 
 
-def compare(T, prec, dz0, calls, pinned):
+def compare(T, prec, dz0, calls, pinned, prep=None):
     znet = T["znet"]
     P1 = gs.Propagator(T, precision=prec)
     P2 = gs.Propagator(T, precision=prec)
+    if prep:
+        prep(P1)
+        prep(P2)
     P1.set_field(T["field"])
     P2.set_field(T["field"])
     _, _, fp, sp, fa, sa = host_bufs(T, pinned)
@@ -70,3 +73,24 @@ def test_step_host_with_rejected_attempts(prec):
     dz0 = tables.init_zstep_kerr(T, T["field"])   # ~8x what the controller accepts: rejected
     _, _, _, step_n = compare(T, prec, dz0, 4, True)
     assert step_n > 4   # rejected attempts counted
+
+
+@pytest.mark.parametrize("prec", [gs.PREC_FP64, gs.PREC_MIXED])
+def test_step_host_with_apertures(prec):
+    # apertures zero FIELD's outer rows after an accepted step and take BIGBUFFER2 anew from it:
+    # after gs_step_host has installed BIGBUFFER2 for the linear step
+    d = tempfile.mkdtemp(prefix="gs_sh_ap_")
+    over = {"N_R": "128", "N_T": "512", "N_Z": "11", "APERTURE_N": "2", "APERTURE_Z0": "0", "APERTURE_R0": "1.5e-4",
+            "APERTURE_Z1": "2.5e-4", "APERTURE_R1": "1e-4"}
+    S = gs.Setup(configs.fused_silica_c1(d), overrides=over, noise_seed=1, noise_sigma=1e-4).as_dict()
+    compare(S, prec, float(S["init_zstep"]), 3, True)
+
+
+def test_step_host_with_the_photon_number_check():
+    # the check repeats the linear step from the saved BIGBUFFER2 until the photon number moves by
+    # at most tol: it reads BIGBUFFER2 before the first linear step
+    d = tempfile.mkdtemp(prefix="gs_sh_en_")
+    p = configs.hot_solid(d, n_r=128, n_t=2048, power_cr=20.0, tol=1e-2)
+    T = tables.build(tables.Config.from_file(p), noise_seed=5, noise_sigma=1e-4)
+    compare(T, gs.PREC_MIXED, tables.init_zstep_kerr(T, T["field"]), 3, True,
+            prep=lambda P: P.set_energy_tolerance(2e-4, T["qdht_x"], T["r_max"]))
