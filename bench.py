@@ -71,6 +71,8 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--batch-pulses", type=int, default=64)
     ap.add_argument("--batch-steps", type=int, default=10)
+    ap.add_argument("--batch-adaptive-calls", type=int, default=8,
+                    help="accepted propagator() calls per pulse in the batch leg's adaptive part (0: skip it)")
     ap.add_argument("--adjoint-steps", type=int, default=1000)
     ap.add_argument("--adjoint-check-steps", type=int, default=100)
     ap.add_argument("--adjoint-dirs", type=int, default=2,
@@ -316,6 +318,45 @@ def batch_leg(args, lrank):
         out[key] = {"value": pts * args.batch_steps / (ms / 1e3), "unit": UNIT, "ms_per_zstep": ms / args.batch_steps,
                     "wall_ms_per_zstep": wall * 1e3 / args.batch_steps, "steps": args.batch_steps,
                     "kernels_per_zstep": (B.launch_count() - n0) / args.batch_steps}
+    B.close()
+    for p in P:
+        p.close()
+    if args.batch_adaptive_calls > 0:
+        out["adaptive"] = batch_adaptive(args, lrank, cfgs)
+    return out
+
+
+def batch_adaptive(args, lrank, cfgs):
+    """The same 64 grids with each pulse's adaptive controller at MAX_TOLERANCE 1e-6 (the
+    workload's own 1e3 lets ZNET clamp every step to 2 um), on the device: gs_batch_advance, one
+    graph launch per attempt of all pulses, rejected attempts included; accepted field-point
+    z-steps/s over the batch, wall clock of the call (graph capture and the host reads of the
+    pulses' states included)."""
+    import gsolver_gb300 as gs
+    S = [gs.Setup(p, overrides={"MAX_TOLERANCE": "1e-6"}, noise_seed=100 + i, noise_sigma=1e-4, device=lrank).as_dict()
+         for i, (p, _) in enumerate(cfgs)]
+    P = [gs.Propagator(s, precision=gs.PREC_MIXED, device=lrank) for s in S]
+    for s, p in zip(S, P):
+        p.set_field(s["field"])
+    B = gs.Batch(P)
+    znets = [s["znet"] for s in S]
+    n = len(P)
+    cz = np.array([float(z[0]) for z in znets])
+    dz = np.array([float(s["init_zstep"]) for s in S])
+    sn = np.zeros(n, np.uint32)
+    nz = [1] * n
+    cz, dz, sn, _, _ = B.advance(znets, nz, cz, dz, sn, 2)   # warm-up: the first calls find each NL path
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    cz1, dz1, sn1, calls, reached = B.advance(znets, nz, cz, dz, sn, args.batch_adaptive_calls)
+    wall = time.perf_counter() - t0
+    pts = sum(s["n_r"] * s["n_t"] * int(c) for s, c in zip(S, calls))
+    attempts = int(np.sum(sn1 - sn))
+    out = {"max_tolerance": 1e-6, "calls_per_pulse": args.batch_adaptive_calls, "accepted_calls": int(np.sum(calls)),
+           "attempts": attempts, "rejected": attempts - int(np.sum(calls)), "value": pts / wall, "unit": UNIT,
+           "ms_per_call_of_all_pulses": wall * 1e3 / max(1, args.batch_adaptive_calls),
+           "api": "gs_batch_advance (every pulse's controller on the device, one graph launch per attempt)"}
     B.close()
     for p in P:
         p.close()

@@ -40,7 +40,7 @@ ABI_FUNCTIONS = (
     "gs_plasma_max_noalloc", "gs_noalloc_max_samples", "gs_noalloc_last_error",
     "gs_forward_fixed", "gs_gradient", "gs_adjoint_step", "gs_adjoint_stride",
     "gs_batch_create", "gs_batch_step", "gs_batch_stream", "gs_batch_launch_count", "gs_batch_last_error",
-    "gs_batch_destroy", "gs_autotune", "gs_set_nl_threads", "gs_get_nl_threads", "gs_batch_autotune",
+    "gs_batch_destroy", "gs_batch_advance", "gs_autotune", "gs_set_nl_threads", "gs_get_nl_threads", "gs_batch_autotune",
     "gs_set_apertures", "gs_setup_apertures", "gs_setup_from_config_dev",
     "gs_energy", "gs_set_energy_tolerance", "gs_energy_stats", "gs_checkpoint_save", "gs_checkpoint_load",
     "gs_selftest_bounded_wait", "gs_check_build", "gs_selftest_bounds",
@@ -139,6 +139,7 @@ def load_library(path: str | None = None):
     L.gs_set_nl_threads.argtypes = [V, I]
     L.gs_get_nl_threads.argtypes = [V]
     L.gs_batch_autotune.argtypes = [V, V, PD, PD, C.POINTER(C.c_int)]
+    L.gs_batch_advance.argtypes = [V, V, V, V, V, V, V, I, V, V]
     L.gs_set_apertures.argtypes = [V, I, V, V, V, D]
     L.gs_setup_apertures.argtypes = [V, C.POINTER(C.c_int), V, V]
     L.gs_energy.argtypes = [V, V, D, PD, PD]
@@ -550,8 +551,9 @@ class Setup:
 
 
 class Batch:
-    """Independent pulses (Propagator objects on one device) advanced together with fixed
-    per-pulse step sizes; one CUDA graph launch per z-step (gs_batch_*)."""
+    """Independent pulses (Propagator objects on one device) advanced together: with fixed
+    per-pulse step sizes, one CUDA graph launch per z-step (step), or with every pulse's
+    adaptive controller on the device, one graph launch per attempt (advance)."""
 
     def __init__(self, pulses):
         self.L = load_library()
@@ -570,6 +572,29 @@ class Batch:
         rc = self.L.gs_batch_step(self.b, int(n_steps), _ptr(d), int(bool(graph)))
         if rc:
             raise GsError(rc, self.L.gs_batch_last_error(self.b).decode())
+
+    def advance(self, znets, n_z, current_z, zstep, step_n, max_calls):
+        """gs_batch_advance: up to max_calls propagator() calls of every pulse (gs_advance for
+        each, all pulses' attempts in one graph launch).  znets: one ZNET array per pulse; n_z,
+        current_z, zstep, step_n: per pulse.  Returns (current_z, zstep, step_n, calls, reached)
+        as arrays."""
+        n = len(self.pulses)
+        zs = [np.ascontiguousarray(z, dtype=np.float64) for z in znets]
+        if len(zs) != n:
+            raise ValueError("one ZNET per pulse")
+        zp = (C.c_void_p * n)(*[z.ctypes.data for z in zs])
+        nz = np.array([len(z) for z in zs], np.int32)
+        nzi = np.ascontiguousarray(n_z, dtype=np.int32)
+        cz = np.ascontiguousarray(current_z, dtype=np.float64).copy()
+        dz = np.ascontiguousarray(zstep, dtype=np.float64).copy()
+        sn = np.ascontiguousarray(step_n, dtype=np.uint32).copy()
+        calls = np.zeros(n, np.int32)
+        reached = np.zeros(n, np.int32)
+        rc = self.L.gs_batch_advance(self.b, zp, _ptr(nz), _ptr(nzi), _ptr(cz), _ptr(dz), _ptr(sn), int(max_calls),
+                                     _ptr(calls), _ptr(reached))
+        if rc:
+            raise GsError(rc, self.L.gs_batch_last_error(self.b).decode())
+        return cz, dz, sn, calls, reached.astype(bool)
 
     def autotune(self, dz):
         """Default vs per-grid tuned launch shapes for the batch as a whole (gs_batch_autotune);

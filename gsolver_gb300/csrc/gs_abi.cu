@@ -692,6 +692,7 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
             const int rs = gsi::field_sync(h);
             if (rs) return rs;
         }
+        h->nl_dev_dz = h->p.nonlinear && fused && !h->pair && !tape && !h->fp64;
     }
     if (!h->p.nonlinear) {
         CK(h, launch_zero_nl<Rl>(A, NB, nel, h->max_dev, h->st, &h->launches));

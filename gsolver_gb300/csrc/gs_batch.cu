@@ -7,9 +7,8 @@
 // batch's stream, so pulses of different grids run concurrently and fill the GPU together.
 // The whole z-step is captured once into a CUDA graph and replayed, so the host issues one
 // launch per z-step instead of ~10 per pulse.  Step sizes are fixed per pulse (the graph
-// holds them; a new set of sizes captures a new graph).  The adaptive controller stays with
-// gs_step / gs_advance: the fused stage kernels of these grids take their step size from the
-// host, so a captured attempt could not follow a controller kernel's decision.
+// holds them; a new set of sizes captures a new graph).  gs_batch_advance runs every pulse's
+// adaptive controller on the device instead: one graph launch per attempt of all pulses.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -182,6 +181,170 @@ int gs_batch_step(gs_batch* b, int n_steps, const double* dz, int use_graph) {
         if (err & gs::GS_ERRBIT_BOUNDS) return bfail(b, GS_ERR_CUDA, "pulse " + std::to_string(i) + ": " + gs::GS_BOUNDS_MSG);
         if (err & 1u) return bfail(b, GS_ERR_BLAST, "pulse " + std::to_string(i) + ": " + gs_status_string(GS_ERR_BLAST));
         if (err & 2u) return bfail(b, GS_ERR_NAN, "pulse " + std::to_string(i) + ": " + gs_status_string(GS_ERR_NAN));
+    }
+    return GS_OK;
+}
+
+// gs_advance for every pulse at once.  Each pulse gets the device z-loop state of gs_advance
+// (DevCtl, its ZNET on the device); one attempt of every pulse -- NL step, controller kernel,
+// linear step, each reading the attempt's step size and decision from the device -- is
+// captured between a fork and a join and replayed, one graph launch per attempt; a pulse
+// whose loop stopped (ZNET point, call budget, collapse, NL error) skips its kernels.  The
+// host reads the pulses' states every REPLAYS launches.  FIELD is kept expanded (the masked
+// inverse not lazy), so the captured attempt is the same whatever state it starts from.
+int gs_batch_advance(gs_batch* b, const double* const* znet, const int* nz, const int* n_z, double* current_z,
+                     double* zstep, unsigned* step_n, int max_calls, int* calls_done, int* reached) {
+    if (!b || !znet || !nz || !n_z || !current_z || !zstep || !step_n || max_calls < 0)
+        return bfail(b, GS_ERR_ARG, "gs_batch_advance: null argument or max_calls < 0");
+    const size_t n = b->h.size();
+    for (size_t i = 0; i < n; i++) {
+        gs_handle* h = b->h[i];
+        const std::string who = "pulse " + std::to_string(i) + ": ";
+        if (!znet[i] || nz[i] < 2 || n_z[i] < 1 || n_z[i] >= nz[i])
+            return bfail(b, GS_ERR_ARG, who + "bad ZNET index or size");
+        if (!h->tables_ok || !h->field_ok) return bfail(b, GS_ERR_STATE, who + "tables / field not set");
+        if (h->time_qdht || h->time_nl) return bfail(b, GS_ERR_STATE, who + "kernel timing is on");
+        if (calls_done) calls_done[i] = 0;
+        if (reached) reached[i] = 0;
+    }
+    BCK(b, cudaSetDevice(b->device));
+    std::vector<int> done(n, 0);
+    // as gs_advance: a pulse whose NL path is not known yet takes its first call on the host
+    for (size_t i = 0; i < n; i++) {
+        gs_handle* h = b->h[i];
+        if (gsi::advance_on_device(h) || h->nl_compact || h->nl_dev_dz || max_calls == 0 ||
+            current_z[i] >= znet[i][n_z[i]])
+            continue;
+        double dz = zstep[i];
+        unsigned sn = step_n[i];
+        const int rc = gs_step(h, current_z[i], znet[i][n_z[i]], znet[i][n_z[i] - 1], &dz, &sn, nullptr, nullptr);
+        if (rc) return bfail(b, rc, "pulse " + std::to_string(i) + ": " + h->err);
+        step_n[i] = sn + 1;
+        current_z[i] += dz;
+        zstep[i] = dz;
+        done[i] = 1;
+    }
+    for (size_t i = 0; i < n; i++)
+        if (!gsi::advance_on_device(b->h[i]))
+            return bfail(b, GS_ERR_UNSUPPORTED, "pulse " + std::to_string(i) +
+                                                    ": its attempts need the host (FP64, the staged or paired NL "
+                                                    "kernels, a photon-number check or an aperture)");
+    // the device z-loops
+    struct Restore {   // every pulse back in host mode on every way out
+        gs_batch* b;
+        ~Restore() {
+            for (gs_handle* h : b->h) {
+                h->ctl = nullptr;
+                h->a_lazy_ok = true;
+            }
+        }
+    } restore{b};
+    std::vector<gs::DevCtl> c(n);
+    for (size_t i = 0; i < n; i++) {
+        gs_handle* h = b->h[i];
+        const std::string who = "pulse " + std::to_string(i) + ": ";
+        if (h->znet_cap < nz[i]) {
+            if (h->znet_dev) cudaFree(h->znet_dev);
+            h->znet_dev = nullptr;
+            h->znet_cap = 0;
+            BCK(b, cudaMalloc(&h->znet_dev, (size_t)nz[i] * sizeof(double)));
+            h->znet_cap = nz[i];
+        }
+        if (!h->ctl_dev) BCK(b, cudaMalloc(&h->ctl_dev, sizeof(gs::DevCtl)));
+        BCK(b, cudaMemcpyAsync(h->znet_dev, znet[i], (size_t)nz[i] * sizeof(double), cudaMemcpyHostToDevice, h->st));
+        h->a_lazy_ok = false;
+        if (gsi::spec_prepare(h) || gsi::field_sync(h)) return bfail(b, GS_ERR_CUDA, who + h->err);
+        gs::DevCtl& ci = c[i];
+        ci = gs::DevCtl{};
+        ci.z = current_z[i];
+        ci.zstep = zstep[i];
+        ci.step_n = step_n[i];
+        ci.n_z = n_z[i];
+        ci.max_calls = max_calls - done[i];
+        ci.field_compact = 0;
+        // a pulse with nothing to do is stopped from the start: its kernels skip
+        if (ci.max_calls <= 0) ci.stop = 2;
+        if (current_z[i] >= znet[i][n_z[i]]) ci.stop = 1;
+        BCK(b, cudaMemcpyAsync(h->ctl_dev, &ci, sizeof(gs::DevCtl), cudaMemcpyHostToDevice, h->st));
+        BCK(b, cudaMemsetAsync(h->max_dev, 0, 16, h->st));
+        BCK(b, cudaMemsetAsync(h->err_dev, 0, 4, h->st));
+        h->ctl = h->ctl_dev;
+    }
+    for (size_t i = 0; i < n; i++) {   // the batch stream waits for the pulses' set-up
+        BCK(b, cudaEventRecord(b->join[i], b->h[i]->st));
+        BCK(b, cudaStreamWaitEvent(b->st, b->join[i], 0));
+    }
+    // one attempt of every pulse, captured
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ex = nullptr;
+    long long nk = 0;
+    BCK(b, cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+    int rc = GS_OK;
+    {
+        cudaError_t e = cudaEventRecord(b->fork, b->st);
+        for (size_t i = 0; i < n && rc == GS_OK && e == cudaSuccess; i++) {
+            gs_handle* h = b->h[i];
+            const long long l0 = h->launches;
+            e = cudaStreamWaitEvent(h->st, b->fork, 0);
+            if (e != cudaSuccess) break;
+            rc = gsi::nl_stages(h, zstep[i], nullptr);   // the kernels read the device's step size
+            if (rc == GS_OK) {
+                e = gs::launch_step_ctl(h->ctl_dev, h->znet_dev, h->max_dev, h->err_dev, h->p.max_tolerance, 0, h->st,
+                                        &h->launches);
+                if (e == cudaSuccess) rc = gsi::lstep(h, zstep[i]);
+            }
+            if (rc == GS_OK && e == cudaSuccess) e = cudaEventRecord(b->join[i], h->st);
+            if (rc == GS_OK && e == cudaSuccess) e = cudaStreamWaitEvent(b->st, b->join[i], 0);
+            nk += h->launches - l0;
+            if (rc) rc = bfail(b, rc, "pulse " + std::to_string(i) + ": " + h->err);
+        }
+        const cudaError_t ee = cudaStreamEndCapture(b->st, &g);
+        if (rc == GS_OK && e != cudaSuccess) rc = bfail(b, GS_ERR_CUDA, std::string("batch attempt: ") + cudaGetErrorString(e));
+        if (rc == GS_OK && ee != cudaSuccess)
+            rc = bfail(b, GS_ERR_CUDA, std::string("stream capture: ") + cudaGetErrorString(ee));
+    }
+    if (rc == GS_OK && cudaGraphInstantiate(&ex, g, 0) != cudaSuccess)
+        rc = bfail(b, GS_ERR_CUDA, "gs_batch_advance: graph instantiation failed");
+    constexpr int REPLAYS = 16;
+    while (rc == GS_OK) {
+        for (int r = 0; r < REPLAYS; r++) {
+            if (cudaGraphLaunch(ex, b->st) != cudaSuccess) {
+                rc = bfail(b, GS_ERR_CUDA, "gs_batch_advance: graph launch failed");
+                break;
+            }
+            b->launches += nk;
+        }
+        if (rc) break;
+        bool all = true;
+        for (size_t i = 0; i < n && rc == GS_OK; i++) {
+            if (cudaMemcpyAsync(&c[i], b->h[i]->ctl_dev, sizeof(gs::DevCtl), cudaMemcpyDeviceToHost, b->st) != cudaSuccess)
+                rc = bfail(b, GS_ERR_CUDA, "gs_batch_advance: state read failed");
+        }
+        if (rc == GS_OK && cudaStreamSynchronize(b->st) != cudaSuccess)
+            rc = bfail(b, GS_ERR_CUDA, "gs_batch_advance: synchronisation failed");
+        for (size_t i = 0; i < n; i++) all = all && c[i].stop != 0;
+        if (all) break;
+    }
+    if (ex) cudaGraphExecDestroy(ex);
+    if (g) cudaGraphDestroy(g);
+    if (rc) return rc;
+    for (size_t i = 0; i < n; i++) {
+        gs_handle* h = b->h[i];
+        const std::string who = "pulse " + std::to_string(i) + ": ";
+        h->a_compact = false;   // every accepted attempt's masked inverse expanded FIELD
+        current_z[i] = c[i].z;
+        zstep[i] = c[i].zstep;
+        step_n[i] = c[i].step_n;
+        if (calls_done) calls_done[i] = done[i] + c[i].calls;
+        if (reached) reached[i] = c[i].z >= znet[i][n_z[i]] ? 1 : 0;
+        std::string m;
+        if (gs::qdht_tc_check(h->tc, &m)) return bfail(b, GS_ERR_CUDA, who + m);
+        if (c[i].stop == 3) return bfail(b, GS_ERR_COLLAPSE, who + gs_status_string(GS_ERR_COLLAPSE));
+        if (c[i].stop == 4) {
+            if (c[i].err & gs::GS_ERRBIT_BOUNDS) return bfail(b, GS_ERR_CUDA, who + gs::GS_BOUNDS_MSG);
+            if (c[i].err & 1u) return bfail(b, GS_ERR_BLAST, who + gs_status_string(GS_ERR_BLAST));
+            return bfail(b, GS_ERR_NAN, who + gs_status_string(GS_ERR_NAN));
+        }
     }
     return GS_OK;
 }

@@ -69,11 +69,13 @@ __global__ void step_ctl_kernel(DevCtl* c, const double* __restrict__ znet, unsi
 // 16384-point FP32 rows reading FIELD compactly and the linear step the compact tensor-core
 // plan; no photon-number check and no aperture left to apply (both need the host)
 bool device_ok(const gs_handle* h) {
-    return !h->fp64 && h->tc && h->p.nonlinear && h->nl_compact && gs::qdht_tc_has_compact(h->tc) &&
+    return !h->fp64 && h->tc && h->p.nonlinear && (h->nl_compact || h->nl_dev_dz) && gs::qdht_tc_has_compact(h->tc) &&
            h->en_tol <= 0 && h->ap_z.empty();
 }
 
 }  // namespace
+
+bool gsi::advance_on_device(const gs_handle* h) { return device_ok(h); }
 
 namespace gs {
 cudaError_t launch_step_ctl(DevCtl* c, const double* znet, unsigned long long* max_dev, unsigned* err, double tol,
@@ -106,8 +108,9 @@ int gs_advance(gs_handle* h, const double* znet, int nz, int n_z, double* curren
         return rc;
     };
     int rc = GS_OK;
-    // the first call on the host when the NL launch shape is not known yet (it decides nl_compact)
-    if (!device_ok(h) && h->nl_compact == false && done < max_calls && cz < znet[n_z]) rc = host_call();
+    // the first call on the host when the NL path is not known yet (it decides nl_compact and
+    // nl_dev_dz: whether the NL kernels take their step size from the device)
+    if (!device_ok(h) && !h->nl_compact && !h->nl_dev_dz && done < max_calls && cz < znet[n_z]) rc = host_call();
     if (rc == GS_OK && !device_ok(h)) {   // everything else on the host, call by call
         while (rc == GS_OK && done < max_calls && cz < znet[n_z]) rc = host_call();
     } else if (rc == GS_OK && done < max_calls && cz < znet[n_z]) {
@@ -191,7 +194,7 @@ int gs_advance(gs_handle* h, const double* znet, int nz, int n_z, double* curren
             CK(h, cudaMemsetAsync(&h->ctl_dev->iter, 0, sizeof(int), h->st));
         }
         if (rc) return rc;
-        h->a_compact = c.field_compact != 0;
+        h->a_compact = h->nl_compact && c.field_compact != 0;   // only the row kernel's masked inverse is lazy
         cz = c.z;
         dz = c.zstep;
         sn = c.step_n;

@@ -71,6 +71,7 @@ struct gs_handle {
     bool a_compact = false;   // FIELD is current only as the masked inverse's compact result
     bool a_lazy_ok = true;    // the masked inverse may leave FIELD compact (not in captured graphs)
     bool nl_compact = false;  // the last NL step ran the kernel that reads a compact FIELD
+    bool nl_dev_dz = false;   // ... ran fused stage kernels, which take dz / halt from the device
     // gs_step_host: BIGBUFFER2 travels host -> staging on io_st (copy engine) while the first NL
     // attempt runs; spec_in_pending until the handle's stream has waited on io_ev[1] and
     // installed it (spec_in_finish, before anything reads BIGBUFFER2 or the staging buffer)
@@ -123,6 +124,8 @@ int spec_sync(gs_handle* h);
 void spec_written(gs_handle* h);
 int spec_prepare(gs_handle* h);
 int spec_in_finish(gs_handle* h);
+// gs_advance's test: the handle's attempts can run with the step controller on the device
+bool advance_on_device(const gs_handle* h);
 // FIELD left compact by the masked inverse (the next NL step reads it so): field_sync expands
 // it into A before A is read by anything else; field_written marks A as rewritten
 int field_sync(gs_handle* h);

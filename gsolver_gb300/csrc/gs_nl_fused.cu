@@ -529,7 +529,13 @@ template <typename Rl, int LOGN = 0, int LC = 0>
 __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage_kernel(FftArgs<Rl> f, PlasmaArgs<Rl> a,
                                                                               const typename Vec2<Rl>::T* __restrict__ A,
                                                                               SpecArgs<Rl> sp) {
-    const StageOv<Rl> ov{f.cdz, f.kp, f.track_max, f.ahead, sp.stage, a.tape_e, a.tape_rho, a.tape_q, a.row_ion,
+    if (f.halt && *f.halt) return;   // gs_advance: the z-loop stopped
+    Rl cdz = f.cdz;
+    if (f.dz_dev) {   // gs_advance: c dz of this stage from the attempt's step size, as the host rounds it
+        const double d = *f.dz_dev;
+        cdz = (Rl)((sp.stage == 0) ? 0.0 : (sp.stage < 3 ? d * 0.5 : d));
+    }
+    const StageOv<Rl> ov{cdz, f.kp, f.track_max, f.ahead, sp.stage, a.tape_e, a.tape_rho, a.tape_q, a.row_ion,
                          (Rl)0, 0};
     nl_stage_row<Rl, LOGN, LC>(f, a, A, sp, ov);
 }
@@ -543,11 +549,13 @@ template <typename Rl, int LOGN = 0, int LC = 0>
 __global__ void __launch_bounds__(sizeof(Rl) == 8 ? 512 : 1024) nl_stage4_kernel(FftArgs<Rl> f, PlasmaArgs<Rl> a,
                                                                                const typename Vec2<Rl>::T* __restrict__ A,
                                                                                SpecArgs<Rl> sp) {
+    if (f.halt && *f.halt) return;   // gs_advance: the z-loop stopped
+    const double dzs = f.dz_dev ? *f.dz_dev : f.dzs;   // gs_advance: the attempt's step size
     for (int s = 0; s < 4; s++) {
-        StageOv<Rl> ov{(Rl)(s == 0 ? 0.0 : (s < 3 ? f.dzs * 0.5 : f.dzs)),   // as the per-stage launches round it
+        StageOv<Rl> ov{(Rl)(s == 0 ? 0.0 : (s < 3 ? dzs * 0.5 : dzs)),   // as the per-stage launches round it
                        s > 0 ? sp.kst[s - 1] : f.kp, s == 0, s == 0 ? f.ahead : 0, s,
                        a.tape_e, a.tape_rho, a.tape_q, a.row_ion,
-                       (Rl)(s < 3 ? (s + 1 < 3 ? f.dzs * 0.5 : f.dzs) : 0.0),   // stage s + 1's c dz
+                       (Rl)(s < 3 ? (s + 1 < 3 ? dzs * 0.5 : dzs) : 0.0),   // stage s + 1's c dz
                        s > 0};
         if (a.tape_e) {   // stage s's record for the adjoint
             const size_t o = (size_t)s * a.tape_stride;

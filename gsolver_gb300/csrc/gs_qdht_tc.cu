@@ -912,7 +912,8 @@ __global__ void lstep_adj_ff_kernel(const float2* __restrict__ fb, float2* __res
 // takes the pair cinv[p] of yc where p is inside the spectral window and zeros elsewhere.
 // Two positions per thread (one 16-byte store), four stores in flight per thread.
 __global__ void qdht_expand_kernel(const float* __restrict__ yc, float* __restrict__ Y, int nr, int nt, int nc,
-                                   const int* __restrict__ cinv) {
+                                   const int* __restrict__ cinv, const int* __restrict__ run) {
+    if (run && *run == 0) return;   // gs_advance: a rejected attempt (the masked inverse did not run)
     const size_t total = (size_t)nr * nt / 2;   // position pairs (n_t even)
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t q0 = (size_t)blockIdx.x * blockDim.x + threadIdx.x; q0 < total; q0 += 4 * stride) {
@@ -1044,7 +1045,9 @@ __global__ void wait_probe_kernel(unsigned* err, unsigned long long limit_ns) {
 
 // Zeros of the masked inverse outside the spectral window: Y[i][2 p], Y[i][2 p + 1] = 0 for
 // the positions p in zpos[nz] (their whole column of the operand is masked)
-__global__ void qdht_zero_cols_kernel(float* __restrict__ Y, int ncols, int nr, const int* __restrict__ zpos, int nz) {
+__global__ void qdht_zero_cols_kernel(float* __restrict__ Y, int ncols, int nr, const int* __restrict__ zpos, int nz,
+                                      const int* __restrict__ run) {
+    if (run && *run == 0) return;   // gs_advance: a rejected attempt
     const size_t total = (size_t)nr * nz;
     for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
         const size_t i = idx / nz;
@@ -1630,7 +1633,7 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
             if (mode == QDHT_MASKED && a.nc == 0 && q->nz > 0) {
                 const size_t tot = (size_t)q->nr * q->nz;
                 const unsigned gz = (unsigned)std::min<size_t>((tot + 255) / 256, (size_t)q->sms * 16);
-                tc::qdht_zero_cols_kernel<<<gz, 256, 0, q->st>>>(Y, a.ncols, q->nr, q->zpos, q->nz);
+                tc::qdht_zero_cols_kernel<<<gz, 256, 0, q->st>>>(Y, a.ncols, q->nr, q->zpos, q->nz, L.run);
                 (*nlaunch)++;
             }
         }
@@ -1667,7 +1670,7 @@ cudaError_t qdht_tc_run(QdhtTc* q, int mode, const float* X, float* Y, const Lst
         const unsigned g2 = (unsigned)(nt2 < q->sms ? nt2 : q->sms);
         tc::qdht_tc2_kernel<<<g2, tc::THREADS2, tc::SMEM2_BYTES, q->st>>>(q->map_hi64, q->map_lo64, q->map_bh, q->map_bl, a);
         (*nlaunch)++;
-        if (a.yc && !(flags & QTC_Y_LAZY)) return qdht_tc_expand(q, Y, nlaunch);
+        if (a.yc && !(flags & QTC_Y_LAZY)) return qdht_tc_expand(q, Y, nlaunch, L.run);
         return cudaGetLastError();
     }
     const int ntiles = (q->nr / tc::BM) * (a.ncols / tc::BN);
@@ -1762,11 +1765,11 @@ const float* qdht_tc_compact_y(QdhtTc* q, int* nc, const int** cmap) {
     return q->yc;
 }
 
-cudaError_t qdht_tc_expand(QdhtTc* q, float* Y, long long* nlaunch) {
+cudaError_t qdht_tc_expand(QdhtTc* q, float* Y, long long* nlaunch, const int* run) {
     if (!q || !q->yc || q->nc_act == 0) return cudaErrorInvalidValue;
     const size_t tot = (size_t)q->nr * q->nt / 2;
     tc::qdht_expand_kernel<<<(unsigned)std::min<size_t>((tot + 1023) / 1024, (size_t)q->sms * 8), 256, 0, q->st>>>(
-        q->yc, Y, q->nr, q->nt, q->nc_act, q->cinv);
+        q->yc, Y, q->nr, q->nt, q->nc_act, q->cinv, run);
     (*nlaunch)++;
     return cudaGetLastError();
 }

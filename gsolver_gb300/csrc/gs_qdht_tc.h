@@ -61,7 +61,7 @@ float* qdht_tc_compact_x(QdhtTc* q, const int** cinv, int* nc);
 // qdht_tc_compact_x; cmap[c]: the real column of compact column c, -1 in the padding), and
 // its expansion into Y (zeros outside the spectral window).
 const float* qdht_tc_compact_y(QdhtTc* q, int* nc, const int** cmap = nullptr);
-cudaError_t qdht_tc_expand(QdhtTc* q, float* Y, long long* nlaunch);
+cudaError_t qdht_tc_expand(QdhtTc* q, float* Y, long long* nlaunch, const int* run = nullptr);
 // Adjoint of the QDHT_LSTEP epilogue's linear step, elementwise over [n_r][n_t]: fb = cotangent
 // of FIELD (k,omega), sb of BIGBUFFER2 (in: after the step, out: before), b1b out: of
 // BIGBUFFER1 (k,omega).  When the plan forms the forward's factors in double-float

@@ -250,7 +250,7 @@ int gs_adjoint_step(gs_handle* h, double dz_rk, double dz_lin, double* field_bar
  * the z-step is captured once into a CUDA graph and replayed (one launch per z-step); a
  * different dz array captures a new graph.  Blast / NaN / tensor-core wait errors are
  * checked after the n_steps and name the pulse.  The pulses' handles stay owned by the
- * caller and must outlive the batch; the adaptive controller stays with gs_step. */
+ * caller and must outlive the batch; gs_batch_advance runs the adaptive controller. */
 typedef struct gs_batch gs_batch;
 int gs_batch_create(int n, gs_handle* const* pulses, gs_batch** out);
 int gs_batch_step(gs_batch* b, int n_steps, const double* dz, int use_graph);
@@ -263,6 +263,18 @@ const char* gs_batch_last_error(const gs_batch* b);
  * gs_autotune shape by timing one graph z-step each way from the same state (the pulses'
  * FIELD and BIGBUFFER2 are restored afterwards); keeps the faster. */
 int gs_batch_autotune(gs_batch* b, const double* dz, double* ms_default, double* ms_tuned, int* chose_tuned);
+/* The z-loops of all pulses advanced together with the adaptive controller: gs_advance for
+ * every pulse (propagator()'s controller and the loop's bookkeeping on the device,
+ * solver_main.cpp:202-225, propagator.cu:139-164), one graph launch per attempt of all pulses.
+ * Per pulse i: its ZNET (znet[i], nz[i] points), the next dump index n_z[i], CURRENT_Z, ZSTEP
+ * and STEP_N in and out, at most max_calls accepted calls; calls_done[i] and reached[i]
+ * (CURRENT_Z >= ZNET[n_z[i]]) out.  A pulse that reaches its ZNET point or its call budget
+ * stops while the others go on; each pulse's results are bit for bit those of gs_advance on
+ * it alone.  Mixed pulses whose NL kernels take their step size from the device (the fused
+ * stage kernels: rows that fit one CTA with the Raman recurrence, one ionization level), no
+ * photon-number check, no aperture; others give GS_ERR_UNSUPPORTED. */
+int gs_batch_advance(gs_batch* b, const double* const* znet, const int* nz, const int* n_z, double* current_z,
+                     double* zstep, unsigned* step_n, int max_calls, int* calls_done, int* reached);
 int gs_batch_destroy(gs_batch* b);
 
 /* Carrier-density maxima without any device allocation.  No counterpart in the reference:

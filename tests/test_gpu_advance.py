@@ -4,9 +4,11 @@
 The same loop through gs_step (the host controller, call by call) and through gs_advance must
 agree bit for bit: CURRENT_Z, ZSTEP, STEP_N (rejected attempts counted), the number of calls,
 the fields at every ZNET point (the dumps) and at the end.  Covered: the 1024 x 16384 workload
-(16384-point FP32 rows with the compact tensor-core plan, the path that runs on the device), a
-strongly ionizing 640-row grid whose first proposal is rejected and whose calls are clamped to
-close ZNET points (dumps in between), and a grid whose calls need the host (gs_step per call).
+(16384-point FP32 rows with the compact tensor-core plan), a strongly ionizing 640-row grid whose
+first proposal is rejected and whose calls are clamped to close ZNET points (dumps in between),
+mixed grids of shorter rows on the fused stage kernels (per-stage launches and the four-stage
+launch), which take their step sizes from the device too, and FP64, whose calls take the host
+(gs_step per call).
 """
 import tempfile
 
@@ -66,7 +68,8 @@ def test_advance_with_rejections_and_znet_points():
     assert [n for n, _ in dumps] == list(range(len(T["znet"])))   # every ZNET point dumped
 
 
-def test_advance_on_a_grid_the_host_drives():
+def test_advance_on_short_rows():
+    # FP64 (host-driven) and mixed on the per-stage fused kernels (device-driven)
     d = tempfile.mkdtemp(prefix="gs_adv_small_")
     p = configs.hot_solid(d, n_r=128, n_t=1024, power_cr=20.0, tol=1e-2)
     T = tables.build(tables.Config.from_file(p), noise_seed=5, noise_sigma=1e-4)
@@ -74,3 +77,21 @@ def test_advance_on_a_grid_the_host_drives():
     for prec in (gs.PREC_FP64, gs.PREC_MIXED):
         host, dev = both(T, dz0, 6, prec)
         same(host, dev)
+        assert host[0][2] > host[0][3]   # rejected attempts on the way
+
+
+def test_advance_on_the_four_stage_fused_kernel():
+    # 8192-point rows, enough of them for the four-stage launch; ZNET points every 2 um with dumps
+    d = tempfile.mkdtemp(prefix="gs_adv_f4_")
+    p = configs.hot_solid(d, n_r=1920, n_t=8192, power_cr=20.0, tol=1e-2, window=1.6e-12)
+    T = tables.build(tables.Config.from_file(p), noise_seed=9, noise_sigma=1e-4)
+    dz0 = tables.init_zstep_kerr(T, T["field"])
+    host, dev = both(T, dz0, 12)
+    same(host, dev)
+    assert host[0][3] == 12 and host[0][2] > 12   # rejected attempts on the way
+    P = gs.Propagator(T)   # the grid takes the four-stage kernel: one NL launch per attempt
+    P.set_field(T["field"])
+    n0 = P.launch_count()
+    P.nl_step(dz0)
+    assert P.launch_count() - n0 == 1
+    P.close()
