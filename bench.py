@@ -414,6 +414,31 @@ def argon_leg(args, lrank):
         Q.close()
     out["mixed_rel_l2_field_err_vs_fp64"] = float(np.linalg.norm(fields[0] - fields[1]) / np.linalg.norm(fields[1]))
     out["err_steps"] = 3
+    if args.batch_adaptive_calls > 0:
+        # the same pulses with their own adaptive controllers (MAX_TOLERANCE 1e-3) on the device:
+        # gs_batch_advance, one graph launch per attempt of all 16 pulses; wall clock of the call
+        P = [gs.Propagator(s, precision=gs.PREC_MIXED, device=lrank) for s in S]
+        for s, p in zip(S, P):
+            p.set_field(s["field"])
+        B = gs.Batch(P)
+        znets = [s["znet"] for s in S]
+        cz = np.array([float(z[0]) for z in znets])
+        dz0 = np.array([float(s["init_zstep"]) for s in S])
+        sn = np.zeros(n, np.uint32)
+        cz, dz0, sn, _, _ = B.advance(znets, [1] * n, cz, dz0, sn, 1)   # warm-up: each NL path found
+        K = max(1, args.batch_adaptive_calls // 2)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _, _, sn1, calls, _ = B.advance(znets, [1] * n, cz, dz0, sn, K)
+        wall = time.perf_counter() - t0
+        acc = int(np.sum(calls))
+        out["adaptive"] = {"max_tolerance": 1e-3, "calls_per_pulse": K, "accepted_calls": acc,
+                           "attempts": int(np.sum(sn1 - sn)), "value": S[0]["n_r"] * S[0]["n_t"] * acc / wall,
+                           "unit": UNIT, "ms_per_call_of_all_pulses": wall * 1e3 / K,
+                           "api": "gs_batch_advance (every pulse's controller on the device, one graph launch per attempt)"}
+        B.close()
+        for p in P:
+            p.close()
     return out
 
 

@@ -692,7 +692,9 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
             const int rs = gsi::field_sync(h);
             if (rs) return rs;
         }
-        h->nl_dev_dz = h->p.nonlinear && fused && !h->pair && !tape && !h->fp64;
+        // the fused stage kernels and the paired ones take dz and the stop flag from the device
+        const bool pair_path = h->pair && !multi && (raman_scan || !raman || !kerr_on);
+        h->nl_dev_dz = h->p.nonlinear && (fused || pair_path) && !tape && !h->fp64;
     }
     if (!h->p.nonlinear) {
         CK(h, launch_zero_nl<Rl>(A, NB, nel, h->max_dev, h->st, &h->launches));
@@ -722,6 +724,7 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
             FftArgs<Rl> f1 = fa;
             f1.rows = nr; f1.kp = KP;
             f1.cdz = (Rl)((s == 0) ? 0.0 : (s < 3 ? dz * 0.5 : dz));
+            f1.c_stage = (s == 0) ? 0.0 : (s < 3 ? 0.5 : 1.0);
             f1.track_max = (s == 0);
             CK(h, launch_nl_pair_front<Rl>(f1, pa, A, nr, h->st, &h->launches));
             SpecArgs<Rl> s2 = sa;

@@ -32,6 +32,7 @@ template <typename Rl> struct FftArgs {
     const double* dz_dev;
     const int* halt;
     const int* ac_on;
+    double c_stage;   // ... the stage's c (0, 1/2, 1/2, 1) where a kernel forms c dz from *dz_dev
 };
 
 template <typename Rl> struct PlasmaArgs {

@@ -70,6 +70,8 @@ template <typename Rl>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape<Rl>::THREADS, 1)
     nl_pair_front_kernel(FftArgs<Rl> f, PlasmaArgs<Rl> a, const typename Vec2<Rl>::T* __restrict__ A) {
     using T2 = C2<Rl>;
+    // gs_advance: the z-loop stopped (both CTAs of the pair read the same flag and return together)
+    if (f.halt && *f.halt) return;
     constexpr int LOGH = PairShape<Rl>::LOGH, H = PairShape<Rl>::H, N = PairShape<Rl>::N;
     constexpr int L = kPairL;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -101,7 +103,8 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape<Rl>::THREA
     load_twiddles<Rl>(twh, twl, f.tw, N, tid, nthr);
     {
         Rl lmax = 0;
-        const Rl cdz = f.cdz;
+        // gs_advance: c dz from the attempt's step size, as the host rounds it
+        const Rl cdz = f.dz_dev ? (Rl)(f.c_stage * *f.dz_dev) : f.cdz;
         T2 v[16];
 #pragma unroll
         for (int u = 0; u < 16; u++) v[u] = A[hbase + tid + u * nthr];
@@ -109,7 +112,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape<Rl>::THREA
 #pragma unroll
             for (int u = 0; u < 16; u++) lmax = fmax(lmax, v[u].x * v[u].x + v[u].y * v[u].y);
         }
-        if (f.cdz != (Rl)0) {
+        if (cdz != (Rl)0) {
 #pragma unroll
             for (int u = 0; u < 16; u++) {
                 const T2 k = f.kp[hbase + tid + u * nthr];
@@ -418,6 +421,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(PairShape<Rl>::THREA
 template <typename Rl>
 __global__ void __launch_bounds__(PairShape<Rl>::THREADS, 1) nl_pair_back_kernel(FftArgs<Rl> f, SpecArgs<Rl> s) {
     using T2 = C2<Rl>;
+    if (f.halt && *f.halt) return;   // gs_advance: the z-loop stopped
     constexpr int LOGH = PairShape<Rl>::LOGH, H = PairShape<Rl>::H, N = PairShape<Rl>::N;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int h = blockIdx.x & 1;

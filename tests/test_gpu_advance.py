@@ -95,3 +95,20 @@ def test_advance_on_the_four_stage_fused_kernel():
     P.nl_step(dz0)
     assert P.launch_count() - n0 == 1
     P.close()
+
+
+def test_advance_on_paired_rows():
+    # 32768-point FP32 rows over a pair of CTAs (solid and the gas build's argon); the paired
+    # kernels take their step sizes from the device as well
+    d = tempfile.mkdtemp(prefix="gs_adv_pair_")
+    p = configs.hot_solid(d, n_r=128, n_t=32768, power_cr=20.0, tol=1e-2, window=1.6e-12)
+    T = tables.build(tables.Config.from_file(p), noise_seed=13, noise_sigma=1e-4)
+    host, dev = both(T, tables.init_zstep_kerr(T, T["field"]), 5)
+    same(host, dev)
+    assert host[0][3] == 5
+    d = tempfile.mkdtemp(prefix="gs_adv_ar_")
+    pa = configs.argon_c5(d, cep=0.0, name="argon_adv", build="gas_qdht")
+    S = gs.Setup(pa, overrides={"N_R": "128"}, noise_seed=200, noise_sigma=1e-4).as_dict()
+    host, dev = both(S, float(S["init_zstep"]), 4)
+    same(host, dev)
+    assert host[0][3] == 4
