@@ -100,7 +100,7 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
 __device__ __forceinline__ bool mbar_try(uint64_t* bar, unsigned parity) {
     uint32_t ok;
     asm volatile(
-        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
         : "=r"(ok)
         : "r"(smem_u32(bar)), "r"(parity)
         : "memory");
@@ -113,14 +113,15 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
     return t;
 }
 
-// wall-clock bounded wait: false when limit_ns expired
+// wall-clock bounded wait: false when limit_ns expired.  try_wait suspends the thread until the
+// phase completes or a short hardware time window passes, so a completed phase wakes the waiter
+// at once (a test_wait poll with a sleep between tries woke it up to a sleep later)
 __device__ __forceinline__ bool mbar_wait_ns(uint64_t* bar, unsigned parity, unsigned long long limit_ns) {
     if (mbar_try(bar, parity)) return true;
     const unsigned long long t0 = globaltimer_ns();
     for (;;) {
         if (mbar_try(bar, parity)) return true;
         if (globaltimer_ns() - t0 > limit_ns) return false;
-        __nanosleep(64);
     }
 }
 __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity) { return mbar_wait_ns(bar, parity, WAIT_NS); }
