@@ -21,8 +21,11 @@ Synthetic: the pulse is generated (seeded 1e-4 complex Gaussian noise), no datas
           algorithmic 8 N_r flop per field-point step
   adjoint the gradient workload (256 x 4096, 1000 steps): forward vs forward+adjoint time
           and the gradient's accuracy (see adjoint_leg)
-  batch   64 pulses with uneven grids, one CUDA graph launch per z-step (see batch_leg)
-  argon   16 argon pulses on the gas build (PPT, third harmonic), 512 x 32768 (see argon_leg)
+  batch   64 pulses with uneven grids, one CUDA graph launch per z-step (see batch_leg), and
+          the same grids with every pulse's adaptive controller on the device, one graph launch
+          per attempt (gs_batch_advance, batch.adaptive)
+  argon   16 argon pulses on the gas build (PPT, third harmonic), 512 x 32768 (see argon_leg),
+          fixed steps and adaptive (argon.adaptive)
   cpu_baseline  the CPU oracle (a port of the reference algorithm) on a bounded sample
 
 Multi-GPU: replicas only (one independent pulse per rank), value = total / max time.
