@@ -90,6 +90,21 @@ def dist_info():
     return r, w, lr
 
 
+def whole_job(ms_local, units_per_rank, world):
+    """Replicas: every rank advanced its own pulse (units_per_rank field-point z-steps) in
+    ms_local; the job's time is the slowest rank's and its value all ranks' units over that
+    time.  Returns (ms, value).  Under torch.distributed (world > 1) the max is an all-reduce
+    over the process group (NCCL on GPUs, gloo on CPU)."""
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([float(ms_local)], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms_local = float(t.item())
+    return ms_local, units_per_rank * world / (ms_local / 1e3)
+
+
 def make_config(workload):
     from gsolver_gb300 import configs
     d = tempfile.mkdtemp(prefix="gs_bench_")
@@ -577,11 +592,7 @@ def main():
     launches = P.launch_count() - n0
     q_ms, q_n = P.qdht_timing(enable=False)
     st_ms, n_st, n_launch = P.nl_timing(enable=False)
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = nr * nt * args.steps * world / (ms / 1e3)
+    ms, value = whole_job(ms, nr * nt * args.steps, world)
 
     # roofline: the QDHT (forward + fused linear step, inverse), 2 N_r^2 flop per real column
     # of the spectral window each: outside it the linear step leaves BIGBUFFER2 untouched and
