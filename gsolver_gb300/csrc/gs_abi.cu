@@ -652,6 +652,12 @@ PlasmaArgs<Rl> gsi::plasma_args(gs_handle* h, bool raman, bool raman_scan) {
 template gs::PlasmaArgs<double> gsi::plasma_args<double>(gs_handle*, bool, bool);
 template gs::PlasmaArgs<float> gsi::plasma_args<float>(gs_handle*, bool, bool);
 
+bool gsi::nl_takes_device_dz(const gs_handle* h) {
+    const bool raman = h->p.raman_fraction > 0.001, kerr_on = h->p.n2 != 0;
+    const bool ok_raman = raman_scan_on(h) || !raman || !kerr_on;
+    return h->p.nonlinear && !h->fp64 && ion_levels(h) == 1 && ok_raman && (h->fused || h->pair);
+}
+
 bool gsi::raman_scan_on(const gs_handle* h) {
     return h->p.raman_fraction > 0.001 && h->p.n2 != 0 && h->p.raman_tau > 0 && h->p.raman_omega > 0;
 }

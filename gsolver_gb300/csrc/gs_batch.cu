@@ -207,6 +207,14 @@ int gs_batch_advance(gs_batch* b, const double* const* znet, const int* nz, cons
         if (calls_done) calls_done[i] = 0;
         if (reached) reached[i] = 0;
     }
+    for (size_t i = 0; i < n; i++) {   // every pulse can run on the device, checked before any work
+        const gs_handle* h = b->h[i];
+        if (h->fp64 || !h->tc || !gs::qdht_tc_has_compact(h->tc) || h->en_tol > 0 || !h->ap_z.empty() ||
+            !gsi::nl_takes_device_dz(h))
+            return bfail(b, GS_ERR_UNSUPPORTED, "pulse " + std::to_string(i) +
+                                                    ": its attempts need the host (FP64, the staged NL kernels, a "
+                                                    "photon-number check or an aperture)");
+    }
     BCK(b, cudaSetDevice(b->device));
     std::vector<int> done(n, 0);
     // as gs_advance: a pulse whose NL path is not known yet takes its first call on the host

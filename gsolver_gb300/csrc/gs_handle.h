@@ -149,6 +149,10 @@ int permute_out(gs_handle* h, const void* src, double* host);
 template <typename Rl> gs::PlasmaArgs<Rl> plasma_args(gs_handle* h, bool raman, bool raman_scan);
 // the Raman recurrence applies (oscillator parameters known, Kerr on)
 bool raman_scan_on(const gs_handle* h);
+// the handle's NL step runs kernels that take dz and the stop flag from the device (the fused
+// stage kernels, the row kernel of 16384 points, the paired kernels): known from its parameters
+// alone, before any step (nl_step_impl sets nl_dev_dz from the same test)
+bool nl_takes_device_dz(const gs_handle* h);
 // position -> omega index of the device FFT of rows N = P M (M = 2^logM per CTA)
 std::vector<int> position_map(int N, int P, int M, int logM);
 // the linear step with the photon-number check of gs_set_energy_tolerance (gs_state.cu): repeated
