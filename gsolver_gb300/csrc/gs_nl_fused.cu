@@ -193,6 +193,7 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
             for (int u = 0; u < 8; u++) {
                 dl[u] = 0;
                 n[u] = (g + u < L && t0 + g + u > 0) ? photo_index<Rl>(Iv[u], &dl[u], a.err) : -1;
+                if (n[u] >= 0 && !in_bounds(n[u] + 1 < 8192, a.err)) n[u] = -1;
             }
             Rl w0[8], w1[8];
 #pragma unroll
@@ -505,7 +506,8 @@ __device__ __forceinline__ void nl_stage_row(const FftArgs<Rl>& f, const PlasmaA
                 if constexpr (sizeof(Rl) == 4) {
                     if (sp.nbc) {
                         const int c = __ldg(sp.cinv + p);
-                        if (c >= 0) *reinterpret_cast<float2*>(sp.nbc + (size_t)blockIdx.x * sp.ncw + c) = make_float2(nb.x, nb.y);
+                        if (c >= 0 && in_bounds(c + 2 <= sp.ncw, a.err))
+                            *reinterpret_cast<float2*>(sp.nbc + (size_t)blockIdx.x * sp.ncw + c) = make_float2(nb.x, nb.y);
                     }
                 }
             }

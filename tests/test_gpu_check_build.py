@@ -6,8 +6,9 @@ skips the access (no trap) and the call returns GS_ERR_CUDA "index out of bounds
 
 * gs_selftest_bounds makes the test fail on purpose on an index that still lies inside its
   buffer (so nothing could fault either way) and must report it, the handle usable afterwards;
-* on the 1024 x 16384 workload (mixed, gs_advance) and on an ionizing 640 x 16384 grid (mixed,
-  gs_step) the checked build reports nothing and gives the main build's results bit for bit."""
+* on the 1024 x 16384 workload (mixed, gs_advance), on an ionizing 640 x 16384 grid (mixed,
+  gs_step) and on an ionizing 256 x 2048 grid (the fused stage kernels, gs_advance) the checked
+  build reports nothing and gives the main build's results bit for bit."""
 import os
 import subprocess
 import sys
@@ -49,6 +50,16 @@ def workloads(out):
         sn += 1
     f, s = P.get_field(want_spec=True)
     res.update(hot_f=f, hot_s=s, hot_scalars=np.array([cz, dz, sn]))
+    P.close()
+    # shorter rows on the fused stage kernels (their compact BIGBUFFER1 columns and rate rows)
+    d = tempfile.mkdtemp(prefix="gs_chk_fused_")
+    p = configs.hot_solid(d, n_r=256, n_t=2048, power_cr=20.0, tol=1e-2)
+    T = tables.build(tables.Config.from_file(p), noise_seed=23, noise_sigma=1e-4)
+    P = gs.Propagator(T, precision=gs.PREC_MIXED)
+    P.set_field(T["field"])
+    out_adv = P.advance(T["znet"], 1, float(T["znet"][0]), tables.init_zstep_kerr(T, T["field"]), 0, 4)
+    f, s = P.get_field(want_spec=True)
+    res.update(fused_f=f, fused_s=s, fused_scalars=np.array(out_adv[:4], dtype=np.float64))
     P.close()
     np.savez(out, **res)
 
