@@ -610,6 +610,7 @@ int gs_get_field(gs_handle* h, double* field, double* spec) {
 
 int gs_get_nl(gs_handle* h, double* bb1) {
     if (!h || !bb1) return GS_ERR_ARG;
+    if (!h->nb_full_current) return fail(h, GS_ERR_STATE, "BIGBUFFER1 is kept in full by gs_nl_step only");
     CK(h, cudaSetDevice(h->p.device));
     return permute_out(h, h->NB, bb1);
 }
@@ -675,6 +676,7 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
     T2* U2 = U1 + nel;
     T2* U3 = U2 + nel;
     h->nbc_valid = false;   // set again below when the fused stages also write NB's compact columns
+    h->nb_full_current = true;   // cleared below where the row kernel leaves the full array out
     const bool raman = h->p.raman_fraction > 0.001;
     const bool kerr_on = h->p.n2 != 0;
     // the oscillator recurrence replaces the RAMAN_FUNCTION FFT pair when its parameters are known
@@ -767,6 +769,9 @@ static int nl_step_impl(gs_handle* h, double dz, const GsTape* tape = nullptr) {
             s2.nbc = nbc;
             s2.cinv = cinv;
             s2.ncw = ncw;
+            // the row kernel leaves out the full BIGBUFFER1 where only its window columns are read
+            if (nbc && !h->nb_full_wanted && !tape && nl_row16k_applies(nt, h->nl_threads)) s2.nb = nullptr;
+            h->nb_full_current = s2.nb != nullptr;
             // nl_compact holds; under gs_advance the device flag ac_on tells whether it is current
             if (h->a_compact || (h->ctl && h->nl_compact)) s2.ac = gs::qdht_tc_compact_y(h->tc, nullptr, &s2.cmap);
             const bool tm = h->time_nl && !tape;
@@ -878,7 +883,10 @@ int gs_nl_step(gs_handle* h, double zstep, double* max_a2, double* max_nl2) {
     if (!h) return GS_ERR_ARG;
     if (!h->tables_ok || !h->field_ok) return fail(h, GS_ERR_STATE, "tables / field not set");
     CK(h, cudaSetDevice(h->p.device));
-    return nl_step(h, zstep, max_a2, max_nl2);
+    h->nb_full_wanted = true;   // calculate_NLstep's BIGBUFFER1, read back by gs_get_nl
+    const int rc = nl_step(h, zstep, max_a2, max_nl2);
+    h->nb_full_wanted = false;
+    return rc;
 }
 
 int gsi::spec_sync(gs_handle* h) {

@@ -67,6 +67,10 @@ struct gs_handle {
     int znet_cap = 0;
     std::vector<cudaEvent_t> adv_ev;
     bool nbc_valid = false;   // the last NL step also wrote NB's window columns compactly (mixed)
+    // BIGBUFFER1 in full: gs_nl_step asks for it (nb_full_wanted); propagator()'s paths need only
+    // the window columns the linear step reads, and the row kernel then writes those alone
+    bool nb_full_wanted = false;
+    bool nb_full_current = true;   // NB holds the last NL increment everywhere
     bool s_compact = false;   // BIGBUFFER2's window columns are current only in the plan's compact copy
     bool a_compact = false;   // FIELD is current only as the masked inverse's compact result
     bool a_lazy_ok = true;    // the masked inverse may leave FIELD compact (not in captured graphs)

@@ -176,7 +176,7 @@ __device__ __forceinline__ void radix4(float2* x) {
 
 // The row's four RK4 stages (step f.dzs): stage s's input is (A + c_s dz k_{s-1}) / N with
 // c = 0, 1/2, 1/2, 1, its k feeds the RK4 sum (k1 + 2 k2 + 2 k3 + k4) / 6 written to sp.nb
-// (and, when sp.nbc is set, its spectral-window positions compactly); max |A|^2 and max |nb|^2
+// (when set) and, when sp.nbc is set, its spectral-window positions compactly; max |A|^2 and max |nb|^2
 // go to f.max_out and sp.max_out.  FIELD is read from sp.ac (compact window columns) when set,
 // else from A.
 __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, PlasmaArgs<float> a,
@@ -686,7 +686,7 @@ __global__ void __launch_bounds__(NT, 1) nl_row16k_kernel(FftArgs<float> f, Plas
         for (int r = 0; r < 8; r++) {
             const int p = 512 * w + 64 * r + 2 * lane;
             const float2 y0 = E[pad16(p)], y1 = E[pad16(p) + 1];
-            *reinterpret_cast<float4*>(sp.nb + base + p) = make_float4(y0.x, y0.y, y1.x, y1.y);
+            if (sp.nb) *reinterpret_cast<float4*>(sp.nb + base + p) = make_float4(y0.x, y0.y, y1.x, y1.y);
             if (nbr) {
                 const int2 c2 = __ldg(reinterpret_cast<const int2*>(sp.cinv + p));
                 if (c2.x >= 0 && in_bounds(c2.x + 2 <= sp.ncw, a.err)) *reinterpret_cast<float2*>(nbr + c2.x) = y0;
@@ -718,7 +718,8 @@ cudaError_t nl_row16k_setup() {
 
 cudaError_t launch_nl_row16k(FftArgs<float> f, PlasmaArgs<float> a, const float2* A, SpecArgs<float> s, int rows,
                              int ahead, cudaStream_t st, long long* nl) {
-    if (f.N != r16k::N || !f.twb || !f.tw || a.tape_e || (s.ac && !s.cinv) || (s.nbc && !s.cinv)) return cudaErrorInvalidValue;
+    if (f.N != r16k::N || !f.twb || !f.tw || a.tape_e || (s.ac && !s.cinv) || (s.nbc && !s.cinv) || (!s.nb && !s.nbc))
+        return cudaErrorInvalidValue;
     f.rows = rows;
     f.ahead = ahead;
     r16k::nl_row16k_kernel<<<rows, r16k::NT, r16k::SMEM, st>>>(f, a, A, s);

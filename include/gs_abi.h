@@ -134,7 +134,9 @@ int gs_get_field(gs_handle* h, double* field_r_omega, double* spec_k_omega);
  * returns max |FIELD|^2 and max |BIGBUFFER1|^2. */
 int gs_nl_step(gs_handle* h, double zstep, double* max_a2, double* max_nl2);
 
-/* Copy BIGBUFFER1 (the last NL increment, (r,omega)) to the host. */
+/* Copy BIGBUFFER1 (the last NL increment, (r,omega)) to the host: after gs_nl_step.  The
+ * propagator() paths (gs_step, gs_advance, gs_step_host, batches) may keep only the window columns
+ * the linear step reads; gs_get_nl then returns GS_ERR_STATE. */
 int gs_get_nl(gs_handle* h, double* bb1_r_omega);
 
 /* ht_run(BIGBUFFER1) -> calculate_Lstep(zstep) -> ht_run(FIELD). */
