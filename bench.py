@@ -199,7 +199,7 @@ def new_state(S):
 # smsp__issue_active.avg.pct_of_peak_sustained_active of one launch, divided by its n_r n_t field
 # points); they are fixed properties of the kernels, re-measured whenever a kernel changes.
 NCU_PER_POINT = {
-    "nl_row16k": {"dram_bytes": 10.61, "warp_instructions": 30.1, "issue_active": 0.593},
+    "nl_row16k": {"dram_bytes": 2.37, "warp_instructions": 30.1, "issue_active": 0.597},
     "qdht_pair": {"dram_bytes": 9.13},
 }
 
