@@ -260,7 +260,7 @@ def cpu_sample(T, nthreads=None):
     t_cols = time.perf_counter() - t0
     t_step = t_rows * nr / len(rows) + t_cols * nt / cols
     desc = (f"oracle (C port of the reference z-step, agreeing with the reference solver itself to 1e-12 on every "
-            f"hot-path function; OpenMP {cores} threads, radix-2 FFT): RK4 NL step + "
+            f"hot-path function; OpenMP {cores} threads, radix-4 Stockham FFT): RK4 NL step + "
             f"linear step on {len(rows)} of {nr} rows, forward+inverse QDHT on {cols} of {nt} omega columns, "
             f"extrapolated to one {nr}x{nt} step ({t_step:.2f} s)")
     return nr * nt / t_step, desc, cores

@@ -8,7 +8,8 @@
  *
  * Third-party arithmetic the reference pulls in and that is restated here:
  *   FFTW3 (version unpinned by the reference Makefile:45): an unnormalised complex DFT
- *   with FFTW's sign convention, computed here by an iterative radix-2 FFT.
+ *   with FFTW's sign convention, computed here by a radix-4 Stockham autosort FFT (a final
+ *   radix-2 pass for odd powers of two).
  */
 #include "gs_oracle.h"
 
@@ -32,10 +33,11 @@ static int omp_get_max_threads(void) { return 1; }
 
 /* ------------------------------------------------------------------ FFT -- */
 
-typedef struct { int n; double* tw; int* rev; } fft_tab;
+typedef struct { int n; double* tw; } fft_tab;
 static fft_tab g_tabs[16];
 static int g_ntabs = 0;
 
+/* tw[j] = (cos, sin)(2 pi j / n), j < n, each rounded once from the libm value */
 static const fft_tab* get_tab(int n)
 {
     const fft_tab* found = NULL;
@@ -46,23 +48,55 @@ static const fft_tab* get_tab(int n)
             fft_tab* t = &g_tabs[g_ntabs];
             t->n = n;
             t->tw = (double*)malloc(sizeof(double) * 2 * (size_t)n);
-            t->rev = (int*)malloc(sizeof(int) * (size_t)n);
             for (int j = 0; j < n; j++) {
                 double a = 2.0 * M_PI * (double)j / (double)n;
                 t->tw[2 * j] = cos(a);
                 t->tw[2 * j + 1] = sin(a);
-            }
-            int lg = 0; while ((1 << lg) < n) lg++;
-            for (int j = 0; j < n; j++) {
-                int r = 0;
-                for (int b = 0; b < lg; b++) if (j & (1 << b)) r |= 1 << (lg - 1 - b);
-                t->rev[j] = r;
             }
             g_ntabs++;
             found = t;
         }
     }
     return found;
+}
+
+/* One radix-4 pass of the Stockham autosort FFT (the published self-sorting formulation:
+ * no bit reversal, the output of each pass in natural order of its sub-transforms): x holds
+ * s interleaved sequences of length m = 4 m1, y receives them transformed by one radix-4
+ * step with the twiddles w_m^{p}, w_m^{2p}, w_m^{3p} (w_m = exp(sign 2 pi i / m) = tw[N/m]). */
+static void stockham4(int m, int s, int sign, const double* tw, int tstride, const double* x, double* y)
+{
+    const int m1 = m / 4;
+    for (int p = 0; p < m1; p++) {
+        const double* w1 = tw + 2 * (size_t)(p * tstride);
+        const double* w2 = tw + 2 * (size_t)(2 * p * tstride);
+        const double* w3 = tw + 2 * (size_t)(3 * p * tstride);
+        const double w1r = w1[0], w1i = sign * w1[1], w2r = w2[0], w2i = sign * w2[1];
+        const double w3r = w3[0], w3i = sign * w3[1];
+        for (int q = 0; q < s; q++) {
+            const double* a = x + 2 * ((size_t)q + (size_t)s * p);
+            const double* b = x + 2 * ((size_t)q + (size_t)s * (p + m1));
+            const double* c = x + 2 * ((size_t)q + (size_t)s * (p + 2 * m1));
+            const double* d = x + 2 * ((size_t)q + (size_t)s * (p + 3 * m1));
+            const double apcr = a[0] + c[0], apci = a[1] + c[1];
+            const double amcr = a[0] - c[0], amci = a[1] - c[1];
+            const double bpdr = b[0] + d[0], bpdi = b[1] + d[1];
+            /* sign i (b - d) */
+            const double jr = -sign * (b[1] - d[1]), ji = sign * (b[0] - d[0]);
+            double* o = y + 2 * ((size_t)q + (size_t)s * 4 * p);
+            const double r1 = amcr + jr, i1 = amci + ji;
+            const double r2 = apcr - bpdr, i2 = apci - bpdi;
+            const double r3 = amcr - jr, i3 = amci - ji;
+            o[0] = apcr + bpdr;
+            o[1] = apci + bpdi;
+            o[2 * s] = r1 * w1r - i1 * w1i;
+            o[2 * s + 1] = r1 * w1i + i1 * w1r;
+            o[4 * s] = r2 * w2r - i2 * w2i;
+            o[4 * s + 1] = r2 * w2i + i2 * w2r;
+            o[6 * s] = r3 * w3r - i3 * w3i;
+            o[6 * s + 1] = r3 * w3i + i3 * w3r;
+        }
+    }
 }
 
 int gso_fft(int n, const double* in, double* out, int sign)
@@ -85,36 +119,53 @@ int gso_fft(int n, const double* in, double* out, int sign)
         free(tmp);
         return GSO_OK;
     }
+    if (n == 1) {
+        out[0] = in[0];
+        out[1] = in[1];
+        return GSO_OK;
+    }
     const fft_tab* t = get_tab(n);
     if (!t) return GSO_ERR_ARG;
-    if (in == out) {
-        for (int j = 0; j < n; j++) {
-            int r = t->rev[j];
-            if (r > j) {
-                double a = out[2 * j], b = out[2 * j + 1];
-                out[2 * j] = out[2 * r]; out[2 * j + 1] = out[2 * r + 1];
-                out[2 * r] = a; out[2 * r + 1] = b;
-            }
-        }
-    } else {
-        for (int j = 0; j < n; j++) {
-            int r = t->rev[j];
-            out[2 * r] = in[2 * j]; out[2 * r + 1] = in[2 * j + 1];
-        }
+    /* radix-4 Stockham passes, then one radix-2 pass when log2 n is odd; the first pass reads
+     * `in`, the last writes `out`, the ones between alternate over two per-thread scratch rows
+     * (so in == out is allowed) */
+    static _Thread_local double* scratch = NULL;
+    static _Thread_local size_t scratch_n = 0;
+    if (scratch_n < (size_t)n) {
+        free(scratch);
+        scratch = (double*)malloc(sizeof(double) * 4 * (size_t)n);
+        scratch_n = scratch ? (size_t)n : 0;
+        if (!scratch) return GSO_ERR_ARG;
     }
-    for (int len = 2; len <= n; len <<= 1) {
-        int half = len >> 1, step = n / len;
-        for (int base = 0; base < n; base += len) {
-            for (int k = 0; k < half; k++) {
-                double wr = t->tw[2 * (k * step)], wi = sign * t->tw[2 * (k * step) + 1];
-                double* p = out + 2 * (base + k);
-                double* q = out + 2 * (base + k + half);
-                double xr = q[0] * wr - q[1] * wi, xi = q[0] * wi + q[1] * wr;
-                q[0] = p[0] - xr; q[1] = p[1] - xi;
-                p[0] = p[0] + xr; p[1] = p[1] + xi;
+    int passes = 0, lg = 0;
+    while ((1 << lg) < n) lg++;
+    passes = lg / 2 + (lg & 1);
+    double* bufs[2] = {scratch, scratch + 2 * (size_t)n};
+    const double* x = in;
+    int m = n, s = 1;
+    for (int k = 0; k < passes; k++) {
+        /* pass k writes buffer (passes - 1 - k) % 2 of the scratch, the last one `out`; with a
+         * single pass and in == out it goes through the scratch */
+        double* y = (k == passes - 1 && !(passes == 1 && in == out)) ? out : bufs[(passes - 1 - k) & 1];
+        if (m >= 4) {
+            stockham4(m, s, sign, t->tw, n / m, x, y);
+            m /= 4;
+            s *= 4;
+        } else {   /* m == 2 */
+            for (int q = 0; q < s; q++) {
+                const double* a = x + 2 * (size_t)q;
+                const double* b = x + 2 * ((size_t)q + (size_t)s);
+                double* o = y + 2 * (size_t)q;
+                o[0] = a[0] + b[0];
+                o[1] = a[1] + b[1];
+                o[2 * s] = a[0] - b[0];
+                o[2 * s + 1] = a[1] - b[1];
             }
+            m = 1;
         }
+        x = y;
     }
+    if (x != out) memcpy(out, x, sizeof(double) * 2 * (size_t)n);
     return GSO_OK;
 }
 
