@@ -105,3 +105,20 @@ def test_aperture_zeroes_rows_once_in_config_order():
     assert np.abs(st["field"][R > 1.5e-4]).max() > 0
     out, st = O.run(T["field"], dz0, steps=4)               # the step from z = 3e-4: aperture 1
     assert np.all(st["field"][R > 1e-4] == 0)
+
+
+def test_fft_is_the_dft_with_fftws_conventions():
+    # the oracle's FFT (FFTW3's unnormalised transform, sign -1 forward / +1 backward, as the
+    # reference calls it): radix-4 Stockham passes and a radix-2 pass for odd powers of two,
+    # the plain DFT for other lengths; in place and out of place
+    T = small(n_r=64, n_t=64)
+    O = oracle.Oracle(T)
+    rng = np.random.default_rng(3)
+    for n in (1, 2, 4, 8, 32, 128, 2048, 16384, 32768, 12):
+        x = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        for sign in (-1, 1):
+            ref = np.fft.fft(x) if sign < 0 else np.fft.ifft(x) * n
+            got = O.fft(x, sign)
+            assert np.linalg.norm(got - ref) <= 1e-14 * max(1.0, np.linalg.norm(ref)), (n, sign)
+    x = rng.standard_normal(1024) + 1j * rng.standard_normal(1024)
+    assert np.allclose(O.fft(O.fft(x, -1), 1) / 1024, x, rtol=0, atol=1e-14)
