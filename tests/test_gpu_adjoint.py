@@ -176,3 +176,19 @@ def test_torch_autograd_function_over_the_c_abi():
     with torch.no_grad():
         J2 = BandEnergy.apply(x - 1e-7 * J / torch.linalg.vector_norm(gx) ** 2 * gx)
     assert float(J2) < float(J.detach())
+
+
+def test_package_autograd_objective_matches_the_adjoint():
+    torch = pytest.importorskip("torch")
+    from gsolver_gb300 import autograd as ga
+    T = hot(n_r=16, n_t=512, power_cr=30.0)
+    dz_rk, dz_lin = schedule(T, 4)
+    w = np.random.default_rng(9).random((T["n_r"], T["n_t"]))
+    P = gs.Propagator(T, precision=gs.PREC_FP64)
+    J_of = ga.objective(P, dz_rk, dz_lin, w)
+    x = torch.tensor(T["field"], dtype=torch.complex128, requires_grad=True)
+    J = J_of(x)
+    (gx,) = torch.autograd.grad(J, x)
+    J_ref, g = P.gradient(T["field"], dz_rk, dz_lin, w)
+    assert float(J) == pytest.approx(J_ref, rel=1e-12) and np.array_equal(gx.numpy(), g)
+    P.close()
